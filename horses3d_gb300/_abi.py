@@ -1,0 +1,155 @@
+"""ctypes view of the C ABI declared in include/horses3d_gb300.h.
+
+The structures mirror the header field for field; every call goes through the shared library
+``horses3d_gb300/lib/libhorses3d_gb300.so`` that ``horses3d_gb300.build`` compiles for sm_103a.
+There is no Python fallback: a missing library raises ``LibraryNotBuilt``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+PKG_DIR = Path(__file__).resolve().parent
+LIB_DIR = PKG_DIR / "lib"
+LIB_NAME = "libhorses3d_gb300.so"
+
+DG_OK = 0
+DG_ERR_INVALID = -1
+DG_ERR_UNSUPPORTED = -2
+DG_ERR_CUDA = -3
+DG_ERR_NAN = -4
+DG_ERR_TIMEOUT = -5
+DG_ERR_NOMEM = -6
+DG_ERR_NODEVICE = -7
+DG_ERR_IO = -8
+
+DG_NODES_GAUSS, DG_NODES_GAUSS_LOBATTO = 0, 1
+DG_INVISCID_STANDARD, DG_INVISCID_SPLIT = 0, 1
+DG_RIEMANN_ROE, DG_RIEMANN_LXF = 0, 1
+DG_AVG_STANDARD, DG_AVG_PIROZZOLI = 0, 1
+DG_PRECISION_FP64, DG_PRECISION_MIXED = 0, 1
+DG_SOURCE_NONE, DG_SOURCE_MMS_CONVERGENCE = 0, 1
+DG_FIELD_Q, DG_FIELD_QDOT, DG_FIELD_G, DG_FIELD_UX, DG_FIELD_UY, DG_FIELD_UZ = range(6)
+
+_i32p = C.POINTER(C.c_int32)
+_f64p = C.POINTER(C.c_double)
+
+
+class DgMeshDesc(C.Structure):
+    _fields_ = [
+        ("n_elements", C.c_int32),
+        ("node_type", C.c_int32),
+        ("order", _i32p),
+        ("x", _f64p),
+        ("ja_xi", _f64p),
+        ("ja_eta", _f64p),
+        ("ja_zeta", _f64p),
+        ("jacobian", _f64p),
+        ("inv_jacobian", _f64p),
+        ("n_faces", C.c_int32),
+        ("face_elem", _i32p),
+        ("face_side", _i32p),
+        ("face_rotation", _i32p),
+        ("face_nf", _i32p),
+        ("face_normal", _f64p),
+        ("face_t1", _f64p),
+        ("face_t2", _f64p),
+        ("face_jacobian", _f64p),
+    ]
+
+
+class DgPhysics(C.Structure):
+    _fields_ = [
+        ("mach", C.c_double),
+        ("reynolds", C.c_double),
+        ("prandtl", C.c_double),
+        ("navier_stokes", C.c_int32),
+    ]
+
+
+class DgOptions(C.Structure):
+    _fields_ = [
+        ("inviscid", C.c_int32),
+        ("riemann", C.c_int32),
+        ("averaging", C.c_int32),
+        ("lambda_stab", C.c_double),
+        ("precision", C.c_int32),
+        ("source", C.c_int32),
+    ]
+
+
+# (name, restype, argtypes) of every entry point in include/horses3d_gb300.h
+SIGNATURES = [
+    ("dg_version", C.c_char_p, []),
+    ("dg_strerror", C.c_char_p, [C.c_int]),
+    ("dg_last_error", C.c_char_p, []),
+    ("dg_device_count", C.c_int, [C.POINTER(C.c_int)]),
+    ("dg_create", C.c_int, [C.POINTER(DgMeshDesc), C.POINTER(DgPhysics), C.POINTER(DgOptions), C.POINTER(C.c_void_p)]),
+    ("dg_destroy", None, [C.c_void_p]),
+    ("dg_upload_state", C.c_int, [C.c_void_p, _f64p]),
+    ("dg_download", C.c_int, [C.c_void_p, C.c_int, _f64p]),
+    ("dg_ndof", C.c_int64, [C.c_void_p]),
+    ("dg_rhs", C.c_int, [C.c_void_p, C.c_double]),
+    ("dg_rk3_step", C.c_int, [C.c_void_p, C.c_double, C.c_double, _f64p]),
+    ("dg_run_steps", C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double]),
+    ("dg_max_dt", C.c_int, [C.c_void_p, C.c_double, C.c_double, _f64p]),
+    ("dg_residuals", C.c_int, [C.c_void_p, _f64p, C.POINTER(C.c_int)]),
+    ("dg_synchronize", C.c_int, [C.c_void_p]),
+    ("h3d_mesh_read_specmesh", C.c_int, [C.c_char_p, C.c_int, C.c_int, _i32p, C.c_char_p, C.POINTER(C.c_void_p)]),
+    ("h3d_mesh_box", C.c_int, [C.c_int, C.c_int, C.c_int, _f64p, _f64p, C.c_double, C.c_int, C.c_int, C.c_int,
+                               _i32p, C.POINTER(C.c_void_p)]),
+    ("h3d_mesh_describe", C.c_int, [C.c_void_p, C.POINTER(DgMeshDesc)]),
+    ("h3d_mesh_volume", C.c_double, [C.c_void_p]),
+    ("h3d_mesh_free", None, [C.c_void_p]),
+    ("h3d_nodal_storage", C.c_int, [C.c_int, C.c_int, _f64p, _f64p, _f64p]),
+]
+
+
+class LibraryNotBuilt(RuntimeError):
+    pass
+
+
+class DgError(RuntimeError):
+    def __init__(self, code: int, where: str, detail: str):
+        super().__init__(f"{where} failed: {code} ({detail})")
+        self.code = code
+
+
+_lib = None
+
+
+def library_path() -> Path:
+    override = os.environ.get("HORSES3D_GB300_LIB")
+    return Path(override) if override else LIB_DIR / LIB_NAME
+
+
+def lib():
+    """Loads the C ABI library once; raises LibraryNotBuilt when it has not been compiled."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not path.exists():
+        raise LibraryNotBuilt(f"{path} is missing: run horses3d_gb300.build.build() (nvcc, sm_103a)")
+    handle = C.CDLL(str(path))
+    for name, res, args in SIGNATURES:
+        fn = getattr(handle, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = handle
+    return _lib
+
+
+def check(code: int, where: str) -> None:
+    if code != DG_OK:
+        L = lib()
+        raise DgError(code, where, f"{L.dg_strerror(code).decode()}: {L.dg_last_error().decode()}")
+
+
+def f64ptr(arr):
+    return arr.ctypes.data_as(_f64p)
+
+
+def i32ptr(arr):
+    return arr.ctypes.data_as(_i32p)

@@ -1,0 +1,167 @@
+/*
+ * horses3d_gb300 -- C ABI of the GB300 (sm_103a) compressible Navier-Stokes DGSEM
+ * right-hand side and Williamson low-storage RK3 update.
+ *
+ * The boundary sits where HORSES3D's time integrator calls the spatial operator:
+ *
+ *   dg_rhs        replaces ComputeTimeDerivative
+ *                 (Solver/src/NavierStokesSolver/SpatialDiscretization.f90:227-320,
+ *                  interface ComputeTimeDerivative_f in
+ *                  Solver/src/libs/discretization/DGSEMClass.f90:78-95)
+ *   dg_rk3_step   replaces TakeRK3Step, the RKStep procedure pointer
+ *                 (Solver/src/libs/timeintegrator/ExplicitMethods.f90:667-788,
+ *                  TimeIntegrator.f90:215,292,809-813)
+ *   dg_max_dt     replaces MaxTimeStep (Solver/src/libs/discretization/DGSEMClass.f90:870-1038)
+ *   dg_residuals  replaces ComputeMaxResiduals (DGSEMClass.f90:770-868) and the NaN test of
+ *                 checkForNan (ExplicitMethods.f90:1856-1908)
+ *
+ * All arrays crossing the boundary use the reference's own column-major layouts, element by
+ * element in element order: Q(1:5,0:Nx,0:Ny,0:Nz) (StorageClass.f90:802), metric terms
+ * jGradXi/Eta/Zeta(1:3,0:Nx,0:Ny,0:Nz), jacobian(0:Nx,0:Ny,0:Nz) (MappedGeometry.f90:24-35),
+ * face geometry normal/t1/t2(1:3,0:Nf1,0:Nf2), jacobian(0:Nf1,0:Nf2) (MappedGeometry.f90:482-760).
+ *
+ * Every entry point returns an int status: DG_OK (0) or a negative DG_ERR_* code. No entry point
+ * exits the process (the reference stops with `error stop`/exit(99); the caller maps the codes).
+ * A context is not thread safe; use one context per host thread. Each context owns one CUDA stream.
+ */
+#ifndef HORSES3D_GB300_H
+#define HORSES3D_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------------ */
+#define DG_OK                0
+#define DG_ERR_INVALID      -1   /* bad argument, inconsistent mesh description */
+#define DG_ERR_UNSUPPORTED  -2   /* option outside the GPU path (caller keeps its CPU path) */
+#define DG_ERR_CUDA         -3   /* a CUDA runtime call failed; dg_last_error() has the text */
+#define DG_ERR_NAN          -4   /* NaN/Inf found in Q (checkForNan equivalent) */
+#define DG_ERR_TIMEOUT      -5   /* a bounded device wait gave up */
+#define DG_ERR_NOMEM        -6   /* device allocation failed */
+#define DG_ERR_NODEVICE     -7   /* no CUDA device visible */
+#define DG_ERR_IO           -8   /* mesh file could not be read */
+
+/* ---- enumerations (values match the reference's keyword choices) ------------------------- */
+enum { DG_NODES_GAUSS = 0, DG_NODES_GAUSS_LOBATTO = 1 };          /* "discretization nodes" */
+enum { DG_INVISCID_STANDARD = 0, DG_INVISCID_SPLIT = 1 };          /* "inviscid discretization" */
+enum { DG_RIEMANN_ROE = 0, DG_RIEMANN_LXF = 1 };                   /* "riemann solver" */
+enum { DG_AVG_STANDARD = 0, DG_AVG_PIROZZOLI = 1 };                /* "averaging" */
+enum { DG_PRECISION_FP64 = 0, DG_PRECISION_MIXED = 1 };            /* plain FP64 / FP32 flux form */
+enum { DG_SOURCE_NONE = 0, DG_SOURCE_MMS_CONVERGENCE = 1 };        /* UserDefinedSourceTermNS */
+enum { DG_FIELD_Q = 0, DG_FIELD_QDOT = 1, DG_FIELD_G = 2,
+       DG_FIELD_UX = 3, DG_FIELD_UY = 4, DG_FIELD_UZ = 5 };
+
+/* Face-local element sides, numbered as the reference (HexElementConnectivityDefinitions.f90:69-77):
+ * 1 FRONT (eta=-1), 2 BACK (eta=+1), 3 BOTTOM (zeta=-1), 4 RIGHT (xi=+1), 5 TOP (zeta=+1), 6 LEFT (xi=-1). */
+
+/* Mesh description: geometry and connectivity as HexMesh holds them after ConstructGeometry.
+ * Only interior faces (periodic faces count as interior, HexMesh.f90:519-736) are supported. */
+typedef struct dg_mesh_desc {
+    int32_t n_elements;
+    int32_t node_type;              /* DG_NODES_* */
+    const int32_t* order;           /* [3*K]  (Nx,Ny,Nz) of every element */
+    const double* x;                /* [3*sum(P)] node coordinates x(1:3,i,j,k) */
+    const double* ja_xi;            /* [3*sum(P)] jGradXi */
+    const double* ja_eta;           /* [3*sum(P)] jGradEta */
+    const double* ja_zeta;          /* [3*sum(P)] jGradZeta */
+    const double* jacobian;         /* [sum(P)] */
+    const double* inv_jacobian;     /* [sum(P)] */
+    int32_t n_faces;
+    const int32_t* face_elem;       /* [2*F] left, right element (0-based) */
+    const int32_t* face_side;       /* [2*F] element side 1..6 of left, right */
+    const int32_t* face_rotation;   /* [F]   0..7 (leftIndexes2Right, MeshTypes.f90:70-107) */
+    const int32_t* face_nf;         /* [2*F] (Nf1,Nf2) face orders */
+    const double* face_normal;      /* [3*sum(Pf)] unit normal, left -> right */
+    const double* face_t1;          /* [3*sum(Pf)] */
+    const double* face_t2;          /* [3*sum(Pf)] */
+    const double* face_jacobian;    /* [sum(Pf)] surface Jacobian Jf */
+} dg_mesh_desc;
+
+/* Physics constants (PhysicsStorage_NS.f90:186-429). gamma=1.4 (air) and Sutherland's law with
+ * S=198.6*5/9 K, TRef=520*5/9 K are fixed as in the reference's defaults. */
+typedef struct dg_physics {
+    double mach;
+    double reynolds;
+    double prandtl;                 /* reference default 0.72 */
+    int32_t navier_stokes;          /* 1: "NS" (BR1 viscous terms), 0: "Euler" (no gradients) */
+} dg_physics;
+
+typedef struct dg_options {
+    int32_t inviscid;               /* DG_INVISCID_* (split form requires Gauss-Lobatto nodes) */
+    int32_t riemann;                /* DG_RIEMANN_* */
+    int32_t averaging;              /* DG_AVG_*  (LxF average and split-form two-point flux) */
+    double lambda_stab;             /* LxF stabilisation factor, reference default 1.0 */
+    int32_t precision;              /* DG_PRECISION_* */
+    int32_t source;                 /* DG_SOURCE_* */
+} dg_options;
+
+typedef struct dg_ctx dg_ctx;
+
+/* Library and device --------------------------------------------------------------------- */
+const char* dg_version(void);
+const char* dg_strerror(int code);
+const char* dg_last_error(void);          /* text of the last failure on this thread */
+int dg_device_count(int* count);
+
+/* Context lifetime: copies the mesh description to device memory once (host pointers are not
+ * retained). Replaces the one-time storage set-up of HexMesh (HexMesh.f90:5802). */
+int dg_create(const dg_mesh_desc* mesh, const dg_physics* phys, const dg_options* opts, dg_ctx** out);
+void dg_destroy(dg_ctx* ctx);
+
+/* State transfer in the reference layout (Q(1:5,i,j,k) element after element). */
+int dg_upload_state(dg_ctx* ctx, const double* q);
+int dg_download(dg_ctx* ctx, int field, double* dst);
+int64_t dg_ndof(const dg_ctx* ctx);
+
+/* ComputeTimeDerivative: QDot = RHS(Q, t) (SpatialDiscretization.f90:227-685). */
+int dg_rhs(dg_ctx* ctx, double t);
+
+/* TakeRK3Step: three RHS evaluations + low-storage updates (ExplicitMethods.f90:748-779).
+ * dt > 0: fixed step. dt <= 0: the step is the CFL step of MaxTimeStep with cfl=-dt and the dcfl
+ * given to dg_set_cfl. dt_used (may be NULL) receives the step taken. */
+int dg_rk3_step(dg_ctx* ctx, double t, double dt, double* dt_used);
+
+/* Fixed-step loop of n RK3 steps at dt on the device (captured in a CUDA graph after the first
+ * step). No host synchronisation between steps. */
+int dg_run_steps(dg_ctx* ctx, int n, double t0, double dt);
+
+/* MaxTimeStep (DGSEMClass.f90:870-1038) on the device. */
+int dg_max_dt(dg_ctx* ctx, double cfl, double dcfl, double* dt);
+
+/* ComputeMaxResiduals: max|QDot| per conserved variable; *nan_found = 1 if Q holds NaN/Inf. */
+int dg_residuals(dg_ctx* ctx, double maxres[5], int* nan_found);
+
+/* Block until all work queued on the context's stream is done. */
+int dg_synchronize(dg_ctx* ctx);
+
+/* Host-side mesh builder (HexMesh construction: Read_SpecMesh.f90:36-342, HexMesh.f90:356-736,
+ * 2677-2990, MappedGeometry.f90:64-760). Produces a dg_mesh_desc whose arrays live in the mesh. */
+typedef struct h3d_mesh h3d_mesh;
+
+/* periodic: comma separated "plus:minus" boundary-name pairs (case-insensitive), e.g.
+ * "front:back,bottom:top,left:right". orders: [3*K] per-element orders or NULL for uniform
+ * (uniform_n used in all three directions). */
+int h3d_mesh_read_specmesh(const char* path, int node_type, int uniform_n, const int32_t* orders,
+                           const char* periodic, h3d_mesh** out);
+/* Periodic box [x0,x1]x[y0,y1]x[z0,z1] of nx*ny*nz hexahedra, optionally warped by
+ * x_i += warp*sin(x)sin(y)sin(z) with curved faces given as Chebyshev-Lobatto patches of order
+ * patch_order (patch_order < 2 and warp == 0 gives straight-sided hex8 elements). */
+int h3d_mesh_box(int nx, int ny, int nz, const double lo[3], const double hi[3], double warp,
+                 int patch_order, int node_type, int uniform_n, const int32_t* orders, h3d_mesh** out);
+int h3d_mesh_describe(const h3d_mesh* mesh, dg_mesh_desc* out);
+/* Total quadrature volume sum_e sum_ijk w_i w_j w_k J (MappedGeometry.f90:132-135). */
+double h3d_mesh_volume(const h3d_mesh* mesh);
+void h3d_mesh_free(h3d_mesh* mesh);
+
+/* Nodal storage of order n (NodalStorageClass.f90:170-338): fills x,w [n+1] and D [(n+1)^2,
+ * row-major D(i,j)]. Any pointer may be NULL. */
+int h3d_nodal_storage(int node_type, int n, double* x, double* w, double* d);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HORSES3D_GB300_H */

@@ -1,0 +1,1052 @@
+// ORACLE -- test infrastructure only. Nothing in the product links or calls this file; it is the
+// CPU FP64 checker that tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg use.
+//
+// A loop-for-loop C++ restatement of HORSES3D's compressible Navier-Stokes right-hand side and
+// Williamson RK3 step. Element arrays keep the reference layout Q(1:NEQ,0:Nx,0:Ny,0:Nz); face arrays
+// keep the per-side FaceStorage layout. Each routine cites the reference routine it follows.
+// It consumes the same dg_mesh_desc as the GPU library (the geometry is an input to both), and it
+// computes its own spectral operators so that a fault in the product's operators cannot hide.
+//
+// Parity: pinned by tests/test_oracle_golden.py against the goldens of
+// Solver/test/NavierStokes/Convergence/SETUP/ProblemFile.f90:617-635 (tol 1e-11, :711-790).
+// Build: oracle/Makefile (g++ -O2 -ffp-contract=off -fopenmp).
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "horses3d_gb300.h"
+
+namespace orc {
+
+constexpr double PI = 3.141592653589793238462643;
+enum { IRHO = 0, IRHOU, IRHOV, IRHOW, IRHOE };
+enum { EFRONT = 1, EBACK, EBOTTOM, ERIGHT, ETOP, ELEFT };
+
+// ---------------------------------------------------------------- spectral (own copy) ------
+static bool almost_equal(double a, double b) {
+    const double tol = 2.0 * DBL_EPSILON;
+    if (a == 0.0 || b == 0.0) return std::fabs(a - b) <= tol;
+    return std::fabs(b - a) <= tol * std::fmax(std::fabs(a), std::fabs(b));
+}
+static void legendre(int N, double x, double& L, double& Lp) {
+    if (N == 0) { L = 1.0; Lp = 0.0; return; }
+    if (N == 1) { L = x; Lp = 1.0; return; }
+    double a = 1.0, ap = 0.0, b = x, bp = 1.0;
+    for (int k = 2; k <= N; ++k) {
+        L = ((2 * k - 1) * x * b - (k - 1) * a) / k;
+        Lp = ap + (2 * k - 1) * b;
+        a = b; b = L; ap = bp; bp = Lp;
+    }
+}
+static void gauss(int N, double* x, double* w) {  // LegendreAlgorithms.f90:137
+    double L, Lp;
+    if (N == 0) { x[0] = 0; w[0] = 2; return; }
+    if (N == 1) { x[0] = -std::sqrt(1.0 / 3.0); w[0] = 1; x[1] = -x[0]; w[1] = 1; }
+    else {
+        for (int j = 0; j < (N + 1) / 2; ++j) {
+            double xj = -std::cos((2 * j + 1) * PI / (2 * N + 2));
+            for (int k = 0; k <= 10; ++k) {
+                legendre(N + 1, xj, L, Lp);
+                const double d = -L / Lp;
+                xj += d;
+                if (std::fabs(d) <= 4.0 * DBL_EPSILON * std::fabs(xj)) break;
+            }
+            legendre(N + 1, xj, L, Lp);
+            x[j] = xj; w[j] = 2.0 / ((1.0 - xj * xj) * (Lp * Lp));
+            x[N - j] = -xj; w[N - j] = w[j];
+        }
+    }
+    if (N % 2 == 0) { legendre(N + 1, 0.0, L, Lp); x[N / 2] = 0.0; w[N / 2] = 2.0 / (Lp * Lp); }
+}
+static void lobatto(int N, double* x, double* w) {  // LegendreAlgorithms.f90:275
+    if (N == 0) { x[0] = 0; w[0] = 2; return; }
+    if (N == 1) { x[0] = -1; w[0] = 1; x[1] = 1; w[1] = 1; }
+    else {
+        x[0] = -1; w[0] = 2.0 / (N * (N + 1)); x[N] = 1; w[N] = w[0];
+        for (int j = 1; j <= (N + 1) / 2 - 1; ++j) {
+            double xj = -std::cos((j + 0.25) * PI / N - 3.0 / (8 * N * PI * (j + 0.25)));
+            double q = 0, qp = 0, LN = 0;
+            auto qandl = [&](double xx) {
+                double a = 1.0, ap = 0.0, b = xx, bp = 1.0, Lk = 0, Lpk = 0;
+                for (int k = 2; k <= N; ++k) {
+                    Lk = ((2 * k - 1) * xx * b - (k - 1) * a) / k; Lpk = ap + (2 * k - 1) * b;
+                    a = b; b = Lk; ap = bp; bp = Lpk;
+                }
+                const int k = N + 1;
+                Lk = ((2 * k - 1) * xx * b - (k - 1) * a) / k; Lpk = ap + (2 * k - 1) * b;
+                q = Lk - a; qp = Lpk - ap; LN = b;
+            };
+            for (int k = 0; k <= 10; ++k) {
+                qandl(xj);
+                const double d = -q / qp;
+                xj += d;
+                if (std::fabs(d) <= 4.0 * DBL_EPSILON * std::fabs(xj)) break;
+            }
+            qandl(xj);
+            x[j] = xj; w[j] = 2.0 / (N * (N + 1) * (LN * LN));
+            x[N - j] = -xj; w[N - j] = w[j];
+        }
+    }
+    if (N % 2 == 0) { double L, Lp; legendre(N, 0.0, L, Lp); x[N / 2] = 0; w[N / 2] = 2.0 / (N * (N + 1) * (L * L)); }
+}
+static void bary(int N, const double* x, double* w) {
+    for (int j = 0; j <= N; ++j) w[j] = 1.0;
+    for (int j = 1; j <= N; ++j)
+        for (int k = 0; k < j; ++k) { w[k] *= (x[k] - x[j]); w[j] *= (x[j] - x[k]); }
+    for (int j = 0; j <= N; ++j) w[j] = 1.0 / w[j];
+}
+static void lagrange_at(double x, int N, const double* nodes, const double* wb, double* p) {
+    bool match = false;
+    for (int j = 0; j <= N; ++j) { p[j] = 0.0; if (almost_equal(x, nodes[j])) { p[j] = 1.0; match = true; } }
+    if (match) return;
+    double d = 0.0;
+    for (int j = 0; j <= N; ++j) { const double t = wb[j] / (x - nodes[j]); p[j] = t; d += t; }
+    for (int j = 0; j <= N; ++j) p[j] /= d;
+}
+static void interp_matrix(int N, int M, const double* on, const double* wb, const double* nn, double* T) {
+    for (int k = 0; k <= M; ++k) {
+        bool match = false;
+        for (int j = 0; j <= N; ++j) { T[k * (N + 1) + j] = 0.0; if (almost_equal(nn[k], on[j])) { match = true; T[k * (N + 1) + j] = 1.0; } }
+        if (!match) {
+            double s = 0.0;
+            for (int j = 0; j <= N; ++j) { const double t = wb[j] / (nn[k] - on[j]); T[k * (N + 1) + j] = t; s += t; }
+            for (int j = 0; j <= N; ++j) T[k * (N + 1) + j] /= s;
+        }
+    }
+}
+
+struct Nodal {  // NodalStorageClass.f90:170-338 (the parts the right-hand side uses)
+    int N;
+    std::vector<double> x, w, D, hatD, sharpD, vL, vR, bL, bR;
+};
+static const Nodal& nodal(int nodes, int N) {
+    static std::map<std::pair<int, int>, Nodal> cache;
+    auto key = std::make_pair(nodes, N);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    Nodal s;
+    s.N = N;
+    const int n1 = N + 1;
+    s.x.resize(n1); s.w.resize(n1);
+    if (nodes == 0) gauss(N, s.x.data(), s.w.data()); else lobatto(N, s.x.data(), s.w.data());
+    std::vector<double> wb(n1);
+    bary(N, s.x.data(), wb.data());
+    s.D.assign(n1 * n1, 0.0);
+    for (int i = 0; i <= N; ++i) {  // InterpolationAndDerivatives.f90:799-828
+        s.D[i * n1 + i] = 0.0;
+        for (int j = 0; j <= N; ++j)
+            if (j != i) {
+                s.D[i * n1 + j] = wb[j] / (wb[i] * (s.x[i] - s.x[j]));
+                s.D[i * n1 + i] -= s.D[i * n1 + j];
+            }
+    }
+    s.hatD.resize(n1 * n1);
+    for (int j = 0; j <= N; ++j)
+        for (int i = 0; i <= N; ++i) s.hatD[i * n1 + j] = s.D[j * n1 + i] * s.w[j] / s.w[i];
+    if (nodes == 1) {
+        s.sharpD.resize(n1 * n1);
+        for (int k = 0; k < n1 * n1; ++k) s.sharpD[k] = 2.0 * s.D[k];
+        s.sharpD[0] = 2.0 * s.D[0] + 1.0 / s.w[0];
+        s.sharpD[N * n1 + N] = 2.0 * s.D[N * n1 + N] - 1.0 / s.w[N];
+    }
+    s.vL.resize(n1); s.vR.resize(n1); s.bL.resize(n1); s.bR.resize(n1);
+    lagrange_at(1.0, N, s.x.data(), wb.data(), s.vR.data());
+    lagrange_at(-1.0, N, s.x.data(), wb.data(), s.vL.data());
+    for (int i = 0; i <= N; ++i) { s.bL[i] = s.vL[i] / s.w[i]; s.bR[i] = s.vR[i] / s.w[i]; }
+    return cache.emplace(key, s).first->second;
+}
+// InterpolationMatrices.f90:42-113: T(0:Nd,0:No) row-major.
+static std::vector<double> tset(int nodes, int No, int Nd) {
+    const Nodal& o = nodal(nodes, No);
+    const Nodal& d = nodal(nodes, Nd);
+    std::vector<double> T((Nd + 1) * (No + 1));
+    std::vector<double> wbo(No + 1), wbd(Nd + 1);
+    bary(No, o.x.data(), wbo.data());
+    bary(Nd, d.x.data(), wbd.data());
+    if (No < Nd) interp_matrix(No, Nd, o.x.data(), wbo.data(), d.x.data(), T.data());
+    else {
+        std::vector<double> Tt((No + 1) * (Nd + 1));
+        interp_matrix(Nd, No, d.x.data(), wbd.data(), o.x.data(), Tt.data());
+        for (int j = 0; j <= No; ++j)
+            for (int i = 0; i <= Nd; ++i) T[i * (No + 1) + j] = Tt[j * (Nd + 1) + i] * o.w[j] / d.w[i];
+    }
+    return T;
+}
+
+// MeshTypes.f90:70-107 leftIndexes2Right.
+static void l2r(int i, int j, int Nx, int Ny, int rot, int& ii, int& jj) {
+    switch (rot) {
+        case 0: ii = i; jj = j; break;
+        case 1: ii = Ny - j; jj = i; break;
+        case 2: ii = Nx - i; jj = Ny - j; break;
+        case 3: ii = j; jj = Nx - i; break;
+        case 4: ii = j; jj = i; break;
+        case 5: ii = Nx - i; jj = j; break;
+        case 6: ii = Ny - j; jj = Nx - i; break;
+        default: ii = i; jj = Ny - j; break;
+    }
+}
+
+// ---------------------------------------------------------------- physics --------------------
+struct Phys {
+    double gamma = 1.4, gm1 = 0.4, Mach, Re, Pr, mu, kappa, mu_to_kappa, gammaM2;
+    double S_div_TRef, TReNorm;
+    bool ns;
+};
+
+static inline double pressure(const Phys& p, const double* Q) {  // VariableConversion_NS.f90:44-57
+    return p.gm1 * (Q[4] - 0.5 * (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) / Q[0]);
+}
+static inline double sutherland(const Phys& p, double T) {  // VariableConversion_NS.f90:170-186
+    const double t = T * p.TReNorm;
+    return (1.0 + p.S_div_TRef) / (t + p.S_div_TRef) * t * std::sqrt(t);
+}
+static inline void mu_kappa(const Phys& p, const double* Q, double& mu, double& kappa) {  // :147-164
+    const double T = p.gammaM2 * pressure(p, Q) / Q[0];
+    const double s = sutherland(p, T);
+    mu = p.mu * s;
+    kappa = mu * p.mu_to_kappa;
+}
+
+// Physics_NS.f90:51-103 EulerFlux: F(1:5,1:3) stored F[v + 5*d].
+static void euler_flux(const Phys& p, const double* Q, double* F) {
+    const double u = Q[1] / Q[0], v = Q[2] / Q[0], w = Q[3] / Q[0];
+    const double pr = p.gm1 * (Q[4] - 0.5 * (Q[1] * u + Q[2] * v + Q[3] * w));
+    F[0] = Q[1]; F[1] = Q[1] * u + pr; F[2] = Q[1] * v; F[3] = Q[1] * w; F[4] = (Q[4] + pr) * u;
+    F[5] = Q[2]; F[6] = F[2]; F[7] = Q[2] * v + pr; F[8] = Q[2] * w; F[9] = (Q[4] + pr) * v;
+    F[10] = Q[3]; F[11] = F[3]; F[12] = F[8]; F[13] = Q[3] * w + pr; F[14] = (Q[4] + pr) * w;
+}
+
+// Physics_NS.f90:246-303 ViscousFlux_STATE.
+static void viscous_flux(const Phys& p, const double* Q, const double* Ux, const double* Uy, const double* Uz,
+                         double mu, double beta, double kappa, double* F) {
+    const double invRho = 1.0 / Q[0];
+    const double u = Q[1] * invRho, v = Q[2] * invRho, w = Q[3] * invRho;
+    const double ud[3] = {u * invRho, v * invRho, w * invRho};
+    double ux[3], uy[3], uz[3];
+    for (int c = 0; c < 3; ++c) {
+        ux[c] = invRho * Ux[1 + c] - ud[c] * Ux[0];
+        uy[c] = invRho * Uy[1 + c] - ud[c] * Uy[0];
+        uz[c] = invRho * Uz[1 + c] - ud[c] * Uz[0];
+    }
+    const double g = p.gm1 * p.gammaM2;
+    const double nTx = g * (invRho * Ux[4] - Q[4] * invRho * invRho * Ux[0] - u * ux[0] - v * ux[1] - w * ux[2]);
+    const double nTy = g * (invRho * Uy[4] - Q[4] * invRho * invRho * Uy[0] - u * uy[0] - v * uy[1] - w * uy[2]);
+    const double nTz = g * (invRho * Uz[4] - Q[4] * invRho * invRho * Uz[0] - u * uz[0] - v * uz[1] - w * uz[2]);
+    const double divV = ux[0] + uy[1] + uz[2];
+    F[0] = 0.0;
+    F[1] = mu * (2.0 * ux[0] - 2.0 / 3.0 * divV) + beta * divV;
+    F[2] = mu * (ux[1] + uy[0]);
+    F[3] = mu * (ux[2] + uz[0]);
+    F[4] = F[1] * u + F[2] * v + F[3] * w + kappa * nTx;
+    F[5] = 0.0;
+    F[6] = F[2];
+    F[7] = mu * (2.0 * uy[1] - 2.0 / 3.0 * divV) + beta * divV;
+    F[8] = mu * (uy[2] + uz[1]);
+    F[9] = F[6] * u + F[7] * v + F[8] * w + kappa * nTy;
+    F[10] = 0.0;
+    F[11] = F[3];
+    F[12] = F[8];
+    F[13] = mu * (2.0 * uz[2] - 2.0 / 3.0 * divV) + beta * divV;
+    F[14] = F[11] * u + F[12] * v + F[13] * w + kappa * nTz;
+}
+
+// RiemannSolvers_NS.f90:1541-1655 RoeRiemannSolver.
+static void roe(const Phys& p, const double* QL, const double* QR, const double* n, double* flux) {
+    const double g = p.gamma;
+    const double rho = QL[0], rhou = QL[1], rhov = QL[2], rhow = QL[3], rhoe = QL[4];
+    const double rhon = QR[0], rhoun = QR[1], rhovn = QR[2], rhown = QR[3], rhoen = QR[4];
+    const double ul = rhou / rho, vl = rhov / rho, wl = rhow / rho;
+    const double pleft = (g - 1.0) * (rhoe - 0.5 / rho * (rhou * rhou + rhov * rhov + rhow * rhow));
+    const double ur = rhoun / rhon, vr = rhovn / rhon, wr = rhown / rhon;
+    const double pright = (g - 1.0) * (rhoen - 0.5 / rhon * (rhoun * rhoun + rhovn * rhovn + rhown * rhown));
+    const double ql = n[0] * ul + n[1] * vl + n[2] * wl;
+    const double qr = n[0] * ur + n[1] * vr + n[2] * wr;
+    const double hl = 0.5 * (ul * ul + vl * vl + wl * wl) + g / (g - 1.0) * pleft / rho;
+    const double hr = 0.5 * (ur * ur + vr * vr + wr * wr) + g / (g - 1.0) * pright / rhon;
+    const double rtd = std::sqrt(rho * rhon);
+    const double betal = rho / (rho + rtd), betar = 1.0 - betal;
+    const double utd = betal * ul + betar * ur, vtd = betal * vl + betar * vr, wtd = betal * wl + betar * wr;
+    const double htd = betal * hl + betar * hr;
+    const double atd2 = (g - 1.0) * (htd - 0.5 * (utd * utd + vtd * vtd + wtd * wtd));
+    const double atd = std::sqrt(atd2);
+    const double qtd = utd * n[0] + vtd * n[1] + wtd * n[2];
+    if (qtd >= 0.0) {
+        const double dw1 = 0.5 * ((pright - pleft) / atd2 - (qr - ql) * rtd / atd);
+        const double sp1 = qtd - atd;
+        const double sp1m = std::fmin(sp1, 0.0);
+        const double hd1m = ((g + 1.0) / 4.0 * atd / rtd) * dw1;
+        const double eta1 = std::fmax(-std::fabs(sp1) - hd1m, 0.0);
+        const double udw1 = dw1 * (sp1m - 0.5 * eta1);
+        const double rql = rho * ql;
+        flux[0] = 1.0 * (rql + udw1);
+        flux[1] = 1.0 * (rql * ul + pleft * n[0] + udw1 * (utd - atd * n[0]));
+        flux[2] = 1.0 * (rql * vl + pleft * n[1] + udw1 * (vtd - atd * n[1]));
+        flux[3] = 1.0 * (rql * wl + pleft * n[2] + udw1 * (wtd - atd * n[2]));
+        flux[4] = 1.0 * (rql * hl + udw1 * (htd - qtd * atd));
+    } else {
+        const double dw4 = 0.5 * ((pright - pleft) / atd2 + (qr - ql) * rtd / atd);
+        const double sp4 = qtd + atd;
+        const double sp4p = std::fmax(sp4, 0.0);
+        const double hd4 = ((g + 1.0) / 4.0 * atd / rtd) * dw4;
+        const double eta4 = std::fmax(-std::fabs(sp4) + hd4, 0.0);
+        const double udw4 = dw4 * (sp4p + 0.5 * eta4);
+        const double rqr = rhon * qr;
+        flux[0] = 1.0 * (rqr - udw4);
+        flux[1] = 1.0 * (rqr * ur + pright * n[0] - udw4 * (utd + atd * n[0]));
+        flux[2] = 1.0 * (rqr * vr + pright * n[1] - udw4 * (vtd + atd * n[1]));
+        flux[3] = 1.0 * (rqr * wr + pright * n[2] - udw4 * (wtd + atd * n[2]));
+        flux[4] = 1.0 * (rqr * hr - udw4 * (htd + qtd * atd));
+    }
+}
+
+// RiemannSolvers_NS.f90:1784-1813 StandardAverage and :1927-1962 PirozzoliAverage (rotated states).
+static void average(int avg, const double* L, const double* R, double pL, double pR, double iL, double iR, double* f) {
+    const double uL = iL * L[1], uR = iR * R[1], vL = iL * L[2], vR = iR * R[2], wL = iL * L[3], wR = iR * R[3];
+    if (avg == DG_AVG_STANDARD) {
+        f[0] = 0.5 * (L[1] + R[1]);
+        f[1] = 0.5 * (L[1] * uL + R[1] * uR + pL + pR);
+        f[2] = 0.5 * (L[1] * vL + R[1] * vR);
+        f[3] = 0.5 * (L[1] * wL + R[1] * wR);
+        f[4] = 0.5 * (uL * (L[4] + pL) + uR * (R[4] + pR));
+    } else {
+        const double rho = 0.5 * (L[0] + R[0]), u = 0.5 * (uL + uR), v = 0.5 * (vL + vR), w = 0.5 * (wL + wR);
+        const double p = 0.5 * (pL + pR);
+        const double h = 0.5 * ((L[4] + pL) * iL + (R[4] + pR) * iR);
+        f[0] = rho * u; f[1] = rho * u * u + p; f[2] = rho * u * v; f[3] = rho * u * w; f[4] = rho * u * h;
+    }
+}
+
+// RiemannSolvers_NS.f90:1251-1334 LxFRiemannSolver.
+static void lxf(const Phys& p, int avg, double lambdaStab, const double* QL, const double* QR, const double* n,
+                const double* t1, const double* t2, double* flux) {
+    const double rhoL = QL[0], rhoR = QR[0];
+    const double iL = 1.0 / rhoL, iR = 1.0 / rhoR;
+    const double rhouL = QL[1] * n[0] + QL[2] * n[1] + QL[3] * n[2];
+    const double rhouR = QR[1] * n[0] + QR[2] * n[1] + QR[3] * n[2];
+    const double rhovL = QL[1] * t1[0] + QL[2] * t1[1] + QL[3] * t1[2];
+    const double rhovR = QR[1] * t1[0] + QR[2] * t1[1] + QR[3] * t1[2];
+    const double rhowL = QL[1] * t2[0] + QL[2] * t2[1] + QL[3] * t2[2];
+    const double rhowR = QR[1] * t2[0] + QR[2] * t2[1] + QR[3] * t2[2];
+    const double V2L = (rhouL * rhouL + rhovL * rhovL + rhowL * rhowL) * iL;
+    const double V2R = (rhouR * rhouR + rhovR * rhovR + rhowR * rhowR) * iR;
+    const double pL = p.gm1 * (QL[4] - 0.5 * V2L), pR = p.gm1 * (QR[4] - 0.5 * V2R);
+    const double aL = std::sqrt(p.gamma * pL * iL), aR = std::sqrt(p.gamma * pR * iR);
+    const double lambda = std::fmax(std::fabs(rhouL * iL) + aL, std::fabs(rhouR * iR) + aR);
+    const double Lr[5] = {rhoL, rhouL, rhovL, rhowL, QL[4]};
+    const double Rr[5] = {rhoR, rhouR, rhovR, rhowR, QR[4]};
+    double f[5];
+    average(avg, Lr, Rr, pL, pR, iL, iR, f);
+    for (int v = 0; v < 5; ++v) f[v] = f[v] - lambdaStab * (0.5 * lambda * (Rr[v] - Lr[v]));
+    flux[0] = f[0];
+    for (int c = 0; c < 3; ++c) flux[1 + c] = n[c] * f[1] + t1[c] * f[2] + t2[c] * f[3];
+    flux[4] = f[4];
+}
+
+// RiemannSolvers_NS.f90:2085-2145 StandardDG_TwoPointFlux and :2369-2437 Pirozzoli_TwoPointFlux.
+static void two_point(const Phys& p, int avg, const double* QL, const double* QR, const double* JaL, const double* JaR,
+                      double* fs) {
+    const double iL = 1.0 / QL[0], iR = 1.0 / QR[0];
+    const double uL = iL * QL[1], uR = iR * QR[1], vL = iL * QL[2], vR = iR * QR[2], wL = iL * QL[3], wR = iR * QR[3];
+    const double pL = p.gm1 * (QL[4] - 0.5 * (QL[1] * uL + QL[2] * vL + QL[3] * wL));
+    const double pR = p.gm1 * (QR[4] - 0.5 * (QR[1] * uR + QR[2] * vR + QR[3] * wR));
+    if (avg == DG_AVG_STANDARD) {
+        const double Ja[3] = {JaL[0] + JaR[0], JaL[1] + JaR[1], JaL[2] + JaR[2]};
+        double f[5], g[5], h[5];
+        f[0] = QL[1] + QR[1]; f[1] = QL[1] * uL + QR[1] * uR + pL + pR; f[2] = QL[1] * vL + QR[1] * vR;
+        f[3] = QL[1] * wL + QR[1] * wR; f[4] = uL * (QL[4] + pL) + uR * (QR[4] + pR);
+        g[0] = QL[2] + QR[2]; g[1] = QL[2] * uL + QR[2] * uR; g[2] = QL[2] * vL + QR[2] * vR + pL + pR;
+        g[3] = QL[2] * wL + QR[2] * wR; g[4] = vL * (QL[4] + pL) + vR * (QR[4] + pR);
+        h[0] = QL[3] + QR[3]; h[1] = QL[3] * uL + QR[3] * uR; h[2] = QL[3] * vL + QR[3] * vR;
+        h[3] = QL[3] * wL + QR[3] * wR + pL + pR; h[4] = wL * (QL[4] + pL) + wR * (QR[4] + pR);
+        for (int v = 0; v < 5; ++v) fs[v] = 0.25 * (f[v] * Ja[0] + g[v] * Ja[1] + h[v] * Ja[2]);
+    } else {
+        const double rho = 0.5 * (QL[0] + QR[0]), u = 0.5 * (uL + uR), v = 0.5 * (vL + vR), w = 0.5 * (wL + wR);
+        const double pp = 0.5 * (pL + pR);
+        const double h = 0.5 * ((QL[4] + pL) * iL + (QR[4] + pR) * iR);
+        const double Ja[3] = {0.5 * (JaL[0] + JaR[0]), 0.5 * (JaL[1] + JaR[1]), 0.5 * (JaL[2] + JaR[2])};
+        const double ff[5] = {rho * u, rho * u * u + pp, rho * u * v, rho * u * w, rho * u * h};
+        const double gg[5] = {rho * v, rho * v * u, rho * v * v + pp, rho * v * w, rho * v * h};
+        const double hh[5] = {rho * w, rho * w * u, rho * w * v, rho * w * w + pp, rho * w * h};
+        for (int q = 0; q < 5; ++q) fs[q] = ff[q] * Ja[0] + gg[q] * Ja[1] + hh[q] * Ja[2];
+    }
+}
+
+// Convergence/SETUP/ProblemFile.f90:31-133 state_source_in_point (manufactured solution).
+static void mms_point(double x, double y, double z, double t, double gm1, double gMa2, double mu, double kap,
+                      double* Q, double* S, double* QDot) {
+    const double c_u = 1.0, c_v = 2.0, c_w = -c_u - c_v;
+    const double Ssu = 0.381923076923077;
+    const double arg = PI * (x + y + z - 2.0 * t), dargdx = PI, dargdt = -2.0 * PI;
+    const double rho = 2.0 + 0.1 * std::sin(arg);
+    const double u = c_u * rho - 1.0, v = c_v * rho - 4.0, w = c_w * rho + 5.0, e = rho;
+    const double vtot = u * u + v * v + w * w;
+    const double p = gm1 * (rho * e - 0.5 * rho * vtot);
+    const double Temp = gMa2 * gm1 * (e - 0.5 * vtot);
+    const double suther = (1.0 + Ssu) / (Temp + Ssu) * Temp * std::sqrt(Temp);
+    const double dsutherdT = 1.5 * suther / Temp - suther / (Ssu + Temp);
+    Q[0] = rho; Q[1] = rho * u; Q[2] = rho * v; Q[3] = rho * w; Q[4] = rho * e;
+    const double rho_t = 0.1 * dargdt * std::cos(arg);
+    const double u_t = c_u * rho_t, v_t = c_v * rho_t, w_t = c_w * rho_t, e_t = rho_t;
+    QDot[0] = rho_t; QDot[1] = rho_t * u + rho * u_t; QDot[2] = rho_t * v + rho * v_t;
+    QDot[3] = rho_t * w + rho * w_t; QDot[4] = rho_t * e + rho * e_t;
+    double rho_x[3], u_x[3], v_x[3], w_x[3], e_x[3], p_x[3], T_x[3];
+    for (int i = 0; i < 3; ++i) {
+        rho_x[i] = 0.1 * dargdx * std::cos(arg);
+        u_x[i] = c_u * rho_x[i]; v_x[i] = c_v * rho_x[i]; w_x[i] = c_w * rho_x[i]; e_x[i] = rho_x[i];
+    }
+    for (int i = 0; i < 3; ++i) {
+        p_x[i] = gm1 * rho_x[i] * (e - 0.5 * vtot) + gm1 * rho * (e_x[i] - u * u_x[i] - v * v_x[i] - w * w_x[i]);
+        T_x[i] = gMa2 * gm1 * (e_x[i] - u * u_x[i] - v * v_x[i] - w * w_x[i]);
+    }
+    const double div_v = u_x[0] + v_x[1] + w_x[2];
+    double gu[3][3], tau[3][3];  // gu[i][j] = grad_u(i,j)
+    for (int i = 0; i < 3; ++i) { gu[i][0] = u_x[i]; gu[i][1] = v_x[i]; gu[i][2] = w_x[i]; }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            tau[i][j] = mu * suther * (gu[i][j] + gu[j][i] - 2.0 * div_v * (i == j ? 1.0 : 0.0) / 3.0);
+    double rxx[3][3], uxx[3][3], vxx[3][3], wxx[3][3], exx[3][3], Txx[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            rxx[i][j] = -0.1 * (dargdx * dargdx) * std::sin(arg);
+            uxx[i][j] = c_u * rxx[i][j]; vxx[i][j] = c_v * rxx[i][j]; wxx[i][j] = c_w * rxx[i][j]; exx[i][j] = rxx[i][j];
+        }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            Txx[i][j] = gMa2 * gm1 * (exx[i][j] - u_x[i] * u_x[j] - v_x[i] * v_x[j] - w_x[i] * w_x[j] - u * uxx[i][j] -
+                                      v * vxx[i][j] - w * wxx[i][j]);
+    double dt[3];
+    const double tr[3] = {uxx[0][0] + uxx[1][1] + uxx[2][2], vxx[0][0] + vxx[1][1] + vxx[2][2], wxx[0][0] + wxx[1][1] + wxx[2][2]};
+    const double gd[3] = {uxx[0][0] + vxx[1][0] + wxx[2][0], uxx[1][0] + vxx[1][1] + wxx[1][2], uxx[0][2] + vxx[1][2] + wxx[2][2]};
+    for (int j = 0; j < 3; ++j) dt[j] = uxx[0][j] + vxx[1][j] + wxx[2][j] + tr[j] - (2.0 / 3.0) * gd[j];
+    for (int j = 0; j < 3; ++j) dt[j] = mu * suther * dt[j];
+    for (int i = 0; i < 3; ++i) {
+        double mt = 0.0;
+        for (int j = 0; j < 3; ++j) mt += tau[i][j] * T_x[j];
+        dt[i] = dt[i] + (dsutherdT / suther) * mt;
+    }
+    double sgt = 0.0;
+    for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) sgt += gu[i][j] * tau[i][j];
+    const double visc_work = sgt + u * dt[0] + v * dt[1] + w * dt[2];
+    const double heat = kap * dsutherdT * (T_x[0] * T_x[0] + T_x[1] * T_x[1] + T_x[2] * T_x[2]) +
+                        kap * suther * (Txx[0][0] + Txx[1][1] + Txx[2][2]);
+    S[0] = rho_t + u * rho_x[0] + v * rho_x[1] + w * rho_x[2] + rho * div_v;
+    S[1] = u * S[0] + rho * u_t + rho * u * u_x[0] + rho * v * u_x[1] + rho * w * u_x[2] + p_x[0] - dt[0];
+    S[2] = v * S[0] + rho * v_t + rho * u * v_x[0] + rho * v * v_x[1] + rho * w * v_x[2] + p_x[1] - dt[1];
+    S[3] = w * S[0] + rho * w_t + rho * u * w_x[0] + rho * v * w_x[1] + rho * w * w_x[2] + p_x[2] - dt[2];
+    S[4] = e * S[0] + rho * e_t + rho * (u * e_x[0] + v * e_x[1] + w * e_x[2]) + p * div_v + u * p_x[0] + v * p_x[1] +
+           w * p_x[2] - visc_work - heat;
+}
+
+// ---------------------------------------------------------------- solver state ---------------
+struct Elem {
+    int N[3];
+    int P[3];
+    int64_t off;
+    int face[6], fside[6];
+};
+struct Face {
+    int elem[2], side[2], rot;
+    int Nf[2], NelL[2], NelR[2], NfL[2], NfR[2], proj[2];
+    int64_t off;  // face point offset in the geometry arrays
+    std::vector<double> Q[2], Ux[2], Uy[2], Uz[2], mu[2];  // at Nf
+    std::vector<double> unStar[2];                         // (5,3, element-face dims)
+    std::vector<double> fStar[2];                          // (5, element-face dims)
+};
+
+struct Solver {
+    Phys ph;
+    dg_options opt;
+    int nodes;
+    int K;
+    std::vector<Elem> el;
+    std::vector<Face> fa;
+    std::vector<double> x, jaXi, jaEta, jaZeta, jac, invJac;
+    std::vector<double> fn, ft1, ft2, fj;
+    std::vector<double> Q, QDot, G, Ux, Uy, Uz, mu2;  // element storage, reference layout
+    int64_t ndof;
+};
+
+static int axis_of(int side, int a) {
+    static const int m[6][2] = {{0, 2}, {0, 2}, {0, 1}, {1, 2}, {0, 1}, {1, 2}};
+    return m[side - 1][a];
+}
+
+// Element-face trace (nv values per point at element-face dims n1 x n2) -> face storage at Nf
+// (FaceClass.f90:281-382 Face_AdaptSolutionToFace, :384-470 Face_AdaptGradientsToFace).
+static void adapt_to_face(const Face& f, int side, int nv, const std::vector<double>& e, int n1, int n2,
+                          std::vector<double>& out, int nodes) {
+    std::vector<double> rot;
+    const std::vector<double>* src = &e;
+    int s1 = n1, s2 = n2;
+    if (side == 1) {
+        s1 = f.NfL[0] + 1; s2 = f.NfL[1] + 1;
+    } else {
+        s1 = f.NfR[0] + 1; s2 = f.NfR[1] + 1;
+        rot.assign(nv * s1 * s2, 0.0);
+        for (int j = 0; j < s2; ++j)
+            for (int i = 0; i < s1; ++i) {
+                int ii, jj;
+                l2r(i, j, f.NfR[0], f.NfR[1], f.rot, ii, jj);
+                for (int v = 0; v < nv; ++v) rot[v + nv * (i + s1 * j)] = e[v + nv * (ii + n1 * jj)];
+            }
+        src = &rot;
+    }
+    const int q1 = f.Nf[0] + 1, q2 = f.Nf[1] + 1;
+    out.assign(nv * q1 * q2, 0.0);
+    const int pt = f.proj[side - 1];
+    const int* Ns = side == 1 ? f.NfL : f.NfR;
+    const std::vector<double>& S = *src;
+    if (pt == 0) { out = S; return; }
+    const std::vector<double> T1 = tset(nodes, Ns[0], f.Nf[0]);
+    const std::vector<double> T2 = tset(nodes, Ns[1], f.Nf[1]);
+    if (pt == 1) {
+        for (int j = 0; j < q2; ++j)
+            for (int l = 0; l < s1; ++l)
+                for (int i = 0; i < q1; ++i)
+                    for (int v = 0; v < nv; ++v) out[v + nv * (i + q1 * j)] += T1[i * s1 + l] * S[v + nv * (l + s1 * j)];
+    } else if (pt == 2) {
+        for (int l = 0; l < s2; ++l)
+            for (int j = 0; j < q2; ++j)
+                for (int i = 0; i < q1; ++i)
+                    for (int v = 0; v < nv; ++v) out[v + nv * (i + q1 * j)] += T2[j * s2 + l] * S[v + nv * (i + s1 * l)];
+    } else {
+        for (int l = 0; l < s2; ++l)
+            for (int j = 0; j < q2; ++j)
+                for (int m = 0; m < s1; ++m)
+                    for (int i = 0; i < q1; ++i)
+                        for (int v = 0; v < nv; ++v)
+                            out[v + nv * (i + q1 * j)] += T1[i * s1 + m] * T2[j * s2 + l] * S[v + nv * (m + s1 * l)];
+    }
+}
+
+// Face flux at Nf -> element-face storage of side (FaceClass.f90:597-703 / 865-963); sign applies
+// to side 2 (-1 for the Riemann flux, +1 for the BR1 jump).
+static void project_to_side(const Face& f, int side, int nv, const std::vector<double>& flux, std::vector<double>& out,
+                            double sign2, int nodes) {
+    const int q1 = f.Nf[0] + 1, q2 = f.Nf[1] + 1;
+    const int* Ns = side == 1 ? f.NfL : f.NfR;
+    const int s1 = Ns[0] + 1, s2 = Ns[1] + 1;
+    std::vector<double> aux(nv * s1 * s2, 0.0);
+    const int pt = f.proj[side - 1];
+    if (pt == 0) aux = flux;
+    else {
+        const std::vector<double> T1 = tset(nodes, f.Nf[0], Ns[0]);
+        const std::vector<double> T2 = tset(nodes, f.Nf[1], Ns[1]);
+        if (pt == 1) {
+            for (int j = 0; j < s2; ++j)
+                for (int l = 0; l < q1; ++l)
+                    for (int i = 0; i < s1; ++i)
+                        for (int v = 0; v < nv; ++v) aux[v + nv * (i + s1 * j)] += T1[i * q1 + l] * flux[v + nv * (l + q1 * j)];
+        } else if (pt == 2) {
+            for (int l = 0; l < q2; ++l)
+                for (int j = 0; j < s2; ++j)
+                    for (int i = 0; i < s1; ++i)
+                        for (int v = 0; v < nv; ++v) aux[v + nv * (i + s1 * j)] += T2[j * q2 + l] * flux[v + nv * (i + q1 * l)];
+        } else {
+            for (int l = 0; l < q2; ++l)
+                for (int j = 0; j < s2; ++j)
+                    for (int m = 0; m < q1; ++m)
+                        for (int i = 0; i < s1; ++i)
+                            for (int v = 0; v < nv; ++v)
+                                aux[v + nv * (i + s1 * j)] += T1[i * q1 + m] * T2[j * q2 + l] * flux[v + nv * (m + q1 * l)];
+        }
+    }
+    if (side == 1) { out = aux; return; }
+    // Right element: element-face dims are the unrotated NelR.
+    const int r1 = f.NelR[0] + 1, r2 = f.NelR[1] + 1;
+    out.assign(nv * r1 * r2, 0.0);
+    for (int j = 0; j < s2; ++j)
+        for (int i = 0; i < s1; ++i) {
+            int ii, jj;
+            l2r(i, j, f.NfR[0], f.NfR[1], f.rot, ii, jj);
+            for (int v = 0; v < nv; ++v) out[v + nv * (ii + r1 * jj)] = aux[v + nv * (i + s1 * j)];
+        }
+    for (auto& v : out) v = sign2 * v;
+}
+
+// Per-element face traces of an element array (HexElementClass.f90:233-372).
+static void prolong(const Solver& s, const Elem& e, int nv, const double* A, std::vector<double> tr[6]) {
+    const Nodal& sx = nodal(s.nodes, e.N[0]);
+    const Nodal& sy = nodal(s.nodes, e.N[1]);
+    const Nodal& sz = nodal(s.nodes, e.N[2]);
+    const int px = e.P[0], py = e.P[1], pz = e.P[2];
+    tr[ELEFT - 1].assign(nv * py * pz, 0.0);
+    tr[ERIGHT - 1].assign(nv * py * pz, 0.0);
+    tr[EFRONT - 1].assign(nv * px * pz, 0.0);
+    tr[EBACK - 1].assign(nv * px * pz, 0.0);
+    tr[EBOTTOM - 1].assign(nv * px * py, 0.0);
+    tr[ETOP - 1].assign(nv * px * py, 0.0);
+    for (int k = 0; k < pz; ++k)
+        for (int j = 0; j < py; ++j)
+            for (int i = 0; i < px; ++i) {
+                const double* a = A + nv * (i + px * (j + py * k));
+                for (int v = 0; v < nv; ++v) {
+                    tr[ELEFT - 1][v + nv * (j + py * k)] += a[v] * sx.vL[i];
+                    tr[ERIGHT - 1][v + nv * (j + py * k)] += a[v] * sx.vR[i];
+                    tr[EFRONT - 1][v + nv * (i + px * k)] += a[v] * sy.vL[j];
+                    tr[EBACK - 1][v + nv * (i + px * k)] += a[v] * sy.vR[j];
+                    tr[EBOTTOM - 1][v + nv * (i + px * j)] += a[v] * sz.vL[k];
+                    tr[ETOP - 1][v + nv * (i + px * j)] += a[v] * sz.vR[k];
+                }
+            }
+}
+
+static int face_dims(const Elem& e, int side, int a) { return e.P[axis_of(side, a)]; }
+
+// ---------------------------------------------------------------- right-hand side ----------
+static void compute_rhs(Solver& s, double t) {
+    const int K = s.K;
+    const bool ns = s.ph.ns;
+    // 1) prolong Q to faces (HexMesh.f90:948-1036)
+#pragma omp parallel for schedule(static)
+    for (int id = 0; id < K; ++id) {
+        const Elem& e = s.el[id];
+        std::vector<double> tr[6];
+        prolong(s, e, 5, &s.Q[5 * e.off], tr);
+        for (int side = 1; side <= 6; ++side) {
+            Face& f = s.fa[e.face[side - 1]];
+            const int fs = e.fside[side - 1];
+            adapt_to_face(f, fs, 5, tr[side - 1], face_dims(e, side, 0), face_dims(e, side, 1), f.Q[fs - 1], s.nodes);
+        }
+    }
+    // 2) BR1 gradients (EllipticBR1.f90:71-159, 168-397)
+    if (ns) {
+#pragma omp parallel for schedule(static)
+        for (int id = 0; id < K; ++id) {  // HexElement_ComputeLocalGradient (HexElementClass.f90:427-531)
+            const Elem& e = s.el[id];
+            const Nodal& sx = nodal(s.nodes, e.N[0]);
+            const Nodal& sy = nodal(s.nodes, e.N[1]);
+            const Nodal& sz = nodal(s.nodes, e.N[2]);
+            const int px = e.P[0], py = e.P[1], pz = e.P[2], np = px * py * pz;
+            const double* U = &s.Q[5 * e.off];
+            std::vector<double> Uxi(5 * np, 0.0), Ueta(5 * np, 0.0), Uzeta(5 * np, 0.0);
+            auto n = [&](int i, int j, int k) { return i + px * (j + py * k); };
+            for (int k = 0; k < pz; ++k) for (int j = 0; j < py; ++j) for (int l = 0; l < px; ++l) for (int i = 0; i < px; ++i)
+                for (int v = 0; v < 5; ++v) Uxi[5 * n(i, j, k) + v] += U[5 * n(l, j, k) + v] * sx.D[i * px + l];
+            for (int k = 0; k < pz; ++k) for (int l = 0; l < py; ++l) for (int j = 0; j < py; ++j) for (int i = 0; i < px; ++i)
+                for (int v = 0; v < 5; ++v) Ueta[5 * n(i, j, k) + v] += U[5 * n(i, l, k) + v] * sy.D[j * py + l];
+            for (int l = 0; l < pz; ++l) for (int k = 0; k < pz; ++k) for (int j = 0; j < py; ++j) for (int i = 0; i < px; ++i)
+                for (int v = 0; v < 5; ++v) Uzeta[5 * n(i, j, k) + v] += U[5 * n(i, j, l) + v] * sz.D[k * pz + l];
+            for (int q = 0; q < np; ++q) {
+                const int64_t g = e.off + q;
+                const double* a = &s.jaXi[3 * g];
+                const double* b = &s.jaEta[3 * g];
+                const double* c = &s.jaZeta[3 * g];
+                for (int v = 0; v < 5; ++v) {
+                    s.Ux[5 * g + v] = (Uxi[5 * q + v] * a[0] + Ueta[5 * q + v] * b[0] + Uzeta[5 * q + v] * c[0]) * s.invJac[g];
+                    s.Uy[5 * g + v] = (Uxi[5 * q + v] * a[1] + Ueta[5 * q + v] * b[1] + Uzeta[5 * q + v] * c[1]) * s.invJac[g];
+                    s.Uz[5 * g + v] = (Uxi[5 * q + v] * a[2] + Ueta[5 * q + v] * b[2] + Uzeta[5 * q + v] * c[2]) * s.invJac[g];
+                }
+            }
+        }
+        // BR1_ComputeElementInterfaceAverage (EllipticBR1.f90:571-627)
+#pragma omp parallel for schedule(static)
+        for (int fid = 0; fid < static_cast<int>(s.fa.size()); ++fid) {
+            Face& f = s.fa[fid];
+            const int q1 = f.Nf[0] + 1, q2 = f.Nf[1] + 1;
+            std::vector<double> us(15 * q1 * q2);
+            for (int j = 0; j < q2; ++j)
+                for (int i = 0; i < q1; ++i) {
+                    const int p = i + q1 * j;
+                    const double J = s.fj[f.off + p];
+                    const double* n = &s.fn[3 * (f.off + p)];
+                    for (int v = 0; v < 5; ++v) {
+                        const double u = 0.5 * (f.Q[1][5 * p + v] - f.Q[0][5 * p + v]) * J;
+                        us[15 * p + v] = u * n[0];
+                        us[15 * p + 5 + v] = u * n[1];
+                        us[15 * p + 10 + v] = u * n[2];
+                    }
+                }
+            project_to_side(f, 1, 15, us, f.unStar[0], 1.0, s.nodes);
+            project_to_side(f, 2, 15, us, f.unStar[1], 1.0, s.nodes);
+        }
+        // BR1_GradientFaceLoop + ProlongGradientsToFaces (EllipticBR1.f90:531-569; DGIntegrals.f90:365-443)
+#pragma omp parallel for schedule(static)
+        for (int id = 0; id < K; ++id) {
+            const Elem& e = s.el[id];
+            const Nodal& sx = nodal(s.nodes, e.N[0]);
+            const Nodal& sy = nodal(s.nodes, e.N[1]);
+            const Nodal& sz = nodal(s.nodes, e.N[2]);
+            const int px = e.P[0], py = e.P[1], pz = e.P[2];
+            auto H = [&](int side) -> const std::vector<double>& {
+                return s.fa[e.face[side - 1]].unStar[e.fside[side - 1] - 1];
+            };
+            const std::vector<double>&HF = H(EFRONT), &HBK = H(EBACK), &HBO = H(EBOTTOM), &HR = H(ERIGHT),
+                                    &HT = H(ETOP), &HL = H(ELEFT);
+            for (int k = 0; k < pz; ++k)
+                for (int j = 0; j < py; ++j)
+                    for (int i = 0; i < px; ++i) {
+                        const int64_t g = e.off + i + px * (j + py * k);
+                        for (int d = 0; d < 3; ++d) {
+                            double* Ud = d == 0 ? &s.Ux[5 * g] : (d == 1 ? &s.Uy[5 * g] : &s.Uz[5 * g]);
+                            for (int v = 0; v < 5; ++v) {
+                                double fi = HL[v + 5 * d + 15 * (j + py * k)] * sx.bL[i];
+                                fi = fi + HR[v + 5 * d + 15 * (j + py * k)] * sx.bR[i];
+                                fi = fi + HF[v + 5 * d + 15 * (i + px * k)] * sy.bL[j];
+                                fi = fi + HBK[v + 5 * d + 15 * (i + px * k)] * sy.bR[j];
+                                fi = fi + HBO[v + 5 * d + 15 * (i + px * j)] * sz.bL[k];
+                                fi = fi + HT[v + 5 * d + 15 * (i + px * j)] * sz.bR[k];
+                                Ud[v] = Ud[v] + fi * s.invJac[g];
+                            }
+                        }
+                    }
+            std::vector<double> tx[6], ty[6], tz[6];
+            prolong(s, e, 5, &s.Ux[5 * e.off], tx);
+            prolong(s, e, 5, &s.Uy[5 * e.off], ty);
+            prolong(s, e, 5, &s.Uz[5 * e.off], tz);
+            for (int side = 1; side <= 6; ++side) {
+                Face& f = s.fa[e.face[side - 1]];
+                const int fs = e.fside[side - 1];
+                const int d1 = face_dims(e, side, 0), d2 = face_dims(e, side, 1);
+                adapt_to_face(f, fs, 5, tx[side - 1], d1, d2, f.Ux[fs - 1], s.nodes);
+                adapt_to_face(f, fs, 5, ty[side - 1], d1, d2, f.Uy[fs - 1], s.nodes);
+                adapt_to_face(f, fs, 5, tz[side - 1], d1, d2, f.Uz[fs - 1], s.nodes);
+            }
+        }
+    }
+    // 3) TimeDerivative_ComputeQDot (SpatialDiscretization.f90:379-685)
+    if (ns) {
+#pragma omp parallel for schedule(static)
+        for (int64_t g = 0; g < s.ndof; ++g) mu_kappa(s.ph, &s.Q[5 * g], s.mu2[2 * g], s.mu2[2 * g + 1]);
+#pragma omp parallel for schedule(static)
+        for (int fid = 0; fid < static_cast<int>(s.fa.size()); ++fid) {
+            Face& f = s.fa[fid];
+            const int np = (f.Nf[0] + 1) * (f.Nf[1] + 1);
+            for (int side = 0; side < 2; ++side) {
+                f.mu[side].resize(2 * np);
+                for (int p = 0; p < np; ++p) mu_kappa(s.ph, &f.Q[side][5 * p], f.mu[side][2 * p], f.mu[side][2 * p + 1]);
+            }
+        }
+    }
+    // Volume integrals (SpatialDiscretization.f90:1602-1682)
+#pragma omp parallel for schedule(static)
+    for (int id = 0; id < K; ++id) {
+        const Elem& e = s.el[id];
+        const Nodal& sx = nodal(s.nodes, e.N[0]);
+        const Nodal& sy = nodal(s.nodes, e.N[1]);
+        const Nodal& sz = nodal(s.nodes, e.N[2]);
+        const int px = e.P[0], py = e.P[1], pz = e.P[2], np = px * py * pz;
+        std::vector<double> Fi(15 * np), Fv(15 * np, 0.0);  // contravariant: F[v + 5*(n) + 5*np*d]
+        auto n = [&](int i, int j, int k) { return i + px * (j + py * k); };
+        for (int q = 0; q < np; ++q) {
+            const int64_t g = e.off + q;
+            double cf[15];
+            euler_flux(s.ph, &s.Q[5 * g], cf);
+            const double* ja[3] = {&s.jaXi[3 * g], &s.jaEta[3 * g], &s.jaZeta[3 * g]};
+            for (int d = 0; d < 3; ++d)
+                for (int v = 0; v < 5; ++v)
+                    Fi[v + 5 * q + 5 * np * d] = cf[v] * ja[d][0] + cf[v + 5] * ja[d][1] + cf[v + 10] * ja[d][2];
+            if (ns) {
+                viscous_flux(s.ph, &s.Q[5 * g], &s.Ux[5 * g], &s.Uy[5 * g], &s.Uz[5 * g], s.mu2[2 * g], 0.0, s.mu2[2 * g + 1], cf);
+                for (int d = 0; d < 3; ++d)
+                    for (int v = 0; v < 5; ++v)
+                        Fv[v + 5 * q + 5 * np * d] = cf[v] * ja[d][0] + cf[v + 5] * ja[d][1] + cf[v + 10] * ja[d][2];
+            }
+        }
+        double* qd = &s.QDot[5 * e.off];
+        for (int q = 0; q < 5 * np; ++q) qd[q] = 0.0;
+        if (s.opt.inviscid == DG_INVISCID_STANDARD) {
+            std::vector<double> Fc(15 * np);
+            for (int q = 0; q < 15 * np; ++q) Fc[q] = Fi[q] - Fv[q];
+            // ScalarWeakIntegrals_StdVolumeGreen (DGIntegrals.f90:56-87)
+            for (int k = 0; k < pz; ++k) for (int j = 0; j < py; ++j) for (int l = 0; l < px; ++l) for (int i = 0; i < px; ++i)
+                for (int v = 0; v < 5; ++v) qd[5 * n(i, j, k) + v] += sx.hatD[i * px + l] * Fc[v + 5 * n(l, j, k)];
+            for (int k = 0; k < pz; ++k) for (int l = 0; l < py; ++l) for (int j = 0; j < py; ++j) for (int i = 0; i < px; ++i)
+                for (int v = 0; v < 5; ++v) qd[5 * n(i, j, k) + v] += sy.hatD[j * py + l] * Fc[v + 5 * n(i, l, k) + 5 * np];
+            for (int l = 0; l < pz; ++l) for (int k = 0; k < pz; ++k) for (int j = 0; j < py; ++j) for (int i = 0; i < px; ++i)
+                for (int v = 0; v < 5; ++v) qd[5 * n(i, j, k) + v] += sz.hatD[k * pz + l] * Fc[v + 5 * n(i, j, l) + 10 * np];
+        } else {
+            // SplitDG_ComputeSplitFormFluxes (HyperbolicSplitForm.f90:64-116) and
+            // ScalarWeakIntegrals_SplitVolumeDivergence (DGIntegrals.f90:92-129), negated.
+            std::vector<double> fS(5 * px * np), gS(5 * py * np), hS(5 * pz * np);
+            auto fi = [&](int l, int q) { return 5 * (l + px * q); };
+            auto gi = [&](int l, int q) { return 5 * (l + py * q); };
+            auto hi = [&](int l, int q) { return 5 * (l + pz * q); };
+            for (int k = 0; k < pz; ++k) for (int j = 0; j < py; ++j) for (int i = 0; i < px; ++i)
+                for (int v = 0; v < 5; ++v) {
+                    fS[fi(i, n(i, j, k)) + v] = Fi[v + 5 * n(i, j, k)];
+                    gS[gi(j, n(i, j, k)) + v] = Fi[v + 5 * n(i, j, k) + 5 * np];
+                    hS[hi(k, n(i, j, k)) + v] = Fi[v + 5 * n(i, j, k) + 10 * np];
+                }
+            const double* Q = &s.Q[5 * e.off];
+            const double* jx = &s.jaXi[3 * e.off];
+            const double* je = &s.jaEta[3 * e.off];
+            const double* jz = &s.jaZeta[3 * e.off];
+            for (int k = 0; k < pz; ++k) for (int j = 0; j < py; ++j) for (int i = 0; i < px; ++i)
+                for (int l = i + 1; l < px; ++l) {
+                    double* o = &fS[fi(l, n(i, j, k))];
+                    two_point(s.ph, s.opt.averaging, Q + 5 * n(i, j, k), Q + 5 * n(l, j, k), jx + 3 * n(i, j, k), jx + 3 * n(l, j, k), o);
+                    for (int v = 0; v < 5; ++v) fS[fi(i, n(l, j, k)) + v] = o[v];
+                }
+            for (int k = 0; k < pz; ++k) for (int j = 0; j < py; ++j) for (int i = 0; i < px; ++i)
+                for (int l = j + 1; l < py; ++l) {
+                    double* o = &gS[gi(l, n(i, j, k))];
+                    two_point(s.ph, s.opt.averaging, Q + 5 * n(i, j, k), Q + 5 * n(i, l, k), je + 3 * n(i, j, k), je + 3 * n(i, l, k), o);
+                    for (int v = 0; v < 5; ++v) gS[gi(j, n(i, l, k)) + v] = o[v];
+                }
+            for (int k = 0; k < pz; ++k) for (int j = 0; j < py; ++j) for (int i = 0; i < px; ++i)
+                for (int l = k + 1; l < pz; ++l) {
+                    double* o = &hS[hi(l, n(i, j, k))];
+                    two_point(s.ph, s.opt.averaging, Q + 5 * n(i, j, k), Q + 5 * n(i, j, l), jz + 3 * n(i, j, k), jz + 3 * n(i, j, l), o);
+                    for (int v = 0; v < 5; ++v) hS[hi(k, n(i, j, l)) + v] = o[v];
+                }
+            std::vector<double> vi(5 * np, 0.0);
+            for (int k = 0; k < pz; ++k) for (int j = 0; j < py; ++j) for (int l = 0; l < px; ++l) for (int i = 0; i < px; ++i)
+                for (int v = 0; v < 5; ++v)
+                    vi[5 * n(i, j, k) + v] = vi[5 * n(i, j, k) + v] + sx.sharpD[i * px + l] * fS[fi(l, n(i, j, k)) + v] +
+                                             sx.hatD[i * px + l] * Fv[v + 5 * n(l, j, k)];
+            for (int k = 0; k < pz; ++k) for (int l = 0; l < py; ++l) for (int j = 0; j < py; ++j) for (int i = 0; i < px; ++i)
+                for (int v = 0; v < 5; ++v)
+                    vi[5 * n(i, j, k) + v] = vi[5 * n(i, j, k) + v] + sy.sharpD[j * py + l] * gS[gi(l, n(i, j, k)) + v] +
+                                             sy.hatD[j * py + l] * Fv[v + 5 * n(i, l, k) + 5 * np];
+            for (int l = 0; l < pz; ++l) for (int k = 0; k < pz; ++k) for (int j = 0; j < py; ++j) for (int i = 0; i < px; ++i)
+                for (int v = 0; v < 5; ++v)
+                    vi[5 * n(i, j, k) + v] = vi[5 * n(i, j, k) + v] + sz.sharpD[k * pz + l] * hS[hi(l, n(i, j, k)) + v] +
+                                             sz.hatD[k * pz + l] * Fv[v + 5 * n(i, j, l) + 10 * np];
+            for (int q = 0; q < 5 * np; ++q) qd[q] = -vi[q];
+        }
+    }
+    // Interface fluxes (SpatialDiscretization.f90:1710-1799)
+#pragma omp parallel for schedule(static)
+    for (int fid = 0; fid < static_cast<int>(s.fa.size()); ++fid) {
+        Face& f = s.fa[fid];
+        const int q1 = f.Nf[0] + 1, q2 = f.Nf[1] + 1, np = q1 * q2;
+        std::vector<double> flux(5 * np);
+        for (int p = 0; p < np; ++p) {
+            double visc[5] = {0, 0, 0, 0, 0};
+            const double* n = &s.fn[3 * (f.off + p)];
+            if (ns) {  // BR1_RiemannSolver (EllipticBR1.f90:816-868)
+                double fL[15], fR[15];
+                viscous_flux(s.ph, &f.Q[0][5 * p], &f.Ux[0][5 * p], &f.Uy[0][5 * p], &f.Uz[0][5 * p], f.mu[0][2 * p], 0.0,
+                             f.mu[0][2 * p + 1], fL);
+                viscous_flux(s.ph, &f.Q[1][5 * p], &f.Ux[1][5 * p], &f.Uy[1][5 * p], &f.Uz[1][5 * p], f.mu[1][2 * p], 0.0,
+                             f.mu[1][2 * p + 1], fR);
+                for (int v = 0; v < 5; ++v) {
+                    const double a = 0.5 * (fL[v] + fR[v]), b = 0.5 * (fL[v + 5] + fR[v + 5]), c = 0.5 * (fL[v + 10] + fR[v + 10]);
+                    visc[v] = a * n[0] + b * n[1] + c * n[2];
+                }
+            }
+            double inv[5];
+            if (s.opt.riemann == DG_RIEMANN_ROE) roe(s.ph, &f.Q[0][5 * p], &f.Q[1][5 * p], n, inv);
+            else lxf(s.ph, s.opt.averaging, s.opt.lambda_stab, &f.Q[0][5 * p], &f.Q[1][5 * p], n, &s.ft1[3 * (f.off + p)],
+                     &s.ft2[3 * (f.off + p)], inv);
+            for (int v = 0; v < 5; ++v) flux[5 * p + v] = (inv[v] - visc[v]) * s.fj[f.off + p];
+        }
+        project_to_side(f, 1, 5, flux, f.fStar[0], -1.0, s.nodes);
+        project_to_side(f, 2, 5, flux, f.fStar[1], -1.0, s.nodes);
+    }
+    // Surface integrals, 1/J, source (SpatialDiscretization.f90:483-494, 1686-1701, 564-639)
+    const double mms_mu = s.ph.mu, mms_kap = s.ph.kappa;
+#pragma omp parallel for schedule(static)
+    for (int id = 0; id < K; ++id) {
+        const Elem& e = s.el[id];
+        const Nodal& sx = nodal(s.nodes, e.N[0]);
+        const Nodal& sy = nodal(s.nodes, e.N[1]);
+        const Nodal& sz = nodal(s.nodes, e.N[2]);
+        const int px = e.P[0], py = e.P[1], pz = e.P[2];
+        auto Fs = [&](int side) -> const std::vector<double>& { return s.fa[e.face[side - 1]].fStar[e.fside[side - 1] - 1]; };
+        const std::vector<double>&FFR = Fs(EFRONT), &FBK = Fs(EBACK), &FBO = Fs(EBOTTOM), &FR = Fs(ERIGHT), &FT = Fs(ETOP),
+                                &FL = Fs(ELEFT);
+        for (int k = 0; k < pz; ++k)
+            for (int j = 0; j < py; ++j)
+                for (int i = 0; i < px; ++i) {
+                    const int64_t g = e.off + i + px * (j + py * k);
+                    for (int v = 0; v < 5; ++v) {
+                        double fi = FL[v + 5 * (j + py * k)] * sx.bL[i];
+                        fi = fi + FR[v + 5 * (j + py * k)] * sx.bR[i];
+                        fi = fi + FFR[v + 5 * (i + px * k)] * sy.bL[j];
+                        fi = fi + FBK[v + 5 * (i + px * k)] * sy.bR[j];
+                        fi = fi + FBO[v + 5 * (i + px * j)] * sz.bL[k];
+                        fi = fi + FT[v + 5 * (i + px * j)] * sz.bR[k];
+                        s.QDot[5 * g + v] = s.QDot[5 * g + v] - fi;
+                        s.QDot[5 * g + v] = s.QDot[5 * g + v] / s.jac[g];
+                    }
+                    if (s.opt.source == DG_SOURCE_MMS_CONVERGENCE) {
+                        double Qe[5], S[5], Qd[5];
+                        const double* xx = &s.x[3 * g];
+                        mms_point(xx[0], xx[1], xx[2], t, s.ph.gm1, s.ph.gammaM2, mms_mu, mms_kap, Qe, S, Qd);
+                        for (int v = 0; v < 5; ++v) s.QDot[5 * g + v] = s.QDot[5 * g + v] + S[v];
+                    }
+                }
+    }
+}
+
+// DGSEMClass.f90:870-1038 MaxTimeStep.
+static double max_dt(const Solver& s, double cfl, double dcfl) {
+    double conv = HUGE_VAL, visc = HUGE_VAL;
+#pragma omp parallel for schedule(static) reduction(min : conv, visc)
+    for (int id = 0; id < s.K; ++id) {
+        const Elem& e = s.el[id];
+        double dd[3], dd2[3];
+        for (int d = 0; d < 3; ++d) {
+            const Nodal& sp = nodal(s.nodes, e.N[d]);
+            dd[d] = e.N[d] != 0 ? 1.0 / std::fabs(sp.x[1] - sp.x[0]) : 0.0;
+            dd2[d] = dd[d] * dd[d];
+        }
+        const int np = e.P[0] * e.P[1] * e.P[2];
+        for (int q = 0; q < np; ++q) {
+            const int64_t g = e.off + q;
+            const double* Q = &s.Q[5 * g];
+            const double a = std::sqrt(s.ph.gamma * pressure(s.ph, Q) / Q[0]);
+            const double ev[3] = {std::fabs(Q[1] / Q[0]) + a, std::fabs(Q[2] / Q[0]) + a, std::fabs(Q[3] / Q[0]) + a};
+            const double* ja[3] = {&s.jaXi[3 * g], &s.jaEta[3 * g], &s.jaZeta[3 * g]};
+            double lam[3];
+            for (int d = 0; d < 3; ++d) lam[d] = std::fabs(ja[d][0] * ev[0] + ja[d][1] * ev[1] + ja[d][2] * ev[2]) * dd[d];
+            conv = std::fmin(conv, cfl * std::fabs(s.jac[g]) / (lam[0] + lam[1] + lam[2]));
+            if (s.ph.ns) {
+                const double T = s.ph.gammaM2 * pressure(s.ph, Q) / Q[0];
+                const double mu = sutherland(s.ph, T);
+                double lv[3];
+                for (int d = 0; d < 3; ++d) lv[d] = mu * dd2[d] * std::fabs(ja[d][0] + ja[d][1] + ja[d][2]);
+                visc = std::fmin(visc, dcfl * std::fabs(s.jac[g]) / (lv[0] + lv[1] + lv[2]));
+            }
+        }
+    }
+    return conv < visc ? conv : visc;
+}
+
+}  // namespace orc
+
+// ---------------------------------------------------------------- C API ----------------------
+using orc::Solver;
+
+extern "C" {
+
+void* orc_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op) {
+    auto* s = new Solver();
+    s->opt = *op;
+    s->nodes = m->node_type;
+    s->K = m->n_elements;
+    s->ph.Mach = ph->mach;
+    s->ph.Re = ph->reynolds;
+    s->ph.Pr = ph->prandtl;
+    s->ph.ns = ph->navier_stokes != 0;
+    // PhysicsStorage_NS.f90:186-290,413-429
+    s->ph.gammaM2 = s->ph.gamma * (ph->mach * ph->mach);
+    if (s->ph.ns) {
+        s->ph.mu = 1.0 / ph->reynolds;
+        s->ph.kappa = 1.0 / (s->ph.gm1 * (ph->mach * ph->mach) * ph->reynolds * ph->prandtl);
+        s->ph.mu_to_kappa = 1.0 / (s->ph.gm1 * (ph->mach * ph->mach) * ph->prandtl);
+    } else {
+        s->ph.mu = s->ph.kappa = s->ph.mu_to_kappa = 0.0;
+    }
+    const double TRef = 520.0 * 5.0 / 9.0;
+    s->ph.S_div_TRef = (198.6 * 5.0 / 9.0) / TRef;
+    s->ph.TReNorm = TRef / TRef;
+    s->el.resize(s->K);
+    int64_t off = 0;
+    for (int e = 0; e < s->K; ++e) {
+        auto& E = s->el[e];
+        for (int d = 0; d < 3; ++d) { E.N[d] = m->order[3 * e + d]; E.P[d] = E.N[d] + 1; }
+        E.off = off;
+        off += static_cast<int64_t>(E.P[0]) * E.P[1] * E.P[2];
+    }
+    s->ndof = off;
+    auto cp = [&](const double* src, int64_t n) { return std::vector<double>(src, src + n); };
+    s->x = cp(m->x, 3 * off);
+    s->jaXi = cp(m->ja_xi, 3 * off); s->jaEta = cp(m->ja_eta, 3 * off); s->jaZeta = cp(m->ja_zeta, 3 * off);
+    s->jac = cp(m->jacobian, off); s->invJac = cp(m->inv_jacobian, off);
+    s->fa.resize(m->n_faces);
+    int64_t foff = 0;
+    for (int f = 0; f < m->n_faces; ++f) {
+        auto& F = s->fa[f];
+        for (int q = 0; q < 2; ++q) {
+            F.elem[q] = m->face_elem[2 * f + q];
+            F.side[q] = m->face_side[2 * f + q];
+            F.Nf[q] = m->face_nf[2 * f + q];
+            s->el[F.elem[q]].face[F.side[q] - 1] = f;
+            s->el[F.elem[q]].fside[F.side[q] - 1] = q + 1;
+        }
+        F.rot = m->face_rotation[f];
+        for (int a = 0; a < 2; ++a) {
+            F.NelL[a] = s->el[F.elem[0]].N[orc::axis_of(F.side[0], a)];
+            F.NelR[a] = s->el[F.elem[1]].N[orc::axis_of(F.side[1], a)];
+            F.NfL[a] = F.NelL[a];
+        }
+        switch (F.rot) {
+            case 0: case 2: case 5: case 7: F.NfR[0] = F.NelR[0]; F.NfR[1] = F.NelR[1]; break;
+            default: F.NfR[0] = F.NelR[1]; F.NfR[1] = F.NelR[0]; break;
+        }
+        auto ptype = [&](const int* Ns) {
+            const bool a = Ns[0] != F.Nf[0], b = Ns[1] != F.Nf[1];
+            return (!a && !b) ? 0 : (a && !b) ? 1 : (!a && b) ? 2 : 3;
+        };
+        F.proj[0] = ptype(F.NfL);
+        F.proj[1] = ptype(F.NfR);
+        F.off = foff;
+        foff += static_cast<int64_t>(F.Nf[0] + 1) * (F.Nf[1] + 1);
+    }
+    s->fn = cp(m->face_normal, 3 * foff); s->ft1 = cp(m->face_t1, 3 * foff); s->ft2 = cp(m->face_t2, 3 * foff);
+    s->fj = cp(m->face_jacobian, foff);
+    s->Q.assign(5 * off, 0.0); s->QDot.assign(5 * off, 0.0); s->G.assign(5 * off, 0.0);
+    s->Ux.assign(5 * off, 0.0); s->Uy.assign(5 * off, 0.0); s->Uz.assign(5 * off, 0.0);
+    s->mu2.assign(2 * off, 0.0);
+    return s;
+}
+
+void orc_destroy(void* h) { delete static_cast<Solver*>(h); }
+int64_t orc_ndof(void* h) { return static_cast<Solver*>(h)->ndof; }
+
+void orc_set_state(void* h, const double* q) {
+    auto* s = static_cast<Solver*>(h);
+    std::memcpy(s->Q.data(), q, sizeof(double) * 5 * s->ndof);
+    std::fill(s->G.begin(), s->G.end(), 0.0);
+}
+
+// field: 0 Q, 1 QDot, 2 G, 3/4/5 U_x/U_y/U_z
+void orc_get(void* h, int field, double* out) {
+    auto* s = static_cast<Solver*>(h);
+    const std::vector<double>* v[] = {&s->Q, &s->QDot, &s->G, &s->Ux, &s->Uy, &s->Uz};
+    std::memcpy(out, v[field]->data(), sizeof(double) * 5 * s->ndof);
+}
+
+void orc_rhs(void* h, double t) { orc::compute_rhs(*static_cast<Solver*>(h), t); }
+
+// ExplicitMethods.f90:748-779 (the dt_vec-free branch).
+void orc_rk3_step(void* h, double t, double dt) {
+    auto* s = static_cast<Solver*>(h);
+    const double a[3] = {0.0, -5.0 / 9.0, -153.0 / 128.0};
+    const double b[3] = {0.0, 1.0 / 3.0, 3.0 / 4.0};
+    const double c[3] = {1.0 / 3.0, 15.0 / 16.0, 8.0 / 15.0};
+    for (int k = 0; k < 3; ++k) {
+        orc::compute_rhs(*s, t + b[k] * dt);
+        const int64_t n = 5 * s->ndof;
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < n; ++i) {
+            s->G[i] = a[k] * s->G[i] + s->QDot[i];
+            s->Q[i] = s->Q[i] + c[k] * dt * s->G[i];
+        }
+    }
+}
+
+double orc_max_dt(void* h, double cfl, double dcfl) { return orc::max_dt(*static_cast<Solver*>(h), cfl, dcfl); }
+
+// DGSEMClass.f90:770-868 ComputeMaxResiduals; returns 1 if Q holds a NaN (checkForNan).
+int orc_residuals(void* h, double* res) {
+    auto* s = static_cast<Solver*>(h);
+    for (int v = 0; v < 5; ++v) res[v] = 0.0;
+    int nan = 0;
+    for (int64_t g = 0; g < s->ndof; ++g)
+        for (int v = 0; v < 5; ++v) {
+            res[v] = std::fmax(res[v], std::fabs(s->QDot[5 * g + v]));
+            if (std::isnan(s->Q[5 * g + v])) nan = 1;
+        }
+    return nan;
+}
+
+// Manufactured solution of the Convergence case at the nodes: writes Q (and QDot) at time t.
+void orc_mms_state(void* h, double t, double* q, double* qdot) {
+    auto* s = static_cast<Solver*>(h);
+    for (int64_t g = 0; g < s->ndof; ++g) {
+        double S[5];
+        orc::mms_point(s->x[3 * g], s->x[3 * g + 1], s->x[3 * g + 2], t, s->ph.gm1, s->ph.gammaM2, s->ph.mu, s->ph.kappa,
+                       q + 5 * g, S, qdot ? qdot + 5 * g : S);
+    }
+}
+
+}  // extern "C"

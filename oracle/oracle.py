@@ -1,0 +1,102 @@
+"""ORACLE -- test infrastructure only (tests/, __graft_entry__.smoke(), bench.py cpu_baseline).
+
+ctypes front end of oracle/dg_oracle.cpp, the CPU FP64 restatement of HORSES3D's
+ComputeTimeDerivative / TakeRK3Step / MaxTimeStep / ComputeMaxResiduals. The product never imports
+this module. ``build()`` compiles the library with oracle/Makefile.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+ORACLE_DIR = Path(__file__).resolve().parent
+LIB = ORACLE_DIR / "_build" / "libh3d_oracle.so"
+
+_f64p = C.POINTER(C.c_double)
+_lib = None
+
+
+def build(quiet: bool = True) -> Path:
+    out = subprocess.run(["make", "-C", str(ORACLE_DIR)], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{out.stdout}\n{out.stderr}")
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build()
+        L = C.CDLL(str(LIB))
+        L.orc_create.restype = C.c_void_p
+        L.orc_create.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_destroy.argtypes = [C.c_void_p]
+        L.orc_ndof.restype = C.c_int64
+        L.orc_ndof.argtypes = [C.c_void_p]
+        L.orc_set_state.argtypes = [C.c_void_p, _f64p]
+        L.orc_get.argtypes = [C.c_void_p, C.c_int, _f64p]
+        L.orc_rhs.argtypes = [C.c_void_p, C.c_double]
+        L.orc_rk3_step.argtypes = [C.c_void_p, C.c_double, C.c_double]
+        L.orc_max_dt.restype = C.c_double
+        L.orc_max_dt.argtypes = [C.c_void_p, C.c_double, C.c_double]
+        L.orc_residuals.restype = C.c_int
+        L.orc_residuals.argtypes = [C.c_void_p, _f64p]
+        L.orc_mms_state.argtypes = [C.c_void_p, C.c_double, _f64p, _f64p]
+        _lib = L
+    return _lib
+
+
+def set_threads(n: int) -> None:
+    os.environ["OMP_NUM_THREADS"] = str(n)
+
+
+class Oracle:
+    """One oracle solver on a mesh (a HexMesh or anything with a ``desc`` dg_mesh_desc)."""
+
+    def __init__(self, mesh, physics, options):
+        self.mesh = mesh
+        self.physics = physics
+        self.options = options
+        self._h = lib().orc_create(C.byref(mesh.desc), C.byref(physics), C.byref(options))
+        self.ndof = int(lib().orc_ndof(self._h))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_destroy(self._h)
+            self._h = None
+
+    def set_state(self, q: np.ndarray) -> None:
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        assert q.size == 5 * self.ndof
+        lib().orc_set_state(self._h, q.ctypes.data_as(_f64p))
+
+    def get(self, field: int) -> np.ndarray:
+        out = np.empty(5 * self.ndof)
+        lib().orc_get(self._h, field, out.ctypes.data_as(_f64p))
+        return out
+
+    def rhs(self, t: float) -> np.ndarray:
+        lib().orc_rhs(self._h, t)
+        return self.get(1)
+
+    def rk3_step(self, t: float, dt: float) -> None:
+        lib().orc_rk3_step(self._h, t, dt)
+
+    def max_dt(self, cfl: float, dcfl: float) -> float:
+        return float(lib().orc_max_dt(self._h, cfl, dcfl))
+
+    def residuals(self):
+        r = np.zeros(5)
+        nan = lib().orc_residuals(self._h, r.ctypes.data_as(_f64p))
+        return r, bool(nan)
+
+    def mms_state(self, t: float):
+        q = np.empty(5 * self.ndof)
+        qd = np.empty(5 * self.ndof)
+        lib().orc_mms_state(self._h, t, q.ctypes.data_as(_f64p), qd.ctypes.data_as(_f64p))
+        return q, qd
