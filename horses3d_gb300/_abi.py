@@ -91,8 +91,10 @@ SIGNATURES = [
     ("dg_download", C.c_int, [C.c_void_p, C.c_int, _f64p]),
     ("dg_ndof", C.c_int64, [C.c_void_p]),
     ("dg_rhs", C.c_int, [C.c_void_p, C.c_double]),
-    ("dg_rk3_step", C.c_int, [C.c_void_p, C.c_double, C.c_double, _f64p]),
-    ("dg_run_steps", C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double]),
+    ("dg_rk3_step", C.c_int, [C.c_void_p, C.c_double, C.c_double]),
+    ("dg_run_steps", C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, _f64p]),
+    ("dg_time_steps", C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, _f64p]),
+    ("dg_kernel_times", C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, _f64p]),
     ("dg_max_dt", C.c_int, [C.c_void_p, C.c_double, C.c_double, _f64p]),
     ("dg_residuals", C.c_int, [C.c_void_p, _f64p, C.POINTER(C.c_int)]),
     ("dg_synchronize", C.c_int, [C.c_void_p]),

@@ -1,0 +1,169 @@
+"""The .control keys that select the hot path, read the way the reference reads them.
+
+``read_control`` follows ReadControlFile (io/ReadInputFile.f90:20-130): ``key = value`` lines,
+keys case-insensitive, ``!`` comments, ``#define boundary <name>`` ... ``#end`` blocks (only the
+periodic ``coupled boundary`` pairs matter here). Defaults are the reference's:
+Gauss nodes (main.f90:239-324), Roe (RiemannSolvers_NS.f90:201-204), standard averaging, lambda 1,
+standard inviscid form, BR1, Prandtl 0.72, RK3. The extra key ``gpu precision = fp64 | mixed``
+selects the plain or the mixed-precision form. Options outside the GPU path raise
+``UnsupportedOption`` so the caller keeps the reference's CPU path for them.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from pathlib import Path
+
+from . import _abi
+
+
+class UnsupportedOption(ValueError):
+    pass
+
+
+@dataclass
+class Config:
+    mesh_file: str | None = None
+    order: int = 3
+    nodes: int = _abi.DG_NODES_GAUSS
+    flow: str = "ns"
+    mach: float = 0.1
+    reynolds: float = 1600.0
+    prandtl: float = 0.72
+    riemann: int = _abi.DG_RIEMANN_ROE
+    averaging: int = _abi.DG_AVG_STANDARD
+    inviscid: int = _abi.DG_INVISCID_STANDARD
+    lambda_stab: float = 1.0
+    precision: int = _abi.DG_PRECISION_FP64
+    source: int = _abi.DG_SOURCE_NONE
+    cfl: float | None = None
+    dcfl: float | None = None
+    dt: float | None = None
+    n_steps: int = 1
+    t_final: float | None = None
+    periodic: list = field(default_factory=list)
+
+    def physics(self) -> _abi.DgPhysics:
+        return _abi.DgPhysics(self.mach, self.reynolds, self.prandtl, 1 if self.flow == "ns" else 0)
+
+    def options(self) -> _abi.DgOptions:
+        return _abi.DgOptions(self.inviscid, self.riemann, self.averaging, self.lambda_stab, self.precision,
+                              self.source)
+
+    def periodic_spec(self) -> str:
+        return ",".join(f"{a}:{b}" for a, b in self.periodic)
+
+
+_RIEMANN = {"roe": _abi.DG_RIEMANN_ROE, "lax-friedrichs": _abi.DG_RIEMANN_LXF}
+_AVERAGING = {"standard": _abi.DG_AVG_STANDARD, "pirozzoli": _abi.DG_AVG_PIROZZOLI}
+
+
+def _value(v: str) -> str:
+    v = v.split("!")[0].strip()
+    if len(v) >= 2 and v[0] == v[-1] and v[0] in "\"'":
+        v = v[1:-1]
+    return v.strip()
+
+
+def parse_control(text: str) -> Config:
+    cfg = Config()
+    keys: dict[str, str] = {}
+    blocks = []
+    block = None
+    for raw in text.splitlines():
+        line = raw.split("!")[0].strip() if not raw.strip().startswith("#") else raw.strip()
+        if not line:
+            continue
+        low = line.lower()
+        if low.startswith("#define"):
+            block = {"kind": low.split()[1] if len(low.split()) > 1 else "", "name": " ".join(low.split()[2:])}
+            continue
+        if low.startswith("#end"):
+            if block is not None:
+                blocks.append(block)
+            block = None
+            continue
+        if "=" not in line:
+            continue
+        k, v = line.split("=", 1)
+        k = " ".join(k.strip().lower().split())
+        if block is not None:
+            block[k] = _value(v)
+        else:
+            keys[k] = _value(v)
+
+    def get(k, default=None):
+        return keys.get(k, default)
+
+    cfg.mesh_file = get("mesh file name")
+    if "polynomial order" in keys:
+        cfg.order = int(float(keys["polynomial order"]))
+    for k in ("polynomial order i", "polynomial order j", "polynomial order k", "polynomial order file"):
+        if k in keys:
+            raise UnsupportedOption(f"'{k}': the GPU path needs one isotropic polynomial order")
+    nodes = (get("discretization nodes", "gauss") or "gauss").lower()
+    cfg.nodes = _abi.DG_NODES_GAUSS_LOBATTO if nodes.replace("_", "-") == "gauss-lobatto" else _abi.DG_NODES_GAUSS
+    flow = (get("flow equations", "ns") or "ns").lower()
+    if flow not in ("ns", "euler"):
+        raise UnsupportedOption(f"flow equations '{flow}'")
+    cfg.flow = flow
+    cfg.mach = float(get("mach number", cfg.mach))
+    if flow == "ns":
+        if "reynolds number" not in keys:
+            raise ValueError("Input file is missing entry for keyword: reynolds number")
+        cfg.reynolds = float(keys["reynolds number"])
+    cfg.prandtl = float(get("prandtl number", 0.72))
+    rs = (get("riemann solver", "roe") or "roe").lower()
+    if rs not in _RIEMANN:
+        raise UnsupportedOption(f"riemann solver '{rs}'")
+    cfg.riemann = _RIEMANN[rs]
+    av = (get("averaging", "standard") or "standard").lower()
+    if av not in _AVERAGING:
+        raise UnsupportedOption(f"averaging '{av}'")
+    cfg.averaging = _AVERAGING[av]
+    inv = (get("inviscid discretization", "standard") or "standard").lower()
+    if inv not in ("standard", "split-form"):
+        raise UnsupportedOption(f"inviscid discretization '{inv}'")
+    cfg.inviscid = _abi.DG_INVISCID_SPLIT if inv == "split-form" else _abi.DG_INVISCID_STANDARD
+    if cfg.inviscid == _abi.DG_INVISCID_SPLIT:
+        cfg.nodes = _abi.DG_NODES_GAUSS_LOBATTO  # main.f90:306-313 forces Gauss-Lobatto for split form
+    vd = (get("viscous discretization", "br1") or "br1").lower()
+    if vd != "br1":
+        raise UnsupportedOption(f"viscous discretization '{vd}'")
+    gv = (get("gradient variables", "state") or "state").lower()
+    if gv != "state":
+        raise UnsupportedOption(f"gradient variables '{gv}'")
+    em = (get("explicit method", "rk3") or "rk3").lower()
+    if em not in ("rk3", "williamson rk3"):
+        raise UnsupportedOption(f"explicit method '{em}'")
+    for k in ("les model", "shock-capturing", "enable particles"):
+        if k in keys and keys[k].lower() not in ("none", ".false.", "false"):
+            raise UnsupportedOption(k)
+    cfg.lambda_stab = float(get("lambda stabilization", 1.0))
+    prec = (get("gpu precision", "fp64") or "fp64").lower()
+    cfg.precision = _abi.DG_PRECISION_MIXED if prec == "mixed" else _abi.DG_PRECISION_FP64
+    if "cfl" in keys:
+        cfg.cfl = float(keys["cfl"])
+        cfg.dcfl = float(keys.get("dcfl", keys["cfl"]))
+    if "dt" in keys:
+        cfg.dt = float(keys["dt"])
+    cfg.n_steps = int(float(get("number of time steps", 1)))
+    if "final time" in keys:
+        cfg.t_final = float(keys["final time"])
+    pairs = []
+    for b in blocks:
+        if b.get("kind") != "boundary":
+            continue
+        if b.get("type", "").lower() != "periodic":
+            raise UnsupportedOption(f"boundary '{b.get('name')}' of type '{b.get('type')}'")
+        pairs.append((b["name"].strip(), b.get("coupled boundary", "").lower().strip()))
+    seen = set()
+    for a, b in pairs:
+        if (b, a) in seen:
+            continue
+        seen.add((a, b))
+        cfg.periodic.append((a, b))
+    return cfg
+
+
+def read_control(path) -> Config:
+    return parse_control(Path(path).read_text())

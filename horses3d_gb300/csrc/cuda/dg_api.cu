@@ -1,0 +1,538 @@
+// C ABI of the GB300 DGSEM right-hand side (include/horses3d_gb300.h): context set-up, state
+// transfer, the RK3 driver, CUDA-graph replay of whole steps and the device reductions.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../host/spectral.hpp"
+#include "../host/status.hpp"
+#include "dg_launch.cuh"
+#include "horses3d_gb300.h"
+
+using dg::Args;
+
+namespace {
+
+int cuda_fail(cudaError_t e, const char* where) {
+    return h3d::fail(e == cudaErrorMemoryAllocation ? DG_ERR_NOMEM : DG_ERR_CUDA,
+                     std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                         \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(size_t count) {
+        n = count;
+        return cudaMalloc(reinterpret_cast<void**>(&p), sizeof(T) * (count ? count : 1));
+    }
+    void free() {
+        if (p) cudaFree(p);
+        p = nullptr;
+    }
+};
+
+// Everything one precision needs on the device.
+template <typename R>
+struct Store {
+    DevBuf<R> ja_xi, ja_eta, ja_zeta, jac, inv_jac, fn, ft1, ft2, fj;
+    DevBuf<R> QDot, Ux, Uy, Uz, QF, UN, GF, FS;
+    Args<R> args;
+    dg::StageFn<R> stage = nullptr;
+    dg::KernelTimesFn<R> times = nullptr;
+    void free() {
+        for (DevBuf<R>* b : {&ja_xi, &ja_eta, &ja_zeta, &jac, &inv_jac, &fn, &ft1, &ft2, &fj, &QDot, &Ux, &Uy, &Uz,
+                             &QF, &UN, &GF, &FS})
+            b->free();
+    }
+};
+
+}  // namespace
+
+struct dg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int K = 0, F = 0, P = 0, nodes = 0;
+    int64_t ndof = 0;
+    dg_physics phys{};
+    dg_options opt{};
+    dg::PhysConst pc{};
+    bool mixed = false;
+    double dxi[3] = {0, 0, 0};
+    DevBuf<double> Q, G, x, scal;      // scal: [0] time, [1] dt
+    DevBuf<unsigned long long> red;    // [0..1] dt reduction, [2..6] residuals
+    DevBuf<int> face_elem, face_side, face_rot, nan_flag;
+    Store<double> s64;
+    Store<float> s32;
+    double* h_scal = nullptr;          // pinned staging for scalars
+    cudaGraphExec_t graph = nullptr;
+    double graph_key[3] = {0, 0, 0};   // (mode, cfl, dcfl) the graph was captured for
+    int graph_mode = -1;
+};
+
+namespace {
+
+template <typename R>
+int upload_convert(DevBuf<R>& dst, const double* src, size_t n, cudaStream_t s) {
+    CK(dst.alloc(n));
+    if (sizeof(R) == sizeof(double)) {
+        CK(cudaMemcpyAsync(dst.p, src, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    } else {
+        std::vector<R> tmp(n);
+        for (size_t i = 0; i < n; ++i) tmp[i] = static_cast<R>(src[i]);
+        CK(cudaMemcpyAsync(dst.p, tmp.data(), sizeof(R) * n, cudaMemcpyHostToDevice, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    return DG_OK;
+}
+
+template <typename R>
+int setup_store(dg_ctx* c, Store<R>& st, const dg_mesh_desc* m) {
+    const size_t nd = static_cast<size_t>(c->ndof);
+    const size_t nfp = static_cast<size_t>(c->F) * c->P * c->P;
+    const size_t nslot = 6 * static_cast<size_t>(c->K) * c->P * c->P;
+    int rc;
+    if ((rc = upload_convert(st.ja_xi, m->ja_xi, 3 * nd, c->stream))) return rc;
+    if ((rc = upload_convert(st.ja_eta, m->ja_eta, 3 * nd, c->stream))) return rc;
+    if ((rc = upload_convert(st.ja_zeta, m->ja_zeta, 3 * nd, c->stream))) return rc;
+    if ((rc = upload_convert(st.jac, m->jacobian, nd, c->stream))) return rc;
+    if ((rc = upload_convert(st.inv_jac, m->inv_jacobian, nd, c->stream))) return rc;
+    if ((rc = upload_convert(st.fn, m->face_normal, 3 * nfp, c->stream))) return rc;
+    if ((rc = upload_convert(st.ft1, m->face_t1, 3 * nfp, c->stream))) return rc;
+    if ((rc = upload_convert(st.ft2, m->face_t2, 3 * nfp, c->stream))) return rc;
+    if ((rc = upload_convert(st.fj, m->face_jacobian, nfp, c->stream))) return rc;
+    CK(st.QDot.alloc(5 * nd));
+    CK(cudaMemsetAsync(st.QDot.p, 0, sizeof(R) * 5 * nd, c->stream));
+    const bool ns = c->phys.navier_stokes != 0;
+    CK(st.Ux.alloc(ns ? 5 * nd : 0));
+    CK(st.Uy.alloc(ns ? 5 * nd : 0));
+    CK(st.Uz.alloc(ns ? 5 * nd : 0));
+    CK(st.QF.alloc(5 * nslot));
+    CK(st.UN.alloc(ns ? 15 * nslot : 0));
+    CK(st.GF.alloc(ns ? 15 * nslot : 0));
+    CK(st.FS.alloc(5 * nslot));
+
+    Args<R>& a = st.args;
+    std::memset(&a, 0, sizeof(a));
+    a.K = c->K;
+    a.F = c->F;
+    a.ph = dg::make_phys<R>(c->pc);
+    const h3d::NodalStorage& ns_ = h3d::nodal_storage(c->nodes, c->P - 1);
+    for (int i = 0; i < c->P; ++i) {
+        for (int l = 0; l < c->P; ++l) {
+            a.ops.D[i * dg::kMaxP + l] = static_cast<R>(ns_.D[i * c->P + l]);
+            a.ops.hatD[i * dg::kMaxP + l] = static_cast<R>(ns_.hatD[i * c->P + l]);
+            a.ops.sharpD[i * dg::kMaxP + l] = c->nodes == 1 ? static_cast<R>(ns_.sharpD[i * c->P + l]) : R(0);
+        }
+        a.ops.vL[i] = static_cast<R>(ns_.vL[i]);
+        a.ops.vR[i] = static_cast<R>(ns_.vR[i]);
+        a.ops.bL[i] = static_cast<R>(ns_.bL[i]);
+        a.ops.bR[i] = static_cast<R>(ns_.bR[i]);
+    }
+    a.inviscid = c->opt.inviscid;
+    a.source = c->opt.source;
+    a.ja_xi = st.ja_xi.p; a.ja_eta = st.ja_eta.p; a.ja_zeta = st.ja_zeta.p;
+    a.jac = st.jac.p; a.inv_jac = st.inv_jac.p;
+    a.x = c->x.p;
+    a.face_elem = c->face_elem.p; a.face_side = c->face_side.p; a.face_rot = c->face_rot.p;
+    a.fn = st.fn.p; a.ft1 = st.ft1.p; a.ft2 = st.ft2.p; a.fj = st.fj.p;
+    a.Q = c->Q.p; a.G = c->G.p; a.QDot = st.QDot.p;
+    a.Ux = st.Ux.p; a.Uy = st.Uy.p; a.Uz = st.Uz.p;
+    a.QF = st.QF.p; a.UN = st.UN.p; a.GF = st.GF.p; a.FS = st.FS.p;
+    a.time = c->scal.p;
+    a.dt = c->scal.p + 1;
+    a.src_gm1 = c->pc.gm1;
+    a.src_gM2 = c->pc.gammaM2;
+    a.src_mu = c->pc.mu;
+    a.src_kappa = c->pc.kappa;
+    return DG_OK;
+}
+
+cudaError_t run_stage(dg_ctx* c, int stage, double tshift, int store_grad) {
+    if (c->mixed) return c->s32.stage(c->s32.args, stage, tshift, store_grad, c->stream);
+    return c->s64.stage(c->s64.args, stage, tshift, store_grad, c->stream);
+}
+
+// Queue one RK3 step (time and dt are read from device memory).
+cudaError_t enqueue_step(dg_ctx* c) {
+    static const double b[3] = {0.0, 1.0 / 3.0, 3.0 / 4.0};
+    for (int k = 0; k < 3; ++k) {
+        cudaError_t e = run_stage(c, k, b[k], 0);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t enqueue_max_dt(dg_ctx* c, double cfl, double dcfl) {
+    dg::DtArgs d;
+    d.ndof = c->ndof;
+    d.cfl = cfl;
+    d.dcfl = dcfl;
+    for (int r = 0; r < 3; ++r) { d.dxi[r] = c->dxi[r]; d.dxi2[r] = c->dxi[r] * c->dxi[r]; }
+    d.ns = c->pc.ns;
+    d.gamma = c->pc.gamma; d.gm1 = c->pc.gm1; d.gammaM2 = c->pc.gammaM2;
+    d.S_div_TRef = c->pc.S_div_TRef; d.TReNorm = c->pc.TReNorm;
+    d.Q = c->Q.p;
+    d.red = c->red.p;
+    const int blocks = 2 * 152 * 4;
+    if (c->mixed)
+        dg::k_max_dt<float><<<blocks, 256, 0, c->stream>>>(d, c->s32.ja_xi.p, c->s32.ja_eta.p, c->s32.ja_zeta.p, c->s32.jac.p);
+    else
+        dg::k_max_dt<double><<<blocks, 256, 0, c->stream>>>(d, c->s64.ja_xi.p, c->s64.ja_eta.p, c->s64.ja_zeta.p, c->s64.jac.p);
+    dg::k_dt_final<<<1, 1, 0, c->stream>>>(c->red.p, c->scal.p + 1);
+    return cudaGetLastError();
+}
+
+int set_scalars(dg_ctx* c, double t, double dt) {
+    c->h_scal[0] = t;
+    c->h_scal[1] = dt;
+    CK(cudaMemcpyAsync(c->scal.p, c->h_scal, 2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    return DG_OK;
+}
+
+int validate(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op) {
+    if (!m || !ph || !op) return h3d::fail(DG_ERR_INVALID, "null argument");
+    if (m->n_elements < 1 || m->n_faces < 1) return h3d::fail(DG_ERR_INVALID, "empty mesh");
+    if (!m->order || !m->x || !m->ja_xi || !m->ja_eta || !m->ja_zeta || !m->jacobian || !m->inv_jacobian ||
+        !m->face_elem || !m->face_side || !m->face_rotation || !m->face_nf || !m->face_normal || !m->face_t1 ||
+        !m->face_t2 || !m->face_jacobian)
+        return h3d::fail(DG_ERR_INVALID, "mesh description has a null array");
+    if (m->node_type != DG_NODES_GAUSS && m->node_type != DG_NODES_GAUSS_LOBATTO)
+        return h3d::fail(DG_ERR_INVALID, "unknown node type");
+    const int N = m->order[0];
+    for (int e = 0; e < m->n_elements; ++e)
+        for (int d = 0; d < 3; ++d)
+            if (m->order[3 * e + d] != N)
+                return h3d::fail(DG_ERR_UNSUPPORTED, "the GPU path needs one isotropic order on every element");
+    if (N + 1 < 2 || N + 1 > dg::kMaxP) return h3d::fail(DG_ERR_UNSUPPORTED, "polynomial order outside 1..7");
+    if (2 * static_cast<int64_t>(m->n_faces) != 6 * static_cast<int64_t>(m->n_elements))
+        return h3d::fail(DG_ERR_UNSUPPORTED, "boundary faces are not supported (periodic/interior meshes only)");
+    for (int f = 0; f < m->n_faces; ++f) {
+        if (m->face_nf[2 * f] != N || m->face_nf[2 * f + 1] != N)
+            return h3d::fail(DG_ERR_INVALID, "face order differs from the element order");
+        if (m->face_rotation[f] < 0 || m->face_rotation[f] > 7) return h3d::fail(DG_ERR_INVALID, "face rotation outside 0..7");
+        for (int s = 0; s < 2; ++s) {
+            const int e = m->face_elem[2 * f + s], side = m->face_side[2 * f + s];
+            if (e < 0 || e >= m->n_elements || side < 1 || side > 6)
+                return h3d::fail(DG_ERR_INVALID, "face connectivity out of range");
+        }
+    }
+    if (ph->mach <= 0.0) return h3d::fail(DG_ERR_INVALID, "Mach number must be positive");
+    if (ph->navier_stokes && ph->reynolds <= 0.0) return h3d::fail(DG_ERR_INVALID, "Reynolds number must be positive");
+    if (op->inviscid != DG_INVISCID_STANDARD && op->inviscid != DG_INVISCID_SPLIT)
+        return h3d::fail(DG_ERR_UNSUPPORTED, "inviscid discretization");
+    if (op->inviscid == DG_INVISCID_SPLIT && m->node_type != DG_NODES_GAUSS_LOBATTO)
+        return h3d::fail(DG_ERR_INVALID, "the split form needs Gauss-Lobatto nodes");
+    if (op->riemann != DG_RIEMANN_ROE && op->riemann != DG_RIEMANN_LXF) return h3d::fail(DG_ERR_UNSUPPORTED, "riemann solver");
+    if (op->averaging != DG_AVG_STANDARD && op->averaging != DG_AVG_PIROZZOLI)
+        return h3d::fail(DG_ERR_UNSUPPORTED, "averaging");
+    if (op->precision != DG_PRECISION_FP64 && op->precision != DG_PRECISION_MIXED)
+        return h3d::fail(DG_ERR_UNSUPPORTED, "precision");
+    if (op->source != DG_SOURCE_NONE && op->source != DG_SOURCE_MMS_CONVERGENCE)
+        return h3d::fail(DG_ERR_UNSUPPORTED, "source");
+    return DG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dg_device_count(int* count) {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (count) *count = (e == cudaSuccess) ? n : 0;
+    if (e != cudaSuccess) return h3d::fail(DG_ERR_NODEVICE, cudaGetErrorString(e));
+    return DG_OK;
+}
+
+int dg_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op, dg_ctx** out) {
+    if (!out) return h3d::fail(DG_ERR_INVALID, "null output pointer");
+    *out = nullptr;
+    int rc = validate(m, ph, op);
+    if (rc) return rc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return h3d::fail(DG_ERR_NODEVICE, "no CUDA device visible");
+    auto* c = new dg_ctx();
+    c->phys = *ph;
+    c->opt = *op;
+    c->K = m->n_elements;
+    c->F = m->n_faces;
+    c->P = m->order[0] + 1;
+    c->nodes = m->node_type;
+    c->ndof = static_cast<int64_t>(c->K) * c->P * c->P * c->P;
+    c->mixed = op->precision == DG_PRECISION_MIXED;
+    // PhysicsStorage_NS.f90:186-290,413-429 (air, Sutherland defaults)
+    dg::PhysConst& pc = c->pc;
+    pc.gamma = 1.4;
+    pc.gm1 = 1.4 - 1.0;
+    pc.gammaM2 = pc.gamma * (ph->mach * ph->mach);
+    pc.ns = ph->navier_stokes ? 1 : 0;
+    if (pc.ns) {
+        pc.mu = 1.0 / ph->reynolds;
+        pc.kappa = 1.0 / (pc.gm1 * (ph->mach * ph->mach) * ph->reynolds * ph->prandtl);
+        pc.mu_to_kappa = 1.0 / (pc.gm1 * (ph->mach * ph->mach) * ph->prandtl);
+    }
+    const double TRef = 520.0 * 5.0 / 9.0;
+    pc.S_div_TRef = (198.6 * 5.0 / 9.0) / TRef;
+    pc.TReNorm = TRef / TRef;
+    pc.lambda_stab = op->lambda_stab;
+    pc.riemann = op->riemann;
+    pc.averaging = op->averaging;
+    pc.inviscid = op->inviscid;
+    pc.source = op->source;
+    const h3d::NodalStorage& nsx = h3d::nodal_storage(c->nodes, c->P - 1);
+    for (int d = 0; d < 3; ++d) c->dxi[d] = 1.0 / std::fabs(nsx.x[1] - nsx.x[0]);
+
+    auto bail = [&](int code) {
+        dg_destroy(c);
+        return code;
+    };
+    cudaError_t e;
+    if ((e = cudaGetDevice(&c->device)) != cudaSuccess) return bail(cuda_fail(e, "cudaGetDevice"));
+    if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return bail(cuda_fail(e, "cudaStreamCreate"));
+    if ((e = cudaMallocHost(reinterpret_cast<void**>(&c->h_scal), 8 * sizeof(double))) != cudaSuccess)
+        return bail(cuda_fail(e, "cudaMallocHost"));
+    const size_t nd = static_cast<size_t>(c->ndof);
+    if ((e = c->Q.alloc(5 * nd)) != cudaSuccess) return bail(cuda_fail(e, "alloc Q"));
+    if ((e = c->G.alloc(5 * nd)) != cudaSuccess) return bail(cuda_fail(e, "alloc G"));
+    if ((e = c->scal.alloc(4)) != cudaSuccess) return bail(cuda_fail(e, "alloc scalars"));
+    if ((e = c->red.alloc(8)) != cudaSuccess) return bail(cuda_fail(e, "alloc reductions"));
+    if ((e = c->nan_flag.alloc(1)) != cudaSuccess) return bail(cuda_fail(e, "alloc flag"));
+    if ((e = c->x.alloc(3 * nd)) != cudaSuccess) return bail(cuda_fail(e, "alloc x"));
+    if ((e = cudaMemcpyAsync(c->x.p, m->x, sizeof(double) * 3 * nd, cudaMemcpyHostToDevice, c->stream)) != cudaSuccess)
+        return bail(cuda_fail(e, "copy x"));
+    if ((e = cudaMemsetAsync(c->G.p, 0, sizeof(double) * 5 * nd, c->stream)) != cudaSuccess) return bail(cuda_fail(e, "memset G"));
+    if ((e = cudaMemsetAsync(c->Q.p, 0, sizeof(double) * 5 * nd, c->stream)) != cudaSuccess) return bail(cuda_fail(e, "memset Q"));
+    // reduction slots start at "+infinity" for the dt minimum
+    {
+        unsigned long long init[8];
+        const double big = 1.0e300;
+        unsigned long long bb;
+        std::memcpy(&bb, &big, 8);
+        for (int i = 0; i < 8; ++i) init[i] = i < 2 ? bb : 0ull;
+        if ((e = cudaMemcpy(c->red.p, init, sizeof(init), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return bail(cuda_fail(e, "init reductions"));
+    }
+    if ((e = c->face_elem.alloc(2 * c->F)) != cudaSuccess) return bail(cuda_fail(e, "alloc faces"));
+    if ((e = c->face_side.alloc(2 * c->F)) != cudaSuccess) return bail(cuda_fail(e, "alloc faces"));
+    if ((e = c->face_rot.alloc(c->F)) != cudaSuccess) return bail(cuda_fail(e, "alloc faces"));
+    if ((e = cudaMemcpyAsync(c->face_elem.p, m->face_elem, sizeof(int) * 2 * c->F, cudaMemcpyHostToDevice, c->stream)) ||
+        (e = cudaMemcpyAsync(c->face_side.p, m->face_side, sizeof(int) * 2 * c->F, cudaMemcpyHostToDevice, c->stream)) ||
+        (e = cudaMemcpyAsync(c->face_rot.p, m->face_rotation, sizeof(int) * c->F, cudaMemcpyHostToDevice, c->stream)))
+        return bail(cuda_fail(e, "copy faces"));
+    if (c->mixed) {
+        if ((rc = setup_store(c, c->s32, m))) return bail(rc);
+        c->s32.stage = dg::stage_fn_fp32(c->P, c->nodes == DG_NODES_GAUSS_LOBATTO);
+        c->s32.times = dg::times_fn_fp32(c->P, c->nodes == DG_NODES_GAUSS_LOBATTO);
+    } else {
+        if ((rc = setup_store(c, c->s64, m))) return bail(rc);
+        c->s64.stage = dg::stage_fn_fp64(c->P, c->nodes == DG_NODES_GAUSS_LOBATTO);
+        c->s64.times = dg::times_fn_fp64(c->P, c->nodes == DG_NODES_GAUSS_LOBATTO);
+    }
+    if ((e = run_stage(c, dg::kPrepare, 0.0, 0)) != cudaSuccess) return bail(cuda_fail(e, "kernel attributes"));
+    if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return bail(cuda_fail(e, "set-up"));
+    *out = c;
+    return DG_OK;
+}
+
+void dg_destroy(dg_ctx* c) {
+    if (!c) return;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    c->s64.free();
+    c->s32.free();
+    c->Q.free(); c->G.free(); c->x.free(); c->scal.free(); c->red.free(); c->nan_flag.free();
+    c->face_elem.free(); c->face_side.free(); c->face_rot.free();
+    if (c->h_scal) cudaFreeHost(c->h_scal);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int64_t dg_ndof(const dg_ctx* c) { return c ? c->ndof : 0; }
+
+int dg_upload_state(dg_ctx* c, const double* q) {
+    if (!c || !q) return h3d::fail(DG_ERR_INVALID, "null argument");
+    CK(cudaMemcpyAsync(c->Q.p, q, sizeof(double) * 5 * c->ndof, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemsetAsync(c->G.p, 0, sizeof(double) * 5 * c->ndof, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return DG_OK;
+}
+
+int dg_download(dg_ctx* c, int field, double* dst) {
+    if (!c || !dst) return h3d::fail(DG_ERR_INVALID, "null argument");
+    const size_t n = 5 * static_cast<size_t>(c->ndof);
+    const void* src = nullptr;
+    bool is_real = false;
+    switch (field) {
+        case DG_FIELD_Q: src = c->Q.p; break;
+        case DG_FIELD_G: src = c->G.p; break;
+        case DG_FIELD_QDOT: src = c->mixed ? static_cast<const void*>(c->s32.QDot.p) : c->s64.QDot.p; is_real = true; break;
+        case DG_FIELD_UX: src = c->mixed ? static_cast<const void*>(c->s32.Ux.p) : c->s64.Ux.p; is_real = true; break;
+        case DG_FIELD_UY: src = c->mixed ? static_cast<const void*>(c->s32.Uy.p) : c->s64.Uy.p; is_real = true; break;
+        case DG_FIELD_UZ: src = c->mixed ? static_cast<const void*>(c->s32.Uz.p) : c->s64.Uz.p; is_real = true; break;
+        default: return h3d::fail(DG_ERR_INVALID, "unknown field");
+    }
+    if (field >= DG_FIELD_UX && !c->phys.navier_stokes) return h3d::fail(DG_ERR_INVALID, "no gradients in Euler mode");
+    if (is_real && c->mixed) {
+        std::vector<float> tmp(n);
+        CK(cudaMemcpyAsync(tmp.data(), src, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        for (size_t i = 0; i < n; ++i) dst[i] = tmp[i];
+    } else {
+        CK(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    return DG_OK;
+}
+
+int dg_rhs(dg_ctx* c, double t) {
+    if (!c) return h3d::fail(DG_ERR_INVALID, "null context");
+    int rc = set_scalars(c, t, 0.0);
+    if (rc) return rc;
+    CK(run_stage(c, -1, 0.0, 1));
+    CK(cudaStreamSynchronize(c->stream));
+    return DG_OK;
+}
+
+int dg_rk3_step(dg_ctx* c, double t, double dt) {
+    if (!c) return h3d::fail(DG_ERR_INVALID, "null context");
+    if (!(dt > 0.0) || !std::isfinite(dt)) return h3d::fail(DG_ERR_INVALID, "dt must be positive and finite");
+    int rc = set_scalars(c, t, dt);
+    if (rc) return rc;
+    CK(enqueue_step(c));
+    CK(cudaStreamSynchronize(c->stream));
+    return DG_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Captures one whole RK3 step (optionally preceded by the device CFL dt) in a CUDA graph, once per
+// (mode, cfl, dcfl).
+int prepare_graph(dg_ctx* c, int mode, double cfl, double dcfl) {
+    const bool stale = !c->graph || c->graph_mode != mode || c->graph_key[1] != cfl || c->graph_key[2] != dcfl;
+    if (!stale) return DG_OK;
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    if (mode == 1) e = enqueue_max_dt(c, cfl, dcfl);
+    if (e == cudaSuccess) e = enqueue_step(c);
+    if (e == cudaSuccess) {
+        dg::k_advance_time<<<1, 1, 0, c->stream>>>(c->scal.p, c->scal.p + 1);
+        e = cudaGetLastError();
+    }
+    cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+    if (e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return cuda_fail(e, "capture RK3 step");
+    }
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&c->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    c->graph_mode = mode;
+    c->graph_key[1] = cfl;
+    c->graph_key[2] = dcfl;
+    return DG_OK;
+}
+
+int steps_common(dg_ctx* c, int n, double t0, double dt, double cfl, double dcfl, double* t_end, double* ms) {
+    if (!c || n < 0) return h3d::fail(DG_ERR_INVALID, "bad arguments");
+    const int mode = dt > 0.0 ? 0 : 1;
+    if (mode == 1 && !(cfl > 0.0)) return h3d::fail(DG_ERR_INVALID, "CFL stepping needs cfl > 0");
+    int rc = set_scalars(c, t0, mode == 0 ? dt : 0.0);
+    if (rc) return rc;
+    if ((rc = prepare_graph(c, mode, cfl, dcfl))) return rc;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (ms) {
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        CK(cudaEventRecord(e0, c->stream));
+    }
+    for (int s = 0; s < n; ++s) CK(cudaGraphLaunch(c->graph, c->stream));
+    if (ms) {
+        CK(cudaEventRecord(e1, c->stream));
+        CK(cudaEventSynchronize(e1));
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, e0, e1));
+        *ms = t;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    if (t_end) {
+        CK(cudaMemcpyAsync(c->h_scal, c->scal.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        *t_end = c->h_scal[0];
+    }
+    return DG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dg_run_steps(dg_ctx* c, int n, double t0, double dt, double cfl, double dcfl, double* t_end) {
+    return steps_common(c, n, t0, dt, cfl, dcfl, t_end, nullptr);
+}
+
+int dg_time_steps(dg_ctx* c, int n, double t0, double dt, double cfl, double dcfl, double* ms) {
+    if (!ms) return h3d::fail(DG_ERR_INVALID, "null argument");
+    return steps_common(c, n, t0, dt, cfl, dcfl, nullptr, ms);
+}
+
+int dg_kernel_times(dg_ctx* c, int reps, double t0, double dt, double ms[5]) {
+    if (!c || !ms || reps < 1) return h3d::fail(DG_ERR_INVALID, "bad arguments");
+    int rc = set_scalars(c, t0, dt);
+    if (rc) return rc;
+    if (c->mixed) CK(c->s32.times(c->s32.args, reps, c->stream, ms));
+    else CK(c->s64.times(c->s64.args, reps, c->stream, ms));
+    return DG_OK;
+}
+
+int dg_max_dt(dg_ctx* c, double cfl, double dcfl, double* dt) {
+    if (!c || !dt) return h3d::fail(DG_ERR_INVALID, "null argument");
+    CK(enqueue_max_dt(c, cfl, dcfl));
+    CK(cudaMemcpyAsync(c->h_scal + 2, c->scal.p + 1, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    *dt = c->h_scal[2];
+    return DG_OK;
+}
+
+int dg_residuals(dg_ctx* c, double maxres[5], int* nan_found) {
+    if (!c || !maxres) return h3d::fail(DG_ERR_INVALID, "null argument");
+    CK(cudaMemsetAsync(c->red.p + 2, 0, 5 * sizeof(unsigned long long), c->stream));
+    CK(cudaMemsetAsync(c->nan_flag.p, 0, sizeof(int), c->stream));
+    const int blocks = 152 * 4;
+    if (c->mixed) dg::k_residuals<float><<<blocks, 256, 0, c->stream>>>(c->ndof, c->s32.QDot.p, c->Q.p, c->red.p + 2, c->nan_flag.p);
+    else dg::k_residuals<double><<<blocks, 256, 0, c->stream>>>(c->ndof, c->s64.QDot.p, c->Q.p, c->red.p + 2, c->nan_flag.p);
+    CK(cudaGetLastError());
+    unsigned long long bits[5];
+    int flag = 0;
+    CK(cudaMemcpyAsync(bits, c->red.p + 2, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&flag, c->nan_flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int v = 0; v < 5; ++v) std::memcpy(&maxres[v], &bits[v], sizeof(double));
+    if (nan_found) *nan_found = flag;
+    return flag ? h3d::fail(DG_ERR_NAN, "NaN or Inf in Q") : DG_OK;
+}
+
+int dg_synchronize(dg_ctx* c) {
+    if (!c) return h3d::fail(DG_ERR_INVALID, "null context");
+    CK(cudaStreamSynchronize(c->stream));
+    return DG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,295 @@
+// Point-wise physics on the device: Euler and BR1 viscous fluxes, Sutherland viscosity, Roe and
+// Lax-Friedrichs Riemann solvers, split-form two-point fluxes and the manufactured-solution source.
+// Templated on the arithmetic type R (double for the plain form, float for the mixed form).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace dg {
+
+// Derived physics constants (PhysicsStorage_NS.f90:186-429), host-filled.
+struct PhysConst {
+    double gamma, gm1, gammaM2, mu, kappa, mu_to_kappa, S_div_TRef, TReNorm;
+    double lambda_stab;
+    int ns, riemann, averaging, inviscid, source;
+};
+
+template <typename R>
+struct PhysR {
+    R gamma, gm1, gammaM2, mu, kappa, mu_to_kappa, S_div_TRef, TReNorm, lambda_stab;
+    R g_over_gm1, gp1_over_4, gm1_gammaM2;
+    int ns, riemann, averaging;
+};
+
+template <typename R>
+PhysR<R> make_phys(const PhysConst& c) {
+    PhysR<R> p;
+    p.gamma = R(c.gamma); p.gm1 = R(c.gm1); p.gammaM2 = R(c.gammaM2); p.mu = R(c.mu); p.kappa = R(c.kappa);
+    p.mu_to_kappa = R(c.mu_to_kappa); p.S_div_TRef = R(c.S_div_TRef); p.TReNorm = R(c.TReNorm);
+    p.lambda_stab = R(c.lambda_stab);
+    p.g_over_gm1 = R(c.gamma / (c.gamma - 1.0));
+    p.gp1_over_4 = R((c.gamma + 1.0) / 4.0);
+    p.gm1_gammaM2 = R(c.gm1 * c.gammaM2);
+    p.ns = c.ns; p.riemann = c.riemann; p.averaging = c.averaging;
+    return p;
+}
+
+template <typename R> __device__ __forceinline__ R dsqrt(R x);
+template <> __device__ __forceinline__ double dsqrt<double>(double x) { return sqrt(x); }
+template <> __device__ __forceinline__ float dsqrt<float>(float x) { return sqrtf(x); }
+
+// VariableConversion_NS.f90:44-57,147-186: pressure, temperature, Sutherland's law.
+template <typename R>
+__device__ __forceinline__ void mu_kappa(const PhysR<R>& p, const R* Q, R& mu, R& kappa) {
+    const R pr = p.gm1 * (Q[4] - R(0.5) * (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) / Q[0]);
+    const R T = p.gammaM2 * pr / Q[0];
+    const R t = T * p.TReNorm;
+    const R s = (R(1) + p.S_div_TRef) / (t + p.S_div_TRef) * t * dsqrt(t);
+    mu = p.mu * s;
+    kappa = mu * p.mu_to_kappa;
+}
+
+// Physics_NS.f90:51-103 EulerFlux contracted with the three metric vectors:
+// F[d][v] = sum_c f_c(Q)[v] Ja^d_c (HyperbolicDiscretizationClass.f90:132-149).
+template <typename R>
+__device__ __forceinline__ void euler_contravariant(const PhysR<R>& p, const R* Q, const R* ja0, const R* ja1,
+                                                    const R* ja2, R F[3][5]) {
+    const R u = Q[1] / Q[0], v = Q[2] / Q[0], w = Q[3] / Q[0];
+    const R pr = p.gm1 * (Q[4] - R(0.5) * (Q[1] * u + Q[2] * v + Q[3] * w));
+    const R f[5] = {Q[1], Q[1] * u + pr, Q[1] * v, Q[1] * w, (Q[4] + pr) * u};
+    const R g[5] = {Q[2], f[2], Q[2] * v + pr, Q[2] * w, (Q[4] + pr) * v};
+    const R h[5] = {Q[3], f[3], g[3], Q[3] * w + pr, (Q[4] + pr) * w};
+    const R* ja[3] = {ja0, ja1, ja2};
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int q = 0; q < 5; ++q) F[d][q] = f[q] * ja[d][0] + g[q] * ja[d][1] + h[q] * ja[d][2];
+}
+
+// Physics_NS.f90:246-303 ViscousFlux_STATE (beta = 0): F[c][v] cartesian component c.
+template <typename R>
+__device__ __forceinline__ void viscous_flux(const PhysR<R>& p, const R* Q, const R* Ux, const R* Uy, const R* Uz,
+                                             R mu, R kappa, R F[3][5]) {
+    const R invRho = R(1) / Q[0];
+    const R u = Q[1] * invRho, v = Q[2] * invRho, w = Q[3] * invRho;
+    const R ud[3] = {u * invRho, v * invRho, w * invRho};
+    R ux[3], uy[3], uz[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        ux[c] = invRho * Ux[1 + c] - ud[c] * Ux[0];
+        uy[c] = invRho * Uy[1 + c] - ud[c] * Uy[0];
+        uz[c] = invRho * Uz[1 + c] - ud[c] * Uz[0];
+    }
+    const R g = p.gm1_gammaM2;
+    const R e2 = Q[4] * invRho * invRho;
+    const R nTx = g * (invRho * Ux[4] - e2 * Ux[0] - u * ux[0] - v * ux[1] - w * ux[2]);
+    const R nTy = g * (invRho * Uy[4] - e2 * Uy[0] - u * uy[0] - v * uy[1] - w * uy[2]);
+    const R nTz = g * (invRho * Uz[4] - e2 * Uz[0] - u * uz[0] - v * uz[1] - w * uz[2]);
+    const R divV = ux[0] + uy[1] + uz[2];
+    const R tt = R(2) / R(3) * divV;
+    const R txx = mu * (R(2) * ux[0] - tt);
+    const R txy = mu * (ux[1] + uy[0]);
+    const R txz = mu * (ux[2] + uz[0]);
+    const R tyy = mu * (R(2) * uy[1] - tt);
+    const R tyz = mu * (uy[2] + uz[1]);
+    const R tzz = mu * (R(2) * uz[2] - tt);
+    F[0][0] = R(0); F[0][1] = txx; F[0][2] = txy; F[0][3] = txz;
+    F[0][4] = txx * u + txy * v + txz * w + kappa * nTx;
+    F[1][0] = R(0); F[1][1] = txy; F[1][2] = tyy; F[1][3] = tyz;
+    F[1][4] = txy * u + tyy * v + tyz * w + kappa * nTy;
+    F[2][0] = R(0); F[2][1] = txz; F[2][2] = tyz; F[2][3] = tzz;
+    F[2][4] = txz * u + tyz * v + tzz * w + kappa * nTz;
+}
+
+// RiemannSolvers_NS.f90:1541-1655 RoeRiemannSolver (with its entropy fix).
+template <typename R>
+__device__ __forceinline__ void roe_flux(const PhysR<R>& p, const R* QL, const R* QR, const R* n, R* flux) {
+    const R gm1 = p.gamma - R(1);
+    const R rho = QL[0], rhon = QR[0];
+    const R ul = QL[1] / rho, vl = QL[2] / rho, wl = QL[3] / rho;
+    const R pleft = gm1 * (QL[4] - R(0.5) / rho * (QL[1] * QL[1] + QL[2] * QL[2] + QL[3] * QL[3]));
+    const R ur = QR[1] / rhon, vr = QR[2] / rhon, wr = QR[3] / rhon;
+    const R pright = gm1 * (QR[4] - R(0.5) / rhon * (QR[1] * QR[1] + QR[2] * QR[2] + QR[3] * QR[3]));
+    const R ql = n[0] * ul + n[1] * vl + n[2] * wl;
+    const R qr = n[0] * ur + n[1] * vr + n[2] * wr;
+    const R hl = R(0.5) * (ul * ul + vl * vl + wl * wl) + p.g_over_gm1 * pleft / rho;
+    const R hr = R(0.5) * (ur * ur + vr * vr + wr * wr) + p.g_over_gm1 * pright / rhon;
+    const R rtd = dsqrt(rho * rhon);
+    const R betal = rho / (rho + rtd), betar = R(1) - betal;
+    const R utd = betal * ul + betar * ur, vtd = betal * vl + betar * vr, wtd = betal * wl + betar * wr;
+    const R htd = betal * hl + betar * hr;
+    const R atd2 = gm1 * (htd - R(0.5) * (utd * utd + vtd * vtd + wtd * wtd));
+    const R atd = dsqrt(atd2);
+    const R qtd = utd * n[0] + vtd * n[1] + wtd * n[2];
+    if (qtd >= R(0)) {
+        const R dw1 = R(0.5) * ((pright - pleft) / atd2 - (qr - ql) * rtd / atd);
+        const R sp1 = qtd - atd;
+        const R sp1m = sp1 < R(0) ? sp1 : R(0);
+        const R hd1m = (p.gp1_over_4 * atd / rtd) * dw1;
+        const R eta0 = -fabs(sp1) - hd1m;
+        const R eta1 = eta0 > R(0) ? eta0 : R(0);
+        const R udw1 = dw1 * (sp1m - R(0.5) * eta1);
+        const R rql = rho * ql;
+        flux[0] = rql + udw1;
+        flux[1] = rql * ul + pleft * n[0] + udw1 * (utd - atd * n[0]);
+        flux[2] = rql * vl + pleft * n[1] + udw1 * (vtd - atd * n[1]);
+        flux[3] = rql * wl + pleft * n[2] + udw1 * (wtd - atd * n[2]);
+        flux[4] = rql * hl + udw1 * (htd - qtd * atd);
+    } else {
+        const R dw4 = R(0.5) * ((pright - pleft) / atd2 + (qr - ql) * rtd / atd);
+        const R sp4 = qtd + atd;
+        const R sp4p = sp4 > R(0) ? sp4 : R(0);
+        const R hd4 = (p.gp1_over_4 * atd / rtd) * dw4;
+        const R eta0 = -fabs(sp4) + hd4;
+        const R eta4 = eta0 > R(0) ? eta0 : R(0);
+        const R udw4 = dw4 * (sp4p + R(0.5) * eta4);
+        const R rqr = rhon * qr;
+        flux[0] = rqr - udw4;
+        flux[1] = rqr * ur + pright * n[0] - udw4 * (utd + atd * n[0]);
+        flux[2] = rqr * vr + pright * n[1] - udw4 * (vtd + atd * n[1]);
+        flux[3] = rqr * wr + pright * n[2] - udw4 * (wtd + atd * n[2]);
+        flux[4] = rqr * hr - udw4 * (htd + qtd * atd);
+    }
+}
+
+// RiemannSolvers_NS.f90:1251-1334 LxFRiemannSolver with StandardAverage (:1784) or PirozzoliAverage (:1927).
+template <typename R>
+__device__ __forceinline__ void lxf_flux(const PhysR<R>& p, const R* QL, const R* QR, const R* n, const R* t1,
+                                         const R* t2, R* flux) {
+    const R iL = R(1) / QL[0], iR = R(1) / QR[0];
+    const R ruL = QL[1] * n[0] + QL[2] * n[1] + QL[3] * n[2];
+    const R ruR = QR[1] * n[0] + QR[2] * n[1] + QR[3] * n[2];
+    const R rvL = QL[1] * t1[0] + QL[2] * t1[1] + QL[3] * t1[2];
+    const R rvR = QR[1] * t1[0] + QR[2] * t1[1] + QR[3] * t1[2];
+    const R rwL = QL[1] * t2[0] + QL[2] * t2[1] + QL[3] * t2[2];
+    const R rwR = QR[1] * t2[0] + QR[2] * t2[1] + QR[3] * t2[2];
+    const R pL = p.gm1 * (QL[4] - R(0.5) * ((ruL * ruL + rvL * rvL + rwL * rwL) * iL));
+    const R pR = p.gm1 * (QR[4] - R(0.5) * ((ruR * ruR + rvR * rvR + rwR * rwR) * iR));
+    const R aL = dsqrt(p.gamma * pL * iL), aR = dsqrt(p.gamma * pR * iR);
+    const R lL = fabs(ruL * iL) + aL, lR = fabs(ruR * iR) + aR;
+    const R lambda = lL > lR ? lL : lR;
+    const R uL = iL * ruL, uR = iR * ruR, vL = iL * rvL, vR = iR * rvR, wL = iL * rwL, wR = iR * rwR;
+    R f[5];
+    if (p.averaging == 0) {
+        f[0] = R(0.5) * (ruL + ruR);
+        f[1] = R(0.5) * (ruL * uL + ruR * uR + pL + pR);
+        f[2] = R(0.5) * (ruL * vL + ruR * vR);
+        f[3] = R(0.5) * (ruL * wL + ruR * wR);
+        f[4] = R(0.5) * (uL * (QL[4] + pL) + uR * (QR[4] + pR));
+    } else {
+        const R rho = R(0.5) * (QL[0] + QR[0]), u = R(0.5) * (uL + uR), v = R(0.5) * (vL + vR), w = R(0.5) * (wL + wR);
+        const R pp = R(0.5) * (pL + pR);
+        const R h = R(0.5) * ((QL[4] + pL) * iL + (QR[4] + pR) * iR);
+        f[0] = rho * u; f[1] = rho * u * u + pp; f[2] = rho * u * v; f[3] = rho * u * w; f[4] = rho * u * h;
+    }
+    const R ls = p.lambda_stab * (R(0.5) * lambda);
+    f[0] = f[0] - ls * (QR[0] - QL[0]);
+    f[1] = f[1] - ls * (ruR - ruL);
+    f[2] = f[2] - ls * (rvR - rvL);
+    f[3] = f[3] - ls * (rwR - rwL);
+    f[4] = f[4] - ls * (QR[4] - QL[4]);
+    flux[0] = f[0];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) flux[1 + c] = n[c] * f[1] + t1[c] * f[2] + t2[c] * f[3];
+    flux[4] = f[4];
+}
+
+// RiemannSolvers_NS.f90:2085-2145 StandardDG_TwoPointFlux and :2369-2437 Pirozzoli_TwoPointFlux.
+template <typename R>
+__device__ __forceinline__ void two_point_flux(const PhysR<R>& p, const R* QL, const R* QR, const R* JaL, const R* JaR,
+                                               R* fs) {
+    const R iL = R(1) / QL[0], iR = R(1) / QR[0];
+    const R uL = iL * QL[1], uR = iR * QR[1], vL = iL * QL[2], vR = iR * QR[2], wL = iL * QL[3], wR = iR * QR[3];
+    const R pL = p.gm1 * (QL[4] - R(0.5) * (QL[1] * uL + QL[2] * vL + QL[3] * wL));
+    const R pR = p.gm1 * (QR[4] - R(0.5) * (QR[1] * uR + QR[2] * vR + QR[3] * wR));
+    if (p.averaging == 0) {
+        const R J0 = JaL[0] + JaR[0], J1 = JaL[1] + JaR[1], J2 = JaL[2] + JaR[2];
+        const R f[5] = {QL[1] + QR[1], QL[1] * uL + QR[1] * uR + pL + pR, QL[1] * vL + QR[1] * vR, QL[1] * wL + QR[1] * wR,
+                        uL * (QL[4] + pL) + uR * (QR[4] + pR)};
+        const R g[5] = {QL[2] + QR[2], QL[2] * uL + QR[2] * uR, QL[2] * vL + QR[2] * vR + pL + pR, QL[2] * wL + QR[2] * wR,
+                        vL * (QL[4] + pL) + vR * (QR[4] + pR)};
+        const R h[5] = {QL[3] + QR[3], QL[3] * uL + QR[3] * uR, QL[3] * vL + QR[3] * vR, QL[3] * wL + QR[3] * wR + pL + pR,
+                        wL * (QL[4] + pL) + wR * (QR[4] + pR)};
+#pragma unroll
+        for (int q = 0; q < 5; ++q) fs[q] = R(0.25) * (f[q] * J0 + g[q] * J1 + h[q] * J2);
+    } else {
+        const R rho = R(0.5) * (QL[0] + QR[0]), u = R(0.5) * (uL + uR), v = R(0.5) * (vL + vR), w = R(0.5) * (wL + wR);
+        const R pp = R(0.5) * (pL + pR);
+        const R h = R(0.5) * ((QL[4] + pL) * iL + (QR[4] + pR) * iR);
+        const R J0 = R(0.5) * (JaL[0] + JaR[0]), J1 = R(0.5) * (JaL[1] + JaR[1]), J2 = R(0.5) * (JaL[2] + JaR[2]);
+        const R ru = rho * u, rv = rho * v, rw = rho * w;
+        fs[0] = ru * J0 + rv * J1 + rw * J2;
+        fs[1] = (ru * u + pp) * J0 + (rv * u) * J1 + (rw * u) * J2;
+        fs[2] = (ru * v) * J0 + (rv * v + pp) * J1 + (rw * v) * J2;
+        fs[3] = (ru * w) * J0 + (rv * w) * J1 + (rw * w + pp) * J2;
+        fs[4] = (ru * h) * J0 + (rv * h) * J1 + (rw * h) * J2;
+    }
+}
+
+// Convergence/SETUP/ProblemFile.f90:31-133 state_source_in_point: the source term S(x,t).
+__device__ __forceinline__ void mms_source(double x, double y, double z, double t, double gm1, double gMa2, double mu,
+                                           double kap, double* S) {
+    const double c_u = 1.0, c_v = 2.0, c_w = -c_u - c_v;
+    const double Ssu = 0.381923076923077;
+    const double PI = 3.141592653589793238462643;
+    const double arg = PI * (x + y + z - 2.0 * t);
+    double sa, ca;
+    sincos(arg, &sa, &ca);
+    const double rho = 2.0 + 0.1 * sa;
+    const double u = c_u * rho - 1.0, v = c_v * rho - 4.0, w = c_w * rho + 5.0, e = rho;
+    const double vtot = u * u + v * v + w * w;
+    const double p = gm1 * (rho * e - 0.5 * rho * vtot);
+    const double Temp = gMa2 * gm1 * (e - 0.5 * vtot);
+    const double suther = (1.0 + Ssu) / (Temp + Ssu) * Temp * sqrt(Temp);
+    const double dsdT = 1.5 * suther / Temp - suther / (Ssu + Temp);
+    const double rho_t = 0.1 * (-2.0 * PI) * ca;
+    const double u_t = c_u * rho_t, v_t = c_v * rho_t, w_t = c_w * rho_t, e_t = rho_t;
+    const double rx = 0.1 * PI * ca;  // every component of grad(rho)
+    const double ux = c_u * rx, vx = c_v * rx, wx = c_w * rx, ex = rx;
+    const double px = gm1 * rx * (e - 0.5 * vtot) + gm1 * rho * (ex - u * ux - v * vx - w * wx);
+    const double Tx = gMa2 * gm1 * (ex - u * ux - v * vx - w * wx);
+    const double div_v = ux + vx + wx;
+    // grad_u(i,j) = d(vel_j)/dx_i is the same for every i: rows (ux, vx, wx)
+    const double gj[3] = {ux, vx, wx};
+    double tau[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) tau[i][j] = mu * suther * (gj[j] + gj[i] - 2.0 * div_v * (i == j ? 1.0 : 0.0) / 3.0);
+    const double rxx = -0.1 * (PI * PI) * sa;
+    const double uxx = c_u * rxx, vxx = c_v * rxx, wxx = c_w * rxx, exx = rxx;
+    double Txx_tr = 0.0;
+    for (int i = 0; i < 3; ++i)
+        Txx_tr += gMa2 * gm1 * (exx - ux * ux - vx * vx - wx * wx - u * uxx - v * vxx - w * wxx);
+    double dtau[3];
+    for (int j = 0; j < 3; ++j) {
+        const double tr[3] = {3.0 * uxx, 3.0 * vxx, 3.0 * wxx};
+        dtau[j] = uxx + vxx + wxx + tr[j] - (2.0 / 3.0) * (uxx + vxx + wxx);
+        dtau[j] = mu * suther * dtau[j];
+        const double mt = tau[j][0] * Tx + tau[j][1] * Tx + tau[j][2] * Tx;
+        dtau[j] = dtau[j] + (dsdT / suther) * mt;
+    }
+    double sgt = 0.0;
+    for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) sgt += gj[j] * tau[i][j];
+    const double vw = sgt + u * dtau[0] + v * dtau[1] + w * dtau[2];
+    const double heat = kap * dsdT * (3.0 * Tx * Tx) + kap * suther * Txx_tr;
+    S[0] = rho_t + u * rx + v * rx + w * rx + rho * div_v;
+    S[1] = u * S[0] + rho * u_t + rho * u * ux + rho * v * ux + rho * w * ux + px - dtau[0];
+    S[2] = v * S[0] + rho * v_t + rho * u * vx + rho * v * vx + rho * w * vx + px - dtau[1];
+    S[3] = w * S[0] + rho * w_t + rho * u * wx + rho * v * wx + rho * w * wx + px - dtau[2];
+    S[4] = e * S[0] + rho * e_t + rho * (u * ex + v * ex + w * ex) + p * div_v + u * px + v * px + w * px - vw - heat;
+}
+
+// MeshTypes.f90:70-107 leftIndexes2Right.
+__device__ __forceinline__ void left2right(int i, int j, int Nx, int Ny, int rot, int& ii, int& jj) {
+    switch (rot) {
+        case 0: ii = i; jj = j; break;
+        case 1: ii = Ny - j; jj = i; break;
+        case 2: ii = Nx - i; jj = Ny - j; break;
+        case 3: ii = j; jj = Nx - i; break;
+        case 4: ii = j; jj = i; break;
+        case 5: ii = Nx - i; jj = j; break;
+        case 6: ii = Ny - j; jj = Nx - i; break;
+        default: ii = i; jj = Ny - j; break;
+    }
+}
+
+}  // namespace dg

@@ -119,14 +119,25 @@ int64_t dg_ndof(const dg_ctx* ctx);
 /* ComputeTimeDerivative: QDot = RHS(Q, t) (SpatialDiscretization.f90:227-685). */
 int dg_rhs(dg_ctx* ctx, double t);
 
-/* TakeRK3Step: three RHS evaluations + low-storage updates (ExplicitMethods.f90:748-779).
- * dt > 0: fixed step. dt <= 0: the step is the CFL step of MaxTimeStep with cfl=-dt and the dcfl
- * given to dg_set_cfl. dt_used (may be NULL) receives the step taken. */
-int dg_rk3_step(dg_ctx* ctx, double t, double dt, double* dt_used);
+/* TakeRK3Step: three RHS evaluations at t + b_k dt and the low-storage updates
+ * G = a_k G + QDot, Q = Q + c_k dt G (ExplicitMethods.f90:748-779). dt must be positive; for
+ * CFL stepping call dg_max_dt first, as the reference's time loop does (TimeIntegrator.f90:748-754). */
+int dg_rk3_step(dg_ctx* ctx, double t, double dt);
 
-/* Fixed-step loop of n RK3 steps at dt on the device (captured in a CUDA graph after the first
- * step). No host synchronisation between steps. */
-int dg_run_steps(dg_ctx* ctx, int n, double t0, double dt);
+/* n RK3 steps from t0 entirely on the device, captured once in a CUDA graph and replayed: no host
+ * synchronisation between steps. dt > 0: fixed step. dt <= 0: every step takes the MaxTimeStep
+ * value for (cfl, dcfl), computed and applied on the device. t_end (may be NULL) receives the final
+ * time (this synchronises). */
+int dg_run_steps(dg_ctx* ctx, int n, double t0, double dt, double cfl, double dcfl, double* t_end);
+
+/* dg_run_steps timed with CUDA events recorded on the context's stream around the graph
+ * launches; *ms receives the elapsed device time. Measurement helper, no reference counterpart. */
+int dg_time_steps(dg_ctx* ctx, int n, double t0, double dt, double cfl, double dcfl, double* ms);
+
+/* Average device time (ms) of each of the five stage kernels launched alone reps times on the
+ * context's stream: prolong+gradient, BR1 face jump, lift+volume, face flux, surface+RK update.
+ * Advances Q by reps RK stage-1 updates of size dt. Measurement helper, no reference counterpart. */
+int dg_kernel_times(dg_ctx* ctx, int reps, double t0, double dt, double ms[5]);
 
 /* MaxTimeStep (DGSEMClass.f90:870-1038) on the device. */
 int dg_max_dt(dg_ctx* ctx, double cfl, double dcfl, double* dt);

@@ -1,0 +1,80 @@
+"""Small versions of the benchmark configurations, shared by the parity tests."""
+from __future__ import annotations
+
+import numpy as np
+
+from horses3d_gb300 import _abi, problems
+from horses3d_gb300.control import Config
+from horses3d_gb300.mesh import HexMesh
+
+TWO_PI = 2.0 * np.pi
+
+
+def tgv_case(n=4, order=3, nodes=_abi.DG_NODES_GAUSS_LOBATTO, riemann=_abi.DG_RIEMANN_ROE,
+             inviscid=_abi.DG_INVISCID_STANDARD, averaging=_abi.DG_AVG_STANDARD, mach=0.1, reynolds=1600.0,
+             warp=0.0, perturbation=0.0, seed=0, precision=_abi.DG_PRECISION_FP64, flow="ns"):
+    mesh = HexMesh.box(n, [0, 0, 0], [TWO_PI] * 3, order, node_type=nodes, warp=warp,
+                       patch_order=order if warp else 0)
+    cfg = Config(order=order, nodes=nodes, flow=flow, mach=mach, reynolds=reynolds, riemann=riemann,
+                 averaging=averaging, inviscid=inviscid, precision=precision)
+    q0 = problems.taylor_green(mesh.x, mach, perturbation=perturbation, seed=seed)
+    return mesh, cfg, q0
+
+
+def vortex_case(n=4, order=3, nodes=_abi.DG_NODES_GAUSS, mach=0.5, precision=_abi.DG_PRECISION_FP64):
+    L = 10.0
+    mesh = HexMesh.box(n, [-L / 2] * 3, [L / 2] * 3, order, node_type=nodes)
+    cfg = Config(order=order, nodes=nodes, flow="euler", mach=mach, riemann=_abi.DG_RIEMANN_LXF, precision=precision)
+    q0 = problems.isentropic_vortex(mesh.x, mach, strength=5.0, period=L)
+    return mesh, cfg, q0
+
+
+def convergence_case(order=7, precision=_abi.DG_PRECISION_FP64):
+    """The reference's NavierStokes/Convergence case: periodic [-1,1]x[0,2]x[-1,1] with 4^3 elements
+    (UnitCube4x4.mesh), Gauss nodes, Roe, BR1, M=0.3, Re=10, manufactured source."""
+    mesh = HexMesh.box(4, [-1, 0, -1], [1, 2, 1], order, node_type=_abi.DG_NODES_GAUSS)
+    cfg = Config(order=order, nodes=_abi.DG_NODES_GAUSS, mach=0.3, reynolds=10.0, riemann=_abi.DG_RIEMANN_ROE,
+                 precision=precision, source=_abi.DG_SOURCE_MMS_CONVERGENCE, cfl=0.5, dcfl=1.0e5, t_final=1.0,
+                 n_steps=1000000)
+    q0, _ = problems.mms_convergence_state(mesh.x, 0.0)
+    return mesh, cfg, q0
+
+
+# Goldens of Solver/test/NavierStokes/Convergence/SETUP/ProblemFile.f90:617-635 (tol 1e-11 on x+1).
+CONVERGENCE_RESIDUALS = np.array([6.2801762330611588E-01, 1.8889640334957627E+00, 2.5256897695536247E+00,
+                                  4.4142472296503827E+00, 2.5163928650671146E+00])
+CONVERGENCE_Q_ERRORS = np.array([1.0983475326313417E-06, 1.4788256133056976E-06, 4.5499827613507929E-07,
+                                 9.0819927730318800E-07, 2.5402026557722347E-06])
+CONVERGENCE_QDOT_ERRORS = np.array([1.1342700947907287E-05, 1.1638989807665964E-05, 3.5549224957856481E-06,
+                                    1.0769093706709006E-05, 2.0658954210939997E-05])
+# The error norm of that test uses these tabulated Gauss-Lobatto weights (ProblemFile.f90:643-650).
+WLGL7 = np.array([0.035714285714286, 0.210704227143506, 0.341122692483504, 0.412458794658704,
+                  0.412458794658704, 0.341122692483504, 0.210704227143506, 0.035714285714286])
+
+
+def convergence_errors(mesh, q, qdot, t):
+    qe, qde = problems.mms_convergence_state(mesh.x, t)
+    w3 = (WLGL7[None, None, :] * WLGL7[None, :, None] * WLGL7[:, None, None]).reshape(-1)
+    J = mesh.jacobian.reshape(mesh.n_elements, -1)
+    dq = (q - qe).reshape(mesh.n_elements, -1, 5)
+    dqd = (qdot - qde).reshape(mesh.n_elements, -1, 5)
+    err = np.sqrt(np.einsum("ep,p,epv->v", J, w3, dq ** 2))
+    qerr = np.sqrt(np.einsum("ep,p,epv->v", J, w3, dqd ** 2))
+    return err, qerr
+
+
+def ftassert_close(expected, actual, tol=1e-11):
+    """FTAssertEqual on (value + 1) as the reference test does (ftobject/Comparisons.f90:238-255)."""
+    x, y = np.asarray(expected) + 1.0, np.asarray(actual) + 1.0
+    lim = np.where(x <= tol, tol, tol * np.maximum(np.abs(x), np.abs(y)))
+    return np.all(np.abs(x - y) <= lim)
+
+
+def quadrature_weights(mesh):
+    """w_i w_j w_k J at every node (for rel-L2 norms)."""
+    from horses3d_gb300.mesh import nodal_storage
+
+    n = mesh.uniform_order()
+    _, w, _ = nodal_storage(mesh.node_type, n)
+    w3 = (w[None, None, :] * w[None, :, None] * w[:, None, None]).reshape(-1)
+    return (mesh.jacobian.reshape(mesh.n_elements, -1) * w3[None, :]).reshape(-1)

@@ -1,0 +1,137 @@
+"""The C ABI library: it loads, exports every entry point the header declares and validates its
+arguments before touching a device (no GPU needed)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from horses3d_gb300 import _abi
+from horses3d_gb300.control import Config, UnsupportedOption, parse_control
+from horses3d_gb300.mesh import HexMesh
+
+HEADER = Path(__file__).resolve().parents[1] / "include" / "horses3d_gb300.h"
+
+
+def declared_functions():
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    return sorted(set(re.findall(r"\b(?:int|void|double|int64_t|const char\*)\s+\**(\w+)\s*\(", text)))
+
+
+def test_header_and_python_signatures_agree():
+    names = declared_functions()
+    assert "dg_create" in names and "dg_rk3_step" in names and "h3d_mesh_box" in names
+    assert sorted(n for n, _, _ in _abi.SIGNATURES) == names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = C.CDLL(str(_abi.library_path()))
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+    L = _abi.lib()
+    assert b"sm_103a" in L.dg_version()
+    assert L.dg_strerror(_abi.DG_ERR_NAN) == b"NaN or Inf in the solution"
+
+
+def _ctx_create(mesh, cfg):
+    h = C.c_void_p()
+    rc = _abi.lib().dg_create(C.byref(mesh.desc), C.byref(cfg.physics()), C.byref(cfg.options()), C.byref(h))
+    if rc == _abi.DG_OK:
+        _abi.lib().dg_destroy(h)
+    return rc
+
+
+def test_create_validates_before_touching_the_device():
+    mesh = HexMesh.box(2, [0, 0, 0], [1, 1, 1], 3, node_type=_abi.DG_NODES_GAUSS)
+    # split form needs Gauss-Lobatto nodes
+    assert _ctx_create(mesh, Config(inviscid=_abi.DG_INVISCID_SPLIT)) == _abi.DG_ERR_INVALID
+    assert _ctx_create(mesh, Config(mach=-1.0)) == _abi.DG_ERR_INVALID
+    assert _ctx_create(mesh, Config(riemann=7)) == _abi.DG_ERR_UNSUPPORTED
+    aniso = HexMesh.box(2, [0, 0, 0], [1, 1, 1], np.tile([2, 3, 4], 8), node_type=_abi.DG_NODES_GAUSS)
+    assert _ctx_create(aniso, Config()) == _abi.DG_ERR_UNSUPPORTED
+    assert b"isotropic" in _abi.lib().dg_last_error()
+    big = HexMesh.box(1, [0, 0, 0], [1, 1, 1], 8, node_type=_abi.DG_NODES_GAUSS)
+    assert _ctx_create(big, Config()) == _abi.DG_ERR_UNSUPPORTED
+
+
+def test_null_arguments_are_rejected():
+    L = _abi.lib()
+    h = C.c_void_p()
+    assert L.dg_create(None, None, None, C.byref(h)) == _abi.DG_ERR_INVALID
+    assert L.dg_rhs(None, 0.0) == _abi.DG_ERR_INVALID
+    assert L.dg_rk3_step(None, 0.0, 1.0) == _abi.DG_ERR_INVALID
+    assert L.dg_upload_state(None, None) == _abi.DG_ERR_INVALID
+
+
+def test_mesh_builder_rejects_bad_input(tmp_path):
+    L = _abi.lib()
+    h = C.c_void_p()
+    lo = np.zeros(3)
+    hi = np.ones(3)
+    assert L.h3d_mesh_box(0, 1, 1, _abi.f64ptr(lo), _abi.f64ptr(hi), 0.0, 0, 0, 3, None, C.byref(h)) == _abi.DG_ERR_INVALID
+    assert L.h3d_mesh_box(2, 2, 2, _abi.f64ptr(lo), _abi.f64ptr(hi), 0.1, 0, 0, 3, None, C.byref(h)) == _abi.DG_ERR_INVALID
+    assert L.h3d_mesh_read_specmesh(str(tmp_path / "missing.mesh").encode(), 0, 3, None, b"", C.byref(h)) == _abi.DG_ERR_IO
+    bad = tmp_path / "bad.mesh"
+    bad.write_text("8 1 1\n")
+    assert L.h3d_mesh_read_specmesh(str(bad).encode(), 0, 3, None, b"", C.byref(h)) == _abi.DG_ERR_IO
+
+
+def test_non_periodic_mesh_is_rejected(tmp_path):
+    L = _abi.lib()
+    h = C.c_void_p()
+    with pytest.raises(_abi.DgError):
+        HexMesh.from_specmesh(_write_single_hex(tmp_path), 2, periodic="")
+
+
+def _write_single_hex(tmp_path):
+    p = tmp_path / "one.mesh"
+    nodes = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+    lines = ["8 1 1"] + [f"{a} {b} {c}" for a, b, c in nodes] + ["1 2 3 4 5 6 7 8", "0 0 0 0 0 0",
+                                                                  "front back bottom right top left"]
+    p.write_text("\n".join(lines) + "\n")
+    return p
+
+
+def test_single_periodic_hex_connects_to_itself(tmp_path):
+    m = HexMesh.from_specmesh(_write_single_hex(tmp_path), 2, periodic="front:back,bottom:top,left:right")
+    assert m.n_elements == 1 and m.n_faces == 3
+
+
+CONTROL = """
+!-- a reduced copy of the keys of the reference's Convergence.control
+                          Mesh file name = ../../TestMeshes/UnitCube4x4.mesh
+                          Flow equations = "NS"
+                             Mach number = 0.3
+                         Reynolds number = 10.0
+                        Polynomial order = 7
+                    Discretization nodes = Gauss
+                          Riemann solver = Roe
+                  Viscous discretization = BR1
+                                     CFL = 0.5
+                                    dCFL = 100000.0
+                    Number of time steps = 1000000.0
+                              Final time = 1.0
+#define boundary Front
+   type = periodic
+   coupled boundary = Back
+#end
+#define boundary Back
+   type = periodic
+   coupled boundary = Front
+#end
+"""
+
+
+def test_control_file_keys():
+    cfg = parse_control(CONTROL)
+    assert cfg.order == 7 and cfg.nodes == _abi.DG_NODES_GAUSS and cfg.riemann == _abi.DG_RIEMANN_ROE
+    assert cfg.mach == 0.3 and cfg.reynolds == 10.0 and cfg.prandtl == 0.72
+    assert cfg.cfl == 0.5 and cfg.dcfl == 1.0e5 and cfg.t_final == 1.0
+    assert cfg.periodic == [("front", "back")]
+    split = parse_control("inviscid discretization = split-form\naveraging = Pirozzoli\nreynolds number = 1\n")
+    assert split.nodes == _abi.DG_NODES_GAUSS_LOBATTO and split.averaging == _abi.DG_AVG_PIROZZOLI
+    with pytest.raises(UnsupportedOption):
+        parse_control("viscous discretization = BR2\nreynolds number = 1\n")
+    with pytest.raises(UnsupportedOption):
+        parse_control("riemann solver = rusanov\nreynolds number = 1\n")

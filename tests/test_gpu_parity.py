@@ -1,0 +1,181 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU FP64 oracle on the same inputs.
+
+Tolerances: the plain FP64 form must hold the solution within 1e-12 relative L2 per conserved
+variable after the steps (STATE_TOL); a single right-hand side is held to 1e-10 (RHS_TOL) because
+QDot is a small difference of O(p0 = 1/(gamma M^2)) flux terms (the Taylor-Green density RHS is
+nearly zero), so one rounding difference of an FMA is amplified by that cancellation. The mixed form
+must hold the solution within 1e-6 relative L2 (FP32 fluxes, FP64 state and RK accumulation).
+"""
+import numpy as np
+import pytest
+
+import cases
+import oracle
+from horses3d_gb300 import _abi
+from horses3d_gb300.problems import rel_l2
+from horses3d_gb300.solver import NavierStokesDG
+
+pytestmark = pytest.mark.gpu
+
+STATE_TOL = 1e-12
+RHS_TOL = 1e-10
+MIXED_TOL = 1e-6
+
+
+def _pair(mesh, cfg, q0):
+    o = oracle.Oracle(mesh, cfg.physics(), cfg.options())
+    o.set_state(q0)
+    g = NavierStokesDG(mesh, cfg)
+    g.set_state(q0)
+    return o, g
+
+
+def _check_rhs(mesh, cfg, q0, tol=RHS_TOL, t=0.0):
+    o, g = _pair(mesh, cfg, q0)
+    ref = o.rhs(t)
+    g.compute_time_derivative(t)
+    got = g.QDot
+    err = rel_l2(got, ref)
+    assert np.all(err <= tol), err
+    if cfg.flow == "ns":
+        for f in (_abi.DG_FIELD_UX, _abi.DG_FIELD_UY, _abi.DG_FIELD_UZ):
+            gr = o.get(f)
+            e2 = np.max(np.abs(g.get(f) - gr)) / max(np.max(np.abs(gr)), 1e-300)
+            assert e2 <= tol, (f, e2)
+    return o, g
+
+
+def _check_steps(mesh, cfg, q0, steps, dt, tol=STATE_TOL):
+    o, g = _pair(mesh, cfg, q0)
+    t = 0.0
+    for _ in range(steps):
+        o.rk3_step(t, dt)
+        g.take_rk3_step(t, dt)
+        t += dt
+    w = cases.quadrature_weights(mesh)
+    err = rel_l2(g.Q, o.get(0), w)
+    assert np.all(err <= tol), err
+    return err
+
+
+@pytest.mark.parametrize("order,nodes", [(3, _abi.DG_NODES_GAUSS_LOBATTO), (2, _abi.DG_NODES_GAUSS),
+                                         (5, _abi.DG_NODES_GAUSS), (4, _abi.DG_NODES_GAUSS_LOBATTO)])
+def test_rhs_tgv_roe(order, nodes):
+    mesh, cfg, q0 = cases.tgv_case(n=3, order=order, nodes=nodes)
+    _check_rhs(mesh, cfg, q0)
+
+
+def test_rhs_curvilinear_lxf_gauss_n5():
+    mesh, cfg, q0 = cases.tgv_case(n=3, order=5, nodes=_abi.DG_NODES_GAUSS, riemann=_abi.DG_RIEMANN_LXF, warp=0.1)
+    _check_rhs(mesh, cfg, q0)
+
+
+@pytest.mark.parametrize("averaging", [_abi.DG_AVG_PIROZZOLI, _abi.DG_AVG_STANDARD])
+def test_rhs_split_form(averaging):
+    mesh, cfg, q0 = cases.tgv_case(n=3, order=4, nodes=_abi.DG_NODES_GAUSS_LOBATTO, riemann=_abi.DG_RIEMANN_LXF,
+                                   inviscid=_abi.DG_INVISCID_SPLIT, averaging=averaging, perturbation=0.01, seed=7)
+    _check_rhs(mesh, cfg, q0)
+
+
+def test_rhs_euler_vortex():
+    mesh, cfg, q0 = cases.vortex_case(n=3, order=3)
+    _check_rhs(mesh, cfg, q0)
+
+
+def test_rk3_steps_tgv_gl_n3():
+    mesh, cfg, q0 = cases.tgv_case(n=4, order=3, nodes=_abi.DG_NODES_GAUSS_LOBATTO)
+    _check_steps(mesh, cfg, q0, steps=20, dt=2e-3)
+
+
+def test_rk3_steps_curvilinear_gauss_n5():
+    mesh, cfg, q0 = cases.tgv_case(n=3, order=5, nodes=_abi.DG_NODES_GAUSS, riemann=_abi.DG_RIEMANN_LXF, warp=0.1)
+    _check_steps(mesh, cfg, q0, steps=10, dt=1e-3)
+
+
+def test_rk3_steps_split_form():
+    mesh, cfg, q0 = cases.tgv_case(n=3, order=4, nodes=_abi.DG_NODES_GAUSS_LOBATTO, riemann=_abi.DG_RIEMANN_LXF,
+                                   inviscid=_abi.DG_INVISCID_SPLIT, averaging=_abi.DG_AVG_PIROZZOLI,
+                                   perturbation=0.01, seed=3)
+    _check_steps(mesh, cfg, q0, steps=10, dt=1e-3)
+
+
+def test_max_dt_matches_oracle():
+    mesh, cfg, q0 = cases.tgv_case(n=3, order=4, nodes=_abi.DG_NODES_GAUSS_LOBATTO, warp=0.0)
+    o, g = _pair(mesh, cfg, q0)
+    for cfl, dcfl in ((0.4, 0.4), (0.5, 1e5)):
+        assert abs(g.max_time_step(cfl, dcfl) - o.max_dt(cfl, dcfl)) <= 1e-15 * o.max_dt(cfl, dcfl)
+
+
+def test_graph_replay_equals_single_steps():
+    mesh, cfg, q0 = cases.tgv_case(n=3, order=3, nodes=_abi.DG_NODES_GAUSS_LOBATTO)
+    g1 = NavierStokesDG(mesh, cfg)
+    g1.set_state(q0)
+    t = 0.0
+    for _ in range(5):
+        g1.take_rk3_step(t, 1e-3)
+        t += 1e-3
+    g2 = NavierStokesDG(mesh, cfg)
+    g2.set_state(q0)
+    t_end = g2.run_steps(5, 0.0, dt=1e-3)
+    assert abs(t_end - 5e-3) < 1e-15
+    assert np.array_equal(g1.Q, g2.Q)
+    # CFL mode on the device: same as host-driven MaxTimeStep + RKStep
+    g3 = NavierStokesDG(mesh, cfg)
+    g3.set_state(q0)
+    g4 = NavierStokesDG(mesh, cfg)
+    g4.set_state(q0)
+    t = 0.0
+    for _ in range(4):
+        dt = g3.max_time_step(0.4, 0.4)
+        g3.take_rk3_step(t, dt)
+        t += dt
+    t4 = g4.run_steps(4, 0.0, dt=0.0, cfl=0.4, dcfl=0.4)
+    assert abs(t4 - t) <= 1e-15 * t
+    assert np.array_equal(g3.Q, g4.Q)
+
+
+def test_convergence_case_on_gpu_reaches_the_reference_goldens():
+    """The whole Convergence regression (215 CFL steps, manufactured source) on the GPU."""
+    mesh, cfg, q0 = cases.convergence_case()
+    g = NavierStokesDG(mesh, cfg)
+    g.set_state(q0)
+    rep = g.integrate_in_time(t0=0.0, compute_after_steps=True)
+    assert rep.iterations == 215
+    err, qerr = cases.convergence_errors(mesh, g.Q, g.QDot, rep.time)
+    assert cases.ftassert_close(cases.CONVERGENCE_RESIDUALS, rep.residuals), rep.residuals - cases.CONVERGENCE_RESIDUALS
+    assert cases.ftassert_close(cases.CONVERGENCE_Q_ERRORS, err), err - cases.CONVERGENCE_Q_ERRORS
+    assert cases.ftassert_close(cases.CONVERGENCE_QDOT_ERRORS, qerr), qerr - cases.CONVERGENCE_QDOT_ERRORS
+
+
+@pytest.mark.parametrize("kind", ["tgv_gl3", "warped_gauss5", "split4"])
+def test_mixed_precision_within_1e6(kind):
+    if kind == "tgv_gl3":
+        mesh, cfg, q0 = cases.tgv_case(n=4, order=3, nodes=_abi.DG_NODES_GAUSS_LOBATTO,
+                                       precision=_abi.DG_PRECISION_MIXED)
+        steps, dt = 20, 2e-3
+    elif kind == "warped_gauss5":
+        mesh, cfg, q0 = cases.tgv_case(n=3, order=5, nodes=_abi.DG_NODES_GAUSS, riemann=_abi.DG_RIEMANN_LXF, warp=0.1,
+                                       precision=_abi.DG_PRECISION_MIXED)
+        steps, dt = 10, 1e-3
+    else:
+        mesh, cfg, q0 = cases.tgv_case(n=3, order=4, nodes=_abi.DG_NODES_GAUSS_LOBATTO, riemann=_abi.DG_RIEMANN_LXF,
+                                       inviscid=_abi.DG_INVISCID_SPLIT, averaging=_abi.DG_AVG_PIROZZOLI,
+                                       perturbation=0.01, seed=3, precision=_abi.DG_PRECISION_MIXED)
+        steps, dt = 10, 1e-3
+    _check_steps(mesh, cfg, q0, steps, dt, tol=MIXED_TOL)
+
+
+def test_nan_is_reported_not_trapped():
+    """A NaN in the host-staged state is detected by the residual reduction (checkForNan)."""
+    mesh, cfg, q0 = cases.tgv_case(n=2, order=3, nodes=_abi.DG_NODES_GAUSS_LOBATTO)
+    g = NavierStokesDG(mesh, cfg)
+    q = q0.copy()
+    q[17] = np.nan
+    g.set_state(q)
+    g.compute_time_derivative(0.0)
+    _, nan = g.compute_max_residuals()
+    assert nan
+    g.set_state(q0)
+    g.compute_time_derivative(0.0)
+    res, nan = g.compute_max_residuals()
+    assert not nan and np.all(np.isfinite(res))

@@ -1,0 +1,84 @@
+"""The CPU oracle against the reference's own golden values (no GPU)."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import cases
+import oracle
+from horses3d_gb300 import _abi
+from horses3d_gb300.mesh import HexMesh, nodal_storage
+
+REF_MESH = Path("/root/reference/Solver/test/TestMeshes/UnitCube4x4.mesh")
+
+
+def _run_convergence(mesh, cfg):
+    o = oracle.Oracle(mesh, cfg.physics(), cfg.options())
+    q0, _ = cases.problems.mms_convergence_state(mesh.x, 0.0)
+    o.set_state(q0)
+    t, it = 0.0, 0
+    eps = np.finfo(float).eps
+    while True:  # IntegrateInTime with CorrectDt (TimeIntegrator.f90:737-890,1100-1133)
+        dt = o.max_dt(cfg.cfl, cfg.dcfl)
+        if t + dt > cfg.t_final:
+            dt = cfg.t_final - t
+        o.rk3_step(t, dt)
+        t += dt
+        it += 1
+        if t >= cfg.t_final or abs(t - cfg.t_final) <= 100 * eps:
+            break
+    qdot = o.rhs(t)  # "compute time derivative after timestep = .true."
+    res, nan = o.residuals()
+    err, qerr = cases.convergence_errors(mesh, o.get(0), qdot, t)
+    return it, res, err, qerr, nan
+
+
+def test_convergence_goldens_generated_mesh():
+    mesh, cfg, _ = cases.convergence_case()
+    it, res, err, qerr, nan = _run_convergence(mesh, cfg)
+    assert not nan
+    assert it == 215
+    assert cases.ftassert_close(cases.CONVERGENCE_RESIDUALS, res), res - cases.CONVERGENCE_RESIDUALS
+    assert cases.ftassert_close(cases.CONVERGENCE_Q_ERRORS, err), err - cases.CONVERGENCE_Q_ERRORS
+    assert cases.ftassert_close(cases.CONVERGENCE_QDOT_ERRORS, qerr), qerr - cases.CONVERGENCE_QDOT_ERRORS
+
+
+@pytest.mark.skipif(not REF_MESH.exists(), reason="reference mesh file not mounted")
+def test_convergence_goldens_reference_mesh_file():
+    _, cfg, _ = cases.convergence_case()
+    mesh = HexMesh.from_specmesh(REF_MESH, 7, node_type=_abi.DG_NODES_GAUSS,
+                                 periodic="front:back,bottom:top,left:right")
+    it, res, err, qerr, nan = _run_convergence(mesh, cfg)
+    assert it == 215
+    assert cases.ftassert_close(cases.CONVERGENCE_RESIDUALS, res)
+    assert cases.ftassert_close(cases.CONVERGENCE_Q_ERRORS, err)
+    assert cases.ftassert_close(cases.CONVERGENCE_QDOT_ERRORS, qerr)
+
+
+def test_nodal_storage_quadrature_and_derivative():
+    # Solver/test/Components/NodalStorage/src/NodalStorageTests.f90:10-63 (N=8 Gauss, tol 1e-12)
+    x, w, D = nodal_storage(_abi.DG_NODES_GAUSS, 8)
+    assert abs(np.sum(x ** 2 * w) - 2.0 / 3.0) <= 1e-12
+    assert np.max(np.abs(D @ (x ** 2) - 2.0 * x)) <= 1e-12
+    xl, wl, Dl = nodal_storage(_abi.DG_NODES_GAUSS_LOBATTO, 7)
+    assert xl[0] == -1.0 and xl[-1] == 1.0
+    assert abs(np.sum(wl) - 2.0) <= 1e-14
+    # the weights tabulated in the Convergence test (rounded to 15 digits)
+    assert np.max(np.abs(wl - cases.WLGL7)) < 1e-14
+
+
+def test_box_geometry_volume_and_free_stream_metrics():
+    for warp, patch in ((0.0, 0), (0.1, 5)):
+        m = HexMesh.box(3, [0, 0, 0], [2 * np.pi] * 3, 5, node_type=_abi.DG_NODES_GAUSS, warp=warp, patch_order=patch)
+        assert abs(m.volume - (2 * np.pi) ** 3) < 1e-9 * (2 * np.pi) ** 3
+        assert m.n_faces == 3 * m.n_elements
+
+
+def test_oracle_free_stream_preservation_on_warped_mesh():
+    """A uniform state has zero right-hand side on a curvilinear mesh (conservative-curl metrics)."""
+    mesh = HexMesh.box(2, [0, 0, 0], [2 * np.pi] * 3, 4, node_type=_abi.DG_NODES_GAUSS, warp=0.1, patch_order=4)
+    cfg = cases.Config(order=4, nodes=_abi.DG_NODES_GAUSS, mach=0.3, reynolds=100.0, riemann=_abi.DG_RIEMANN_LXF)
+    o = oracle.Oracle(mesh, cfg.physics(), cfg.options())
+    q = np.tile([1.0, 0.3, -0.2, 0.1, 1.0 / (1.4 * 0.4 * 0.09) + 0.5 * 0.14], mesh.ndof)
+    o.set_state(q)
+    assert np.max(np.abs(o.rhs(0.0))) < 1e-11
