@@ -1,0 +1,326 @@
+"""Benchmark: DOF x RK-stage updates per second of the DGSEM Navier-Stokes RHS + Williamson RK3.
+
+Workload: the curvilinear Taylor-Green case, 32^3 hexahedra on [0,2pi]^3 warped by
+x_i += 0.1 sin x sin y sin z, order N=5 on Gauss nodes (7,077,888 DOF), Lax-Friedrichs, BR1,
+M=0.1, Re=1600, Pr=0.72, fixed dt from CFL 0.4 at t=0. One bench step = one RK3 time step of the
+whole mesh (3 RHS evaluations + 3 low-storage updates) = 3*NDOF DOF-stage updates.
+
+value    : mixed form (FP32 fluxes/contractions, FP64 state and RK accumulation), state resident in
+           HBM, K steps replayed from a CUDA graph, timed with CUDA events on the solver's stream.
+plain    : the plain FP64 form timed the same way (the spec ratio is value/plain).
+e2e      : the reference-facing C ABI driven like IntegrateInTime with host buffers: upload Q from
+           pinned host memory, per step dg_max_dt + dg_rk3_step + dg_residuals (host scalars in,
+           residuals out), download Q at the end; all inside the timed region.
+roofline : the dominant kernel's algorithmic bytes per launch over its CUDA-event launch time,
+           against the measured HBM copy bandwidth (MEASURED_PEAKS.json).
+cpu_baseline: the CPU FP64 oracle (port of the reference loops) on the host cores.
+
+--impl reference times the reference's CPU implementation of this path. The Fortran reference does
+not build on this image (no Fortran compiler), so the reference arm runs the oracle port with all
+host threads on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_ELEM = 32
+ORDER = 5
+MACH, RE = 0.1, 1600.0
+WARP = 0.1
+CFL = 0.4
+WORKLOAD = "tgv_curvilinear_32^3_N5_gauss_lxf_br1"
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def _allreduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        self.file.flush()
+        rows = [r.split(",") for r in Path(self.file.name).read_text().splitlines() if r.strip()]
+        sm = [float(r[1]) for r in rows if len(r) > 2 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) > 2 and r[2].strip().replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for name, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def build_case():
+    from horses3d_gb300 import _abi, problems
+    from horses3d_gb300.control import Config
+    from horses3d_gb300.mesh import HexMesh
+
+    mesh = HexMesh.box(N_ELEM, [0, 0, 0], [2 * np.pi] * 3, ORDER, node_type=_abi.DG_NODES_GAUSS, warp=WARP,
+                       patch_order=ORDER)
+    q0 = problems.taylor_green(mesh.x, MACH)
+    base = dict(order=ORDER, nodes=_abi.DG_NODES_GAUSS, mach=MACH, reynolds=RE, riemann=_abi.DG_RIEMANN_LXF)
+    return mesh, q0, base
+
+
+def lift_volume_bytes(P: int, word: int) -> float:
+    """Algorithmic bytes per DOF of the lift+volume kernel (Gauss nodes, NS): reads Q (5 FP64), the
+    local gradient (15), the BR1 jumps of the 6 sides (15*6P^2/P^3 per DOF), Ja (9) and 1/J (1) in the
+    storage word; writes the gradient traces (15*6/P per DOF) and QDot (5)."""
+    face = 6.0 / P
+    return 5 * 8 + word * (15 + 15 * face + 9 + 1 + 15 * face + 5)
+
+
+def run_gpu_arm(args, rank, world, local, case):
+    import ctypes as C
+
+    from horses3d_gb300 import _abi
+    from horses3d_gb300.control import Config
+    from horses3d_gb300.problems import rel_l2
+    from horses3d_gb300.solver import NavierStokesDG
+
+    mesh, q0, base = case
+    ndof = mesh.ndof
+    dof_stage_per_step = 3.0 * ndof
+    L = _abi.lib()
+
+    def timed(precision):
+        g = NavierStokesDG(mesh, Config(**base, precision=precision))
+        g.set_state(q0)
+        dt = g.max_time_step(CFL, CFL)
+        t = g.run_steps(args.warmup, 0.0, dt=dt)
+        g.synchronize()
+        _barrier(world)
+        ms = C.c_double()
+        _abi.check(L.dg_time_steps(g._h, args.steps, t, dt, 0.0, 0.0, C.byref(ms)), "dg_time_steps")
+        _barrier(world)
+        return g, dt, ms.value
+
+    from horses3d_gb300._abi import DG_PRECISION_FP64, DG_PRECISION_MIXED
+
+    with ClockSampler(local) as clk:
+        gm, dt, ms_mixed = timed(DG_PRECISION_MIXED)
+    clocks = clk.summary()
+    gp, _, ms_plain = timed(DG_PRECISION_FP64)
+    ms_mixed = _allreduce_max(ms_mixed, world)
+    ms_plain = _allreduce_max(ms_plain, world)
+    value = world * dof_stage_per_step * args.steps / (ms_mixed * 1e-3)
+    plain = world * dof_stage_per_step * args.steps / (ms_plain * 1e-3)
+    # accuracy of the mixed form against the FP64 form after the same steps
+    acc = rel_l2(gm.Q, gp.Q)
+
+    # per-kernel launch times of the mixed form (dominant kernel for the roofline)
+    kt = np.zeros(5)
+    _abi.check(L.dg_kernel_times(gm._h, 10, 0.0, dt, _abi.f64ptr(kt)), "dg_kernel_times")
+    kt_plain = np.zeros(5)
+    _abi.check(L.dg_kernel_times(gp._h, 3, 0.0, dt, _abi.f64ptr(kt_plain)), "dg_kernel_times")
+    names = ["prolong_grad", "br1_face", "lift_volume", "flux_face", "surface_rk"]
+    P = ORDER + 1
+    hbm, peak_kind = _peaks()
+    alg = lift_volume_bytes(P, 4) * ndof
+    achieved = alg / (kt[2] * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "k_lift_volume<6,gauss,float>", "achieved": round(achieved, 1),
+                "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / hbm, 4),
+                "traffic": None, "alg_bytes_per_launch": alg}
+
+    # e2e through the C ABI with host buffers (IntegrateInTime-shaped loop)
+    import torch
+
+    pinned = torch.empty(q0.size, dtype=torch.float64).pin_memory()
+    pinned.numpy()[:] = q0
+    out = torch.empty(q0.size, dtype=torch.float64).pin_memory()
+    ge = NavierStokesDG(mesh, Config(**base, precision=DG_PRECISION_MIXED))
+    qp = C.cast(pinned.data_ptr(), C.POINTER(C.c_double))
+    op = C.cast(out.data_ptr(), C.POINTER(C.c_double))
+    res = np.zeros(5)
+    nan = C.c_int()
+    dtv = C.c_double()
+    e2e_steps = max(1, args.steps)
+
+    def e2e_once():
+        _abi.check(L.dg_upload_state(ge._h, qp), "dg_upload_state")
+        t = 0.0
+        for _ in range(e2e_steps):
+            _abi.check(L.dg_max_dt(ge._h, CFL, CFL, C.byref(dtv)), "dg_max_dt")
+            _abi.check(L.dg_rk3_step(ge._h, t, dtv.value), "dg_rk3_step")
+            t += dtv.value
+            L.dg_residuals(ge._h, _abi.f64ptr(res), C.byref(nan))
+        _abi.check(L.dg_download(ge._h, _abi.DG_FIELD_Q, op), "dg_download")
+
+    e2e_once()  # warm-up
+    _barrier(world)
+    t0 = time.perf_counter()
+    e2e_once()
+    e2e_s = _allreduce_max(time.perf_counter() - t0, world)
+    e2e_value = world * dof_stage_per_step * e2e_steps / e2e_s
+    qbytes = 8 * q0.size
+    e2e = {"value": e2e_value, "unit": "DOF*stage/s", "h2d_bytes_per_step": int(qbytes / e2e_steps + 16 * 1),
+           "d2h_bytes_per_step": int(qbytes / e2e_steps + 8 + 40 + 4),
+           "loop": "upload Q; per step dg_max_dt + dg_rk3_step + dg_residuals; download Q"}
+
+    return {
+        "value": value, "ms_per_step": ms_mixed / args.steps, "plain": plain,
+        "plain_ms_per_step": ms_plain / args.steps, "mixed_over_plain": value / plain,
+        "rel_l2_mixed_vs_fp64": [float(v) for v in acc], "roofline": roofline, "e2e": e2e, "clocks": clocks,
+        "kernel_ms_mixed": dict(zip(names, [round(float(v), 5) for v in kt])),
+        "kernel_ms_fp64": dict(zip(names, [round(float(v), 5) for v in kt_plain])), "ndof": ndof, "dt": dt,
+        "gpu_launches": int(args.steps * (3 * 5 + 1)),
+    }
+
+
+def cpu_oracle_rate(case, steps: int = 1):
+    """Oracle FP64 throughput on the host cores (OpenMP, all threads) on RK3 steps of the workload."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
+    mesh, q0, base = case
+    from horses3d_gb300.control import Config
+
+    cfg = Config(**base)
+    o = oracle.Oracle(mesh, cfg.physics(), cfg.options())
+    o.set_state(q0)
+    dt = o.max_dt(CFL, CFL)
+    t0 = time.perf_counter()
+    for s in range(steps):
+        o.rk3_step(s * dt, dt)
+    el = time.perf_counter() - t0
+    return 3.0 * mesh.ndof * steps / el, el
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+    threads = os.cpu_count() or 1
+    metric = "DOF*RK-stage updates/s"
+    config = {"workload": WORKLOAD, "elements": N_ELEM ** 3, "order": ORDER, "ndof": (N_ELEM * (ORDER + 1)) ** 3,
+              "nodes": "gauss", "riemann": "lax-friedrichs", "viscous": "br1", "mach": MACH, "reynolds": RE,
+              "warp": WARP, "dt": "CFL 0.4 at t=0, fixed", "l2": "inputs larger than L2 (Q alone 283 MB)",
+              "parallelism": f"replicas x{world}"}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from horses3d_gb300 import build as product_build
+
+        product_build.build()
+        rate, el = cpu_oracle_rate(build_case(), steps=1)
+        line = {"impl": "reference", "metric": metric, "value": rate, "unit": "DOF*stage/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+                "cpu_baseline": {"value": rate, "unit": "DOF*stage/s", "cores": threads, "kind": "port",
+                                 "sample": "one RK3 step of the full 32^3 N=5 workload (7.08 M DOF)"},
+                "e2e": {"value": rate, "unit": "DOF*stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "note": "Fortran reference not buildable here (no Fortran compiler); the oracle port of its "
+                        "loops runs on all host threads"}
+        print(json.dumps(line))
+        return
+    from horses3d_gb300 import build as product_build
+
+    if rank == 0:
+        product_build.build()
+    _barrier(world)
+    if world > 1:
+        import torch
+
+        torch.cuda.set_device(local)
+    case = build_case()
+    r = run_gpu_arm(args, rank, world, local, case)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        rate, el = cpu_oracle_rate(case, steps=1)
+        cpu = {"value": rate, "unit": "DOF*stage/s", "cores": threads, "kind": "port",
+               "sample": f"one RK3 step of the full workload ({el:.1f} s)"}
+    if rank != 0:
+        return
+    line = {"metric": metric, "value": r["value"], "unit": "DOF*stage/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 fluxes / f64 state", "data": "synthetic", "config": config,
+            "plain_fp64": {"value": r["plain"], "ms_per_step": r["plain_ms_per_step"]},
+            "mixed_over_plain": r["mixed_over_plain"], "rel_l2_mixed_vs_fp64": r["rel_l2_mixed_vs_fp64"],
+            "roofline": r["roofline"], "cpu_baseline": cpu, "e2e": r["e2e"], "clocks": r["clocks"],
+            "gpu_launches": r["gpu_launches"], "kernel_ms_mixed": r["kernel_ms_mixed"],
+            "kernel_ms_fp64": r["kernel_ms_fp64"]}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

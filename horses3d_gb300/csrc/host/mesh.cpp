@@ -8,6 +8,7 @@
 #include <fstream>
 #include <map>
 #include <sstream>
+#include <stdexcept>
 
 #include "spectral.hpp"
 
@@ -66,6 +67,7 @@ void FacePatch::construct(const std::vector<double>& u, const std::vector<double
                           const std::vector<double>& points) {
     nu = static_cast<int>(u.size());
     nv = static_cast<int>(v.size());
+    if (nu > kMaxKnots || nv > kMaxKnots) throw std::invalid_argument("face patch order above 31");
     uk = u; vk = v;
     wbu.assign(nu, 0.0); wbv.assign(nv, 0.0);
     Du.assign(nu * nu, 0.0); Dv.assign(nv * nv, 0.0);
@@ -86,9 +88,9 @@ void FacePatch::point(double u1, double u2, double p[3]) const {
         }
         return;
     }
-    std::vector<double> li(nu), lj(nv);
-    interpolating_polynomial_vector(u1, nu - 1, uk.data(), wbu.data(), li.data());
-    interpolating_polynomial_vector(u2, nv - 1, vk.data(), wbv.data(), lj.data());
+    double li[kMaxKnots], lj[kMaxKnots];
+    interpolating_polynomial_vector(u1, nu - 1, uk.data(), wbu.data(), li);
+    interpolating_polynomial_vector(u2, nv - 1, vk.data(), wbv.data(), lj);
     p[0] = p[1] = p[2] = 0.0;
     for (int j = 0; j < nv; ++j)
         for (int i = 0; i < nu; ++i)
@@ -108,9 +110,9 @@ void FacePatch::deriv(double u1, double u2, double g[3][2]) const {
         }
         return;
     }
-    std::vector<double> li(nu), lj(nv), dli(nu, 0.0), dlj(nv, 0.0);
-    interpolating_polynomial_vector(u1, nu - 1, uk.data(), wbu.data(), li.data());
-    interpolating_polynomial_vector(u2, nv - 1, vk.data(), wbv.data(), lj.data());
+    double li[kMaxKnots], lj[kMaxKnots], dli[kMaxKnots] = {}, dlj[kMaxKnots] = {};
+    interpolating_polynomial_vector(u1, nu - 1, uk.data(), wbu.data(), li);
+    interpolating_polynomial_vector(u2, nv - 1, vk.data(), wbv.data(), lj);
     for (int i = 0; i < nu; ++i)
         for (int j = 0; j < nu; ++j) dli[i] = dli[i] + Du[j * nu + i] * li[j];
     for (int i = 0; i < nv; ++i)

@@ -15,6 +15,7 @@ namespace h3d {
 enum Side { EFRONT = 1, EBACK = 2, EBOTTOM = 3, ERIGHT = 4, ETOP = 5, ELEFT = 6 };
 
 // Lagrange surface patch through points given on a tensor grid of knots (FacePatchClass.f90).
+constexpr int kMaxKnots = 32;
 struct FacePatch {
     int nu = 0, nv = 0;
     std::vector<double> uk, vk, wbu, wbv, Du, Dv;
