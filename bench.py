@@ -154,10 +154,11 @@ def run_gpu_arm(args, rank, world, local, case):
     dof_stage_per_step = 3.0 * ndof
     L = _abi.lib()
 
-    def timed(precision):
+    def timed(precision, dt=None):
         g = NavierStokesDG(mesh, Config(**base, precision=precision))
         g.set_state(q0)
-        dt = g.max_time_step(CFL, CFL)
+        if dt is None:
+            dt = g.max_time_step(CFL, CFL)
         t = g.run_steps(args.warmup, 0.0, dt=dt)
         g.synchronize()
         _barrier(world)
@@ -168,10 +169,10 @@ def run_gpu_arm(args, rank, world, local, case):
 
     from horses3d_gb300._abi import DG_PRECISION_FP64, DG_PRECISION_MIXED
 
+    gp, dt, ms_plain = timed(DG_PRECISION_FP64)  # dt: the FP64 MaxTimeStep at t=0, shared by both forms
     with ClockSampler(local) as clk:
-        gm, dt, ms_mixed = timed(DG_PRECISION_MIXED)
+        gm, _, ms_mixed = timed(DG_PRECISION_MIXED, dt)
     clocks = clk.summary()
-    gp, _, ms_plain = timed(DG_PRECISION_FP64)
     ms_mixed = _allreduce_max(ms_mixed, world)
     ms_plain = _allreduce_max(ms_plain, world)
     value = world * dof_stage_per_step * args.steps / (ms_mixed * 1e-3)
@@ -264,7 +265,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--elements", type=int, default=N_ELEM, help="elements per direction (profiling runs)")
+    ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
+                    help="profiling run: only warm-up + timed steps of one form, no extra legs")
     args = ap.parse_args()
+    global N_ELEM
+    N_ELEM = args.elements
     rank, world, local = _dist()
     if world > 1:
         import torch.distributed as dist
@@ -303,6 +309,19 @@ def main():
 
         torch.cuda.set_device(local)
     case = build_case()
+    if args.profile:
+        from horses3d_gb300.control import Config
+        from horses3d_gb300.solver import NavierStokesDG
+
+        mesh, q0, base = case
+        prec = 1 if args.profile == "mixed" else 0
+        g = NavierStokesDG(mesh, Config(**base, precision=prec))
+        g.set_state(q0)
+        dt = g.max_time_step(CFL, CFL)
+        t = g.run_steps(args.warmup, 0.0, dt=dt)
+        t = g.run_steps(args.steps, t, dt=dt)
+        print(json.dumps({"profile": args.profile, "elements": N_ELEM, "ndof": mesh.ndof, "t_end": t}))
+        return
     r = run_gpu_arm(args, rank, world, local, case)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -362,6 +362,19 @@ int64_t dg_ndof(const dg_ctx* c) { return c ? c->ndof : 0; }
 
 int dg_upload_state(dg_ctx* c, const double* q) {
     if (!c || !q) return h3d::fail(DG_ERR_INVALID, "null argument");
+    if (c->mixed) {
+        // energy reference of the mixed form: the mean energy of the uploaded state
+        double sum = 0.0;
+        for (int64_t g = 0; g < c->ndof; ++g) sum += q[5 * g + 4];
+        const double e_ref = sum / static_cast<double>(c->ndof);
+        if (!std::isfinite(e_ref)) return h3d::fail(DG_ERR_NAN, "NaN or Inf in the uploaded state");
+        if (e_ref != c->s32.args.e_ref) {
+            c->s32.args.e_ref = e_ref;
+            dg::set_reference_energy(c->s32.args.ph, c->pc.gm1, e_ref);
+            if (c->graph) cudaGraphExecDestroy(c->graph);  // kernel arguments changed
+            c->graph = nullptr;
+        }
+    }
     CK(cudaMemcpyAsync(c->Q.p, q, sizeof(double) * 5 * c->ndof, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemsetAsync(c->G.p, 0, sizeof(double) * 5 * c->ndof, c->stream));
     CK(cudaStreamSynchronize(c->stream));

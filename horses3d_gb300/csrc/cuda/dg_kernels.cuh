@@ -65,6 +65,7 @@ struct Args {
     R* FS;   // [6K][P^2][5]
     const double* time;  // device scalars: step start time and dt
     const double* dt;
+    double e_ref;        // energy reference of the mixed form (0 for the plain form)
     // MMS source constants
     double src_gm1, src_gM2, src_mu, src_kappa;
 };
@@ -78,6 +79,14 @@ struct Geo {
 
 // Element-face slot index of side s (1..6) and the face coordinates (a,b) of node (i,j,k).
 __device__ __forceinline__ int64_t slot(int e, int side) { return 6 * static_cast<int64_t>(e) + (side - 1); }
+
+// The FP64 state of node g in the working precision; the energy relative to e_ref (FP64 difference).
+template <typename R>
+__device__ __forceinline__ void load_state(const Args<R>& a, int64_t g, R* q) {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) q[v] = R(a.Q[5 * g + v]);
+    q[4] = R(a.Q[5 * g + 4] - a.e_ref);
+}
 
 // ------------------------------------------------------------------------------------------------
 // k_prolong_grad: local gradient U_x,U_y,U_z (state gradient variables U = Q) and Q face traces.
@@ -93,8 +102,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS) k_prolong_grad(Args<R> a) {
     const int64_t g = static_cast<int64_t>(e) * P3 + n;
     R q[5];
     if (active) {
-#pragma unroll
-        for (int v = 0; v < 5; ++v) q[v] = R(a.Q[5 * g + v]);
+        load_state(a, g, q);
 #pragma unroll
         for (int v = 0; v < 5; ++v) sQ[le][v][n] = q[v];
     }
@@ -218,10 +226,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS) k_lift_volume(Args<R> a, int 
     const bool ns = a.ph.ns;
     R U[3][5];
     R q[5];
-    if (active) {
-#pragma unroll
-        for (int v = 0; v < 5; ++v) q[v] = R(a.Q[5 * g + v]);
-    }
+    if (active) load_state(a, g, q);
     if (ns && active) {
 #pragma unroll
         for (int v = 0; v < 5; ++v) { U[0][v] = a.Ux[5 * g + v]; U[1][v] = a.Uy[5 * g + v]; U[2][v] = a.Uz[5 * g + v]; }

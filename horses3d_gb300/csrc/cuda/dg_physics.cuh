@@ -13,10 +13,17 @@ struct PhysConst {
     int ns, riemann, averaging, inviscid, source;
 };
 
+// The mixed form stores the energy relative to a constant reference E_ref (Q5' = E - E_ref, formed in
+// FP64 before the conversion to FP32). Pressures are then p' = p - p_ref with p_ref = (gamma-1) E_ref,
+// and total enthalpies add h_ref = E_ref + p_ref back. The constant p_ref is left out of the momentum
+// fluxes: a constant flux has zero DG divergence on these metrics (free-stream preservation), while
+// carrying it in FP32 would bury the O(1) pressure gradient under the O(1/(gamma M^2)) background.
+// The plain FP64 form uses E_ref = p_ref = h_ref = 0, i.e. the reference's formulas unchanged.
 template <typename R>
 struct PhysR {
     R gamma, gm1, gammaM2, mu, kappa, mu_to_kappa, S_div_TRef, TReNorm, lambda_stab;
     R g_over_gm1, gp1_over_4, gm1_gammaM2;
+    R e_ref, p_ref, h_ref;
     int ns, riemann, averaging;
 };
 
@@ -29,8 +36,16 @@ PhysR<R> make_phys(const PhysConst& c) {
     p.g_over_gm1 = R(c.gamma / (c.gamma - 1.0));
     p.gp1_over_4 = R((c.gamma + 1.0) / 4.0);
     p.gm1_gammaM2 = R(c.gm1 * c.gammaM2);
+    p.e_ref = R(0); p.p_ref = R(0); p.h_ref = R(0);
     p.ns = c.ns; p.riemann = c.riemann; p.averaging = c.averaging;
     return p;
+}
+
+template <typename R>
+void set_reference_energy(PhysR<R>& p, double gm1, double e_ref) {
+    p.e_ref = R(e_ref);
+    p.p_ref = R(gm1 * e_ref);
+    p.h_ref = R(e_ref + gm1 * e_ref);
 }
 
 template <typename R> __device__ __forceinline__ R dsqrt(R x);
@@ -40,7 +55,7 @@ template <> __device__ __forceinline__ float dsqrt<float>(float x) { return sqrt
 // VariableConversion_NS.f90:44-57,147-186: pressure, temperature, Sutherland's law.
 template <typename R>
 __device__ __forceinline__ void mu_kappa(const PhysR<R>& p, const R* Q, R& mu, R& kappa) {
-    const R pr = p.gm1 * (Q[4] - R(0.5) * (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) / Q[0]);
+    const R pr = p.gm1 * (Q[4] - R(0.5) * (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) / Q[0]) + p.p_ref;
     const R T = p.gammaM2 * pr / Q[0];
     const R t = T * p.TReNorm;
     const R s = (R(1) + p.S_div_TRef) / (t + p.S_div_TRef) * t * dsqrt(t);
@@ -55,9 +70,10 @@ __device__ __forceinline__ void euler_contravariant(const PhysR<R>& p, const R* 
                                                     const R* ja2, R F[3][5]) {
     const R u = Q[1] / Q[0], v = Q[2] / Q[0], w = Q[3] / Q[0];
     const R pr = p.gm1 * (Q[4] - R(0.5) * (Q[1] * u + Q[2] * v + Q[3] * w));
-    const R f[5] = {Q[1], Q[1] * u + pr, Q[1] * v, Q[1] * w, (Q[4] + pr) * u};
-    const R g[5] = {Q[2], f[2], Q[2] * v + pr, Q[2] * w, (Q[4] + pr) * v};
-    const R h[5] = {Q[3], f[3], g[3], Q[3] * w + pr, (Q[4] + pr) * w};
+    const R H = Q[4] + pr + p.h_ref;  // rho * total enthalpy
+    const R f[5] = {Q[1], Q[1] * u + pr, Q[1] * v, Q[1] * w, H * u};
+    const R g[5] = {Q[2], f[2], Q[2] * v + pr, Q[2] * w, H * v};
+    const R h[5] = {Q[3], f[3], g[3], Q[3] * w + pr, H * w};
     const R* ja[3] = {ja0, ja1, ja2};
 #pragma unroll
     for (int d = 0; d < 3; ++d)
@@ -80,7 +96,7 @@ __device__ __forceinline__ void viscous_flux(const PhysR<R>& p, const R* Q, cons
         uz[c] = invRho * Uz[1 + c] - ud[c] * Uz[0];
     }
     const R g = p.gm1_gammaM2;
-    const R e2 = Q[4] * invRho * invRho;
+    const R e2 = (Q[4] + p.e_ref) * invRho * invRho;
     const R nTx = g * (invRho * Ux[4] - e2 * Ux[0] - u * ux[0] - v * ux[1] - w * ux[2]);
     const R nTy = g * (invRho * Uy[4] - e2 * Uy[0] - u * uy[0] - v * uy[1] - w * uy[2]);
     const R nTz = g * (invRho * Uz[4] - e2 * Uz[0] - u * uz[0] - v * uz[1] - w * uz[2]);
@@ -111,8 +127,8 @@ __device__ __forceinline__ void roe_flux(const PhysR<R>& p, const R* QL, const R
     const R pright = gm1 * (QR[4] - R(0.5) / rhon * (QR[1] * QR[1] + QR[2] * QR[2] + QR[3] * QR[3]));
     const R ql = n[0] * ul + n[1] * vl + n[2] * wl;
     const R qr = n[0] * ur + n[1] * vr + n[2] * wr;
-    const R hl = R(0.5) * (ul * ul + vl * vl + wl * wl) + p.g_over_gm1 * pleft / rho;
-    const R hr = R(0.5) * (ur * ur + vr * vr + wr * wr) + p.g_over_gm1 * pright / rhon;
+    const R hl = R(0.5) * (ul * ul + vl * vl + wl * wl) + p.g_over_gm1 * (pleft + p.p_ref) / rho;
+    const R hr = R(0.5) * (ur * ur + vr * vr + wr * wr) + p.g_over_gm1 * (pright + p.p_ref) / rhon;
     const R rtd = dsqrt(rho * rhon);
     const R betal = rho / (rho + rtd), betar = R(1) - betal;
     const R utd = betal * ul + betar * ur, vtd = betal * vl + betar * vr, wtd = betal * wl + betar * wr;
@@ -164,7 +180,7 @@ __device__ __forceinline__ void lxf_flux(const PhysR<R>& p, const R* QL, const R
     const R rwR = QR[1] * t2[0] + QR[2] * t2[1] + QR[3] * t2[2];
     const R pL = p.gm1 * (QL[4] - R(0.5) * ((ruL * ruL + rvL * rvL + rwL * rwL) * iL));
     const R pR = p.gm1 * (QR[4] - R(0.5) * ((ruR * ruR + rvR * rvR + rwR * rwR) * iR));
-    const R aL = dsqrt(p.gamma * pL * iL), aR = dsqrt(p.gamma * pR * iR);
+    const R aL = dsqrt(p.gamma * (pL + p.p_ref) * iL), aR = dsqrt(p.gamma * (pR + p.p_ref) * iR);
     const R lL = fabs(ruL * iL) + aL, lR = fabs(ruR * iR) + aR;
     const R lambda = lL > lR ? lL : lR;
     const R uL = iL * ruL, uR = iR * ruR, vL = iL * rvL, vR = iR * rvR, wL = iL * rwL, wR = iR * rwR;
@@ -174,11 +190,11 @@ __device__ __forceinline__ void lxf_flux(const PhysR<R>& p, const R* QL, const R
         f[1] = R(0.5) * (ruL * uL + ruR * uR + pL + pR);
         f[2] = R(0.5) * (ruL * vL + ruR * vR);
         f[3] = R(0.5) * (ruL * wL + ruR * wR);
-        f[4] = R(0.5) * (uL * (QL[4] + pL) + uR * (QR[4] + pR));
+        f[4] = R(0.5) * (uL * (QL[4] + pL + p.h_ref) + uR * (QR[4] + pR + p.h_ref));
     } else {
         const R rho = R(0.5) * (QL[0] + QR[0]), u = R(0.5) * (uL + uR), v = R(0.5) * (vL + vR), w = R(0.5) * (wL + wR);
         const R pp = R(0.5) * (pL + pR);
-        const R h = R(0.5) * ((QL[4] + pL) * iL + (QR[4] + pR) * iR);
+        const R h = R(0.5) * ((QL[4] + pL + p.h_ref) * iL + (QR[4] + pR + p.h_ref) * iR);
         f[0] = rho * u; f[1] = rho * u * u + pp; f[2] = rho * u * v; f[3] = rho * u * w; f[4] = rho * u * h;
     }
     const R ls = p.lambda_stab * (R(0.5) * lambda);
@@ -203,18 +219,19 @@ __device__ __forceinline__ void two_point_flux(const PhysR<R>& p, const R* QL, c
     const R pR = p.gm1 * (QR[4] - R(0.5) * (QR[1] * uR + QR[2] * vR + QR[3] * wR));
     if (p.averaging == 0) {
         const R J0 = JaL[0] + JaR[0], J1 = JaL[1] + JaR[1], J2 = JaL[2] + JaR[2];
+        const R HL = QL[4] + pL + p.h_ref, HR = QR[4] + pR + p.h_ref;
         const R f[5] = {QL[1] + QR[1], QL[1] * uL + QR[1] * uR + pL + pR, QL[1] * vL + QR[1] * vR, QL[1] * wL + QR[1] * wR,
-                        uL * (QL[4] + pL) + uR * (QR[4] + pR)};
+                        uL * HL + uR * HR};
         const R g[5] = {QL[2] + QR[2], QL[2] * uL + QR[2] * uR, QL[2] * vL + QR[2] * vR + pL + pR, QL[2] * wL + QR[2] * wR,
-                        vL * (QL[4] + pL) + vR * (QR[4] + pR)};
+                        vL * HL + vR * HR};
         const R h[5] = {QL[3] + QR[3], QL[3] * uL + QR[3] * uR, QL[3] * vL + QR[3] * vR, QL[3] * wL + QR[3] * wR + pL + pR,
-                        wL * (QL[4] + pL) + wR * (QR[4] + pR)};
+                        wL * HL + wR * HR};
 #pragma unroll
         for (int q = 0; q < 5; ++q) fs[q] = R(0.25) * (f[q] * J0 + g[q] * J1 + h[q] * J2);
     } else {
         const R rho = R(0.5) * (QL[0] + QR[0]), u = R(0.5) * (uL + uR), v = R(0.5) * (vL + vR), w = R(0.5) * (wL + wR);
         const R pp = R(0.5) * (pL + pR);
-        const R h = R(0.5) * ((QL[4] + pL) * iL + (QR[4] + pR) * iR);
+        const R h = R(0.5) * ((QL[4] + pL + p.h_ref) * iL + (QR[4] + pR + p.h_ref) * iR);
         const R J0 = R(0.5) * (JaL[0] + JaR[0]), J1 = R(0.5) * (JaL[1] + JaR[1]), J2 = R(0.5) * (JaL[2] + JaR[2]);
         const R ru = rho * u, rv = rho * v, rw = rho * w;
         fs[0] = ru * J0 + rv * J1 + rw * J2;

@@ -106,10 +106,15 @@ def mms_convergence_state(x: np.ndarray, t: float):
 
 
 def rel_l2(a: np.ndarray, b: np.ndarray, weights: np.ndarray | None = None) -> np.ndarray:
-    """Relative L2 difference per conserved variable: sqrt(sum w (a-b)^2) / sqrt(sum w b^2)."""
+    """Relative L2 difference per conserved variable: sqrt(sum w (a-b)^2) / sqrt(sum w b^2).
+
+    The three momentum components share one denominator, the L2 norm of the momentum vector
+    sqrt(sum w |rho u|^2): a single component can vanish identically (w = 0 in the Taylor-Green
+    vortex), which would turn its own norm into a division by ~0."""
     a = np.asarray(a).reshape(-1, 5)
     b = np.asarray(b).reshape(-1, 5)
     w = np.ones(a.shape[0]) if weights is None else np.asarray(weights).reshape(-1)
     num = np.sqrt(np.einsum("n,nv->v", w, (a - b) ** 2))
     den = np.sqrt(np.einsum("n,nv->v", w, b ** 2))
+    den[1:4] = np.sqrt(np.sum(den[1:4] ** 2))
     return num / np.where(den > 0, den, 1.0)
