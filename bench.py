@@ -121,12 +121,11 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
-def build_case():
+def build_case(n_elem: int = N_ELEM):
     from horses3d_gb300 import _abi, problems
-    from horses3d_gb300.control import Config
     from horses3d_gb300.mesh import HexMesh
 
-    mesh = HexMesh.box(N_ELEM, [0, 0, 0], [2 * np.pi] * 3, ORDER, node_type=_abi.DG_NODES_GAUSS, warp=WARP,
+    mesh = HexMesh.box(n_elem, [0, 0, 0], [2 * np.pi] * 3, ORDER, node_type=_abi.DG_NODES_GAUSS, warp=WARP,
                        patch_order=ORDER)
     q0 = problems.taylor_green(mesh.x, MACH)
     base = dict(order=ORDER, nodes=_abi.DG_NODES_GAUSS, mach=MACH, reynolds=RE, riemann=_abi.DG_RIEMANN_LXF)
@@ -269,8 +268,6 @@ def main():
     ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
                     help="profiling run: only warm-up + timed steps of one form, no extra legs")
     args = ap.parse_args()
-    global N_ELEM
-    N_ELEM = args.elements
     rank, world, local = _dist()
     if world > 1:
         import torch.distributed as dist
@@ -278,7 +275,8 @@ def main():
         dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
     threads = os.cpu_count() or 1
     metric = "DOF*RK-stage updates/s"
-    config = {"workload": WORKLOAD, "elements": N_ELEM ** 3, "order": ORDER, "ndof": (N_ELEM * (ORDER + 1)) ** 3,
+    config = {"workload": WORKLOAD, "elements": args.elements ** 3, "order": ORDER,
+              "ndof": (args.elements * (ORDER + 1)) ** 3,
               "nodes": "gauss", "riemann": "lax-friedrichs", "viscous": "br1", "mach": MACH, "reynolds": RE,
               "warp": WARP, "dt": "CFL 0.4 at t=0, fixed", "l2": "inputs larger than L2 (Q alone 283 MB)",
               "parallelism": f"replicas x{world}"}
@@ -288,7 +286,7 @@ def main():
         from horses3d_gb300 import build as product_build
 
         product_build.build()
-        rate, el = cpu_oracle_rate(build_case(), steps=1)
+        rate, el = cpu_oracle_rate(build_case(args.elements), steps=1)
         line = {"impl": "reference", "metric": metric, "value": rate, "unit": "DOF*stage/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
@@ -308,7 +306,7 @@ def main():
         import torch
 
         torch.cuda.set_device(local)
-    case = build_case()
+    case = build_case(args.elements)
     if args.profile:
         from horses3d_gb300.control import Config
         from horses3d_gb300.solver import NavierStokesDG
@@ -320,7 +318,7 @@ def main():
         dt = g.max_time_step(CFL, CFL)
         t = g.run_steps(args.warmup, 0.0, dt=dt)
         t = g.run_steps(args.steps, t, dt=dt)
-        print(json.dumps({"profile": args.profile, "elements": N_ELEM, "ndof": mesh.ndof, "t_end": t}))
+        print(json.dumps({"profile": args.profile, "elements": args.elements, "ndof": mesh.ndof, "t_end": t}))
         return
     r = run_gpu_arm(args, rank, world, local, case)
     cpu = None
