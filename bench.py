@@ -132,12 +132,13 @@ def build_case(n_elem: int = N_ELEM):
     return mesh, q0, base
 
 
-def lift_volume_bytes(P: int, word: int) -> float:
-    """Algorithmic bytes per DOF of the lift+volume kernel (Gauss nodes, NS): reads Q (5 FP64), the
-    local gradient (15), the BR1 jumps of the 6 sides (15*6P^2/P^3 per DOF), Ja (9) and 1/J (1) in the
-    storage word; writes the gradient traces (15*6/P per DOF) and QDot (5)."""
+def volume_bytes(P: int, word: int) -> float:
+    """Algorithmic bytes per DOF of k_volume (NS): reads Q (5 FP64), Ja (9) and 1/J (1), and per face
+    point of its six sides (6 P^2 / P^3 = 6/P per DOF) the neighbour's Q trace (5) and the side
+    geometry n, Jf (4), all in the storage word; writes the viscous normal fluxes (5 per face point)
+    and QDot (5)."""
     face = 6.0 / P
-    return 5 * 8 + word * (15 + 15 * face + 9 + 1 + 15 * face + 5)
+    return 5 * 8 + word * (9 + 1 + (5 + 4) * face + 5 * face + 5)
 
 
 def run_gpu_arm(args, rank, world, local, case):
@@ -184,12 +185,12 @@ def run_gpu_arm(args, rank, world, local, case):
     _abi.check(L.dg_kernel_times(gm._h, 10, 0.0, dt, _abi.f64ptr(kt)), "dg_kernel_times")
     kt_plain = np.zeros(5)
     _abi.check(L.dg_kernel_times(gp._h, 3, 0.0, dt, _abi.f64ptr(kt_plain)), "dg_kernel_times")
-    names = ["prolong_grad", "br1_face", "lift_volume", "flux_face", "surface_rk"]
+    names = ["volume", "flux", "update", "traces", "unused"]
     P = ORDER + 1
     hbm, peak_kind = _peaks()
-    alg = lift_volume_bytes(P, 4) * ndof
-    achieved = alg / (kt[2] * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "kernel": "k_lift_volume<6,gauss,float>", "achieved": round(achieved, 1),
+    alg = volume_bytes(P, 4) * ndof
+    achieved = alg / (kt[0] * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "k_volume<6,gauss,float>", "achieved": round(achieved, 1),
                 "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / hbm, 4),
                 "traffic": None, "alg_bytes_per_launch": alg}
 
@@ -234,7 +235,7 @@ def run_gpu_arm(args, rank, world, local, case):
         "rel_l2_mixed_vs_fp64": [float(v) for v in acc], "roofline": roofline, "e2e": e2e, "clocks": clocks,
         "kernel_ms_mixed": dict(zip(names, [round(float(v), 5) for v in kt])),
         "kernel_ms_fp64": dict(zip(names, [round(float(v), 5) for v in kt_plain])), "ndof": ndof, "dt": dt,
-        "gpu_launches": int(args.steps * (3 * 5 + 1)),
+        "gpu_launches": int(args.steps * (3 * 3 + 1)),
     }
 
 

@@ -44,17 +44,31 @@ struct DevBuf {
 // Everything one precision needs on the device.
 template <typename R>
 struct Store {
-    DevBuf<R> ja_xi, ja_eta, ja_zeta, jac, inv_jac, fn, ft1, ft2, fj;
-    DevBuf<R> QDot, Ux, Uy, Uz, QF, UN, GF, FS;
+    DevBuf<R> ja_xi, ja_eta, ja_zeta, jac, inv_jac, fn, ft1, ft2, fj, sgeo;
+    DevBuf<R> QDot, Ux, Uy, Uz, QF, FV, FS;
     Args<R> args;
     dg::StageFn<R> stage = nullptr;
     dg::KernelTimesFn<R> times = nullptr;
     void free() {
-        for (DevBuf<R>* b : {&ja_xi, &ja_eta, &ja_zeta, &jac, &inv_jac, &fn, &ft1, &ft2, &fj, &QDot, &Ux, &Uy, &Uz,
-                             &QF, &UN, &GF, &FS})
+        for (DevBuf<R>* b : {&ja_xi, &ja_eta, &ja_zeta, &jac, &inv_jac, &fn, &ft1, &ft2, &fj, &sgeo, &QDot, &Ux, &Uy,
+                             &Uz, &QF, &FV, &FS})
             b->free();
     }
 };
+
+// The face point (i, j) whose leftIndexes2Right image is (ii, jj) (MeshTypes.f90:70-107 inverted).
+void right_to_left(int ii, int jj, int N, int rot, int& i, int& j) {
+    switch (rot) {
+        case 0: i = ii; j = jj; break;
+        case 1: i = jj; j = N - ii; break;
+        case 2: i = N - ii; j = N - jj; break;
+        case 3: i = N - jj; j = ii; break;
+        case 4: i = jj; j = ii; break;
+        case 5: i = N - ii; j = jj; break;
+        case 6: i = N - jj; j = N - ii; break;
+        default: i = ii; j = N - jj; break;
+    }
+}
 
 }  // namespace
 
@@ -70,7 +84,7 @@ struct dg_ctx {
     double dxi[3] = {0, 0, 0};
     DevBuf<double> Q, G, x, scal;      // scal: [0] time, [1] dt
     DevBuf<unsigned long long> red;    // [0..1] dt reduction, [2..6] residuals
-    DevBuf<int> face_elem, face_side, face_rot, nan_flag;
+    DevBuf<int> face_elem, face_side, face_rot, nan_flag, nb_slot, nb_map;
     Store<double> s64;
     Store<float> s32;
     double* h_scal = nullptr;          // pinned staging for scalars
@@ -99,27 +113,56 @@ template <typename R>
 int setup_store(dg_ctx* c, Store<R>& st, const dg_mesh_desc* m) {
     const size_t nd = static_cast<size_t>(c->ndof);
     const size_t nfp = static_cast<size_t>(c->F) * c->P * c->P;
-    const size_t nslot = 6 * static_cast<size_t>(c->K) * c->P * c->P;
+    const size_t nslot = 6 * static_cast<size_t>(c->K);
     int rc;
     if ((rc = upload_convert(st.ja_xi, m->ja_xi, 3 * nd, c->stream))) return rc;
     if ((rc = upload_convert(st.ja_eta, m->ja_eta, 3 * nd, c->stream))) return rc;
     if ((rc = upload_convert(st.ja_zeta, m->ja_zeta, 3 * nd, c->stream))) return rc;
     if ((rc = upload_convert(st.jac, m->jacobian, nd, c->stream))) return rc;
     if ((rc = upload_convert(st.inv_jac, m->inv_jacobian, nd, c->stream))) return rc;
-    if ((rc = upload_convert(st.fn, m->face_normal, 3 * nfp, c->stream))) return rc;
-    if ((rc = upload_convert(st.ft1, m->face_t1, 3 * nfp, c->stream))) return rc;
-    if ((rc = upload_convert(st.ft2, m->face_t2, 3 * nfp, c->stream))) return rc;
+    // face geometry in face order, one component after the other (coalesced per component)
+    {
+        std::vector<double> soa(3 * nfp);
+        const double* src[3] = {m->face_normal, m->face_t1, m->face_t2};
+        DevBuf<R>* dst[3] = {&st.fn, &st.ft1, &st.ft2};
+        for (int a = 0; a < 3; ++a) {
+            for (size_t fp = 0; fp < nfp; ++fp)
+                for (int c3 = 0; c3 < 3; ++c3) soa[c3 * nfp + fp] = src[a][3 * fp + c3];
+            if ((rc = upload_convert(*dst[a], soa.data(), 3 * nfp, c->stream))) return rc;
+            CK(cudaStreamSynchronize(c->stream));
+        }
+    }
     if ((rc = upload_convert(st.fj, m->face_jacobian, nfp, c->stream))) return rc;
+    // per-slot geometry (n, Jf) in each side's own face coordinates
+    {
+        const int P = c->P, P2 = P * P;
+        std::vector<double> sg(4 * nslot * P2);
+        for (int f = 0; f < c->F; ++f)
+            for (int side = 0; side < 2; ++side) {
+                const size_t sl = 6 * static_cast<size_t>(m->face_elem[2 * f + side]) + (m->face_side[2 * f + side] - 1);
+                for (int cb = 0; cb < P; ++cb)
+                    for (int ca = 0; ca < P; ++ca) {
+                        int i = ca, j = cb;
+                        if (side == 1) right_to_left(ca, cb, P - 1, m->face_rotation[f], i, j);
+                        const size_t fp = static_cast<size_t>(f) * P2 + i + P * j;
+                        const int p = ca + P * cb;
+                        for (int c3 = 0; c3 < 3; ++c3) sg[(sl * 4 + c3) * P2 + p] = m->face_normal[3 * fp + c3];
+                        sg[(sl * 4 + 3) * P2 + p] = m->face_jacobian[fp];
+                    }
+            }
+        if ((rc = upload_convert(st.sgeo, sg.data(), 4 * nslot * P2, c->stream))) return rc;
+        CK(cudaStreamSynchronize(c->stream));
+    }
     CK(st.QDot.alloc(5 * nd));
     CK(cudaMemsetAsync(st.QDot.p, 0, sizeof(R) * 5 * nd, c->stream));
     const bool ns = c->phys.navier_stokes != 0;
     CK(st.Ux.alloc(ns ? 5 * nd : 0));
     CK(st.Uy.alloc(ns ? 5 * nd : 0));
     CK(st.Uz.alloc(ns ? 5 * nd : 0));
-    CK(st.QF.alloc(5 * nslot));
-    CK(st.UN.alloc(ns ? 15 * nslot : 0));
-    CK(st.GF.alloc(ns ? 15 * nslot : 0));
-    CK(st.FS.alloc(5 * nslot));
+    const size_t P2s = static_cast<size_t>(c->P) * c->P;
+    CK(st.QF.alloc(5 * nslot * P2s));
+    CK(st.FV.alloc(ns ? 5 * nslot * P2s : 0));
+    CK(st.FS.alloc(5 * nslot * P2s));
 
     Args<R>& a = st.args;
     std::memset(&a, 0, sizeof(a));
@@ -145,9 +188,10 @@ int setup_store(dg_ctx* c, Store<R>& st, const dg_mesh_desc* m) {
     a.x = c->x.p;
     a.face_elem = c->face_elem.p; a.face_side = c->face_side.p; a.face_rot = c->face_rot.p;
     a.fn = st.fn.p; a.ft1 = st.ft1.p; a.ft2 = st.ft2.p; a.fj = st.fj.p;
+    a.nb_slot = c->nb_slot.p; a.nb_map = c->nb_map.p; a.sgeo = st.sgeo.p;
     a.Q = c->Q.p; a.G = c->G.p; a.QDot = st.QDot.p;
     a.Ux = st.Ux.p; a.Uy = st.Uy.p; a.Uz = st.Uz.p;
-    a.QF = st.QF.p; a.UN = st.UN.p; a.GF = st.GF.p; a.FS = st.FS.p;
+    a.QF = st.QF.p; a.FV = st.FV.p; a.FS = st.FS.p;
     a.time = c->scal.p;
     a.dt = c->scal.p + 1;
     a.src_gm1 = c->pc.gm1;
@@ -157,16 +201,17 @@ int setup_store(dg_ctx* c, Store<R>& st, const dg_mesh_desc* m) {
     return DG_OK;
 }
 
-cudaError_t run_stage(dg_ctx* c, int stage, double tshift, int store_grad) {
-    if (c->mixed) return c->s32.stage(c->s32.args, stage, tshift, store_grad, c->stream);
-    return c->s64.stage(c->s64.args, stage, tshift, store_grad, c->stream);
+cudaError_t run_stage(dg_ctx* c, int stage, double tshift, int flags) {
+    if (c->mixed) return c->s32.stage(c->s32.args, stage, tshift, flags, c->stream);
+    return c->s64.stage(c->s64.args, stage, tshift, flags, c->stream);
 }
 
-// Queue one RK3 step (time and dt are read from device memory).
+// Queue one RK3 step (time and dt are read from device memory). The last stage keeps its QDot for
+// the residuals, as TakeRK3Step leaves the third stage's QDot in storage.
 cudaError_t enqueue_step(dg_ctx* c) {
     static const double b[3] = {0.0, 1.0 / 3.0, 3.0 / 4.0};
     for (int k = 0; k < 3; ++k) {
-        cudaError_t e = run_stage(c, k, b[k], 0);
+        cudaError_t e = run_stage(c, k, b[k], k == 2 ? dg::kWriteQDot : 0);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -330,6 +375,25 @@ int dg_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op,
         (e = cudaMemcpyAsync(c->face_side.p, m->face_side, sizeof(int) * 2 * c->F, cudaMemcpyHostToDevice, c->stream)) ||
         (e = cudaMemcpyAsync(c->face_rot.p, m->face_rotation, sizeof(int) * c->F, cudaMemcpyHostToDevice, c->stream)))
         return bail(cuda_fail(e, "copy faces"));
+    {  // slot neighbour tables: the other side's slot and (rotation | own side << 3)
+        const size_t nslot = 6 * static_cast<size_t>(c->K);
+        std::vector<int> nbs(nslot, -1), nbm(nslot, 0);
+        for (int f = 0; f < c->F; ++f)
+            for (int side = 0; side < 2; ++side) {
+                const size_t sl = 6 * static_cast<size_t>(m->face_elem[2 * f + side]) + (m->face_side[2 * f + side] - 1);
+                const size_t so = 6 * static_cast<size_t>(m->face_elem[2 * f + 1 - side]) + (m->face_side[2 * f + 1 - side] - 1);
+                if (nbs[sl] != -1) return bail(h3d::fail(DG_ERR_INVALID, "an element side belongs to two faces"));
+                nbs[sl] = static_cast<int>(so);
+                nbm[sl] = m->face_rotation[f] | ((side + 1) << 3);
+            }
+        for (size_t sl = 0; sl < nslot; ++sl)
+            if (nbs[sl] < 0) return bail(h3d::fail(DG_ERR_INVALID, "an element side has no face"));
+        if ((e = c->nb_slot.alloc(nslot)) != cudaSuccess || (e = c->nb_map.alloc(nslot)) != cudaSuccess)
+            return bail(cuda_fail(e, "alloc slot tables"));
+        if ((e = cudaMemcpy(c->nb_slot.p, nbs.data(), sizeof(int) * nslot, cudaMemcpyHostToDevice)) != cudaSuccess ||
+            (e = cudaMemcpy(c->nb_map.p, nbm.data(), sizeof(int) * nslot, cudaMemcpyHostToDevice)) != cudaSuccess)
+            return bail(cuda_fail(e, "copy slot tables"));
+    }
     if (c->mixed) {
         if ((rc = setup_store(c, c->s32, m))) return bail(rc);
         c->s32.stage = dg::stage_fn_fp32(c->P, c->nodes == DG_NODES_GAUSS_LOBATTO);
@@ -352,7 +416,7 @@ void dg_destroy(dg_ctx* c) {
     c->s64.free();
     c->s32.free();
     c->Q.free(); c->G.free(); c->x.free(); c->scal.free(); c->red.free(); c->nan_flag.free();
-    c->face_elem.free(); c->face_side.free(); c->face_rot.free();
+    c->face_elem.free(); c->face_side.free(); c->face_rot.free(); c->nb_slot.free(); c->nb_map.free();
     if (c->h_scal) cudaFreeHost(c->h_scal);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -377,6 +441,7 @@ int dg_upload_state(dg_ctx* c, const double* q) {
     }
     CK(cudaMemcpyAsync(c->Q.p, q, sizeof(double) * 5 * c->ndof, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemsetAsync(c->G.p, 0, sizeof(double) * 5 * c->ndof, c->stream));
+    CK(run_stage(c, dg::kTraces, 0.0, 0));  // face traces of the new state
     CK(cudaStreamSynchronize(c->stream));
     return DG_OK;
 }
@@ -412,7 +477,7 @@ int dg_rhs(dg_ctx* c, double t) {
     if (!c) return h3d::fail(DG_ERR_INVALID, "null context");
     int rc = set_scalars(c, t, 0.0);
     if (rc) return rc;
-    CK(run_stage(c, -1, 0.0, 1));
+    CK(run_stage(c, -1, 0.0, dg::kStoreGrad | dg::kWriteQDot));
     CK(cudaStreamSynchronize(c->stream));
     return DG_OK;
 }
@@ -510,6 +575,7 @@ int dg_kernel_times(dg_ctx* c, int reps, double t0, double dt, double ms[5]) {
     if (!c || !ms || reps < 1) return h3d::fail(DG_ERR_INVALID, "bad arguments");
     int rc = set_scalars(c, t0, dt);
     if (rc) return rc;
+    for (int kk = 0; kk < 5; ++kk) ms[kk] = 0.0;
     if (c->mixed) CK(c->s32.times(c->s32.args, reps, c->stream, ms));
     else CK(c->s64.times(c->s64.args, reps, c->stream, ms));
     return DG_OK;

@@ -1,22 +1,26 @@
 // DGSEM right-hand-side kernels for uniform-order hexahedral meshes, templated on the number of
-// nodes per direction P = N+1, the node family (GL = Gauss-Lobatto) and the arithmetic type R.
+// nodes per direction P = N+1, the node family (GL = Gauss-Lobatto) and the arithmetic type R
+// (double: plain form, float: mixed form; the state Q and the RK register G are FP64 in both).
 //
-// One RK stage runs five kernels (the two face kernels have one thread per face point, the three
-// element kernels one thread per node and one element per P^3 threads):
-//   k_prolong_grad  element: BR1 local gradient (HexElementClass.f90:427-531) and Q face traces
-//                   (HexElementClass.f90:233-302)
-//   k_br1_face      face:    BR1 interface jump 1/2 (UR-UL) Jf n to both sides
-//                   (EllipticBR1.f90:571-627, FaceClass.f90:865-963)
-//   k_lift_volume   element: BR1 lifting (EllipticBR1.f90:531-569), gradient traces
-//                   (HexElementClass.f90:304-372), viscosity, contravariant fluxes and the weak or
-//                   split-form volume integral (SpatialDiscretization.f90:1602-1682, DGIntegrals.f90:56-129)
-//   k_flux_face     face:    Roe/LxF + BR1 averaged viscous flux times Jf, minus on side 2
-//                   (SpatialDiscretization.f90:1710-1799, FaceClass.f90:597-703)
-//   k_surface_rk    element: surface integral, 1/J, source, Williamson RK3 update
-//                   (DGIntegrals.f90:214-273, SpatialDiscretization.f90:483-494, ExplicitMethods.f90:748-779)
+// One RK stage is three kernels; the fourth runs once after an upload:
+//   k_volume    element: local BR1 gradient (HexElementClass.f90:427-531); BR1 interface jump
+//               1/2 (U_R - U_L) Jf n from the own and the neighbour's Q traces
+//               (EllipticBR1.f90:571-627, FaceClass.f90:865-963); lifting (EllipticBR1.f90:531-569);
+//               gradient traces (HexElementClass.f90:304-372) turned into each side's viscous
+//               normal flux Fv(Q, grad U) . n (EllipticBR1.f90:816-868); viscosity, contravariant
+//               fluxes and the weak or split-form volume integral
+//               (SpatialDiscretization.f90:1602-1682, DGIntegrals.f90:56-129) -> QDot
+//   k_flux      face:    Roe/LxF flux minus the averaged viscous normal flux, times Jf; side 1 gets
+//               f*, side 2 gets -f* (SpatialDiscretization.f90:1710-1799, FaceClass.f90:597-703)
+//   k_update    element: surface integral, 1/J, source (DGIntegrals.f90:214-273,
+//               SpatialDiscretization.f90:483-494,564-639), the Williamson RK3 update
+//               (ExplicitMethods.f90:748-779) and the Q face traces of the updated state for the next
+//               stage (HexElementClass.f90:233-302)
+//   k_traces    element: Q face traces of the current state (after an upload)
 //
-// Face data live in element-face "slots": slot = 6*e + side-1 (sides numbered as the reference),
-// point index a + P*b in the element's own face coordinates (the FaceStorage(side) arrays).
+// Face data live in element-face "slots" (slot = 6e + side-1, sides numbered as the reference), in
+// the element's own face coordinates (the FaceStorage(side) arrays), stored per variable:
+// value(slot, var, p) at [(slot*NV + var)*P^2 + p], p = a + P*b.
 #pragma once
 #include <cstdint>
 
@@ -38,13 +42,14 @@ struct Args {
     PhysR<R> ph;
     Ops<R> ops;
     int inviscid, source;
-    // geometry (per node / per face point)
+    // geometry per node
     const R* ja_xi;
     const R* ja_eta;
     const R* ja_zeta;
     const R* jac;
     const R* inv_jac;
     const double* x;
+    // faces: connectivity and geometry in face order (SoA: component c at [c*nfp + fp])
     const int* face_elem;
     const int* face_side;
     const int* face_rot;
@@ -52,21 +57,24 @@ struct Args {
     const R* ft1;
     const R* ft2;
     const R* fj;
+    // slots: neighbour slot, (rotation | own side << 3), geometry (n_x,n_y,n_z,Jf) in own coordinates
+    const int* nb_slot;
+    const int* nb_map;
+    const R* sgeo;  // [6K][4][P^2]
     // state
     double* Q;
     double* G;
     R* QDot;
-    R* Ux;
+    R* Ux;  // lifted gradient, written only when store_grad is set
     R* Uy;
     R* Uz;
-    R* QF;   // [6K][P^2][5]
-    R* UN;   // [6K][P^2][15]
-    R* GF;   // [6K][P^2][15]
-    R* FS;   // [6K][P^2][5]
+    R* QF;   // Q traces          [6K][5][P^2]
+    R* FV;   // viscous n-fluxes  [6K][5][P^2]
+    R* FS;   // surface fluxes    [6K][5][P^2]
     const double* time;  // device scalars: step start time and dt
     const double* dt;
     double e_ref;        // energy reference of the mixed form (0 for the plain form)
-    // MMS source constants
+    // manufactured-solution source constants
     double src_gm1, src_gM2, src_mu, src_kappa;
 };
 
@@ -77,7 +85,6 @@ struct Geo {
     static constexpr int THREADS = EPB * P3;
 };
 
-// Element-face slot index of side s (1..6) and the face coordinates (a,b) of node (i,j,k).
 __device__ __forceinline__ int64_t slot(int e, int side) { return 6 * static_cast<int64_t>(e) + (side - 1); }
 
 // The FP64 state of node g in the working precision; the energy relative to e_ref (FP64 difference).
@@ -88,259 +95,268 @@ __device__ __forceinline__ void load_state(const Args<R>& a, int64_t g, R* q) {
     q[4] = R(a.Q[5 * g + 4] - a.e_ref);
 }
 
+// Node of line position l through face point (ca, cb) of a side.
+template <int P>
+__device__ __forceinline__ int line_node(int side, int ca, int cb, int l) {
+    switch (side) {
+        case 1: case 2: return ca + P * (l + P * cb);   // FRONT/BACK: (i, k)
+        case 3: case 5: return ca + P * (cb + P * l);   // BOTTOM/TOP: (i, j)
+        default: return l + P * (ca + P * cb);          // RIGHT/LEFT: (j, k)
+    }
+}
+__device__ __forceinline__ bool right_end(int side) { return side == 2 || side == 4 || side == 5; }
+
+// Trace of NV values stored per variable in s (value v of node m at s[v*P3 + m]) at face point
+// (ca,cb) of a side: sum_l v(l) s(line node l) in line order (HexElementClass.f90:233-372); the
+// Gauss-Lobatto end weights are unit vectors, so the end node is picked.
+template <int P, bool GL, int NV, typename R>
+__device__ __forceinline__ void trace(const Ops<R>& ops, const R* s, int side, int ca, int cb, R* out) {
+    constexpr int P3 = P * P * P;
+    if (GL) {
+        const int m = line_node<P>(side, ca, cb, right_end(side) ? P - 1 : 0);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) out[v] = s[v * P3 + m];
+        return;
+    }
+    const R* w = right_end(side) ? ops.vR : ops.vL;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) out[v] = R(0);
+#pragma unroll
+    for (int l = 0; l < P; ++l) {
+        const int m = line_node<P>(side, ca, cb, l);
+        const R wl = w[l];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) out[v] = out[v] + s[v * P3 + m] * wl;
+    }
+}
+
+// Neighbour point of own face point (ca,cb): leftIndexes2Right from side 1, its inverse from side 2.
+template <int P>
+__device__ __forceinline__ int neighbour_point(int map, int ca, int cb) {
+    const int rot = map & 7, side = map >> 3;
+    constexpr int N = P - 1;
+    int ii, jj;
+    if (side == 1) {
+        left2right(ca, cb, N, N, rot, ii, jj);
+    } else {
+        switch (rot) {  // the (i, j) with left2right(i, j) = (ca, cb)
+            case 0: ii = ca; jj = cb; break;
+            case 1: ii = cb; jj = N - ca; break;
+            case 2: ii = N - ca; jj = N - cb; break;
+            case 3: ii = N - cb; jj = ca; break;
+            case 4: ii = cb; jj = ca; break;
+            case 5: ii = N - ca; jj = cb; break;
+            case 6: ii = N - cb; jj = N - ca; break;
+            default: ii = ca; jj = N - cb; break;
+        }
+    }
+    return ii + P * jj;
+}
+
+// Shared memory values (of R) per element of k_volume: state, gradient (later the fluxes), BR1
+// jumps of the six sides, metric vectors (split form only).
+template <int P>
+constexpr int volume_smem_values(bool split) {
+    return (5 + 15) * Geo<P>::P3 + 6 * 15 * Geo<P>::P2 + (split ? 9 * Geo<P>::P3 : 0);
+}
+
 // ------------------------------------------------------------------------------------------------
-// k_prolong_grad: local gradient U_x,U_y,U_z (state gradient variables U = Q) and Q face traces.
+// k_traces: Q face traces of the current state.
 // ------------------------------------------------------------------------------------------------
 template <int P, bool GL, typename R>
-__global__ void __launch_bounds__(Geo<P>::THREADS) k_prolong_grad(Args<R> a) {
+__global__ void __launch_bounds__(Geo<P>::THREADS) k_traces(Args<R> a) {
     constexpr int P2 = Geo<P>::P2, P3 = Geo<P>::P3, EPB = Geo<P>::EPB;
-    __shared__ R sQ[EPB][5][P3];
+    __shared__ R sQ[EPB][5 * P3];
     const int le = threadIdx.x / P3, n = threadIdx.x - le * P3;
     const int e = blockIdx.x * EPB + le;
     const bool active = e < a.K;
-    const int i = n % P, j = (n / P) % P, k = n / P2;
-    const int64_t g = static_cast<int64_t>(e) * P3 + n;
-    R q[5];
     if (active) {
-        load_state(a, g, q);
+        R q[5];
+        load_state(a, static_cast<int64_t>(e) * P3 + n, q);
 #pragma unroll
-        for (int v = 0; v < 5; ++v) sQ[le][v][n] = q[v];
+        for (int v = 0; v < 5; ++v) sQ[le][v * P3 + n] = q[v];
     }
     __syncthreads();
     if (!active) return;
-    const bool ns = a.ph.ns;
-    if (ns) {
-        R uxi[5] = {0, 0, 0, 0, 0}, ueta[5] = {0, 0, 0, 0, 0}, uzeta[5] = {0, 0, 0, 0, 0};
+    for (int t = n; t < 6 * P2; t += P3) {
+        const int side = 1 + t / P2, p = t - (side - 1) * P2;
+        R tq[5];
+        trace<P, GL, 5>(a.ops, sQ[le], side, p % P, p / P, tq);
+        R* d = a.QF + slot(e, side) * 5 * P2 + p;
 #pragma unroll
-        for (int l = 0; l < P; ++l) {
-            const R dx = a.ops.D[i * kMaxP + l], dy = a.ops.D[j * kMaxP + l], dz = a.ops.D[k * kMaxP + l];
-#pragma unroll
-            for (int v = 0; v < 5; ++v) {
-                uxi[v] = uxi[v] + sQ[le][v][l + P * (j + P * k)] * dx;
-                ueta[v] = ueta[v] + sQ[le][v][i + P * (l + P * k)] * dy;
-                uzeta[v] = uzeta[v] + sQ[le][v][i + P * (j + P * l)] * dz;
-            }
-        }
-        const R* jx = a.ja_xi + 3 * g;
-        const R* je = a.ja_eta + 3 * g;
-        const R* jz = a.ja_zeta + 3 * g;
-        const R ij = a.inv_jac[g];
-        const R jx0 = jx[0], jx1 = jx[1], jx2 = jx[2], je0 = je[0], je1 = je[1], je2 = je[2];
-        const R jz0 = jz[0], jz1 = jz[1], jz2 = jz[2];
-#pragma unroll
-        for (int v = 0; v < 5; ++v) {
-            a.Ux[5 * g + v] = (uxi[v] * jx0 + ueta[v] * je0 + uzeta[v] * jz0) * ij;
-            a.Uy[5 * g + v] = (uxi[v] * jx1 + ueta[v] * je1 + uzeta[v] * jz1) * ij;
-            a.Uz[5 * g + v] = (uxi[v] * jx2 + ueta[v] * je2 + uzeta[v] * jz2) * ij;
-        }
-    }
-    // Q face traces, written in each side's own coordinates.
-    if (GL) {
-        auto put = [&](int side, int p) {
-            R* d = a.QF + (slot(e, side) * P2 + p) * 5;
-#pragma unroll
-            for (int v = 0; v < 5; ++v) d[v] = q[v];
-        };
-        if (i == 0) put(6, j + P * k);
-        if (i == P - 1) put(4, j + P * k);
-        if (j == 0) put(1, i + P * k);
-        if (j == P - 1) put(2, i + P * k);
-        if (k == 0) put(3, i + P * j);
-        if (k == P - 1) put(5, i + P * j);
-    } else {
-        for (int t = n; t < 6 * P2; t += P3) {
-            const int side = 1 + t / P2, p = t - (side - 1) * P2;
-            const int ca = p % P, cb = p / P;
-            R acc[5] = {0, 0, 0, 0, 0};
-#pragma unroll
-            for (int l = 0; l < P; ++l) {
-                int idx;
-                R w;
-                switch (side) {
-                    case 1: idx = ca + P * (l + P * cb); w = a.ops.vL[l]; break;   // FRONT (i,k)
-                    case 2: idx = ca + P * (l + P * cb); w = a.ops.vR[l]; break;   // BACK
-                    case 3: idx = ca + P * (cb + P * l); w = a.ops.vL[l]; break;   // BOTTOM (i,j)
-                    case 4: idx = l + P * (ca + P * cb); w = a.ops.vR[l]; break;   // RIGHT (j,k)
-                    case 5: idx = ca + P * (cb + P * l); w = a.ops.vR[l]; break;   // TOP
-                    default: idx = l + P * (ca + P * cb); w = a.ops.vL[l]; break;  // LEFT
-                }
-#pragma unroll
-                for (int v = 0; v < 5; ++v) acc[v] = acc[v] + sQ[le][v][idx] * w;
-            }
-            R* d = a.QF + (slot(e, side) * P2 + p) * 5;
-#pragma unroll
-            for (int v = 0; v < 5; ++v) d[v] = acc[v];
-        }
+        for (int v = 0; v < 5; ++v) d[v * P2] = tq[v];
     }
 }
 
 // ------------------------------------------------------------------------------------------------
-// k_br1_face: uStar_n = 1/2 (UR - UL) Jf n, the same value on both sides (factor +1).
-// ------------------------------------------------------------------------------------------------
-template <int P, typename R>
-__global__ void __launch_bounds__(128) k_br1_face(Args<R> a) {
-    constexpr int P2 = P * P;
-    const int64_t gid = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (gid >= static_cast<int64_t>(a.F) * P2) return;
-    const int f = static_cast<int>(gid / P2), p = static_cast<int>(gid - static_cast<int64_t>(f) * P2);
-    const int i = p % P, j = p / P;
-    int ii, jj;
-    left2right(i, j, P - 1, P - 1, a.face_rot[f], ii, jj);
-    const int pr = ii + P * jj;
-    const int eL = a.face_elem[2 * f], eR = a.face_elem[2 * f + 1];
-    const int64_t sL = slot(eL, a.face_side[2 * f]) * P2 + p;
-    const int64_t sR = slot(eR, a.face_side[2 * f + 1]) * P2 + pr;
-    const R* QL = a.QF + 5 * sL;
-    const R* QR = a.QF + 5 * sR;
-    const int64_t fp = gid;
-    const R J = a.fj[fp];
-    const R n0 = a.fn[3 * fp], n1 = a.fn[3 * fp + 1], n2 = a.fn[3 * fp + 2];
-    R* dL = a.UN + 15 * sL;
-    R* dR = a.UN + 15 * sR;
-#pragma unroll
-    for (int v = 0; v < 5; ++v) {
-        const R u = R(0.5) * (QR[v] - QL[v]) * J;
-        const R x = u * n0, y = u * n1, z = u * n2;
-        dL[v] = x; dL[5 + v] = y; dL[10 + v] = z;
-        dR[v] = x; dR[5 + v] = y; dR[10 + v] = z;
-    }
-}
-
-// ------------------------------------------------------------------------------------------------
-// k_lift_volume: BR1 lifting, gradient traces, viscosity, fluxes and the volume integral -> QDot.
-// store_grad writes the lifted gradient back to Ux/Uy/Uz.
+// k_volume: gradient, BR1 lifting, viscous normal fluxes on the faces, volume integral -> QDot.
 // ------------------------------------------------------------------------------------------------
 template <int P, bool GL, typename R>
-__global__ void __launch_bounds__(Geo<P>::THREADS) k_lift_volume(Args<R> a, int store_grad) {
+__global__ void __launch_bounds__(Geo<P>::THREADS) k_volume(Args<R> a, int store_grad) {
     constexpr int P2 = Geo<P>::P2, P3 = Geo<P>::P3, EPB = Geo<P>::EPB;
-    // Dynamic shared memory, per element: standard form 15*P3 values (gradient for the Gauss traces,
-    // then the contravariant flux); split form 29*P3 values (Q, viscous flux, metric vectors).
+    const bool split = a.inviscid != 0;
+    const bool ns = a.ph.ns;
     extern __shared__ __align__(16) unsigned char dsm[];
-    const int stride = (a.inviscid == 0 ? 15 : 29) * P3;
+    const int stride = volume_smem_values<P>(split);
     const int le = threadIdx.x / P3, n = threadIdx.x - le * P3;
-    R* sF = reinterpret_cast<R*>(dsm) + le * stride;
+    R* sQ = reinterpret_cast<R*>(dsm) + le * stride;  // 5*P3: state
+    R* sG = sQ + 5 * P3;                              // 15*P3: lifted gradient (values v + 5 d)
+    R* sF = sG;                                       // 15*P3: then the contravariant or viscous fluxes
+    R* sU = sG + 15 * P3;                             // 6*15*P2: BR1 jumps uStar n per face point
+    R* sM = sU + 6 * 15 * P2;                         // 9*P3: metric vectors (split form)
     const int e = blockIdx.x * EPB + le;
     const bool active = e < a.K;
     const int i = n % P, j = (n / P) % P, k = n / P2;
     const int64_t g = static_cast<int64_t>(e) * P3 + n;
-    const bool ns = a.ph.ns;
-    R U[3][5];
+
     R q[5];
-    if (active) load_state(a, g, q);
-    if (ns && active) {
+    R jxs[3], jes[3], jzs[3];
+    if (active) {
+        load_state(a, g, q);
 #pragma unroll
-        for (int v = 0; v < 5; ++v) { U[0][v] = a.Ux[5 * g + v]; U[1][v] = a.Uy[5 * g + v]; U[2][v] = a.Uz[5 * g + v]; }
-        // lifting: faceInt = sum over sides of b (x) unStar (VectorWeakIntegrals_StdFace)
-        const R ij = a.inv_jac[g];
-        const R* HL = a.UN + (slot(e, 6) * P2 + (j + P * k)) * 15;
-        const R* HR = a.UN + (slot(e, 4) * P2 + (j + P * k)) * 15;
-        const R* HF = a.UN + (slot(e, 1) * P2 + (i + P * k)) * 15;
-        const R* HB = a.UN + (slot(e, 2) * P2 + (i + P * k)) * 15;
-        const R* HO = a.UN + (slot(e, 3) * P2 + (i + P * j)) * 15;
-        const R* HT = a.UN + (slot(e, 5) * P2 + (i + P * j)) * 15;
-        if (GL) {
-            // b(:,LEFT) and b(:,RIGHT) vanish away from the end nodes: only boundary nodes lift.
-            const R bL = a.ops.bL[0], bR = a.ops.bR[P - 1];
-            const bool iL = i == 0, iR = i == P - 1, jL = j == 0, jR = j == P - 1, kL = k == 0, kR = k == P - 1;
-            if (iL || iR || jL || jR || kL || kR) {
+        for (int v = 0; v < 5; ++v) sQ[v * P3 + n] = q[v];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            jxs[c] = a.ja_xi[3 * g + c];
+            jes[c] = a.ja_eta[3 * g + c];
+            jzs[c] = a.ja_zeta[3 * g + c];
+        }
+    }
+    __syncthreads();
+
+    R U[3][5];
+    if (ns) {
+        if (active) {
+            // local gradient: U_x = (U_xi Ja^xi_x + U_eta Ja^eta_x + U_zeta Ja^zeta_x) / J
+            R uxi[5] = {0, 0, 0, 0, 0}, ueta[5] = {0, 0, 0, 0, 0}, uzeta[5] = {0, 0, 0, 0, 0};
+#pragma unroll
+            for (int l = 0; l < P; ++l) {
+                const R dx = a.ops.D[i * kMaxP + l], dy = a.ops.D[j * kMaxP + l], dz = a.ops.D[k * kMaxP + l];
+#pragma unroll
+                for (int v = 0; v < 5; ++v) {
+                    uxi[v] = uxi[v] + sQ[v * P3 + l + P * (j + P * k)] * dx;
+                    ueta[v] = ueta[v] + sQ[v * P3 + i + P * (l + P * k)] * dy;
+                    uzeta[v] = uzeta[v] + sQ[v * P3 + i + P * (j + P * l)] * dz;
+                }
+            }
+            const R ij = a.inv_jac[g];
+#pragma unroll
+            for (int v = 0; v < 5; ++v) {
+                U[0][v] = (uxi[v] * jxs[0] + ueta[v] * jes[0] + uzeta[v] * jzs[0]) * ij;
+                U[1][v] = (uxi[v] * jxs[1] + ueta[v] * jes[1] + uzeta[v] * jzs[1]) * ij;
+                U[2][v] = (uxi[v] * jxs[2] + ueta[v] * jes[2] + uzeta[v] * jzs[2]) * ij;
+            }
+            // BR1 jumps at the six sides: 1/2 (U_R - U_L) Jf n in the face's orientation (left -> right)
+            for (int t = n; t < 6 * P2; t += P3) {
+                const int side = 1 + t / P2, p = t - (side - 1) * P2;
+                const int ca = p % P, cb = p / P;
+                const int64_t s = slot(e, side);
+                R own[5], nbr[5];
+                trace<P, GL, 5>(a.ops, sQ, side, ca, cb, own);
+                const int map = a.nb_map[s];
+                const int pn = neighbour_point<P>(map, ca, cb);
+                const R* nq = a.QF + static_cast<int64_t>(a.nb_slot[s]) * 5 * P2 + pn;
+#pragma unroll
+                for (int v = 0; v < 5; ++v) nbr[v] = nq[v * P2];
+                const R* sg = a.sgeo + s * 4 * P2 + p;
+                const R n0 = sg[0], n1 = sg[P2], n2 = sg[2 * P2], J = sg[3 * P2];
+                const bool left = (map >> 3) == 1;
+                R* d = sU + (side - 1) * 15 * P2 + p;
+#pragma unroll
+                for (int v = 0; v < 5; ++v) {
+                    const R u = R(0.5) * (left ? (nbr[v] - own[v]) : (own[v] - nbr[v])) * J;
+                    d[v * P2] = u * n0;
+                    d[(5 + v) * P2] = u * n1;
+                    d[(10 + v) * P2] = u * n2;
+                }
+            }
+        }
+        __syncthreads();
+        if (active) {
+            // lifting: U += (sum over sides of b (x) uStar n) / J (VectorWeakIntegrals_StdFace order)
+            const R ij = a.inv_jac[g];
+            const R* HL = sU + 5 * 15 * P2 + (j + P * k);
+            const R* HR = sU + 3 * 15 * P2 + (j + P * k);
+            const R* HF = sU + 0 * 15 * P2 + (i + P * k);
+            const R* HB = sU + 1 * 15 * P2 + (i + P * k);
+            const R* HO = sU + 2 * 15 * P2 + (i + P * j);
+            const R* HT = sU + 4 * 15 * P2 + (i + P * j);
+            if (GL) {  // b(:,LEFT/RIGHT) vanish away from the end nodes
+                const R bl = a.ops.bL[0], br = a.ops.bR[P - 1];
+                const bool iL = i == 0, iR = i == P - 1, jL = j == 0, jR = j == P - 1, kL = k == 0, kR = k == P - 1;
+                if (iL || iR || jL || jR || kL || kR) {
+#pragma unroll
+                    for (int d = 0; d < 3; ++d)
+#pragma unroll
+                        for (int v = 0; v < 5; ++v) {
+                            const int c = (v + 5 * d) * P2;
+                            R fi = R(0);
+                            if (iL) fi = HL[c] * bl;
+                            if (iR) fi = fi + HR[c] * br;
+                            if (jL) fi = fi + HF[c] * bl;
+                            if (jR) fi = fi + HB[c] * br;
+                            if (kL) fi = fi + HO[c] * bl;
+                            if (kR) fi = fi + HT[c] * br;
+                            U[d][v] = U[d][v] + fi * ij;
+                        }
+                }
+            } else {
+                const R bxl = a.ops.bL[i], bxr = a.ops.bR[i], byl = a.ops.bL[j], byr = a.ops.bR[j];
+                const R bzl = a.ops.bL[k], bzr = a.ops.bR[k];
 #pragma unroll
                 for (int d = 0; d < 3; ++d)
 #pragma unroll
                     for (int v = 0; v < 5; ++v) {
-                        const int c = v + 5 * d;
-                        R fi = R(0);
-                        if (iL) fi = HL[c] * bL;
-                        if (iR) fi = fi + HR[c] * bR;
-                        if (jL) fi = fi + HF[c] * bL;
-                        if (jR) fi = fi + HB[c] * bR;
-                        if (kL) fi = fi + HO[c] * bL;
-                        if (kR) fi = fi + HT[c] * bR;
+                        const int c = (v + 5 * d) * P2;
+                        R fi = HL[c] * bxl;
+                        fi = fi + HR[c] * bxr;
+                        fi = fi + HF[c] * byl;
+                        fi = fi + HB[c] * byr;
+                        fi = fi + HO[c] * bzl;
+                        fi = fi + HT[c] * bzr;
                         U[d][v] = U[d][v] + fi * ij;
                     }
             }
-        } else {
-            const R bxl = a.ops.bL[i], bxr = a.ops.bR[i], byl = a.ops.bL[j], byr = a.ops.bR[j];
-            const R bzl = a.ops.bL[k], bzr = a.ops.bR[k];
 #pragma unroll
             for (int d = 0; d < 3; ++d)
+#pragma unroll
+                for (int v = 0; v < 5; ++v) sG[(v + 5 * d) * P3 + n] = U[d][v];
+            if (store_grad) {
 #pragma unroll
                 for (int v = 0; v < 5; ++v) {
-                    const int c = v + 5 * d;
-                    R fi = HL[c] * bxl;
-                    fi = fi + HR[c] * bxr;
-                    fi = fi + HF[c] * byl;
-                    fi = fi + HB[c] * byr;
-                    fi = fi + HO[c] * bzl;
-                    fi = fi + HT[c] * bzr;
-                    U[d][v] = U[d][v] + fi * ij;
+                    a.Ux[5 * g + v] = U[0][v];
+                    a.Uy[5 * g + v] = U[1][v];
+                    a.Uz[5 * g + v] = U[2][v];
                 }
-        }
-        if (store_grad) {
-#pragma unroll
-            for (int v = 0; v < 5; ++v) { a.Ux[5 * g + v] = U[0][v]; a.Uy[5 * g + v] = U[1][v]; a.Uz[5 * g + v] = U[2][v]; }
-        }
-        if (GL) {  // gradient face traces: end nodes copy
-            auto put = [&](int side, int p) {
-                R* d = a.GF + (slot(e, side) * P2 + p) * 15;
-#pragma unroll
-                for (int dd = 0; dd < 3; ++dd)
-#pragma unroll
-                    for (int v = 0; v < 5; ++v) d[v + 5 * dd] = U[dd][v];
-            };
-            if (i == 0) put(6, j + P * k);
-            if (i == P - 1) put(4, j + P * k);
-            if (j == 0) put(1, i + P * k);
-            if (j == P - 1) put(2, i + P * k);
-            if (k == 0) put(3, i + P * j);
-            if (k == P - 1) put(5, i + P * j);
-        }
-    }
-    if (ns && !GL) {  // gradient face traces: contraction with v(:,LEFT/RIGHT)
-        if (active) {
-#pragma unroll
-            for (int d = 0; d < 3; ++d)
-#pragma unroll
-                for (int v = 0; v < 5; ++v) sF[(v + 5 * d) * P3 + n] = U[d][v];
-        }
-        __syncthreads();
-        if (active) {
-            for (int t = n; t < 6 * P2; t += P3) {
-                const int side = 1 + t / P2, p = t - (side - 1) * P2;
-                const int ca = p % P, cb = p / P;
-                R acc[15];
-#pragma unroll
-                for (int c = 0; c < 15; ++c) acc[c] = R(0);
-#pragma unroll
-                for (int l = 0; l < P; ++l) {
-                    int idx;
-                    R w;
-                    switch (side) {
-                        case 1: idx = ca + P * (l + P * cb); w = a.ops.vL[l]; break;
-                        case 2: idx = ca + P * (l + P * cb); w = a.ops.vR[l]; break;
-                        case 3: idx = ca + P * (cb + P * l); w = a.ops.vL[l]; break;
-                        case 4: idx = l + P * (ca + P * cb); w = a.ops.vR[l]; break;
-                        case 5: idx = ca + P * (cb + P * l); w = a.ops.vR[l]; break;
-                        default: idx = l + P * (ca + P * cb); w = a.ops.vL[l]; break;
-                    }
-#pragma unroll
-                    for (int c = 0; c < 15; ++c) acc[c] = acc[c] + sF[c * P3 + idx] * w;
-                }
-                R* d = a.GF + (slot(e, side) * P2 + p) * 15;
-#pragma unroll
-                for (int c = 0; c < 15; ++c) d[c] = acc[c];
             }
         }
         __syncthreads();
+        if (active) {
+            // viscous normal flux of this side at its face points: Fv(Q, grad U, mu(Q)) . n
+            for (int t = n; t < 6 * P2; t += P3) {
+                const int side = 1 + t / P2, p = t - (side - 1) * P2;
+                const int ca = p % P, cb = p / P;
+                const int64_t s = slot(e, side);
+                R tq[5], tg[15];
+                trace<P, GL, 5>(a.ops, sQ, side, ca, cb, tq);
+                trace<P, GL, 15>(a.ops, sG, side, ca, cb, tg);
+                R mu, kap;
+                mu_kappa(a.ph, tq, mu, kap);
+                R C[3][5];
+                viscous_flux(a.ph, tq, tg, tg + 5, tg + 10, mu, kap, C);
+                const R* sg = a.sgeo + s * 4 * P2 + p;
+                const R n0 = sg[0], n1 = sg[P2], n2 = sg[2 * P2];
+                R* d = a.FV + s * 5 * P2 + p;
+#pragma unroll
+                for (int v = 0; v < 5; ++v) d[v * P2] = C[0][v] * n0 + C[1][v] * n1 + C[2][v] * n2;
+            }
+        }
     }
+
+    __syncthreads();  // sG is read above and reused as sF below
     // contravariant fluxes (HyperbolicDiscretizationClass.f90:132-149, EllipticBR1.f90:794-812)
     R Fi[3][5], Fv[3][5];
-    R jxs[3], jes[3], jzs[3];
     if (active) {
-        const R* jx = a.ja_xi + 3 * g;
-        const R* je = a.ja_eta + 3 * g;
-        const R* jz = a.ja_zeta + 3 * g;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) { jxs[c] = jx[c]; jes[c] = je[c]; jzs[c] = jz[c]; }
         euler_contravariant(a.ph, q, jxs, jes, jzs, Fi);
         if (ns) {
             R mu, kappa;
@@ -359,7 +375,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS) k_lift_volume(Args<R> a, int 
                 for (int v = 0; v < 5; ++v) Fv[d][v] = R(0);
         }
     }
-    if (a.inviscid == 0) {
+    if (!split) {
         // ScalarWeakIntegrals_StdVolumeGreen on F = Finv - Fvisc
         if (active) {
 #pragma unroll
@@ -391,19 +407,14 @@ __global__ void __launch_bounds__(Geo<P>::THREADS) k_lift_volume(Args<R> a, int 
 #pragma unroll
         for (int v = 0; v < 5; ++v) a.QDot[5 * g + v] = acc[v];
     } else {
-        // Split form (Gauss-Lobatto only): the two-point flux of each node with every node of its
-        // xi/eta/zeta line (HyperbolicSplitForm.f90:64-116), accumulated as
-        // volInt += sharpD(i,l) f#(l,i) + hatD(i,l) Fv(l) line by line (DGIntegrals.f90:92-129).
-        R* sQ = sF;               // 5*P3
-        R* sV = sF + 5 * P3;      // 15*P3
-        R* sM = sF + 20 * P3;     // 9*P3: Ja^d_c at [(3d+c)*P3]
+        // Split form (Gauss-Lobatto): two-point fluxes of each node with the nodes of its lines
+        // (HyperbolicSplitForm.f90:64-116), accumulated line by line as
+        // volInt += sharpD(i,l) f#(l,i) + hatD(i,l) Fv(l) (DGIntegrals.f90:92-129), QDot = -volInt.
         if (active) {
-#pragma unroll
-            for (int v = 0; v < 5; ++v) sQ[v * P3 + n] = q[v];
 #pragma unroll
             for (int d = 0; d < 3; ++d)
 #pragma unroll
-                for (int v = 0; v < 5; ++v) sV[(v + 5 * d) * P3 + n] = Fv[d][v];
+                for (int v = 0; v < 5; ++v) sF[(v + 5 * d) * P3 + n] = Fv[d][v];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 sM[c * P3 + n] = jxs[c];
@@ -431,14 +442,14 @@ __global__ void __launch_bounds__(Geo<P>::THREADS) k_lift_volume(Args<R> a, int 
                     for (int v = 0; v < 5; ++v) qo[v] = sQ[v * P3 + m];
 #pragma unroll
                     for (int c = 0; c < 3; ++c) jo[c] = sM[(3 * d + c) * P3 + m];
-                    // the reference evaluates each pair once with the lower index as "left"
+                    // each pair is evaluated with the lower line index as "left", as the reference does
                     if (self < l) two_point_flux(a.ph, q, qo, myJ[d], jo, fs);
                     else two_point_flux(a.ph, qo, q, jo, myJ[d], fs);
                 }
-                const R s = a.ops.sharpD[self * kMaxP + l];
+                const R sh = a.ops.sharpD[self * kMaxP + l];
                 const R h = a.ops.hatD[self * kMaxP + l];
 #pragma unroll
-                for (int v = 0; v < 5; ++v) acc[v] = acc[v] + s * fs[v] + h * sV[(v + 5 * d) * P3 + m];
+                for (int v = 0; v < 5; ++v) acc[v] = acc[v] + sh * fs[v] + h * sF[(v + 5 * d) * P3 + m];
             }
         }
 #pragma unroll
@@ -447,127 +458,134 @@ __global__ void __launch_bounds__(Geo<P>::THREADS) k_lift_volume(Args<R> a, int 
 }
 
 // ------------------------------------------------------------------------------------------------
-// k_flux_face: f* = (F_inv(QL,QR) - 1/2 (Fv_L + Fv_R).n) Jf; side 1 gets f*, side 2 gets -f*.
+// k_flux: f* = (F_inv(QL,QR) - 1/2 (Fv_L.n + Fv_R.n)) Jf; side 1 gets f*, side 2 gets -f*.
 // ------------------------------------------------------------------------------------------------
 template <int P, typename R>
-__global__ void __launch_bounds__(128) k_flux_face(Args<R> a) {
+__global__ void __launch_bounds__(128) k_flux(Args<R> a) {
     constexpr int P2 = P * P;
+    const int64_t nfp = static_cast<int64_t>(a.F) * P2;
     const int64_t gid = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (gid >= static_cast<int64_t>(a.F) * P2) return;
+    if (gid >= nfp) return;
     const int f = static_cast<int>(gid / P2), p = static_cast<int>(gid - static_cast<int64_t>(f) * P2);
-    const int i = p % P, j = p / P;
     int ii, jj;
-    left2right(i, j, P - 1, P - 1, a.face_rot[f], ii, jj);
-    const int eL = a.face_elem[2 * f], eR = a.face_elem[2 * f + 1];
-    const int64_t sL = slot(eL, a.face_side[2 * f]) * P2 + p;
-    const int64_t sR = slot(eR, a.face_side[2 * f + 1]) * P2 + ii + P * jj;
+    left2right(p % P, p / P, P - 1, P - 1, a.face_rot[f], ii, jj);
+    const int pr = ii + P * jj;
+    const int64_t bL = slot(a.face_elem[2 * f], a.face_side[2 * f]) * 5 * P2;
+    const int64_t bR = slot(a.face_elem[2 * f + 1], a.face_side[2 * f + 1]) * 5 * P2;
     R QL[5], QR[5];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) { QL[v] = a.QF[5 * sL + v]; QR[v] = a.QF[5 * sR + v]; }
-    const R n[3] = {a.fn[3 * gid], a.fn[3 * gid + 1], a.fn[3 * gid + 2]};
-    const R J = a.fj[gid];
-    R visc[5] = {0, 0, 0, 0, 0};
-    if (a.ph.ns) {
-        R gl[15], gr[15];
-#pragma unroll
-        for (int c = 0; c < 15; ++c) { gl[c] = a.GF[15 * sL + c]; gr[c] = a.GF[15 * sR + c]; }
-        R muL, kL, muR, kR;
-        mu_kappa(a.ph, QL, muL, kL);
-        mu_kappa(a.ph, QR, muR, kR);
-        R fL[3][5], fR[3][5];
-        viscous_flux(a.ph, QL, gl, gl + 5, gl + 10, muL, kL, fL);
-        viscous_flux(a.ph, QR, gr, gr + 5, gr + 10, muR, kR, fR);
-#pragma unroll
-        for (int v = 0; v < 5; ++v) {
-            const R x = R(0.5) * (fL[0][v] + fR[0][v]), y = R(0.5) * (fL[1][v] + fR[1][v]), z = R(0.5) * (fL[2][v] + fR[2][v]);
-            visc[v] = x * n[0] + y * n[1] + z * n[2];
-        }
+    for (int v = 0; v < 5; ++v) {
+        QL[v] = a.QF[bL + v * P2 + p];
+        QR[v] = a.QF[bR + v * P2 + pr];
     }
+    const R n[3] = {a.fn[gid], a.fn[nfp + gid], a.fn[2 * nfp + gid]};
+    const R J = a.fj[gid];
     R inv[5];
     if (a.ph.riemann == 0) {
         roe_flux(a.ph, QL, QR, n, inv);
     } else {
-        const R t1[3] = {a.ft1[3 * gid], a.ft1[3 * gid + 1], a.ft1[3 * gid + 2]};
-        const R t2[3] = {a.ft2[3 * gid], a.ft2[3 * gid + 1], a.ft2[3 * gid + 2]};
+        const R t1[3] = {a.ft1[gid], a.ft1[nfp + gid], a.ft1[2 * nfp + gid]};
+        const R t2[3] = {a.ft2[gid], a.ft2[nfp + gid], a.ft2[2 * nfp + gid]};
         lxf_flux(a.ph, QL, QR, n, t1, t2, inv);
     }
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
-        const R fl = (inv[v] - visc[v]) * J;
-        a.FS[5 * sL + v] = fl;
-        a.FS[5 * sR + v] = -fl;
+        R visc = R(0);
+        if (a.ph.ns) visc = R(0.5) * (a.FV[bL + v * P2 + p] + a.FV[bR + v * P2 + pr]);
+        const R fl = (inv[v] - visc) * J;
+        a.FS[bL + v * P2 + p] = fl;
+        a.FS[bR + v * P2 + pr] = -fl;
     }
 }
 
 // ------------------------------------------------------------------------------------------------
-// k_surface_rk: QDot = (QDot - surface integral)/J + S; then (stage >= 0) the low-storage update
-// G = a_k G + QDot, Q = Q + c_k dt G in FP64.
+// k_update: QDot = (QDot - surface integral)/J + S; stage >= 0 adds the low-storage update
+// G = a_k G + QDot, Q = Q + c_k dt G in FP64 and writes the Q traces of the new state.
+// write_qdot stores the final QDot (residuals, downloads).
 // ------------------------------------------------------------------------------------------------
 template <int P, bool GL, typename R>
-__global__ void __launch_bounds__(Geo<P>::THREADS) k_surface_rk(Args<R> a, int stage, double tshift) {
+__global__ void __launch_bounds__(Geo<P>::THREADS) k_update(Args<R> a, int stage, double tshift, int write_qdot) {
     constexpr int P2 = Geo<P>::P2, P3 = Geo<P>::P3, EPB = Geo<P>::EPB;
+    __shared__ R sQ[EPB][5 * P3];
     const int le = threadIdx.x / P3, n = threadIdx.x - le * P3;
     const int e = blockIdx.x * EPB + le;
-    if (e >= a.K) return;
+    const bool active = e < a.K;
     const int i = n % P, j = (n / P) % P, k = n / P2;
     const int64_t g = static_cast<int64_t>(e) * P3 + n;
-    const R* FL = a.FS + (slot(e, 6) * P2 + (j + P * k)) * 5;
-    const R* FR = a.FS + (slot(e, 4) * P2 + (j + P * k)) * 5;
-    const R* FF = a.FS + (slot(e, 1) * P2 + (i + P * k)) * 5;
-    const R* FB = a.FS + (slot(e, 2) * P2 + (i + P * k)) * 5;
-    const R* FO = a.FS + (slot(e, 3) * P2 + (i + P * j)) * 5;
-    const R* FT = a.FS + (slot(e, 5) * P2 + (i + P * j)) * 5;
-    const R J = a.jac[g];
-    R qd[5];
+    if (active) {
+        const R* FS = a.FS + slot(e, 1) * 5 * P2;  // the six slots of e are contiguous
+        const int pL = j + P * k, pF = i + P * k, pO = i + P * j;
+        const R J = a.jac[g];
+        R qd[5];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) qd[v] = a.QDot[5 * g + v];
-    if (GL) {
-        const R bL = a.ops.bL[0], bR = a.ops.bR[P - 1];
-        const bool iL = i == 0, iR = i == P - 1, jL = j == 0, jR = j == P - 1, kL = k == 0, kR = k == P - 1;
+        for (int v = 0; v < 5; ++v) qd[v] = a.QDot[5 * g + v];
+        if (GL) {
+            const R bl = a.ops.bL[0], br = a.ops.bR[P - 1];
+            const bool iL = i == 0, iR = i == P - 1, jL = j == 0, jR = j == P - 1, kL = k == 0, kR = k == P - 1;
 #pragma unroll
-        for (int v = 0; v < 5; ++v) {
-            R fi = R(0);
-            if (iL) fi = FL[v] * bL;
-            if (iR) fi = fi + FR[v] * bR;
-            if (jL) fi = fi + FF[v] * bL;
-            if (jR) fi = fi + FB[v] * bR;
-            if (kL) fi = fi + FO[v] * bL;
-            if (kR) fi = fi + FT[v] * bR;
-            qd[v] = (qd[v] - fi) / J;
+            for (int v = 0; v < 5; ++v) {
+                R fi = R(0);
+                if (iL) fi = FS[(5 * 5 + v) * P2 + pL] * bl;
+                if (iR) fi = fi + FS[(3 * 5 + v) * P2 + pL] * br;
+                if (jL) fi = fi + FS[(0 * 5 + v) * P2 + pF] * bl;
+                if (jR) fi = fi + FS[(1 * 5 + v) * P2 + pF] * br;
+                if (kL) fi = fi + FS[(2 * 5 + v) * P2 + pO] * bl;
+                if (kR) fi = fi + FS[(4 * 5 + v) * P2 + pO] * br;
+                qd[v] = (qd[v] - fi) / J;
+            }
+        } else {
+            const R bxl = a.ops.bL[i], bxr = a.ops.bR[i], byl = a.ops.bL[j], byr = a.ops.bR[j];
+            const R bzl = a.ops.bL[k], bzr = a.ops.bR[k];
+#pragma unroll
+            for (int v = 0; v < 5; ++v) {
+                R fi = FS[(5 * 5 + v) * P2 + pL] * bxl;
+                fi = fi + FS[(3 * 5 + v) * P2 + pL] * bxr;
+                fi = fi + FS[(0 * 5 + v) * P2 + pF] * byl;
+                fi = fi + FS[(1 * 5 + v) * P2 + pF] * byr;
+                fi = fi + FS[(2 * 5 + v) * P2 + pO] * bzl;
+                fi = fi + FS[(4 * 5 + v) * P2 + pO] * bzr;
+                qd[v] = (qd[v] - fi) / J;
+            }
         }
-    } else {
-        const R bxl = a.ops.bL[i], bxr = a.ops.bR[i], byl = a.ops.bL[j], byr = a.ops.bR[j];
-        const R bzl = a.ops.bL[k], bzr = a.ops.bR[k];
+        const double dt = *a.dt;
+        if (a.source == 1) {
+            double S[5];
+            const double t = *a.time + tshift * dt;
+            mms_source(a.x[3 * g], a.x[3 * g + 1], a.x[3 * g + 2], t, a.src_gm1, a.src_gM2, a.src_mu, a.src_kappa, S);
 #pragma unroll
-        for (int v = 0; v < 5; ++v) {
-            R fi = FL[v] * bxl;
-            fi = fi + FR[v] * bxr;
-            fi = fi + FF[v] * byl;
-            fi = fi + FB[v] * byr;
-            fi = fi + FO[v] * bzl;
-            fi = fi + FT[v] * bzr;
-            qd[v] = (qd[v] - fi) / J;
+            for (int v = 0; v < 5; ++v) qd[v] = R(double(qd[v]) + S[v]);
+        }
+        if (write_qdot) {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) a.QDot[5 * g + v] = qd[v];
+        }
+        if (stage >= 0) {
+            const double ak = stage == 0 ? 0.0 : (stage == 1 ? -5.0 / 9.0 : -153.0 / 128.0);
+            const double ck = stage == 0 ? 1.0 / 3.0 : (stage == 1 ? 15.0 / 16.0 : 8.0 / 15.0);
+            const double cdt = ck * dt;
+            double qn[5];
+#pragma unroll
+            for (int v = 0; v < 5; ++v) {
+                const double gn = ak * a.G[5 * g + v] + double(qd[v]);
+                a.G[5 * g + v] = gn;
+                qn[v] = a.Q[5 * g + v] + cdt * gn;
+                a.Q[5 * g + v] = qn[v];
+            }
+#pragma unroll
+            for (int v = 0; v < 4; ++v) sQ[le][v * P3 + n] = R(qn[v]);
+            sQ[le][4 * P3 + n] = R(qn[4] - a.e_ref);
         }
     }
-    const double dt = *a.dt;
-    if (a.source == 1) {
-        double S[5];
-        const double t = *a.time + tshift * dt;
-        mms_source(a.x[3 * g], a.x[3 * g + 1], a.x[3 * g + 2], t, a.src_gm1, a.src_gM2, a.src_mu, a.src_kappa, S);
-#pragma unroll
-        for (int v = 0; v < 5; ++v) qd[v] = R(double(qd[v]) + S[v]);
-    }
-#pragma unroll
-    for (int v = 0; v < 5; ++v) a.QDot[5 * g + v] = qd[v];
     if (stage < 0) return;
-    const double ak = stage == 0 ? 0.0 : (stage == 1 ? -5.0 / 9.0 : -153.0 / 128.0);
-    const double ck = stage == 0 ? 1.0 / 3.0 : (stage == 1 ? 15.0 / 16.0 : 8.0 / 15.0);
-    const double cdt = ck * dt;
+    __syncthreads();
+    if (!active) return;
+    for (int t = n; t < 6 * P2; t += P3) {  // Q traces of the updated state
+        const int side = 1 + t / P2, p = t - (side - 1) * P2;
+        R tq[5];
+        trace<P, GL, 5>(a.ops, sQ[le], side, p % P, p / P, tq);
+        R* d = a.QF + slot(e, side) * 5 * P2 + p;
 #pragma unroll
-    for (int v = 0; v < 5; ++v) {
-        const double gn = ak * a.G[5 * g + v] + double(qd[v]);
-        a.G[5 * g + v] = gn;
-        a.Q[5 * g + v] = a.Q[5 * g + v] + cdt * gn;
+        for (int v = 0; v < 5; ++v) d[v * P2] = tq[v];
     }
 }
 

@@ -7,38 +7,43 @@
 
 namespace dg {
 
-// One stage of the RHS (stage -1: RHS only; 0..2: RHS + RK3 stage update; kPrepare: set the kernel
-// attributes and launch nothing).
+// One stage of the RHS. stage -1: RHS only; 0..2: RHS + RK3 stage update (+ traces of the new
+// state); kTraces: Q traces of the current state only; kPrepare: set kernel attributes, no launch.
+// flags: kStoreGrad writes the lifted gradient, kWriteQDot stores the final QDot.
 constexpr int kPrepare = -2;
-template <typename R>
-using StageFn = cudaError_t (*)(const Args<R>& a, int stage, double tshift, int store_grad, cudaStream_t s);
+constexpr int kTraces = -3;
+constexpr int kStoreGrad = 1;
+constexpr int kWriteQDot = 2;
 
-template <int P, bool GL, typename R>
-size_t lift_smem_bytes(int inviscid) {
-    return static_cast<size_t>(Geo<P>::EPB) * (inviscid == 0 ? 15 : 29) * Geo<P>::P3 * sizeof(R);
+template <typename R>
+using StageFn = cudaError_t (*)(const Args<R>& a, int stage, double tshift, int flags, cudaStream_t s);
+
+template <int P, typename R>
+size_t volume_smem_bytes(int inviscid) {
+    return static_cast<size_t>(Geo<P>::EPB) * volume_smem_values<P>(inviscid != 0) * sizeof(R);
 }
 
 template <int P, bool GL, typename R>
-cudaError_t run_stage(const Args<R>& a, int stage, double tshift, int store_grad, cudaStream_t s) {
+cudaError_t run_stage(const Args<R>& a, int stage, double tshift, int flags, cudaStream_t s) {
     constexpr int EPB = Geo<P>::EPB, THREADS = Geo<P>::THREADS;
     const int eblocks = (a.K + EPB - 1) / EPB;
     const long long fp = static_cast<long long>(a.F) * P * P;
     const int fblocks = static_cast<int>((fp + 127) / 128);
-    const size_t smem = lift_smem_bytes<P, GL, R>(a.inviscid);
     if (stage == kPrepare)  // opt in to the large dynamic shared memory once, outside any capture
-        return cudaFuncSetAttribute(k_lift_volume<P, GL, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    static_cast<int>(lift_smem_bytes<P, GL, R>(1)));
-    k_prolong_grad<P, GL, R><<<eblocks, THREADS, 0, s>>>(a);
-    if (a.ph.ns) k_br1_face<P, R><<<fblocks, 128, 0, s>>>(a);
-    k_lift_volume<P, GL, R><<<eblocks, THREADS, smem, s>>>(a, store_grad);
-    k_flux_face<P, R><<<fblocks, 128, 0, s>>>(a);
-    k_surface_rk<P, GL, R><<<eblocks, THREADS, 0, s>>>(a, stage, tshift);
+        return cudaFuncSetAttribute(k_volume<P, GL, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(volume_smem_bytes<P, R>(1)));
+    if (stage == kTraces) {
+        k_traces<P, GL, R><<<eblocks, THREADS, 0, s>>>(a);
+        return cudaGetLastError();
+    }
+    k_volume<P, GL, R><<<eblocks, THREADS, volume_smem_bytes<P, R>(a.inviscid), s>>>(a, flags & kStoreGrad);
+    k_flux<P, R><<<fblocks, 128, 0, s>>>(a);
+    k_update<P, GL, R><<<eblocks, THREADS, 0, s>>>(a, stage, tshift, (flags & kWriteQDot) ? 1 : 0);
     return cudaGetLastError();
 }
 
-// Average device time of each stage kernel alone, measured with CUDA events on stream s over reps
-// launches (k_surface_rk runs its RK stage-1 update). ms[0..4]: prolong_grad, br1_face, lift_volume,
-// flux_face, surface_rk (br1_face is 0 in Euler mode).
+// Average device time of each kernel alone, measured with CUDA events on stream s over reps
+// launches (k_update runs its RK stage-1 update). ms[0..3]: volume, flux, update, traces.
 template <typename R>
 using KernelTimesFn = cudaError_t (*)(const Args<R>& a, int reps, cudaStream_t s, double* ms);
 
@@ -48,22 +53,21 @@ cudaError_t kernel_times(const Args<R>& a, int reps, cudaStream_t s, double* ms)
     const int eblocks = (a.K + EPB - 1) / EPB;
     const long long fp = static_cast<long long>(a.F) * P * P;
     const int fblocks = static_cast<int>((fp + 127) / 128);
-    const size_t smem = lift_smem_bytes<P, GL, R>(a.inviscid);
     cudaEvent_t e0, e1;
     cudaError_t err = cudaEventCreate(&e0);
     if (err != cudaSuccess) return err;
-    if ((err = cudaEventCreate(&e1)) != cudaSuccess) { cudaEventDestroy(e0); return err; }
-    for (int kk = 0; kk < 5; ++kk) {
-        ms[kk] = 0.0;
-        if (kk == 1 && !a.ph.ns) continue;
+    if ((err = cudaEventCreate(&e1)) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return err;
+    }
+    for (int kk = 0; kk < 4; ++kk) {
         cudaEventRecord(e0, s);
         for (int r = 0; r < reps; ++r) {
             switch (kk) {
-                case 0: k_prolong_grad<P, GL, R><<<eblocks, THREADS, 0, s>>>(a); break;
-                case 1: k_br1_face<P, R><<<fblocks, 128, 0, s>>>(a); break;
-                case 2: k_lift_volume<P, GL, R><<<eblocks, THREADS, smem, s>>>(a, 0); break;
-                case 3: k_flux_face<P, R><<<fblocks, 128, 0, s>>>(a); break;
-                default: k_surface_rk<P, GL, R><<<eblocks, THREADS, 0, s>>>(a, 1, 1.0 / 3.0); break;
+                case 0: k_volume<P, GL, R><<<eblocks, THREADS, volume_smem_bytes<P, R>(a.inviscid), s>>>(a, 0); break;
+                case 1: k_flux<P, R><<<fblocks, 128, 0, s>>>(a); break;
+                case 2: k_update<P, GL, R><<<eblocks, THREADS, 0, s>>>(a, 1, 1.0 / 3.0, 0); break;
+                default: k_traces<P, GL, R><<<eblocks, THREADS, 0, s>>>(a); break;
             }
         }
         cudaEventRecord(e1, s);

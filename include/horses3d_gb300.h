@@ -134,9 +134,10 @@ int dg_run_steps(dg_ctx* ctx, int n, double t0, double dt, double cfl, double dc
  * launches; *ms receives the elapsed device time. Measurement helper, no reference counterpart. */
 int dg_time_steps(dg_ctx* ctx, int n, double t0, double dt, double cfl, double dcfl, double* ms);
 
-/* Average device time (ms) of each of the five stage kernels launched alone reps times on the
- * context's stream: prolong+gradient, BR1 face jump, lift+volume, face flux, surface+RK update.
- * Advances Q by reps RK stage-1 updates of size dt. Measurement helper, no reference counterpart. */
+/* Average device time (ms) of each kernel launched alone reps times on the context's stream:
+ * ms[0] volume (gradient, BR1 lifting, volume integral), ms[1] face flux, ms[2] surface integral +
+ * RK update + traces, ms[3] traces alone, ms[4] unused (0). Advances Q by reps RK stage-1 updates
+ * of size dt. Measurement helper, no reference counterpart. */
 int dg_kernel_times(dg_ctx* ctx, int reps, double t0, double dt, double ms[5]);
 
 /* MaxTimeStep (DGSEMClass.f90:870-1038) on the device. */
