@@ -85,6 +85,17 @@ struct Geo {
     static constexpr int THREADS = EPB * P3;
 };
 
+// Minimum resident blocks per SM requested from the register allocator: the kernels are latency
+// bound at one element per block, so occupancy is bought with a register budget per thread.
+template <int P, typename R>
+struct Occupancy {
+    static constexpr int blocks(int regs) {
+        return (65536 / (Geo<P>::THREADS * regs)) > 0 ? (65536 / (Geo<P>::THREADS * regs)) : 1;
+    }
+    static constexpr int volume = blocks(sizeof(R) == 4 ? 96 : 168);
+    static constexpr int update = blocks(sizeof(R) == 4 ? 64 : 96);
+};
+
 __device__ __forceinline__ int64_t slot(int e, int side) { return 6 * static_cast<int64_t>(e) + (side - 1); }
 
 // The FP64 state of node g in the working precision; the energy relative to e_ref (FP64 difference).
@@ -192,7 +203,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS) k_traces(Args<R> a) {
 // k_volume: gradient, BR1 lifting, viscous normal fluxes on the faces, volume integral -> QDot.
 // ------------------------------------------------------------------------------------------------
 template <int P, bool GL, typename R>
-__global__ void __launch_bounds__(Geo<P>::THREADS) k_volume(Args<R> a, int store_grad) {
+__global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_volume(Args<R> a, int store_grad) {
     constexpr int P2 = Geo<P>::P2, P3 = Geo<P>::P3, EPB = Geo<P>::EPB;
     const bool split = a.inviscid != 0;
     const bool ns = a.ph.ns;
@@ -354,15 +365,19 @@ __global__ void __launch_bounds__(Geo<P>::THREADS) k_volume(Args<R> a, int store
     }
 
     __syncthreads();  // sG is read above and reused as sF below
-    // contravariant fluxes (HyperbolicDiscretizationClass.f90:132-149, EllipticBR1.f90:794-812)
+    // contravariant fluxes (HyperbolicDiscretizationClass.f90:132-149, EllipticBR1.f90:794-812);
+    // the lifted gradient is read back from this node's own column of sG
     R Fi[3][5], Fv[3][5];
     if (active) {
         euler_contravariant(a.ph, q, jxs, jes, jzs, Fi);
         if (ns) {
+            R Ug[15];
+#pragma unroll
+            for (int c = 0; c < 15; ++c) Ug[c] = sG[c * P3 + n];
             R mu, kappa;
             mu_kappa(a.ph, q, mu, kappa);
             R C[3][5];
-            viscous_flux(a.ph, q, U[0], U[1], U[2], mu, kappa, C);
+            viscous_flux(a.ph, q, Ug, Ug + 5, Ug + 10, mu, kappa, C);
             const R* ja[3] = {jxs, jes, jzs};
 #pragma unroll
             for (int d = 0; d < 3; ++d)
@@ -503,8 +518,9 @@ __global__ void __launch_bounds__(128) k_flux(Args<R> a) {
 // G = a_k G + QDot, Q = Q + c_k dt G in FP64 and writes the Q traces of the new state.
 // write_qdot stores the final QDot (residuals, downloads).
 // ------------------------------------------------------------------------------------------------
-template <int P, bool GL, typename R>
-__global__ void __launch_bounds__(Geo<P>::THREADS) k_update(Args<R> a, int stage, double tshift, int write_qdot) {
+template <int P, bool GL, bool SRC, typename R>
+__global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
+    k_update(Args<R> a, int stage, double tshift, int write_qdot) {
     constexpr int P2 = Geo<P>::P2, P3 = Geo<P>::P3, EPB = Geo<P>::EPB;
     __shared__ R sQ[EPB][5 * P3];
     const int le = threadIdx.x / P3, n = threadIdx.x - le * P3;
@@ -548,7 +564,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS) k_update(Args<R> a, int stage
             }
         }
         const double dt = *a.dt;
-        if (a.source == 1) {
+        if (SRC) {
             double S[5];
             const double t = *a.time + tshift * dt;
             mms_source(a.x[3 * g], a.x[3 * g + 1], a.x[3 * g + 2], t, a.src_gm1, a.src_gM2, a.src_mu, a.src_kappa, S);

@@ -38,7 +38,8 @@ cudaError_t run_stage(const Args<R>& a, int stage, double tshift, int flags, cud
     }
     k_volume<P, GL, R><<<eblocks, THREADS, volume_smem_bytes<P, R>(a.inviscid), s>>>(a, flags & kStoreGrad);
     k_flux<P, R><<<fblocks, 128, 0, s>>>(a);
-    k_update<P, GL, R><<<eblocks, THREADS, 0, s>>>(a, stage, tshift, (flags & kWriteQDot) ? 1 : 0);
+    if (a.source) k_update<P, GL, true, R><<<eblocks, THREADS, 0, s>>>(a, stage, tshift, (flags & kWriteQDot) ? 1 : 0);
+    else k_update<P, GL, false, R><<<eblocks, THREADS, 0, s>>>(a, stage, tshift, (flags & kWriteQDot) ? 1 : 0);
     return cudaGetLastError();
 }
 
@@ -66,7 +67,7 @@ cudaError_t kernel_times(const Args<R>& a, int reps, cudaStream_t s, double* ms)
             switch (kk) {
                 case 0: k_volume<P, GL, R><<<eblocks, THREADS, volume_smem_bytes<P, R>(a.inviscid), s>>>(a, 0); break;
                 case 1: k_flux<P, R><<<fblocks, 128, 0, s>>>(a); break;
-                case 2: k_update<P, GL, R><<<eblocks, THREADS, 0, s>>>(a, 1, 1.0 / 3.0, 0); break;
+                case 2: k_update<P, GL, false, R><<<eblocks, THREADS, 0, s>>>(a, 1, 1.0 / 3.0, 0); break;
                 default: k_traces<P, GL, R><<<eblocks, THREADS, 0, s>>>(a); break;
             }
         }
