@@ -15,6 +15,7 @@
 #include <cstdint>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <vector>
 
 #include "horses3d_gb300.h"
@@ -122,8 +123,12 @@ struct Nodal {  // NodalStorageClass.f90:170-338 (the parts the right-hand side 
     int N;
     std::vector<double> x, w, D, hatD, sharpD, vL, vR, bL, bR;
 };
+// Cached per (nodes, N). Called from OpenMP regions: the lookup is serialised (map nodes are stable,
+// so the returned reference stays valid); orc_create fills the cache before any parallel region.
 static const Nodal& nodal(int nodes, int N) {
     static std::map<std::pair<int, int>, Nodal> cache;
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
     auto key = std::make_pair(nodes, N);
     auto it = cache.find(key);
     if (it != cache.end()) return it->second;
@@ -981,6 +986,10 @@ void* orc_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* 
         F.off = foff;
         foff += static_cast<int64_t>(F.Nf[0] + 1) * (F.Nf[1] + 1);
     }
+    for (const auto& E : s->el)
+        for (int d = 0; d < 3; ++d) orc::nodal(s->nodes, E.N[d]);
+    for (const auto& F : s->fa)
+        for (int d = 0; d < 2; ++d) orc::nodal(s->nodes, F.Nf[d]);
     s->fn = cp(m->face_normal, 3 * foff); s->ft1 = cp(m->face_t1, 3 * foff); s->ft2 = cp(m->face_t2, 3 * foff);
     s->fj = cp(m->face_jacobian, foff);
     s->Q.assign(5 * off, 0.0); s->QDot.assign(5 * off, 0.0); s->G.assign(5 * off, 0.0);
