@@ -96,6 +96,9 @@ SIGNATURES = [
     ("dg_time_steps", C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, _f64p]),
     ("dg_kernel_times", C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, _f64p]),
     ("dg_max_dt", C.c_int, [C.c_void_p, C.c_double, C.c_double, _f64p]),
+    ("dg_max_dt_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int,
+                                    C.c_int, C.POINTER(DgPhysics), C.c_double, C.c_double, C.c_void_p, _f64p]),
+    ("dg_max_dt_noalloc_max_dof", C.c_int64, []),
     ("dg_residuals", C.c_int, [C.c_void_p, _f64p, C.POINTER(C.c_int)]),
     ("dg_synchronize", C.c_int, [C.c_void_p]),
     ("h3d_mesh_read_specmesh", C.c_int, [C.c_char_p, C.c_int, C.c_int, _i32p, C.c_char_p, C.POINTER(C.c_void_p)]),

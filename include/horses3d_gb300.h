@@ -143,6 +143,21 @@ int dg_kernel_times(dg_ctx* ctx, int reps, double t0, double dt, double ms[5]);
 /* MaxTimeStep (DGSEMClass.f90:870-1038) on the device. */
 int dg_max_dt(dg_ctx* ctx, double cfl, double dcfl, double* dt);
 
+/* MaxTimeStep without any device allocation, for callers that cannot call cudaMalloc (a host that
+ * owns all device memory through its own pool, or code running after an allocation freeze). No
+ * counterpart in the reference. The caller passes device pointers in the reference layouts:
+ * q (5*ndof), ja_xi/ja_eta/ja_zeta (3*ndof), jacobian (ndof), for uniform order `order`. The only
+ * scratch is a fixed 128 KiB file-scope device array that every GPU loading the library keeps until
+ * exit; it bounds ndof to dg_max_dt_noalloc_max_dof() (67,108,864) and larger sizes are rejected
+ * with DG_ERR_INVALID. The first call on a device looks up that array's address (make it before any
+ * stream capture). Every call reuses the array, so calls that overlap on the GPU (other streams or
+ * threads) race; each call overwrites the entries it reads. stream may be NULL (default stream);
+ * the call synchronises it and writes dt to host memory. */
+int dg_max_dt_noalloc(const double* q, const double* ja_xi, const double* ja_eta, const double* ja_zeta,
+                      const double* jacobian, int64_t ndof, int order, int node_type, const dg_physics* phys,
+                      double cfl, double dcfl, void* stream, double* dt);
+int64_t dg_max_dt_noalloc_max_dof(void);
+
 /* ComputeMaxResiduals: max|QDot| per conserved variable; *nan_found = 1 if Q holds NaN/Inf. */
 int dg_residuals(dg_ctx* ctx, double maxres[5], int* nan_found);
 
