@@ -47,12 +47,18 @@ def _stale(target: Path, deps) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
+# The FP32 (mixed-form) kernels use the fast single-precision division/sqrt and flush denormals;
+# the FP64 translation units keep IEEE arithmetic.
+FAST_FP32_UNITS = {"dg_inst_fp32.cu"}
+
+
 def _compile(src: Path) -> Path:
     out = OBJ / (src.stem + (".cu.o" if src.suffix == ".cu" else ".o"))
-    if not _stale(out, _deps(src)):
+    if not _stale(out, _deps(src) + [Path(__file__)]):
         return out
     if src.suffix == ".cu":
-        cmd = [_nvcc(), *NVCCFLAGS, "-c", str(src), "-o", str(out)]
+        extra = ["--use_fast_math"] if src.name in FAST_FP32_UNITS else []
+        cmd = [_nvcc(), *NVCCFLAGS, *extra, "-c", str(src), "-o", str(out)]
     else:
         cmd = [os.environ.get("CXX", "g++"), *CXXFLAGS, "-c", str(src), "-o", str(out)]
     res = subprocess.run(cmd, capture_output=True, text=True)

@@ -92,7 +92,7 @@ struct Occupancy {
     static constexpr int blocks(int regs) {
         return (65536 / (Geo<P>::THREADS * regs)) > 0 ? (65536 / (Geo<P>::THREADS * regs)) : 1;
     }
-    static constexpr int volume = blocks(sizeof(R) == 4 ? 96 : 168);
+    static constexpr int volume = blocks(sizeof(R) == 4 ? 72 : 168);
     static constexpr int update = blocks(sizeof(R) == 4 ? 64 : 96);
 };
 
@@ -531,22 +531,38 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
     if (active) {
         const R* FS = a.FS + slot(e, 1) * 5 * P2;  // the six slots of e are contiguous
         const int pL = j + P * k, pF = i + P * k, pO = i + P * j;
-        const R J = a.jac[g];
-        R qd[5];
+        // every load of the node up front (QDot, J, the six surface fluxes, G and Q), then the math
+        R qd[5], fs[6][5];
+        double gq[5], qq[5];
 #pragma unroll
         for (int v = 0; v < 5; ++v) qd[v] = a.QDot[5 * g + v];
+        const R J = a.jac[g];
+        const bool use[6] = {GL ? j == 0 : true, GL ? j == P - 1 : true, GL ? k == 0 : true,
+                             GL ? i == P - 1 : true, GL ? k == P - 1 : true, GL ? i == 0 : true};
+        const int pt[6] = {pF, pF, pO, pL, pO, pL};
+#pragma unroll
+        for (int sd = 0; sd < 6; ++sd)
+#pragma unroll
+            for (int v = 0; v < 5; ++v) fs[sd][v] = use[sd] ? FS[(sd * 5 + v) * P2 + pt[sd]] : R(0);
+        if (stage >= 0) {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) {
+                gq[v] = a.G[5 * g + v];
+                qq[v] = a.Q[5 * g + v];
+            }
+        }
+        // surface integral in the reference's order: left, right, front, back, bottom, top
         if (GL) {
             const R bl = a.ops.bL[0], br = a.ops.bR[P - 1];
-            const bool iL = i == 0, iR = i == P - 1, jL = j == 0, jR = j == P - 1, kL = k == 0, kR = k == P - 1;
 #pragma unroll
             for (int v = 0; v < 5; ++v) {
                 R fi = R(0);
-                if (iL) fi = FS[(5 * 5 + v) * P2 + pL] * bl;
-                if (iR) fi = fi + FS[(3 * 5 + v) * P2 + pL] * br;
-                if (jL) fi = fi + FS[(0 * 5 + v) * P2 + pF] * bl;
-                if (jR) fi = fi + FS[(1 * 5 + v) * P2 + pF] * br;
-                if (kL) fi = fi + FS[(2 * 5 + v) * P2 + pO] * bl;
-                if (kR) fi = fi + FS[(4 * 5 + v) * P2 + pO] * br;
+                if (use[5]) fi = fs[5][v] * bl;
+                if (use[3]) fi = fi + fs[3][v] * br;
+                if (use[0]) fi = fi + fs[0][v] * bl;
+                if (use[1]) fi = fi + fs[1][v] * br;
+                if (use[2]) fi = fi + fs[2][v] * bl;
+                if (use[4]) fi = fi + fs[4][v] * br;
                 qd[v] = (qd[v] - fi) / J;
             }
         } else {
@@ -554,12 +570,12 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
             const R bzl = a.ops.bL[k], bzr = a.ops.bR[k];
 #pragma unroll
             for (int v = 0; v < 5; ++v) {
-                R fi = FS[(5 * 5 + v) * P2 + pL] * bxl;
-                fi = fi + FS[(3 * 5 + v) * P2 + pL] * bxr;
-                fi = fi + FS[(0 * 5 + v) * P2 + pF] * byl;
-                fi = fi + FS[(1 * 5 + v) * P2 + pF] * byr;
-                fi = fi + FS[(2 * 5 + v) * P2 + pO] * bzl;
-                fi = fi + FS[(4 * 5 + v) * P2 + pO] * bzr;
+                R fi = fs[5][v] * bxl;
+                fi = fi + fs[3][v] * bxr;
+                fi = fi + fs[0][v] * byl;
+                fi = fi + fs[1][v] * byr;
+                fi = fi + fs[2][v] * bzl;
+                fi = fi + fs[4][v] * bzr;
                 qd[v] = (qd[v] - fi) / J;
             }
         }
@@ -579,17 +595,19 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
             const double ak = stage == 0 ? 0.0 : (stage == 1 ? -5.0 / 9.0 : -153.0 / 128.0);
             const double ck = stage == 0 ? 1.0 / 3.0 : (stage == 1 ? 15.0 / 16.0 : 8.0 / 15.0);
             const double cdt = ck * dt;
-            double qn[5];
 #pragma unroll
             for (int v = 0; v < 5; ++v) {
-                const double gn = ak * a.G[5 * g + v] + double(qd[v]);
-                a.G[5 * g + v] = gn;
-                qn[v] = a.Q[5 * g + v] + cdt * gn;
-                a.Q[5 * g + v] = qn[v];
+                gq[v] = ak * gq[v] + double(qd[v]);
+                qq[v] = qq[v] + cdt * gq[v];
             }
 #pragma unroll
-            for (int v = 0; v < 4; ++v) sQ[le][v * P3 + n] = R(qn[v]);
-            sQ[le][4 * P3 + n] = R(qn[4] - a.e_ref);
+            for (int v = 0; v < 5; ++v) {
+                a.G[5 * g + v] = gq[v];
+                a.Q[5 * g + v] = qq[v];
+            }
+#pragma unroll
+            for (int v = 0; v < 4; ++v) sQ[le][v * P3 + n] = R(qq[v]);
+            sQ[le][4 * P3 + n] = R(qq[4] - a.e_ref);
         }
     }
     if (stage < 0) return;
