@@ -132,6 +132,11 @@ def build_case(n_elem: int = N_ELEM):
     return mesh, q0, base
 
 
+# DRAM bytes per DOF of one k_volume<6, gauss, float> launch, measured with ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum = 443.65 MB over 2,985,984 DOF, 24^3 elements, N=5).
+VOLUME_DRAM_BYTES_PER_DOF = 148.6
+
+
 def volume_bytes(P: int, word: int) -> float:
     """Algorithmic bytes per DOF of k_volume (NS): reads Q (5 FP64), Ja (9) and 1/J (1), and per face
     point of its six sides (6 P^2 / P^3 = 6/P per DOF) the neighbour's Q trace (5) and the side
@@ -190,9 +195,12 @@ def run_gpu_arm(args, rank, world, local, case):
     hbm, peak_kind = _peaks()
     alg = volume_bytes(P, 4) * ndof
     achieved = alg / (kt[0] * 1e-3) / 1e9
+    traffic = VOLUME_DRAM_BYTES_PER_DOF * ndof if P == 6 else None
     roofline = {"bound": "hbm", "kernel": "k_volume<6,gauss,float>", "achieved": round(achieved, 1),
                 "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / hbm, 4),
-                "traffic": None, "alg_bytes_per_launch": alg}
+                "traffic": traffic, "alg_bytes_per_launch": alg,
+                "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_volume launch on the "
+                                "24^3-element case (148.6 B/DOF), scaled by the DOF count"}
 
     # e2e through the C ABI with host buffers (IntegrateInTime-shaped loop)
     import torch
@@ -261,7 +269,7 @@ def cpu_oracle_rate(case, steps: int = 1):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -168,7 +168,7 @@ __device__ __forceinline__ int neighbour_point(int map, int ca, int cb) {
 // jumps of the six sides, metric vectors (split form only).
 template <int P>
 constexpr int volume_smem_values(bool split) {
-    return (5 + 15) * Geo<P>::P3 + 6 * 15 * Geo<P>::P2 + (split ? 9 * Geo<P>::P3 : 0);
+    return (5 + 15) * Geo<P>::P3 + 6 * (15 + 5) * Geo<P>::P2 + (split ? 9 * Geo<P>::P3 : 0);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -214,7 +214,8 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
     R* sG = sQ + 5 * P3;                              // 15*P3: lifted gradient (values v + 5 d)
     R* sF = sG;                                       // 15*P3: then the contravariant or viscous fluxes
     R* sU = sG + 15 * P3;                             // 6*15*P2: BR1 jumps uStar n per face point
-    R* sM = sU + 6 * 15 * P2;                         // 9*P3: metric vectors (split form)
+    R* sT = sU + 6 * 15 * P2;                         // 6*5*P2: own Q traces, reused for the viscous fluxes
+    R* sM = sT + 6 * 5 * P2;                          // 9*P3: metric vectors (split form)
     const int e = blockIdx.x * EPB + le;
     const bool active = e < a.K;
     const int i = n % P, j = (n / P) % P, k = n / P2;
@@ -264,6 +265,8 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
                 const int64_t s = slot(e, side);
                 R own[5], nbr[5];
                 trace<P, GL, 5>(a.ops, sQ, side, ca, cb, own);
+#pragma unroll
+                for (int v = 0; v < 5; ++v) sT[((side - 1) * 5 + v) * P2 + p] = own[v];
                 const int map = a.nb_map[s];
                 const int pn = neighbour_point<P>(map, ca, cb);
                 const R* nq = a.QF + static_cast<int64_t>(a.nb_slot[s]) * 5 * P2 + pn;
@@ -349,7 +352,8 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
                 const int ca = p % P, cb = p / P;
                 const int64_t s = slot(e, side);
                 R tq[5], tg[15];
-                trace<P, GL, 5>(a.ops, sQ, side, ca, cb, tq);
+#pragma unroll
+                for (int v = 0; v < 5; ++v) tq[v] = sT[((side - 1) * 5 + v) * P2 + p];
                 trace<P, GL, 15>(a.ops, sG, side, ca, cb, tg);
                 R mu, kap;
                 mu_kappa(a.ph, tq, mu, kap);
