@@ -101,6 +101,15 @@ SIGNATURES = [
     ("dg_max_dt_noalloc_max_dof", C.c_int64, []),
     ("dg_residuals", C.c_int, [C.c_void_p, _f64p, C.POINTER(C.c_int)]),
     ("dg_synchronize", C.c_int, [C.c_void_p]),
+    ("dg_create_batch", C.c_int, [C.c_int, C.POINTER(DgMeshDesc), C.POINTER(DgPhysics), C.POINTER(DgOptions),
+                                  C.POINTER(C.c_void_p)]),
+    ("dg_batch_size", C.c_int, [C.c_void_p]),
+    ("dg_case_offset", C.c_int64, [C.c_void_p, C.c_int]),
+    ("dg_batch_set_clock", C.c_int, [C.c_void_p, _f64p, _f64p]),
+    ("dg_batch_get_clock", C.c_int, [C.c_void_p, _f64p, _f64p]),
+    ("dg_batch_max_dt", C.c_int, [C.c_void_p, C.c_double, C.c_double, _f64p]),
+    ("dg_batch_residuals", C.c_int, [C.c_void_p, _f64p, C.POINTER(C.c_int)]),
+    ("dg_batch_run_steps", C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, _f64p]),
     ("h3d_mesh_read_specmesh", C.c_int, [C.c_char_p, C.c_int, C.c_int, _i32p, C.c_char_p, C.POINTER(C.c_void_p)]),
     ("h3d_mesh_box", C.c_int, [C.c_int, C.c_int, C.c_int, _f64p, _f64p, C.c_double, C.c_int, C.c_int, C.c_int,
                                _i32p, C.POINTER(C.c_void_p)]),

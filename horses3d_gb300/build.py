@@ -49,7 +49,7 @@ def _stale(target: Path, deps) -> bool:
 
 # The FP32 (mixed-form) kernels use the fast single-precision division/sqrt and flush denormals;
 # the FP64 translation units keep IEEE arithmetic.
-FAST_FP32_UNITS = {"dg_inst_fp32.cu"}
+FAST_FP32_UNITS = {"dg_inst_fp32.cu", "dg_var_fp32.cu"}
 
 
 def _compile(src: Path) -> Path:

@@ -13,6 +13,8 @@ from __future__ import annotations
 from dataclasses import dataclass, field
 from pathlib import Path
 
+import numpy as np
+
 from . import _abi
 
 
@@ -41,6 +43,17 @@ class Config:
     n_steps: int = 1
     t_final: float | None = None
     periodic: list = field(default_factory=list)
+    order_file: str | None = None
+
+    def element_orders(self, base_dir=None):
+        """(Nx, Ny, Nz) per element from "polynomial order file" (ReadInputFile.f90:132-153: the element
+        count, then one "Nx Ny Nz" line per element), else the scalar or (i, j, k) order."""
+        if self.order_file is None:
+            return self.order
+        path = Path(self.order_file)
+        if base_dir is not None and not path.is_absolute():
+            path = Path(base_dir) / path
+        return read_order_file(path)
 
     def physics(self) -> _abi.DgPhysics:
         return _abi.DgPhysics(self.mach, self.reynolds, self.prandtl, 1 if self.flow == "ns" else 0)
@@ -95,11 +108,15 @@ def parse_control(text: str) -> Config:
         return keys.get(k, default)
 
     cfg.mesh_file = get("mesh file name")
-    if "polynomial order" in keys:
+    # pAdaptationClass.f90:218-239: an order file wins over "polynomial order", which wins over i/j/k
+    if "polynomial order file" in keys:
+        cfg.order_file = keys["polynomial order file"]
+    elif "polynomial order" in keys:
         cfg.order = int(float(keys["polynomial order"]))
-    for k in ("polynomial order i", "polynomial order j", "polynomial order k", "polynomial order file"):
-        if k in keys:
-            raise UnsupportedOption(f"'{k}': the GPU path needs one isotropic polynomial order")
+    elif all(f"polynomial order {a}" in keys for a in "ijk"):
+        cfg.order = tuple(int(float(keys[f"polynomial order {a}"])) for a in "ijk")
+    elif any(f"polynomial order {a}" in keys for a in "ijk"):
+        raise ValueError("The polynomial order(s) must be specified")
     nodes = (get("discretization nodes", "gauss") or "gauss").lower()
     cfg.nodes = _abi.DG_NODES_GAUSS_LOBATTO if nodes.replace("_", "-") == "gauss-lobatto" else _abi.DG_NODES_GAUSS
     flow = (get("flow equations", "ns") or "ns").lower()
@@ -163,6 +180,15 @@ def parse_control(text: str) -> Config:
         seen.add((a, b))
         cfg.periodic.append((a, b))
     return cfg
+
+
+def read_order_file(path) -> np.ndarray:
+    tokens = Path(path).read_text().split()
+    n = int(tokens[0])
+    vals = np.array([int(t) for t in tokens[1:1 + 3 * n]], dtype=np.int32)
+    if vals.size != 3 * n:
+        raise ValueError(f"{path}: expected {n} order triples")
+    return vals.reshape(n, 3)
 
 
 def read_control(path) -> Config:

@@ -9,52 +9,15 @@
 
 #include "../host/spectral.hpp"
 #include "../host/status.hpp"
-#include "dg_launch.cuh"
-#include "horses3d_gb300.h"
+#include "dg_context.cuh"
 
 using dg::Args;
 
+using h3dctx::cuda_fail;
+using h3dctx::DevBuf;
+using h3dctx::Store;
+
 namespace {
-
-int cuda_fail(cudaError_t e, const char* where) {
-    return h3d::fail(e == cudaErrorMemoryAllocation ? DG_ERR_NOMEM : DG_ERR_CUDA,
-                     std::string(where) + ": " + cudaGetErrorString(e));
-}
-
-#define CK(call)                                         \
-    do {                                                 \
-        cudaError_t e_ = (call);                         \
-        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
-    } while (0)
-
-template <typename T>
-struct DevBuf {
-    T* p = nullptr;
-    size_t n = 0;
-    cudaError_t alloc(size_t count) {
-        n = count;
-        return cudaMalloc(reinterpret_cast<void**>(&p), sizeof(T) * (count ? count : 1));
-    }
-    void free() {
-        if (p) cudaFree(p);
-        p = nullptr;
-    }
-};
-
-// Everything one precision needs on the device.
-template <typename R>
-struct Store {
-    DevBuf<R> ja_xi, ja_eta, ja_zeta, jac, inv_jac, fn, ft1, ft2, fj, sgeo;
-    DevBuf<R> QDot, Ux, Uy, Uz, QF, FV, FS;
-    Args<R> args;
-    dg::StageFn<R> stage = nullptr;
-    dg::KernelTimesFn<R> times = nullptr;
-    void free() {
-        for (DevBuf<R>* b : {&ja_xi, &ja_eta, &ja_zeta, &jac, &inv_jac, &fn, &ft1, &ft2, &fj, &sgeo, &QDot, &Ux, &Uy,
-                             &Uz, &QF, &FV, &FS})
-            b->free();
-    }
-};
 
 // The face point (i, j) whose leftIndexes2Right image is (ii, jj) (MeshTypes.f90:70-107 inverted).
 void right_to_left(int ii, int jj, int N, int rot, int& i, int& j) {
@@ -71,27 +34,6 @@ void right_to_left(int ii, int jj, int N, int rot, int& i, int& j) {
 }
 
 }  // namespace
-
-struct dg_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    int K = 0, F = 0, P = 0, nodes = 0;
-    int64_t ndof = 0;
-    dg_physics phys{};
-    dg_options opt{};
-    dg::PhysConst pc{};
-    bool mixed = false;
-    double dxi[3] = {0, 0, 0};
-    DevBuf<double> Q, G, x, scal;      // scal: [0] time, [1] dt
-    DevBuf<unsigned long long> red;    // [0..1] dt reduction, [2..6] residuals
-    DevBuf<int> face_elem, face_side, face_rot, nan_flag, nb_slot, nb_map;
-    Store<double> s64;
-    Store<float> s32;
-    double* h_scal = nullptr;          // pinned staging for scalars
-    cudaGraphExec_t graph = nullptr;
-    double graph_key[3] = {0, 0, 0};   // (mode, cfl, dcfl) the graph was captured for
-    int graph_mode = -1;
-};
 
 namespace {
 
@@ -202,6 +144,7 @@ int setup_store(dg_ctx* c, Store<R>& st, const dg_mesh_desc* m) {
 }
 
 cudaError_t run_stage(dg_ctx* c, int stage, double tshift, int flags) {
+    if (c->var) return h3dvar::stage(c, stage, tshift, flags);
     if (c->mixed) return c->s32.stage(c->s32.args, stage, tshift, flags, c->stream);
     return c->s64.stage(c->s64.args, stage, tshift, flags, c->stream);
 }
@@ -218,6 +161,7 @@ cudaError_t enqueue_step(dg_ctx* c) {
 }
 
 cudaError_t enqueue_max_dt(dg_ctx* c, double cfl, double dcfl) {
+    if (c->var) return h3dvar::enqueue_max_dt(c, cfl, dcfl);
     dg::DtArgs d;
     d.ndof = c->ndof;
     d.cfl = cfl;
@@ -237,10 +181,14 @@ cudaError_t enqueue_max_dt(dg_ctx* c, double cfl, double dcfl) {
     return cudaGetLastError();
 }
 
+// Every case's step start time and dt (one case unless the context is a batch).
 int set_scalars(dg_ctx* c, double t, double dt) {
-    c->h_scal[0] = t;
-    c->h_scal[1] = dt;
-    CK(cudaMemcpyAsync(c->scal.p, c->h_scal, 2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    const int n = c->n_cases;
+    for (int k = 0; k < n; ++k) {
+        c->h_scal[k] = t;
+        c->h_scal[n + k] = dt;
+    }
+    CK(cudaMemcpyAsync(c->scal.p, c->h_scal, 2 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     return DG_OK;
 }
 
@@ -302,6 +250,7 @@ int dg_device_count(int* count) {
 int dg_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op, dg_ctx** out) {
     if (!out) return h3d::fail(DG_ERR_INVALID, "null output pointer");
     *out = nullptr;
+    if (m && ph && op && h3dvar::needs_variable_path(m)) return h3dvar::create(1, m, ph, op, out);
     int rc = validate(m, ph, op);
     if (rc) return rc;
     int ndev = 0;
@@ -413,6 +362,7 @@ void dg_destroy(dg_ctx* c) {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->graph) cudaGraphExecDestroy(c->graph);
+    if (c->var) h3dvar::release(c);
     c->s64.free();
     c->s32.free();
     c->Q.free(); c->G.free(); c->x.free(); c->scal.free(); c->red.free(); c->nan_flag.free();
@@ -426,6 +376,7 @@ int64_t dg_ndof(const dg_ctx* c) { return c ? c->ndof : 0; }
 
 int dg_upload_state(dg_ctx* c, const double* q) {
     if (!c || !q) return h3d::fail(DG_ERR_INVALID, "null argument");
+    if (c->var) return h3dvar::upload(c, q);  // per-case constants live in device memory: graphs stay valid
     if (c->mixed) {
         // energy reference of the mixed form: the mean energy of the uploaded state
         double sum = 0.0;
@@ -454,10 +405,26 @@ int dg_download(dg_ctx* c, int field, double* dst) {
     switch (field) {
         case DG_FIELD_Q: src = c->Q.p; break;
         case DG_FIELD_G: src = c->G.p; break;
-        case DG_FIELD_QDOT: src = c->mixed ? static_cast<const void*>(c->s32.QDot.p) : c->s64.QDot.p; is_real = true; break;
-        case DG_FIELD_UX: src = c->mixed ? static_cast<const void*>(c->s32.Ux.p) : c->s64.Ux.p; is_real = true; break;
-        case DG_FIELD_UY: src = c->mixed ? static_cast<const void*>(c->s32.Uy.p) : c->s64.Uy.p; is_real = true; break;
-        case DG_FIELD_UZ: src = c->mixed ? static_cast<const void*>(c->s32.Uz.p) : c->s64.Uz.p; is_real = true; break;
+        case DG_FIELD_QDOT:
+            src = c->var ? (c->mixed ? static_cast<const void*>(c->v32.QDot.p) : c->v64.QDot.p)
+                         : (c->mixed ? static_cast<const void*>(c->s32.QDot.p) : c->s64.QDot.p);
+            is_real = true;
+            break;
+        case DG_FIELD_UX:
+            src = c->var ? (c->mixed ? static_cast<const void*>(c->v32.Ux.p) : c->v64.Ux.p)
+                         : (c->mixed ? static_cast<const void*>(c->s32.Ux.p) : c->s64.Ux.p);
+            is_real = true;
+            break;
+        case DG_FIELD_UY:
+            src = c->var ? (c->mixed ? static_cast<const void*>(c->v32.Uy.p) : c->v64.Uy.p)
+                         : (c->mixed ? static_cast<const void*>(c->s32.Uy.p) : c->s64.Uy.p);
+            is_real = true;
+            break;
+        case DG_FIELD_UZ:
+            src = c->var ? (c->mixed ? static_cast<const void*>(c->v32.Uz.p) : c->v64.Uz.p)
+                         : (c->mixed ? static_cast<const void*>(c->s32.Uz.p) : c->s64.Uz.p);
+            is_real = true;
+            break;
         default: return h3d::fail(DG_ERR_INVALID, "unknown field");
     }
     if (field >= DG_FIELD_UX && !c->phys.navier_stokes) return h3d::fail(DG_ERR_INVALID, "no gradients in Euler mode");
@@ -509,8 +476,12 @@ int prepare_graph(dg_ctx* c, int mode, double cfl, double dcfl) {
     if (mode == 1) e = enqueue_max_dt(c, cfl, dcfl);
     if (e == cudaSuccess) e = enqueue_step(c);
     if (e == cudaSuccess) {
-        dg::k_advance_time<<<1, 1, 0, c->stream>>>(c->scal.p, c->scal.p + 1);
-        e = cudaGetLastError();
+        if (c->var) {
+            e = h3dvar::enqueue_advance_time(c);
+        } else {
+            dg::k_advance_time<<<1, 1, 0, c->stream>>>(c->scal.p, c->scal.p + 1);
+            e = cudaGetLastError();
+        }
     }
     cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
     if (e != cudaSuccess) {
@@ -527,13 +498,10 @@ int prepare_graph(dg_ctx* c, int mode, double cfl, double dcfl) {
     return DG_OK;
 }
 
-int steps_common(dg_ctx* c, int n, double t0, double dt, double cfl, double dcfl, double* t_end, double* ms) {
-    if (!c || n < 0) return h3d::fail(DG_ERR_INVALID, "bad arguments");
-    const int mode = dt > 0.0 ? 0 : 1;
-    if (mode == 1 && !(cfl > 0.0)) return h3d::fail(DG_ERR_INVALID, "CFL stepping needs cfl > 0");
-    int rc = set_scalars(c, t0, mode == 0 ? dt : 0.0);
+// n graph launches of one RK3 step (mode 0: the dt on the device; mode 1: MaxTimeStep first).
+int run_graph(dg_ctx* c, int n, int mode, double cfl, double dcfl, double* ms) {
+    int rc = prepare_graph(c, mode, cfl, dcfl);
     if (rc) return rc;
-    if ((rc = prepare_graph(c, mode, cfl, dcfl))) return rc;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (ms) {
         CK(cudaEventCreate(&e0));
@@ -550,6 +518,16 @@ int steps_common(dg_ctx* c, int n, double t0, double dt, double cfl, double dcfl
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
     }
+    return DG_OK;
+}
+
+int steps_common(dg_ctx* c, int n, double t0, double dt, double cfl, double dcfl, double* t_end, double* ms) {
+    if (!c || n < 0) return h3d::fail(DG_ERR_INVALID, "bad arguments");
+    const int mode = dt > 0.0 ? 0 : 1;
+    if (mode == 1 && !(cfl > 0.0)) return h3d::fail(DG_ERR_INVALID, "CFL stepping needs cfl > 0");
+    int rc = set_scalars(c, t0, mode == 0 ? dt : 0.0);
+    if (rc) return rc;
+    if ((rc = run_graph(c, n, mode, cfl, dcfl, ms))) return rc;
     if (t_end) {
         CK(cudaMemcpyAsync(c->h_scal, c->scal.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
@@ -576,6 +554,7 @@ int dg_kernel_times(dg_ctx* c, int reps, double t0, double dt, double ms[5]) {
     int rc = set_scalars(c, t0, dt);
     if (rc) return rc;
     for (int kk = 0; kk < 5; ++kk) ms[kk] = 0.0;
+    if (c->var) return h3dvar::kernel_times(c, reps, ms);
     if (c->mixed) CK(c->s32.times(c->s32.args, reps, c->stream, ms));
     else CK(c->s64.times(c->s64.args, reps, c->stream, ms));
     return DG_OK;
@@ -584,14 +563,31 @@ int dg_kernel_times(dg_ctx* c, int reps, double t0, double dt, double ms[5]) {
 int dg_max_dt(dg_ctx* c, double cfl, double dcfl, double* dt) {
     if (!c || !dt) return h3d::fail(DG_ERR_INVALID, "null argument");
     CK(enqueue_max_dt(c, cfl, dcfl));
-    CK(cudaMemcpyAsync(c->h_scal + 2, c->scal.p + 1, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    const int n = c->n_cases;
+    CK(cudaMemcpyAsync(c->h_scal + 2 * n, c->scal.p + n, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    *dt = c->h_scal[2];
+    double m = c->h_scal[2 * n];
+    for (int k = 1; k < n; ++k) m = std::fmin(m, c->h_scal[2 * n + k]);
+    *dt = m;  // a batch reports the smallest case dt; every case keeps its own on the device
     return DG_OK;
 }
 
 int dg_residuals(dg_ctx* c, double maxres[5], int* nan_found) {
     if (!c || !maxres) return h3d::fail(DG_ERR_INVALID, "null argument");
+    if (c->var) {  // the maximum over the cases of a batch
+        std::vector<double> r(5 * static_cast<size_t>(c->n_cases));
+        std::vector<int> nan(c->n_cases);
+        const int rc = h3dvar::residuals(c, r.data(), nan.data());
+        if (rc != DG_OK && rc != DG_ERR_NAN) return rc;
+        int any = 0;
+        for (int v = 0; v < 5; ++v) maxres[v] = 0.0;
+        for (int k = 0; k < c->n_cases; ++k) {
+            for (int v = 0; v < 5; ++v) maxres[v] = std::fmax(maxres[v], r[5 * k + v]);
+            any |= nan[k];
+        }
+        if (nan_found) *nan_found = any;
+        return rc;
+    }
     CK(cudaMemsetAsync(c->red.p + 2, 0, 5 * sizeof(unsigned long long), c->stream));
     CK(cudaMemsetAsync(c->nan_flag.p, 0, sizeof(int), c->stream));
     const int blocks = 152 * 4;
@@ -612,6 +608,70 @@ int dg_synchronize(dg_ctx* c) {
     if (!c) return h3d::fail(DG_ERR_INVALID, "null context");
     CK(cudaStreamSynchronize(c->stream));
     return DG_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ batches of cases ----------
+extern "C" {
+
+int dg_create_batch(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, const dg_options* opts,
+                    dg_ctx** out) {
+    return h3dvar::create(n_cases, meshes, phys, opts, out);
+}
+
+int dg_batch_size(const dg_ctx* c) { return c ? c->n_cases : 0; }
+
+int64_t dg_case_offset(const dg_ctx* c, int k) {
+    if (!c || k < 0 || k > c->n_cases) return -1;
+    if (!c->var) return k == 0 ? 0 : c->ndof;
+    return c->case_ndof_off[k];
+}
+
+int dg_batch_set_clock(dg_ctx* c, const double* t, const double* dt) {
+    if (!c || !t || !dt) return h3d::fail(DG_ERR_INVALID, "null argument");
+    const int n = c->n_cases;
+    for (int k = 0; k < n; ++k) {
+        if (!std::isfinite(t[k]) || !(dt[k] >= 0.0) || !std::isfinite(dt[k]))
+            return h3d::fail(DG_ERR_INVALID, "case times must be finite and dt non-negative");
+        c->h_scal[k] = t[k];
+        c->h_scal[n + k] = dt[k];
+    }
+    CK(cudaMemcpyAsync(c->scal.p, c->h_scal, 2 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return DG_OK;
+}
+
+int dg_batch_get_clock(dg_ctx* c, double* t, double* dt) {
+    if (!c || !t || !dt) return h3d::fail(DG_ERR_INVALID, "null argument");
+    const int n = c->n_cases;
+    CK(cudaMemcpyAsync(c->h_scal, c->scal.p, 2 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int k = 0; k < n; ++k) {
+        t[k] = c->h_scal[k];
+        dt[k] = c->h_scal[n + k];
+    }
+    return DG_OK;
+}
+
+int dg_batch_max_dt(dg_ctx* c, double cfl, double dcfl, double* dt) {
+    if (!c || !dt) return h3d::fail(DG_ERR_INVALID, "null argument");
+    CK(enqueue_max_dt(c, cfl, dcfl));
+    const int n = c->n_cases;
+    CK(cudaMemcpyAsync(dt, c->scal.p + n, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return DG_OK;
+}
+
+int dg_batch_residuals(dg_ctx* c, double* maxres, int* nan_found) {
+    if (!c || !maxres) return h3d::fail(DG_ERR_INVALID, "null argument");
+    if (!c->var) return dg_residuals(c, maxres, nan_found);
+    return h3dvar::residuals(c, maxres, nan_found);
+}
+
+int dg_batch_run_steps(dg_ctx* c, int n, double cfl, double dcfl, double* ms) {
+    if (!c || n < 0) return h3d::fail(DG_ERR_INVALID, "bad arguments");
+    return run_graph(c, n, cfl > 0.0 ? 1 : 0, cfl, dcfl, ms);
 }
 
 }  // extern "C"

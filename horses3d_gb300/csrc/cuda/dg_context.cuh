@@ -1,0 +1,132 @@
+// Internal: the context behind the opaque dg_ctx handle of the C ABI, shared by the uniform-order
+// path (dg_api.cu) and the variable-order / multi-case path (dg_var_api.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../host/status.hpp"
+#include "dg_var.cuh"
+#include "horses3d_gb300.h"
+
+namespace h3dctx {
+
+inline int cuda_fail(cudaError_t e, const char* where) {
+    return h3d::fail(e == cudaErrorMemoryAllocation ? DG_ERR_NOMEM : DG_ERR_CUDA,
+                     std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                                       \
+    do {                                                               \
+        cudaError_t e_ = (call);                                       \
+        if (e_ != cudaSuccess) return h3dctx::cuda_fail(e_, #call);    \
+    } while (0)
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(size_t count) {
+        n = count;
+        return cudaMalloc(reinterpret_cast<void**>(&p), sizeof(T) * (count ? count : 1));
+    }
+    cudaError_t upload(const T* src, size_t count, cudaStream_t s) {
+        cudaError_t e = alloc(count);
+        if (e != cudaSuccess) return e;
+        if (count == 0) return cudaSuccess;
+        e = cudaMemcpyAsync(p, src, sizeof(T) * count, cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return e;
+        return cudaStreamSynchronize(s);
+    }
+    void free() {
+        if (p) cudaFree(p);
+        p = nullptr;
+    }
+};
+
+// Uniform-order path: everything one precision needs on the device.
+template <typename R>
+struct Store {
+    DevBuf<R> ja_xi, ja_eta, ja_zeta, jac, inv_jac, fn, ft1, ft2, fj, sgeo;
+    DevBuf<R> QDot, Ux, Uy, Uz, QF, FV, FS;
+    dg::Args<R> args;
+    dg::StageFn<R> stage = nullptr;
+    dg::KernelTimesFn<R> times = nullptr;
+    void free() {
+        for (DevBuf<R>* b : {&ja_xi, &ja_eta, &ja_zeta, &jac, &inv_jac, &fn, &ft1, &ft2, &fj, &sgeo, &QDot, &Ux, &Uy,
+                             &Uz, &QF, &FV, &FS})
+            b->free();
+    }
+};
+
+// Variable-order path: per-precision buffers.
+template <typename R>
+struct VStore {
+    DevBuf<R> ja_xi, ja_eta, ja_zeta, jac, inv_jac, fn, ft1, ft2, fj, tset;
+    DevBuf<R> QDot, Ux, Uy, Uz, QF, GF, UJ, FS;
+    DevBuf<dg::OpsP<R>> ops;
+    DevBuf<dg::PhysR<R>> ph;
+    dg::VArgs<R> args;
+    dg::VStageFn<R> stage = nullptr;
+    dg::VTimesFn<R> times = nullptr;
+    void free() {
+        for (DevBuf<R>* b : {&ja_xi, &ja_eta, &ja_zeta, &jac, &inv_jac, &fn, &ft1, &ft2, &fj, &tset, &QDot, &Ux, &Uy,
+                             &Uz, &QF, &GF, &UJ, &FS})
+            b->free();
+        ops.free();
+        ph.free();
+    }
+};
+
+}  // namespace h3dctx
+
+struct dg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int K = 0, F = 0, P = 0, nodes = 0;
+    int64_t ndof = 0;
+    dg_physics phys{};
+    dg_options opt{};
+    dg::PhysConst pc{};
+    bool mixed = false;
+    double dxi[3] = {0, 0, 0};
+    h3dctx::DevBuf<double> Q, G, x, scal;    // scal: time[n_cases], then dt[n_cases]
+    h3dctx::DevBuf<unsigned long long> red;  // uniform: [0..1] dt, [2..6] residuals; variable: 8 per case
+    h3dctx::DevBuf<int> face_elem, face_side, face_rot, nan_flag, nb_slot, nb_map;
+    h3dctx::Store<double> s64;
+    h3dctx::Store<float> s32;
+    double* h_scal = nullptr;  // pinned staging for the per-case scalars (4 * n_cases doubles)
+    cudaGraphExec_t graph = nullptr;
+    double graph_key[3] = {0, 0, 0};  // (mode, cfl, dcfl) the graph was captured for
+    int graph_mode = -1;
+
+    // variable-order / multi-case path
+    bool var = false;
+    int n_cases = 1;
+    std::vector<int64_t> case_ndof_off;  // [n_cases + 1] node offsets of the cases
+    std::vector<dg::CaseConst> case_const;
+    std::vector<dg::PhysConst> case_pc;
+    h3dctx::DevBuf<int4> items, faces4;
+    h3dctx::DevBuf<int> item_elems, eord, vnan;
+    h3dctx::DevBuf<long long> eoff, soff, foff;
+    h3dctx::DevBuf<dg::CaseConst> cc;
+    h3dctx::DevBuf<double> dxi_table, gamma_M2;
+    h3dctx::VStore<double> v64;
+    h3dctx::VStore<float> v32;
+    int n_items = 0;
+};
+
+// Variable-order / multi-case path (dg_var_api.cu).
+namespace h3dvar {
+bool needs_variable_path(const dg_mesh_desc* m);
+int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, const dg_options* opt, dg_ctx** out);
+void release(dg_ctx* c);
+int upload(dg_ctx* c, const double* q);
+cudaError_t stage(dg_ctx* c, int stage, double tshift, int flags);
+cudaError_t enqueue_max_dt(dg_ctx* c, double cfl, double dcfl);
+cudaError_t enqueue_advance_time(dg_ctx* c);
+int residuals(dg_ctx* c, double* maxres, int* nan_case);  // maxres [5*n_cases], nan_case [n_cases]
+int kernel_times(dg_ctx* c, int reps, double* ms);
+}  // namespace h3dvar

@@ -1,0 +1,907 @@
+// DGSEM right-hand side for p-anisotropic elements and for batches of independent cases: every
+// element has its own orders (Nx,Ny,Nz) and belongs to one case, each case with its own physics
+// constants, time and dt. The arithmetic type R is double (plain form) or float (mixed form); Q and
+// the RK register G are FP64 in both.
+//
+// Work is cut into items: one CTA processes `count` consecutive elements of one order triple and one
+// case (the elements are bucketed by order triple on the host), so the per-element loops of a CTA
+// have one trip count and the operators of the three directions sit in shared memory. Threads loop
+// over the item's nodes, so an item may hold more nodes than the CTA has threads.
+//
+// Faces follow the reference's conforming treatment (FaceClass.f90:281-470, 597-703, 865-963): each
+// face has its own order (Nf1,Nf2) = max of its two sides; the element traces are interpolated to the
+// face points with Tset (InterpolationMatrices.f90:42-113), the face quantity is formed there and
+// projected back to each side's order with the transposed, weight-scaled Tset. A CTA processes
+// FPB faces with one 64-thread group each (a face has at most 8 x 8 points).
+//
+// Kernels of one RK stage (Navier-Stokes; Euler skips kv_face<JUMP>):
+//   kv_face<kJump>   BR1 interface jump 1/2 (U_R - U_L) Jf n at the face points, projected to both sides
+//                    (EllipticBR1.f90:571-627)
+//   kv_volume        local gradient, lifting, gradient traces, contravariant fluxes and the weak
+//                    volume integral -> QDot (HexElementClass.f90:304-531, EllipticBR1.f90:531-569,
+//                    SpatialDiscretization.f90:1602-1682, DGIntegrals.f90:56-87)
+//   kv_face<kFlux*>  Roe/LxF flux minus the averaged viscous normal flux, times Jf, projected to both
+//                    sides, side 2 negated (SpatialDiscretization.f90:1710-1799, EllipticBR1.f90:816-868)
+//   kv_update        surface integral, 1/J, source, Williamson RK3 update, Q traces of the new state
+//
+// Slot data (slot = 6e + side - 1) are stored per slot and variable: value(slot, v, p) at
+// [soff[slot]*NV + v*n_slot + p], n_slot the side's point count at the element's own orders.
+#pragma once
+#include <cstdint>
+
+#include "dg_launch.cuh"
+
+namespace dg {
+
+// Operators of one node count P (NodalStorageClass.f90:170-338), row stride kMaxP.
+template <typename R>
+struct OpsP {
+    R D[kMaxP * kMaxP], hatD[kMaxP * kMaxP];
+    R vL[kMaxP], vR[kMaxP], bL[kMaxP], bR[kMaxP];
+};
+
+constexpr int kTsetStride = kMaxP * kMaxP;  // Tset(No -> Nd) at tset[(No * kMaxP + Nd) * kTsetStride]
+
+// Per-case FP64 constants: energy reference of the mixed form and the manufactured-source constants.
+struct CaseConst {
+    double e_ref, gm1, gM2, mu, kappa;
+};
+
+template <typename R>
+struct VArgs {
+    int n_items, n_faces, cap;  // cap: largest node count of an item
+    int ns, source;
+    const int4* items;          // x: first index into item_elems, y: count, z: px|py<<8|pz<<16, w: case
+    const int* item_elems;
+    const int* eord;            // px|py<<8|pz<<16 per element
+    const long long* eoff;      // first node of each element
+    const long long* soff;      // first point of each slot
+    const int4* faces;          // x: left elem, y: right elem, z: sideL|sideR<<4|rot<<8|q1<<12|q2<<16, w: case
+    const long long* foff;      // first face point of each face
+    const OpsP<R>* ops;         // [kMaxP + 1], indexed by P
+    const R* tset;
+    const PhysR<R>* ph;         // per case
+    const CaseConst* cc;        // per case
+    const double* time;         // per case: step start time
+    const double* dt;           // per case
+    const R* ja_xi;
+    const R* ja_eta;
+    const R* ja_zeta;
+    const R* jac;
+    const R* inv_jac;
+    const double* x;
+    const R* fn;                // face points, 3 per point
+    const R* ft1;
+    const R* ft2;
+    const R* fj;
+    double* Q;
+    double* G;
+    R* QDot;
+    R* Ux;
+    R* Uy;
+    R* Uz;
+    R* QF;  // Q traces        (5 per slot point)
+    R* GF;  // gradient traces (15 per slot point)
+    R* UJ;  // BR1 jumps       (15 per slot point)
+    R* FS;  // surface fluxes  (5 per slot point)
+};
+
+struct ItemDims {
+    int first, count, px, py, pz, kase, np, ntot;
+};
+
+__device__ __forceinline__ ItemDims item_dims(const int4 it) {
+    ItemDims d;
+    d.first = it.x;
+    d.count = it.y;
+    d.px = it.z & 255;
+    d.py = (it.z >> 8) & 255;
+    d.pz = (it.z >> 16) & 255;
+    d.kase = it.w;
+    d.np = d.px * d.py * d.pz;
+    d.ntot = d.count * d.np;
+    return d;
+}
+
+// Face point counts of a side (first, second face direction), sides numbered as the reference.
+__device__ __forceinline__ void side_dims(int side, int ord, int& d1, int& d2) {
+    const int px = ord & 255, py = (ord >> 8) & 255, pz = (ord >> 16) & 255;
+    switch (side) {
+        case 1: case 2: d1 = px; d2 = pz; break;
+        case 3: case 5: d1 = px; d2 = py; break;
+        default: d1 = py; d2 = pz; break;
+    }
+}
+
+// Node at line position l through face point (ca, cb) of a side.
+__device__ __forceinline__ int vline_node(int side, int ca, int cb, int l, int px, int py) {
+    switch (side) {
+        case 1: case 2: return ca + px * (l + py * cb);
+        case 3: case 5: return ca + px * (cb + py * l);
+        default: return l + px * (ca + py * cb);
+    }
+}
+
+// Trace task r of an element (tasks ordered side 1..6, point p within the side).
+__device__ __forceinline__ int side_of_task(int r, int A, int B, int C, int& p) {
+    if (r < A) { p = r; return 1; }
+    r -= A;
+    if (r < A) { p = r; return 2; }
+    r -= A;
+    if (r < B) { p = r; return 3; }
+    r -= B;
+    if (r < C) { p = r; return 4; }
+    r -= C;
+    if (r < B) { p = r; return 5; }
+    p = r - B;
+    return 6;
+}
+
+// The three directions' operators of an item into shared memory.
+template <typename R>
+__device__ __forceinline__ void load_ops(const OpsP<R>* ops, OpsP<R>* s, int px, int py, int pz) {
+    constexpr int W = static_cast<int>(sizeof(OpsP<R>) / sizeof(R));
+    for (int t = threadIdx.x; t < 3 * W; t += blockDim.x) {
+        const int d = t / W, w = t - d * W;
+        const int P = d == 0 ? px : (d == 1 ? py : pz);
+        reinterpret_cast<R*>(s)[t] = reinterpret_cast<const R*>(ops + P)[w];
+    }
+}
+
+// NV traces of the item's nodes held in s (value v of item node m at s[v*ntot + m]) into the slots.
+template <typename R, int NV>
+__device__ __forceinline__ void write_traces(const VArgs<R>& a, const ItemDims& d, const OpsP<R>* sO, const R* s,
+                                             R* dst) {
+    const int A = d.px * d.pz, B = d.px * d.py, C = d.py * d.pz, Te = 2 * (A + B + C);
+    for (int t = threadIdx.x; t < d.count * Te; t += blockDim.x) {
+        const int le = t / Te;
+        int p;
+        const int side = side_of_task(t - le * Te, A, B, C, p);
+        const int ns = side <= 2 ? A : ((side == 3 || side == 5) ? B : C);
+        const int d1 = side <= 2 ? d.px : ((side == 3 || side == 5) ? d.px : d.py);
+        const int ca = p % d1, cb = p / d1;
+        const int dir = side <= 2 ? 1 : ((side == 3 || side == 5) ? 2 : 0);
+        const int L = dir == 0 ? d.px : (dir == 1 ? d.py : d.pz);
+        const R* v = (side == 2 || side == 4 || side == 5) ? sO[dir].vR : sO[dir].vL;
+        const R* base = s + le * d.np;
+        R acc[NV];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) acc[c] = R(0);
+        for (int l = 0; l < L; ++l) {
+            const R w = v[l];
+            const int m = vline_node(side, ca, cb, l, d.px, d.py);
+#pragma unroll
+            for (int c = 0; c < NV; ++c) acc[c] = acc[c] + base[c * d.ntot + m] * w;
+        }
+        const int e = a.item_elems[d.first + le];
+        R* o = dst + a.soff[6LL * e + side - 1] * NV + p;
+#pragma unroll
+        for (int c = 0; c < NV; ++c) o[c * ns] = acc[c];
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// kv_traces: Q traces of the current state (after an upload).
+// ------------------------------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(256) kv_traces(VArgs<R> a) {
+    extern __shared__ __align__(16) unsigned char vsm[];
+    const ItemDims d = item_dims(a.items[blockIdx.x]);
+    OpsP<R>* sO = reinterpret_cast<OpsP<R>*>(vsm);
+    R* sQ = reinterpret_cast<R*>(sO + 3);
+    load_ops(a.ops, sO, d.px, d.py, d.pz);
+    const double eref = a.cc[d.kase].e_ref;
+    for (int t = threadIdx.x; t < d.ntot; t += blockDim.x) {
+        const int le = t / d.np, n = t - le * d.np;
+        const long long g = a.eoff[a.item_elems[d.first + le]] + n;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) sQ[v * d.ntot + t] = R(a.Q[5 * g + v]);
+        sQ[4 * d.ntot + t] = R(a.Q[5 * g + 4] - eref);
+    }
+    __syncthreads();
+    write_traces<R, 5>(a, d, sO, sQ, a.QF);
+}
+
+// ------------------------------------------------------------------------------------------------
+// kv_volume: gradient + lifting + gradient traces (Navier-Stokes), fluxes, weak volume integral.
+// ------------------------------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(256) kv_volume(VArgs<R> a, int store_grad) {
+    extern __shared__ __align__(16) unsigned char vsm[];
+    const ItemDims d = item_dims(a.items[blockIdx.x]);
+    const int px = d.px, py = d.py, pz = d.pz, np = d.np, ntot = d.ntot;
+    OpsP<R>* sO = reinterpret_cast<OpsP<R>*>(vsm);  // xi, eta, zeta operators
+    R* sQ = reinterpret_cast<R*>(sO + 3);            // 5*ntot: state
+    R* sG = sQ + 5 * ntot;                           // 15*ntot: lifted gradient, then the fluxes
+    load_ops(a.ops, sO, px, py, pz);
+    const PhysR<R> ph = a.ph[d.kase];
+    const double eref = a.cc[d.kase].e_ref;
+    for (int t = threadIdx.x; t < ntot; t += blockDim.x) {
+        const int le = t / np, n = t - le * np;
+        const long long g = a.eoff[a.item_elems[d.first + le]] + n;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) sQ[v * ntot + t] = R(a.Q[5 * g + v]);
+        sQ[4 * ntot + t] = R(a.Q[5 * g + 4] - eref);
+    }
+    __syncthreads();
+    if (a.ns) {
+        const int A = px * pz, B = px * py, C = py * pz;
+        for (int t = threadIdx.x; t < ntot; t += blockDim.x) {
+            const int le = t / np, n = t - le * np;
+            const int i = n % px, j = (n / px) % py, k = n / (px * py);
+            const int e = a.item_elems[d.first + le];
+            const long long g = a.eoff[e] + n;
+            const R* q0 = sQ + le * np;
+            R uxi[5] = {0, 0, 0, 0, 0}, ueta[5] = {0, 0, 0, 0, 0}, uzeta[5] = {0, 0, 0, 0, 0};
+            for (int l = 0; l < px; ++l) {
+                const R w = sO[0].D[i * kMaxP + l];
+#pragma unroll
+                for (int v = 0; v < 5; ++v) uxi[v] = uxi[v] + q0[v * ntot + l + px * (j + py * k)] * w;
+            }
+            for (int l = 0; l < py; ++l) {
+                const R w = sO[1].D[j * kMaxP + l];
+#pragma unroll
+                for (int v = 0; v < 5; ++v) ueta[v] = ueta[v] + q0[v * ntot + i + px * (l + py * k)] * w;
+            }
+            for (int l = 0; l < pz; ++l) {
+                const R w = sO[2].D[k * kMaxP + l];
+#pragma unroll
+                for (int v = 0; v < 5; ++v) uzeta[v] = uzeta[v] + q0[v * ntot + i + px * (j + py * l)] * w;
+            }
+            R jx[3], je[3], jz[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                jx[c] = a.ja_xi[3 * g + c];
+                je[c] = a.ja_eta[3 * g + c];
+                jz[c] = a.ja_zeta[3 * g + c];
+            }
+            const R ij = a.inv_jac[g];
+            R U[3][5];
+#pragma unroll
+            for (int v = 0; v < 5; ++v) {
+                U[0][v] = (uxi[v] * jx[0] + ueta[v] * je[0] + uzeta[v] * jz[0]) * ij;
+                U[1][v] = (uxi[v] * jx[1] + ueta[v] * je[1] + uzeta[v] * jz[1]) * ij;
+                U[2][v] = (uxi[v] * jx[2] + ueta[v] * je[2] + uzeta[v] * jz[2]) * ij;
+            }
+            // lifting (VectorWeakIntegrals_StdFace order: left, right, front, back, bottom, top)
+            const long long s0 = 6LL * e;
+            const R* HF = a.UJ + a.soff[s0 + 0] * 15 + (i + px * k);
+            const R* HB = a.UJ + a.soff[s0 + 1] * 15 + (i + px * k);
+            const R* HO = a.UJ + a.soff[s0 + 2] * 15 + (i + px * j);
+            const R* HR = a.UJ + a.soff[s0 + 3] * 15 + (j + py * k);
+            const R* HT = a.UJ + a.soff[s0 + 4] * 15 + (i + px * j);
+            const R* HL = a.UJ + a.soff[s0 + 5] * 15 + (j + py * k);
+            const R bxl = sO[0].bL[i], bxr = sO[0].bR[i], byl = sO[1].bL[j], byr = sO[1].bR[j];
+            const R bzl = sO[2].bL[k], bzr = sO[2].bR[k];
+#pragma unroll
+            for (int dd = 0; dd < 3; ++dd)
+#pragma unroll
+                for (int v = 0; v < 5; ++v) {
+                    const int c = v + 5 * dd;
+                    R fi = HL[c * C] * bxl;
+                    fi = fi + HR[c * C] * bxr;
+                    fi = fi + HF[c * A] * byl;
+                    fi = fi + HB[c * A] * byr;
+                    fi = fi + HO[c * B] * bzl;
+                    fi = fi + HT[c * B] * bzr;
+                    U[dd][v] = U[dd][v] + fi * ij;
+                }
+#pragma unroll
+            for (int dd = 0; dd < 3; ++dd)
+#pragma unroll
+                for (int v = 0; v < 5; ++v) sG[(v + 5 * dd) * ntot + t] = U[dd][v];
+            if (store_grad) {
+#pragma unroll
+                for (int v = 0; v < 5; ++v) {
+                    a.Ux[5 * g + v] = U[0][v];
+                    a.Uy[5 * g + v] = U[1][v];
+                    a.Uz[5 * g + v] = U[2][v];
+                }
+            }
+        }
+        __syncthreads();
+        write_traces<R, 15>(a, d, sO, sG, a.GF);
+        __syncthreads();
+    }
+    // contravariant fluxes F = Finv - Fvisc at each node, over the node's own gradient column
+    for (int t = threadIdx.x; t < ntot; t += blockDim.x) {
+        const int le = t / np, n = t - le * np;
+        const long long g = a.eoff[a.item_elems[d.first + le]] + n;
+        R q[5], jx[3], je[3], jz[3];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) q[v] = sQ[v * ntot + t];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            jx[c] = a.ja_xi[3 * g + c];
+            je[c] = a.ja_eta[3 * g + c];
+            jz[c] = a.ja_zeta[3 * g + c];
+        }
+        R F[3][5];
+        euler_contravariant(ph, q, jx, je, jz, F);
+        if (a.ns) {
+            R Ug[15];
+#pragma unroll
+            for (int c = 0; c < 15; ++c) Ug[c] = sG[c * ntot + t];
+            R mu, kap;
+            mu_kappa(ph, q, mu, kap);
+            R Cv[3][5];
+            viscous_flux(ph, q, Ug, Ug + 5, Ug + 10, mu, kap, Cv);
+            const R* ja[3] = {jx, je, jz};
+#pragma unroll
+            for (int dd = 0; dd < 3; ++dd)
+#pragma unroll
+                for (int v = 0; v < 5; ++v)
+                    F[dd][v] = F[dd][v] - (Cv[0][v] * ja[dd][0] + Cv[1][v] * ja[dd][1] + Cv[2][v] * ja[dd][2]);
+        }
+#pragma unroll
+        for (int dd = 0; dd < 3; ++dd)
+#pragma unroll
+            for (int v = 0; v < 5; ++v) sG[(v + 5 * dd) * ntot + t] = F[dd][v];
+    }
+    __syncthreads();
+    // ScalarWeakIntegrals_StdVolumeGreen
+    for (int t = threadIdx.x; t < ntot; t += blockDim.x) {
+        const int le = t / np, n = t - le * np;
+        const int i = n % px, j = (n / px) % py, k = n / (px * py);
+        const long long g = a.eoff[a.item_elems[d.first + le]] + n;
+        const R* F0 = sG + le * np;
+        R acc[5] = {0, 0, 0, 0, 0};
+        for (int l = 0; l < px; ++l) {
+            const R h = sO[0].hatD[i * kMaxP + l];
+#pragma unroll
+            for (int v = 0; v < 5; ++v) acc[v] = acc[v] + h * F0[v * ntot + l + px * (j + py * k)];
+        }
+        for (int l = 0; l < py; ++l) {
+            const R h = sO[1].hatD[j * kMaxP + l];
+#pragma unroll
+            for (int v = 0; v < 5; ++v) acc[v] = acc[v] + h * F0[(5 + v) * ntot + i + px * (l + py * k)];
+        }
+        for (int l = 0; l < pz; ++l) {
+            const R h = sO[2].hatD[k * kMaxP + l];
+#pragma unroll
+            for (int v = 0; v < 5; ++v) acc[v] = acc[v] + h * F0[(10 + v) * ntot + i + px * (j + py * l)];
+        }
+#pragma unroll
+        for (int v = 0; v < 5; ++v) a.QDot[5 * g + v] = acc[v];
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// kv_face: BR1 jump (kJump) or interface flux (kFluxEuler / kFluxNS) at the face points.
+// ------------------------------------------------------------------------------------------------
+constexpr int kJump = 0;
+constexpr int kFluxEuler = 1;
+constexpr int kFluxNS = 2;
+constexpr int kFacePts = kMaxP * kMaxP;  // threads per face group
+
+template <typename R, int MODE>
+struct FaceCfg {
+    static constexpr int NVIN = MODE == kFluxNS ? 20 : 5;
+    static constexpr int NVOUT = MODE == kJump ? 15 : 5;
+    static constexpr int NVB = NVIN > NVOUT ? NVIN : NVOUT;
+    static constexpr int FPB = (sizeof(R) == 8 && NVB > 5) ? 2 : 4;  // faces per CTA
+    static constexpr int THREADS = FPB * kFacePts;
+    static constexpr size_t SMEM = static_cast<size_t>(FPB) * 4 * NVB * kFacePts * sizeof(R);
+};
+
+// Interpolation of NV values from (s1 x s2) points in S to the face's (q1 x q2) points; returns the
+// buffer that holds the result (S or A). Every thread of the CTA must call it (it synchronises).
+template <typename R, int NV>
+__device__ __forceinline__ R* to_face_points(const R* tset, R* S, R* A, int s1, int s2, int q1, int q2, int lane,
+                                             bool active) {
+    const bool d1 = active && s1 != q1, d2 = active && s2 != q2;
+    if (d1) {  // along the first face direction: A(i, l) = sum_m T1(i, m) S(m, l)
+        const R* T = tset + ((s1 - 1) * kMaxP + (q1 - 1)) * kTsetStride;
+        for (int p = lane; p < q1 * s2; p += kFacePts) {
+            const int i = p % q1, l = p / q1;
+            R acc[NV];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) acc[v] = R(0);
+            for (int m = 0; m < s1; ++m) {
+                const R w = T[i * kMaxP + m];
+#pragma unroll
+                for (int v = 0; v < NV; ++v) acc[v] = acc[v] + w * S[v * kFacePts + m + s1 * l];
+            }
+#pragma unroll
+            for (int v = 0; v < NV; ++v) A[v * kFacePts + p] = acc[v];
+        }
+    }
+    __syncthreads();
+    R* cur = d1 ? A : S;
+    R* nxt = d1 ? S : A;
+    if (d2) {  // along the second: nxt(i, j) = sum_l T2(j, l) cur(i, l)
+        const R* T = tset + ((s2 - 1) * kMaxP + (q2 - 1)) * kTsetStride;
+        for (int p = lane; p < q1 * q2; p += kFacePts) {
+            const int i = p % q1, j = p / q1;
+            R acc[NV];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) acc[v] = R(0);
+            for (int l = 0; l < s2; ++l) {
+                const R w = T[j * kMaxP + l];
+#pragma unroll
+                for (int v = 0; v < NV; ++v) acc[v] = acc[v] + w * cur[v * kFacePts + i + q1 * l];
+            }
+#pragma unroll
+            for (int v = 0; v < NV; ++v) nxt[v * kFacePts + p] = acc[v];
+        }
+    }
+    __syncthreads();
+    return d2 ? nxt : cur;
+}
+
+template <typename R, int MODE>
+__global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS) kv_face(VArgs<R> a) {
+    using Cfg = FaceCfg<R, MODE>;
+    constexpr int NVIN = Cfg::NVIN, NVOUT = Cfg::NVOUT, NVB = Cfg::NVB, NP = kFacePts;
+    extern __shared__ __align__(16) unsigned char fsm[];
+    const int grp = threadIdx.x / NP, lane = threadIdx.x - grp * NP;
+    R* SL = reinterpret_cast<R*>(fsm) + grp * 4 * NVB * NP;
+    R* AL = SL + NVB * NP;
+    R* SR = AL + NVB * NP;
+    R* AR = SR + NVB * NP;
+    const int f = blockIdx.x * Cfg::FPB + grp;
+    const bool active = f < a.n_faces;
+    int eL = 0, eR = 0, rot = 0, q1 = 1, q2 = 1, kase = 0;
+    int l1 = 1, l2 = 1, r1 = 1, r2 = 1, s1R = 1, s2R = 1;
+    long long offL = 0, offR = 0, fo = 0;
+    if (active) {
+        const int4 fd = a.faces[f];
+        eL = fd.x;
+        eR = fd.y;
+        const int sL = fd.z & 15, sR = (fd.z >> 4) & 15;
+        rot = (fd.z >> 8) & 15;
+        q1 = (fd.z >> 12) & 15;
+        q2 = (fd.z >> 16) & 15;
+        kase = fd.w;
+        side_dims(sL, a.eord[eL], l1, l2);
+        side_dims(sR, a.eord[eR], r1, r2);
+        const bool swap = !(rot == 0 || rot == 2 || rot == 5 || rot == 7);
+        s1R = swap ? r2 : r1;
+        s2R = swap ? r1 : r2;
+        offL = a.soff[6LL * eL + sL - 1];
+        offR = a.soff[6LL * eR + sR - 1];
+        fo = a.foff[f];
+    }
+    const int nL = l1 * l2, nR = r1 * r2;
+    if (active) {
+        for (int p = lane; p < nL; p += NP) {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) SL[v * NP + p] = a.QF[offL * 5 + v * nL + p];
+            if (MODE == kFluxNS) {
+#pragma unroll
+                for (int c = 0; c < 15; ++c) SL[(5 + c) * NP + p] = a.GF[offL * 15 + c * nL + p];
+            }
+        }
+        for (int p = lane; p < nR; p += NP) {  // right trace in the left side's orientation
+            const int i = p % s1R, j = p / s1R;
+            int ii, jj;
+            left2right(i, j, s1R - 1, s2R - 1, rot, ii, jj);
+            const int src = ii + r1 * jj;
+#pragma unroll
+            for (int v = 0; v < 5; ++v) SR[v * NP + p] = a.QF[offR * 5 + v * nR + src];
+            if (MODE == kFluxNS) {
+#pragma unroll
+                for (int c = 0; c < 15; ++c) SR[(5 + c) * NP + p] = a.GF[offR * 15 + c * nR + src];
+            }
+        }
+    }
+    __syncthreads();
+    const R* XL = to_face_points<R, NVIN>(a.tset, SL, AL, l1, l2, q1, q2, lane, active);
+    const R* XR = to_face_points<R, NVIN>(a.tset, SR, AR, s1R, s2R, q1, q2, lane, active);
+    R out[NVOUT];
+    const bool point = active && lane < q1 * q2;
+    if (point) {
+        const long long gp = fo + lane;
+        const R n[3] = {a.fn[3 * gp], a.fn[3 * gp + 1], a.fn[3 * gp + 2]};
+        const R J = a.fj[gp];
+        if (MODE == kJump) {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) {
+                const R u = R(0.5) * (XR[v * NP + lane] - XL[v * NP + lane]) * J;
+                out[v] = u * n[0];
+                out[5 + v] = u * n[1];
+                out[10 + v] = u * n[2];
+            }
+        } else {
+            const PhysR<R> ph = a.ph[kase];
+            R QL[5], QR[5], inv[5];
+#pragma unroll
+            for (int v = 0; v < 5; ++v) {
+                QL[v] = XL[v * NP + lane];
+                QR[v] = XR[v * NP + lane];
+            }
+            if (ph.riemann == 0) {
+                roe_flux(ph, QL, QR, n, inv);
+            } else {
+                const R t1[3] = {a.ft1[3 * gp], a.ft1[3 * gp + 1], a.ft1[3 * gp + 2]};
+                const R t2[3] = {a.ft2[3 * gp], a.ft2[3 * gp + 1], a.ft2[3 * gp + 2]};
+                lxf_flux(ph, QL, QR, n, t1, t2, inv);
+            }
+            R visc[5] = {0, 0, 0, 0, 0};
+            if (MODE == kFluxNS) {
+                R gl[15], gr[15];
+#pragma unroll
+                for (int c = 0; c < 15; ++c) {
+                    gl[c] = XL[(5 + c) * NP + lane];
+                    gr[c] = XR[(5 + c) * NP + lane];
+                }
+                R mu, kap, FL[3][5], FR[3][5];
+                mu_kappa(ph, QL, mu, kap);
+                viscous_flux(ph, QL, gl, gl + 5, gl + 10, mu, kap, FL);
+                mu_kappa(ph, QR, mu, kap);
+                viscous_flux(ph, QR, gr, gr + 5, gr + 10, mu, kap, FR);
+#pragma unroll
+                for (int v = 0; v < 5; ++v)
+                    visc[v] = R(0.5) * (FL[0][v] + FR[0][v]) * n[0] + R(0.5) * (FL[1][v] + FR[1][v]) * n[1] +
+                              R(0.5) * (FL[2][v] + FR[2][v]) * n[2];
+            }
+#pragma unroll
+            for (int v = 0; v < 5; ++v) out[v] = (inv[v] - visc[v]) * J;
+        }
+    }
+    __syncthreads();  // the traces are consumed: SL holds the face values from here on
+    if (point) {
+#pragma unroll
+        for (int v = 0; v < NVOUT; ++v) SL[v * NP + lane] = out[v];
+    }
+    __syncthreads();
+    // projection to each side's order (transposed Tset), first direction into AL / AR
+    const bool pL1 = active && l1 != q1, pL2 = active && l2 != q2;
+    const bool pR1 = active && s1R != q1, pR2 = active && s2R != q2;
+    if (pL1) {
+        const R* T = a.tset + ((q1 - 1) * kMaxP + (l1 - 1)) * kTsetStride;
+        for (int p = lane; p < l1 * q2; p += NP) {
+            const int i = p % l1, l = p / l1;
+#pragma unroll
+            for (int v = 0; v < NVOUT; ++v) {
+                R acc = R(0);
+                for (int m = 0; m < q1; ++m) acc = acc + T[i * kMaxP + m] * SL[v * NP + m + q1 * l];
+                AL[v * NP + p] = acc;
+            }
+        }
+    }
+    if (pR1) {
+        const R* T = a.tset + ((q1 - 1) * kMaxP + (s1R - 1)) * kTsetStride;
+        for (int p = lane; p < s1R * q2; p += NP) {
+            const int i = p % s1R, l = p / s1R;
+#pragma unroll
+            for (int v = 0; v < NVOUT; ++v) {
+                R acc = R(0);
+                for (int m = 0; m < q1; ++m) acc = acc + T[i * kMaxP + m] * SL[v * NP + m + q1 * l];
+                AR[v * NP + p] = acc;
+            }
+        }
+    }
+    __syncthreads();
+    if (!active) return;
+    R* dstL = MODE == kJump ? a.UJ + offL * 15 : a.FS + offL * 5;
+    R* dstR = MODE == kJump ? a.UJ + offR * 15 : a.FS + offR * 5;
+    const R sign2 = MODE == kJump ? R(1) : R(-1);
+    {
+        const R* src = pL1 ? AL : SL;  // (l1 x q2) points
+        const R* T = a.tset + ((q2 - 1) * kMaxP + (l2 - 1)) * kTsetStride;
+        for (int p = lane; p < nL; p += NP) {
+            const int i = p % l1, j = p / l1;
+#pragma unroll
+            for (int v = 0; v < NVOUT; ++v) {
+                R val;
+                if (pL2) {
+                    val = R(0);
+                    for (int l = 0; l < q2; ++l) val = val + T[j * kMaxP + l] * src[v * NP + i + l1 * l];
+                } else {
+                    val = src[v * NP + i + l1 * j];
+                }
+                dstL[v * nL + p] = val;
+            }
+        }
+    }
+    {
+        const R* src = pR1 ? AR : SL;  // (s1R x q2) points
+        const R* T = a.tset + ((q2 - 1) * kMaxP + (s2R - 1)) * kTsetStride;
+        for (int p = lane; p < nR; p += NP) {
+            const int i = p % s1R, j = p / s1R;
+            int ii, jj;
+            left2right(i, j, s1R - 1, s2R - 1, rot, ii, jj);
+            const int o = ii + r1 * jj;
+#pragma unroll
+            for (int v = 0; v < NVOUT; ++v) {
+                R val;
+                if (pR2) {
+                    val = R(0);
+                    for (int l = 0; l < q2; ++l) val = val + T[j * kMaxP + l] * src[v * NP + i + s1R * l];
+                } else {
+                    val = src[v * NP + i + s1R * j];
+                }
+                dstR[v * nR + o] = sign2 * val;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// kv_update: surface integral, 1/J, source, RK3 stage update (per-case dt), traces of the new Q.
+// ------------------------------------------------------------------------------------------------
+template <typename R, bool SRC>
+__global__ void __launch_bounds__(256) kv_update(VArgs<R> a, int stage, double tshift, int write_qdot) {
+    extern __shared__ __align__(16) unsigned char vsm[];
+    const ItemDims d = item_dims(a.items[blockIdx.x]);
+    const int px = d.px, py = d.py, np = d.np, ntot = d.ntot;
+    OpsP<R>* sO = reinterpret_cast<OpsP<R>*>(vsm);
+    R* sQ = reinterpret_cast<R*>(sO + 3);
+    load_ops(a.ops, sO, px, py, d.pz);
+    __syncthreads();
+    const CaseConst cc = a.cc[d.kase];
+    const double dt = stage >= 0 ? a.dt[d.kase] : 0.0;
+    const double ak = stage == 0 ? 0.0 : (stage == 1 ? -5.0 / 9.0 : -153.0 / 128.0);
+    const double ck = stage == 0 ? 1.0 / 3.0 : (stage == 1 ? 15.0 / 16.0 : 8.0 / 15.0);
+    const int A = px * d.pz, B = px * py, C = py * d.pz;
+    for (int t = threadIdx.x; t < ntot; t += blockDim.x) {
+        const int le = t / np, n = t - le * np;
+        const int i = n % px, j = (n / px) % py, k = n / (px * py);
+        const int e = a.item_elems[d.first + le];
+        const long long g = a.eoff[e] + n;
+        const long long s0 = 6LL * e;
+        const R* FF = a.FS + a.soff[s0 + 0] * 5 + (i + px * k);
+        const R* FB = a.FS + a.soff[s0 + 1] * 5 + (i + px * k);
+        const R* FO = a.FS + a.soff[s0 + 2] * 5 + (i + px * j);
+        const R* FR = a.FS + a.soff[s0 + 3] * 5 + (j + py * k);
+        const R* FT = a.FS + a.soff[s0 + 4] * 5 + (i + px * j);
+        const R* FL = a.FS + a.soff[s0 + 5] * 5 + (j + py * k);
+        const R bxl = sO[0].bL[i], bxr = sO[0].bR[i], byl = sO[1].bL[j], byr = sO[1].bR[j];
+        const R bzl = sO[2].bL[k], bzr = sO[2].bR[k];
+        const R J = a.jac[g];
+        R qd[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+            R fi = FL[v * C] * bxl;
+            fi = fi + FR[v * C] * bxr;
+            fi = fi + FF[v * A] * byl;
+            fi = fi + FB[v * A] * byr;
+            fi = fi + FO[v * B] * bzl;
+            fi = fi + FT[v * B] * bzr;
+            qd[v] = (a.QDot[5 * g + v] - fi) / J;
+        }
+        if (SRC) {
+            double S[5];
+            const double tt = a.time[d.kase] + tshift * dt;
+            mms_source(a.x[3 * g], a.x[3 * g + 1], a.x[3 * g + 2], tt, cc.gm1, cc.gM2, cc.mu, cc.kappa, S);
+#pragma unroll
+            for (int v = 0; v < 5; ++v) qd[v] = R(double(qd[v]) + S[v]);
+        }
+        if (write_qdot) {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) a.QDot[5 * g + v] = qd[v];
+        }
+        if (stage >= 0) {
+            const double cdt = ck * dt;
+            double qq[5];
+#pragma unroll
+            for (int v = 0; v < 5; ++v) {
+                const double gq = ak * a.G[5 * g + v] + double(qd[v]);
+                qq[v] = a.Q[5 * g + v] + cdt * gq;
+                a.G[5 * g + v] = gq;
+                a.Q[5 * g + v] = qq[v];
+            }
+#pragma unroll
+            for (int v = 0; v < 4; ++v) sQ[v * ntot + t] = R(qq[v]);
+            sQ[4 * ntot + t] = R(qq[4] - cc.e_ref);
+        }
+    }
+    if (stage < 0) return;
+    __syncthreads();
+    write_traces<R, 5>(a, d, sO, sQ, a.QF);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Per-case reductions: CFL time step (MaxTimeStep with per-direction node spacing, DGSEMClass.f90:
+// 870-1038) and residuals (ComputeMaxResiduals / checkForNan). red holds 8 words per case:
+// [0] convective dt, [1] viscous dt, [2..6] max |QDot| per variable (bit images).
+// ------------------------------------------------------------------------------------------------
+struct VDtArgs {
+    const int4* items;
+    const int* item_elems;
+    const long long* eoff;
+    const double* Q;
+    const double* dxi;       // [kMaxP + 1]: 1/|x_1 - x_0| of the node set with P nodes
+    const double* gamma_M2;  // per case: gamma M^2
+    double cfl, dcfl, gamma, gm1, S_div_TRef, TReNorm;
+    int ns;
+    unsigned long long* red;
+};
+
+template <typename R>
+__global__ void __launch_bounds__(256) kv_max_dt(VDtArgs d, const R* ja_xi, const R* ja_eta, const R* ja_zeta,
+                                                 const R* jac) {
+    const ItemDims it = item_dims(d.items[blockIdx.x]);
+    const double dx[3] = {d.dxi[it.px], d.dxi[it.py], d.dxi[it.pz]};
+    const double gM2 = d.gamma_M2[it.kase];
+    double conv = 1.0e300, visc = 1.0e300;
+    for (int t = threadIdx.x; t < it.ntot; t += blockDim.x) {
+        const int le = t / it.np, n = t - le * it.np;
+        const long long g = d.eoff[d.item_elems[it.first + le]] + n;
+        const double* Q = d.Q + 5 * g;
+        const double p = d.gm1 * (Q[4] - 0.5 * (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) / Q[0]);
+        const double a = sqrt(d.gamma * p / Q[0]);
+        const double ev[3] = {fabs(Q[1] / Q[0]) + a, fabs(Q[2] / Q[0]) + a, fabs(Q[3] / Q[0]) + a};
+        const R* ja[3] = {ja_xi + 3 * g, ja_eta + 3 * g, ja_zeta + 3 * g};
+        const double J = fabs(double(jac[g]));
+        double lam = 0.0;
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+            lam += fabs(double(ja[r][0]) * ev[0] + double(ja[r][1]) * ev[1] + double(ja[r][2]) * ev[2]) * dx[r];
+        conv = fmin(conv, d.cfl * J / lam);
+        if (d.ns) {
+            const double T = gM2 * p / Q[0];
+            const double tt = T * d.TReNorm;
+            const double mu = (1.0 + d.S_div_TRef) / (tt + d.S_div_TRef) * tt * sqrt(tt);
+            double lv = 0.0;
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+                lv += mu * (dx[r] * dx[r]) * fabs(double(ja[r][0]) + double(ja[r][1]) + double(ja[r][2]));
+            visc = fmin(visc, d.dcfl * J / lv);
+        }
+    }
+    __shared__ double sc[8], sv[8];
+    for (int o = 16; o > 0; o >>= 1) {
+        conv = fmin(conv, __shfl_down_sync(0xffffffffu, conv, o));
+        visc = fmin(visc, __shfl_down_sync(0xffffffffu, visc, o));
+    }
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        sc[w] = conv;
+        sv[w] = visc;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 1; q < static_cast<int>(blockDim.x >> 5); ++q) {
+            conv = fmin(conv, sc[q]);
+            visc = fmin(visc, sv[q]);
+        }
+        atomicMin(&d.red[8 * it.kase], dbits(conv));
+        atomicMin(&d.red[8 * it.kase + 1], dbits(visc));
+    }
+}
+
+// dt of every case = min(convective, viscous); resets the dt slots.
+static __global__ void kv_dt_final(unsigned long long* red, double* dt, int n_cases) {
+    for (int c = threadIdx.x; c < n_cases; c += blockDim.x) {
+        const double conv = __longlong_as_double(static_cast<long long>(red[8 * c]));
+        const double visc = __longlong_as_double(static_cast<long long>(red[8 * c + 1]));
+        dt[c] = conv < visc ? conv : visc;
+        red[8 * c] = dbits(1.0e300);
+        red[8 * c + 1] = dbits(1.0e300);
+    }
+}
+
+static __global__ void kv_advance_time(double* t, const double* dt, int n_cases) {
+    for (int c = threadIdx.x; c < n_cases; c += blockDim.x) t[c] = t[c] + dt[c];
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) kv_residuals(const int4* items, const int* item_elems, const long long* eoff,
+                                                    const R* qdot, const double* Q, unsigned long long* red,
+                                                    int* nan_flag) {
+    const ItemDims it = item_dims(items[blockIdx.x]);
+    double m[5] = {0, 0, 0, 0, 0};
+    int bad = 0;
+    for (int t = threadIdx.x; t < it.ntot; t += blockDim.x) {
+        const int le = t / it.np, n = t - le * it.np;
+        const long long g = eoff[item_elems[it.first + le]] + n;
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+            m[v] = fmax(m[v], fabs(double(qdot[5 * g + v])));
+            const double q = Q[5 * g + v];
+            if (!(q == q) || fabs(q) > 1.7976931348623157e308) bad = 1;
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v)
+        for (int o = 16; o > 0; o >>= 1) m[v] = fmax(m[v], __shfl_down_sync(0xffffffffu, m[v], o));
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) atomicMax(&red[8 * it.kase + 2 + v], dbits(m[v]));
+    }
+    if (bad) atomicOr(&nan_flag[it.kase], 1);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Launch wrappers
+// ------------------------------------------------------------------------------------------------
+template <typename R>
+size_t vitem_smem(int cap, int nv) {
+    return 3 * sizeof(OpsP<R>) + static_cast<size_t>(nv) * cap * sizeof(R);
+}
+
+template <typename R>
+using VStageFn = cudaError_t (*)(const VArgs<R>& a, int stage, double tshift, int flags, cudaStream_t s);
+
+template <typename R>
+using VTimesFn = cudaError_t (*)(const VArgs<R>& a, int reps, cudaStream_t s, double* ms);
+
+template <typename R, int MODE>
+cudaError_t launch_face(const VArgs<R>& a, cudaStream_t s) {
+    using Cfg = FaceCfg<R, MODE>;
+    const int blocks = (a.n_faces + Cfg::FPB - 1) / Cfg::FPB;
+    kv_face<R, MODE><<<blocks, Cfg::THREADS, Cfg::SMEM, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t vrun_stage(const VArgs<R>& a, int stage, double tshift, int flags, cudaStream_t s) {
+    const size_t vol = vitem_smem<R>(a.cap, 20), upd = vitem_smem<R>(a.cap, 5);
+    if (stage == kPrepare) {
+        cudaError_t e;
+        if ((e = cudaFuncSetAttribute(kv_volume<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(vol))) ||
+            (e = cudaFuncSetAttribute(kv_update<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(upd))) ||
+            (e = cudaFuncSetAttribute(kv_update<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(upd))) ||
+            (e = cudaFuncSetAttribute(kv_traces<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(upd))) ||
+            (e = cudaFuncSetAttribute(kv_face<R, kJump>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(FaceCfg<R, kJump>::SMEM))) ||
+            (e = cudaFuncSetAttribute(kv_face<R, kFluxEuler>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(FaceCfg<R, kFluxEuler>::SMEM))) ||
+            (e = cudaFuncSetAttribute(kv_face<R, kFluxNS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(FaceCfg<R, kFluxNS>::SMEM))))
+            return e;
+        return cudaSuccess;
+    }
+    if (stage == kTraces) {
+        kv_traces<R><<<a.n_items, 256, upd, s>>>(a);
+        return cudaGetLastError();
+    }
+    cudaError_t e;
+    if (a.ns && (e = launch_face<R, kJump>(a, s)) != cudaSuccess) return e;
+    kv_volume<R><<<a.n_items, 256, vol, s>>>(a, flags & kStoreGrad);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = a.ns ? launch_face<R, kFluxNS>(a, s) : launch_face<R, kFluxEuler>(a, s)) != cudaSuccess) return e;
+    const int wq = (flags & kWriteQDot) ? 1 : 0;
+    if (a.source) kv_update<R, true><<<a.n_items, 256, upd, s>>>(a, stage, tshift, wq);
+    else kv_update<R, false><<<a.n_items, 256, upd, s>>>(a, stage, tshift, wq);
+    return cudaGetLastError();
+}
+
+// Average device time of each kernel alone: ms[0] volume, [1] face flux, [2] update (stage 1),
+// [3] traces, [4] BR1 jump faces.
+template <typename R>
+cudaError_t vkernel_times(const VArgs<R>& a, int reps, cudaStream_t s, double* ms) {
+    const size_t vol = vitem_smem<R>(a.cap, 20), upd = vitem_smem<R>(a.cap, 5);
+    cudaEvent_t e0, e1;
+    cudaError_t err = cudaEventCreate(&e0);
+    if (err != cudaSuccess) return err;
+    if ((err = cudaEventCreate(&e1)) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return err;
+    }
+    for (int kk = 0; kk < 5; ++kk) {
+        if (kk == 4 && !a.ns) {
+            ms[kk] = 0.0;
+            continue;
+        }
+        cudaEventRecord(e0, s);
+        for (int r = 0; r < reps; ++r) {
+            switch (kk) {
+                case 0: kv_volume<R><<<a.n_items, 256, vol, s>>>(a, 0); break;
+                case 1: a.ns ? launch_face<R, kFluxNS>(a, s) : launch_face<R, kFluxEuler>(a, s); break;
+                case 2: kv_update<R, false><<<a.n_items, 256, upd, s>>>(a, 1, 1.0 / 3.0, 0); break;
+                case 3: kv_traces<R><<<a.n_items, 256, upd, s>>>(a); break;
+                default: launch_face<R, kJump>(a, s); break;
+            }
+        }
+        cudaEventRecord(e1, s);
+        if ((err = cudaEventSynchronize(e1)) != cudaSuccess) break;
+        float t = 0.f;
+        cudaEventElapsedTime(&t, e0, e1);
+        ms[kk] = reps > 0 ? t / reps : 0.0;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (err != cudaSuccess) return err;
+    return cudaGetLastError();
+}
+
+// Resolved in the instantiation translation units.
+VStageFn<double> vstage_fn_fp64();
+VStageFn<float> vstage_fn_fp32();
+VTimesFn<double> vtimes_fn_fp64();
+VTimesFn<float> vtimes_fn_fp32();
+
+}  // namespace dg

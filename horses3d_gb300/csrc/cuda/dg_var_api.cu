@@ -1,0 +1,511 @@
+// Variable-order (p-anisotropic) and multi-case contexts: host set-up of the work items, slot and
+// face tables, operator and Tset tables, and the per-case reductions. The public entry points of
+// dg_api.cu dispatch here when a context holds anisotropic orders or several cases.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../host/spectral.hpp"
+#include "dg_context.cuh"
+
+using h3dctx::cuda_fail;
+
+namespace {
+
+constexpr int kItemNodes = 256;  // nodes per work item (one element when it holds more)
+
+int side_count(int side, const int32_t* ord) {
+    const int px = ord[0] + 1, py = ord[1] + 1, pz = ord[2] + 1;
+    switch (side) {
+        case 1: case 2: return px * pz;
+        case 3: case 5: return px * py;
+        default: return py * pz;
+    }
+}
+
+void side_orders(int side, const int32_t* ord, int& n1, int& n2) {
+    switch (side) {
+        case 1: case 2: n1 = ord[0]; n2 = ord[2]; break;
+        case 3: case 5: n1 = ord[0]; n2 = ord[1]; break;
+        default: n1 = ord[1]; n2 = ord[2]; break;
+    }
+}
+
+int validate_case(const dg_mesh_desc* m, const dg_physics* ph, int c) {
+    const std::string tag = "case " + std::to_string(c) + ": ";
+    if (m->n_elements < 1 || m->n_faces < 1) return h3d::fail(DG_ERR_INVALID, tag + "empty mesh");
+    if (!m->order || !m->x || !m->ja_xi || !m->ja_eta || !m->ja_zeta || !m->jacobian || !m->inv_jacobian ||
+        !m->face_elem || !m->face_side || !m->face_rotation || !m->face_nf || !m->face_normal || !m->face_t1 ||
+        !m->face_t2 || !m->face_jacobian)
+        return h3d::fail(DG_ERR_INVALID, tag + "mesh description has a null array");
+    if (m->node_type != DG_NODES_GAUSS && m->node_type != DG_NODES_GAUSS_LOBATTO)
+        return h3d::fail(DG_ERR_INVALID, tag + "unknown node type");
+    for (int e = 0; e < m->n_elements; ++e)
+        for (int d = 0; d < 3; ++d)
+            if (m->order[3 * e + d] < 1 || m->order[3 * e + d] + 1 > dg::kMaxP)
+                return h3d::fail(DG_ERR_UNSUPPORTED, tag + "polynomial order outside 1..7");
+    if (2 * static_cast<int64_t>(m->n_faces) != 6 * static_cast<int64_t>(m->n_elements))
+        return h3d::fail(DG_ERR_UNSUPPORTED, tag + "boundary faces are not supported (periodic/interior meshes only)");
+    for (int f = 0; f < m->n_faces; ++f) {
+        if (m->face_rotation[f] < 0 || m->face_rotation[f] > 7)
+            return h3d::fail(DG_ERR_INVALID, tag + "face rotation outside 0..7");
+        int dims[2][2];
+        for (int s = 0; s < 2; ++s) {
+            const int e = m->face_elem[2 * f + s], side = m->face_side[2 * f + s];
+            if (e < 0 || e >= m->n_elements || side < 1 || side > 6)
+                return h3d::fail(DG_ERR_INVALID, tag + "face connectivity out of range");
+            side_orders(side, m->order + 3 * e, dims[s][0], dims[s][1]);
+        }
+        const int r = m->face_rotation[f];
+        if (!(r == 0 || r == 2 || r == 5 || r == 7)) std::swap(dims[1][0], dims[1][1]);
+        for (int a = 0; a < 2; ++a)
+            if (m->face_nf[2 * f + a] != std::max(dims[0][a], dims[1][a]))
+                return h3d::fail(DG_ERR_INVALID, tag + "face order is not the larger of its two sides' orders");
+    }
+    if (ph->mach <= 0.0) return h3d::fail(DG_ERR_INVALID, tag + "Mach number must be positive");
+    if (ph->navier_stokes && ph->reynolds <= 0.0) return h3d::fail(DG_ERR_INVALID, tag + "Reynolds number must be positive");
+    return DG_OK;
+}
+
+dg::PhysConst phys_const(const dg_physics* ph, const dg_options* op) {
+    // PhysicsStorage_NS.f90:186-290,413-429 (air, Sutherland defaults)
+    dg::PhysConst pc{};
+    pc.gamma = 1.4;
+    pc.gm1 = 1.4 - 1.0;
+    pc.gammaM2 = pc.gamma * (ph->mach * ph->mach);
+    pc.ns = ph->navier_stokes ? 1 : 0;
+    if (pc.ns) {
+        pc.mu = 1.0 / ph->reynolds;
+        pc.kappa = 1.0 / (pc.gm1 * (ph->mach * ph->mach) * ph->reynolds * ph->prandtl);
+        pc.mu_to_kappa = 1.0 / (pc.gm1 * (ph->mach * ph->mach) * ph->prandtl);
+    }
+    const double TRef = 520.0 * 5.0 / 9.0;
+    pc.S_div_TRef = (198.6 * 5.0 / 9.0) / TRef;
+    pc.TReNorm = TRef / TRef;
+    pc.lambda_stab = op->lambda_stab;
+    pc.riemann = op->riemann;
+    pc.averaging = op->averaging;
+    pc.inviscid = op->inviscid;
+    pc.source = op->source;
+    return pc;
+}
+
+template <typename R>
+cudaError_t upload_as(h3dctx::DevBuf<R>& dst, const std::vector<double>& src, cudaStream_t s) {
+    std::vector<R> tmp(src.size());
+    for (size_t i = 0; i < src.size(); ++i) tmp[i] = static_cast<R>(src[i]);
+    return dst.upload(tmp.data(), tmp.size(), s);
+}
+
+// Host copies of the concatenated case data, kept only during set-up.
+struct Gathered {
+    std::vector<double> ja_xi, ja_eta, ja_zeta, jac, inv_jac, x, fn, ft1, ft2, fj;
+    int64_t slot_points = 0;
+};
+
+template <typename R>
+int setup_vstore(dg_ctx* c, h3dctx::VStore<R>& st, const Gathered& h) {
+    cudaStream_t s = c->stream;
+    const size_t nd = static_cast<size_t>(c->ndof);
+    const size_t sp = static_cast<size_t>(h.slot_points);
+    CK(upload_as(st.ja_xi, h.ja_xi, s));
+    CK(upload_as(st.ja_eta, h.ja_eta, s));
+    CK(upload_as(st.ja_zeta, h.ja_zeta, s));
+    CK(upload_as(st.jac, h.jac, s));
+    CK(upload_as(st.inv_jac, h.inv_jac, s));
+    CK(upload_as(st.fn, h.fn, s));
+    CK(upload_as(st.ft1, h.ft1, s));
+    CK(upload_as(st.ft2, h.ft2, s));
+    CK(upload_as(st.fj, h.fj, s));
+    // operators per node count and Tset per (origin, destination) order
+    std::vector<dg::OpsP<R>> ops(dg::kMaxP + 1);
+    std::memset(ops.data(), 0, sizeof(dg::OpsP<R>) * ops.size());
+    for (int P = 2; P <= dg::kMaxP; ++P) {
+        const h3d::NodalStorage& ns = h3d::nodal_storage(c->nodes, P - 1);
+        for (int i = 0; i < P; ++i) {
+            for (int l = 0; l < P; ++l) {
+                ops[P].D[i * dg::kMaxP + l] = static_cast<R>(ns.D[i * P + l]);
+                ops[P].hatD[i * dg::kMaxP + l] = static_cast<R>(ns.hatD[i * P + l]);
+            }
+            ops[P].vL[i] = static_cast<R>(ns.vL[i]);
+            ops[P].vR[i] = static_cast<R>(ns.vR[i]);
+            ops[P].bL[i] = static_cast<R>(ns.bL[i]);
+            ops[P].bR[i] = static_cast<R>(ns.bR[i]);
+        }
+    }
+    CK(st.ops.upload(ops.data(), ops.size(), s));
+    std::vector<double> ts(static_cast<size_t>(dg::kMaxP) * dg::kMaxP * dg::kTsetStride, 0.0);
+    for (int No = 1; No < dg::kMaxP; ++No)
+        for (int Nd = 1; Nd < dg::kMaxP; ++Nd) {
+            const std::vector<double> T = h3d::interpolation_matrix(c->nodes, No, Nd);
+            double* o = ts.data() + (No * dg::kMaxP + Nd) * dg::kTsetStride;
+            for (int i = 0; i <= Nd; ++i)
+                for (int j = 0; j <= No; ++j) o[i * dg::kMaxP + j] = T[i * (No + 1) + j];
+        }
+    CK(upload_as(st.tset, ts, s));
+    std::vector<dg::PhysR<R>> ph(c->n_cases);
+    for (int k = 0; k < c->n_cases; ++k) ph[k] = dg::make_phys<R>(c->case_pc[k]);
+    CK(st.ph.upload(ph.data(), ph.size(), s));
+    const bool ns = c->pc.ns != 0;
+    CK(st.QDot.alloc(5 * nd));
+    CK(cudaMemsetAsync(st.QDot.p, 0, sizeof(R) * 5 * nd, s));
+    CK(st.Ux.alloc(ns ? 5 * nd : 0));
+    CK(st.Uy.alloc(ns ? 5 * nd : 0));
+    CK(st.Uz.alloc(ns ? 5 * nd : 0));
+    CK(st.QF.alloc(5 * sp));
+    CK(st.GF.alloc(ns ? 15 * sp : 0));
+    CK(st.UJ.alloc(ns ? 15 * sp : 0));
+    CK(st.FS.alloc(5 * sp));
+
+    dg::VArgs<R>& a = st.args;
+    std::memset(&a, 0, sizeof(a));
+    a.n_items = c->n_items;
+    a.n_faces = c->F;
+    a.ns = c->pc.ns;
+    a.source = c->opt.source;
+    a.items = c->items.p;
+    a.item_elems = c->item_elems.p;
+    a.eord = c->eord.p;
+    a.eoff = c->eoff.p;
+    a.soff = c->soff.p;
+    a.faces = c->faces4.p;
+    a.foff = c->foff.p;
+    a.ops = st.ops.p;
+    a.tset = st.tset.p;
+    a.ph = st.ph.p;
+    a.cc = c->cc.p;
+    a.time = c->scal.p;
+    a.dt = c->scal.p + c->n_cases;
+    a.ja_xi = st.ja_xi.p; a.ja_eta = st.ja_eta.p; a.ja_zeta = st.ja_zeta.p;
+    a.jac = st.jac.p; a.inv_jac = st.inv_jac.p;
+    a.x = c->x.p;
+    a.fn = st.fn.p; a.ft1 = st.ft1.p; a.ft2 = st.ft2.p; a.fj = st.fj.p;
+    a.Q = c->Q.p; a.G = c->G.p; a.QDot = st.QDot.p;
+    a.Ux = st.Ux.p; a.Uy = st.Uy.p; a.Uz = st.Uz.p;
+    a.QF = st.QF.p; a.GF = st.GF.p; a.UJ = st.UJ.p; a.FS = st.FS.p;
+    return DG_OK;
+}
+
+}  // namespace
+
+namespace h3dvar {
+
+bool needs_variable_path(const dg_mesh_desc* m) {
+    if (!m || !m->order || m->n_elements < 1) return false;
+    const int N = m->order[0];
+    for (int e = 0; e < m->n_elements; ++e)
+        for (int d = 0; d < 3; ++d)
+            if (m->order[3 * e + d] != N) return true;
+    return false;
+}
+
+int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, const dg_options* op, dg_ctx** out) {
+    if (!out) return h3d::fail(DG_ERR_INVALID, "null output pointer");
+    *out = nullptr;
+    if (n_cases < 1 || !meshes || !phys || !op) return h3d::fail(DG_ERR_INVALID, "null argument or no case");
+    if (op->inviscid != DG_INVISCID_STANDARD)
+        return h3d::fail(DG_ERR_UNSUPPORTED, "the variable-order path implements the standard (weak) volume form");
+    if (op->riemann != DG_RIEMANN_ROE && op->riemann != DG_RIEMANN_LXF) return h3d::fail(DG_ERR_UNSUPPORTED, "riemann solver");
+    if (op->averaging != DG_AVG_STANDARD && op->averaging != DG_AVG_PIROZZOLI)
+        return h3d::fail(DG_ERR_UNSUPPORTED, "averaging");
+    if (op->precision != DG_PRECISION_FP64 && op->precision != DG_PRECISION_MIXED)
+        return h3d::fail(DG_ERR_UNSUPPORTED, "precision");
+    if (op->source != DG_SOURCE_NONE && op->source != DG_SOURCE_MMS_CONVERGENCE)
+        return h3d::fail(DG_ERR_UNSUPPORTED, "source");
+    for (int k = 0; k < n_cases; ++k) {
+        int rc = validate_case(&meshes[k], &phys[k], k);
+        if (rc) return rc;
+        if (meshes[k].node_type != meshes[0].node_type)
+            return h3d::fail(DG_ERR_UNSUPPORTED, "all cases of a batch need the same node type");
+        if ((phys[k].navier_stokes != 0) != (phys[0].navier_stokes != 0))
+            return h3d::fail(DG_ERR_UNSUPPORTED, "all cases of a batch need the same equations (Euler or NS)");
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return h3d::fail(DG_ERR_NODEVICE, "no CUDA device visible");
+
+    auto* c = new dg_ctx();
+    auto bail = [&](int code) {
+        dg_destroy(c);
+        return code;
+    };
+    c->var = true;
+    c->n_cases = n_cases;
+    c->phys = phys[0];
+    c->opt = *op;
+    c->nodes = meshes[0].node_type;
+    c->mixed = op->precision == DG_PRECISION_MIXED;
+    c->pc = phys_const(&phys[0], op);
+    c->case_pc.resize(n_cases);
+    c->case_const.resize(n_cases);
+    for (int k = 0; k < n_cases; ++k) {
+        c->case_pc[k] = phys_const(&phys[k], op);
+        const dg::PhysConst& pc = c->case_pc[k];
+        c->case_const[k] = dg::CaseConst{0.0, pc.gm1, pc.gammaM2, pc.mu, pc.kappa};
+    }
+
+    // element, slot and face tables of the concatenated cases
+    std::vector<int> eord;
+    std::vector<long long> eoff, soff, foff;
+    std::vector<int4> faces;
+    std::vector<int> ecase;
+    Gathered h;
+    c->case_ndof_off.assign(n_cases + 1, 0);
+    int64_t nodes = 0, spts = 0, fpts = 0;
+    int kbase = 0;
+    for (int k = 0; k < n_cases; ++k) {
+        const dg_mesh_desc& m = meshes[k];
+        int64_t case_nodes = 0;
+        for (int e = 0; e < m.n_elements; ++e) {
+            const int32_t* o = m.order + 3 * e;
+            eord.push_back((o[0] + 1) | ((o[1] + 1) << 8) | ((o[2] + 1) << 16));
+            eoff.push_back(nodes + case_nodes);
+            ecase.push_back(k);
+            case_nodes += static_cast<int64_t>(o[0] + 1) * (o[1] + 1) * (o[2] + 1);
+            for (int side = 1; side <= 6; ++side) {
+                soff.push_back(spts);
+                spts += side_count(side, o);
+            }
+        }
+        auto append = [](std::vector<double>& dst, const double* src, int64_t n) { dst.insert(dst.end(), src, src + n); };
+        append(h.ja_xi, m.ja_xi, 3 * case_nodes);
+        append(h.ja_eta, m.ja_eta, 3 * case_nodes);
+        append(h.ja_zeta, m.ja_zeta, 3 * case_nodes);
+        append(h.jac, m.jacobian, case_nodes);
+        append(h.inv_jac, m.inv_jacobian, case_nodes);
+        append(h.x, m.x, 3 * case_nodes);
+        int64_t case_fpts = 0;
+        std::vector<int> seen(6 * static_cast<size_t>(m.n_elements), 0);
+        for (int f = 0; f < m.n_faces; ++f) {
+            const int q1 = m.face_nf[2 * f] + 1, q2 = m.face_nf[2 * f + 1] + 1;
+            for (int s = 0; s < 2; ++s) {
+                int& mark = seen[6 * static_cast<size_t>(m.face_elem[2 * f + s]) + m.face_side[2 * f + s] - 1];
+                if (mark) return bail(h3d::fail(DG_ERR_INVALID, "an element side belongs to two faces"));
+                mark = 1;
+            }
+            int4 fd;
+            fd.x = kbase + m.face_elem[2 * f];
+            fd.y = kbase + m.face_elem[2 * f + 1];
+            fd.z = m.face_side[2 * f] | (m.face_side[2 * f + 1] << 4) | (m.face_rotation[f] << 8) | (q1 << 12) | (q2 << 16);
+            fd.w = k;
+            faces.push_back(fd);
+            foff.push_back(fpts + case_fpts);
+            case_fpts += static_cast<int64_t>(q1) * q2;
+        }
+        append(h.fn, m.face_normal, 3 * case_fpts);
+        append(h.ft1, m.face_t1, 3 * case_fpts);
+        append(h.ft2, m.face_t2, 3 * case_fpts);
+        append(h.fj, m.face_jacobian, case_fpts);
+        nodes += case_nodes;
+        fpts += case_fpts;
+        kbase += m.n_elements;
+        c->case_ndof_off[k + 1] = nodes;
+    }
+    c->K = kbase;
+    c->F = static_cast<int>(faces.size());
+    c->ndof = nodes;
+    h.slot_points = spts;
+
+    // work items: elements bucketed by (case, order triple), heaviest buckets first
+    std::map<std::tuple<int, int, int>, std::vector<int>> buckets;  // (-np, case, ord) -> elements
+    for (int e = 0; e < c->K; ++e) {
+        const int o = eord[e];
+        const int np = (o & 255) * ((o >> 8) & 255) * ((o >> 16) & 255);
+        buckets[std::make_tuple(-np, ecase[e], o)].push_back(e);
+    }
+    std::vector<int4> items;
+    std::vector<int> item_elems;
+    int cap = 0;
+    for (const auto& b : buckets) {
+        const int np = -std::get<0>(b.first);
+        const int per = std::max(1, kItemNodes / np);
+        const std::vector<int>& els = b.second;
+        for (size_t i0 = 0; i0 < els.size(); i0 += per) {
+            const int cnt = static_cast<int>(std::min<size_t>(per, els.size() - i0));
+            int4 it;
+            it.x = static_cast<int>(item_elems.size());
+            it.y = cnt;
+            it.z = std::get<2>(b.first);
+            it.w = std::get<1>(b.first);
+            items.push_back(it);
+            for (int q = 0; q < cnt; ++q) item_elems.push_back(els[i0 + q]);
+            cap = std::max(cap, cnt * np);
+        }
+    }
+    c->n_items = static_cast<int>(items.size());
+
+    cudaError_t e;
+    if ((e = cudaGetDevice(&c->device)) != cudaSuccess) return bail(cuda_fail(e, "cudaGetDevice"));
+    if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return bail(cuda_fail(e, "cudaStreamCreate"));
+    if ((e = cudaMallocHost(reinterpret_cast<void**>(&c->h_scal), sizeof(double) * (4 * n_cases + 8))) != cudaSuccess)
+        return bail(cuda_fail(e, "cudaMallocHost"));
+    cudaStream_t s = c->stream;
+    const size_t nd = static_cast<size_t>(c->ndof);
+    if ((e = c->Q.alloc(5 * nd)) || (e = c->G.alloc(5 * nd)) || (e = c->scal.alloc(2 * n_cases)) ||
+        (e = c->red.alloc(8 * n_cases)) || (e = c->vnan.alloc(n_cases)) || (e = c->nan_flag.alloc(1)))
+        return bail(cuda_fail(e, "alloc state"));
+    if ((e = cudaMemsetAsync(c->Q.p, 0, sizeof(double) * 5 * nd, s)) ||
+        (e = cudaMemsetAsync(c->G.p, 0, sizeof(double) * 5 * nd, s)) ||
+        (e = cudaMemsetAsync(c->scal.p, 0, sizeof(double) * 2 * n_cases, s)))
+        return bail(cuda_fail(e, "clear state"));
+    {
+        std::vector<unsigned long long> init(8 * static_cast<size_t>(n_cases), 0ull);
+        const double big = 1.0e300;
+        unsigned long long bb;
+        std::memcpy(&bb, &big, 8);
+        for (int k = 0; k < n_cases; ++k) init[8 * k] = init[8 * k + 1] = bb;
+        if ((e = c->red.upload(init.data(), init.size(), s)) != cudaSuccess) return bail(cuda_fail(e, "init reductions"));
+    }
+    if ((e = c->x.upload(h.x.data(), h.x.size(), s)) || (e = c->items.upload(items.data(), items.size(), s)) ||
+        (e = c->item_elems.upload(item_elems.data(), item_elems.size(), s)) ||
+        (e = c->eord.upload(eord.data(), eord.size(), s)) || (e = c->eoff.upload(eoff.data(), eoff.size(), s)) ||
+        (e = c->soff.upload(soff.data(), soff.size(), s)) || (e = c->faces4.upload(faces.data(), faces.size(), s)) ||
+        (e = c->foff.upload(foff.data(), foff.size(), s)) ||
+        (e = c->cc.upload(c->case_const.data(), c->case_const.size(), s)))
+        return bail(cuda_fail(e, "upload tables"));
+    {
+        std::vector<double> dxi(dg::kMaxP + 1, 0.0), gm2(n_cases);
+        for (int P = 2; P <= dg::kMaxP; ++P) {
+            const h3d::NodalStorage& ns = h3d::nodal_storage(c->nodes, P - 1);
+            dxi[P] = 1.0 / std::fabs(ns.x[1] - ns.x[0]);
+        }
+        for (int k = 0; k < n_cases; ++k) gm2[k] = c->case_pc[k].gammaM2;
+        if ((e = c->dxi_table.upload(dxi.data(), dxi.size(), s)) || (e = c->gamma_M2.upload(gm2.data(), gm2.size(), s)))
+            return bail(cuda_fail(e, "upload dt tables"));
+    }
+    int rc;
+    if (c->mixed) {
+        if ((rc = setup_vstore(c, c->v32, h))) return bail(rc);
+        c->v32.args.cap = cap;
+        c->v32.stage = dg::vstage_fn_fp32();
+        c->v32.times = dg::vtimes_fn_fp32();
+    } else {
+        if ((rc = setup_vstore(c, c->v64, h))) return bail(rc);
+        c->v64.args.cap = cap;
+        c->v64.stage = dg::vstage_fn_fp64();
+        c->v64.times = dg::vtimes_fn_fp64();
+    }
+    if ((e = stage(c, dg::kPrepare, 0.0, 0)) != cudaSuccess) return bail(cuda_fail(e, "kernel attributes"));
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return bail(cuda_fail(e, "set-up"));
+    *out = c;
+    return DG_OK;
+}
+
+void release(dg_ctx* c) {
+    c->v64.free();
+    c->v32.free();
+    for (auto* b : {&c->items, &c->faces4}) b->free();
+    for (auto* b : {&c->item_elems, &c->eord, &c->vnan}) b->free();
+    for (auto* b : {&c->eoff, &c->soff, &c->foff}) b->free();
+    c->cc.free();
+    c->dxi_table.free();
+    c->gamma_M2.free();
+}
+
+int upload(dg_ctx* c, const double* q) {
+    bool changed = false;
+    if (c->mixed) {  // energy reference of every case: the mean energy of its uploaded state
+        for (int k = 0; k < c->n_cases; ++k) {
+            const int64_t g0 = c->case_ndof_off[k], g1 = c->case_ndof_off[k + 1];
+            double sum = 0.0;
+            for (int64_t g = g0; g < g1; ++g) sum += q[5 * g + 4];
+            const double e_ref = sum / static_cast<double>(g1 - g0);
+            if (!std::isfinite(e_ref)) return h3d::fail(DG_ERR_NAN, "NaN or Inf in the uploaded state");
+            if (e_ref != c->case_const[k].e_ref) {
+                c->case_const[k].e_ref = e_ref;
+                changed = true;
+            }
+        }
+        if (changed) {
+            std::vector<dg::PhysR<float>> ph(c->n_cases);
+            for (int k = 0; k < c->n_cases; ++k) {
+                ph[k] = dg::make_phys<float>(c->case_pc[k]);
+                dg::set_reference_energy(ph[k], c->case_pc[k].gm1, c->case_const[k].e_ref);
+            }
+            CK(cudaMemcpyAsync(c->v32.ph.p, ph.data(), sizeof(ph[0]) * ph.size(), cudaMemcpyHostToDevice, c->stream));
+            CK(cudaMemcpyAsync(c->cc.p, c->case_const.data(), sizeof(dg::CaseConst) * c->n_cases, cudaMemcpyHostToDevice,
+                               c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+        }
+    }
+    CK(cudaMemcpyAsync(c->Q.p, q, sizeof(double) * 5 * c->ndof, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemsetAsync(c->G.p, 0, sizeof(double) * 5 * c->ndof, c->stream));
+    CK(stage(c, dg::kTraces, 0.0, 0));
+    CK(cudaStreamSynchronize(c->stream));
+    return DG_OK;
+}
+
+cudaError_t stage(dg_ctx* c, int st, double tshift, int flags) {
+    if (c->mixed) return c->v32.stage(c->v32.args, st, tshift, flags, c->stream);
+    return c->v64.stage(c->v64.args, st, tshift, flags, c->stream);
+}
+
+cudaError_t enqueue_max_dt(dg_ctx* c, double cfl, double dcfl) {
+    dg::VDtArgs d;
+    d.items = c->items.p;
+    d.item_elems = c->item_elems.p;
+    d.eoff = c->eoff.p;
+    d.Q = c->Q.p;
+    d.dxi = c->dxi_table.p;
+    d.gamma_M2 = c->gamma_M2.p;
+    d.cfl = cfl;
+    d.dcfl = dcfl;
+    d.gamma = c->pc.gamma;
+    d.gm1 = c->pc.gm1;
+    d.S_div_TRef = c->pc.S_div_TRef;
+    d.TReNorm = c->pc.TReNorm;
+    d.ns = c->pc.ns;
+    d.red = c->red.p;
+    if (c->mixed)
+        dg::kv_max_dt<float><<<c->n_items, 256, 0, c->stream>>>(d, c->v32.ja_xi.p, c->v32.ja_eta.p, c->v32.ja_zeta.p,
+                                                                 c->v32.jac.p);
+    else
+        dg::kv_max_dt<double><<<c->n_items, 256, 0, c->stream>>>(d, c->v64.ja_xi.p, c->v64.ja_eta.p, c->v64.ja_zeta.p,
+                                                                  c->v64.jac.p);
+    dg::kv_dt_final<<<1, 256, 0, c->stream>>>(c->red.p, c->scal.p + c->n_cases, c->n_cases);
+    return cudaGetLastError();
+}
+
+cudaError_t enqueue_advance_time(dg_ctx* c) {
+    dg::kv_advance_time<<<1, 256, 0, c->stream>>>(c->scal.p, c->scal.p + c->n_cases, c->n_cases);
+    return cudaGetLastError();
+}
+
+int residuals(dg_ctx* c, double* maxres, int* nan_case) {
+    for (int k = 0; k < c->n_cases; ++k)
+        CK(cudaMemsetAsync(c->red.p + 8 * k + 2, 0, 5 * sizeof(unsigned long long), c->stream));
+    CK(cudaMemsetAsync(c->vnan.p, 0, sizeof(int) * c->n_cases, c->stream));
+    if (c->mixed)
+        dg::kv_residuals<float><<<c->n_items, 256, 0, c->stream>>>(c->items.p, c->item_elems.p, c->eoff.p,
+                                                                    c->v32.QDot.p, c->Q.p, c->red.p, c->vnan.p);
+    else
+        dg::kv_residuals<double><<<c->n_items, 256, 0, c->stream>>>(c->items.p, c->item_elems.p, c->eoff.p,
+                                                                     c->v64.QDot.p, c->Q.p, c->red.p, c->vnan.p);
+    CK(cudaGetLastError());
+    std::vector<unsigned long long> bits(8 * static_cast<size_t>(c->n_cases));
+    std::vector<int> flags(c->n_cases);
+    CK(cudaMemcpyAsync(bits.data(), c->red.p, sizeof(unsigned long long) * bits.size(), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(flags.data(), c->vnan.p, sizeof(int) * flags.size(), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    int any = 0;
+    for (int k = 0; k < c->n_cases; ++k) {
+        for (int v = 0; v < 5; ++v) std::memcpy(&maxres[5 * k + v], &bits[8 * k + 2 + v], sizeof(double));
+        if (nan_case) nan_case[k] = flags[k];
+        any |= flags[k];
+    }
+    return any ? h3d::fail(DG_ERR_NAN, "NaN or Inf in Q") : DG_OK;
+}
+
+int kernel_times(dg_ctx* c, int reps, double* ms) {
+    if (c->mixed) CK(c->v32.times(c->v32.args, reps, c->stream, ms));
+    else CK(c->v64.times(c->v64.args, reps, c->stream, ms));
+    return DG_OK;
+}
+
+}  // namespace h3dvar

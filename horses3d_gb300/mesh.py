@@ -36,6 +36,10 @@ class HexMesh:
     def from_specmesh(cls, path: str, order, node_type: int = _abi.DG_NODES_GAUSS,
                       periodic: str = "front:back,bottom:top,left:right") -> "HexMesh":
         h = C.c_void_p()
+        if np.ndim(order) == 1 and len(order) == 3:  # one (Nx, Ny, Nz) for every element
+            with open(path) as fh:
+                n_elements = int(fh.readline().split()[1])  # header: nodes, elements, boundary order
+            order = np.tile(np.asarray(order, dtype=np.int32), (n_elements, 1))
         if np.ndim(order) == 0:
             rc = _abi.lib().h3d_mesh_read_specmesh(str(path).encode(), node_type, int(order), None,
                                                    periodic.encode(), C.byref(h))
@@ -87,6 +91,20 @@ class HexMesh:
     @property
     def volume(self) -> float:
         return float(_abi.lib().h3d_mesh_volume(self._h))
+
+    def quadrature_weights(self) -> np.ndarray:
+        """w_i w_j w_k J at every node, element by element (the volume quadrature of
+        MappedGeometry.f90:132-135), for any per-element orders."""
+        out = np.empty(self.ndof)
+        J = self.jacobian
+        local = np.concatenate([np.arange(n) for n in self.nodes_per_element]) if self.n_elements else np.zeros(0, int)
+        for key in {tuple(int(v) for v in o) for o in self.order}:
+            ws = [nodal_storage(self.node_type, n)[1] for n in key]
+            w3 = (ws[2][:, None, None] * ws[1][None, :, None] * ws[0][None, None, :]).reshape(-1)
+            for e in np.nonzero(np.all(self.order == key, axis=1))[0]:
+                s, t = self.elem_offset[e], self.elem_offset[e + 1]
+                out[s:t] = w3[local[s:t]] * J[s:t]
+        return out
 
     def uniform_order(self):
         """(N, N, N) when every element has the same isotropic order, else None."""

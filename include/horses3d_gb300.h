@@ -164,6 +164,30 @@ int dg_residuals(dg_ctx* ctx, double maxres[5], int* nan_found);
 /* Block until all work queued on the context's stream is done. */
 int dg_synchronize(dg_ctx* ctx);
 
+/* Batches of independent cases in one context (no reference counterpart: the reference runs one
+ * case per process). Every case has its own mesh (any orders), physics constants, time and dt;
+ * the options and the node type are shared. All cases are advanced by the same kernel launches
+ * (elements bucketed by order triple), each with its own dt. The state arrays of the single-case
+ * entry points (dg_upload_state, dg_download) hold the cases one after the other, case k starting
+ * at node dg_case_offset(ctx, k). On a batch, dg_rk3_step/dg_run_steps give every case the same
+ * t and dt, dg_max_dt returns the smallest case dt (each case keeps its own on the device) and
+ * dg_residuals the maximum over the cases. dg_create itself routes a mesh with anisotropic or
+ * element-varying orders to this path as a batch of one. */
+int dg_create_batch(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, const dg_options* opts,
+                    dg_ctx** out);
+int dg_batch_size(const dg_ctx* ctx);
+int64_t dg_case_offset(const dg_ctx* ctx, int k);                    /* k in 0..n_cases; -1 if out of range */
+int dg_batch_set_clock(dg_ctx* ctx, const double* t, const double* dt);   /* [n_cases] each */
+int dg_batch_get_clock(dg_ctx* ctx, double* t, double* dt);
+/* MaxTimeStep of every case into dt[n_cases]; the values also become the cases' device dt. */
+int dg_batch_max_dt(dg_ctx* ctx, double cfl, double dcfl, double* dt);
+/* Per-case residuals maxres[5*n_cases] and NaN flags nan_found[n_cases] (may be NULL). */
+int dg_batch_residuals(dg_ctx* ctx, double* maxres, int* nan_found);
+/* n RK3 steps of every case from its device clock (CUDA-graph replay). cfl > 0: every step takes
+ * each case's MaxTimeStep(cfl, dcfl); otherwise each case's current dt. ms (may be NULL) receives
+ * the device time measured with events on the context's stream. */
+int dg_batch_run_steps(dg_ctx* ctx, int n, double cfl, double dcfl, double* ms);
+
 /* Host-side mesh builder (HexMesh construction: Read_SpecMesh.f90:36-342, HexMesh.f90:356-736,
  * 2677-2990, MappedGeometry.f90:64-760). Produces a dg_mesh_desc whose arrays live in the mesh. */
 typedef struct h3d_mesh h3d_mesh;

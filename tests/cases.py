@@ -72,9 +72,32 @@ def ftassert_close(expected, actual, tol=1e-11):
 
 def quadrature_weights(mesh):
     """w_i w_j w_k J at every node (for rel-L2 norms)."""
-    from horses3d_gb300.mesh import nodal_storage
+    return mesh.quadrature_weights()
 
-    n = mesh.uniform_order()
-    _, w, _ = nodal_storage(mesh.node_type, n)
-    w3 = (w[None, None, :] * w[None, :, None] * w[:, None, None]).reshape(-1)
-    return (mesh.jacobian.reshape(mesh.n_elements, -1) * w3[None, :]).reshape(-1)
+
+def random_orders(n_elements, lo, hi, seed):
+    """(Nx, Ny, Nz) per element drawn i.i.d. uniform from {lo..hi} (numpy PCG64 with the seed)."""
+    return np.random.default_rng(seed).integers(lo, hi + 1, size=(n_elements, 3)).astype(np.int32)
+
+
+def aniso_tgv_case(n=3, lo=1, hi=4, seed=1, nodes=_abi.DG_NODES_GAUSS, riemann=_abi.DG_RIEMANN_ROE, warp=0.0,
+                   mach=0.1, reynolds=1600.0, precision=_abi.DG_PRECISION_FP64, perturbation=0.01):
+    """Taylor-Green vortex on a p-anisotropic periodic box (faces at the larger order of their sides)."""
+    orders = random_orders(n ** 3, lo, hi, seed)
+    mesh = HexMesh.box(n, [0, 0, 0], [TWO_PI] * 3, orders, node_type=nodes, warp=warp,
+                       patch_order=hi if warp else 0)
+    cfg = Config(order=hi, nodes=nodes, flow="ns", mach=mach, reynolds=reynolds, riemann=riemann, precision=precision)
+    q0 = problems.taylor_green(mesh.x, mach, perturbation=perturbation, seed=seed)
+    return mesh, cfg, q0
+
+
+def aniso_vortex_case(n=3, lo=2, hi=5, seed=2, nodes=_abi.DG_NODES_GAUSS, riemann=_abi.DG_RIEMANN_LXF,
+                      mach=0.5, precision=_abi.DG_PRECISION_FP64, averaging=_abi.DG_AVG_STANDARD):
+    """Euler isentropic vortex (strength 5) advected diagonally on a p-anisotropic periodic box."""
+    L = 10.0
+    orders = random_orders(n ** 3, lo, hi, seed)
+    mesh = HexMesh.box(n, [-L / 2] * 3, [L / 2] * 3, orders, node_type=nodes)
+    cfg = Config(order=hi, nodes=nodes, flow="euler", mach=mach, riemann=riemann, averaging=averaging,
+                 precision=precision)
+    q0 = problems.isentropic_vortex(mesh.x, mach, strength=5.0, period=L)
+    return mesh, cfg, q0

@@ -48,11 +48,36 @@ def test_create_validates_before_touching_the_device():
     assert _ctx_create(mesh, Config(inviscid=_abi.DG_INVISCID_SPLIT)) == _abi.DG_ERR_INVALID
     assert _ctx_create(mesh, Config(mach=-1.0)) == _abi.DG_ERR_INVALID
     assert _ctx_create(mesh, Config(riemann=7)) == _abi.DG_ERR_UNSUPPORTED
-    aniso = HexMesh.box(2, [0, 0, 0], [1, 1, 1], np.tile([2, 3, 4], 8), node_type=_abi.DG_NODES_GAUSS)
-    assert _ctx_create(aniso, Config()) == _abi.DG_ERR_UNSUPPORTED
-    assert b"isotropic" in _abi.lib().dg_last_error()
     big = HexMesh.box(1, [0, 0, 0], [1, 1, 1], 8, node_type=_abi.DG_NODES_GAUSS)
     assert _ctx_create(big, Config()) == _abi.DG_ERR_UNSUPPORTED
+
+
+def test_variable_order_path_validates_before_touching_the_device():
+    # anisotropic orders go to the variable-order path (a batch of one case)
+    aniso = HexMesh.box(2, [0, 0, 0], [1, 1, 1], np.tile([2, 3, 4], 8), node_type=_abi.DG_NODES_GAUSS)
+    assert _ctx_create(aniso, Config(inviscid=_abi.DG_INVISCID_SPLIT)) == _abi.DG_ERR_UNSUPPORTED
+    assert b"standard" in _abi.lib().dg_last_error()
+    assert _ctx_create(aniso, Config(mach=0.0)) == _abi.DG_ERR_INVALID
+    # a face order that is not the larger of its two sides' orders
+    nf = np.ctypeslib.as_array(aniso.desc.face_nf, shape=(2 * aniso.desc.n_faces,))
+    saved = nf.copy()
+    nf[0] += 1
+    try:
+        assert _ctx_create(aniso, Config()) == _abi.DG_ERR_INVALID
+        assert b"face order" in _abi.lib().dg_last_error()
+    finally:
+        nf[:] = saved
+    # batches: every case validated, shared node type and equations
+    L = _abi.lib()
+    h = C.c_void_p()
+    descs = (_abi.DgMeshDesc * 2)(aniso.desc, aniso.desc)
+    phys = (_abi.DgPhysics * 2)(Config().physics(), Config(mach=-1.0).physics())
+    assert L.dg_create_batch(2, descs, phys, C.byref(Config().options()), C.byref(h)) == _abi.DG_ERR_INVALID
+    assert b"case 1" in L.dg_last_error()
+    phys = (_abi.DgPhysics * 2)(Config().physics(), Config(flow="euler").physics())
+    assert L.dg_create_batch(2, descs, phys, C.byref(Config().options()), C.byref(h)) == _abi.DG_ERR_UNSUPPORTED
+    assert L.dg_create_batch(0, descs, phys, C.byref(Config().options()), C.byref(h)) == _abi.DG_ERR_INVALID
+    assert L.dg_batch_size(None) == 0 and L.dg_case_offset(None, 0) == -1
 
 
 def test_null_arguments_are_rejected():
@@ -135,3 +160,13 @@ def test_control_file_keys():
         parse_control("viscous discretization = BR2\nreynolds number = 1\n")
     with pytest.raises(UnsupportedOption):
         parse_control("riemann solver = rusanov\nreynolds number = 1\n")
+
+
+def test_anisotropic_order_keys(tmp_path):
+    ijk = parse_control("polynomial order i = 2\npolynomial order j = 3\npolynomial order k = 4\nreynolds number = 1\n")
+    assert ijk.element_orders() == (2, 3, 4)
+    with pytest.raises(ValueError):
+        parse_control("polynomial order i = 2\nreynolds number = 1\n")
+    (tmp_path / "orders.omesh").write_text("3\n1 2 3\n4 5 6\n7 1 2\n")
+    f = parse_control("polynomial order = 5\npolynomial order file = orders.omesh\nreynolds number = 1\n")
+    assert f.element_orders(tmp_path).tolist() == [[1, 2, 3], [4, 5, 6], [7, 1, 2]]

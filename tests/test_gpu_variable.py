@@ -1,0 +1,214 @@
+"""GPU parity of the variable-order / multi-case path against the CPU FP64 oracle.
+
+p-anisotropic meshes: every element draws its own (Nx, Ny, Nz); each face takes the larger order of
+its two sides in each direction and the element traces are interpolated to it (and the face fluxes
+projected back) with Tset, as FaceClass.f90:281-470,597-703,865-963 do. Batches: several independent
+cases in one context, each compared with the oracle run on that case alone. Tolerances as in
+test_gpu_parity: 1e-10 for one right-hand side, 1e-12 for the state after RK3 steps, 1e-6 for the
+mixed form.
+"""
+import numpy as np
+import pytest
+
+import cases
+import oracle
+from horses3d_gb300 import _abi, problems
+from horses3d_gb300.batch import CaseBatch
+from horses3d_gb300.control import Config
+from horses3d_gb300.mesh import HexMesh
+from horses3d_gb300.problems import rel_l2
+from horses3d_gb300.solver import NavierStokesDG
+
+pytestmark = pytest.mark.gpu
+
+STATE_TOL = 1e-12
+RHS_TOL = 1e-10
+MIXED_TOL = 1e-6
+
+
+def _pair(mesh, cfg, q0):
+    o = oracle.Oracle(mesh, cfg.physics(), cfg.options())
+    o.set_state(q0)
+    g = NavierStokesDG(mesh, cfg)
+    g.set_state(q0)
+    return o, g
+
+
+def _check_rhs(mesh, cfg, q0, t=0.0):
+    o, g = _pair(mesh, cfg, q0)
+    ref = o.rhs(t)
+    g.compute_time_derivative(t)
+    err = rel_l2(g.QDot, ref)
+    assert np.all(err <= RHS_TOL), err
+    if cfg.flow == "ns":
+        for f in (_abi.DG_FIELD_UX, _abi.DG_FIELD_UY, _abi.DG_FIELD_UZ):
+            gr = o.get(f)
+            e2 = np.max(np.abs(g.get(f) - gr)) / max(np.max(np.abs(gr)), 1e-300)
+            assert e2 <= RHS_TOL, (f, e2)
+
+
+def _check_steps(mesh, cfg, q0, steps, dt, tol=STATE_TOL):
+    o, g = _pair(mesh, cfg, q0)
+    t = 0.0
+    for _ in range(steps):
+        o.rk3_step(t, dt)
+        g.take_rk3_step(t, dt)
+        t += dt
+    err = rel_l2(g.Q, o.get(0), mesh.quadrature_weights())
+    assert np.all(err <= tol), err
+    return err
+
+
+def test_anisotropic_mesh_has_nonconforming_orders():
+    mesh, _, _ = cases.aniso_tgv_case(n=3)
+    assert mesh.uniform_order() is None
+    nf = np.ctypeslib.as_array(mesh.desc.face_nf, shape=(mesh.n_faces, 2))
+    assert nf.max() == 4 and nf.min() >= 1
+
+
+@pytest.mark.parametrize("nodes,riemann", [(_abi.DG_NODES_GAUSS, _abi.DG_RIEMANN_ROE),
+                                           (_abi.DG_NODES_GAUSS_LOBATTO, _abi.DG_RIEMANN_LXF)])
+def test_rhs_anisotropic_ns(nodes, riemann):
+    mesh, cfg, q0 = cases.aniso_tgv_case(n=3, nodes=nodes, riemann=riemann)
+    _check_rhs(mesh, cfg, q0)
+
+
+def test_rhs_anisotropic_curvilinear():
+    mesh, cfg, q0 = cases.aniso_tgv_case(n=3, lo=2, hi=5, seed=5, warp=0.1, riemann=_abi.DG_RIEMANN_LXF)
+    _check_rhs(mesh, cfg, q0)
+
+
+@pytest.mark.parametrize("averaging", [_abi.DG_AVG_STANDARD, _abi.DG_AVG_PIROZZOLI])
+def test_rhs_anisotropic_euler_vortex(averaging):
+    mesh, cfg, q0 = cases.aniso_vortex_case(n=3, averaging=averaging)
+    _check_rhs(mesh, cfg, q0)
+
+
+def test_rk3_steps_anisotropic_ns():
+    mesh, cfg, q0 = cases.aniso_tgv_case(n=3, lo=2, hi=5, seed=3, warp=0.1)
+    _check_steps(mesh, cfg, q0, steps=3, dt=2e-3)
+
+
+def test_rk3_steps_anisotropic_euler():
+    mesh, cfg, q0 = cases.aniso_vortex_case(n=4, lo=1, hi=6, seed=4)
+    _check_steps(mesh, cfg, q0, steps=3, dt=5e-3)
+
+
+def test_max_dt_anisotropic():
+    mesh, cfg, q0 = cases.aniso_tgv_case(n=3, lo=1, hi=6, seed=6)
+    o, g = _pair(mesh, cfg, q0)
+    for cfl, dcfl in ((0.4, 0.4), (0.5, 1e5)):
+        ref = o.max_dt(cfl, dcfl)
+        assert abs(g.max_time_step(cfl, dcfl) - ref) <= 1e-15 * ref
+
+
+def test_anisotropic_graph_replay_with_cfl():
+    mesh, cfg, q0 = cases.aniso_tgv_case(n=3, seed=8)
+    g1 = NavierStokesDG(mesh, cfg)
+    g1.set_state(q0)
+    t = 0.0
+    for _ in range(3):
+        dt = g1.max_time_step(0.4, 0.4)
+        g1.take_rk3_step(t, dt)
+        t += dt
+    g2 = NavierStokesDG(mesh, cfg)
+    g2.set_state(q0)
+    t2 = g2.run_steps(3, 0.0, dt=0.0, cfl=0.4, dcfl=0.4)
+    assert abs(t2 - t) <= 1e-15 * t
+    assert np.array_equal(g1.Q, g2.Q)
+
+
+def test_variable_path_equals_uniform_path_on_a_uniform_mesh():
+    """A batch of one uniform case runs the variable-order kernels; it must agree with the
+    uniform-order kernels to rounding."""
+    mesh, cfg, q0 = cases.tgv_case(n=3, order=3, nodes=_abi.DG_NODES_GAUSS, perturbation=0.01, seed=3)
+    g = NavierStokesDG(mesh, cfg)
+    g.set_state(q0)
+    b = CaseBatch([mesh], [cfg])
+    b.set_state([q0])
+    g.run_steps(2, 0.0, dt=1e-3)
+    b.set_clock(0.0, 1e-3)
+    b.run_steps(2)
+    err = rel_l2(b.get()[0], g.Q, mesh.quadrature_weights())
+    assert np.all(err <= STATE_TOL), err
+
+
+def test_mixed_anisotropic_within_1e6():
+    mesh, cfg, q0 = cases.aniso_tgv_case(n=3, lo=2, hi=5, seed=9, precision=_abi.DG_PRECISION_MIXED)
+    o = oracle.Oracle(mesh, cfg.physics(), cfg.options())
+    o.set_state(q0)
+    g = NavierStokesDG(mesh, cfg)
+    g.set_state(q0)
+    dt = 2e-3
+    for s in range(5):
+        o.rk3_step(s * dt, dt)
+    g.run_steps(5, 0.0, dt=dt)
+    err = rel_l2(g.Q, o.get(0), mesh.quadrature_weights())
+    assert np.all(err <= MIXED_TOL), err
+
+
+def _batch_cases(precision=_abi.DG_PRECISION_FP64):
+    out = []
+    m, c, q = cases.tgv_case(n=3, order=2, nodes=_abi.DG_NODES_GAUSS, mach=0.3, reynolds=400.0, perturbation=0.01,
+                             seed=11, precision=precision)
+    out.append((m, c, q))
+    m, c, q = cases.aniso_tgv_case(n=2, lo=1, hi=4, seed=12, mach=0.6, reynolds=2500.0, precision=precision)
+    out.append((m, c, q))
+    m = HexMesh.box(4, [-5.0] * 3, [5.0] * 3, 3, node_type=_abi.DG_NODES_GAUSS)
+    c = Config(order=3, nodes=_abi.DG_NODES_GAUSS, mach=0.2, reynolds=150.0, precision=precision)
+    q = problems.isentropic_vortex(m.x, 0.2, strength=5.0, period=10.0)
+    out.append((m, c, q))
+    return out
+
+
+def test_batch_matches_each_case_alone():
+    cs = _batch_cases()
+    b = CaseBatch([m for m, _, _ in cs], [c for _, c, _ in cs])
+    b.set_state([q for _, _, q in cs])
+    assert b.n_cases == 3 and b.ndof == sum(m.ndof for m, _, _ in cs)
+    dts = b.max_time_steps(0.4, 0.4)
+    refs = []
+    for k, (m, c, q) in enumerate(cs):
+        o = oracle.Oracle(m, c.physics(), c.options())
+        o.set_state(q)
+        ref_dt = o.max_dt(0.4, 0.4)
+        assert abs(dts[k] - ref_dt) <= 1e-15 * ref_dt, (k, dts[k], ref_dt)
+        refs.append(o)
+    # every case advances with its own fixed dt
+    steps = 3
+    b.set_clock(np.zeros(3), dts)
+    b.run_steps(steps)
+    t, dt = b.clock()
+    got = b.get()
+    res, nan = b.compute_max_residuals()
+    assert not nan.any()
+    for k, (m, c, q) in enumerate(cs):
+        o = refs[k]
+        for s in range(steps):
+            o.rk3_step(s * dts[k], dts[k])
+        assert abs(t[k] - steps * dts[k]) <= 1e-14 * t[k]
+        err = rel_l2(got[k], o.get(0), m.quadrature_weights())
+        assert np.all(err <= STATE_TOL), (k, err)
+        ref_res, _ = o.residuals()
+        assert np.allclose(res[k], ref_res, rtol=1e-9, atol=0.0), (k, res[k], ref_res)
+
+
+def test_batch_cfl_steps_and_mixed_form():
+    cs = _batch_cases(precision=_abi.DG_PRECISION_MIXED)
+    b = CaseBatch([m for m, _, _ in cs], [c for _, c, _ in cs])
+    b.set_state([q for _, _, q in cs])
+    b.set_clock(np.zeros(3), np.zeros(3))
+    b.run_steps(4, cfl=0.4, dcfl=0.4)
+    t, _ = b.clock()
+    got = b.get()
+    for k, (m, c, q) in enumerate(cs):
+        o = oracle.Oracle(m, c.physics(), c.options())
+        o.set_state(q)
+        tt = 0.0
+        for _ in range(4):
+            dt = o.max_dt(0.4, 0.4)
+            o.rk3_step(tt, dt)
+            tt += dt
+        assert abs(t[k] - tt) <= 1e-6 * tt, (k, t[k], tt)
+        err = rel_l2(got[k], o.get(0), m.quadrature_weights())
+        assert np.all(err <= MIXED_TOL), (k, err)
