@@ -247,6 +247,142 @@ def run_gpu_arm(args, rank, world, local, case):
     }
 
 
+# ------------------------------------------------------------------ secondary workloads ----------
+# The other benchmark configurations, measured one at a time with --workload NAME (one JSON line
+# each). Every one reports the mixed form against the plain FP64 form on the same GPU, with the
+# same fixed dt (MaxTimeStep at t=0 of the FP64 form), and the relative L2 difference of the two.
+SECONDARY = {
+    "tgv8_n3_gl_roe": "Taylor-Green 8^3 elements, N=3 Gauss-Lobatto, standard form, Roe, BR1, M=0.1, Re=1600, 100 steps",
+    "split16_n4_pirozzoli": "Taylor-Green 16^3, N=4 Gauss-Lobatto, split form (Pirozzoli two-point flux), LxF, BR1, "
+                            "+-1% seeded velocity perturbation, 200 steps",
+    "aniso24_vortex": "p-anisotropic 24^3 box, (Nx,Ny,Nz) i.i.d. uniform {2..7} (seed 4), Euler isentropic vortex "
+                      "(strength 5, M=0.5) advected diagonally, Gauss, LxF, 500 steps",
+    "batch64": "64 independent NS cases: 8^3..12^3 periodic boxes, uniform N in {2..6}, M ~ U[0.1,0.8], "
+               "Re ~ U[100,3000], Taylor-Green or isentropic vortex by seed (seed 5), Gauss, LxF, 200 steps",
+}
+
+
+def build_secondary(name: str):
+    """(meshes, FP64 configs, initial states, steps) of a secondary workload."""
+    from horses3d_gb300 import _abi, problems
+    from horses3d_gb300.control import Config
+    from horses3d_gb300.mesh import HexMesh
+
+    two_pi = 2 * np.pi
+    if name == "tgv8_n3_gl_roe":
+        m = HexMesh.box(8, [0, 0, 0], [two_pi] * 3, 3, node_type=_abi.DG_NODES_GAUSS_LOBATTO)
+        c = Config(order=3, nodes=_abi.DG_NODES_GAUSS_LOBATTO, mach=0.1, reynolds=1600.0, riemann=_abi.DG_RIEMANN_ROE)
+        return [m], [c], [problems.taylor_green(m.x, 0.1)], 100
+    if name == "split16_n4_pirozzoli":
+        m = HexMesh.box(16, [0, 0, 0], [two_pi] * 3, 4, node_type=_abi.DG_NODES_GAUSS_LOBATTO)
+        c = Config(order=4, nodes=_abi.DG_NODES_GAUSS_LOBATTO, mach=0.1, reynolds=1600.0, riemann=_abi.DG_RIEMANN_LXF,
+                   inviscid=_abi.DG_INVISCID_SPLIT, averaging=_abi.DG_AVG_PIROZZOLI)
+        return [m], [c], [problems.taylor_green(m.x, 0.1, perturbation=0.01, seed=2)], 200
+    if name == "aniso24_vortex":
+        n = 24
+        orders = np.random.default_rng(4).integers(2, 8, size=(n ** 3, 3)).astype(np.int32)
+        m = HexMesh.box(n, [-5.0] * 3, [5.0] * 3, orders, node_type=_abi.DG_NODES_GAUSS)
+        c = Config(order=7, nodes=_abi.DG_NODES_GAUSS, flow="euler", mach=0.5, riemann=_abi.DG_RIEMANN_LXF)
+        return [m], [c], [problems.isentropic_vortex(m.x, 0.5, strength=5.0, period=10.0)], 500
+    if name == "batch64":
+        rng = np.random.default_rng(5)
+        meshes, cfgs, qs = [], [], []
+        for _ in range(64):
+            n = int(rng.integers(8, 13))
+            N = int(rng.integers(2, 7))
+            mach = float(rng.uniform(0.1, 0.8))
+            re = float(rng.uniform(100.0, 3000.0))
+            vortex = bool(rng.integers(0, 2))
+            if vortex:
+                m = HexMesh.box(n, [-5.0] * 3, [5.0] * 3, N, node_type=_abi.DG_NODES_GAUSS)
+                q = problems.isentropic_vortex(m.x, mach, strength=5.0, period=10.0)
+            else:
+                m = HexMesh.box(n, [0, 0, 0], [two_pi] * 3, N, node_type=_abi.DG_NODES_GAUSS)
+                q = problems.taylor_green(m.x, mach)
+            meshes.append(m)
+            cfgs.append(Config(order=N, nodes=_abi.DG_NODES_GAUSS, mach=mach, reynolds=re, riemann=_abi.DG_RIEMANN_LXF))
+            qs.append(q)
+        return meshes, cfgs, qs, 200
+    raise ValueError(f"unknown workload {name}")
+
+
+def run_secondary(name: str, args):
+    import dataclasses
+
+    from horses3d_gb300 import _abi
+    from horses3d_gb300.batch import CaseBatch
+    from horses3d_gb300.problems import rel_l2
+
+    meshes, cfgs, qs, steps = build_secondary(name)
+    steps = args.steps if args.steps_given else steps
+    ndof = sum(m.ndof for m in meshes)
+
+    def make(precision):
+        b = CaseBatch(meshes, [dataclasses.replace(c, precision=precision) for c in cfgs])
+        b.set_state(qs)
+        return b
+
+    def timed(b, dts):
+        b.set_clock(np.zeros(len(meshes)), dts)
+        b.run_steps(args.warmup)
+        b.set_clock(np.zeros(len(meshes)), dts)
+        b.set_state(qs)
+        return b.run_steps(steps)
+
+    if len(meshes) == 1 and meshes[0].uniform_order() is not None:
+        # one uniform case: the uniform-order kernels (the batch path would also run it)
+        from horses3d_gb300.solver import NavierStokesDG
+
+        def make_single(precision):
+            g = NavierStokesDG(meshes[0], dataclasses.replace(cfgs[0], precision=precision))
+            g.set_state(qs[0])
+            return g
+
+        g64 = make_single(_abi.DG_PRECISION_FP64)
+        dt = g64.max_time_step(CFL, CFL)
+        ms = {}
+        outs = {}
+        for prec, g in ((_abi.DG_PRECISION_FP64, g64), (_abi.DG_PRECISION_MIXED, make_single(_abi.DG_PRECISION_MIXED))):
+            g.run_steps(args.warmup, 0.0, dt=dt)
+            g.set_state(qs[0])
+            import ctypes as C
+
+            t = C.c_double()
+            _abi.check(_abi.lib().dg_time_steps(g._h, steps, 0.0, dt, 0.0, 0.0, C.byref(t)), "dg_time_steps")
+            ms[prec] = t.value
+            outs[prec] = [g.Q]
+        kt = np.zeros(5)
+        gm = make_single(_abi.DG_PRECISION_MIXED)
+        _abi.check(_abi.lib().dg_kernel_times(gm._h, 10, 0.0, dt, _abi.f64ptr(kt)), "dg_kernel_times")
+        kernels = dict(zip(["volume", "flux", "update", "traces"], [round(float(v), 5) for v in kt[:4]]))
+        launches = steps * 9
+    else:
+        b64 = make(_abi.DG_PRECISION_FP64)
+        dts = b64.max_time_steps(CFL, CFL)
+        bm = make(_abi.DG_PRECISION_MIXED)
+        ms = {_abi.DG_PRECISION_FP64: timed(b64, dts), _abi.DG_PRECISION_MIXED: timed(bm, dts)}
+        outs = {_abi.DG_PRECISION_FP64: b64.get(), _abi.DG_PRECISION_MIXED: bm.get()}
+        kt = np.zeros(5)
+        _abi.check(_abi.lib().dg_kernel_times(bm._h, 10, 0.0, 0.0, _abi.f64ptr(kt)), "dg_kernel_times")
+        kernels = dict(zip(["volume", "face_flux", "update", "traces", "face_jump"], [round(float(v), 5) for v in kt]))
+        launches = steps * 3 * (4 if cfgs[0].flow == "ns" else 3)
+    errs = np.array([rel_l2(a, b, m.quadrature_weights())
+                     for a, b, m in zip(outs[_abi.DG_PRECISION_MIXED], outs[_abi.DG_PRECISION_FP64], meshes)])
+    mixed = 3.0 * ndof * steps / (ms[_abi.DG_PRECISION_MIXED] * 1e-3)
+    plain = 3.0 * ndof * steps / (ms[_abi.DG_PRECISION_FP64] * 1e-3)
+    line = {"workload": name, "metric": "DOF*RK-stage updates/s", "value": mixed, "unit": "DOF*stage/s",
+            "n_gpus": 1, "steps": steps, "warmup": args.warmup,
+            "ms_per_step": ms[_abi.DG_PRECISION_MIXED] / steps, "higher_is_better": True,
+            "dtype": "f32 fluxes / f64 state", "data": "synthetic",
+            "config": {"workload": SECONDARY[name], "cases": len(meshes), "ndof": ndof,
+                       "elements": sum(m.n_elements for m in meshes), "dt": "CFL 0.4 at t=0 per case, fixed"},
+            "plain_fp64": {"value": plain, "ms_per_step": ms[_abi.DG_PRECISION_FP64] / steps},
+            "mixed_over_plain": mixed / plain,
+            "rel_l2_mixed_vs_fp64_max": [float(v) for v in errs.max(axis=0)],
+            "kernel_ms_mixed": kernels, "gpu_launches": launches}
+    print(json.dumps(line))
+
+
 def cpu_oracle_rate(case, steps: int = 1):
     """Oracle FP64 throughput on the host cores (OpenMP, all threads) on RK3 steps of the workload."""
     sys.path.insert(0, str(ROOT / "oracle"))
@@ -276,7 +412,10 @@ def main():
     ap.add_argument("--elements", type=int, default=N_ELEM, help="elements per direction (profiling runs)")
     ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
                     help="profiling run: only warm-up + timed steps of one form, no extra legs")
+    ap.add_argument("--workload", choices=["tgv32_curvilinear", *SECONDARY], default="tgv32_curvilinear",
+                    help="the headline workload (default) or one of the other benchmark configurations")
     args = ap.parse_args()
+    args.steps_given = "--steps" in sys.argv
     rank, world, local = _dist()
     if world > 1:
         import torch.distributed as dist
@@ -311,6 +450,10 @@ def main():
     if rank == 0:
         product_build.build()
     _barrier(world)
+    if args.workload != "tgv32_curvilinear":
+        if rank == 0:
+            run_secondary(args.workload, args)
+        return
     if world > 1:
         import torch
 

@@ -172,11 +172,19 @@ cudaError_t enqueue_max_dt(dg_ctx* c, double cfl, double dcfl) {
     d.S_div_TRef = c->pc.S_div_TRef; d.TReNorm = c->pc.TReNorm;
     d.Q = c->Q.p;
     d.red = c->red.p;
+    const dg::DtConst32 c32 = dg::dt_const32(cfl, dcfl, c->dxi, d.gamma, d.gm1, d.gammaM2, d.S_div_TRef, d.TReNorm, d.ns);
     const int blocks = 2 * 152 * 4;
-    if (c->mixed)
-        dg::k_max_dt<float><<<blocks, 256, 0, c->stream>>>(d, c->s32.ja_xi.p, c->s32.ja_eta.p, c->s32.ja_zeta.p, c->s32.jac.p);
-    else
-        dg::k_max_dt<double><<<blocks, 256, 0, c->stream>>>(d, c->s64.ja_xi.p, c->s64.ja_eta.p, c->s64.ja_zeta.p, c->s64.jac.p);
+    if (c->mixed) {
+        const Store<float>& st = c->s32;
+        dg::k_dt_estimate<float><<<blocks, 256, 0, c->stream>>>(c32, c->ndof, c->Q.p, st.ja_xi.p, st.ja_eta.p,
+                                                                 st.ja_zeta.p, st.jac.p, c->red.p);
+        dg::k_dt_exact<float><<<blocks, 256, 0, c->stream>>>(d, c32, st.ja_xi.p, st.ja_eta.p, st.ja_zeta.p, st.jac.p);
+    } else {
+        const Store<double>& st = c->s64;
+        dg::k_dt_estimate<double><<<blocks, 256, 0, c->stream>>>(c32, c->ndof, c->Q.p, st.ja_xi.p, st.ja_eta.p,
+                                                                  st.ja_zeta.p, st.jac.p, c->red.p);
+        dg::k_dt_exact<double><<<blocks, 256, 0, c->stream>>>(d, c32, st.ja_xi.p, st.ja_eta.p, st.ja_zeta.p, st.jac.p);
+    }
     dg::k_dt_final<<<1, 1, 0, c->stream>>>(c->red.p, c->scal.p + 1);
     return cudaGetLastError();
 }
@@ -314,6 +322,7 @@ int dg_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op,
         unsigned long long bb;
         std::memcpy(&bb, &big, 8);
         for (int i = 0; i < 8; ++i) init[i] = i < 2 ? bb : 0ull;
+        init[7] = dg::kDtEstimateInit;
         if ((e = cudaMemcpy(c->red.p, init, sizeof(init), cudaMemcpyHostToDevice)) != cudaSuccess)
             return bail(cuda_fail(e, "init reductions"));
     }

@@ -100,60 +100,170 @@ struct DtArgs {
     int ns;
     double gamma, gm1, gammaM2, S_div_TRef, TReNorm;
     const double* Q;
-    unsigned long long* red;  // [0] convective, [1] viscous (bit images)
+    unsigned long long* red;  // [0] convective, [1] viscous (FP64 bit images), [7] FP32 estimates (2 x 32 bit)
 };
 
-// MaxTimeStep (DGSEMClass.f90:870-1038) per node, block-reduced, then atomically folded.
+// MaxTimeStep (DGSEMClass.f90:870-1038) in two passes. The minimum is taken over FP64 quotients
+// that need about ten FP64 divisions and square roots per node, so evaluating every node in FP64
+// costs milliseconds on a part whose FP64 rate is 1/64 of FP32. Pass 1 estimates each node's
+// convective and viscous limits in FP32 and reduces their minima m32. Pass 2 repeats the estimate
+// and evaluates the exact FP64 expressions only at nodes whose estimate is within kDtWindow of m32
+// (or not a number). An FP32 estimate differs from the FP64 value by a relative 1e-6 or less for
+// physical states, far inside the window, so the node that attains the FP64 minimum is always
+// evaluated and the result equals the FP64 minimum over all nodes bit for bit.
+constexpr float kDtWindow = 1.0e-3f;
+constexpr unsigned long long kDtEstimateInit = 0x7F8000007F800000ull;  // two FP32 +inf
+
+struct DtConst32 {
+    float cfl, dcfl, dxi[3], dxi2[3], gamma, gm1, gammaM2, S_div_TRef, TReNorm;
+    int ns;
+};
+
+__host__ __device__ inline DtConst32 dt_const32(double cfl, double dcfl, const double* dxi, double gamma, double gm1,
+                                                double gammaM2, double S_div_TRef, double TReNorm, int ns) {
+    DtConst32 c;
+    c.cfl = float(cfl);
+    c.dcfl = float(dcfl);
+    for (int r = 0; r < 3; ++r) {
+        c.dxi[r] = float(dxi[r]);
+        c.dxi2[r] = float(dxi[r] * dxi[r]);
+    }
+    c.gamma = float(gamma);
+    c.gm1 = float(gm1);
+    c.gammaM2 = float(gammaM2);
+    c.S_div_TRef = float(S_div_TRef);
+    c.TReNorm = float(TReNorm);
+    c.ns = ns;
+    return c;
+}
+
+// FP32 estimates of one node's convective and viscous time-step limits.
 template <typename R>
-__global__ void k_max_dt(DtArgs d, const R* ja_xi, const R* ja_eta, const R* ja_zeta, const R* jac) {
+__device__ __forceinline__ void dt_estimate(const DtConst32& d, const double* Q, const R* jx, const R* je, const R* jz,
+                                            R jac, float& conv, float& visc) {
+    const float rho = float(Q[0]), ru = float(Q[1]), rv = float(Q[2]), rw = float(Q[3]), E = float(Q[4]);
+    const float ir = 1.0f / rho;
+    const float p = d.gm1 * (E - 0.5f * (ru * ru + rv * rv + rw * rw) * ir);
+    const float a = sqrtf(d.gamma * p * ir);
+    const float ev[3] = {fabsf(ru * ir) + a, fabsf(rv * ir) + a, fabsf(rw * ir) + a};
+    const float J = fabsf(float(jac));
+    const R* ja[3] = {jx, je, jz};
+    float lam = 0.0f;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+        lam += fabsf(float(ja[r][0]) * ev[0] + float(ja[r][1]) * ev[1] + float(ja[r][2]) * ev[2]) * d.dxi[r];
+    conv = d.cfl * J / lam;
+    visc = 3.0e38f;
+    if (d.ns) {
+        const float t = d.gammaM2 * p * ir * d.TReNorm;
+        const float mu = (1.0f + d.S_div_TRef) / (t + d.S_div_TRef) * t * sqrtf(t);
+        float lv = 0.0f;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) lv += mu * d.dxi2[r] * fabsf(float(ja[r][0]) + float(ja[r][1]) + float(ja[r][2]));
+        visc = d.dcfl * J / lv;
+    }
+}
+
+// The exact FP64 limits of one node (the reference's expressions and operation order).
+template <typename R>
+__device__ __forceinline__ void dt_exact(const DtArgs& d, const double* dx, const double* dx2, const double* Q,
+                                         const R* jx, const R* je, const R* jz, R jac, double gammaM2, bool want_conv,
+                                         bool want_visc, double& conv, double& visc) {
+    const double p = d.gm1 * (Q[4] - 0.5 * (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) / Q[0]);
+    const double J = fabs(double(jac));
+    const R* ja[3] = {jx, je, jz};
+    if (want_conv) {
+        const double a = sqrt(d.gamma * p / Q[0]);
+        const double ev[3] = {fabs(Q[1] / Q[0]) + a, fabs(Q[2] / Q[0]) + a, fabs(Q[3] / Q[0]) + a};
+        double l3[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+            l3[r] = fabs(double(ja[r][0]) * ev[0] + double(ja[r][1]) * ev[1] + double(ja[r][2]) * ev[2]) * dx[r];
+        conv = d.cfl * J / (l3[0] + l3[1] + l3[2]);
+    }
+    if (want_visc) {
+        const double T = gammaM2 * p / Q[0];
+        const double t = T * d.TReNorm;
+        const double mu = (1.0 + d.S_div_TRef) / (t + d.S_div_TRef) * t * sqrt(t);
+        double v3[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) v3[r] = mu * dx2[r] * fabs(double(ja[r][0]) + double(ja[r][1]) + double(ja[r][2]));
+        visc = d.dcfl * J / (v3[0] + v3[1] + v3[2]);
+    }
+}
+
+__device__ __forceinline__ unsigned int fbits(float x) { return __float_as_uint(x); }
+
+// Block minimum of two values, folded into the 64-bit (double) or 32-bit (float) slots by atomicMin on
+// the bit images (non-negative values order like their bit patterns).
+template <typename T>
+__device__ __forceinline__ void block_min2(T a, T b, T* slot_a_out, T* slot_b_out) {
+    __shared__ T sa[32], sb[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        a = fmin(a, __shfl_down_sync(0xffffffffu, a, o));
+        b = fmin(b, __shfl_down_sync(0xffffffffu, b, o));
+    }
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        sa[w] = a;
+        sb[w] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        for (int q = 1; q < nw; ++q) {
+            a = fmin(a, sa[q]);
+            b = fmin(b, sb[q]);
+        }
+        *slot_a_out = a;
+        *slot_b_out = b;
+    }
+}
+
+template <typename R>
+__global__ void k_dt_estimate(DtConst32 c, long long ndof, const double* Q, const R* ja_xi, const R* ja_eta,
+                              const R* ja_zeta, const R* jac, unsigned long long* red) {
+    float conv = 3.0e38f, visc = 3.0e38f;
+    for (long long g = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; g < ndof;
+         g += static_cast<long long>(gridDim.x) * blockDim.x) {
+        float cv, vs;
+        dt_estimate(c, Q + 5 * g, ja_xi + 3 * g, ja_eta + 3 * g, ja_zeta + 3 * g, jac[g], cv, vs);
+        conv = fminf(conv, cv);
+        visc = fminf(visc, vs);
+    }
+    float bc, bv;
+    block_min2(conv, visc, &bc, &bv);
+    if (threadIdx.x == 0) {
+        unsigned int* s32 = reinterpret_cast<unsigned int*>(red + 7);
+        atomicMin(&s32[0], fbits(bc));
+        atomicMin(&s32[1], fbits(bv));
+    }
+}
+
+template <typename R>
+__global__ void k_dt_exact(DtArgs d, DtConst32 c, const R* ja_xi, const R* ja_eta, const R* ja_zeta, const R* jac) {
+    const unsigned int* s32 = reinterpret_cast<const unsigned int*>(d.red + 7);
+    const float thr_c = __uint_as_float(s32[0]) * (1.0f + kDtWindow);
+    const float thr_v = __uint_as_float(s32[1]) * (1.0f + kDtWindow);
     double conv = 1.0e300, visc = 1.0e300;
     for (long long g = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; g < d.ndof;
          g += static_cast<long long>(gridDim.x) * blockDim.x) {
         const double* Q = d.Q + 5 * g;
-        const double p = d.gm1 * (Q[4] - 0.5 * (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) / Q[0]);
-        const double a = sqrt(d.gamma * p / Q[0]);
-        const double ev[3] = {fabs(Q[1] / Q[0]) + a, fabs(Q[2] / Q[0]) + a, fabs(Q[3] / Q[0]) + a};
-        const R* ja[3] = {ja_xi + 3 * g, ja_eta + 3 * g, ja_zeta + 3 * g};
-        double lam = 0.0, lamv = 0.0;
-        const double J = fabs(double(jac[g]));
-        double l3[3];
-#pragma unroll
-        for (int r = 0; r < 3; ++r)
-            l3[r] = fabs(double(ja[r][0]) * ev[0] + double(ja[r][1]) * ev[1] + double(ja[r][2]) * ev[2]) * d.dxi[r];
-        lam = l3[0] + l3[1] + l3[2];
-        conv = fmin(conv, d.cfl * J / lam);
-        if (d.ns) {
-            const double T = d.gammaM2 * p / Q[0];
-            const double t = T * d.TReNorm;
-            const double mu = (1.0 + d.S_div_TRef) / (t + d.S_div_TRef) * t * sqrt(t);
-            double v3[3];
-#pragma unroll
-            for (int r = 0; r < 3; ++r)
-                v3[r] = mu * d.dxi2[r] * fabs(double(ja[r][0]) + double(ja[r][1]) + double(ja[r][2]));
-            lamv = v3[0] + v3[1] + v3[2];
-            visc = fmin(visc, d.dcfl * J / lamv);
+        float cv, vs;
+        dt_estimate(c, Q, ja_xi + 3 * g, ja_eta + 3 * g, ja_zeta + 3 * g, jac[g], cv, vs);
+        const bool wc = !(cv > thr_c), wv = d.ns && !(vs > thr_v);
+        if (wc || wv) {
+            double ec = 1.0e300, evv = 1.0e300;
+            dt_exact(d, d.dxi, d.dxi2, Q, ja_xi + 3 * g, ja_eta + 3 * g, ja_zeta + 3 * g, jac[g], d.gammaM2, wc, wv, ec, evv);
+            conv = fmin(conv, ec);
+            visc = fmin(visc, evv);
         }
     }
-    __shared__ double sc[32], sv[32];
-    for (int o = 16; o > 0; o >>= 1) {
-        conv = fmin(conv, __shfl_down_sync(0xffffffffu, conv, o));
-        visc = fmin(visc, __shfl_down_sync(0xffffffffu, visc, o));
-    }
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) { sc[w] = conv; sv[w] = visc; }
-    __syncthreads();
-    if (w == 0) {
-        const int nw = (blockDim.x + 31) >> 5;
-        conv = lane < nw ? sc[lane] : 1.0e300;
-        visc = lane < nw ? sv[lane] : 1.0e300;
-        for (int o = 16; o > 0; o >>= 1) {
-            conv = fmin(conv, __shfl_down_sync(0xffffffffu, conv, o));
-            visc = fmin(visc, __shfl_down_sync(0xffffffffu, visc, o));
-        }
-        if (lane == 0) {
-            atomicMin(&d.red[0], dbits(conv));
-            atomicMin(&d.red[1], dbits(visc));
-        }
+    double bc, bv;
+    block_min2(conv, visc, &bc, &bv);
+    if (threadIdx.x == 0) {
+        atomicMin(&d.red[0], dbits(bc));
+        atomicMin(&d.red[1], dbits(bv));
     }
 }
 
@@ -164,6 +274,7 @@ static __global__ void k_dt_final(unsigned long long* red, double* dt) {
     *dt = conv < visc ? conv : visc;
     red[0] = dbits(1.0e300);
     red[1] = dbits(1.0e300);
+    red[7] = kDtEstimateInit;
 }
 
 static __global__ void k_advance_time(double* t, const double* dt) { *t = *t + *dt; }

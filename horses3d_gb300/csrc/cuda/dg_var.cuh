@@ -709,56 +709,68 @@ struct VDtArgs {
     unsigned long long* red;
 };
 
+// Two-pass MaxTimeStep per case (the FP32 filter and exact FP64 pass of k_dt_estimate/k_dt_exact),
+// with the node spacing of each item's own orders. exact = 0: FP32 estimates into red[8c+7];
+// exact = 1: exact FP64 limits of the nodes inside the window into red[8c], red[8c+1].
 template <typename R>
-__global__ void __launch_bounds__(256) kv_max_dt(VDtArgs d, const R* ja_xi, const R* ja_eta, const R* ja_zeta,
-                                                 const R* jac) {
-    const ItemDims it = item_dims(d.items[blockIdx.x]);
-    const double dx[3] = {d.dxi[it.px], d.dxi[it.py], d.dxi[it.pz]};
-    const double gM2 = d.gamma_M2[it.kase];
+__global__ void __launch_bounds__(256) kv_dt_pass(VDtArgs v, const R* ja_xi, const R* ja_eta, const R* ja_zeta,
+                                                  const R* jac, int exact) {
+    const ItemDims it = item_dims(v.items[blockIdx.x]);
+    const double dx[3] = {v.dxi[it.px], v.dxi[it.py], v.dxi[it.pz]};
+    const double dx2[3] = {dx[0] * dx[0], dx[1] * dx[1], dx[2] * dx[2]};
+    const double gM2 = v.gamma_M2[it.kase];
+    const DtConst32 c = dt_const32(v.cfl, v.dcfl, dx, v.gamma, v.gm1, gM2, v.S_div_TRef, v.TReNorm, v.ns);
+    unsigned long long* red = v.red + 8 * it.kase;
+    if (!exact) {
+        float conv = 3.0e38f, visc = 3.0e38f;
+        for (int t = threadIdx.x; t < it.ntot; t += blockDim.x) {
+            const int le = t / it.np, n = t - le * it.np;
+            const long long g = v.eoff[v.item_elems[it.first + le]] + n;
+            float cv, vs;
+            dt_estimate(c, v.Q + 5 * g, ja_xi + 3 * g, ja_eta + 3 * g, ja_zeta + 3 * g, jac[g], cv, vs);
+            conv = fminf(conv, cv);
+            visc = fminf(visc, vs);
+        }
+        float bc, bv;
+        block_min2(conv, visc, &bc, &bv);
+        if (threadIdx.x == 0) {
+            unsigned int* s32 = reinterpret_cast<unsigned int*>(red + 7);
+            atomicMin(&s32[0], fbits(bc));
+            atomicMin(&s32[1], fbits(bv));
+        }
+        return;
+    }
+    DtArgs d;
+    d.cfl = v.cfl;
+    d.dcfl = v.dcfl;
+    d.gamma = v.gamma;
+    d.gm1 = v.gm1;
+    d.S_div_TRef = v.S_div_TRef;
+    d.TReNorm = v.TReNorm;
+    d.ns = v.ns;
+    const unsigned int* s32 = reinterpret_cast<const unsigned int*>(red + 7);
+    const float thr_c = __uint_as_float(s32[0]) * (1.0f + kDtWindow);
+    const float thr_v = __uint_as_float(s32[1]) * (1.0f + kDtWindow);
     double conv = 1.0e300, visc = 1.0e300;
     for (int t = threadIdx.x; t < it.ntot; t += blockDim.x) {
         const int le = t / it.np, n = t - le * it.np;
-        const long long g = d.eoff[d.item_elems[it.first + le]] + n;
-        const double* Q = d.Q + 5 * g;
-        const double p = d.gm1 * (Q[4] - 0.5 * (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) / Q[0]);
-        const double a = sqrt(d.gamma * p / Q[0]);
-        const double ev[3] = {fabs(Q[1] / Q[0]) + a, fabs(Q[2] / Q[0]) + a, fabs(Q[3] / Q[0]) + a};
-        const R* ja[3] = {ja_xi + 3 * g, ja_eta + 3 * g, ja_zeta + 3 * g};
-        const double J = fabs(double(jac[g]));
-        double lam = 0.0;
-#pragma unroll
-        for (int r = 0; r < 3; ++r)
-            lam += fabs(double(ja[r][0]) * ev[0] + double(ja[r][1]) * ev[1] + double(ja[r][2]) * ev[2]) * dx[r];
-        conv = fmin(conv, d.cfl * J / lam);
-        if (d.ns) {
-            const double T = gM2 * p / Q[0];
-            const double tt = T * d.TReNorm;
-            const double mu = (1.0 + d.S_div_TRef) / (tt + d.S_div_TRef) * tt * sqrt(tt);
-            double lv = 0.0;
-#pragma unroll
-            for (int r = 0; r < 3; ++r)
-                lv += mu * (dx[r] * dx[r]) * fabs(double(ja[r][0]) + double(ja[r][1]) + double(ja[r][2]));
-            visc = fmin(visc, d.dcfl * J / lv);
+        const long long g = v.eoff[v.item_elems[it.first + le]] + n;
+        const double* Q = v.Q + 5 * g;
+        float cv, vs;
+        dt_estimate(c, Q, ja_xi + 3 * g, ja_eta + 3 * g, ja_zeta + 3 * g, jac[g], cv, vs);
+        const bool wc = !(cv > thr_c), wv = v.ns && !(vs > thr_v);
+        if (wc || wv) {
+            double ec = 1.0e300, ev = 1.0e300;
+            dt_exact(d, dx, dx2, Q, ja_xi + 3 * g, ja_eta + 3 * g, ja_zeta + 3 * g, jac[g], gM2, wc, wv, ec, ev);
+            conv = fmin(conv, ec);
+            visc = fmin(visc, ev);
         }
     }
-    __shared__ double sc[8], sv[8];
-    for (int o = 16; o > 0; o >>= 1) {
-        conv = fmin(conv, __shfl_down_sync(0xffffffffu, conv, o));
-        visc = fmin(visc, __shfl_down_sync(0xffffffffu, visc, o));
-    }
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) {
-        sc[w] = conv;
-        sv[w] = visc;
-    }
-    __syncthreads();
+    double bc, bv;
+    block_min2(conv, visc, &bc, &bv);
     if (threadIdx.x == 0) {
-        for (int q = 1; q < static_cast<int>(blockDim.x >> 5); ++q) {
-            conv = fmin(conv, sc[q]);
-            visc = fmin(visc, sv[q]);
-        }
-        atomicMin(&d.red[8 * it.kase], dbits(conv));
-        atomicMin(&d.red[8 * it.kase + 1], dbits(visc));
+        atomicMin(&red[0], dbits(bc));
+        atomicMin(&red[1], dbits(bv));
     }
 }
 
@@ -770,6 +782,7 @@ static __global__ void kv_dt_final(unsigned long long* red, double* dt, int n_ca
         dt[c] = conv < visc ? conv : visc;
         red[8 * c] = dbits(1.0e300);
         red[8 * c + 1] = dbits(1.0e300);
+        red[8 * c + 7] = kDtEstimateInit;
     }
 }
 

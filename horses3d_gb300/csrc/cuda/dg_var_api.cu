@@ -359,7 +359,10 @@ int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, cons
         const double big = 1.0e300;
         unsigned long long bb;
         std::memcpy(&bb, &big, 8);
-        for (int k = 0; k < n_cases; ++k) init[8 * k] = init[8 * k + 1] = bb;
+        for (int k = 0; k < n_cases; ++k) {
+            init[8 * k] = init[8 * k + 1] = bb;
+            init[8 * k + 7] = dg::kDtEstimateInit;
+        }
         if ((e = c->red.upload(init.data(), init.size(), s)) != cudaSuccess) return bail(cuda_fail(e, "init reductions"));
     }
     if ((e = c->x.upload(h.x.data(), h.x.size(), s)) || (e = c->items.upload(items.data(), items.size(), s)) ||
@@ -462,12 +465,14 @@ cudaError_t enqueue_max_dt(dg_ctx* c, double cfl, double dcfl) {
     d.TReNorm = c->pc.TReNorm;
     d.ns = c->pc.ns;
     d.red = c->red.p;
-    if (c->mixed)
-        dg::kv_max_dt<float><<<c->n_items, 256, 0, c->stream>>>(d, c->v32.ja_xi.p, c->v32.ja_eta.p, c->v32.ja_zeta.p,
-                                                                 c->v32.jac.p);
-    else
-        dg::kv_max_dt<double><<<c->n_items, 256, 0, c->stream>>>(d, c->v64.ja_xi.p, c->v64.ja_eta.p, c->v64.ja_zeta.p,
-                                                                  c->v64.jac.p);
+    for (int pass = 0; pass < 2; ++pass) {
+        if (c->mixed)
+            dg::kv_dt_pass<float><<<c->n_items, 256, 0, c->stream>>>(d, c->v32.ja_xi.p, c->v32.ja_eta.p,
+                                                                      c->v32.ja_zeta.p, c->v32.jac.p, pass);
+        else
+            dg::kv_dt_pass<double><<<c->n_items, 256, 0, c->stream>>>(d, c->v64.ja_xi.p, c->v64.ja_eta.p,
+                                                                       c->v64.ja_zeta.p, c->v64.jac.p, pass);
+    }
     dg::kv_dt_final<<<1, 256, 0, c->stream>>>(c->red.p, c->scal.p + c->n_cases, c->n_cases);
     return cudaGetLastError();
 }

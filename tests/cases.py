@@ -101,3 +101,57 @@ def aniso_vortex_case(n=3, lo=2, hi=5, seed=2, nodes=_abi.DG_NODES_GAUSS, rieman
                  precision=precision)
     q0 = problems.isentropic_vortex(mesh.x, mach, strength=5.0, period=L)
     return mesh, cfg, q0
+
+
+# Proper rotations of the reference cube (det +1), as matrices acting on local coordinates.
+CUBE_ROTATIONS = [
+    np.array([[0, -1, 0], [1, 0, 0], [0, 0, 1]]),   # 90 deg about zeta
+    np.array([[1, 0, 0], [0, 0, -1], [0, 1, 0]]),   # 90 deg about xi
+    np.array([[0, 0, 1], [0, 1, 0], [-1, 0, 0]]),   # 90 deg about eta
+    np.array([[0, 0, 1], [1, 0, 0], [0, 1, 0]]),    # cyclic xi -> eta -> zeta
+    np.array([[-1, 0, 0], [0, -1, 0], [0, 0, 1]]),  # 180 deg about zeta
+    np.array([[0, 1, 0], [1, 0, 0], [0, 0, -1]]),   # 180 deg about the xi=eta diagonal
+]
+_CORNERS = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]])
+
+
+def rotated_box_specmesh(path, n=4, length=TWO_PI, seed=0):
+    """A periodic n^3 box of straight hexahedra written as a SpecMesh file in which every interior
+    element lists its corners in a rotated local frame (a proper rotation of the reference cube, chosen
+    by seed), so the faces between elements carry non-zero leftIndexes2Right rotations."""
+    rng = np.random.default_rng(seed)
+    h = length / n
+    m1 = n + 1
+    nid = lambda i, j, k: 1 + i + m1 * (j + m1 * k)
+    lines = [f"{m1 ** 3} {n ** 3} 1"]
+    for k in range(m1):
+        for j in range(m1):
+            for i in range(m1):
+                lines.append(f"{i * h!r} {j * h!r} {k * h!r}")
+    for k in range(n):
+        for j in range(n):
+            for i in range(n):
+                ids = [nid(i + a, j + b, k + c) for a, b, c in _CORNERS]
+                names = ["front" if j == 0 else "---", "back" if j == n - 1 else "---",
+                         "bottom" if k == 0 else "---", "right" if i == n - 1 else "---",
+                         "top" if k == n - 1 else "---", "left" if i == 0 else "---"]
+                if all(nm == "---" for nm in names):
+                    R = CUBE_ROTATIONS[int(rng.integers(len(CUBE_ROTATIONS)))]
+                    old = {tuple(c): ids[q] for q, c in enumerate(_CORNERS)}
+                    ids = [old[tuple(int(v) for v in (R @ (2 * c - 1) + 1) // 2)] for c in _CORNERS]
+                lines.append(" ".join(str(v) for v in ids))
+                lines.append("0 0 0 0 0 0")
+                lines.append(" ".join(names))
+    path.write_text("\n".join(lines) + "\n")
+    return path
+
+
+def rotated_tgv_case(path, order, nodes=_abi.DG_NODES_GAUSS, riemann=_abi.DG_RIEMANN_ROE, n=4, seed=0,
+                     flow="ns", inviscid=_abi.DG_INVISCID_STANDARD, averaging=_abi.DG_AVG_STANDARD):
+    """Taylor-Green vortex (+1% perturbation) on the rotated-element box; order may be per element."""
+    rotated_box_specmesh(path, n=n, seed=seed)
+    mesh = HexMesh.from_specmesh(path, order, node_type=nodes)
+    cfg = Config(order=int(np.max(order)), nodes=nodes, flow=flow, mach=0.2, reynolds=800.0, riemann=riemann,
+                 inviscid=inviscid, averaging=averaging)
+    q0 = problems.taylor_green(mesh.x, 0.2, perturbation=0.01, seed=seed + 1)
+    return mesh, cfg, q0

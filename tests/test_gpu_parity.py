@@ -179,3 +179,36 @@ def test_nan_is_reported_not_trapped():
     g.compute_time_derivative(0.0)
     res, nan = g.compute_max_residuals()
     assert not nan and np.all(np.isfinite(res))
+
+
+@pytest.mark.parametrize("nodes,inviscid", [(_abi.DG_NODES_GAUSS, _abi.DG_INVISCID_STANDARD),
+                                            (_abi.DG_NODES_GAUSS_LOBATTO, _abi.DG_INVISCID_SPLIT)])
+def test_rotated_elements(tmp_path, nodes, inviscid):
+    """Faces with non-zero leftIndexes2Right rotations (interior elements in rotated local frames)."""
+    mesh, cfg, q0 = cases.rotated_tgv_case(tmp_path / "rot.mesh", 3, nodes=nodes, riemann=_abi.DG_RIEMANN_LXF,
+                                           inviscid=inviscid, averaging=_abi.DG_AVG_PIROZZOLI)
+    assert np.any(np.ctypeslib.as_array(mesh.desc.face_rotation, shape=(mesh.n_faces,)) != 0)
+    _check_rhs(mesh, cfg, q0)
+    _check_steps(mesh, cfg, q0, steps=3, dt=2e-3)
+
+
+@pytest.mark.parametrize("precision", [_abi.DG_PRECISION_FP64, _abi.DG_PRECISION_MIXED])
+def test_max_dt_filter_ties_and_high_mach(precision):
+    """The CFL reduction estimates every node in FP32 and evaluates the FP64 expressions only near the
+    estimated minimum. A uniform state makes every node tie; a supersonic perturbed state has large
+    kinetic-to-internal energy ratios; both must still give the oracle's FP64 minimum."""
+    mesh, cfg, q0 = cases.tgv_case(n=3, order=4, nodes=_abi.DG_NODES_GAUSS, warp=0.1, precision=precision)
+    uniform = np.tile([1.0, 0.3, -0.2, 0.1, 180.0], mesh.ndof)
+    fast = q0.reshape(-1, 5).copy()
+    fast[:, 1:4] *= 40.0  # |u| ~ 40 against a ~ 10: Mach ~ 4
+    fast[:, 4] += 0.5 * np.sum(fast[:, 1:4] ** 2, axis=1) / fast[:, 0]
+    for q in (uniform, fast.reshape(-1)):
+        o = oracle.Oracle(mesh, cfg.physics(), cfg.options())
+        o.set_state(q)
+        g = NavierStokesDG(mesh, cfg)
+        g.set_state(q)
+        for cfl, dcfl in ((0.4, 0.4), (0.5, 1e5), (0.3, 1e-3)):
+            ref = o.max_dt(cfl, dcfl)
+            # the mixed form keeps the metric terms in FP32, so its FP64 quotients see rounded metrics
+            tol = 1e-15 if precision == _abi.DG_PRECISION_FP64 else 1e-6
+            assert abs(g.max_time_step(cfl, dcfl) - ref) <= tol * ref, (cfl, dcfl)

@@ -212,3 +212,14 @@ def test_batch_cfl_steps_and_mixed_form():
         assert abs(t[k] - tt) <= 1e-6 * tt, (k, t[k], tt)
         err = rel_l2(got[k], o.get(0), m.quadrature_weights())
         assert np.all(err <= MIXED_TOL), (k, err)
+
+
+def test_anisotropic_rotated_elements(tmp_path):
+    """Per-element orders on elements in rotated local frames: the right side's face dimensions swap
+    under the odd rotations and the Tset interpolation runs in the rotated frame."""
+    orders = cases.random_orders(64, 1, 4, seed=3)
+    mesh, cfg, q0 = cases.rotated_tgv_case(tmp_path / "rot.mesh", orders)
+    rot = np.ctypeslib.as_array(mesh.desc.face_rotation, shape=(mesh.n_faces,))
+    assert np.any(np.isin(rot, [1, 3, 4, 6]))
+    _check_rhs(mesh, cfg, q0)
+    _check_steps(mesh, cfg, q0, steps=3, dt=2e-3)

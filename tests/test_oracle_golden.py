@@ -82,3 +82,25 @@ def test_oracle_free_stream_preservation_on_warped_mesh():
     q = np.tile([1.0, 0.3, -0.2, 0.1, 1.0 / (1.4 * 0.4 * 0.09) + 0.5 * 0.14], mesh.ndof)
     o.set_state(q)
     assert np.max(np.abs(o.rhs(0.0))) < 1e-11
+
+
+def test_rotated_elements_leave_the_rhs_unchanged(tmp_path):
+    """A box whose interior elements list their corners in rotated local frames has faces with non-zero
+    leftIndexes2Right rotations (MeshTypes.f90:70-107). The right-hand side of the same physical field
+    must have the same weighted L2 norm and integral as on the unrotated box, and a uniform state stays
+    uniform."""
+    mesh, cfg, _ = cases.rotated_tgv_case(tmp_path / "rot.mesh", 3)
+    rot = np.ctypeslib.as_array(mesh.desc.face_rotation, shape=(mesh.n_faces,))
+    assert len(set(rot.tolist()) - {0}) >= 4
+    box = HexMesh.box(4, [0, 0, 0], [cases.TWO_PI] * 3, 3, node_type=_abi.DG_NODES_GAUSS)
+    norms = []
+    for m in (box, mesh):
+        o = oracle.Oracle(m, cfg.physics(), cfg.options())
+        o.set_state(cases.problems.taylor_green(m.x, 0.2))
+        r = o.rhs(0.0).reshape(-1, 5)
+        w = m.quadrature_weights()
+        norms.append(np.sqrt(np.einsum("n,nv->v", w, r * r)))
+    assert np.allclose(norms[0], norms[1], rtol=1e-12, atol=0.0), norms
+    o = oracle.Oracle(mesh, cfg.physics(), cfg.options())
+    o.set_state(np.tile([1.0, 0.3, -0.2, 0.1, 45.0], mesh.ndof))
+    assert np.max(np.abs(o.rhs(0.0))) < 1e-10
