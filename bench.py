@@ -370,6 +370,19 @@ def run_secondary(name: str, args):
                      for a, b, m in zip(outs[_abi.DG_PRECISION_MIXED], outs[_abi.DG_PRECISION_FP64], meshes)])
     mixed = 3.0 * ndof * steps / (ms[_abi.DG_PRECISION_MIXED] * 1e-3)
     plain = 3.0 * ndof * steps / (ms[_abi.DG_PRECISION_FP64] * 1e-3)
+    cpu = None
+    if not args.no_cpu_baseline:  # one oracle RK3 step of every case, on all host cores
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle as oracle_mod
+
+        t0 = time.perf_counter()
+        for m, c, q in zip(meshes, cfgs, qs):
+            o = oracle_mod.Oracle(m, c.physics(), c.options())
+            o.set_state(q)
+            o.rk3_step(0.0, 1e-4)
+        el = time.perf_counter() - t0
+        cpu = {"value": 3.0 * ndof / el, "unit": "DOF*stage/s", "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"one RK3 step of every case ({el:.1f} s)"}
     line = {"workload": name, "metric": "DOF*RK-stage updates/s", "value": mixed, "unit": "DOF*stage/s",
             "n_gpus": 1, "steps": steps, "warmup": args.warmup,
             "ms_per_step": ms[_abi.DG_PRECISION_MIXED] / steps, "higher_is_better": True,
@@ -379,7 +392,7 @@ def run_secondary(name: str, args):
             "plain_fp64": {"value": plain, "ms_per_step": ms[_abi.DG_PRECISION_FP64] / steps},
             "mixed_over_plain": mixed / plain,
             "rel_l2_mixed_vs_fp64_max": [float(v) for v in errs.max(axis=0)],
-            "kernel_ms_mixed": kernels, "gpu_launches": launches}
+            "kernel_ms_mixed": kernels, "gpu_launches": launches, "cpu_baseline": cpu}
     print(json.dumps(line))
 
 
