@@ -164,11 +164,98 @@ __device__ __forceinline__ int neighbour_point(int map, int ca, int cb) {
     return ii + P * jj;
 }
 
-// Shared memory values (of R) per element of k_volume: state, gradient (later the fluxes), BR1
-// jumps of the six sides, metric vectors (split form only).
-template <int P>
-constexpr int volume_smem_values(bool split) {
-    return (5 + 15) * Geo<P>::P3 + 6 * (15 + 5) * Geo<P>::P2 + (split ? 9 * Geo<P>::P3 : 0);
+// Shared-memory operands of k_volume are 5-vectors (the five conserved variables, or the five
+// components of one direction of a gradient or flux) stored as a 16-byte part holding values 0..3 at
+// v4[4*i4] and the fifth value at v1[i1]: a 5-vector costs one 128-bit and one 32-bit load (two
+// 128-bit and one 64-bit for double) instead of five scalar loads, and nodes 16 or 48 bytes apart
+// keep the 128-bit load phases free of bank conflicts.
+template <typename R>
+__device__ __forceinline__ void ld5(const R* v4, int i4, const R* v1, int i1, R* o);
+template <>
+__device__ __forceinline__ void ld5<float>(const float* v4, int i4, const float* v1, int i1, float* o) {
+    const float4 t = *reinterpret_cast<const float4*>(v4 + 4 * i4);
+    o[0] = t.x;
+    o[1] = t.y;
+    o[2] = t.z;
+    o[3] = t.w;
+    o[4] = v1[i1];
+}
+template <>
+__device__ __forceinline__ void ld5<double>(const double* v4, int i4, const double* v1, int i1, double* o) {
+    const double2 x = *reinterpret_cast<const double2*>(v4 + 4 * i4);
+    const double2 y = *reinterpret_cast<const double2*>(v4 + 4 * i4 + 2);
+    o[0] = x.x;
+    o[1] = x.y;
+    o[2] = y.x;
+    o[3] = y.y;
+    o[4] = v1[i1];
+}
+template <typename R>
+__device__ __forceinline__ void st5(R* v4, int i4, R* v1, int i1, const R* x);
+template <>
+__device__ __forceinline__ void st5<float>(float* v4, int i4, float* v1, int i1, const float* x) {
+    *reinterpret_cast<float4*>(v4 + 4 * i4) = make_float4(x[0], x[1], x[2], x[3]);
+    v1[i1] = x[4];
+}
+template <>
+__device__ __forceinline__ void st5<double>(double* v4, int i4, double* v1, int i1, const double* x) {
+    *reinterpret_cast<double2*>(v4 + 4 * i4) = make_double2(x[0], x[1]);
+    *reinterpret_cast<double2*>(v4 + 4 * i4 + 2) = make_double2(x[2], x[3]);
+    v1[i1] = x[4];
+}
+
+// Offsets (values of R) of one element's k_volume workspace; every region starts on 16 bytes.
+//   Q4/Q1  state, 5-vector per node
+//   G4/G1  lifted gradient, 3 directions per node (later the contravariant or viscous fluxes)
+//   U4/U1  BR1 jumps uStar n per face point of the six sides, 3 directions
+//   T4/T1  own Q traces per face point of the six sides
+//   M      metric vectors per node (split form only)
+template <int P, typename R>
+struct VolLayout {
+    static constexpr int P2 = P * P, P3 = P * P * P, A = 16 / static_cast<int>(sizeof(R));
+    __host__ __device__ static constexpr int up(int x) { return (x + A - 1) / A * A; }
+    static constexpr int Q4 = 0, Q1 = Q4 + up(4 * P3);
+    static constexpr int G4 = Q1 + up(P3), G1 = G4 + up(12 * P3);
+    static constexpr int U4 = G1 + up(3 * P3), U1 = U4 + up(72 * P2);
+    static constexpr int T4 = U1 + up(18 * P2), T1 = T4 + up(24 * P2);
+    static constexpr int M = T1 + up(6 * P2);
+    __host__ __device__ static constexpr int values(bool split) { return M + (split ? up(9 * P3) : 0); }
+};
+
+template <int P, typename R>
+__host__ __device__ constexpr int volume_smem_values(bool split) {
+    return VolLayout<P, R>::values(split);
+}
+
+// Trace at face point (ca,cb) of a side of D 5-vectors per entry (entry m, direction d at
+// v4[(m*D+d)*4], v1[d*n+m]): sum_l v(l) s(line node l) in line order (HexElementClass.f90:233-372);
+// the Gauss-Lobatto end weights are unit vectors, so the end node is picked.
+template <int P, bool GL, int D, typename R>
+__device__ __forceinline__ void trace5(const Ops<R>& ops, const R* v4, const R* v1, int n, int side, int ca, int cb,
+                                       R out[D][5]) {
+    if (GL) {
+        const int m = line_node<P>(side, ca, cb, right_end(side) ? P - 1 : 0);
+#pragma unroll
+        for (int d = 0; d < D; ++d) ld5(v4, m * D + d, v1, d * n + m, out[d]);
+        return;
+    }
+    const R* w = right_end(side) ? ops.vR : ops.vL;
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+#pragma unroll
+        for (int v = 0; v < 5; ++v) out[d][v] = R(0);
+#pragma unroll
+    for (int l = 0; l < P; ++l) {
+        const int m = line_node<P>(side, ca, cb, l);
+        const R wl = w[l];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            R x[5];
+            ld5(v4, m * D + d, v1, d * n + m, x);
+#pragma unroll
+            for (int v = 0; v < 5; ++v) out[d][v] = out[d][v] + x[v] * wl;
+        }
+    }
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -204,19 +291,23 @@ __global__ void __launch_bounds__(Geo<P>::THREADS) k_traces(Args<R> a) {
 // ------------------------------------------------------------------------------------------------
 template <int P, bool GL, typename R>
 __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_volume(Args<R> a, int store_grad) {
-    constexpr int P2 = Geo<P>::P2, P3 = Geo<P>::P3, EPB = Geo<P>::EPB;
+    using L = VolLayout<P, R>;
+    constexpr int P2 = Geo<P>::P2, P3 = Geo<P>::P3, F6 = 6 * P2;
     const bool split = a.inviscid != 0;
     const bool ns = a.ph.ns;
     extern __shared__ __align__(16) unsigned char dsm[];
-    const int stride = volume_smem_values<P>(split);
     const int le = threadIdx.x / P3, n = threadIdx.x - le * P3;
-    R* sQ = reinterpret_cast<R*>(dsm) + le * stride;  // 5*P3: state
-    R* sG = sQ + 5 * P3;                              // 15*P3: lifted gradient (values v + 5 d)
-    R* sF = sG;                                       // 15*P3: then the contravariant or viscous fluxes
-    R* sU = sG + 15 * P3;                             // 6*15*P2: BR1 jumps uStar n per face point
-    R* sT = sU + 6 * 15 * P2;                         // 6*5*P2: own Q traces, reused for the viscous fluxes
-    R* sM = sT + 6 * 5 * P2;                          // 9*P3: metric vectors (split form)
-    const int e = blockIdx.x * EPB + le;
+    R* base = reinterpret_cast<R*>(dsm) + le * L::values(split);
+    R* Q4 = base + L::Q4;
+    R* Q1 = base + L::Q1;
+    R* G4 = base + L::G4;  // lifted gradient, then the fluxes (same layout)
+    R* G1 = base + L::G1;
+    R* U4 = base + L::U4;
+    R* U1 = base + L::U1;
+    R* T4 = base + L::T4;
+    R* T1 = base + L::T1;
+    R* sM = base + L::M;
+    const int e = blockIdx.x * Geo<P>::EPB + le;
     const bool active = e < a.K;
     const int i = n % P, j = (n / P) % P, k = n / P2;
     const int64_t g = static_cast<int64_t>(e) * P3 + n;
@@ -225,8 +316,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
     R jxs[3], jes[3], jzs[3];
     if (active) {
         load_state(a, g, q);
-#pragma unroll
-        for (int v = 0; v < 5; ++v) sQ[v * P3 + n] = q[v];
+        st5(Q4, n, Q1, n, q);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             jxs[c] = a.ja_xi[3 * g + c];
@@ -243,13 +333,30 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
             R uxi[5] = {0, 0, 0, 0, 0}, ueta[5] = {0, 0, 0, 0, 0}, uzeta[5] = {0, 0, 0, 0, 0};
 #pragma unroll
             for (int l = 0; l < P; ++l) {
-                const R dx = a.ops.D[i * kMaxP + l], dy = a.ops.D[j * kMaxP + l], dz = a.ops.D[k * kMaxP + l];
+                const R w = a.ops.D[i * kMaxP + l];
+                const int m = l + P * (j + P * k);
+                R x[5];
+                ld5(Q4, m, Q1, m, x);
 #pragma unroll
-                for (int v = 0; v < 5; ++v) {
-                    uxi[v] = uxi[v] + sQ[v * P3 + l + P * (j + P * k)] * dx;
-                    ueta[v] = ueta[v] + sQ[v * P3 + i + P * (l + P * k)] * dy;
-                    uzeta[v] = uzeta[v] + sQ[v * P3 + i + P * (j + P * l)] * dz;
-                }
+                for (int v = 0; v < 5; ++v) uxi[v] = uxi[v] + x[v] * w;
+            }
+#pragma unroll
+            for (int l = 0; l < P; ++l) {
+                const R w = a.ops.D[j * kMaxP + l];
+                const int m = i + P * (l + P * k);
+                R x[5];
+                ld5(Q4, m, Q1, m, x);
+#pragma unroll
+                for (int v = 0; v < 5; ++v) ueta[v] = ueta[v] + x[v] * w;
+            }
+#pragma unroll
+            for (int l = 0; l < P; ++l) {
+                const R w = a.ops.D[k * kMaxP + l];
+                const int m = i + P * (j + P * l);
+                R x[5];
+                ld5(Q4, m, Q1, m, x);
+#pragma unroll
+                for (int v = 0; v < 5; ++v) uzeta[v] = uzeta[v] + x[v] * w;
             }
             const R ij = a.inv_jac[g];
 #pragma unroll
@@ -259,82 +366,74 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
                 U[2][v] = (uxi[v] * jxs[2] + ueta[v] * jes[2] + uzeta[v] * jzs[2]) * ij;
             }
             // BR1 jumps at the six sides: 1/2 (U_R - U_L) Jf n in the face's orientation (left -> right)
-            for (int t = n; t < 6 * P2; t += P3) {
+            for (int t = n; t < F6; t += P3) {
                 const int side = 1 + t / P2, p = t - (side - 1) * P2;
                 const int ca = p % P, cb = p / P;
                 const int64_t s = slot(e, side);
-                R own[5], nbr[5];
-                trace<P, GL, 5>(a.ops, sQ, side, ca, cb, own);
-#pragma unroll
-                for (int v = 0; v < 5; ++v) sT[((side - 1) * 5 + v) * P2 + p] = own[v];
+                R own[1][5], nbr[5];
+                trace5<P, GL, 1>(a.ops, Q4, Q1, P3, side, ca, cb, own);
+                st5(T4, t, T1, t, own[0]);
                 const int map = a.nb_map[s];
                 const int pn = neighbour_point<P>(map, ca, cb);
                 const R* nq = a.QF + static_cast<int64_t>(a.nb_slot[s]) * 5 * P2 + pn;
 #pragma unroll
                 for (int v = 0; v < 5; ++v) nbr[v] = nq[v * P2];
                 const R* sg = a.sgeo + s * 4 * P2 + p;
-                const R n0 = sg[0], n1 = sg[P2], n2 = sg[2 * P2], J = sg[3 * P2];
+                const R nn[3] = {sg[0], sg[P2], sg[2 * P2]};
+                const R J = sg[3 * P2];
                 const bool left = (map >> 3) == 1;
-                R* d = sU + (side - 1) * 15 * P2 + p;
+                R u[5];
 #pragma unroll
-                for (int v = 0; v < 5; ++v) {
-                    const R u = R(0.5) * (left ? (nbr[v] - own[v]) : (own[v] - nbr[v])) * J;
-                    d[v * P2] = u * n0;
-                    d[(5 + v) * P2] = u * n1;
-                    d[(10 + v) * P2] = u * n2;
+                for (int v = 0; v < 5; ++v) u[v] = R(0.5) * (left ? (nbr[v] - own[0][v]) : (own[0][v] - nbr[v])) * J;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    R x[5];
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) x[v] = u[v] * nn[d];
+                    st5(U4, t * 3 + d, U1, d * F6 + t, x);
                 }
             }
         }
         __syncthreads();
         if (active) {
-            // lifting: U += (sum over sides of b (x) uStar n) / J (VectorWeakIntegrals_StdFace order)
+            // lifting: U += (sum over sides of b (x) uStar n) / J in VectorWeakIntegrals_StdFace order
+            // (left, right, front, back, bottom, top)
             const R ij = a.inv_jac[g];
-            const R* HL = sU + 5 * 15 * P2 + (j + P * k);
-            const R* HR = sU + 3 * 15 * P2 + (j + P * k);
-            const R* HF = sU + 0 * 15 * P2 + (i + P * k);
-            const R* HB = sU + 1 * 15 * P2 + (i + P * k);
-            const R* HO = sU + 2 * 15 * P2 + (i + P * j);
-            const R* HT = sU + 4 * 15 * P2 + (i + P * j);
+            const int pt[6] = {(5 * P2) + (j + P * k), (3 * P2) + (j + P * k), (0 * P2) + (i + P * k),
+                               (1 * P2) + (i + P * k), (2 * P2) + (i + P * j), (4 * P2) + (i + P * j)};
+            R bw[6];
+            bool use[6];
             if (GL) {  // b(:,LEFT/RIGHT) vanish away from the end nodes
                 const R bl = a.ops.bL[0], br = a.ops.bR[P - 1];
-                const bool iL = i == 0, iR = i == P - 1, jL = j == 0, jR = j == P - 1, kL = k == 0, kR = k == P - 1;
-                if (iL || iR || jL || jR || kL || kR) {
-#pragma unroll
-                    for (int d = 0; d < 3; ++d)
-#pragma unroll
-                        for (int v = 0; v < 5; ++v) {
-                            const int c = (v + 5 * d) * P2;
-                            R fi = R(0);
-                            if (iL) fi = HL[c] * bl;
-                            if (iR) fi = fi + HR[c] * br;
-                            if (jL) fi = fi + HF[c] * bl;
-                            if (jR) fi = fi + HB[c] * br;
-                            if (kL) fi = fi + HO[c] * bl;
-                            if (kR) fi = fi + HT[c] * br;
-                            U[d][v] = U[d][v] + fi * ij;
-                        }
-                }
+                use[0] = i == 0; use[1] = i == P - 1; use[2] = j == 0; use[3] = j == P - 1; use[4] = k == 0;
+                use[5] = k == P - 1;
+                bw[0] = bl; bw[1] = br; bw[2] = bl; bw[3] = br; bw[4] = bl; bw[5] = br;
             } else {
-                const R bxl = a.ops.bL[i], bxr = a.ops.bR[i], byl = a.ops.bL[j], byr = a.ops.bR[j];
-                const R bzl = a.ops.bL[k], bzr = a.ops.bR[k];
+                bw[0] = a.ops.bL[i]; bw[1] = a.ops.bR[i]; bw[2] = a.ops.bL[j]; bw[3] = a.ops.bR[j];
+                bw[4] = a.ops.bL[k]; bw[5] = a.ops.bR[k];
 #pragma unroll
-                for (int d = 0; d < 3; ++d)
+                for (int sd = 0; sd < 6; ++sd) use[sd] = true;
+            }
+            if (!GL || use[0] || use[1] || use[2] || use[3] || use[4] || use[5]) {
 #pragma unroll
-                    for (int v = 0; v < 5; ++v) {
-                        const int c = (v + 5 * d) * P2;
-                        R fi = HL[c] * bxl;
-                        fi = fi + HR[c] * bxr;
-                        fi = fi + HF[c] * byl;
-                        fi = fi + HB[c] * byr;
-                        fi = fi + HO[c] * bzl;
-                        fi = fi + HT[c] * bzr;
-                        U[d][v] = U[d][v] + fi * ij;
+                for (int d = 0; d < 3; ++d) {
+                    R fi[5] = {0, 0, 0, 0, 0};
+                    bool first = true;
+#pragma unroll
+                    for (int sd = 0; sd < 6; ++sd) {
+                        if (!use[sd]) continue;
+                        R h[5];
+                        ld5(U4, pt[sd] * 3 + d, U1, d * F6 + pt[sd], h);
+#pragma unroll
+                        for (int v = 0; v < 5; ++v) fi[v] = first ? h[v] * bw[sd] : fi[v] + h[v] * bw[sd];
+                        first = false;
                     }
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) U[d][v] = U[d][v] + fi[v] * ij;
+                }
             }
 #pragma unroll
-            for (int d = 0; d < 3; ++d)
-#pragma unroll
-                for (int v = 0; v < 5; ++v) sG[(v + 5 * d) * P3 + n] = U[d][v];
+            for (int d = 0; d < 3; ++d) st5(G4, n * 3 + d, G1, d * P3 + n, U[d]);
             if (store_grad) {
 #pragma unroll
                 for (int v = 0; v < 5; ++v) {
@@ -347,18 +446,17 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
         __syncthreads();
         if (active) {
             // viscous normal flux of this side at its face points: Fv(Q, grad U, mu(Q)) . n
-            for (int t = n; t < 6 * P2; t += P3) {
+            for (int t = n; t < F6; t += P3) {
                 const int side = 1 + t / P2, p = t - (side - 1) * P2;
                 const int ca = p % P, cb = p / P;
                 const int64_t s = slot(e, side);
-                R tq[5], tg[15];
-#pragma unroll
-                for (int v = 0; v < 5; ++v) tq[v] = sT[((side - 1) * 5 + v) * P2 + p];
-                trace<P, GL, 15>(a.ops, sG, side, ca, cb, tg);
+                R tq[5], tg[3][5];
+                ld5(T4, t, T1, t, tq);
+                trace5<P, GL, 3>(a.ops, G4, G1, P3, side, ca, cb, tg);
                 R mu, kap;
                 mu_kappa(a.ph, tq, mu, kap);
                 R C[3][5];
-                viscous_flux(a.ph, tq, tg, tg + 5, tg + 10, mu, kap, C);
+                viscous_flux(a.ph, tq, tg[0], tg[1], tg[2], mu, kap, C);
                 const R* sg = a.sgeo + s * 4 * P2 + p;
                 const R n0 = sg[0], n1 = sg[P2], n2 = sg[2 * P2];
                 R* d = a.FV + s * 5 * P2 + p;
@@ -368,20 +466,20 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
         }
     }
 
-    __syncthreads();  // sG is read above and reused as sF below
+    __syncthreads();  // the gradient is read above and its space reused for the fluxes below
     // contravariant fluxes (HyperbolicDiscretizationClass.f90:132-149, EllipticBR1.f90:794-812);
-    // the lifted gradient is read back from this node's own column of sG
+    // the lifted gradient is read back from this node's own entries
     R Fi[3][5], Fv[3][5];
     if (active) {
         euler_contravariant(a.ph, q, jxs, jes, jzs, Fi);
         if (ns) {
-            R Ug[15];
+            R Ug[3][5];
 #pragma unroll
-            for (int c = 0; c < 15; ++c) Ug[c] = sG[c * P3 + n];
+            for (int d = 0; d < 3; ++d) ld5(G4, n * 3 + d, G1, d * P3 + n, Ug[d]);
             R mu, kappa;
             mu_kappa(a.ph, q, mu, kappa);
             R C[3][5];
-            viscous_flux(a.ph, q, Ug, Ug + 5, Ug + 10, mu, kappa, C);
+            viscous_flux(a.ph, q, Ug[0], Ug[1], Ug[2], mu, kappa, C);
             const R* ja[3] = {jxs, jes, jzs};
 #pragma unroll
             for (int d = 0; d < 3; ++d)
@@ -398,9 +496,12 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
         // ScalarWeakIntegrals_StdVolumeGreen on F = Finv - Fvisc
         if (active) {
 #pragma unroll
-            for (int d = 0; d < 3; ++d)
+            for (int d = 0; d < 3; ++d) {
+                R x[5];
 #pragma unroll
-                for (int v = 0; v < 5; ++v) sF[(v + 5 * d) * P3 + n] = Fi[d][v] - Fv[d][v];
+                for (int v = 0; v < 5; ++v) x[v] = Fi[d][v] - Fv[d][v];
+                st5(G4, n * 3 + d, G1, d * P3 + n, x);
+            }
         }
         __syncthreads();
         if (!active) return;
@@ -408,20 +509,29 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
 #pragma unroll
         for (int l = 0; l < P; ++l) {
             const R h = a.ops.hatD[i * kMaxP + l];
+            const int m = l + P * (j + P * k);
+            R x[5];
+            ld5(G4, m * 3 + 0, G1, 0 * P3 + m, x);
 #pragma unroll
-            for (int v = 0; v < 5; ++v) acc[v] = acc[v] + h * sF[v * P3 + l + P * (j + P * k)];
+            for (int v = 0; v < 5; ++v) acc[v] = acc[v] + h * x[v];
         }
 #pragma unroll
         for (int l = 0; l < P; ++l) {
             const R h = a.ops.hatD[j * kMaxP + l];
+            const int m = i + P * (l + P * k);
+            R x[5];
+            ld5(G4, m * 3 + 1, G1, 1 * P3 + m, x);
 #pragma unroll
-            for (int v = 0; v < 5; ++v) acc[v] = acc[v] + h * sF[(5 + v) * P3 + i + P * (l + P * k)];
+            for (int v = 0; v < 5; ++v) acc[v] = acc[v] + h * x[v];
         }
 #pragma unroll
         for (int l = 0; l < P; ++l) {
             const R h = a.ops.hatD[k * kMaxP + l];
+            const int m = i + P * (j + P * l);
+            R x[5];
+            ld5(G4, m * 3 + 2, G1, 2 * P3 + m, x);
 #pragma unroll
-            for (int v = 0; v < 5; ++v) acc[v] = acc[v] + h * sF[(10 + v) * P3 + i + P * (j + P * l)];
+            for (int v = 0; v < 5; ++v) acc[v] = acc[v] + h * x[v];
         }
 #pragma unroll
         for (int v = 0; v < 5; ++v) a.QDot[5 * g + v] = acc[v];
@@ -431,9 +541,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
         // volInt += sharpD(i,l) f#(l,i) + hatD(i,l) Fv(l) (DGIntegrals.f90:92-129), QDot = -volInt.
         if (active) {
 #pragma unroll
-            for (int d = 0; d < 3; ++d)
-#pragma unroll
-                for (int v = 0; v < 5; ++v) sF[(v + 5 * d) * P3 + n] = Fv[d][v];
+            for (int d = 0; d < 3; ++d) st5(G4, n * 3 + d, G1, d * P3 + n, Fv[d]);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 sM[c * P3 + n] = jxs[c];
@@ -457,8 +565,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
                     for (int v = 0; v < 5; ++v) fs[v] = Fi[d][v];
                 } else {
                     R qo[5], jo[3];
-#pragma unroll
-                    for (int v = 0; v < 5; ++v) qo[v] = sQ[v * P3 + m];
+                    ld5(Q4, m, Q1, m, qo);
 #pragma unroll
                     for (int c = 0; c < 3; ++c) jo[c] = sM[(3 * d + c) * P3 + m];
                     // each pair is evaluated with the lower line index as "left", as the reference does
@@ -467,8 +574,10 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
                 }
                 const R sh = a.ops.sharpD[self * kMaxP + l];
                 const R h = a.ops.hatD[self * kMaxP + l];
+                R fv[5];
+                ld5(G4, m * 3 + d, G1, d * P3 + m, fv);
 #pragma unroll
-                for (int v = 0; v < 5; ++v) acc[v] = acc[v] + sh * fs[v] + h * sF[(v + 5 * d) * P3 + m];
+                for (int v = 0; v < 5; ++v) acc[v] = acc[v] + sh * fs[v] + h * fv[v];
             }
         }
 #pragma unroll

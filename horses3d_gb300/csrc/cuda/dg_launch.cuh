@@ -20,7 +20,7 @@ using StageFn = cudaError_t (*)(const Args<R>& a, int stage, double tshift, int 
 
 template <int P, typename R>
 size_t volume_smem_bytes(int inviscid) {
-    return static_cast<size_t>(Geo<P>::EPB) * volume_smem_values<P>(inviscid != 0) * sizeof(R);
+    return static_cast<size_t>(Geo<P>::EPB) * volume_smem_values<P, R>(inviscid != 0) * sizeof(R);
 }
 
 template <int P, bool GL, typename R>
