@@ -134,6 +134,7 @@ int setup_store(dg_ctx* c, Store<R>& st, const dg_mesh_desc* m) {
     a.Q = c->Q.p; a.G = c->G.p; a.QDot = st.QDot.p;
     a.Ux = st.Ux.p; a.Uy = st.Uy.p; a.Uz = st.Uz.p;
     a.QF = st.QF.p; a.FV = st.FV.p; a.FS = st.FS.p;
+    a.nsp = static_cast<int64_t>(nslot) * c->P * c->P;
     a.time = c->scal.p;
     a.dt = c->scal.p + 1;
     a.src_gm1 = c->pc.gm1;

@@ -19,11 +19,12 @@
 //   k_traces    element: Q face traces of the current state (after an upload)
 //
 // Face data live in element-face "slots" (slot = 6e + side-1, sides numbered as the reference), in
-// the element's own face coordinates (the FaceStorage(side) arrays), stored per variable:
-// value(slot, var, p) at [(slot*NV + var)*P^2 + p], p = a + P*b.
+// the element's own face coordinates (the FaceStorage(side) arrays), one 5-vector per slot point
+// idx = slot*P^2 + p, p = a + P*b: values 0..3 at [4*idx], the fifth at [4*nsp + idx].
 #pragma once
 #include <cstdint>
 
+#include "dg_convert.cuh"
 #include "dg_physics.cuh"
 
 namespace dg {
@@ -68,9 +69,12 @@ struct Args {
     R* Ux;  // lifted gradient, written only when store_grad is set
     R* Uy;
     R* Uz;
-    R* QF;   // Q traces          [6K][5][P^2]
-    R* FV;   // viscous n-fluxes  [6K][5][P^2]
-    R* FS;   // surface fluxes    [6K][5][P^2]
+    // slot arrays, one 5-vector per slot point idx = slot*P^2 + p (see gld5): Q traces, viscous
+    // normal fluxes of each side, surface fluxes
+    R* QF;
+    R* FV;
+    R* FS;
+    int64_t nsp;  // slot points, 6 K P^2
     const double* time;  // device scalars: step start time and dt
     const double* dt;
     double e_ref;        // energy reference of the mixed form (0 for the plain form)
@@ -99,11 +103,19 @@ struct Occupancy {
 __device__ __forceinline__ int64_t slot(int e, int side) { return 6 * static_cast<int64_t>(e) + (side - 1); }
 
 // The FP64 state of node g in the working precision; the energy relative to e_ref (FP64 difference).
-template <typename R>
+// INT selects the integer-pipe conversion (kernels whose FP64 pipe is their bottleneck) over the
+// hardware one (issue-bound kernels, where the extra integer instructions cost more).
+template <bool INT = false, typename R>
 __device__ __forceinline__ void load_state(const Args<R>& a, int64_t g, R* q) {
+    if (INT) {
 #pragma unroll
-    for (int v = 0; v < 4; ++v) q[v] = R(a.Q[5 * g + v]);
-    q[4] = R(a.Q[5 * g + 4] - a.e_ref);
+        for (int v = 0; v < 4; ++v) q[v] = from_f64<R>(a.Q[5 * g + v]);
+        q[4] = from_f64<R>(a.Q[5 * g + 4] - a.e_ref);
+    } else {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) q[v] = R(a.Q[5 * g + v]);
+        q[4] = R(a.Q[5 * g + 4] - a.e_ref);
+    }
 }
 
 // Node of line position l through face point (ca, cb) of a side.
@@ -116,30 +128,6 @@ __device__ __forceinline__ int line_node(int side, int ca, int cb, int l) {
     }
 }
 __device__ __forceinline__ bool right_end(int side) { return side == 2 || side == 4 || side == 5; }
-
-// Trace of NV values stored per variable in s (value v of node m at s[v*P3 + m]) at face point
-// (ca,cb) of a side: sum_l v(l) s(line node l) in line order (HexElementClass.f90:233-372); the
-// Gauss-Lobatto end weights are unit vectors, so the end node is picked.
-template <int P, bool GL, int NV, typename R>
-__device__ __forceinline__ void trace(const Ops<R>& ops, const R* s, int side, int ca, int cb, R* out) {
-    constexpr int P3 = P * P * P;
-    if (GL) {
-        const int m = line_node<P>(side, ca, cb, right_end(side) ? P - 1 : 0);
-#pragma unroll
-        for (int v = 0; v < NV; ++v) out[v] = s[v * P3 + m];
-        return;
-    }
-    const R* w = right_end(side) ? ops.vR : ops.vL;
-#pragma unroll
-    for (int v = 0; v < NV; ++v) out[v] = R(0);
-#pragma unroll
-    for (int l = 0; l < P; ++l) {
-        const int m = line_node<P>(side, ca, cb, l);
-        const R wl = w[l];
-#pragma unroll
-        for (int v = 0; v < NV; ++v) out[v] = out[v] + s[v * P3 + m] * wl;
-    }
-}
 
 // Neighbour point of own face point (ca,cb): leftIndexes2Right from side 1, its inverse from side 2.
 template <int P>
@@ -204,6 +192,17 @@ __device__ __forceinline__ void st5<double>(double* v4, int i4, double* v1, int 
     v1[i1] = x[4];
 }
 
+// Slot arrays in global memory use the same split: the 16-byte parts of all slot points first, then
+// the fifth values; the threads of a face read consecutive 16-byte parts (coalesced 128-bit loads).
+template <typename R>
+__device__ __forceinline__ void gld5(const R* base, int64_t nsp, int64_t idx, R* o) {
+    ld5(base + 4 * idx, 0, base + 4 * nsp + idx, 0, o);
+}
+template <typename R>
+__device__ __forceinline__ void gst5(R* base, int64_t nsp, int64_t idx, const R* x) {
+    st5(base + 4 * idx, 0, base + 4 * nsp + idx, 0, x);
+}
+
 // Offsets (values of R) of one element's k_volume workspace; every region starts on 16 bytes.
 //   Q4/Q1  state, 5-vector per node
 //   G4/G1  lifted gradient, 3 directions per node (later the contravariant or viscous fluxes)
@@ -264,25 +263,23 @@ __device__ __forceinline__ void trace5(const Ops<R>& ops, const R* v4, const R* 
 template <int P, bool GL, typename R>
 __global__ void __launch_bounds__(Geo<P>::THREADS) k_traces(Args<R> a) {
     constexpr int P2 = Geo<P>::P2, P3 = Geo<P>::P3, EPB = Geo<P>::EPB;
-    __shared__ R sQ[EPB][5 * P3];
+    __shared__ __align__(16) R sQ4[EPB][4 * P3];
+    __shared__ R sQ1[EPB][P3];
     const int le = threadIdx.x / P3, n = threadIdx.x - le * P3;
     const int e = blockIdx.x * EPB + le;
     const bool active = e < a.K;
     if (active) {
         R q[5];
-        load_state(a, static_cast<int64_t>(e) * P3 + n, q);
-#pragma unroll
-        for (int v = 0; v < 5; ++v) sQ[le][v * P3 + n] = q[v];
+        load_state<true>(a, static_cast<int64_t>(e) * P3 + n, q);
+        st5(sQ4[le], n, sQ1[le], n, q);
     }
     __syncthreads();
     if (!active) return;
     for (int t = n; t < 6 * P2; t += P3) {
         const int side = 1 + t / P2, p = t - (side - 1) * P2;
-        R tq[5];
-        trace<P, GL, 5>(a.ops, sQ[le], side, p % P, p / P, tq);
-        R* d = a.QF + slot(e, side) * 5 * P2 + p;
-#pragma unroll
-        for (int v = 0; v < 5; ++v) d[v * P2] = tq[v];
+        R tq[1][5];
+        trace5<P, GL, 1>(a.ops, sQ4[le], sQ1[le], P3, side, p % P, p / P, tq);
+        gst5(a.QF, a.nsp, slot(e, side) * P2 + p, tq[0]);
     }
 }
 
@@ -375,9 +372,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
                 st5(T4, t, T1, t, own[0]);
                 const int map = a.nb_map[s];
                 const int pn = neighbour_point<P>(map, ca, cb);
-                const R* nq = a.QF + static_cast<int64_t>(a.nb_slot[s]) * 5 * P2 + pn;
-#pragma unroll
-                for (int v = 0; v < 5; ++v) nbr[v] = nq[v * P2];
+                gld5(a.QF, a.nsp, static_cast<int64_t>(a.nb_slot[s]) * P2 + pn, nbr);
                 const R* sg = a.sgeo + s * 4 * P2 + p;
                 const R nn[3] = {sg[0], sg[P2], sg[2 * P2]};
                 const R J = sg[3 * P2];
@@ -459,9 +454,10 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
                 viscous_flux(a.ph, tq, tg[0], tg[1], tg[2], mu, kap, C);
                 const R* sg = a.sgeo + s * 4 * P2 + p;
                 const R n0 = sg[0], n1 = sg[P2], n2 = sg[2 * P2];
-                R* d = a.FV + s * 5 * P2 + p;
+                R fv[5];
 #pragma unroll
-                for (int v = 0; v < 5; ++v) d[v * P2] = C[0][v] * n0 + C[1][v] * n1 + C[2][v] * n2;
+                for (int v = 0; v < 5; ++v) fv[v] = C[0][v] * n0 + C[1][v] * n1 + C[2][v] * n2;
+                gst5(a.FV, a.nsp, s * P2 + p, fv);
             }
         }
     }
@@ -598,14 +594,11 @@ __global__ void __launch_bounds__(128) k_flux(Args<R> a) {
     int ii, jj;
     left2right(p % P, p / P, P - 1, P - 1, a.face_rot[f], ii, jj);
     const int pr = ii + P * jj;
-    const int64_t bL = slot(a.face_elem[2 * f], a.face_side[2 * f]) * 5 * P2;
-    const int64_t bR = slot(a.face_elem[2 * f + 1], a.face_side[2 * f + 1]) * 5 * P2;
+    const int64_t iL = slot(a.face_elem[2 * f], a.face_side[2 * f]) * P2 + p;
+    const int64_t iR = slot(a.face_elem[2 * f + 1], a.face_side[2 * f + 1]) * P2 + pr;
     R QL[5], QR[5];
-#pragma unroll
-    for (int v = 0; v < 5; ++v) {
-        QL[v] = a.QF[bL + v * P2 + p];
-        QR[v] = a.QF[bR + v * P2 + pr];
-    }
+    gld5(a.QF, a.nsp, iL, QL);
+    gld5(a.QF, a.nsp, iR, QR);
     const R n[3] = {a.fn[gid], a.fn[nfp + gid], a.fn[2 * nfp + gid]};
     const R J = a.fj[gid];
     R inv[5];
@@ -616,14 +609,20 @@ __global__ void __launch_bounds__(128) k_flux(Args<R> a) {
         const R t2[3] = {a.ft2[gid], a.ft2[nfp + gid], a.ft2[2 * nfp + gid]};
         lxf_flux(a.ph, QL, QR, n, t1, t2, inv);
     }
+    R vL[5] = {0, 0, 0, 0, 0}, vR[5] = {0, 0, 0, 0, 0};
+    if (a.ph.ns) {
+        gld5(a.FV, a.nsp, iL, vL);
+        gld5(a.FV, a.nsp, iR, vR);
+    }
+    R fl[5], fr[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
-        R visc = R(0);
-        if (a.ph.ns) visc = R(0.5) * (a.FV[bL + v * P2 + p] + a.FV[bR + v * P2 + pr]);
-        const R fl = (inv[v] - visc) * J;
-        a.FS[bL + v * P2 + p] = fl;
-        a.FS[bR + v * P2 + pr] = -fl;
+        const R visc = a.ph.ns ? R(0.5) * (vL[v] + vR[v]) : R(0);
+        fl[v] = (inv[v] - visc) * J;
+        fr[v] = -fl[v];
     }
+    gst5(a.FS, a.nsp, iL, fl);
+    gst5(a.FS, a.nsp, iR, fr);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -635,14 +634,15 @@ template <int P, bool GL, bool SRC, typename R>
 __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
     k_update(Args<R> a, int stage, double tshift, int write_qdot) {
     constexpr int P2 = Geo<P>::P2, P3 = Geo<P>::P3, EPB = Geo<P>::EPB;
-    __shared__ R sQ[EPB][5 * P3];
+    __shared__ __align__(16) R sQ4[EPB][4 * P3];
+    __shared__ R sQ1[EPB][P3];
     const int le = threadIdx.x / P3, n = threadIdx.x - le * P3;
     const int e = blockIdx.x * EPB + le;
     const bool active = e < a.K;
     const int i = n % P, j = (n / P) % P, k = n / P2;
     const int64_t g = static_cast<int64_t>(e) * P3 + n;
     if (active) {
-        const R* FS = a.FS + slot(e, 1) * 5 * P2;  // the six slots of e are contiguous
+        const int64_t s1 = slot(e, 1) * P2;  // the six slots of e are contiguous
         const int pL = j + P * k, pF = i + P * k, pO = i + P * j;
         // every load of the node up front (QDot, J, the six surface fluxes, G and Q), then the math
         R qd[5], fs[6][5];
@@ -654,9 +654,14 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
                              GL ? i == P - 1 : true, GL ? k == P - 1 : true, GL ? i == 0 : true};
         const int pt[6] = {pF, pF, pO, pL, pO, pL};
 #pragma unroll
-        for (int sd = 0; sd < 6; ++sd)
+        for (int sd = 0; sd < 6; ++sd) {
+            if (use[sd]) {
+                gld5(a.FS, a.nsp, s1 + sd * P2 + pt[sd], fs[sd]);
+            } else {
 #pragma unroll
-            for (int v = 0; v < 5; ++v) fs[sd][v] = use[sd] ? FS[(sd * 5 + v) * P2 + pt[sd]] : R(0);
+                for (int v = 0; v < 5; ++v) fs[sd][v] = R(0);
+            }
+        }
         if (stage >= 0) {
 #pragma unroll
             for (int v = 0; v < 5; ++v) {
@@ -710,7 +715,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
             const double cdt = ck * dt;
 #pragma unroll
             for (int v = 0; v < 5; ++v) {
-                gq[v] = ak * gq[v] + double(qd[v]);
+                gq[v] = ak * gq[v] + widen(qd[v]);
                 qq[v] = qq[v] + cdt * gq[v];
             }
 #pragma unroll
@@ -718,9 +723,9 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
                 a.G[5 * g + v] = gq[v];
                 a.Q[5 * g + v] = qq[v];
             }
-#pragma unroll
-            for (int v = 0; v < 4; ++v) sQ[le][v * P3 + n] = R(qq[v]);
-            sQ[le][4 * P3 + n] = R(qq[4] - a.e_ref);
+            const R qn[5] = {from_f64<R>(qq[0]), from_f64<R>(qq[1]), from_f64<R>(qq[2]), from_f64<R>(qq[3]),
+                             from_f64<R>(qq[4] - a.e_ref)};
+            st5(sQ4[le], n, sQ1[le], n, qn);
         }
     }
     if (stage < 0) return;
@@ -728,11 +733,9 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
     if (!active) return;
     for (int t = n; t < 6 * P2; t += P3) {  // Q traces of the updated state
         const int side = 1 + t / P2, p = t - (side - 1) * P2;
-        R tq[5];
-        trace<P, GL, 5>(a.ops, sQ[le], side, p % P, p / P, tq);
-        R* d = a.QF + slot(e, side) * 5 * P2 + p;
-#pragma unroll
-        for (int v = 0; v < 5; ++v) d[v * P2] = tq[v];
+        R tq[1][5];
+        trace5<P, GL, 1>(a.ops, sQ4[le], sQ1[le], P3, side, p % P, p / P, tq);
+        gst5(a.QF, a.nsp, slot(e, side) * P2 + p, tq[0]);
     }
 }
 

@@ -141,7 +141,7 @@ __host__ __device__ inline DtConst32 dt_const32(double cfl, double dcfl, const d
 template <typename R>
 __device__ __forceinline__ void dt_estimate(const DtConst32& d, const double* Q, const R* jx, const R* je, const R* jz,
                                             R jac, float& conv, float& visc) {
-    const float rho = float(Q[0]), ru = float(Q[1]), rv = float(Q[2]), rw = float(Q[3]), E = float(Q[4]);
+    const float rho = to_f32(Q[0]), ru = to_f32(Q[1]), rv = to_f32(Q[2]), rw = to_f32(Q[3]), E = to_f32(Q[4]);
     const float ir = 1.0f / rho;
     const float p = d.gm1 * (E - 0.5f * (ru * ru + rv * rv + rw * rw) * ir);
     const float a = sqrtf(d.gamma * p * ir);
