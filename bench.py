@@ -360,11 +360,17 @@ def run_secondary(name: str, args):
         b64 = make(_abi.DG_PRECISION_FP64)
         dts = b64.max_time_steps(CFL, CFL)
         bm = make(_abi.DG_PRECISION_MIXED)
+        t_tune = time.perf_counter()
+        if not args.no_autotune:
+            b64.autotune(5)  # elements per CTA of every order triple (cached for the process)
+            bm.autotune(5)
+        t_tune = time.perf_counter() - t_tune
         ms = {_abi.DG_PRECISION_FP64: timed(b64, dts), _abi.DG_PRECISION_MIXED: timed(bm, dts)}
         outs = {_abi.DG_PRECISION_FP64: b64.get(), _abi.DG_PRECISION_MIXED: bm.get()}
         kt = np.zeros(5)
         _abi.check(_abi.lib().dg_kernel_times(bm._h, 10, 0.0, 0.0, _abi.f64ptr(kt)), "dg_kernel_times")
         kernels = dict(zip(["volume", "face_flux", "update", "traces", "face_jump"], [round(float(v), 5) for v in kt]))
+        kernels["autotune_s"] = round(t_tune, 2)
         launches = steps * 3 * (4 if cfgs[0].flow == "ns" else 3)
     errs = np.array([rel_l2(a, b, m.quadrature_weights())
                      for a, b, m in zip(outs[_abi.DG_PRECISION_MIXED], outs[_abi.DG_PRECISION_FP64], meshes)])
@@ -427,6 +433,7 @@ def main():
                     help="profiling run: only warm-up + timed steps of one form, no extra legs")
     ap.add_argument("--workload", choices=["tgv32_curvilinear", *SECONDARY], default="tgv32_curvilinear",
                     help="the headline workload (default) or one of the other benchmark configurations")
+    ap.add_argument("--no-autotune", action="store_true", help="variable-order workloads: default item sizes")
     args = ap.parse_args()
     args.steps_given = "--steps" in sys.argv
     rank, world, local = _dist()

@@ -110,6 +110,7 @@ SIGNATURES = [
     ("dg_batch_max_dt", C.c_int, [C.c_void_p, C.c_double, C.c_double, _f64p]),
     ("dg_batch_residuals", C.c_int, [C.c_void_p, _f64p, C.POINTER(C.c_int)]),
     ("dg_batch_run_steps", C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, _f64p]),
+    ("dg_autotune", C.c_int, [C.c_void_p, C.c_int]),
     ("h3d_mesh_read_specmesh", C.c_int, [C.c_char_p, C.c_int, C.c_int, _i32p, C.c_char_p, C.POINTER(C.c_void_p)]),
     ("h3d_mesh_box", C.c_int, [C.c_int, C.c_int, C.c_int, _f64p, _f64p, C.c_double, C.c_int, C.c_int, C.c_int,
                                _i32p, C.POINTER(C.c_void_p)]),

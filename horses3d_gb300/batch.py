@@ -97,3 +97,7 @@ class CaseBatch:
 
     def synchronize(self):
         _abi.check(_abi.lib().dg_synchronize(self._h), "dg_synchronize")
+
+    def autotune(self, reps: int = 5) -> None:
+        """Elements per CTA of every order triple, timed on this batch and cached for the process."""
+        _abi.check(_abi.lib().dg_autotune(self._h, int(reps)), "dg_autotune")

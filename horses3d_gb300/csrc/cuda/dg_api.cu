@@ -464,7 +464,12 @@ int dg_rk3_step(dg_ctx* c, double t, double dt) {
     if (!(dt > 0.0) || !std::isfinite(dt)) return h3d::fail(DG_ERR_INVALID, "dt must be positive and finite");
     int rc = set_scalars(c, t, dt);
     if (rc) return rc;
-    CK(enqueue_step(c));
+    dg::failed_launch()[0] = 0;
+    {
+        const cudaError_t e = enqueue_step(c);
+        if (e != cudaSuccess)
+            return h3d::fail(DG_ERR_CUDA, std::string("enqueue_step: ") + cudaGetErrorString(e) + " " + dg::failed_launch());
+    }
     CK(cudaStreamSynchronize(c->stream));
     return DG_OK;
 }
@@ -677,6 +682,12 @@ int dg_batch_residuals(dg_ctx* c, double* maxres, int* nan_found) {
     if (!c || !maxres) return h3d::fail(DG_ERR_INVALID, "null argument");
     if (!c->var) return dg_residuals(c, maxres, nan_found);
     return h3dvar::residuals(c, maxres, nan_found);
+}
+
+int dg_autotune(dg_ctx* c, int reps) {
+    if (!c) return h3d::fail(DG_ERR_INVALID, "null context");
+    if (!c->var) return DG_OK;  // the uniform-order kernels have one fixed shape per order
+    return h3dvar::autotune(c, reps);
 }
 
 int dg_batch_run_steps(dg_ctx* c, int n, double cfl, double dcfl, double* ms) {

@@ -71,6 +71,7 @@ struct VStore {
     dg::VArgs<R> args;
     dg::VStageFn<R> stage = nullptr;
     dg::VTimesFn<R> times = nullptr;
+    dg::VTuneFn<R> tune = nullptr;
     void free() {
         for (DevBuf<R>* b : {&ja_xi, &ja_eta, &ja_zeta, &jac, &inv_jac, &fn, &ft1, &ft2, &fj, &tset, &QDot, &Ux, &Uy,
                              &Uz, &QF, &GF, &UJ, &FS})
@@ -116,6 +117,9 @@ struct dg_ctx {
     h3dctx::VStore<double> v64;
     h3dctx::VStore<float> v32;
     int n_items = 0;
+    int cls[dg::kItemClasses + 1] = {};  // item class ranges (see dg::VArgs::cls)
+    int ccap[dg::kItemClasses] = {};     // largest item per class
+    std::vector<int> h_eord, h_ecase;    // per element: packed orders, case (to rebuild the items)
 };
 
 // Variable-order / multi-case path (dg_var_api.cu).
@@ -129,4 +133,5 @@ cudaError_t enqueue_max_dt(dg_ctx* c, double cfl, double dcfl);
 cudaError_t enqueue_advance_time(dg_ctx* c);
 int residuals(dg_ctx* c, double* maxres, int* nan_case);  // maxres [5*n_cases], nan_case [n_cases]
 int kernel_times(dg_ctx* c, int reps, double* ms);
+int autotune(dg_ctx* c, int reps);
 }  // namespace h3dvar

@@ -28,6 +28,7 @@
 // [soff[slot]*NV + v*n_slot + p], n_slot the side's point count at the element's own orders.
 #pragma once
 #include <cstdint>
+#include <cstdio>
 
 #include "dg_launch.cuh"
 
@@ -47,10 +48,18 @@ struct CaseConst {
     double e_ref, gm1, gM2, mu, kappa;
 };
 
+// Item classes: 0 holds the items of anisotropic order triples (runtime loop bounds), class P
+// (2..kMaxP) the items of the isotropic triple (P,P,P), whose kernels have P as a compile-time
+// constant. The items of a class are contiguous.
+constexpr int kItemClasses = kMaxP + 1;
+
 template <typename R>
 struct VArgs {
     int n_items, n_faces, cap;  // cap: largest node count of an item
     int ns, source;
+    int item0;                     // first item of the launch (the grid covers one class)
+    int cls[kItemClasses + 1];     // class c holds items [cls[c], cls[c+1])
+    int ccap[kItemClasses];        // largest node count of an item of class c (its shared memory)
     const int4* items;          // x: first index into item_elems, y: count, z: px|py<<8|pz<<16, w: case
     const int* item_elems;
     const int* eord;            // px|py<<8|pz<<16 per element
@@ -90,13 +99,15 @@ struct ItemDims {
     int first, count, px, py, pz, kase, np, ntot;
 };
 
+// PC > 0: the item belongs to the isotropic class P = PC and its orders are compile-time constants.
+template <int PC = 0>
 __device__ __forceinline__ ItemDims item_dims(const int4 it) {
     ItemDims d;
     d.first = it.x;
     d.count = it.y;
-    d.px = it.z & 255;
-    d.py = (it.z >> 8) & 255;
-    d.pz = (it.z >> 16) & 255;
+    d.px = PC ? PC : (it.z & 255);
+    d.py = PC ? PC : ((it.z >> 8) & 255);
+    d.pz = PC ? PC : ((it.z >> 16) & 255);
     d.kase = it.w;
     d.np = d.px * d.py * d.pz;
     d.ntot = d.count * d.np;
@@ -149,7 +160,7 @@ __device__ __forceinline__ void load_ops(const OpsP<R>* ops, OpsP<R>* s, int px,
 }
 
 // NV traces of the item's nodes held in s (value v of item node m at s[v*ntot + m]) into the slots.
-template <typename R, int NV>
+template <typename R, int NV, int PC>
 __device__ __forceinline__ void write_traces(const VArgs<R>& a, const ItemDims& d, const OpsP<R>* sO, const R* s,
                                              R* dst) {
     const int A = d.px * d.pz, B = d.px * d.py, C = d.py * d.pz, Te = 2 * (A + B + C);
@@ -167,6 +178,7 @@ __device__ __forceinline__ void write_traces(const VArgs<R>& a, const ItemDims& 
         R acc[NV];
 #pragma unroll
         for (int c = 0; c < NV; ++c) acc[c] = R(0);
+        #pragma unroll
         for (int l = 0; l < L; ++l) {
             const R w = v[l];
             const int m = vline_node(side, ca, cb, l, d.px, d.py);
@@ -183,10 +195,10 @@ __device__ __forceinline__ void write_traces(const VArgs<R>& a, const ItemDims& 
 // ------------------------------------------------------------------------------------------------
 // kv_traces: Q traces of the current state (after an upload).
 // ------------------------------------------------------------------------------------------------
-template <typename R>
+template <typename R, int PC>
 __global__ void __launch_bounds__(256) kv_traces(VArgs<R> a) {
     extern __shared__ __align__(16) unsigned char vsm[];
-    const ItemDims d = item_dims(a.items[blockIdx.x]);
+    const ItemDims d = item_dims<PC>(a.items[a.item0 + blockIdx.x]);
     OpsP<R>* sO = reinterpret_cast<OpsP<R>*>(vsm);
     R* sQ = reinterpret_cast<R*>(sO + 3);
     load_ops(a.ops, sO, d.px, d.py, d.pz);
@@ -199,16 +211,16 @@ __global__ void __launch_bounds__(256) kv_traces(VArgs<R> a) {
         sQ[4 * d.ntot + t] = R(a.Q[5 * g + 4] - eref);
     }
     __syncthreads();
-    write_traces<R, 5>(a, d, sO, sQ, a.QF);
+    write_traces<R, 5, PC>(a, d, sO, sQ, a.QF);
 }
 
 // ------------------------------------------------------------------------------------------------
 // kv_volume: gradient + lifting + gradient traces (Navier-Stokes), fluxes, weak volume integral.
 // ------------------------------------------------------------------------------------------------
-template <typename R>
+template <typename R, int PC>
 __global__ void __launch_bounds__(256) kv_volume(VArgs<R> a, int store_grad) {
     extern __shared__ __align__(16) unsigned char vsm[];
-    const ItemDims d = item_dims(a.items[blockIdx.x]);
+    const ItemDims d = item_dims<PC>(a.items[a.item0 + blockIdx.x]);
     const int px = d.px, py = d.py, pz = d.pz, np = d.np, ntot = d.ntot;
     OpsP<R>* sO = reinterpret_cast<OpsP<R>*>(vsm);  // xi, eta, zeta operators
     R* sQ = reinterpret_cast<R*>(sO + 3);            // 5*ntot: state
@@ -233,16 +245,19 @@ __global__ void __launch_bounds__(256) kv_volume(VArgs<R> a, int store_grad) {
             const long long g = a.eoff[e] + n;
             const R* q0 = sQ + le * np;
             R uxi[5] = {0, 0, 0, 0, 0}, ueta[5] = {0, 0, 0, 0, 0}, uzeta[5] = {0, 0, 0, 0, 0};
+            #pragma unroll
             for (int l = 0; l < px; ++l) {
                 const R w = sO[0].D[i * kMaxP + l];
 #pragma unroll
                 for (int v = 0; v < 5; ++v) uxi[v] = uxi[v] + q0[v * ntot + l + px * (j + py * k)] * w;
             }
+            #pragma unroll
             for (int l = 0; l < py; ++l) {
                 const R w = sO[1].D[j * kMaxP + l];
 #pragma unroll
                 for (int v = 0; v < 5; ++v) ueta[v] = ueta[v] + q0[v * ntot + i + px * (l + py * k)] * w;
             }
+            #pragma unroll
             for (int l = 0; l < pz; ++l) {
                 const R w = sO[2].D[k * kMaxP + l];
 #pragma unroll
@@ -300,7 +315,7 @@ __global__ void __launch_bounds__(256) kv_volume(VArgs<R> a, int store_grad) {
             }
         }
         __syncthreads();
-        write_traces<R, 15>(a, d, sO, sG, a.GF);
+        write_traces<R, 15, PC>(a, d, sO, sG, a.GF);
         __syncthreads();
     }
     // contravariant fluxes F = Finv - Fvisc at each node, over the node's own gradient column
@@ -346,16 +361,19 @@ __global__ void __launch_bounds__(256) kv_volume(VArgs<R> a, int store_grad) {
         const long long g = a.eoff[a.item_elems[d.first + le]] + n;
         const R* F0 = sG + le * np;
         R acc[5] = {0, 0, 0, 0, 0};
+        #pragma unroll
         for (int l = 0; l < px; ++l) {
             const R h = sO[0].hatD[i * kMaxP + l];
 #pragma unroll
             for (int v = 0; v < 5; ++v) acc[v] = acc[v] + h * F0[v * ntot + l + px * (j + py * k)];
         }
+        #pragma unroll
         for (int l = 0; l < py; ++l) {
             const R h = sO[1].hatD[j * kMaxP + l];
 #pragma unroll
             for (int v = 0; v < 5; ++v) acc[v] = acc[v] + h * F0[(5 + v) * ntot + i + px * (l + py * k)];
         }
+        #pragma unroll
         for (int l = 0; l < pz; ++l) {
             const R h = sO[2].hatD[k * kMaxP + l];
 #pragma unroll
@@ -621,10 +639,10 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS) kv_face(VArgs<R> a)
 // ------------------------------------------------------------------------------------------------
 // kv_update: surface integral, 1/J, source, RK3 stage update (per-case dt), traces of the new Q.
 // ------------------------------------------------------------------------------------------------
-template <typename R, bool SRC>
+template <typename R, int PC, bool SRC>
 __global__ void __launch_bounds__(256) kv_update(VArgs<R> a, int stage, double tshift, int write_qdot) {
     extern __shared__ __align__(16) unsigned char vsm[];
-    const ItemDims d = item_dims(a.items[blockIdx.x]);
+    const ItemDims d = item_dims<PC>(a.items[a.item0 + blockIdx.x]);
     const int px = d.px, py = d.py, np = d.np, ntot = d.ntot;
     OpsP<R>* sO = reinterpret_cast<OpsP<R>*>(vsm);
     R* sQ = reinterpret_cast<R*>(sO + 3);
@@ -689,7 +707,7 @@ __global__ void __launch_bounds__(256) kv_update(VArgs<R> a, int stage, double t
     }
     if (stage < 0) return;
     __syncthreads();
-    write_traces<R, 5>(a, d, sO, sQ, a.QF);
+    write_traces<R, 5, PC>(a, d, sO, sQ, a.QF);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -839,15 +857,89 @@ cudaError_t launch_face(const VArgs<R>& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// Item kernels of one class: 0 traces, 1 volume, 2 update, 3 update with the manufactured source.
+// Description of the last item launch that failed (kernel, class, grid, shared memory), for the
+// error text of the entry point.
+inline char* failed_launch() {
+    static thread_local char buf[160] = "";
+    return buf;
+}
+
+template <typename R, int PC>
+cudaError_t launch_item_class(const VArgs<R>& a, int which, int n, size_t smem, cudaStream_t s, int store_grad,
+                              int stage, double tshift, int wq) {
+    switch (which) {
+        case 0: kv_traces<R, PC><<<n, 256, smem, s>>>(a); break;
+        case 1: kv_volume<R, PC><<<n, 256, smem, s>>>(a, store_grad); break;
+        // the update kernel is bound by its memory traffic; compile-time orders only lengthen it
+        case 2: kv_update<R, 0, false><<<n, 256, smem, s>>>(a, stage, tshift, wq); break;
+        default: kv_update<R, 0, true><<<n, 256, smem, s>>>(a, stage, tshift, wq); break;
+    }
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        cudaFuncAttributes fa{};
+        const void* fn = which == 0 ? reinterpret_cast<const void*>(kv_traces<R, PC>)
+                         : which == 1 ? reinterpret_cast<const void*>(kv_volume<R, PC>)
+                         : which == 2 ? reinterpret_cast<const void*>(kv_update<R, 0, false>)
+                                      : reinterpret_cast<const void*>(kv_update<R, 0, true>);
+        cudaFuncGetAttributes(&fa, fn);
+        snprintf(failed_launch(), 160, "item kernel %d class %d grid %d smem %zu (limit %d, static %zu, regs %d)", which,
+                 PC, n, smem, fa.maxDynamicSharedSizeBytes, fa.sharedSizeBytes, fa.numRegs);
+    }
+    return e;
+}
+
+// One launch per non-empty item class (anisotropic items with runtime orders, isotropic items with
+// compile-time P), each with the shared memory of its own largest item. which: 0 traces, 1 volume,
+// 2 update, 3 update with the manufactured source.
+template <typename R>
+cudaError_t launch_items(const VArgs<R>& a0, int which, cudaStream_t s, int store_grad = 0, int stage = 0,
+                         double tshift = 0.0, int wq = 0) {
+    for (int c = 0; c < kItemClasses; ++c) {
+        const int n = a0.cls[c + 1] - a0.cls[c];
+        if (n <= 0) continue;
+        VArgs<R> a = a0;
+        a.item0 = a0.cls[c];
+        const size_t smem = vitem_smem<R>(a0.ccap[c], which == 1 ? 20 : 5);
+        cudaError_t e;
+        switch (c) {
+            case 0: e = launch_item_class<R, 0>(a, which, n, smem, s, store_grad, stage, tshift, wq); break;
+            case 2: e = launch_item_class<R, 2>(a, which, n, smem, s, store_grad, stage, tshift, wq); break;
+            case 3: e = launch_item_class<R, 3>(a, which, n, smem, s, store_grad, stage, tshift, wq); break;
+            case 4: e = launch_item_class<R, 4>(a, which, n, smem, s, store_grad, stage, tshift, wq); break;
+            case 5: e = launch_item_class<R, 5>(a, which, n, smem, s, store_grad, stage, tshift, wq); break;
+            case 6: e = launch_item_class<R, 6>(a, which, n, smem, s, store_grad, stage, tshift, wq); break;
+            case 7: e = launch_item_class<R, 7>(a, which, n, smem, s, store_grad, stage, tshift, wq); break;
+            case 8: e = launch_item_class<R, 8>(a, which, n, smem, s, store_grad, stage, tshift, wq); break;
+            default: e = cudaErrorInvalidValue; break;  // no item has a single node per direction
+        }
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+template <typename R, int PC>
+cudaError_t set_item_attributes(size_t vol, size_t upd) {
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(kv_volume<R, PC>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(vol))) ||
+        (e = cudaFuncSetAttribute(kv_update<R, 0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(upd))) ||
+        (e = cudaFuncSetAttribute(kv_update<R, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(upd))) ||
+        (e = cudaFuncSetAttribute(kv_traces<R, PC>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(upd))))
+        return e;
+    return cudaSuccess;
+}
+
 template <typename R>
 cudaError_t vrun_stage(const VArgs<R>& a, int stage, double tshift, int flags, cudaStream_t s) {
     const size_t vol = vitem_smem<R>(a.cap, 20), upd = vitem_smem<R>(a.cap, 5);
     if (stage == kPrepare) {
         cudaError_t e;
-        if ((e = cudaFuncSetAttribute(kv_volume<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(vol))) ||
-            (e = cudaFuncSetAttribute(kv_update<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(upd))) ||
-            (e = cudaFuncSetAttribute(kv_update<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(upd))) ||
-            (e = cudaFuncSetAttribute(kv_traces<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(upd))) ||
+        if ((e = set_item_attributes<R, 0>(vol, upd)) || (e = set_item_attributes<R, 2>(vol, upd)) ||
+            (e = set_item_attributes<R, 3>(vol, upd)) || (e = set_item_attributes<R, 4>(vol, upd)) ||
+            (e = set_item_attributes<R, 5>(vol, upd)) || (e = set_item_attributes<R, 6>(vol, upd)) ||
+            (e = set_item_attributes<R, 7>(vol, upd)) || (e = set_item_attributes<R, 8>(vol, upd)) ||
             (e = cudaFuncSetAttribute(kv_face<R, kJump>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       static_cast<int>(FaceCfg<R, kJump>::SMEM))) ||
             (e = cudaFuncSetAttribute(kv_face<R, kFluxEuler>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -857,26 +949,19 @@ cudaError_t vrun_stage(const VArgs<R>& a, int stage, double tshift, int flags, c
             return e;
         return cudaSuccess;
     }
-    if (stage == kTraces) {
-        kv_traces<R><<<a.n_items, 256, upd, s>>>(a);
-        return cudaGetLastError();
-    }
+    if (stage == kTraces) return launch_items(a, 0, s);
     cudaError_t e;
     if (a.ns && (e = launch_face<R, kJump>(a, s)) != cudaSuccess) return e;
-    kv_volume<R><<<a.n_items, 256, vol, s>>>(a, flags & kStoreGrad);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = launch_items(a, 1, s, flags & kStoreGrad)) != cudaSuccess) return e;
     if ((e = a.ns ? launch_face<R, kFluxNS>(a, s) : launch_face<R, kFluxEuler>(a, s)) != cudaSuccess) return e;
     const int wq = (flags & kWriteQDot) ? 1 : 0;
-    if (a.source) kv_update<R, true><<<a.n_items, 256, upd, s>>>(a, stage, tshift, wq);
-    else kv_update<R, false><<<a.n_items, 256, upd, s>>>(a, stage, tshift, wq);
-    return cudaGetLastError();
+    return launch_items(a, a.source ? 3 : 2, s, 0, stage, tshift, wq);
 }
 
 // Average device time of each kernel alone: ms[0] volume, [1] face flux, [2] update (stage 1),
 // [3] traces, [4] BR1 jump faces.
 template <typename R>
 cudaError_t vkernel_times(const VArgs<R>& a, int reps, cudaStream_t s, double* ms) {
-    const size_t vol = vitem_smem<R>(a.cap, 20), upd = vitem_smem<R>(a.cap, 5);
     cudaEvent_t e0, e1;
     cudaError_t err = cudaEventCreate(&e0);
     if (err != cudaSuccess) return err;
@@ -892,10 +977,10 @@ cudaError_t vkernel_times(const VArgs<R>& a, int reps, cudaStream_t s, double* m
         cudaEventRecord(e0, s);
         for (int r = 0; r < reps; ++r) {
             switch (kk) {
-                case 0: kv_volume<R><<<a.n_items, 256, vol, s>>>(a, 0); break;
+                case 0: launch_items(a, 1, s, 0); break;
                 case 1: a.ns ? launch_face<R, kFluxNS>(a, s) : launch_face<R, kFluxEuler>(a, s); break;
-                case 2: kv_update<R, false><<<a.n_items, 256, upd, s>>>(a, 1, 1.0 / 3.0, 0); break;
-                case 3: kv_traces<R><<<a.n_items, 256, upd, s>>>(a); break;
+                case 2: launch_items(a, 2, s, 0, 1, 1.0 / 3.0, 0); break;
+                case 3: launch_items(a, 0, s); break;
                 default: launch_face<R, kJump>(a, s); break;
             }
         }
@@ -911,7 +996,39 @@ cudaError_t vkernel_times(const VArgs<R>& a, int reps, cudaStream_t s, double* m
     return cudaGetLastError();
 }
 
-// Resolved in the instantiation translation units.
+// Autotuner timing: reps launches of the volume and update (stage 1) kernels over the items of b;
+// *ms receives the elapsed device time.
+template <typename R>
+cudaError_t vtime_items(const VArgs<R>& b, int reps, cudaStream_t s, float* ms) {
+    cudaEvent_t e0, e1;
+    cudaError_t err = cudaEventCreate(&e0);
+    if (err != cudaSuccess) return err;
+    if ((err = cudaEventCreate(&e1)) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return err;
+    }
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < reps && err == cudaSuccess; ++r) {
+        err = launch_items(b, 1, s, 0);
+        if (err == cudaSuccess) err = launch_items(b, 2, s, 0, 1, 1.0 / 3.0, 0);
+    }
+    cudaEventRecord(e1, s);
+    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+    if (err == cudaSuccess) err = cudaEventElapsedTime(ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return err;
+}
+
+template <typename R>
+using VTuneFn = cudaError_t (*)(const VArgs<R>& b, int reps, cudaStream_t s, float* ms);
+
+// Resolved in the instantiation translation units. The item and face kernels are launched only
+// from there: a __global__ template instantiated in two translation units (without relocatable
+// device code) registers two device functions under one host stub, so an attribute set through one
+// would not reach the copy the other launches.
+VTuneFn<double> vtune_fn_fp64();
+VTuneFn<float> vtune_fn_fp32();
 VStageFn<double> vstage_fn_fp64();
 VStageFn<float> vstage_fn_fp32();
 VTimesFn<double> vtimes_fn_fp64();

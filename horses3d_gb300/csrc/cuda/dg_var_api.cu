@@ -5,8 +5,11 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -167,6 +170,9 @@ int setup_vstore(dg_ctx* c, h3dctx::VStore<R>& st, const Gathered& h) {
     std::memset(&a, 0, sizeof(a));
     a.n_items = c->n_items;
     a.n_faces = c->F;
+    a.item0 = 0;
+    for (int q = 0; q <= dg::kItemClasses; ++q) a.cls[q] = c->cls[q];
+    for (int q = 0; q < dg::kItemClasses; ++q) a.ccap[q] = c->ccap[q];
     a.ns = c->pc.ns;
     a.source = c->opt.source;
     a.items = c->items.p;
@@ -190,6 +196,132 @@ int setup_vstore(dg_ctx* c, h3dctx::VStore<R>& st, const Gathered& h) {
     a.Ux = st.Ux.p; a.Uy = st.Uy.p; a.Uz = st.Uz.p;
     a.QF = st.QF.p; a.GF = st.GF.p; a.UJ = st.UJ.p; a.FS = st.FS.p;
     return DG_OK;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Work items and their autotuned size
+// ------------------------------------------------------------------------------------------------
+// Elements per item for each order triple, chosen by dg_autotune and kept for the process (and, with
+// HORSES3D_GB300_TUNE_FILE set, in that file): key (px, py, pz, FP32?, NS?, node type) -> nodes per item.
+struct TuneKey {
+    int ord, mixed, ns, nodes;
+    bool operator<(const TuneKey& o) const {
+        return std::tie(ord, mixed, ns, nodes) < std::tie(o.ord, o.mixed, o.ns, o.nodes);
+    }
+};
+std::mutex g_tune_mutex;
+std::map<TuneKey, int> g_tune;
+bool g_tune_loaded = false;
+
+const char* tune_file() { return std::getenv("HORSES3D_GB300_TUNE_FILE"); }
+
+void load_tune_file_locked() {
+    if (g_tune_loaded) return;
+    g_tune_loaded = true;
+    const char* path = tune_file();
+    if (!path) return;
+    std::FILE* f = std::fopen(path, "r");
+    if (!f) return;
+    int px, py, pz, mx, ns, nd, cap;
+    while (std::fscanf(f, "%d %d %d %d %d %d %d", &px, &py, &pz, &mx, &ns, &nd, &cap) == 7)
+        if (px >= 2 && py >= 2 && pz >= 2 && px <= dg::kMaxP && py <= dg::kMaxP && pz <= dg::kMaxP && cap > 0)
+            g_tune[TuneKey{px | (py << 8) | (pz << 16), mx, ns, nd}] = cap;
+    std::fclose(f);
+}
+
+void save_tune_file_locked() {
+    const char* path = tune_file();
+    if (!path) return;
+    std::FILE* f = std::fopen(path, "w");
+    if (!f) return;
+    for (const auto& kv : g_tune)
+        std::fprintf(f, "%d %d %d %d %d %d %d\n", kv.first.ord & 255, (kv.first.ord >> 8) & 255, (kv.first.ord >> 16) & 255,
+                     kv.first.mixed, kv.first.ns, kv.first.nodes, kv.second);
+    std::fclose(f);
+}
+
+int tuned_item_nodes(int ord, bool mixed, bool ns, int nodes) {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    load_tune_file_locked();
+    auto it = g_tune.find(TuneKey{ord, mixed ? 1 : 0, ns ? 1 : 0, nodes});
+    return it == g_tune.end() ? kItemNodes : it->second;
+}
+
+struct ItemTable {
+    std::vector<int4> items;
+    std::vector<int> elems;
+    int cls[dg::kItemClasses + 1];
+    int ccap[dg::kItemClasses] = {};  // largest item (nodes) per class
+    int cap = 0;                      // largest item overall
+};
+
+// Elements bucketed by (item class, case, order triple), heaviest buckets first within a class;
+// class 0 = anisotropic triples, class P = the isotropic triple (P,P,P). An item holds up to
+// item_nodes nodes of one bucket (at least one element). only_cls >= 0 keeps that item class alone
+// (autotuning); item_nodes_override > 0 replaces the tuned size.
+int isotropic_class(int ord) {
+    const int px = ord & 255, py = (ord >> 8) & 255, pz = (ord >> 16) & 255;
+    return (px == py && py == pz) ? px : 0;
+}
+
+// An isotropic order gets its own class (its own launch with compile-time P) only when it has enough
+// nodes to fill the GPU twice over (152 SMs x 2 CTAs x 256 nodes); smaller ones join class 0, whose
+// launch would otherwise be followed by a nearly empty one.
+constexpr int64_t kClassMinNodes = 152LL * 2 * 256;
+
+std::vector<int> class_of_orders(const std::vector<int>& eord) {
+    std::map<int, int64_t> nodes_of;  // isotropic P -> nodes
+    for (int o : eord) {
+        const int p = isotropic_class(o);
+        if (p) nodes_of[p] += static_cast<int64_t>(p) * p * p;
+    }
+    std::vector<int> cls_of_p(dg::kItemClasses, 0);
+    for (const auto& kv : nodes_of)
+        if (kv.second >= kClassMinNodes) cls_of_p[kv.first] = kv.first;
+    return cls_of_p;
+}
+
+int item_class(int ord, const std::vector<int>& cls_of_p) { return cls_of_p[isotropic_class(ord)]; }
+
+ItemTable build_items(const std::vector<int>& eord, const std::vector<int>& ecase, int only_cls, bool mixed, bool ns,
+                      int nodes, int item_nodes_override = 0) {
+    std::map<std::tuple<int, int, int, int>, std::vector<int>> buckets;  // (class, -np, case, ord) -> elements
+    const std::vector<int> cls_of_p = class_of_orders(eord);
+    for (size_t e = 0; e < eord.size(); ++e) {
+        const int o = eord[e];
+        const int cls = item_class(o, cls_of_p);
+        if (only_cls >= 0 && cls != only_cls) continue;
+        const int px = o & 255, py = (o >> 8) & 255, pz = (o >> 16) & 255;
+        buckets[std::make_tuple(cls, -px * py * pz, ecase[e], o)].push_back(static_cast<int>(e));
+    }
+    ItemTable t;
+    int start[dg::kItemClasses + 1];
+    for (int q = 0; q <= dg::kItemClasses; ++q) start[q] = -1;
+    for (const auto& b : buckets) {
+        const int cls = std::get<0>(b.first);
+        if (start[cls] < 0) start[cls] = static_cast<int>(t.items.size());
+        const int np = -std::get<1>(b.first);
+        const int ord = std::get<3>(b.first);
+        const int nodes_per_item = item_nodes_override > 0 ? item_nodes_override : tuned_item_nodes(ord, mixed, ns, nodes);
+        const int per = std::max(1, nodes_per_item / np);
+        const std::vector<int>& els = b.second;
+        for (size_t i0 = 0; i0 < els.size(); i0 += per) {
+            const int cnt = static_cast<int>(std::min<size_t>(per, els.size() - i0));
+            int4 it;
+            it.x = static_cast<int>(t.elems.size());
+            it.y = cnt;
+            it.z = ord;
+            it.w = std::get<2>(b.first);
+            t.items.push_back(it);
+            for (int q = 0; q < cnt; ++q) t.elems.push_back(els[i0 + q]);
+            t.cap = std::max(t.cap, cnt * np);
+            t.ccap[cls] = std::max(t.ccap[cls], cnt * np);
+        }
+    }
+    // class ranges: an empty class starts where the next non-empty one does
+    t.cls[dg::kItemClasses] = static_cast<int>(t.items.size());
+    for (int q = dg::kItemClasses - 1; q >= 0; --q) t.cls[q] = start[q] >= 0 ? start[q] : t.cls[q + 1];
+    return t;
 }
 
 }  // namespace
@@ -311,33 +443,15 @@ int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, cons
     c->ndof = nodes;
     h.slot_points = spts;
 
-    // work items: elements bucketed by (case, order triple), heaviest buckets first
-    std::map<std::tuple<int, int, int>, std::vector<int>> buckets;  // (-np, case, ord) -> elements
-    for (int e = 0; e < c->K; ++e) {
-        const int o = eord[e];
-        const int np = (o & 255) * ((o >> 8) & 255) * ((o >> 16) & 255);
-        buckets[std::make_tuple(-np, ecase[e], o)].push_back(e);
-    }
-    std::vector<int4> items;
-    std::vector<int> item_elems;
-    int cap = 0;
-    for (const auto& b : buckets) {
-        const int np = -std::get<0>(b.first);
-        const int per = std::max(1, kItemNodes / np);
-        const std::vector<int>& els = b.second;
-        for (size_t i0 = 0; i0 < els.size(); i0 += per) {
-            const int cnt = static_cast<int>(std::min<size_t>(per, els.size() - i0));
-            int4 it;
-            it.x = static_cast<int>(item_elems.size());
-            it.y = cnt;
-            it.z = std::get<2>(b.first);
-            it.w = std::get<1>(b.first);
-            items.push_back(it);
-            for (int q = 0; q < cnt; ++q) item_elems.push_back(els[i0 + q]);
-            cap = std::max(cap, cnt * np);
-        }
-    }
+    c->h_eord = eord;
+    c->h_ecase = ecase;
+    ItemTable tab = build_items(c->h_eord, c->h_ecase, -1, c->mixed, c->pc.ns != 0, c->nodes);
+    const std::vector<int4>& items = tab.items;
+    const std::vector<int>& item_elems = tab.elems;
+    const int cap = tab.cap;
     c->n_items = static_cast<int>(items.size());
+    for (int q = 0; q <= dg::kItemClasses; ++q) c->cls[q] = tab.cls[q];
+    for (int q = 0; q < dg::kItemClasses; ++q) c->ccap[q] = tab.ccap[q];
 
     cudaError_t e;
     if ((e = cudaGetDevice(&c->device)) != cudaSuccess) return bail(cuda_fail(e, "cudaGetDevice"));
@@ -388,11 +502,13 @@ int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, cons
         c->v32.args.cap = cap;
         c->v32.stage = dg::vstage_fn_fp32();
         c->v32.times = dg::vtimes_fn_fp32();
+        c->v32.tune = dg::vtune_fn_fp32();
     } else {
         if ((rc = setup_vstore(c, c->v64, h))) return bail(rc);
         c->v64.args.cap = cap;
         c->v64.stage = dg::vstage_fn_fp64();
         c->v64.times = dg::vtimes_fn_fp64();
+        c->v64.tune = dg::vtune_fn_fp64();
     }
     if ((e = stage(c, dg::kPrepare, 0.0, 0)) != cudaSuccess) return bail(cuda_fail(e, "kernel attributes"));
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return bail(cuda_fail(e, "set-up"));
@@ -511,6 +627,129 @@ int kernel_times(dg_ctx* c, int reps, double* ms) {
     if (c->mixed) CK(c->v32.times(c->v32.args, reps, c->stream, ms));
     else CK(c->v64.times(c->v64.args, reps, c->stream, ms));
     return DG_OK;
+}
+
+namespace {
+
+// Installs an item table in the context: device copies, launch arguments, kernel attributes for
+// its largest item; drops the captured graph (its launches used the old table).
+template <typename R>
+int apply_items(dg_ctx* c, h3dctx::VStore<R>& st, const ItemTable& t) {
+    c->items.free();
+    c->item_elems.free();
+    CK(c->items.upload(t.items.data(), t.items.size(), c->stream));
+    CK(c->item_elems.upload(t.elems.data(), t.elems.size(), c->stream));
+    c->n_items = static_cast<int>(t.items.size());
+    for (int q = 0; q <= dg::kItemClasses; ++q) c->cls[q] = t.cls[q];
+    for (int q = 0; q < dg::kItemClasses; ++q) c->ccap[q] = t.ccap[q];
+    dg::VArgs<R>& a = st.args;
+    a.items = c->items.p;
+    a.item_elems = c->item_elems.p;
+    a.n_items = c->n_items;
+    a.cap = t.cap;
+    for (int q = 0; q <= dg::kItemClasses; ++q) a.cls[q] = t.cls[q];
+    for (int q = 0; q < dg::kItemClasses; ++q) a.ccap[q] = t.ccap[q];
+    CK(st.stage(a, dg::kPrepare, 0.0, 0, c->stream));
+    if (c->graph) {
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+    }
+    return DG_OK;
+}
+
+// For every item class of the context (the anisotropic triples together; each isotropic order on its
+// own) times the volume and update kernels over that class with each candidate item size; the class
+// is one launch in a stage, so its time alone is the time it takes in the step. The fastest size is
+// recorded for every order triple of the class.
+template <typename R>
+int autotune_store(dg_ctx* c, h3dctx::VStore<R>& st, int reps) {
+    cudaStream_t s = c->stream;
+    const size_t n5 = 5 * static_cast<size_t>(c->ndof);
+    h3dctx::DevBuf<double> q0, g0;
+    h3dctx::DevBuf<R> d0;
+    int rc = DG_OK;
+    CK(q0.alloc(n5));
+    CK(g0.alloc(n5));
+    CK(d0.alloc(n5));
+    CK(cudaMemcpyAsync(q0.p, c->Q.p, sizeof(double) * n5, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(g0.p, c->G.p, sizeof(double) * n5, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(d0.p, st.QDot.p, sizeof(R) * n5, cudaMemcpyDeviceToDevice, s));
+    {
+        dg::VArgs<R> big = st.args;
+        big.cap = 2 * kItemNodes;  // kernel attributes for the largest candidate
+        CK(st.stage(big, dg::kPrepare, 0.0, 0, s));
+    }
+    const int candidates[] = {kItemNodes / 4, kItemNodes / 2, kItemNodes, 2 * kItemNodes};
+    std::map<int, std::vector<int>> class_ords;  // class -> its order triples
+    const std::vector<int> cls_of_p = class_of_orders(c->h_eord);
+    for (int o : c->h_eord) {
+        std::vector<int>& v = class_ords[item_class(o, cls_of_p)];
+        if (std::find(v.begin(), v.end(), o) == v.end()) v.push_back(o);
+    }
+    h3dctx::DevBuf<int4> titems;
+    h3dctx::DevBuf<int> telems;
+    std::map<TuneKey, int> chosen;
+    for (const auto& co : class_ords) {
+        const int cls = co.first;
+        double best_ms = 1e300;
+        int best = kItemNodes;
+        std::vector<int> seen_caps;
+        for (int cand : candidates) {
+            const ItemTable t = build_items(c->h_eord, c->h_ecase, cls, c->mixed, c->pc.ns != 0, c->nodes, cand);
+            if (std::find(seen_caps.begin(), seen_caps.end(), static_cast<int>(t.items.size())) != seen_caps.end())
+                continue;  // same grouping as a smaller candidate
+            seen_caps.push_back(static_cast<int>(t.items.size()));
+            titems.free();
+            telems.free();
+            CK(titems.upload(t.items.data(), t.items.size(), s));
+            CK(telems.upload(t.elems.data(), t.elems.size(), s));
+            dg::VArgs<R> b = st.args;
+            b.items = titems.p;
+            b.item_elems = telems.p;
+            b.n_items = static_cast<int>(t.items.size());
+            b.cap = t.cap;
+            for (int q = 0; q <= dg::kItemClasses; ++q) b.cls[q] = t.cls[q];
+            for (int q = 0; q < dg::kItemClasses; ++q) b.ccap[q] = t.ccap[q];
+            double ms_min = 1e300;
+            for (int trial = 0; trial < 3; ++trial) {
+                float ms = 0.f;
+                CK(st.tune(b, reps, s, &ms));
+                ms_min = std::min(ms_min, static_cast<double>(ms));
+            }
+            if (ms_min < best_ms) {
+                best_ms = ms_min;
+                best = cand;
+            }
+        }
+        for (int o : co.second) chosen[TuneKey{o, c->mixed ? 1 : 0, c->pc.ns ? 1 : 0, c->nodes}] = best;
+    }
+    titems.free();
+    telems.free();
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        load_tune_file_locked();
+        for (const auto& kv : chosen) g_tune[kv.first] = kv.second;
+        save_tune_file_locked();
+    }
+    CK(cudaMemcpyAsync(c->Q.p, q0.p, sizeof(double) * n5, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(c->G.p, g0.p, sizeof(double) * n5, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(st.QDot.p, d0.p, sizeof(R) * n5, cudaMemcpyDeviceToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    q0.free();
+    g0.free();
+    d0.free();
+    const ItemTable t = build_items(c->h_eord, c->h_ecase, -1, c->mixed, c->pc.ns != 0, c->nodes);
+    if ((rc = apply_items(c, st, t))) return rc;
+    CK(stage(c, dg::kTraces, 0.0, 0));  // Q traces of the restored state
+    CK(cudaStreamSynchronize(s));
+    return DG_OK;
+}
+
+}  // namespace
+
+int autotune(dg_ctx* c, int reps) {
+    if (reps < 1) return h3d::fail(DG_ERR_INVALID, "reps must be positive");
+    return c->mixed ? autotune_store(c, c->v32, reps) : autotune_store(c, c->v64, reps);
 }
 
 }  // namespace h3dvar

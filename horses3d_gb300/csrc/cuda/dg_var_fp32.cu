@@ -6,5 +6,6 @@ namespace dg {
 
 VStageFn<float> vstage_fn_fp32() { return vrun_stage<float>; }
 VTimesFn<float> vtimes_fn_fp32() { return vkernel_times<float>; }
+VTuneFn<float> vtune_fn_fp32() { return vtime_items<float>; }
 
 }  // namespace dg

@@ -104,6 +104,10 @@ class NavierStokesDG:
     def synchronize(self):
         _abi.check(_abi.lib().dg_synchronize(self._h), "dg_synchronize")
 
+    def autotune(self, reps: int = 5) -> None:
+        """Per-order-triple item sizes of the variable-order kernels (a no-op for uniform orders)."""
+        _abi.check(_abi.lib().dg_autotune(self._h, int(reps)), "dg_autotune")
+
     def integrate_in_time(self, t0: float = 0.0, n_steps: int | None = None, t_final: float | None = None,
                           cfl: float | None = None, dcfl: float | None = None, dt: float | None = None,
                           compute_after_steps: bool = False) -> StepReport:

@@ -183,6 +183,13 @@ int dg_batch_get_clock(dg_ctx* ctx, double* t, double* dt);
 int dg_batch_max_dt(dg_ctx* ctx, double cfl, double dcfl, double* dt);
 /* Per-case residuals maxres[5*n_cases] and NaN flags nan_found[n_cases] (may be NULL). */
 int dg_batch_residuals(dg_ctx* ctx, double* maxres, int* nan_found);
+/* Autotuner of the variable-order / batch kernels: for every order triple of the context, times the
+ * volume and update kernels with several elements-per-CTA sizes (reps launches each, best of three)
+ * and keeps the fastest per DOF. The choice is cached per (order triple, precision, equations, node
+ * type) for the process, so later contexts with those triples start tuned; with the environment
+ * variable HORSES3D_GB300_TUNE_FILE set, the table is read from and written to that file. The
+ * state (Q, G, QDot) is restored afterwards. A no-op (DG_OK) on uniform-order contexts. */
+int dg_autotune(dg_ctx* ctx, int reps);
 /* n RK3 steps of every case from its device clock (CUDA-graph replay). cfl > 0: every step takes
  * each case's MaxTimeStep(cfl, dcfl); otherwise each case's current dt. ms (may be NULL) receives
  * the device time measured with events on the context's stream. */

@@ -223,3 +223,21 @@ def test_anisotropic_rotated_elements(tmp_path):
     assert np.any(np.isin(rot, [1, 3, 4, 6]))
     _check_rhs(mesh, cfg, q0)
     _check_steps(mesh, cfg, q0, steps=3, dt=2e-3)
+
+
+def test_autotune_keeps_results_and_persists(tmp_path, monkeypatch):
+    """Item sizes change how elements are grouped into CTAs, never the arithmetic of a node: results
+    after autotuning equal those before, bit for bit, and the state is restored by the tuner."""
+    monkeypatch.setenv("HORSES3D_GB300_TUNE_FILE", str(tmp_path / "tune.txt"))
+    mesh, cfg, q0 = cases.aniso_tgv_case(n=3, lo=1, hi=5, seed=21)
+    g1 = NavierStokesDG(mesh, cfg)
+    g1.set_state(q0)
+    g1.run_steps(2, 0.0, dt=1e-3)
+    g2 = NavierStokesDG(mesh, cfg)
+    g2.set_state(q0)
+    g2.autotune(reps=2)
+    assert np.array_equal(g2.Q, q0)
+    g2.run_steps(2, 0.0, dt=1e-3)
+    assert np.array_equal(g1.Q, g2.Q)
+    rows = {tuple(int(v) for v in ln.split()[:3]) for ln in (tmp_path / "tune.txt").read_text().splitlines() if ln.strip()}
+    assert {tuple(int(v) + 1 for v in o) for o in mesh.order} <= rows
