@@ -120,6 +120,14 @@ struct dg_ctx {
     int cls[dg::kItemClasses + 1] = {};  // item class ranges (see dg::VArgs::cls)
     int ccap[dg::kItemClasses] = {};     // largest item per class
     std::vector<int> h_eord, h_ecase;    // per element: packed orders, case (to rebuild the items)
+    // face lists: staged (Tset) faces and per-point faces grouped by point counts (see dg::VArgs)
+    std::vector<int> h_nc, h_direct;
+    h3dctx::DevBuf<int> nc_faces, direct_faces;
+    int n_groups = 0;
+    int gf0[dg::kMaxP * dg::kMaxP + 1] = {};
+    int gp0[dg::kMaxP * dg::kMaxP + 1] = {};
+    unsigned char gq1[dg::kMaxP * dg::kMaxP] = {};
+    unsigned char gq2[dg::kMaxP * dg::kMaxP] = {};
 };
 
 // Variable-order / multi-case path (dg_var_api.cu).

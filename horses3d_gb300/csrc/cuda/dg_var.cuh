@@ -60,6 +60,18 @@ struct VArgs {
     int item0;                     // first item of the launch (the grid covers one class)
     int cls[kItemClasses + 1];     // class c holds items [cls[c], cls[c+1])
     int ccap[kItemClasses];        // largest node count of an item of class c (its shared memory)
+    // faces whose two sides need a Tset interpolation (kv_face, one 64-thread group per face)
+    int n_nc;
+    const int* nc_faces;
+    // faces whose sides already have the face's point counts (kv_face_direct, one thread per point),
+    // grouped by point counts (q1, q2): group g holds face-list entries [gf0[g], gf0[g+1]) and
+    // points [gp0[g], gp0[g+1])
+    int n_groups;
+    const int* direct_faces;
+    int gf0[kMaxP * kMaxP + 1];
+    int gp0[kMaxP * kMaxP + 1];
+    unsigned char gq1[kMaxP * kMaxP];
+    unsigned char gq2[kMaxP * kMaxP];
     const int4* items;          // x: first index into item_elems, y: count, z: px|py<<8|pz<<16, w: case
     const int* item_elems;
     const int* eord;            // px|py<<8|pz<<16 per element
@@ -457,8 +469,9 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS) kv_face(VArgs<R> a)
     R* AL = SL + NVB * NP;
     R* SR = AL + NVB * NP;
     R* AR = SR + NVB * NP;
-    const int f = blockIdx.x * Cfg::FPB + grp;
-    const bool active = f < a.n_faces;
+    const int fi = blockIdx.x * Cfg::FPB + grp;
+    const bool active = fi < a.n_nc;
+    const int f = active ? a.nc_faces[fi] : 0;
     int eL = 0, eR = 0, rot = 0, q1 = 1, q2 = 1, kase = 0;
     int l1 = 1, l2 = 1, r1 = 1, r2 = 1, s1R = 1, s2R = 1;
     long long offL = 0, offR = 0, fo = 0;
@@ -633,6 +646,97 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS) kv_face(VArgs<R> a)
                 dstR[v * nR + o] = sign2 * val;
             }
         }
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// kv_face_direct: the same face quantities for faces whose sides already have the face's point
+// counts (the Tset interpolation is the identity there, FaceClass.f90:281-382 projection type 0):
+// one thread per face point reads both sides' traces in place, the right side re-indexed by
+// leftIndexes2Right, and writes both sides' results.
+// ------------------------------------------------------------------------------------------------
+template <typename R, int MODE>
+__global__ void __launch_bounds__(128) kv_face_direct(VArgs<R> a) {
+    using Cfg = FaceCfg<R, MODE>;
+    constexpr int NVOUT = Cfg::NVOUT;
+    const int gp = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gp >= a.gp0[a.n_groups]) return;
+    int g = 0;
+    while (gp >= a.gp0[g + 1]) ++g;
+    const int q1 = a.gq1[g], q2 = a.gq2[g], np = q1 * q2;
+    const int local = gp - a.gp0[g];
+    const int f = a.direct_faces[a.gf0[g] + local / np];
+    const int p = local % np;
+    const int i = p % q1, j = p / q1;
+    const int4 fd = a.faces[f];
+    const int eL = fd.x, eR = fd.y, sL = fd.z & 15, sR = (fd.z >> 4) & 15, rot = (fd.z >> 8) & 15;
+    int r1, r2;
+    side_dims(sR, a.eord[eR], r1, r2);
+    int ii, jj;
+    left2right(i, j, q1 - 1, q2 - 1, rot, ii, jj);
+    const int pr = ii + r1 * jj;
+    const long long offL = a.soff[6LL * eL + sL - 1], offR = a.soff[6LL * eR + sR - 1];
+    const long long gpt = a.foff[f] + p;
+    const R n[3] = {a.fn[3 * gpt], a.fn[3 * gpt + 1], a.fn[3 * gpt + 2]};
+    const R J = a.fj[gpt];
+    R QL[5], QR[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+        QL[v] = a.QF[offL * 5 + v * np + p];
+        QR[v] = a.QF[offR * 5 + v * np + pr];
+    }
+    R out[NVOUT];
+    if (MODE == kJump) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+            const R u = R(0.5) * (QR[v] - QL[v]) * J;
+            out[v] = u * n[0];
+            out[5 + v] = u * n[1];
+            out[10 + v] = u * n[2];
+        }
+        R* dL = a.UJ + offL * 15 + p;
+        R* dR = a.UJ + offR * 15 + pr;
+#pragma unroll
+        for (int c = 0; c < 15; ++c) {
+            dL[c * np] = out[c];
+            dR[c * np] = out[c];
+        }
+        return;
+    }
+    const PhysR<R> ph = a.ph[fd.w];
+    R inv[5];
+    if (ph.riemann == 0) {
+        roe_flux(ph, QL, QR, n, inv);
+    } else {
+        const R t1[3] = {a.ft1[3 * gpt], a.ft1[3 * gpt + 1], a.ft1[3 * gpt + 2]};
+        const R t2[3] = {a.ft2[3 * gpt], a.ft2[3 * gpt + 1], a.ft2[3 * gpt + 2]};
+        lxf_flux(ph, QL, QR, n, t1, t2, inv);
+    }
+    R visc[5] = {0, 0, 0, 0, 0};
+    if (MODE == kFluxNS) {
+        R gl[15], gr[15];
+#pragma unroll
+        for (int c = 0; c < 15; ++c) {
+            gl[c] = a.GF[offL * 15 + c * np + p];
+            gr[c] = a.GF[offR * 15 + c * np + pr];
+        }
+        R mu, kap, FL[3][5], FR[3][5];
+        mu_kappa(ph, QL, mu, kap);
+        viscous_flux(ph, QL, gl, gl + 5, gl + 10, mu, kap, FL);
+        mu_kappa(ph, QR, mu, kap);
+        viscous_flux(ph, QR, gr, gr + 5, gr + 10, mu, kap, FR);
+#pragma unroll
+        for (int v = 0; v < 5; ++v)
+            visc[v] = R(0.5) * (FL[0][v] + FR[0][v]) * n[0] + R(0.5) * (FL[1][v] + FR[1][v]) * n[1] +
+                      R(0.5) * (FL[2][v] + FR[2][v]) * n[2];
+    }
+    R* dL = a.FS + offL * 5 + p;
+    R* dR = a.FS + offR * 5 + pr;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+        const R fl = (inv[v] - visc[v]) * J;
+        dL[v * np] = fl;
+        dR[v * np] = -fl;
     }
 }
 
@@ -852,9 +956,18 @@ using VTimesFn = cudaError_t (*)(const VArgs<R>& a, int reps, cudaStream_t s, do
 template <typename R, int MODE>
 cudaError_t launch_face(const VArgs<R>& a, cudaStream_t s) {
     using Cfg = FaceCfg<R, MODE>;
-    const int blocks = (a.n_faces + Cfg::FPB - 1) / Cfg::FPB;
-    kv_face<R, MODE><<<blocks, Cfg::THREADS, Cfg::SMEM, s>>>(a);
-    return cudaGetLastError();
+    if (a.n_nc > 0) {
+        const int blocks = (a.n_nc + Cfg::FPB - 1) / Cfg::FPB;
+        kv_face<R, MODE><<<blocks, Cfg::THREADS, Cfg::SMEM, s>>>(a);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    const int npts = a.gp0[a.n_groups];
+    if (npts > 0) {
+        kv_face_direct<R, MODE><<<(npts + 127) / 128, 128, 0, s>>>(a);
+        return cudaGetLastError();
+    }
+    return cudaSuccess;
 }
 
 // Item kernels of one class: 0 traces, 1 volume, 2 update, 3 update with the manufactured source.

@@ -171,6 +171,18 @@ int setup_vstore(dg_ctx* c, h3dctx::VStore<R>& st, const Gathered& h) {
     a.n_items = c->n_items;
     a.n_faces = c->F;
     a.item0 = 0;
+    a.n_nc = static_cast<int>(c->h_nc.size());
+    a.nc_faces = c->nc_faces.p;
+    a.n_groups = c->n_groups;
+    a.direct_faces = c->direct_faces.p;
+    for (int g = 0; g <= c->n_groups; ++g) {
+        a.gf0[g] = c->gf0[g];
+        a.gp0[g] = c->gp0[g];
+    }
+    for (int g = 0; g < c->n_groups; ++g) {
+        a.gq1[g] = c->gq1[g];
+        a.gq2[g] = c->gq2[g];
+    }
     for (int q = 0; q <= dg::kItemClasses; ++q) a.cls[q] = c->cls[q];
     for (int q = 0; q < dg::kItemClasses; ++q) a.ccap[q] = c->ccap[q];
     a.ns = c->pc.ns;
@@ -443,6 +455,40 @@ int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, cons
     c->ndof = nodes;
     h.slot_points = spts;
 
+    // faces whose sides already carry the face's point counts need no Tset interpolation and go to
+    // the one-thread-per-point kernel, grouped by point counts; the others keep the staged kernel
+    {
+        std::map<std::pair<int, int>, std::vector<int>> groups;
+        std::vector<int> nc;
+        for (int f = 0; f < c->F; ++f) {
+            const int4& fd = faces[f];
+            const int q1 = (fd.z >> 12) & 15, q2 = (fd.z >> 16) & 15;
+            const int oL = eord[fd.x], oR = eord[fd.y];
+            const int32_t ordL[3] = {(oL & 255) - 1, ((oL >> 8) & 255) - 1, ((oL >> 16) & 255) - 1};
+            const int32_t ordR[3] = {(oR & 255) - 1, ((oR >> 8) & 255) - 1, ((oR >> 16) & 255) - 1};
+            int l1, l2, r1, r2;
+            side_orders(fd.z & 15, ordL, l1, l2);
+            side_orders((fd.z >> 4) & 15, ordR, r1, r2);
+            const int rot = (fd.z >> 8) & 15;
+            if (!(rot == 0 || rot == 2 || rot == 5 || rot == 7)) std::swap(r1, r2);
+            if (l1 + 1 == q1 && l2 + 1 == q2 && r1 + 1 == q1 && r2 + 1 == q2) groups[{q1, q2}].push_back(f);
+            else nc.push_back(f);
+        }
+        c->h_nc = nc;
+        c->h_direct.clear();
+        c->n_groups = 0;
+        c->gf0[0] = 0;
+        c->gp0[0] = 0;
+        for (const auto& kv : groups) {
+            const int g = c->n_groups++;
+            c->gq1[g] = static_cast<unsigned char>(kv.first.first);
+            c->gq2[g] = static_cast<unsigned char>(kv.first.second);
+            c->h_direct.insert(c->h_direct.end(), kv.second.begin(), kv.second.end());
+            c->gf0[g + 1] = static_cast<int>(c->h_direct.size());
+            c->gp0[g + 1] = c->gp0[g] + static_cast<int>(kv.second.size()) * kv.first.first * kv.first.second;
+        }
+    }
+
     c->h_eord = eord;
     c->h_ecase = ecase;
     ItemTable tab = build_items(c->h_eord, c->h_ecase, -1, c->mixed, c->pc.ns != 0, c->nodes);
@@ -484,6 +530,8 @@ int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, cons
         (e = c->eord.upload(eord.data(), eord.size(), s)) || (e = c->eoff.upload(eoff.data(), eoff.size(), s)) ||
         (e = c->soff.upload(soff.data(), soff.size(), s)) || (e = c->faces4.upload(faces.data(), faces.size(), s)) ||
         (e = c->foff.upload(foff.data(), foff.size(), s)) ||
+        (e = c->nc_faces.upload(c->h_nc.data(), c->h_nc.size(), s)) ||
+        (e = c->direct_faces.upload(c->h_direct.data(), c->h_direct.size(), s)) ||
         (e = c->cc.upload(c->case_const.data(), c->case_const.size(), s)))
         return bail(cuda_fail(e, "upload tables"));
     {
@@ -520,7 +568,7 @@ void release(dg_ctx* c) {
     c->v64.free();
     c->v32.free();
     for (auto* b : {&c->items, &c->faces4}) b->free();
-    for (auto* b : {&c->item_elems, &c->eord, &c->vnan}) b->free();
+    for (auto* b : {&c->item_elems, &c->eord, &c->vnan, &c->nc_faces, &c->direct_faces}) b->free();
     for (auto* b : {&c->eoff, &c->soff, &c->foff}) b->free();
     c->cc.free();
     c->dxi_table.free();
