@@ -141,6 +141,7 @@ int setup_store(dg_ctx* c, Store<R>& st, const dg_mesh_desc* m) {
     a.src_gM2 = c->pc.gammaM2;
     a.src_mu = c->pc.mu;
     a.src_kappa = c->pc.kappa;
+    a.err = c->err_flag.p;
     return DG_OK;
 }
 
@@ -191,6 +192,16 @@ cudaError_t enqueue_max_dt(dg_ctx* c, double cfl, double dcfl) {
 }
 
 // Every case's step start time and dt (one case unless the context is a batch).
+// Reads and clears the device flag a kernel sets when a bounded wait gave up (after a synchronise).
+int check_device_error(dg_ctx* c) {
+    if (!c->err_flag.p) return DG_OK;
+    int flag = 0;
+    CK(cudaMemcpy(&flag, c->err_flag.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (!flag) return DG_OK;
+    CK(cudaMemset(c->err_flag.p, 0, sizeof(int)));
+    return h3d::fail(DG_ERR_TIMEOUT, "a kernel's bounded wait for a bulk copy gave up; the step is incomplete");
+}
+
 int set_scalars(dg_ctx* c, double t, double dt) {
     const int n = c->n_cases;
     for (int k = 0; k < n; ++k) {
@@ -311,6 +322,8 @@ int dg_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op,
     if ((e = c->scal.alloc(4)) != cudaSuccess) return bail(cuda_fail(e, "alloc scalars"));
     if ((e = c->red.alloc(8)) != cudaSuccess) return bail(cuda_fail(e, "alloc reductions"));
     if ((e = c->nan_flag.alloc(1)) != cudaSuccess) return bail(cuda_fail(e, "alloc flag"));
+    if ((e = c->err_flag.alloc(1)) != cudaSuccess || (e = cudaMemset(c->err_flag.p, 0, sizeof(int))) != cudaSuccess)
+        return bail(cuda_fail(e, "alloc error flag"));
     if ((e = c->x.alloc(3 * nd)) != cudaSuccess) return bail(cuda_fail(e, "alloc x"));
     if ((e = cudaMemcpyAsync(c->x.p, m->x, sizeof(double) * 3 * nd, cudaMemcpyHostToDevice, c->stream)) != cudaSuccess)
         return bail(cuda_fail(e, "copy x"));
@@ -375,7 +388,7 @@ void dg_destroy(dg_ctx* c) {
     if (c->var) h3dvar::release(c);
     c->s64.free();
     c->s32.free();
-    c->Q.free(); c->G.free(); c->x.free(); c->scal.free(); c->red.free(); c->nan_flag.free();
+    c->Q.free(); c->G.free(); c->x.free(); c->scal.free(); c->red.free(); c->nan_flag.free(); c->err_flag.free();
     c->face_elem.free(); c->face_side.free(); c->face_rot.free(); c->nb_slot.free(); c->nb_map.free();
     if (c->h_scal) cudaFreeHost(c->h_scal);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -456,7 +469,7 @@ int dg_rhs(dg_ctx* c, double t) {
     if (rc) return rc;
     CK(run_stage(c, -1, 0.0, dg::kStoreGrad | dg::kWriteQDot));
     CK(cudaStreamSynchronize(c->stream));
-    return DG_OK;
+    return check_device_error(c);
 }
 
 int dg_rk3_step(dg_ctx* c, double t, double dt) {
@@ -471,7 +484,7 @@ int dg_rk3_step(dg_ctx* c, double t, double dt) {
             return h3d::fail(DG_ERR_CUDA, std::string("enqueue_step: ") + cudaGetErrorString(e) + " " + dg::failed_launch());
     }
     CK(cudaStreamSynchronize(c->stream));
-    return DG_OK;
+    return check_device_error(c);
 }
 
 }  // extern "C"
@@ -532,6 +545,7 @@ int run_graph(dg_ctx* c, int n, int mode, double cfl, double dcfl, double* ms) {
         *ms = t;
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
+        return check_device_error(c);
     }
     return DG_OK;
 }
@@ -547,6 +561,7 @@ int steps_common(dg_ctx* c, int n, double t0, double dt, double cfl, double dcfl
         CK(cudaMemcpyAsync(c->h_scal, c->scal.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         *t_end = c->h_scal[0];
+        return check_device_error(c);
     }
     return DG_OK;
 }

@@ -96,6 +96,7 @@ struct dg_ctx {
     h3dctx::DevBuf<double> Q, G, x, scal;    // scal: time[n_cases], then dt[n_cases]
     h3dctx::DevBuf<unsigned long long> red;  // uniform: [0..1] dt, [2..6] residuals; variable: 8 per case
     h3dctx::DevBuf<int> face_elem, face_side, face_rot, nan_flag, nb_slot, nb_map;
+    h3dctx::DevBuf<int> err_flag;  // set by kernels whose bounded waits gave up
     h3dctx::Store<double> s64;
     h3dctx::Store<float> s32;
     double* h_scal = nullptr;  // pinned staging for the per-case scalars (4 * n_cases doubles)

@@ -26,6 +26,7 @@
 
 #include "dg_convert.cuh"
 #include "dg_physics.cuh"
+#include "dg_tma.cuh"
 
 namespace dg {
 
@@ -78,6 +79,7 @@ struct Args {
     const double* time;  // device scalars: step start time and dt
     const double* dt;
     double e_ref;        // energy reference of the mixed form (0 for the plain form)
+    int* err;            // set by a kernel whose bounded wait on a bulk copy gave up
     // manufactured-solution source constants
     double src_gm1, src_gM2, src_mu, src_kappa;
 };
@@ -625,6 +627,83 @@ __global__ void __launch_bounds__(128) k_flux(Args<R> a) {
     gst5(a.FS, a.nsp, iR, fr);
 }
 
+// Surface integral in the reference's order (left, right, front, back, bottom, top), division by J
+// and the manufactured source at time t_src: qd = (qd - sum b f*)/J + S.
+template <int P, bool GL, bool SRC, typename R>
+__device__ __forceinline__ void surface_integral(const Args<R>& a, int i, int j, int k, int64_t g,
+                                                 const bool use[6], const R fs[6][5], R J, double t_src, R qd[5]) {
+    if (GL) {
+        const R bl = a.ops.bL[0], br = a.ops.bR[P - 1];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+            R fi = R(0);
+            if (use[5]) fi = fs[5][v] * bl;
+            if (use[3]) fi = fi + fs[3][v] * br;
+            if (use[0]) fi = fi + fs[0][v] * bl;
+            if (use[1]) fi = fi + fs[1][v] * br;
+            if (use[2]) fi = fi + fs[2][v] * bl;
+            if (use[4]) fi = fi + fs[4][v] * br;
+            qd[v] = (qd[v] - fi) / J;
+        }
+    } else {
+        const R bxl = a.ops.bL[i], bxr = a.ops.bR[i], byl = a.ops.bL[j], byr = a.ops.bR[j];
+        const R bzl = a.ops.bL[k], bzr = a.ops.bR[k];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+            R fi = fs[5][v] * bxl;
+            fi = fi + fs[3][v] * bxr;
+            fi = fi + fs[0][v] * byl;
+            fi = fi + fs[1][v] * byr;
+            fi = fi + fs[2][v] * bzl;
+            fi = fi + fs[4][v] * bzr;
+            qd[v] = (qd[v] - fi) / J;
+        }
+    }
+    if (SRC) {
+        double S[5];
+        mms_source(a.x[3 * g], a.x[3 * g + 1], a.x[3 * g + 2], t_src, a.src_gm1, a.src_gM2, a.src_mu, a.src_kappa, S);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) qd[v] = R(double(qd[v]) + S[v]);
+    }
+}
+
+// Williamson low-storage RK3 stage in FP64 (ExplicitMethods.f90:748-779): G = a_k G + QDot,
+// Q = Q + c_k dt G.
+template <typename R>
+__device__ __forceinline__ void rk3_stage(int stage, double dt, const R qd[5], double gq[5], double qq[5]) {
+    const double ak = stage == 0 ? 0.0 : (stage == 1 ? -5.0 / 9.0 : -153.0 / 128.0);
+    const double ck = stage == 0 ? 1.0 / 3.0 : (stage == 1 ? 15.0 / 16.0 : 8.0 / 15.0);
+    const double cdt = ck * dt;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+        gq[v] = ak * gq[v] + widen(qd[v]);
+        qq[v] = qq[v] + cdt * gq[v];
+    }
+}
+
+// The six surface fluxes of node (i,j,k) of element e (Gauss-Lobatto: only the sides the node
+// touches); use[] marks the loaded ones.
+template <int P, bool GL, typename R>
+__device__ __forceinline__ void load_surface_fluxes(const Args<R>& a, int e, int i, int j, int k, bool use[6],
+                                                    R fs[6][5]) {
+    constexpr int P2 = P * P;
+    const int64_t s1 = slot(e, 1) * P2;  // the six slots of e are contiguous
+    const int pL = j + P * k, pF = i + P * k, pO = i + P * j;
+    const bool u[6] = {GL ? j == 0 : true, GL ? j == P - 1 : true, GL ? k == 0 : true,
+                       GL ? i == P - 1 : true, GL ? k == P - 1 : true, GL ? i == 0 : true};
+    const int pt[6] = {pF, pF, pO, pL, pO, pL};
+#pragma unroll
+    for (int sd = 0; sd < 6; ++sd) {
+        use[sd] = u[sd];
+        if (u[sd]) {
+            gld5(a.FS, a.nsp, s1 + sd * P2 + pt[sd], fs[sd]);
+        } else {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) fs[sd][v] = R(0);
+        }
+    }
+}
+
 // ------------------------------------------------------------------------------------------------
 // k_update: QDot = (QDot - surface integral)/J + S; stage >= 0 adds the low-storage update
 // G = a_k G + QDot, Q = Q + c_k dt G in FP64 and writes the Q traces of the new state.
@@ -642,26 +721,14 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
     const int i = n % P, j = (n / P) % P, k = n / P2;
     const int64_t g = static_cast<int64_t>(e) * P3 + n;
     if (active) {
-        const int64_t s1 = slot(e, 1) * P2;  // the six slots of e are contiguous
-        const int pL = j + P * k, pF = i + P * k, pO = i + P * j;
         // every load of the node up front (QDot, J, the six surface fluxes, G and Q), then the math
         R qd[5], fs[6][5];
+        bool use[6];
         double gq[5], qq[5];
 #pragma unroll
         for (int v = 0; v < 5; ++v) qd[v] = a.QDot[5 * g + v];
         const R J = a.jac[g];
-        const bool use[6] = {GL ? j == 0 : true, GL ? j == P - 1 : true, GL ? k == 0 : true,
-                             GL ? i == P - 1 : true, GL ? k == P - 1 : true, GL ? i == 0 : true};
-        const int pt[6] = {pF, pF, pO, pL, pO, pL};
-#pragma unroll
-        for (int sd = 0; sd < 6; ++sd) {
-            if (use[sd]) {
-                gld5(a.FS, a.nsp, s1 + sd * P2 + pt[sd], fs[sd]);
-            } else {
-#pragma unroll
-                for (int v = 0; v < 5; ++v) fs[sd][v] = R(0);
-            }
-        }
+        load_surface_fluxes<P, GL>(a, e, i, j, k, use, fs);
         if (stage >= 0) {
 #pragma unroll
             for (int v = 0; v < 5; ++v) {
@@ -669,55 +736,14 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
                 qq[v] = a.Q[5 * g + v];
             }
         }
-        // surface integral in the reference's order: left, right, front, back, bottom, top
-        if (GL) {
-            const R bl = a.ops.bL[0], br = a.ops.bR[P - 1];
-#pragma unroll
-            for (int v = 0; v < 5; ++v) {
-                R fi = R(0);
-                if (use[5]) fi = fs[5][v] * bl;
-                if (use[3]) fi = fi + fs[3][v] * br;
-                if (use[0]) fi = fi + fs[0][v] * bl;
-                if (use[1]) fi = fi + fs[1][v] * br;
-                if (use[2]) fi = fi + fs[2][v] * bl;
-                if (use[4]) fi = fi + fs[4][v] * br;
-                qd[v] = (qd[v] - fi) / J;
-            }
-        } else {
-            const R bxl = a.ops.bL[i], bxr = a.ops.bR[i], byl = a.ops.bL[j], byr = a.ops.bR[j];
-            const R bzl = a.ops.bL[k], bzr = a.ops.bR[k];
-#pragma unroll
-            for (int v = 0; v < 5; ++v) {
-                R fi = fs[5][v] * bxl;
-                fi = fi + fs[3][v] * bxr;
-                fi = fi + fs[0][v] * byl;
-                fi = fi + fs[1][v] * byr;
-                fi = fi + fs[2][v] * bzl;
-                fi = fi + fs[4][v] * bzr;
-                qd[v] = (qd[v] - fi) / J;
-            }
-        }
         const double dt = *a.dt;
-        if (SRC) {
-            double S[5];
-            const double t = *a.time + tshift * dt;
-            mms_source(a.x[3 * g], a.x[3 * g + 1], a.x[3 * g + 2], t, a.src_gm1, a.src_gM2, a.src_mu, a.src_kappa, S);
-#pragma unroll
-            for (int v = 0; v < 5; ++v) qd[v] = R(double(qd[v]) + S[v]);
-        }
+        surface_integral<P, GL, SRC>(a, i, j, k, g, use, fs, J, *a.time + tshift * dt, qd);
         if (write_qdot) {
 #pragma unroll
             for (int v = 0; v < 5; ++v) a.QDot[5 * g + v] = qd[v];
         }
         if (stage >= 0) {
-            const double ak = stage == 0 ? 0.0 : (stage == 1 ? -5.0 / 9.0 : -153.0 / 128.0);
-            const double ck = stage == 0 ? 1.0 / 3.0 : (stage == 1 ? 15.0 / 16.0 : 8.0 / 15.0);
-            const double cdt = ck * dt;
-#pragma unroll
-            for (int v = 0; v < 5; ++v) {
-                gq[v] = ak * gq[v] + widen(qd[v]);
-                qq[v] = qq[v] + cdt * gq[v];
-            }
+            rk3_stage(stage, dt, qd, gq, qq);
 #pragma unroll
             for (int v = 0; v < 5; ++v) {
                 a.G[5 * g + v] = gq[v];
@@ -737,6 +763,96 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
         trace5<P, GL, 1>(a.ops, sQ4[le], sQ1[le], P3, side, p % P, p / P, tq);
         gst5(a.QF, a.nsp, slot(e, side) * P2 + p, tq[0]);
     }
+}
+
+// ------------------------------------------------------------------------------------------------
+// k_update_tma: k_update for one element per CTA whose Q, G (FP64), QDot and J blocks are 16-byte
+// aligned (P = 6): the four element blocks arrive in shared memory as TMA bulk copies on an
+// mbarrier while the threads fetch their surface fluxes; the updated Q and G leave as bulk stores.
+// A copy that does not complete within the bounded wait sets *a.err and the CTA returns.
+// ------------------------------------------------------------------------------------------------
+template <int P, bool GL, bool SRC, typename R>
+__global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
+    k_update_tma(Args<R> a, int stage, double tshift, int write_qdot) {
+    static_assert(Geo<P>::EPB == 1, "one element per CTA");
+    constexpr int P2 = Geo<P>::P2, P3 = Geo<P>::P3;
+    constexpr uint32_t BQ = 5 * P3 * sizeof(double), BD = 5 * P3 * sizeof(R), BJ = P3 * sizeof(R);
+    static_assert(BQ % 16 == 0 && BD % 16 == 0 && BJ % 16 == 0, "bulk copies move multiples of 16 bytes");
+    __shared__ __align__(128) double sQd[5 * P3];
+    __shared__ __align__(128) double sGd[5 * P3];
+    __shared__ __align__(128) R sDot[5 * P3];
+    __shared__ __align__(128) R sJ[P3];
+    __shared__ __align__(16) R sQ4[4 * P3];
+    __shared__ R sQ1[P3];
+    __shared__ __align__(8) uint64_t bar;
+    const int n = threadIdx.x;
+    const int e = blockIdx.x;
+    const int i = n % P, j = (n / P) % P, k = n / P2;
+    const int64_t g0 = static_cast<int64_t>(e) * P3, g = g0 + n;
+    if (n == 0) {
+        mbar_init(&bar, 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    if (n == 0) {
+        mbar_arrive_expect_tx(&bar, (stage >= 0 ? 2 * BQ : 0) + BD + BJ);
+        if (stage >= 0) {
+            bulk_load(sQd, a.Q + 5 * g0, BQ, &bar);
+            bulk_load(sGd, a.G + 5 * g0, BQ, &bar);
+        }
+        bulk_load(sDot, a.QDot + 5 * g0, BD, &bar);
+        bulk_load(sJ, a.jac + g0, BJ, &bar);
+    }
+    R fs[6][5];
+    bool use[6];
+    load_surface_fluxes<P, GL>(a, e, i, j, k, use, fs);
+    const bool arrived = mbar_wait(&bar, 0);
+    if (__syncthreads_or(!arrived)) {  // block-uniform: every thread leaves
+        if (n == 0) {
+            atomicOr(a.err, 1);
+            mbar_wait(&bar, 0);  // bounded: let a late copy land before the CTA's memory is reused
+        }
+        return;
+    }
+    R qd[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) qd[v] = sDot[5 * n + v];
+    const double dt = *a.dt;
+    surface_integral<P, GL, SRC>(a, i, j, k, g, use, fs, sJ[n], *a.time + tshift * dt, qd);
+    if (write_qdot) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) a.QDot[5 * g + v] = qd[v];
+    }
+    if (stage < 0) return;
+    double gq[5], qq[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+        gq[v] = sGd[5 * n + v];
+        qq[v] = sQd[5 * n + v];
+    }
+    rk3_stage(stage, dt, qd, gq, qq);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+        sGd[5 * n + v] = gq[v];
+        sQd[5 * n + v] = qq[v];
+    }
+    const R qn[5] = {from_f64<R>(qq[0]), from_f64<R>(qq[1]), from_f64<R>(qq[2]), from_f64<R>(qq[3]),
+                     from_f64<R>(qq[4] - a.e_ref)};
+    st5(sQ4, n, sQ1, n, qn);
+    fence_proxy_async_smem();  // this thread's Q, G writes before the bulk stores read them
+    __syncthreads();
+    if (n == 0) {
+        bulk_store(a.Q + 5 * g0, sQd, BQ);
+        bulk_store(a.G + 5 * g0, sGd, BQ);
+        bulk_commit();
+    }
+    for (int t = n; t < 6 * P2; t += P3) {  // Q traces of the updated state
+        const int side = 1 + t / P2, p = t - (side - 1) * P2;
+        R tq[1][5];
+        trace5<P, GL, 1>(a.ops, sQ4, sQ1, P3, side, p % P, p / P, tq);
+        gst5(a.QF, a.nsp, slot(e, side) * P2 + p, tq[0]);
+    }
+    if (n == 0) bulk_wait_all();
 }
 
 }  // namespace dg
