@@ -23,6 +23,7 @@ DG_ERR_TIMEOUT = -5
 DG_ERR_NOMEM = -6
 DG_ERR_NODEVICE = -7
 DG_ERR_IO = -8
+DG_FAULT_NONE, DG_FAULT_TMA_WAIT = 0, 1
 
 DG_NODES_GAUSS, DG_NODES_GAUSS_LOBATTO = 0, 1
 DG_INVISCID_STANDARD, DG_INVISCID_SPLIT = 0, 1
@@ -111,6 +112,7 @@ SIGNATURES = [
     ("dg_batch_residuals", C.c_int, [C.c_void_p, _f64p, C.POINTER(C.c_int)]),
     ("dg_batch_run_steps", C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, _f64p]),
     ("dg_autotune", C.c_int, [C.c_void_p, C.c_int]),
+    ("dg_inject_fault", C.c_int, [C.c_void_p, C.c_int]),
     ("h3d_mesh_read_specmesh", C.c_int, [C.c_char_p, C.c_int, C.c_int, _i32p, C.c_char_p, C.POINTER(C.c_void_p)]),
     ("h3d_mesh_box", C.c_int, [C.c_int, C.c_int, C.c_int, _f64p, _f64p, C.c_double, C.c_int, C.c_int, C.c_int,
                                _i32p, C.POINTER(C.c_void_p)]),

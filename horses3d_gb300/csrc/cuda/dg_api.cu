@@ -699,6 +699,20 @@ int dg_batch_residuals(dg_ctx* c, double* maxres, int* nan_found) {
     return h3dvar::residuals(c, maxres, nan_found);
 }
 
+int dg_inject_fault(dg_ctx* c, int kind) {
+    if (!c) return h3d::fail(DG_ERR_INVALID, "null context");
+    if (kind != DG_FAULT_NONE && kind != DG_FAULT_TMA_WAIT) return h3d::fail(DG_ERR_INVALID, "unknown fault kind");
+    if (c->var) return h3d::fail(DG_ERR_UNSUPPORTED, "the variable-order kernels have no bulk-copy waits");
+    const uint32_t extra = kind == DG_FAULT_TMA_WAIT ? 16u : 0u;
+    c->s32.args.extra_tx = extra;
+    c->s64.args.extra_tx = extra;
+    if (c->graph) {  // the captured launches carry the old arguments
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+    }
+    return DG_OK;
+}
+
 int dg_autotune(dg_ctx* c, int reps) {
     if (!c) return h3d::fail(DG_ERR_INVALID, "null context");
     if (!c->var) return DG_OK;  // the uniform-order kernels have one fixed shape per order

@@ -80,6 +80,7 @@ struct Args {
     const double* dt;
     double e_ref;        // energy reference of the mixed form (0 for the plain form)
     int* err;            // set by a kernel whose bounded wait on a bulk copy gave up
+    uint32_t extra_tx;   // bytes the update kernel's mbarrier expects beyond its copies (fault injection; 0)
     // manufactured-solution source constants
     double src_gm1, src_gM2, src_mu, src_kappa;
 };
@@ -795,7 +796,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
     }
     __syncthreads();
     if (n == 0) {
-        mbar_arrive_expect_tx(&bar, (stage >= 0 ? 2 * BQ : 0) + BD + BJ);
+        mbar_arrive_expect_tx(&bar, (stage >= 0 ? 2 * BQ : 0) + BD + BJ + a.extra_tx);
         if (stage >= 0) {
             bulk_load(sQd, a.Q + 5 * g0, BQ, &bar);
             bulk_load(sGd, a.G + 5 * g0, BQ, &bar);
@@ -810,7 +811,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
     if (__syncthreads_or(!arrived)) {  // block-uniform: every thread leaves
         if (n == 0) {
             atomicOr(a.err, 1);
-            mbar_wait(&bar, 0);  // bounded: let a late copy land before the CTA's memory is reused
+            mbar_wait(&bar, 0, kWaitNs / 4);  // bounded: let a late copy land before the CTA's memory is reused
         }
         return;
     }

@@ -2,15 +2,22 @@
 // sm_90 and later (sm_103a here). The copies need 16-byte aligned addresses and sizes that are
 // multiples of 16 bytes; callers check that before choosing a TMA kernel.
 //
-// Every wait on an mbarrier is bounded: after kWaitPolls polls the caller sees a failure, records it
-// in a device error flag and leaves the kernel, so no kernel can spin forever on a copy that does not
-// complete.
+// Every wait on an mbarrier is bounded in time: after kWaitNs nanoseconds of the global timer the
+// caller sees a failure, records it in a device error flag and leaves the kernel, so no kernel can
+// spin forever on a copy that does not complete. The bound is far above any copy's latency and
+// leaves room for the time slices of other contexts sharing the GPU.
 #pragma once
 #include <cstdint>
 
 namespace dg {
 
-constexpr int kWaitPolls = 1 << 22;
+constexpr unsigned long long kWaitNs = 2000000000ull;
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -41,10 +48,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Bounded wait for the phase with the given parity; false if it did not complete.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (int i = 0; i < kWaitPolls; ++i)
-        if (mbar_try_wait(bar, parity)) return true;
+// Bounded wait for the phase with the given parity; false if it did not complete within limit_ns
+// (and, independently of the timer, within 2^24 rounds of 256 polls).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned long long limit_ns = kWaitNs) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long start = global_ns();
+    for (int round = 0; round < (1 << 24); ++round) {
+        for (int i = 0; i < 256; ++i)
+            if (mbar_try_wait(bar, parity)) return true;
+        if (global_ns() - start > limit_ns) return false;
+    }
     return false;
 }
 

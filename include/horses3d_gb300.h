@@ -190,6 +190,14 @@ int dg_batch_residuals(dg_ctx* ctx, double* maxres, int* nan_found);
  * variable HORSES3D_GB300_TUNE_FILE set, the table is read from and written to that file. The
  * state (Q, G, QDot) is restored afterwards. A no-op (DG_OK) on uniform-order contexts. */
 int dg_autotune(dg_ctx* ctx, int reps);
+/* Failure-path test hook. DG_FAULT_TMA_WAIT makes the update kernels of the bulk-copy (TMA) path
+ * (uniform order N=5) expect 16 bytes that no copy delivers, so their bounded mbarrier waits run
+ * out (after about two seconds): every CTA records the failure and leaves, and the entry point
+ * returns DG_ERR_TIMEOUT; the state is then invalid and must be uploaded again. DG_FAULT_NONE
+ * restores normal operation. No copy is left in flight by the injected fault. DG_ERR_UNSUPPORTED on
+ * contexts without such waits. */
+enum { DG_FAULT_NONE = 0, DG_FAULT_TMA_WAIT = 1 };
+int dg_inject_fault(dg_ctx* ctx, int kind);
 /* n RK3 steps of every case from its device clock (CUDA-graph replay). cfl > 0: every step takes
  * each case's MaxTimeStep(cfl, dcfl); otherwise each case's current dt. ms (may be NULL) receives
  * the device time measured with events on the context's stream. */
