@@ -59,12 +59,14 @@ def _barrier(world):
 
 
 def _allreduce_max(x, world):
+    """Maximum of x over the ranks (NCCL reduces device tensors, gloo host tensors)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], dtype=torch.float64)
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -440,6 +442,10 @@ def main():
     if world > 1:
         import torch.distributed as dist
 
+        if args.impl == "gb300":
+            import torch
+
+            torch.cuda.set_device(local)  # one GPU per rank, before NCCL picks one
         dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
     threads = os.cpu_count() or 1
     metric = "DOF*RK-stage updates/s"
@@ -474,10 +480,6 @@ def main():
         if rank == 0:
             run_secondary(args.workload, args)
         return
-    if world > 1:
-        import torch
-
-        torch.cuda.set_device(local)
     case = build_case(args.elements)
     if args.profile:
         from horses3d_gb300.control import Config
