@@ -66,8 +66,11 @@ class Config:
         return ",".join(f"{a}:{b}" for a, b in self.periodic)
 
 
-_RIEMANN = {"roe": _abi.DG_RIEMANN_ROE, "lax-friedrichs": _abi.DG_RIEMANN_LXF}
-_AVERAGING = {"standard": _abi.DG_AVG_STANDARD, "pirozzoli": _abi.DG_AVG_PIROZZOLI}
+# RiemannSolvers_NS.f90:5-40 keyword values
+_RIEMANN = {"roe": _abi.DG_RIEMANN_ROE, "lax-friedrichs": _abi.DG_RIEMANN_LXF, "central": _abi.DG_RIEMANN_CENTRAL,
+            "rusanov": _abi.DG_RIEMANN_RUSANOV}
+_AVERAGING = {"standard": _abi.DG_AVG_STANDARD, "pirozzoli": _abi.DG_AVG_PIROZZOLI, "ducros": _abi.DG_AVG_DUCROS,
+              "morinishi": _abi.DG_AVG_MORINISHI, "kennedy-gruber": _abi.DG_AVG_KENNEDY_GRUBER}
 
 
 def _value(v: str) -> str:

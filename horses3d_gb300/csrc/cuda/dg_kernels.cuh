@@ -607,6 +607,8 @@ __global__ void __launch_bounds__(128) k_flux(Args<R> a) {
     R inv[5];
     if (a.ph.riemann == 0) {
         roe_flux(a.ph, QL, QR, n, inv);
+    } else if (a.ph.riemann == 3) {
+        rusanov_flux(a.ph, QL, QR, n, inv);
     } else {
         const R t1[3] = {a.ft1[gid], a.ft1[nfp + gid], a.ft1[2 * nfp + gid]};
         const R t2[3] = {a.ft2[gid], a.ft2[nfp + gid], a.ft2[2 * nfp + gid]};

@@ -167,7 +167,68 @@ __device__ __forceinline__ void roe_flux(const PhysR<R>& p, const R* QL, const R
     }
 }
 
-// RiemannSolvers_NS.f90:1251-1334 LxFRiemannSolver with StandardAverage (:1784) or PirozzoliAverage (:1927).
+// Averaged states of the face-normal frame (L, R = rho, rho u_n, rho u_t1, rho u_t2, E with the mixed
+// form's E'): StandardAverage (RiemannSolvers_NS.f90:1784-1819), DucrosAverage (:1821-1848),
+// MorinishiAverage (:1850-1886), KennedyGruberAverage (:1888-1925), PirozzoliAverage (:1927-1962).
+// Absolute energies and pressures are E' + e_ref, p' + p_ref; momentum fluxes carry p' only.
+template <typename R>
+__device__ __forceinline__ void averaged_states(const PhysR<R>& p, const R* L, const R* Rt, R pL, R pR, R iL, R iR,
+                                                R* f) {
+    const R uL = iL * L[1], uR = iR * Rt[1], vL = iL * L[2], vR = iR * Rt[2], wL = iL * L[3], wR = iR * Rt[3];
+    switch (p.averaging) {
+        case 0: {  // standard
+            f[0] = R(0.5) * (L[1] + Rt[1]);
+            f[1] = R(0.5) * (L[1] * uL + Rt[1] * uR + pL + pR);
+            f[2] = R(0.5) * (L[1] * vL + Rt[1] * vR);
+            f[3] = R(0.5) * (L[1] * wL + Rt[1] * wR);
+            f[4] = R(0.5) * (uL * (L[4] + pL + p.h_ref) + uR * (Rt[4] + pR + p.h_ref));
+            break;
+        }
+        case 2: {  // Ducros
+            const R su = uL + uR;
+            f[0] = R(0.25) * (L[0] + Rt[0]) * su;
+            f[1] = R(0.25) * (L[1] + Rt[1]) * su + R(0.5) * (pL + pR);
+            f[2] = R(0.25) * (L[2] + Rt[2]) * su;
+            f[3] = R(0.25) * (L[3] + Rt[3]) * su;
+            f[4] = R(0.25) * (L[4] + pL + Rt[4] + pR + R(2) * p.h_ref) * su;
+            break;
+        }
+        case 3: {  // Morinishi: the enthalpy without kinetic energy, cp p
+            const R hL = p.g_over_gm1 * (pL + p.p_ref), hR = p.g_over_gm1 * (pR + p.p_ref);
+            const R m = L[1] + Rt[1];
+            f[0] = R(0.5) * m;
+            f[1] = R(0.25) * m * (uL + uR) + R(0.5) * (pL + pR);
+            f[2] = R(0.25) * m * (vL + vR);
+            f[3] = R(0.25) * m * (wL + wR);
+            f[4] = R(0.5) * (uL * hL + uR * hR) + R(0.25) * (L[1] * uL + Rt[1] * uR) * (uL + uR) +
+                   R(0.25) * (L[1] * vL + Rt[1] * vR) * (vL + vR) + R(0.25) * (L[1] * wL + Rt[1] * wR) * (wL + wR) -
+                   R(0.25) * (L[1] * uL * uL + Rt[1] * uR * uR) - R(0.25) * (L[1] * vL * vL + Rt[1] * vR * vR) -
+                   R(0.25) * (L[1] * wL * wL + Rt[1] * wR * wR);
+            break;
+        }
+        case 4: {  // Kennedy-Gruber
+            const R rho = R(0.5) * (L[0] + Rt[0]), u = R(0.5) * (uL + uR), v = R(0.5) * (vL + vR);
+            const R w = R(0.5) * (wL + wR), pp = R(0.5) * (pL + pR);
+            const R e = R(0.5) * ((L[4] + p.e_ref) * iL + (Rt[4] + p.e_ref) * iR);
+            f[0] = rho * u;
+            f[1] = rho * u * u + pp;
+            f[2] = rho * u * v;
+            f[3] = rho * u * w;
+            f[4] = rho * u * e + (pp + p.p_ref) * u;
+            break;
+        }
+        default: {  // Pirozzoli
+            const R rho = R(0.5) * (L[0] + Rt[0]), u = R(0.5) * (uL + uR), v = R(0.5) * (vL + vR);
+            const R w = R(0.5) * (wL + wR), pp = R(0.5) * (pL + pR);
+            const R h = R(0.5) * ((L[4] + pL + p.h_ref) * iL + (Rt[4] + pR + p.h_ref) * iR);
+            f[0] = rho * u; f[1] = rho * u * u + pp; f[2] = rho * u * v; f[3] = rho * u * w; f[4] = rho * u * h;
+            break;
+        }
+    }
+}
+
+// RiemannSolvers_NS.f90:1251-1334 LxFRiemannSolver (the averaging of the control file) and :375-428
+// CentralRiemannSolver, which is the same average with lambda_stab = 0 (SetRiemannSolver, :224).
 template <typename R>
 __device__ __forceinline__ void lxf_flux(const PhysR<R>& p, const R* QL, const R* QR, const R* n, const R* t1,
                                          const R* t2, R* flux) {
@@ -180,36 +241,69 @@ __device__ __forceinline__ void lxf_flux(const PhysR<R>& p, const R* QL, const R
     const R rwR = QR[1] * t2[0] + QR[2] * t2[1] + QR[3] * t2[2];
     const R pL = p.gm1 * (QL[4] - R(0.5) * ((ruL * ruL + rvL * rvL + rwL * rwL) * iL));
     const R pR = p.gm1 * (QR[4] - R(0.5) * ((ruR * ruR + rvR * rvR + rwR * rwR) * iR));
-    const R aL = dsqrt(p.gamma * (pL + p.p_ref) * iL), aR = dsqrt(p.gamma * (pR + p.p_ref) * iR);
-    const R lL = fabs(ruL * iL) + aL, lR = fabs(ruR * iR) + aR;
-    const R lambda = lL > lR ? lL : lR;
-    const R uL = iL * ruL, uR = iR * ruR, vL = iL * rvL, vR = iR * rvR, wL = iL * rwL, wR = iR * rwR;
+    const R Lr[5] = {QL[0], ruL, rvL, rwL, QL[4]};
+    const R Rr[5] = {QR[0], ruR, rvR, rwR, QR[4]};
     R f[5];
-    if (p.averaging == 0) {
-        f[0] = R(0.5) * (ruL + ruR);
-        f[1] = R(0.5) * (ruL * uL + ruR * uR + pL + pR);
-        f[2] = R(0.5) * (ruL * vL + ruR * vR);
-        f[3] = R(0.5) * (ruL * wL + ruR * wR);
-        f[4] = R(0.5) * (uL * (QL[4] + pL + p.h_ref) + uR * (QR[4] + pR + p.h_ref));
-    } else {
-        const R rho = R(0.5) * (QL[0] + QR[0]), u = R(0.5) * (uL + uR), v = R(0.5) * (vL + vR), w = R(0.5) * (wL + wR);
-        const R pp = R(0.5) * (pL + pR);
-        const R h = R(0.5) * ((QL[4] + pL + p.h_ref) * iL + (QR[4] + pR + p.h_ref) * iR);
-        f[0] = rho * u; f[1] = rho * u * u + pp; f[2] = rho * u * v; f[3] = rho * u * w; f[4] = rho * u * h;
+    averaged_states(p, Lr, Rr, pL, pR, iL, iR, f);
+    if (p.riemann != 2) {  // central fluxes carry no dissipation
+        const R aL = dsqrt(p.gamma * (pL + p.p_ref) * iL), aR = dsqrt(p.gamma * (pR + p.p_ref) * iR);
+        const R lL = fabs(ruL * iL) + aL, lR = fabs(ruR * iR) + aR;
+        const R lambda = lL > lR ? lL : lR;
+        const R ls = p.lambda_stab * (R(0.5) * lambda);
+        f[0] = f[0] - ls * (QR[0] - QL[0]);
+        f[1] = f[1] - ls * (ruR - ruL);
+        f[2] = f[2] - ls * (rvR - rvL);
+        f[3] = f[3] - ls * (rwR - rwL);
+        f[4] = f[4] - ls * (QR[4] - QL[4]);
     }
-    const R ls = p.lambda_stab * (R(0.5) * lambda);
-    f[0] = f[0] - ls * (QR[0] - QL[0]);
-    f[1] = f[1] - ls * (ruR - ruL);
-    f[2] = f[2] - ls * (rvR - rvL);
-    f[3] = f[3] - ls * (rwR - rwL);
-    f[4] = f[4] - ls * (QR[4] - QL[4]);
     flux[0] = f[0];
 #pragma unroll
     for (int c = 0; c < 3; ++c) flux[1 + c] = n[c] * f[1] + t1[c] * f[2] + t2[c] * f[3];
     flux[4] = f[4];
 }
 
-// RiemannSolvers_NS.f90:2085-2145 StandardDG_TwoPointFlux and :2369-2437 Pirozzoli_TwoPointFlux.
+// RiemannSolvers_NS.f90:1661-1762 RusanovRiemannSolver: the mean of the two normal fluxes minus
+// max(|q| + a) times the jump, over two.
+template <typename R>
+__device__ __forceinline__ void rusanov_flux(const PhysR<R>& p, const R* QL, const R* QR, const R* n, R* flux) {
+    const R gm1 = p.gamma - R(1);
+    const R rho = QL[0], rhon = QR[0];
+    const R ul = QL[1] / rho, vl = QL[2] / rho, wl = QL[3] / rho;
+    const R pleft = gm1 * (QL[4] - R(0.5) / rho * (QL[1] * QL[1] + QL[2] * QL[2] + QL[3] * QL[3]));
+    const R ur = QR[1] / rhon, vr = QR[2] / rhon, wr = QR[3] / rhon;
+    const R pright = gm1 * (QR[4] - R(0.5) / rhon * (QR[1] * QR[1] + QR[2] * QR[2] + QR[3] * QR[3]));
+    const R ql = n[0] * ul + n[1] * vl + n[2] * wl;
+    const R qr = n[0] * ur + n[1] * vr + n[2] * wr;
+    const R kl = R(0.5) * (ul * ul + vl * vl + wl * wl), kr = R(0.5) * (ur * ur + vr * vr + wr * wr);
+    const R hl = kl + p.g_over_gm1 * (pleft + p.p_ref) / rho;
+    const R hr = kr + p.g_over_gm1 * (pright + p.p_ref) / rhon;
+    const R ar = dsqrt(gm1 * (hr - kr)), al = dsqrt(gm1 * (hl - kl));
+    const R rql = rho * ql, rqr = rhon * qr;
+    R f[5];
+    f[0] = rql + rqr;
+    f[1] = rql * ul + pleft * n[0] + rqr * ur + pright * n[0];
+    f[2] = rql * vl + pleft * n[1] + rqr * vr + pright * n[1];
+    f[3] = rql * wl + pleft * n[2] + rqr * wr + pright * n[2];
+    f[4] = rql * hl + rqr * hr;
+    const R sR = ar + fabs(qr), sL = al + fabs(ql);
+    const R smax = sR > sL ? sR : sL;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) flux[v] = (f[v] - smax * (QR[v] - QL[v])) / R(2);
+}
+
+// The interface flux of the chosen solver (Roe, LxF / central with the chosen average, Rusanov).
+template <typename R>
+__device__ __forceinline__ void riemann_flux(const PhysR<R>& p, const R* QL, const R* QR, const R* n, const R* t1,
+                                             const R* t2, R* flux) {
+    if (p.riemann == 0) roe_flux(p, QL, QR, n, flux);
+    else if (p.riemann == 3) rusanov_flux(p, QL, QR, n, flux);
+    else lxf_flux(p, QL, QR, n, t1, t2, flux);
+}
+
+// Two-point fluxes of the split form, contracted with the averaged metric vector:
+// StandardDG_TwoPointFlux (RiemannSolvers_NS.f90:2085-2145), Morinishi_TwoPointFlux (:2147-2229),
+// Ducros_TwoPointFlux (:2231-2294), KennedyGruber_TwoPointFlux (:2296-2367), Pirozzoli_TwoPointFlux
+// (:2369-2437).
 template <typename R>
 __device__ __forceinline__ void two_point_flux(const PhysR<R>& p, const R* QL, const R* QR, const R* JaL, const R* JaR,
                                                R* fs) {
@@ -228,18 +322,67 @@ __device__ __forceinline__ void two_point_flux(const PhysR<R>& p, const R* QL, c
                         wL * HL + wR * HR};
 #pragma unroll
         for (int q = 0; q < 5; ++q) fs[q] = R(0.25) * (f[q] * J0 + g[q] * J1 + h[q] * J2);
-    } else {
+        return;
+    }
+    const R J0 = R(0.5) * (JaL[0] + JaR[0]), J1 = R(0.5) * (JaL[1] + JaR[1]), J2 = R(0.5) * (JaL[2] + JaR[2]);
+    const R vel[2][3] = {{uL, vL, wL}, {uR, vR, wR}};
+    R F[3][5];
+    if (p.averaging == 2) {  // Ducros
+        const R pp = R(0.5) * (pL + pR);
+        const R HL = QL[4] + pL + p.h_ref, HR = QR[4] + pR + p.h_ref;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const R su = vel[0][d] + vel[1][d];
+            F[d][0] = R(0.25) * (QL[0] + QR[0]) * su;
+            F[d][1] = R(0.25) * (QL[1] + QR[1]) * su + (d == 0 ? pp : R(0));
+            F[d][2] = R(0.25) * (QL[2] + QR[2]) * su + (d == 1 ? pp : R(0));
+            F[d][3] = R(0.25) * (QL[3] + QR[3]) * su + (d == 2 ? pp : R(0));
+            F[d][4] = R(0.25) * (HL + HR) * su;
+        }
+    } else if (p.averaging == 3) {  // Morinishi
+        const R pp = R(0.5) * (pL + pR);
+        const R hL = p.g_over_gm1 * (pL + p.p_ref), hR = p.g_over_gm1 * (pR + p.p_ref);
+        const R kL2 = uL * uL + vL * vL + wL * wL, kR2 = uR * uR + vR * vR + wR * wR;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const R mL = QL[1 + d], mR = QR[1 + d], m = mL + mR;
+            F[d][0] = R(0.5) * m;
+            F[d][1] = R(0.25) * m * (uL + uR) + (d == 0 ? pp : R(0));
+            F[d][2] = R(0.25) * m * (vL + vR) + (d == 1 ? pp : R(0));
+            F[d][3] = R(0.25) * m * (wL + wR) + (d == 2 ? pp : R(0));
+            F[d][4] = R(0.5) * (vel[0][d] * hL + vel[1][d] * hR) + R(0.25) * (mL * uL + mR * uR) * (uL + uR) +
+                      R(0.25) * (mL * vL + mR * vR) * (vL + vR) + R(0.25) * (mL * wL + mR * wR) * (wL + wR) -
+                      R(0.25) * (mL * kL2 + mR * kR2);
+        }
+    } else if (p.averaging == 4) {  // Kennedy-Gruber
+        const R rho = R(0.5) * (QL[0] + QR[0]), u = R(0.5) * (uL + uR), v = R(0.5) * (vL + vR);
+        const R w = R(0.5) * (wL + wR), pp = R(0.5) * (pL + pR);
+        const R e = R(0.5) * ((QL[4] + p.e_ref) * iL + (QR[4] + p.e_ref) * iR);
+        const R pa = pp + p.p_ref;
+        const R um[3] = {u, v, w};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const R ru = rho * um[d];
+            F[d][0] = ru;
+            F[d][1] = ru * u + (d == 0 ? pp : R(0));
+            F[d][2] = ru * v + (d == 1 ? pp : R(0));
+            F[d][3] = ru * w + (d == 2 ? pp : R(0));
+            F[d][4] = ru * e + pa * um[d];
+        }
+    } else {  // Pirozzoli
         const R rho = R(0.5) * (QL[0] + QR[0]), u = R(0.5) * (uL + uR), v = R(0.5) * (vL + vR), w = R(0.5) * (wL + wR);
         const R pp = R(0.5) * (pL + pR);
         const R h = R(0.5) * ((QL[4] + pL + p.h_ref) * iL + (QR[4] + pR + p.h_ref) * iR);
-        const R J0 = R(0.5) * (JaL[0] + JaR[0]), J1 = R(0.5) * (JaL[1] + JaR[1]), J2 = R(0.5) * (JaL[2] + JaR[2]);
         const R ru = rho * u, rv = rho * v, rw = rho * w;
         fs[0] = ru * J0 + rv * J1 + rw * J2;
         fs[1] = (ru * u + pp) * J0 + (rv * u) * J1 + (rw * u) * J2;
         fs[2] = (ru * v) * J0 + (rv * v + pp) * J1 + (rw * v) * J2;
         fs[3] = (ru * w) * J0 + (rv * w) * J1 + (rw * w + pp) * J2;
         fs[4] = (ru * h) * J0 + (rv * h) * J1 + (rw * h) * J2;
+        return;
     }
+#pragma unroll
+    for (int q = 0; q < 5; ++q) fs[q] = F[0][q] * J0 + F[1][q] * J1 + F[2][q] * J2;
 }
 
 // Convergence/SETUP/ProblemFile.f90:31-133 state_source_in_point: the source term S(x,t).

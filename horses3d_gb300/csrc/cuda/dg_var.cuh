@@ -543,6 +543,8 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS) kv_face(VArgs<R> a)
             }
             if (ph.riemann == 0) {
                 roe_flux(ph, QL, QR, n, inv);
+            } else if (ph.riemann == 3) {
+                rusanov_flux(ph, QL, QR, n, inv);
             } else {
                 const R t1[3] = {a.ft1[3 * gp], a.ft1[3 * gp + 1], a.ft1[3 * gp + 2]};
                 const R t2[3] = {a.ft2[3 * gp], a.ft2[3 * gp + 1], a.ft2[3 * gp + 2]};
@@ -707,6 +709,8 @@ __global__ void __launch_bounds__(128) kv_face_direct(VArgs<R> a) {
     R inv[5];
     if (ph.riemann == 0) {
         roe_flux(ph, QL, QR, n, inv);
+    } else if (ph.riemann == 3) {
+        rusanov_flux(ph, QL, QR, n, inv);
     } else {
         const R t1[3] = {a.ft1[3 * gpt], a.ft1[3 * gpt + 1], a.ft1[3 * gpt + 2]};
         const R t2[3] = {a.ft2[3 * gpt], a.ft2[3 * gpt + 1], a.ft2[3 * gpt + 2]};

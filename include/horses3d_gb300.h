@@ -47,8 +47,11 @@ extern "C" {
 /* ---- enumerations (values match the reference's keyword choices) ------------------------- */
 enum { DG_NODES_GAUSS = 0, DG_NODES_GAUSS_LOBATTO = 1 };          /* "discretization nodes" */
 enum { DG_INVISCID_STANDARD = 0, DG_INVISCID_SPLIT = 1 };          /* "inviscid discretization" */
-enum { DG_RIEMANN_ROE = 0, DG_RIEMANN_LXF = 1 };                   /* "riemann solver" */
-enum { DG_AVG_STANDARD = 0, DG_AVG_PIROZZOLI = 1 };                /* "averaging" */
+enum { DG_RIEMANN_ROE = 0, DG_RIEMANN_LXF = 1,                    /* "riemann solver" */
+       DG_RIEMANN_CENTRAL = 2, DG_RIEMANN_RUSANOV = 3 };
+enum { DG_AVG_STANDARD = 0, DG_AVG_PIROZZOLI = 1,                  /* "averaging" (LxF, central and */
+       DG_AVG_DUCROS = 2, DG_AVG_MORINISHI = 3,                    /*  the split form's two-point */
+       DG_AVG_KENNEDY_GRUBER = 4 };                                /*  fluxes) */
 enum { DG_PRECISION_FP64 = 0, DG_PRECISION_MIXED = 1 };            /* plain FP64 / FP32 flux form */
 enum { DG_SOURCE_NONE = 0, DG_SOURCE_MMS_CONVERGENCE = 1 };        /* UserDefinedSourceTermNS */
 enum { DG_FIELD_Q = 0, DG_FIELD_QDOT = 1, DG_FIELD_G = 2,

@@ -308,8 +308,11 @@ static void roe(const Phys& p, const double* QL, const double* QR, const double*
     }
 }
 
-// RiemannSolvers_NS.f90:1784-1813 StandardAverage and :1927-1962 PirozzoliAverage (rotated states).
-static void average(int avg, const double* L, const double* R, double pL, double pR, double iL, double iR, double* f) {
+// Averaged states of the rotated (normal, t1, t2) frame: RiemannSolvers_NS.f90:1784-1819 StandardAverage,
+// :1821-1848 DucrosAverage, :1850-1886 MorinishiAverage, :1888-1925 KennedyGruberAverage,
+// :1927-1962 PirozzoliAverage.
+static void average(const Phys& ph, int avg, const double* L, const double* R, double pL, double pR, double iL,
+                    double iR, double* f) {
     const double uL = iL * L[1], uR = iR * R[1], vL = iL * L[2], vR = iR * R[2], wL = iL * L[3], wR = iR * R[3];
     if (avg == DG_AVG_STANDARD) {
         f[0] = 0.5 * (L[1] + R[1]);
@@ -317,6 +320,27 @@ static void average(int avg, const double* L, const double* R, double pL, double
         f[2] = 0.5 * (L[1] * vL + R[1] * vR);
         f[3] = 0.5 * (L[1] * wL + R[1] * wR);
         f[4] = 0.5 * (uL * (L[4] + pL) + uR * (R[4] + pR));
+    } else if (avg == DG_AVG_DUCROS) {
+        f[0] = 0.25 * (L[0] + R[0]) * (uL + uR);
+        f[1] = 0.25 * (L[1] + R[1]) * (uL + uR) + 0.5 * (pL + pR);
+        f[2] = 0.25 * (L[2] + R[2]) * (uL + uR);
+        f[3] = 0.25 * (L[3] + R[3]) * (uL + uR);
+        f[4] = 0.25 * (L[4] + pL + R[4] + pR) * (uL + uR);
+    } else if (avg == DG_AVG_MORINISHI) {
+        const double cp = ph.gamma / ph.gm1;
+        const double hL = cp * pL, hR = cp * pR;
+        f[0] = 0.5 * (L[1] + R[1]);
+        f[1] = 0.25 * (L[1] + R[1]) * (uL + uR) + 0.5 * (pL + pR);
+        f[2] = 0.25 * (L[1] + R[1]) * (vL + vR);
+        f[3] = 0.25 * (L[1] + R[1]) * (wL + wR);
+        f[4] = 0.5 * (uL * hL + uR * hR) + 0.25 * (L[1] * uL + R[1] * uR) * (uL + uR) +
+               0.25 * (L[1] * vL + R[1] * vR) * (vL + vR) + 0.25 * (L[1] * wL + R[1] * wR) * (wL + wR) -
+               0.25 * (L[1] * uL * uL + R[1] * uR * uR) - 0.25 * (L[1] * vL * vL + R[1] * vR * vR) -
+               0.25 * (L[1] * wL * wL + R[1] * wR * wR);
+    } else if (avg == DG_AVG_KENNEDY_GRUBER) {
+        const double rho = 0.5 * (L[0] + R[0]), u = 0.5 * (uL + uR), v = 0.5 * (vL + vR), w = 0.5 * (wL + wR);
+        const double p = 0.5 * (pL + pR), e = 0.5 * (L[4] * iL + R[4] * iR);
+        f[0] = rho * u; f[1] = rho * u * u + p; f[2] = rho * u * v; f[3] = rho * u * w; f[4] = rho * u * e + p * u;
     } else {
         const double rho = 0.5 * (L[0] + R[0]), u = 0.5 * (uL + uR), v = 0.5 * (vL + vR), w = 0.5 * (wL + wR);
         const double p = 0.5 * (pL + pR);
@@ -344,11 +368,37 @@ static void lxf(const Phys& p, int avg, double lambdaStab, const double* QL, con
     const double Lr[5] = {rhoL, rhouL, rhovL, rhowL, QL[4]};
     const double Rr[5] = {rhoR, rhouR, rhovR, rhowR, QR[4]};
     double f[5];
-    average(avg, Lr, Rr, pL, pR, iL, iR, f);
+    average(p, avg, Lr, Rr, pL, pR, iL, iR, f);
     for (int v = 0; v < 5; ++v) f[v] = f[v] - lambdaStab * (0.5 * lambda * (Rr[v] - Lr[v]));
     flux[0] = f[0];
     for (int c = 0; c < 3; ++c) flux[1 + c] = n[c] * f[1] + t1[c] * f[2] + t2[c] * f[3];
     flux[4] = f[4];
+}
+
+// RiemannSolvers_NS.f90:1661-1762 RusanovRiemannSolver.
+static void rusanov(const Phys& p, const double* QL, const double* QR, const double* n, double* flux) {
+    const double g = p.gamma;
+    const double rho = QL[0], rhou = QL[1], rhov = QL[2], rhow = QL[3], rhoe = QL[4];
+    const double rhon = QR[0], rhoun = QR[1], rhovn = QR[2], rhown = QR[3], rhoen = QR[4];
+    const double ul = rhou / rho, vl = rhov / rho, wl = rhow / rho;
+    const double pleft = (g - 1.0) * (rhoe - 0.5 / rho * (rhou * rhou + rhov * rhov + rhow * rhow));
+    const double ur = rhoun / rhon, vr = rhovn / rhon, wr = rhown / rhon;
+    const double pright = (g - 1.0) * (rhoen - 0.5 / rhon * (rhoun * rhoun + rhovn * rhovn + rhown * rhown));
+    const double ql = n[0] * ul + n[1] * vl + n[2] * wl;
+    const double qr = n[0] * ur + n[1] * vr + n[2] * wr;
+    const double hl = 0.5 * (ul * ul + vl * vl + wl * wl) + g / (g - 1.0) * pleft / rho;
+    const double hr = 0.5 * (ur * ur + vr * vr + wr * wr) + g / (g - 1.0) * pright / rhon;
+    const double ar = std::sqrt((g - 1.0) * (hr - 0.5 * (ur * ur + vr * vr + wr * wr)));
+    const double al = std::sqrt((g - 1.0) * (hl - 0.5 * (ul * ul + vl * vl + wl * wl)));
+    const double rql = rho * ql, rqr = rhon * qr;
+    double f[5];
+    f[0] = rql + rqr;
+    f[1] = rql * ul + pleft * n[0] + rqr * ur + pright * n[0];
+    f[2] = rql * vl + pleft * n[1] + rqr * vr + pright * n[1];
+    f[3] = rql * wl + pleft * n[2] + rqr * wr + pright * n[2];
+    f[4] = rql * hl + rqr * hr;
+    const double smax = std::fmax(ar + std::fabs(qr), al + std::fabs(ql));
+    for (int v = 0; v < 5; ++v) flux[v] = (f[v] - smax * (QR[v] - QL[v])) / 2.0;
 }
 
 // RiemannSolvers_NS.f90:2085-2145 StandardDG_TwoPointFlux and :2369-2437 Pirozzoli_TwoPointFlux.
@@ -358,9 +408,9 @@ static void two_point(const Phys& p, int avg, const double* QL, const double* QR
     const double uL = iL * QL[1], uR = iR * QR[1], vL = iL * QL[2], vR = iR * QR[2], wL = iL * QL[3], wR = iR * QR[3];
     const double pL = p.gm1 * (QL[4] - 0.5 * (QL[1] * uL + QL[2] * vL + QL[3] * wL));
     const double pR = p.gm1 * (QR[4] - 0.5 * (QR[1] * uR + QR[2] * vR + QR[3] * wR));
+    double f[5], g[5], h[5];
     if (avg == DG_AVG_STANDARD) {
         const double Ja[3] = {JaL[0] + JaR[0], JaL[1] + JaR[1], JaL[2] + JaR[2]};
-        double f[5], g[5], h[5];
         f[0] = QL[1] + QR[1]; f[1] = QL[1] * uL + QR[1] * uR + pL + pR; f[2] = QL[1] * vL + QR[1] * vR;
         f[3] = QL[1] * wL + QR[1] * wR; f[4] = uL * (QL[4] + pL) + uR * (QR[4] + pR);
         g[0] = QL[2] + QR[2]; g[1] = QL[2] * uL + QR[2] * uR; g[2] = QL[2] * vL + QR[2] * vR + pL + pR;
@@ -368,16 +418,60 @@ static void two_point(const Phys& p, int avg, const double* QL, const double* QR
         h[0] = QL[3] + QR[3]; h[1] = QL[3] * uL + QR[3] * uR; h[2] = QL[3] * vL + QR[3] * vR;
         h[3] = QL[3] * wL + QR[3] * wR + pL + pR; h[4] = wL * (QL[4] + pL) + wR * (QR[4] + pR);
         for (int v = 0; v < 5; ++v) fs[v] = 0.25 * (f[v] * Ja[0] + g[v] * Ja[1] + h[v] * Ja[2]);
-    } else {
+        return;
+    }
+    const double Ja[3] = {0.5 * (JaL[0] + JaR[0]), 0.5 * (JaL[1] + JaR[1]), 0.5 * (JaL[2] + JaR[2])};
+    if (avg == DG_AVG_DUCROS) {  // :2231-2294
+        const double su[3] = {uL + uR, vL + vR, wL + wR};
+        double* F[3] = {f, g, h};
+        for (int d = 0; d < 3; ++d) {
+            F[d][0] = 0.25 * (QL[0] + QR[0]) * su[d];
+            F[d][1] = 0.25 * (QL[1] + QR[1]) * su[d];
+            F[d][2] = 0.25 * (QL[2] + QR[2]) * su[d];
+            F[d][3] = 0.25 * (QL[3] + QR[3]) * su[d];
+            F[d][1 + d] += 0.5 * (pL + pR);
+            F[d][4] = 0.25 * (QL[4] + pL + QR[4] + pR) * su[d];
+        }
+    } else if (avg == DG_AVG_MORINISHI) {  // :2147-2229
+        const double hL = p.gamma / p.gm1 * pL, hR = p.gamma / p.gm1 * pR;
+        const double velL[3] = {uL, vL, wL}, velR[3] = {uR, vR, wR};
+        double* F[3] = {f, g, h};
+        for (int d = 0; d < 3; ++d) {
+            const double mL = QL[1 + d], mR = QR[1 + d];
+            F[d][0] = 0.5 * (mL + mR);
+            F[d][1] = 0.25 * (mL + mR) * (uL + uR);
+            F[d][2] = 0.25 * (mL + mR) * (vL + vR);
+            F[d][3] = 0.25 * (mL + mR) * (wL + wR);
+            F[d][1 + d] += 0.5 * (pL + pR);
+            F[d][4] = 0.5 * (velL[d] * hL + velR[d] * hR) + 0.25 * (mL * uL + mR * uR) * (uL + uR) +
+                      0.25 * (mL * vL + mR * vR) * (vL + vR) + 0.25 * (mL * wL + mR * wR) * (wL + wR) -
+                      0.25 * (mL * uL * uL + mR * uR * uR) - 0.25 * (mL * vL * vL + mR * vR * vR) -
+                      0.25 * (mL * wL * wL + mR * wR * wR);
+        }
+    } else if (avg == DG_AVG_KENNEDY_GRUBER) {  // :2296-2367
+        const double rho = 0.5 * (QL[0] + QR[0]), u = 0.5 * (uL + uR), v = 0.5 * (vL + vR), w = 0.5 * (wL + wR);
+        const double pp = 0.5 * (pL + pR), e = 0.5 * (QL[4] * iL + QR[4] * iR);
+        const double um[3] = {u, v, w};
+        double* F[3] = {f, g, h};
+        for (int d = 0; d < 3; ++d) {
+            F[d][0] = rho * um[d];
+            F[d][1] = rho * um[d] * u;
+            F[d][2] = rho * um[d] * v;
+            F[d][3] = rho * um[d] * w;
+            F[d][1 + d] += pp;
+            F[d][4] = rho * um[d] * e + pp * um[d];
+        }
+    } else {  // Pirozzoli, :2369-2437
         const double rho = 0.5 * (QL[0] + QR[0]), u = 0.5 * (uL + uR), v = 0.5 * (vL + vR), w = 0.5 * (wL + wR);
         const double pp = 0.5 * (pL + pR);
-        const double h = 0.5 * ((QL[4] + pL) * iL + (QR[4] + pR) * iR);
-        const double Ja[3] = {0.5 * (JaL[0] + JaR[0]), 0.5 * (JaL[1] + JaR[1]), 0.5 * (JaL[2] + JaR[2])};
-        const double ff[5] = {rho * u, rho * u * u + pp, rho * u * v, rho * u * w, rho * u * h};
-        const double gg[5] = {rho * v, rho * v * u, rho * v * v + pp, rho * v * w, rho * v * h};
-        const double hh[5] = {rho * w, rho * w * u, rho * w * v, rho * w * w + pp, rho * w * h};
-        for (int q = 0; q < 5; ++q) fs[q] = ff[q] * Ja[0] + gg[q] * Ja[1] + hh[q] * Ja[2];
+        const double hh = 0.5 * ((QL[4] + pL) * iL + (QR[4] + pR) * iR);
+        const double ff[5] = {rho * u, rho * u * u + pp, rho * u * v, rho * u * w, rho * u * hh};
+        const double gg[5] = {rho * v, rho * v * u, rho * v * v + pp, rho * v * w, rho * v * hh};
+        const double hhh[5] = {rho * w, rho * w * u, rho * w * v, rho * w * w + pp, rho * w * hh};
+        for (int q = 0; q < 5; ++q) fs[q] = ff[q] * Ja[0] + gg[q] * Ja[1] + hhh[q] * Ja[2];
+        return;
     }
+    for (int q = 0; q < 5; ++q) fs[q] = f[q] * Ja[0] + g[q] * Ja[1] + h[q] * Ja[2];
 }
 
 // Convergence/SETUP/ProblemFile.f90:31-133 state_source_in_point (manufactured solution).
@@ -838,8 +932,10 @@ static void compute_rhs(Solver& s, double t) {
             }
             double inv[5];
             if (s.opt.riemann == DG_RIEMANN_ROE) roe(s.ph, &f.Q[0][5 * p], &f.Q[1][5 * p], n, inv);
-            else lxf(s.ph, s.opt.averaging, s.opt.lambda_stab, &f.Q[0][5 * p], &f.Q[1][5 * p], n, &s.ft1[3 * (f.off + p)],
-                     &s.ft2[3 * (f.off + p)], inv);
+            else if (s.opt.riemann == DG_RIEMANN_RUSANOV) rusanov(s.ph, &f.Q[0][5 * p], &f.Q[1][5 * p], n, inv);
+            else  // LxF, or central = LxF with lambdaStab = 0 (RiemannSolvers_NS.f90:224)
+                lxf(s.ph, s.opt.averaging, s.opt.riemann == DG_RIEMANN_CENTRAL ? 0.0 : s.opt.lambda_stab,
+                    &f.Q[0][5 * p], &f.Q[1][5 * p], n, &s.ft1[3 * (f.off + p)], &s.ft2[3 * (f.off + p)], inv);
             for (int v = 0; v < 5; ++v) flux[5 * p + v] = (inv[v] - visc[v]) * s.fj[f.off + p];
         }
         project_to_side(f, 1, 5, flux, f.fStar[0], -1.0, s.nodes);

@@ -159,7 +159,15 @@ def test_control_file_keys():
     with pytest.raises(UnsupportedOption):
         parse_control("viscous discretization = BR2\nreynolds number = 1\n")
     with pytest.raises(UnsupportedOption):
-        parse_control("riemann solver = rusanov\nreynolds number = 1\n")
+        parse_control("riemann solver = roe-pike\nreynolds number = 1\n")
+
+
+def test_riemann_and_averaging_keys():
+    c = parse_control("riemann solver = Rusanov\naveraging = Kennedy-Gruber\nreynolds number = 1\n")
+    assert c.riemann == _abi.DG_RIEMANN_RUSANOV and c.averaging == _abi.DG_AVG_KENNEDY_GRUBER
+    c = parse_control("riemann solver = central\naveraging = ducros\nreynolds number = 1\n")
+    assert c.riemann == _abi.DG_RIEMANN_CENTRAL and c.averaging == _abi.DG_AVG_DUCROS
+    assert parse_control("averaging = morinishi\nreynolds number = 1\n").averaging == _abi.DG_AVG_MORINISHI
 
 
 def test_anisotropic_order_keys(tmp_path):

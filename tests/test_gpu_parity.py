@@ -212,3 +212,35 @@ def test_max_dt_filter_ties_and_high_mach(precision):
             # the mixed form keeps the metric terms in FP32, so its FP64 quotients see rounded metrics
             tol = 1e-15 if precision == _abi.DG_PRECISION_FP64 else 1e-6
             assert abs(g.max_time_step(cfl, dcfl) - ref) <= tol * ref, (cfl, dcfl)
+
+
+SOLVERS = [(_abi.DG_RIEMANN_LXF, _abi.DG_AVG_DUCROS), (_abi.DG_RIEMANN_LXF, _abi.DG_AVG_MORINISHI),
+           (_abi.DG_RIEMANN_LXF, _abi.DG_AVG_KENNEDY_GRUBER), (_abi.DG_RIEMANN_CENTRAL, _abi.DG_AVG_STANDARD),
+           (_abi.DG_RIEMANN_CENTRAL, _abi.DG_AVG_KENNEDY_GRUBER), (_abi.DG_RIEMANN_RUSANOV, _abi.DG_AVG_STANDARD)]
+
+
+@pytest.mark.parametrize("riemann,averaging", SOLVERS)
+def test_more_riemann_solvers_and_averages(riemann, averaging):
+    """Central, Rusanov and the Ducros / Morinishi / Kennedy-Gruber averages (RiemannSolvers_NS.f90),
+    plain form against the oracle and mixed form within 1e-6 of it."""
+    mesh, cfg, q0 = cases.tgv_case(n=3, order=4, nodes=_abi.DG_NODES_GAUSS, riemann=riemann, averaging=averaging,
+                                   warp=0.1, mach=0.3, perturbation=0.02, seed=3)
+    _check_rhs(mesh, cfg, q0)
+    _check_steps(mesh, cfg, q0, steps=2, dt=2e-3)
+    import dataclasses
+
+    mixed = dataclasses.replace(cfg, precision=_abi.DG_PRECISION_MIXED)
+    _check_steps(mesh, mixed, q0, steps=2, dt=2e-3, tol=MIXED_TOL)
+
+
+@pytest.mark.parametrize("averaging", [_abi.DG_AVG_DUCROS, _abi.DG_AVG_MORINISHI, _abi.DG_AVG_KENNEDY_GRUBER])
+def test_split_form_two_point_fluxes(averaging):
+    """Split form with the Ducros, Morinishi and Kennedy-Gruber two-point fluxes."""
+    mesh, cfg, q0 = cases.tgv_case(n=3, order=4, nodes=_abi.DG_NODES_GAUSS_LOBATTO, riemann=_abi.DG_RIEMANN_LXF,
+                                   inviscid=_abi.DG_INVISCID_SPLIT, averaging=averaging, perturbation=0.01, seed=5)
+    _check_rhs(mesh, cfg, q0)
+    _check_steps(mesh, cfg, q0, steps=2, dt=2e-3)
+    import dataclasses
+
+    mixed = dataclasses.replace(cfg, precision=_abi.DG_PRECISION_MIXED)
+    _check_steps(mesh, mixed, q0, steps=2, dt=2e-3, tol=MIXED_TOL)

@@ -241,3 +241,15 @@ def test_autotune_keeps_results_and_persists(tmp_path, monkeypatch):
     assert np.array_equal(g1.Q, g2.Q)
     rows = {tuple(int(v) for v in ln.split()[:3]) for ln in (tmp_path / "tune.txt").read_text().splitlines() if ln.strip()}
     assert {tuple(int(v) + 1 for v in o) for o in mesh.order} <= rows
+
+
+@pytest.mark.parametrize("riemann,averaging", [(_abi.DG_RIEMANN_RUSANOV, _abi.DG_AVG_STANDARD),
+                                               (_abi.DG_RIEMANN_CENTRAL, _abi.DG_AVG_DUCROS),
+                                               (_abi.DG_RIEMANN_LXF, _abi.DG_AVG_KENNEDY_GRUBER)])
+def test_anisotropic_more_solvers(riemann, averaging):
+    mesh, cfg, q0 = cases.aniso_tgv_case(n=3, lo=1, hi=4, seed=31, riemann=riemann)
+    import dataclasses
+
+    cfg = dataclasses.replace(cfg, averaging=averaging)
+    _check_rhs(mesh, cfg, q0)
+    _check_steps(mesh, cfg, q0, steps=2, dt=2e-3)
