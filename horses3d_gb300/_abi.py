@@ -81,6 +81,12 @@ class DgOptions(C.Structure):
 
 
 # (name, restype, argtypes) of every entry point in include/horses3d_gb300.h
+class SolutionHeader(C.Structure):
+    """h3d_solution_header: the .hsol header (io/SolutionFile.f90)."""
+    _fields_ = [("name", C.c_char * 128), ("file_type", C.c_int32), ("node_type", C.c_int32),
+                ("n_elements", C.c_int32), ("iteration", C.c_int32), ("time", C.c_double), ("refs", C.c_double * 6)]
+
+
 SIGNATURES = [
     ("dg_version", C.c_char_p, []),
     ("dg_strerror", C.c_char_p, [C.c_int]),
@@ -113,6 +119,11 @@ SIGNATURES = [
     ("dg_batch_run_steps", C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, _f64p]),
     ("dg_autotune", C.c_int, [C.c_void_p, C.c_int]),
     ("dg_inject_fault", C.c_int, [C.c_void_p, C.c_int]),
+    ("h3d_read_solution_header", C.c_int, [C.c_char_p, C.POINTER(SolutionHeader)]),
+    ("h3d_read_solution", C.c_int, [C.c_char_p, C.c_int32, _i32p, _f64p, _f64p]),
+    ("h3d_write_solution", C.c_int, [C.c_char_p, C.POINTER(SolutionHeader), _i32p, _f64p, _f64p]),
+    ("dg_save_solution", C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.c_int, C.c_double, C.c_int]),
+    ("dg_load_solution", C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     ("h3d_mesh_read_specmesh", C.c_int, [C.c_char_p, C.c_int, C.c_int, _i32p, C.c_char_p, C.POINTER(C.c_void_p)]),
     ("h3d_mesh_box", C.c_int, [C.c_int, C.c_int, C.c_int, _f64p, _f64p, C.c_double, C.c_int, C.c_int, C.c_int,
                                _i32p, C.POINTER(C.c_void_p)]),

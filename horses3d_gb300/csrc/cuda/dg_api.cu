@@ -725,3 +725,111 @@ int dg_batch_run_steps(dg_ctx* c, int n, double cfl, double dcfl, double* ms) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ solution files ------------
+namespace {
+
+// Element range, node range and orders of case k of a context.
+struct CaseView {
+    int e0 = 0, e1 = 0;
+    int64_t g0 = 0, g1 = 0;
+    std::vector<int32_t> orders;
+    double mach = 0.0;
+};
+
+int case_view(const dg_ctx* c, int k, CaseView& v) {
+    if (k < 0 || k >= c->n_cases) return h3d::fail(DG_ERR_INVALID, "case index out of range");
+    if (!c->var) {
+        v.e0 = 0;
+        v.e1 = c->K;
+        v.g0 = 0;
+        v.g1 = c->ndof;
+        v.orders.assign(3 * static_cast<size_t>(c->K), c->P - 1);
+        v.mach = c->phys.mach;
+        return DG_OK;
+    }
+    v.e0 = c->case_elem_off[k];
+    v.e1 = c->case_elem_off[k + 1];
+    v.g0 = c->case_ndof_off[k];
+    v.g1 = c->case_ndof_off[k + 1];
+    v.orders.resize(3 * static_cast<size_t>(v.e1 - v.e0));
+    for (int e = v.e0; e < v.e1; ++e) {
+        const int o = c->h_eord[e];
+        v.orders[3 * (e - v.e0)] = (o & 255) - 1;
+        v.orders[3 * (e - v.e0) + 1] = ((o >> 8) & 255) - 1;
+        v.orders[3 * (e - v.e0) + 2] = ((o >> 16) & 255) - 1;
+    }
+    v.mach = c->case_mach[k];
+    return DG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dg_save_solution(dg_ctx* c, int k, const char* path, int iteration, double time, int with_gradients) {
+    if (!c || !path) return h3d::fail(DG_ERR_INVALID, "null argument");
+    CaseView v;
+    int rc = case_view(c, k, v);
+    if (rc) return rc;
+    if (with_gradients && !c->phys.navier_stokes) return h3d::fail(DG_ERR_INVALID, "no gradients in Euler mode");
+    const size_t n5 = 5 * static_cast<size_t>(c->ndof);
+    std::vector<double> q(n5);
+    if ((rc = dg_download(c, DG_FIELD_Q, q.data()))) return rc;
+    std::vector<double> grad;
+    if (with_gradients) {
+        if ((rc = dg_rhs(c, time))) return rc;
+        std::vector<double> ux(n5), uy(n5), uz(n5);
+        if ((rc = dg_download(c, DG_FIELD_UX, ux.data())) || (rc = dg_download(c, DG_FIELD_UY, uy.data())) ||
+            (rc = dg_download(c, DG_FIELD_UZ, uz.data())))
+            return rc;
+        grad.resize(3 * 5 * static_cast<size_t>(v.g1 - v.g0));
+        int64_t off = v.g0;
+        for (int e = 0; e < v.e1 - v.e0; ++e) {
+            const int64_t np = static_cast<int64_t>(v.orders[3 * e] + 1) * (v.orders[3 * e + 1] + 1) * (v.orders[3 * e + 2] + 1);
+            const std::vector<double>* src[3] = {&ux, &uy, &uz};
+            for (int d = 0; d < 3; ++d)
+                std::memcpy(grad.data() + 15 * (off - v.g0) + 5 * np * d, src[d]->data() + 5 * off, sizeof(double) * 5 * np);
+            off += np;
+        }
+    }
+    h3d_solution_header h;
+    std::memset(&h, 0, sizeof(h));
+    std::strncpy(h.name, path, sizeof(h.name));
+    h.file_type = with_gradients ? 3 : 2;
+    h.node_type = c->nodes == DG_NODES_GAUSS ? 1 : 2;
+    h.n_elements = v.e1 - v.e0;
+    h.iteration = iteration;
+    h.time = time;
+    // PhysicsStorage_NS.f90:290-310 reference values (air defaults)
+    const double R = 287.15, T = 520.0 * 5.0 / 9.0;
+    h.refs[0] = 1.4;
+    h.refs[1] = R;
+    h.refs[2] = v.mach * std::sqrt(1.4 * R * T);
+    h.refs[3] = 101325.0 / (R * T);
+    h.refs[4] = T;
+    h.refs[5] = v.mach;
+    return h3d_write_solution(path, &h, v.orders.data(), q.data() + 5 * v.g0, with_gradients ? grad.data() : nullptr);
+}
+
+int dg_load_solution(dg_ctx* c, int k, const char* path, int* iteration, double* time) {
+    if (!c || !path) return h3d::fail(DG_ERR_INVALID, "null argument");
+    CaseView v;
+    int rc = case_view(c, k, v);
+    if (rc) return rc;
+    h3d_solution_header h;
+    if ((rc = h3d_read_solution_header(path, &h))) return rc;
+    if (h.file_type != 2 && h.file_type != 3)
+        return h3d::fail(DG_ERR_UNSUPPORTED, std::string(path) + ": only solution files (types 2 and 3) are read");
+    if (h.node_type != (c->nodes == DG_NODES_GAUSS ? 1 : 2))
+        return h3d::fail(DG_ERR_INVALID, std::string(path) + ": the file was written for the other node type");
+    std::vector<double> q(5 * static_cast<size_t>(c->ndof));
+    if ((rc = dg_download(c, DG_FIELD_Q, q.data()))) return rc;
+    if ((rc = h3d_read_solution(path, v.e1 - v.e0, v.orders.data(), q.data() + 5 * v.g0, nullptr))) return rc;
+    if ((rc = dg_upload_state(c, q.data()))) return rc;
+    if (iteration) *iteration = h.iteration;
+    if (time) *time = h.time;
+    return DG_OK;
+}
+
+}  // extern "C"

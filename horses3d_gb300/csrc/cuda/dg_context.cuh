@@ -108,6 +108,8 @@ struct dg_ctx {
     bool var = false;
     int n_cases = 1;
     std::vector<int64_t> case_ndof_off;  // [n_cases + 1] node offsets of the cases
+    std::vector<int> case_elem_off;      // [n_cases + 1] element offsets of the cases
+    std::vector<double> case_mach;
     std::vector<dg::CaseConst> case_const;
     std::vector<dg::PhysConst> case_pc;
     h3dctx::DevBuf<int4> items, faces4;

@@ -400,6 +400,9 @@ int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, cons
     std::vector<int> ecase;
     Gathered h;
     c->case_ndof_off.assign(n_cases + 1, 0);
+    c->case_elem_off.assign(n_cases + 1, 0);
+    c->case_mach.resize(n_cases);
+    for (int k = 0; k < n_cases; ++k) c->case_mach[k] = phys[k].mach;
     int64_t nodes = 0, spts = 0, fpts = 0;
     int kbase = 0;
     for (int k = 0; k < n_cases; ++k) {
@@ -448,6 +451,7 @@ int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, cons
         nodes += case_nodes;
         fpts += case_fpts;
         kbase += m.n_elements;
+        c->case_elem_off[k + 1] = kbase;
         c->case_ndof_off[k + 1] = nodes;
     }
     c->K = kbase;

@@ -104,6 +104,19 @@ class NavierStokesDG:
     def synchronize(self):
         _abi.check(_abi.lib().dg_synchronize(self._h), "dg_synchronize")
 
+    def save_solution(self, path, iteration: int, time: float, gradients: bool = False) -> None:
+        """HexMesh_SaveSolution (HexMesh.f90:3376-3555) from the device state."""
+        _abi.check(_abi.lib().dg_save_solution(self._h, 0, str(path).encode(), int(iteration), float(time),
+                                               1 if gradients else 0), "dg_save_solution")
+
+    def load_solution(self, path):
+        """Restart (HexMesh_LoadSolution, HexMesh.f90:4708-): uploads Q; returns (iteration, time)."""
+        it = C.c_int()
+        t = C.c_double()
+        _abi.check(_abi.lib().dg_load_solution(self._h, 0, str(path).encode(), C.byref(it), C.byref(t)),
+                   "dg_load_solution")
+        return it.value, t.value
+
     def autotune(self, reps: int = 5) -> None:
         """Per-order-triple item sizes of the variable-order kernels (a no-op for uniform orders)."""
         _abi.check(_abi.lib().dg_autotune(self._h, int(reps)), "dg_autotune")

@@ -206,6 +206,36 @@ int dg_inject_fault(dg_ctx* ctx, int kind);
  * the device time measured with events on the context's stream. */
 int dg_batch_run_steps(dg_ctx* ctx, int n, double cfl, double dcfl, double* ms);
 
+/* HORSES3D solution files (.hsol; io/SolutionFile.f90, HexMesh_SaveSolution/LoadSolution in
+ * HexMesh.f90:3376-3555,4708-). Host functions, no device needed. The gradient array of a type-3
+ * file holds, element after element, U_x, U_y, U_z (5 values per node each, reference layout). */
+typedef struct h3d_solution_header {
+    char name[128];          /* the name given at creation (not NUL-terminated when 128 long) */
+    int32_t file_type;       /* 2 solution, 3 solution and gradients (SolutionFile.f90:61-70) */
+    int32_t node_type;       /* 1 Gauss, 2 Gauss-Lobatto (the reference's numbering) */
+    int32_t n_elements;
+    int32_t iteration;
+    double time;
+    double refs[6];          /* gamma, R, V_ref, rho_ref, T_ref, Mach */
+} h3d_solution_header;
+int h3d_read_solution_header(const char* path, h3d_solution_header* header);
+/* Reads Q (5 per node, element order) and, when gradients is not NULL, the gradients of a type-3
+ * file; every element record must have the orders given in orders[3*n_elements]. */
+int h3d_read_solution(const char* path, int32_t n_elements, const int32_t* orders, double* q, double* gradients);
+/* Writes a type-2 file (gradients NULL) or a type-3 file (header->file_type must agree). */
+int h3d_write_solution(const char* path, const h3d_solution_header* header, const int32_t* orders, const double* q,
+                       const double* gradients);
+
+/* Saves case case_index of a context (0 for a single case) as a solution file written from the
+ * device state, with iteration and time in the header and the reference values of the case's Mach
+ * number (PhysicsStorage_NS.f90:290-310: T_ref = 520*5/9 K, p_ref = 101325 Pa, R = 287.15). With
+ * with_gradients (Navier-Stokes only) the lifted gradients of the current state are computed (one
+ * right-hand side at `time`) and written too (file type 3). */
+int dg_save_solution(dg_ctx* ctx, int case_index, const char* path, int iteration, double time, int with_gradients);
+/* Restart: loads Q of case case_index from a solution file (type 2 or 3, matching node type and
+ * element orders), uploads it and returns the file's iteration and time (either may be NULL). */
+int dg_load_solution(dg_ctx* ctx, int case_index, const char* path, int* iteration, double* time);
+
 /* Host-side mesh builder (HexMesh construction: Read_SpecMesh.f90:36-342, HexMesh.f90:356-736,
  * 2677-2990, MappedGeometry.f90:64-760). Produces a dg_mesh_desc whose arrays live in the mesh. */
 typedef struct h3d_mesh h3d_mesh;

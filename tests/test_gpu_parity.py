@@ -244,3 +244,28 @@ def test_split_form_two_point_fluxes(averaging):
 
     mixed = dataclasses.replace(cfg, precision=_abi.DG_PRECISION_MIXED)
     _check_steps(mesh, mixed, q0, steps=2, dt=2e-3, tol=MIXED_TOL)
+
+
+def test_solution_file_restart_continues_the_run(tmp_path):
+    """Save the device state after two steps, restart a new context from the file and step on: the
+    result equals four uninterrupted steps bit for bit (HexMesh_SaveSolution / LoadSolution)."""
+    mesh, cfg, q0 = cases.tgv_case(n=3, order=3, nodes=_abi.DG_NODES_GAUSS, perturbation=0.01, seed=2)
+    g = NavierStokesDG(mesh, cfg)
+    g.set_state(q0)
+    dt = 2e-3
+    t = g.run_steps(2, 0.0, dt=dt)
+    path = tmp_path / "restart.hsol"
+    g.save_solution(path, iteration=2, time=t, gradients=True)
+    g.run_steps(2, t, dt=dt)
+    h = NavierStokesDG(mesh, cfg)
+    h.set_state(q0 * 0 + 1.0)
+    it, t2 = h.load_solution(path)
+    assert it == 2 and t2 == t
+    h.run_steps(2, t2, dt=dt)
+    assert np.array_equal(g.Q, h.Q)
+    from horses3d_gb300 import solution_file
+
+    hd = solution_file.read_header(path)
+    assert hd.file_type == 3 and hd.node_type == 1 and hd.n_elements == mesh.n_elements
+    q, grad = solution_file.read(path, mesh.order, gradients=True)
+    assert np.all(np.isfinite(grad)) and np.abs(grad).max() > 0
