@@ -30,7 +30,7 @@ DG_INVISCID_STANDARD, DG_INVISCID_SPLIT = 0, 1
 DG_RIEMANN_ROE, DG_RIEMANN_LXF, DG_RIEMANN_CENTRAL, DG_RIEMANN_RUSANOV = 0, 1, 2, 3
 DG_AVG_STANDARD, DG_AVG_PIROZZOLI, DG_AVG_DUCROS, DG_AVG_MORINISHI, DG_AVG_KENNEDY_GRUBER = 0, 1, 2, 3, 4
 DG_PRECISION_FP64, DG_PRECISION_MIXED = 0, 1
-DG_SOURCE_NONE, DG_SOURCE_MMS_CONVERGENCE = 0, 1
+DG_SOURCE_NONE, DG_SOURCE_MMS_CONVERGENCE, DG_SOURCE_MMS_LAMB_VECTOR = 0, 1, 2
 DG_FIELD_Q, DG_FIELD_QDOT, DG_FIELD_G, DG_FIELD_UX, DG_FIELD_UY, DG_FIELD_UZ = range(6)
 
 _i32p = C.POINTER(C.c_int32)

@@ -98,6 +98,20 @@ class CaseBatch:
     def synchronize(self):
         _abi.check(_abi.lib().dg_synchronize(self._h), "dg_synchronize")
 
+    def save_solution(self, case: int, path, iteration: int, time: float, gradients: bool = False) -> None:
+        """One case's state (and gradients) as a HORSES3D solution file (HexMesh_SaveSolution)."""
+        _abi.check(_abi.lib().dg_save_solution(self._h, int(case), str(path).encode(), int(iteration), float(time),
+                                               1 if gradients else 0), "dg_save_solution")
+
+    def load_solution(self, case: int, path):
+        """Restarts one case from a solution file; the other cases keep their state. Returns
+        (iteration, time) from the file's header."""
+        it = C.c_int()
+        t = C.c_double()
+        _abi.check(_abi.lib().dg_load_solution(self._h, int(case), str(path).encode(), C.byref(it), C.byref(t)),
+                   "dg_load_solution")
+        return it.value, t.value
+
     def autotune(self, reps: int = 5) -> None:
         """Elements per CTA of every order triple, timed on this batch and cached for the process."""
         _abi.check(_abi.lib().dg_autotune(self._h, int(reps)), "dg_autotune")

@@ -139,8 +139,8 @@ int setup_store(dg_ctx* c, Store<R>& st, const dg_mesh_desc* m) {
     a.dt = c->scal.p + 1;
     a.src_gm1 = c->pc.gm1;
     a.src_gM2 = c->pc.gammaM2;
-    a.src_mu = c->pc.mu;
-    a.src_kappa = c->pc.kappa;
+    dg::source_constants(c->opt.source, c->phys.mach, c->phys.reynolds, c->phys.prandtl, c->pc.ns, &a.src_mu,
+                         &a.src_kappa);
     a.err = c->err_flag.p;
     return DG_OK;
 }
@@ -250,7 +250,7 @@ int validate(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op) 
         return h3d::fail(DG_ERR_UNSUPPORTED, "averaging");
     if (op->precision != DG_PRECISION_FP64 && op->precision != DG_PRECISION_MIXED)
         return h3d::fail(DG_ERR_UNSUPPORTED, "precision");
-    if (op->source != DG_SOURCE_NONE && op->source != DG_SOURCE_MMS_CONVERGENCE)
+    if (op->source < DG_SOURCE_NONE || op->source > DG_SOURCE_MMS_LAMB_VECTOR)
         return h3d::fail(DG_ERR_UNSUPPORTED, "source");
     return DG_OK;
 }

@@ -664,7 +664,8 @@ __device__ __forceinline__ void surface_integral(const Args<R>& a, int i, int j,
     }
     if (SRC) {
         double S[5];
-        mms_source(a.x[3 * g], a.x[3 * g + 1], a.x[3 * g + 2], t_src, a.src_gm1, a.src_gM2, a.src_mu, a.src_kappa, S);
+        manufactured_source(a.source, a.x[3 * g], a.x[3 * g + 1], a.x[3 * g + 2], t_src, a.src_gm1, a.src_gM2,
+                            a.src_mu, a.src_kappa, S);
 #pragma unroll
         for (int v = 0; v < 5; ++v) qd[v] = R(double(qd[v]) + S[v]);
     }

@@ -438,6 +438,75 @@ __device__ __forceinline__ void mms_source(double x, double y, double z, double 
     S[4] = e * S[0] + rho * e_t + rho * (u * ex + v * ex + w * ex) + p * div_v + u * px + v * px + w * px - vw - heat;
 }
 
+// LambVector/SETUP/ProblemFile.f90:377-423 UserDefinedSourceTermNS for the state of :8-27,
+//   rho = 3 + sin(phi) e^t, (u, v, w) = (cos phi, sin phi, cos phi) e^-t, E = rho |u|^2 / 2 + 1,
+// phi = x + y + z: the residual dQ/dt + div(F_inviscid - F_viscous / Re) of the dimensionless NS
+// equations for that state, with the constant viscosity mu and conductivity kappa the source term
+// is defined with (the solver's own fluxes keep Sutherland's law). Every field depends on phi
+// only, so d/dx = d/dy = d/dz = d/dphi; primes below are d/dphi. mu_re = mu / Re and
+// kap_re = kappa / Re.
+__host__ __device__ inline void lamb_vector_source(double x, double y, double z, double t, double gm1, double gMa2,
+                                                   double mu_re, double kap_re, double* S) {
+    const double ph = x + y + z;
+    const double a = sin(ph), b = cos(ph), ep = exp(t), em = exp(-t);
+    const double r = 3.0 + a * ep, r1 = b * ep, r2 = -a * ep, rt = a * ep;
+    const double U[3] = {b * em, a * em, b * em};     // dU/dt = -U
+    const double U1[3] = {-a * em, b * em, -a * em};
+    const double U2[3] = {-b * em, -a * em, -b * em};
+    double s = 0.0, D = 0.0, D1 = 0.0, k = 0.0, k1 = 0.0, k2 = 0.0, uu2 = 0.0, g1 = 0.0;
+    for (int i = 0; i < 3; ++i) {
+        s += U[i];              // u + v + w
+        D += U1[i];             // div u
+        D1 += U2[i];
+        k += 0.5 * U[i] * U[i];  // |u|^2 / 2
+        k1 += U[i] * U1[i];
+        uu2 += U[i] * U2[i];
+        g1 += U1[i] * U1[i];
+    }
+    k2 = g1 + uu2;
+    const double kt = -2.0 * k;
+    const double E = r * k + 1.0, E1 = r1 * k + r * k1, E2 = r2 * k + 2.0 * r1 * k1 + r * k2, Et = rt * k + r * kt;
+    const double ei = E - k, ei1 = E1 - k1, ei2 = E2 - k2;  // internal energy
+    const double p = gm1 * r * ei, p1 = gm1 * (r1 * ei + r * ei1);
+    const double T2 = gMa2 * gm1 * ei2;  // T = gamma M^2 (gamma - 1) e
+    S[0] = rt + r1 * s + r * D;
+    for (int j = 0; j < 3; ++j)
+        S[1 + j] = rt * U[j] - r * U[j] + (r1 * U[j] + r * U1[j]) * s + r * U[j] * D + p1 -
+                   mu_re * (3.0 * U2[j] + D1 / 3.0);
+    S[4] = rt * E + r * Et + (r1 * E + r * E1 + p1) * s + (r * E + p) * D -
+           mu_re * (D1 * s / 3.0 + 3.0 * uu2 + D * D / 3.0 + 3.0 * g1) - 3.0 * kap_re * T2;
+}
+
+// The source of the given DG_SOURCE_* kind (1 Convergence, 2 LambVector) with its constants.
+__device__ __forceinline__ void manufactured_source(int kind, double x, double y, double z, double t, double gm1,
+                                                    double gMa2, double mu, double kap, double* S) {
+    if (kind == 2) lamb_vector_source(x, y, z, t, gm1, gMa2, mu, kap, S);
+    else mms_source(x, y, z, t, gm1, gMa2, mu, kap, S);
+}
+
+// Viscosity and conductivity the sources are evaluated with, (mu, kappa) as the source functions
+// take them. Convergence: the dimensionless 1/Re and 1/((gamma-1) M^2 Re Pr). LambVector: the
+// dimensional reference viscosity refValues%mu = rho_ref V_ref L_ref / Re (PhysicsStorage_NS.f90:
+// 292-309; T_ref = 520*5/9 K, p_ref = 101325 Pa, R = 287.15 J/(kg K), L_ref = 1 m) and
+// kappa = mu * mu_to_kappa, both divided by Re; zero for the Euler equations.
+inline void source_constants(int kind, double mach, double reynolds, double prandtl, int ns, double* mu,
+                             double* kap) {
+    const double gamma = 1.4, gm1 = 1.4 - 1.0;
+    *mu = 0.0;
+    *kap = 0.0;
+    if (!ns) return;
+    if (kind == 2) {
+        const double R = 287.15, T = 520.0 * 5.0 / 9.0;
+        const double rho_ref = 101325.0 / (R * T), V_ref = mach * sqrt(gamma * R * T);
+        const double mu_ref = rho_ref * V_ref * 1.0 * (1.0 / reynolds);
+        *mu = mu_ref / reynolds;
+        *kap = mu_ref * (1.0 / (gm1 * (mach * mach) * prandtl)) / reynolds;
+    } else {
+        *mu = 1.0 / reynolds;
+        *kap = 1.0 / (gm1 * (mach * mach) * reynolds * prandtl);
+    }
+}
+
 // MeshTypes.f90:70-107 leftIndexes2Right.
 __device__ __forceinline__ void left2right(int i, int j, int Nx, int Ny, int rot, int& ii, int& jj) {
     switch (rot) {

@@ -790,7 +790,8 @@ __global__ void __launch_bounds__(256) kv_update(VArgs<R> a, int stage, double t
         if (SRC) {
             double S[5];
             const double tt = a.time[d.kase] + tshift * dt;
-            mms_source(a.x[3 * g], a.x[3 * g + 1], a.x[3 * g + 2], tt, cc.gm1, cc.gM2, cc.mu, cc.kappa, S);
+            manufactured_source(a.source, a.x[3 * g], a.x[3 * g + 1], a.x[3 * g + 2], tt, cc.gm1, cc.gM2, cc.mu,
+                                cc.kappa, S);
 #pragma unroll
             for (int v = 0; v < 5; ++v) qd[v] = R(double(qd[v]) + S[v]);
         }

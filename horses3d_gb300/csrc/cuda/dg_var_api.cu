@@ -360,7 +360,7 @@ int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, cons
         return h3d::fail(DG_ERR_UNSUPPORTED, "averaging");
     if (op->precision != DG_PRECISION_FP64 && op->precision != DG_PRECISION_MIXED)
         return h3d::fail(DG_ERR_UNSUPPORTED, "precision");
-    if (op->source != DG_SOURCE_NONE && op->source != DG_SOURCE_MMS_CONVERGENCE)
+    if (op->source < DG_SOURCE_NONE || op->source > DG_SOURCE_MMS_LAMB_VECTOR)
         return h3d::fail(DG_ERR_UNSUPPORTED, "source");
     for (int k = 0; k < n_cases; ++k) {
         int rc = validate_case(&meshes[k], &phys[k], k);
@@ -390,7 +390,9 @@ int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, cons
     for (int k = 0; k < n_cases; ++k) {
         c->case_pc[k] = phys_const(&phys[k], op);
         const dg::PhysConst& pc = c->case_pc[k];
-        c->case_const[k] = dg::CaseConst{0.0, pc.gm1, pc.gammaM2, pc.mu, pc.kappa};
+        c->case_const[k] = dg::CaseConst{0.0, pc.gm1, pc.gammaM2, 0.0, 0.0};
+        dg::source_constants(op->source, phys[k].mach, phys[k].reynolds, phys[k].prandtl, pc.ns,
+                             &c->case_const[k].mu, &c->case_const[k].kappa);
     }
 
     // element, slot and face tables of the concatenated cases

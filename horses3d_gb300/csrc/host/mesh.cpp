@@ -331,33 +331,47 @@ static FacePatch flat_patch(const double* p1, const double* p2, const double* p3
     return f;
 }
 
+// Fortran list-directed input as the SpecMesh reader uses it: every READ statement starts at a new
+// record (line), takes its values from as many records as it needs and skips the rest of its last
+// record (so element records with more face flags than the six read are accepted).
+template <typename T>
+static bool read_record(std::istream& in, T* v, int n) {
+    int got = 0;
+    std::string line;
+    while (got < n) {
+        if (!std::getline(in, line)) return false;
+        std::istringstream ls(line);
+        while (got < n && (ls >> v[got])) ++got;
+    }
+    return true;
+}
+
 // Read_SpecMesh.f90:36-342 (serial path): header, nodes, element records with optional curved
 // face patches given at Chebyshev-Lobatto knots, boundary names.
 bool read_specmesh(const std::string& path, MeshSource& src, std::string& err) {
     std::ifstream in(path);
     if (!in) { err = "cannot open mesh file " + path; return false; }
-    int nNodes = 0, nElem = 0, bOrder = 0;
-    if (!(in >> nNodes >> nElem >> bOrder)) { err = "bad SpecMesh header"; return false; }
+    int head[3] = {0, 0, 0};
+    if (!read_record(in, head, 3)) { err = "bad SpecMesh header"; return false; }
+    const int nNodes = head[0], nElem = head[1], bOrder = head[2];
+    if (nNodes < 8 || nElem < 1 || bOrder < 1) { err = "bad SpecMesh header"; return false; }
     src.bface_order = bOrder;
     const int nb = bOrder + 1;
     std::vector<double> knots(nb);
     for (int i = 0; i < nb; ++i) knots[i] = -std::cos((i * 1.0) * kPi / (nb - 1.0));
     src.nodes.resize(3 * static_cast<size_t>(nNodes));
     for (int j = 0; j < nNodes; ++j)
-        if (!(in >> src.nodes[3 * j] >> src.nodes[3 * j + 1] >> src.nodes[3 * j + 2])) {
-            err = "bad node record"; return false;
-        }
+        if (!read_record(in, &src.nodes[3 * j], 3)) { err = "bad node record"; return false; }
     src.elem_nodes.resize(8 * static_cast<size_t>(nElem));
     src.maps.assign(nElem, HexMap());
     src.bnames.assign(6 * static_cast<size_t>(nElem), "---");
     for (int l = 0; l < nElem; ++l) {
-        int flags[6];
+        int ids[8], flags[6];
+        if (!read_record(in, ids, 8) || !read_record(in, flags, 6)) { err = "bad element record"; return false; }
         for (int k = 0; k < 8; ++k) {
-            int id;
-            if (!(in >> id)) { err = "bad element record"; return false; }
-            src.elem_nodes[8 * l + k] = id - 1;
+            if (ids[k] < 1 || ids[k] > nNodes) { err = "element node id out of range"; return false; }
+            src.elem_nodes[8 * l + k] = ids[k] - 1;
         }
-        for (int k = 0; k < 6; ++k) in >> flags[k];
         HexMap& m = src.maps[l];
         const int maxflag = *std::max_element(flags, flags + 6);
         if (maxflag == 0) {
@@ -374,18 +388,17 @@ bool read_specmesh(const std::string& path, MeshSource& src, std::string& err) {
                     std::vector<double> pts(3 * nb * nb);
                     for (int j = 0; j < nb; ++j)
                         for (int i = 0; i < nb; ++i)
-                            in >> pts[3 * (i + nb * j)] >> pts[3 * (i + nb * j) + 1] >> pts[3 * (i + nb * j) + 2];
+                            if (!read_record(in, &pts[3 * (i + nb * j)], 3)) {
+                                err = "bad face patch record"; return false;
+                            }
                     m.faces[k].construct(knots, knots, pts);
                 }
             }
             m.set_faces();
         }
-        for (int k = 0; k < 6; ++k) {
-            std::string name;
-            in >> name;
-            src.bnames[6 * l + k] = lower(name);
-        }
-        if (!in) { err = "truncated SpecMesh file"; return false; }
+        std::string names[6];
+        if (!read_record(in, names, 6)) { err = "truncated SpecMesh file"; return false; }
+        for (int k = 0; k < 6; ++k) src.bnames[6 * l + k] = lower(names[k]);
     }
     return true;
 }

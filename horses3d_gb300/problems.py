@@ -105,6 +105,20 @@ def mms_convergence_state(x: np.ndarray, t: float):
     return q.reshape(-1), qd.reshape(-1)
 
 
+def mms_lamb_vector_state(x: np.ndarray, t: float) -> np.ndarray:
+    """Manufactured state of the reference's NavierStokes/LambVector case
+    (test/NavierStokes/LambVector/SETUP/ProblemFile.f90:8-27): rho = 3 + sin(phi) e^t,
+    (u, v, w) = (cos phi, sin phi, cos phi) e^-t, E = rho |u|^2 / 2 + 1, phi = x + y + z."""
+    x = np.asarray(x).reshape(-1, 3)
+    phi = x[:, 0] + x[:, 1] + x[:, 2]
+    rho = 3.0 + np.sin(phi) * np.exp(t)
+    u = np.cos(phi) * np.exp(-t)
+    v = np.sin(phi) * np.exp(-t)
+    w = np.cos(phi) * np.exp(-t)
+    e = rho * (u ** 2 + v ** 2 + w ** 2) / 2.0 + 1.0
+    return np.stack([rho, rho * u, rho * v, rho * w, rho * e], axis=1).reshape(-1)
+
+
 def rel_l2(a: np.ndarray, b: np.ndarray, weights: np.ndarray | None = None) -> np.ndarray:
     """Relative L2 difference per conserved variable: sqrt(sum w (a-b)^2) / sqrt(sum w b^2).
 

@@ -53,7 +53,9 @@ enum { DG_AVG_STANDARD = 0, DG_AVG_PIROZZOLI = 1,                  /* "averaging
        DG_AVG_DUCROS = 2, DG_AVG_MORINISHI = 3,                    /*  the split form's two-point */
        DG_AVG_KENNEDY_GRUBER = 4 };                                /*  fluxes) */
 enum { DG_PRECISION_FP64 = 0, DG_PRECISION_MIXED = 1 };            /* plain FP64 / FP32 flux form */
-enum { DG_SOURCE_NONE = 0, DG_SOURCE_MMS_CONVERGENCE = 1 };        /* UserDefinedSourceTermNS */
+enum { DG_SOURCE_NONE = 0,                                         /* UserDefinedSourceTermNS of */
+       DG_SOURCE_MMS_CONVERGENCE = 1,                              /*  NavierStokes/Convergence */
+       DG_SOURCE_MMS_LAMB_VECTOR = 2 };                            /*  NavierStokes/LambVector */
 enum { DG_FIELD_Q = 0, DG_FIELD_QDOT = 1, DG_FIELD_G = 2,
        DG_FIELD_UX = 3, DG_FIELD_UY = 4, DG_FIELD_UZ = 5 };
 

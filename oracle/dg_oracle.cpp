@@ -541,6 +541,60 @@ static void mms_point(double x, double y, double z, double t, double gm1, double
            w * p_x[2] - visc_work - heat;
 }
 
+// LambVector/SETUP/ProblemFile.f90:377-423 UserDefinedSourceTermNS, for the manufactured state of
+// :8-27 (rho = 3 + sin(phi) e^t, u = w = cos(phi) e^-t, v = sin(phi) e^-t, E = rho |u|^2/2 + 1,
+// phi = x + y + z). The source is dQ/dt + div(F_inviscid) - div(F_viscous)/Re with the constant
+// viscosity mu = refValues%mu and kappa = mu * mu_to_kappa it is defined with. Written here in
+// tensor form, term by term (d_i of every flux column by the product rule); every field depends
+// on phi only, so d_i f = f' and d_i d_l f = f'' for all i, l.
+static void lamb_point(double x, double y, double z, double t, double gm1, double gMa2, double mu_ref,
+                       double kap_ref, double Re, double* S) {
+    const double phi = x + y + z;
+    const double sn = std::sin(phi), cs = std::cos(phi), et = std::exp(t), emt = std::exp(-t);
+    const double rho = 3.0 + sn * et, rho_t = sn * et, rho_d = cs * et, rho_dd = -sn * et;
+    const double V[3] = {cs * emt, sn * emt, cs * emt};
+    const double V_t[3] = {-cs * emt, -sn * emt, -cs * emt};
+    const double V_d[3] = {-sn * emt, cs * emt, -sn * emt};
+    const double V_dd[3] = {-cs * emt, -sn * emt, -cs * emt};
+    const double q2 = V[0] * V[0] + V[1] * V[1] + V[2] * V[2];
+    const double q2_t = 2.0 * (V[0] * V_t[0] + V[1] * V_t[1] + V[2] * V_t[2]);
+    const double q2_d = 2.0 * (V[0] * V_d[0] + V[1] * V_d[1] + V[2] * V_d[2]);
+    const double q2_dd = 2.0 * (V_d[0] * V_d[0] + V_d[1] * V_d[1] + V_d[2] * V_d[2] + V[0] * V_dd[0] +
+                                V[1] * V_dd[1] + V[2] * V_dd[2]);
+    const double E = rho * q2 / 2.0 + 1.0;
+    const double E_t = rho_t * q2 / 2.0 + rho * q2_t / 2.0;
+    const double E_d = rho_d * q2 / 2.0 + rho * q2_d / 2.0;
+    const double E_dd = rho_dd * q2 / 2.0 + rho_d * q2_d + rho * q2_dd / 2.0;
+    const double p = gm1 * (rho * E - 0.5 * rho * q2);
+    const double p_d = gm1 * (rho_d * E + rho * E_d - 0.5 * (rho_d * q2 + rho * q2_d));
+    const double T_dd = gm1 * gMa2 * (E_dd - 0.5 * q2_dd);
+    // d_i(u_i): the divergence and its derivative
+    const double div = V_d[0] + V_d[1] + V_d[2], div_d = V_dd[0] + V_dd[1] + V_dd[2];
+    // time derivatives of Q
+    double dQ[5] = {rho_t, rho_t * V[0] + rho * V_t[0], rho_t * V[1] + rho * V_t[1], rho_t * V[2] + rho * V_t[2],
+                    rho_t * E + rho * E_t};
+    // inviscid divergence
+    double dF[5] = {0, 0, 0, 0, 0};
+    for (int i = 0; i < 3; ++i) {
+        dF[0] += rho_d * V[i] + rho * V_d[i];
+        for (int j = 0; j < 3; ++j)
+            dF[1 + j] += rho_d * V[j] * V[i] + rho * V_d[j] * V[i] + rho * V[j] * V_d[i] + (i == j ? p_d : 0.0);
+        dF[4] += (rho_d * E + rho * E_d + p_d) * V[i] + (rho * E + p) * V_d[i];
+    }
+    // viscous divergence: tau_ji = mu (d_i u_j + d_j u_i - 2/3 delta_ij div u)
+    double dG[5] = {0, 0, 0, 0, 0};
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j) {
+            const double tau = mu_ref * (V_d[j] + V_d[i] - (i == j ? 2.0 / 3.0 * div : 0.0));
+            const double tau_d = mu_ref * (V_dd[j] + V_dd[i] - (i == j ? 2.0 / 3.0 * div_d : 0.0));
+            dG[1 + j] += tau_d;
+            dG[4] += tau_d * V[j] + tau * V_d[j];
+        }
+        dG[4] += kap_ref * T_dd;
+    }
+    for (int q = 0; q < 5; ++q) S[q] = dQ[q] + dF[q] - dG[q] / Re;
+}
+
 // ---------------------------------------------------------------- solver state ---------------
 struct Elem {
     int N[3];
@@ -943,6 +997,13 @@ static void compute_rhs(Solver& s, double t) {
     }
     // Surface integrals, 1/J, source (SpatialDiscretization.f90:483-494, 1686-1701, 564-639)
     const double mms_mu = s.ph.mu, mms_kap = s.ph.kappa;
+    // LambVector's source viscosity: refValues%mu = rho_ref V_ref L_ref mu (PhysicsStorage_NS.f90:292-309),
+    // with T_ref = 520*5/9 K, p_ref = 101325 Pa, R = 287.15 J/(kg K), L_ref = 1; zero for Euler.
+    const double T_ref = 520.0 * 5.0 / 9.0, R_gas = 287.15;
+    const double lamb_mu = s.ph.ns ? (101325.0 / (R_gas * T_ref)) * (s.ph.Mach * std::sqrt(s.ph.gamma * R_gas * T_ref)) *
+                                         1.0 * s.ph.mu
+                                   : 0.0;
+    const double lamb_kap = lamb_mu * s.ph.mu_to_kappa;
 #pragma omp parallel for schedule(static)
     for (int id = 0; id < K; ++id) {
         const Elem& e = s.el[id];
@@ -966,6 +1027,12 @@ static void compute_rhs(Solver& s, double t) {
                         fi = fi + FT[v + 5 * (i + px * j)] * sz.bR[k];
                         s.QDot[5 * g + v] = s.QDot[5 * g + v] - fi;
                         s.QDot[5 * g + v] = s.QDot[5 * g + v] / s.jac[g];
+                    }
+                    if (s.opt.source == DG_SOURCE_MMS_LAMB_VECTOR) {
+                        double S[5];
+                        const double* xx = &s.x[3 * g];
+                        lamb_point(xx[0], xx[1], xx[2], t, s.ph.gm1, s.ph.gammaM2, lamb_mu, lamb_kap, s.ph.Re, S);
+                        for (int v = 0; v < 5; ++v) s.QDot[5 * g + v] = s.QDot[5 * g + v] + S[v];
                     }
                     if (s.opt.source == DG_SOURCE_MMS_CONVERGENCE) {
                         double Qe[5], S[5], Qd[5];

@@ -63,6 +63,41 @@ def convergence_errors(mesh, q, qdot, t):
     return err, qerr
 
 
+def lamb_vector_case(precision=_abi.DG_PRECISION_FP64):
+    """The reference's NavierStokes/LambVector case: periodic [0, 2 pi]^3 with 8^3 elements
+    (TaylorGreen8.mesh), N=5 Gauss nodes, Roe, BR1, M=0.08, Re=1600, dt=0.005 to t=0.100001,
+    manufactured source (LambVector/TaylorGreen.control)."""
+    mesh = HexMesh.box(8, [0, 0, 0], [TWO_PI] * 3, 5, node_type=_abi.DG_NODES_GAUSS)
+    cfg = Config(order=5, nodes=_abi.DG_NODES_GAUSS, mach=0.08, reynolds=1600.0, riemann=_abi.DG_RIEMANN_ROE,
+                 precision=precision, source=_abi.DG_SOURCE_MMS_LAMB_VECTOR, dt=0.005, t_final=0.100001,
+                 n_steps=10000)
+    return mesh, cfg, problems.mms_lamb_vector_state(mesh.x, 0.0)
+
+
+# Golden of Solver/test/NavierStokes/LambVector/SETUP/ProblemFile.f90:753-756 (tol 1e-7).
+LAMB_VECTOR_L2 = 3.4755642143319206E-05
+# Gauss weights N=5 tabulated in that test (ProblemFile.f90:587-594).
+WG5 = np.array([0.17132449237917019, 0.36076157304813833, 0.46791393457269093, 0.46791393457269093,
+                0.36076157304813833, 0.17132449237917019])
+
+
+def lamb_vector_l2_error(mesh, q, t):
+    """sqrt(sum_e sum_ijk w_i w_j w_k J |Q_exact - Q|^2 / K) (ProblemFile.f90:637-750)."""
+    qe = problems.mms_lamb_vector_state(mesh.x, t)
+    w3 = (WG5[None, None, :] * WG5[None, :, None] * WG5[:, None, None]).reshape(-1)
+    J = mesh.jacobian.reshape(mesh.n_elements, -1)
+    d2 = np.sum(((q - qe).reshape(mesh.n_elements, -1, 5)) ** 2, axis=2)
+    return float(np.sqrt(np.sum(J * w3[None, :] * d2) / mesh.n_elements))
+
+
+def ftassert_equal(expected, actual, tol):
+    """FTAssertEqual of two reals (ftobject/Comparisons.f90:238-255): relative tolerance, absolute
+    below tol."""
+    x, y = float(expected), float(actual)
+    lim = tol if x <= tol else tol * max(abs(x), abs(y))
+    return abs(x - y) <= lim
+
+
 def ftassert_close(expected, actual, tol=1e-11):
     """FTAssertEqual on (value + 1) as the reference test does (ftobject/Comparisons.f90:238-255)."""
     x, y = np.asarray(expected) + 1.0, np.asarray(actual) + 1.0

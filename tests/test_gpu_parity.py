@@ -269,3 +269,40 @@ def test_solution_file_restart_continues_the_run(tmp_path):
     assert hd.file_type == 3 and hd.node_type == 1 and hd.n_elements == mesh.n_elements
     q, grad = solution_file.read(path, mesh.order, gradients=True)
     assert np.all(np.isfinite(grad)) and np.abs(grad).max() > 0
+
+
+@pytest.mark.parametrize("precision", [_abi.DG_PRECISION_FP64, _abi.DG_PRECISION_MIXED])
+def test_lamb_vector_case_on_gpu(precision):
+    """NavierStokes/LambVector on the GPU (21 fixed steps to t=0.100001, manufactured source): the
+    plain form reaches the reference's L2-error golden (ProblemFile.f90:753-756, tol 1e-7
+    relative) and matches the oracle's state to 1e-12; the mixed form is within 1e-6 of it."""
+    mesh, cfg, q0 = cases.lamb_vector_case(precision=precision)
+    g = NavierStokesDG(mesh, cfg)
+    g.set_state(q0)
+    rep = g.integrate_in_time(t0=0.0)
+    assert rep.iterations == 21 and abs(rep.time - 0.100001) < 1e-15
+    o = oracle.Oracle(mesh, cfg.physics(), cfg.options())
+    o.set_state(q0)
+    t = 0.0
+    for _ in range(20):
+        o.rk3_step(t, 0.005)
+        t += 0.005
+    o.rk3_step(t, 0.100001 - t)
+    err = rel_l2(g.Q, o.get(0), cases.quadrature_weights(mesh))
+    if precision == _abi.DG_PRECISION_FP64:
+        l2 = cases.lamb_vector_l2_error(mesh, g.Q, rep.time)
+        assert cases.ftassert_equal(cases.LAMB_VECTOR_L2, l2, 1e-7), l2 - cases.LAMB_VECTOR_L2
+        assert np.all(err <= STATE_TOL), err
+    else:
+        assert np.all(err <= MIXED_TOL), err
+
+
+def test_lamb_vector_source_on_per_element_orders():
+    """The LambVector source on the variable-order kernels (orders 2..5 per element and direction)."""
+    orders = cases.random_orders(27, 2, 5, 7)
+    mesh = cases.HexMesh.box(3, [0, 0, 0], [cases.TWO_PI] * 3, orders, node_type=_abi.DG_NODES_GAUSS)
+    cfg = cases.Config(order=5, nodes=_abi.DG_NODES_GAUSS, mach=0.08, reynolds=1600.0, riemann=_abi.DG_RIEMANN_ROE,
+                       source=_abi.DG_SOURCE_MMS_LAMB_VECTOR)
+    q0 = cases.problems.mms_lamb_vector_state(mesh.x, 0.0)
+    _check_rhs(mesh, cfg, q0, t=0.03)
+    _check_steps(mesh, cfg, q0, 5, 0.005)

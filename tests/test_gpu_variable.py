@@ -253,3 +253,29 @@ def test_anisotropic_more_solvers(riemann, averaging):
     cfg = dataclasses.replace(cfg, averaging=averaging)
     _check_rhs(mesh, cfg, q0)
     _check_steps(mesh, cfg, q0, steps=2, dt=2e-3)
+
+
+def test_batch_save_and_restart_one_case(tmp_path):
+    """A case of a batch saved to a solution file and loaded into another batch: that case continues
+    bit for bit; a file written from the anisotropic case reads back with its per-element orders."""
+    cs = _batch_cases()
+    b = CaseBatch([m for m, _, _ in cs], [c for _, c, _ in cs])
+    b.set_state([q for _, _, q in cs])
+    dts = b.max_time_steps(0.4, 0.4)
+    b.set_clock(np.zeros(3), dts)
+    b.run_steps(2)
+    t, _ = b.clock()
+    path = tmp_path / "case1.hsol"
+    b.save_solution(1, path, iteration=2, time=t[1])
+    from horses3d_gb300 import solution_file
+
+    q_file = solution_file.read(path, cs[1][0].order)
+    assert np.array_equal(q_file.reshape(-1), b.get()[1])
+    b.run_steps(2)
+    c2 = CaseBatch([m for m, _, _ in cs], [c for _, c, _ in cs])
+    c2.set_state([q for _, _, q in cs])
+    it, t1 = c2.load_solution(1, path)
+    assert it == 2 and t1 == t[1]
+    c2.set_clock(np.array([0.0, t1, 0.0]), dts)
+    c2.run_steps(2)
+    assert np.array_equal(c2.get()[1], b.get()[1])

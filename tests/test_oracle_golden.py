@@ -10,6 +10,7 @@ from horses3d_gb300 import _abi
 from horses3d_gb300.mesh import HexMesh, nodal_storage
 
 REF_MESH = Path("/root/reference/Solver/test/TestMeshes/UnitCube4x4.mesh")
+TGV8_MESH = Path("/root/reference/Solver/test/TestMeshes/TaylorGreen8.mesh")
 
 
 def _run_convergence(mesh, cfg):
@@ -53,6 +54,46 @@ def test_convergence_goldens_reference_mesh_file():
     assert cases.ftassert_close(cases.CONVERGENCE_RESIDUALS, res)
     assert cases.ftassert_close(cases.CONVERGENCE_Q_ERRORS, err)
     assert cases.ftassert_close(cases.CONVERGENCE_QDOT_ERRORS, qerr)
+
+
+def run_lamb_vector(mesh, cfg, q0, rk3_step, get_state):
+    """IntegrateInTime with a fixed dt and CorrectDt's final-time clip: 20 steps of 0.005 and one
+    of 1e-6 to t=0.100001."""
+    t, it = 0.0, 0
+    eps = np.finfo(float).eps
+    while it < cfg.n_steps:
+        dt = cfg.dt if t + cfg.dt <= cfg.t_final else cfg.t_final - t
+        rk3_step(t, dt)
+        t += dt
+        it += 1
+        if t >= cfg.t_final or abs(t - cfg.t_final) <= 100 * eps:
+            break
+    return it, t, cases.lamb_vector_l2_error(mesh, get_state(), t)
+
+
+def _lamb_vector_on_oracle(mesh):
+    _, cfg, _ = cases.lamb_vector_case()
+    o = oracle.Oracle(mesh, cfg.physics(), cfg.options())
+    o.set_state(cases.problems.mms_lamb_vector_state(mesh.x, 0.0))
+    return run_lamb_vector(mesh, cfg, None, o.rk3_step, lambda: o.get(0))
+
+
+def test_lamb_vector_golden_generated_mesh():
+    """NavierStokes/LambVector: the L2 error of the solution at t=0.100001 against the manufactured
+    state (ProblemFile.f90:753-756, tol 1e-7 relative)."""
+    mesh, _, _ = cases.lamb_vector_case()
+    it, t, err = _lamb_vector_on_oracle(mesh)
+    assert it == 21 and abs(t - 0.100001) < 1e-15
+    assert cases.ftassert_equal(cases.LAMB_VECTOR_L2, err, 1e-7), err - cases.LAMB_VECTOR_L2
+
+
+@pytest.mark.skipif(not TGV8_MESH.exists(), reason="reference mesh file not mounted")
+def test_lamb_vector_golden_reference_mesh_file():
+    mesh = HexMesh.from_specmesh(TGV8_MESH, 5, node_type=_abi.DG_NODES_GAUSS,
+                                 periodic="front:back,bottom:top,left:right")
+    it, t, err = _lamb_vector_on_oracle(mesh)
+    assert it == 21
+    assert cases.ftassert_equal(cases.LAMB_VECTOR_L2, err, 1e-7), err - cases.LAMB_VECTOR_L2
 
 
 def test_nodal_storage_quadrature_and_derivative():
