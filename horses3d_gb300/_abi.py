@@ -28,7 +28,10 @@ DG_FAULT_NONE, DG_FAULT_TMA_WAIT = 0, 1
 DG_NODES_GAUSS, DG_NODES_GAUSS_LOBATTO = 0, 1
 DG_INVISCID_STANDARD, DG_INVISCID_SPLIT = 0, 1
 DG_RIEMANN_ROE, DG_RIEMANN_LXF, DG_RIEMANN_CENTRAL, DG_RIEMANN_RUSANOV = 0, 1, 2, 3
+DG_RIEMANN_STD_ROE, DG_RIEMANN_ROE_PIKE, DG_RIEMANN_LOW_DISS_ROE = 4, 5, 6
+DG_RIEMANN_MATRIX_DISS, DG_RIEMANN_VISCOUS_NS, DG_RIEMANN_U_DISS = 7, 8, 9
 DG_AVG_STANDARD, DG_AVG_PIROZZOLI, DG_AVG_DUCROS, DG_AVG_MORINISHI, DG_AVG_KENNEDY_GRUBER = 0, 1, 2, 3, 4
+DG_AVG_ENTROPY_CONSERVING, DG_AVG_CHANDRASEKAR = 5, 6
 DG_PRECISION_FP64, DG_PRECISION_MIXED = 0, 1
 DG_SOURCE_NONE, DG_SOURCE_MMS_CONVERGENCE, DG_SOURCE_MMS_LAMB_VECTOR = 0, 1, 2
 DG_FIELD_Q, DG_FIELD_QDOT, DG_FIELD_G, DG_FIELD_UX, DG_FIELD_UY, DG_FIELD_UZ = range(6)

@@ -68,9 +68,13 @@ class Config:
 
 # RiemannSolvers_NS.f90:5-40 keyword values
 _RIEMANN = {"roe": _abi.DG_RIEMANN_ROE, "lax-friedrichs": _abi.DG_RIEMANN_LXF, "central": _abi.DG_RIEMANN_CENTRAL,
-            "rusanov": _abi.DG_RIEMANN_RUSANOV}
+            "rusanov": _abi.DG_RIEMANN_RUSANOV, "standard roe": _abi.DG_RIEMANN_STD_ROE,
+            "roe-pike": _abi.DG_RIEMANN_ROE_PIKE, "low dissipation roe": _abi.DG_RIEMANN_LOW_DISS_ROE,
+            "matrix dissipation": _abi.DG_RIEMANN_MATRIX_DISS, "viscous ns": _abi.DG_RIEMANN_VISCOUS_NS,
+            "u-diss": _abi.DG_RIEMANN_U_DISS}
 _AVERAGING = {"standard": _abi.DG_AVG_STANDARD, "pirozzoli": _abi.DG_AVG_PIROZZOLI, "ducros": _abi.DG_AVG_DUCROS,
-              "morinishi": _abi.DG_AVG_MORINISHI, "kennedy-gruber": _abi.DG_AVG_KENNEDY_GRUBER}
+              "morinishi": _abi.DG_AVG_MORINISHI, "kennedy-gruber": _abi.DG_AVG_KENNEDY_GRUBER,
+              "entropy conserving": _abi.DG_AVG_ENTROPY_CONSERVING, "chandrasekar": _abi.DG_AVG_CHANDRASEKAR}
 
 
 def _value(v: str) -> str:

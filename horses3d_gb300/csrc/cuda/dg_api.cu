@@ -245,8 +245,8 @@ int validate(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op) 
         return h3d::fail(DG_ERR_UNSUPPORTED, "inviscid discretization");
     if (op->inviscid == DG_INVISCID_SPLIT && m->node_type != DG_NODES_GAUSS_LOBATTO)
         return h3d::fail(DG_ERR_INVALID, "the split form needs Gauss-Lobatto nodes");
-    if (op->riemann < DG_RIEMANN_ROE || op->riemann > DG_RIEMANN_RUSANOV) return h3d::fail(DG_ERR_UNSUPPORTED, "riemann solver");
-    if (op->averaging < DG_AVG_STANDARD || op->averaging > DG_AVG_KENNEDY_GRUBER)
+    if (op->riemann < DG_RIEMANN_ROE || op->riemann > DG_RIEMANN_U_DISS) return h3d::fail(DG_ERR_UNSUPPORTED, "riemann solver");
+    if (op->averaging < DG_AVG_STANDARD || op->averaging > DG_AVG_CHANDRASEKAR)
         return h3d::fail(DG_ERR_UNSUPPORTED, "averaging");
     if (op->precision != DG_PRECISION_FP64 && op->precision != DG_PRECISION_MIXED)
         return h3d::fail(DG_ERR_UNSUPPORTED, "precision");
@@ -299,6 +299,7 @@ int dg_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op,
     pc.S_div_TRef = (198.6 * 5.0 / 9.0) / TRef;
     pc.TReNorm = TRef / TRef;
     pc.lambda_stab = op->riemann == DG_RIEMANN_CENTRAL ? 0.0 : op->lambda_stab;  // SetRiemannSolver
+    pc.vns_kappa = 1.0 / (3.0 / 4.0 * pc.gm1 * (ph->mach * ph->mach));              // FluidData_NS.f90:173-181
     pc.riemann = op->riemann;
     pc.averaging = op->averaging;
     pc.inviscid = op->inviscid;

@@ -612,7 +612,7 @@ __global__ void __launch_bounds__(128) k_flux(Args<R> a) {
     } else {
         const R t1[3] = {a.ft1[gid], a.ft1[nfp + gid], a.ft1[2 * nfp + gid]};
         const R t2[3] = {a.ft2[gid], a.ft2[nfp + gid], a.ft2[2 * nfp + gid]};
-        lxf_flux(a.ph, QL, QR, n, t1, t2, inv);
+        riemann_flux(a.ph, QL, QR, n, t1, t2, inv);  // the solvers that need the tangents
     }
     R vL[5] = {0, 0, 0, 0, 0}, vR[5] = {0, 0, 0, 0, 0};
     if (a.ph.ns) {

@@ -9,6 +9,7 @@ namespace dg {
 // Derived physics constants (PhysicsStorage_NS.f90:186-429), host-filled.
 struct PhysConst {
     double gamma, gm1, gammaM2, mu, kappa, mu_to_kappa, S_div_TRef, TReNorm;
+    double vns_kappa;  // conductivity of the viscous-NS Riemann solver, 1 / (3/4 (gamma-1) M^2)
     double lambda_stab;
     int ns, riemann, averaging, inviscid, source;
 };
@@ -23,6 +24,7 @@ template <typename R>
 struct PhysR {
     R gamma, gm1, gammaM2, mu, kappa, mu_to_kappa, S_div_TRef, TReNorm, lambda_stab;
     R g_over_gm1, gp1_over_4, gm1_gammaM2;
+    R gp1_over_2, gm1_over_2, inv_gamma, inv_gm1, gm1_over_2g, vns_kappa;
     R e_ref, p_ref, h_ref;
     int ns, riemann, averaging;
 };
@@ -36,6 +38,14 @@ PhysR<R> make_phys(const PhysConst& c) {
     p.g_over_gm1 = R(c.gamma / (c.gamma - 1.0));
     p.gp1_over_4 = R((c.gamma + 1.0) / 4.0);
     p.gm1_gammaM2 = R(c.gm1 * c.gammaM2);
+    // PhysicsStorage_NS.f90:115-133 (gammaPlus1Div2, gammaMinus1Div2, InvGamma, InvGammaMinus1,
+    // gammaMinus1Div2g)
+    p.gp1_over_2 = R((c.gamma + 1.0) / 2.0);
+    p.gm1_over_2 = R(c.gm1 / 2.0);
+    p.inv_gamma = R(1.0 / c.gamma);
+    p.inv_gm1 = R(1.0 / c.gm1);
+    p.gm1_over_2g = R(c.gm1 / (2.0 * c.gamma));
+    p.vns_kappa = R(c.vns_kappa);
     p.e_ref = R(0); p.p_ref = R(0); p.h_ref = R(0);
     p.ns = c.ns; p.riemann = c.riemann; p.averaging = c.averaging;
     return p;
@@ -51,6 +61,22 @@ void set_reference_energy(PhysR<R>& p, double gm1, double e_ref) {
 template <typename R> __device__ __forceinline__ R dsqrt(R x);
 template <> __device__ __forceinline__ double dsqrt<double>(double x) { return sqrt(x); }
 template <> __device__ __forceinline__ float dsqrt<float>(float x) { return sqrtf(x); }
+template <typename R> __device__ __forceinline__ R dlog(R x);
+template <> __device__ __forceinline__ double dlog<double>(double x) { return log(x); }
+template <> __device__ __forceinline__ float dlog<float>(float x) { return logf(x); }
+
+// Utilities.f90:269-301 logarithmicMean (Ismail and Roe): (aL - aR) / (ln aL - ln aR), with a
+// series in ((xi - 1) / (xi + 1))^2 near xi = aL / aR = 1.
+template <typename R>
+__device__ __forceinline__ R log_mean(R aL, R aR) {
+    const R xi = aL / aR;
+    const R f = (xi - R(1)) / (xi + R(1));
+    const R u = f * f;
+    R FF;
+    if (u < R(0.01)) FF = R(1) + (R(1) / R(3)) * u + (R(1) / R(5)) * (u * u) + (R(1) / R(7)) * ((u * u) * u);
+    else FF = dlog(xi) / (R(2) * f);
+    return R(0.5) * (aL + aR) / FF;
+}
 
 // VariableConversion_NS.f90:44-57,147-186: pressure, temperature, Sutherland's law.
 template <typename R>
@@ -167,15 +193,64 @@ __device__ __forceinline__ void roe_flux(const PhysR<R>& p, const R* QL, const R
     }
 }
 
+// The Ismail-Roe (entropy conserving) and Chandrasekar mean states of two states: density,
+// velocity, ABSOLUTE pressure and total enthalpy. The pressures pL, pR given are the absolute ones.
+// EntropyConservingAverage (RiemannSolvers_NS.f90:1964-2026, z-sums; the two-point flux :2439-2558
+// uses z-means, so `half` selects 1/2 zSum), ChandrasekarAverage (:2028-2077, :2560-2641).
+template <typename R>
+__device__ __forceinline__ void log_mean_state(const PhysR<R>& p, bool entropy_conserving, R rhoL, R rhoR, R uL, R uR,
+                                               R vL, R vR, R wL, R wR, R pL, R pR, R& rho, R& u, R& v, R& w,
+                                               R& pm, R& h, bool zmean) {
+    if (entropy_conserving) {
+        const R z5L = dsqrt(rhoL * pL), z5R = dsqrt(rhoR * pR);
+        const R z1L = rhoL / z5L, z1R = rhoR / z5R;
+        R s1, s2, s3, s4, s5;
+        if (zmean) {
+            s1 = R(0.5) * (z1L + z1R); s2 = R(0.5) * (z1L * uL + z1R * uR); s3 = R(0.5) * (z1L * vL + z1R * vR);
+            s4 = R(0.5) * (z1L * wL + z1R * wR); s5 = R(0.5) * (z5L + z5R);
+        } else {
+            s1 = z1L + z1R; s2 = z1L * uL + z1R * uR; s3 = z1L * vL + z1R * vR; s4 = z1L * wL + z1R * wR;
+            s5 = z5L + z5R;
+        }
+        const R inv1 = R(1) / s1;
+        const R z1Log = log_mean(z1L, z1R), z5Log = log_mean(z5L, z5R);
+        rho = zmean ? s1 * z5Log : R(0.5) * s1 * z5Log;
+        u = s2 * inv1; v = s3 * inv1; w = s4 * inv1; pm = s5 * inv1;
+        const R p2 = (p.gp1_over_2 * z5Log / z1Log + p.gm1_over_2 * pm) * p.inv_gamma;
+        h = p.g_over_gm1 * p2 / rho + R(0.5) * (u * u + v * v + w * w);
+    } else {
+        const R betaL = R(0.5) * rhoL / pL, betaR = R(0.5) * rhoR / pR;
+        const R betaLog = log_mean(betaL, betaR);
+        rho = log_mean(rhoL, rhoR);
+        u = R(0.5) * (uL + uR); v = R(0.5) * (vL + vR); w = R(0.5) * (wL + wR);
+        pm = R(0.5) * (rhoL + rhoR) / (betaL + betaR);
+        h = R(0.5) / (betaLog * p.gm1) - R(0.5) * (R(0.5) * ((uL * uL + vL * vL + wL * wL) + (uR * uR + vR * vR + wR * wR))) +
+            pm / rho + u * u + v * v + w * w;
+    }
+}
+
 // Averaged states of the face-normal frame (L, R = rho, rho u_n, rho u_t1, rho u_t2, E with the mixed
 // form's E'): StandardAverage (RiemannSolvers_NS.f90:1784-1819), DucrosAverage (:1821-1848),
-// MorinishiAverage (:1850-1886), KennedyGruberAverage (:1888-1925), PirozzoliAverage (:1927-1962).
+// MorinishiAverage (:1850-1886), KennedyGruberAverage (:1888-1925), PirozzoliAverage (:1927-1962),
+// EntropyConservingAverage (:1964-2026), ChandrasekarAverage (:2028-2077).
 // Absolute energies and pressures are E' + e_ref, p' + p_ref; momentum fluxes carry p' only.
 template <typename R>
 __device__ __forceinline__ void averaged_states(const PhysR<R>& p, const R* L, const R* Rt, R pL, R pR, R iL, R iR,
                                                 R* f) {
     const R uL = iL * L[1], uR = iR * Rt[1], vL = iL * L[2], vR = iR * Rt[2], wL = iL * L[3], wR = iR * Rt[3];
     switch (p.averaging) {
+        case 5:
+        case 6: {  // entropy conserving, Chandrasekar
+            R rho, u, v, w, pm, h;
+            log_mean_state(p, p.averaging == 5, L[0], Rt[0], uL, uR, vL, vR, wL, wR, pL + p.p_ref, pR + p.p_ref, rho,
+                           u, v, w, pm, h, false);
+            f[0] = rho * u;
+            f[1] = rho * u * u + (pm - p.p_ref);
+            f[2] = rho * u * v;
+            f[3] = rho * u * w;
+            f[4] = rho * u * h;
+            break;
+        }
         case 0: {  // standard
             f[0] = R(0.5) * (L[1] + Rt[1]);
             f[1] = R(0.5) * (L[1] * uL + Rt[1] * uR + pL + pR);
@@ -246,7 +321,9 @@ __device__ __forceinline__ void lxf_flux(const PhysR<R>& p, const R* QL, const R
     R f[5];
     averaged_states(p, Lr, Rr, pL, pR, iL, iR, f);
     if (p.riemann != 2) {  // central fluxes carry no dissipation
-        const R aL = dsqrt(p.gamma * (pL + p.p_ref) * iL), aR = dsqrt(p.gamma * (pR + p.p_ref) * iR);
+        // u-diss (RiemannSolvers_NS.f90:1336-1425) drops the sound speeds
+        const R aL = p.riemann == 9 ? R(0) : dsqrt(p.gamma * (pL + p.p_ref) * iL);
+        const R aR = p.riemann == 9 ? R(0) : dsqrt(p.gamma * (pR + p.p_ref) * iR);
         const R lL = fabs(ruL * iL) + aL, lR = fabs(ruR * iR) + aR;
         const R lambda = lL > lR ? lL : lR;
         const R ls = p.lambda_stab * (R(0.5) * lambda);
@@ -291,19 +368,293 @@ __device__ __forceinline__ void rusanov_flux(const PhysR<R>& p, const R* QL, con
     for (int v = 0; v < 5; ++v) flux[v] = (f[v] - smax * (QR[v] - QL[v])) / R(2);
 }
 
-// The interface flux of the chosen solver (Roe, LxF / central with the chosen average, Rusanov).
+template <typename R>
+__device__ __forceinline__ void to_face_frame(const R* Q, const R* n, const R* t1, const R* t2, R* r) {
+    r[0] = Q[0];
+    r[1] = Q[1] * n[0] + Q[2] * n[1] + Q[3] * n[2];
+    r[2] = Q[1] * t1[0] + Q[2] * t1[1] + Q[3] * t1[2];
+    r[3] = Q[1] * t2[0] + Q[2] * t2[1] + Q[3] * t2[2];
+    r[4] = Q[4];
+}
+template <typename R>
+__device__ __forceinline__ void from_face_frame(const R* f, const R* n, const R* t1, const R* t2, R* flux) {
+    flux[0] = f[0];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) flux[1 + c] = n[c] * f[1] + t1[c] * f[2] + t2[c] * f[3];
+    flux[4] = f[4];
+}
+
+// Van Leer's modification of Harten's entropy fix of an acoustic wave speed (RiemannSolvers_NS.f90:
+// 507-530): sL, sR are the one-sided speeds u -/+ a.
+template <typename R>
+__device__ __forceinline__ R entropy_fix(R lambda, R sL, R sR) {
+    const R d = sR - sL;
+    const R dl = d > R(0) ? d : R(0);
+    const R al = fabs(lambda);
+    if (al >= R(2) * dl) return al;
+    return lambda * lambda / (R(4) * dl) + dl;
+}
+
+// average - lambda_stab sum_i 1/2 alpha_i |lambda_i| K_i with the Roe eigenvectors K of (u, v, w, H, a)
+// in the face frame; the Pirozzoli and Kennedy-Gruber averages take lambda_1 = lambda_5 (Winters et
+// al., as the reference does).
+template <typename R>
+__device__ __forceinline__ void roe_stabilised(const PhysR<R>& p, const R* L, const R* Rt, R pL, R pR, R iL, R iR, R u,
+                                               R v, R w, R V2, R H, R a, const R* alpha, R* lambda, R* f) {
+    averaged_states(p, L, Rt, pL, pR, iL, iR, f);
+    if (p.averaging == 1 || p.averaging == 4) lambda[0] = lambda[4];
+    const R K[5][5] = {{R(1), u - a, v, w, H - u * a},
+                       {R(1), u, v, w, R(0.5) * V2},
+                       {R(0), R(0), R(1), R(0), v},
+                       {R(0), R(0), R(0), R(1), w},
+                       {R(1), u + a, v, w, H + u * a}};
+    R stab[5] = {R(0), R(0), R(0), R(0), R(0)};
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        const R c = R(0.5) * alpha[i] * fabs(lambda[i]);
+#pragma unroll
+        for (int q = 0; q < 5; ++q) stab[q] = stab[q] + c * K[i][q];
+    }
+#pragma unroll
+    for (int q = 0; q < 5; ++q) f[q] = f[q] - p.lambda_stab * stab[q];
+}
+
+// StdRoeRiemannSolver (RiemannSolvers_NS.f90:430-576) and RoePikeRiemannSolver (:721-861): the chosen
+// average plus the Roe dissipation with getRoeVariables' averages (VariableConversion_NS.f90:323-365);
+// the wave strengths are the projections of the jump (standard) or of the primitive jumps (Roe-Pike).
+template <typename R>
+__device__ __forceinline__ void std_roe_flux(const PhysR<R>& p, bool pike, const R* QL, const R* QR, const R* n,
+                                             const R* t1, const R* t2, R* flux) {
+    R L[5], Rt[5];
+    to_face_frame(QL, n, t1, t2, L);
+    to_face_frame(QR, n, t1, t2, Rt);
+    // getPrimitiveVariables (VariableConversion_NS.f90:266-294)
+    const R iL = R(1) / L[0], iR = R(1) / Rt[0];
+    const R uL = L[1] * iL, vL = L[2] * iL, wL = L[3] * iL, uR = Rt[1] * iR, vR = Rt[2] * iR, wR = Rt[3] * iR;
+    const R pL = p.gm1 * (L[4] - R(0.5) * (uL * L[1] + vL * L[2] + wL * L[3]));
+    const R pR = p.gm1 * (Rt[4] - R(0.5) * (uR * Rt[1] + vR * Rt[2] + wR * Rt[3]));
+    const R aL = dsqrt(p.gamma * (pL + p.p_ref) * iL), aR = dsqrt(p.gamma * (pR + p.p_ref) * iR);
+    const R sL = dsqrt(L[0]), sR = dsqrt(Rt[0]);
+    const R inv = R(1) / (sL + sR);
+    const R HL = (pL + L[4] + p.h_ref) * iL, HR = (pR + Rt[4] + p.h_ref) * iR;
+    const R rho = sL * sR;
+    const R u = (sL * uL + sR * uR) * inv, v = (sL * vL + sR * vR) * inv, w = (sL * wL + sR * wR) * inv;
+    const R H = (sL * HL + sR * HR) * inv;
+    const R V2 = u * u + v * v + w * w;
+    const R a = dsqrt(p.gm1 * (H - R(0.5) * V2));
+    R lambda[5] = {u - a, u, u, u, u + a};
+    R alpha[5];
+    if (!pike) {
+        R dQ[5];
+#pragma unroll
+        for (int q = 0; q < 5; ++q) dQ[q] = Rt[q] - L[q];
+        alpha[2] = dQ[2] - v * dQ[0];
+        alpha[3] = dQ[3] - w * dQ[0];
+        dQ[4] = dQ[4] - alpha[2] * v - alpha[3] * w;
+        alpha[1] = p.gm1 * (dQ[0] * (H - u * u) + u * dQ[1] - dQ[4]) / (a * a);
+        alpha[0] = R(0.5) * (dQ[0] * lambda[4] - dQ[1] - a * alpha[1]) / a;
+        alpha[4] = dQ[0] - alpha[0] - alpha[1];
+    } else {
+        const R dp = pR - pL, du = uR - uL;
+        alpha[0] = (dp - rho * a * du) / (R(2) * a * a);
+        alpha[1] = (Rt[0] - L[0]) - dp / (a * a);
+        alpha[2] = rho * (vR - vL);
+        alpha[3] = rho * (wR - wL);
+        alpha[4] = (dp + rho * a * du) / (R(2) * a * a);
+    }
+    lambda[0] = entropy_fix(lambda[0], uL - aL, uR - aR);
+    lambda[4] = entropy_fix(lambda[4], uL + aL, uR + aR);
+    R f[5];
+    roe_stabilised(p, L, Rt, pL, pR, iL, iR, u, v, w, V2, H, a, alpha, lambda, f);
+    from_face_frame(f, n, t1, t2, flux);
+}
+
+// Face-frame states and Roe-Pike averages written with 1/sqrt(rho), as LowDissipationRoeRiemannSolver
+// (:863-1058) and ViscousNSRiemannSolver (:1060-1247) form them.
+template <typename R>
+struct RoePike {
+    R L[5], Rt[5], iL, iR, uL, vL, wL, uR, vR, wR, pL, pR, aL, aR, rho, u, v, w, H, V2, a;
+};
+template <typename R>
+__device__ __forceinline__ void roe_pike_state(const PhysR<R>& p, const R* QL, const R* QR, const R* n, const R* t1,
+                                               const R* t2, RoePike<R>& s) {
+    to_face_frame(QL, n, t1, t2, s.L);
+    to_face_frame(QR, n, t1, t2, s.Rt);
+    s.iL = R(1) / s.L[0]; s.iR = R(1) / s.Rt[0];
+    const R sL = dsqrt(s.L[0]), sR = dsqrt(s.Rt[0]);
+    const R isL = R(1) / sL, isR = R(1) / sR;
+    const R inv = R(1) / (sL + sR);
+    s.uL = s.L[1] * s.iL; s.uR = s.Rt[1] * s.iR;
+    s.vL = s.L[2] * s.iL; s.vR = s.Rt[2] * s.iR;
+    s.wL = s.L[3] * s.iL; s.wR = s.Rt[3] * s.iR;
+    const R rV2L = (s.uL * s.uL + s.vL * s.vL + s.wL * s.wL) * s.L[0];
+    const R rV2R = (s.uR * s.uR + s.vR * s.vR + s.wR * s.wR) * s.Rt[0];
+    const R rHL = p.gamma * s.L[4] - R(0.5) * p.gm1 * rV2L + p.h_ref;
+    const R rHR = p.gamma * s.Rt[4] - R(0.5) * p.gm1 * rV2R + p.h_ref;
+    s.pL = p.gm1 * (s.L[4] - R(0.5) * rV2L);
+    s.pR = p.gm1 * (s.Rt[4] - R(0.5) * rV2R);
+    s.aL = dsqrt(p.gamma * (s.pL + p.p_ref) * s.iL);
+    s.aR = dsqrt(p.gamma * (s.pR + p.p_ref) * s.iR);
+    s.rho = sL * sR;
+    s.u = (isL * s.L[1] + isR * s.Rt[1]) * inv;
+    s.v = (isL * s.L[2] + isR * s.Rt[2]) * inv;
+    s.w = (isL * s.L[3] + isR * s.Rt[3]) * inv;
+    s.H = (isL * rHL + isR * rHR) * inv;
+    s.V2 = s.u * s.u + s.v * s.v + s.w * s.w;
+    s.a = dsqrt(p.gm1 * (s.H - R(0.5) * s.V2));
+}
+
+// LowDissipationRoeRiemannSolver (:863-1058): Roe-Pike wave strengths with the velocity jumps scaled
+// by z = min(1, max(M_L, M_R)) (L2Roe).
+template <typename R>
+__device__ __forceinline__ void low_diss_roe_flux(const PhysR<R>& p, const R* QL, const R* QR, const R* n, const R* t1,
+                                                  const R* t2, R* flux) {
+    RoePike<R> s;
+    roe_pike_state(p, QL, QR, n, t1, t2, s);
+    const R u = s.u, a = s.a, rho = s.rho;
+    R lambda[5] = {u - a, u, u, u, u + a};
+    const R ML = fabs(s.uL) / s.aL, MR = fabs(s.uR) / s.aR;
+    const R mx = ML > MR ? ML : MR;
+    const R z = mx < R(1) ? mx : R(1);
+    const R du = z * (s.uR - s.uL), dv = z * (s.vR - s.vL), dw = z * (s.wR - s.wL), dp = s.pR - s.pL;
+    R alpha[5];
+    alpha[0] = (dp - rho * a * du) / (R(2) * a * a);
+    alpha[1] = (s.Rt[0] - s.L[0]) - dp / (a * a);
+    alpha[2] = rho * dv;
+    alpha[3] = rho * dw;
+    alpha[4] = (dp + rho * a * du) / (R(2) * a * a);
+    lambda[0] = entropy_fix(lambda[0], s.uL - s.aL, s.uR - s.aR);
+    lambda[4] = entropy_fix(lambda[4], s.uL + s.aL, s.uR + s.aR);
+    R f[5];
+    roe_stabilised(p, s.L, s.Rt, s.pL, s.pR, s.iL, s.iR, s.u, s.v, s.w, s.V2, s.H, a, alpha, lambda, f);
+    from_face_frame(f, n, t1, t2, flux);
+}
+
+// ViscousNSRiemannSolver (:1060-1247): the average plus a dissipation shaped like the NS viscous
+// terms of the velocity and temperature jumps, times the largest wave speed, added in the
+// Cartesian frame (conductivity with Pr = 3/4, FluidData_NS.f90:173-181).
+template <typename R>
+__device__ __forceinline__ void viscous_ns_flux(const PhysR<R>& p, const R* QL, const R* QR, const R* n, const R* t1,
+                                                const R* t2, R* flux) {
+    RoePike<R> s;
+    roe_pike_state(p, QL, QR, n, t1, t2, s);
+    R lambda[5] = {s.u - s.a, s.u, s.u, s.u, s.u + s.a};
+    lambda[0] = entropy_fix(lambda[0], s.uL - s.aL, s.uR - s.aR);
+    lambda[4] = entropy_fix(lambda[4], s.uL + s.aL, s.uR + s.aR);
+    R f[5];
+    averaged_states(p, s.L, s.Rt, s.pL, s.pR, s.iL, s.iR, f);
+    if (p.averaging == 1 || p.averaging == 4) lambda[0] = lambda[4];
+    const R uL = QL[1] / QL[0], uR = QR[1] / QR[0];
+    const R vL = QL[2] / QL[0], vR = QR[2] / QR[0];
+    const R wL = QL[3] / QL[0], wR = QR[3] / QR[0];
+    const R u = R(0.5) * (uL + uR), v = R(0.5) * (vL + vR), w = R(0.5) * (wL + wR);
+    const R du = uR - uL, dv = vR - vL, dw = wR - wL;
+    const R divV = du * n[0] + dv * n[1] + dw * n[2];
+    const R third = R(1) / R(3);
+    const R t11 = R(2) * du * n[0] - third * divV;
+    const R t22 = R(2) * dv * n[1] - third * divV;
+    const R t33 = R(2) * dw * n[2] - third * divV;
+    const R t12 = du * n[1] + dv * n[0];
+    const R t13 = du * n[2] + dw * n[0];
+    const R t23 = dv * n[2] + dw * n[1];
+    const R TL = (s.pL + p.p_ref) * p.gammaM2 / s.L[0], TR = (s.pR + p.p_ref) * p.gammaM2 / s.Rt[0];
+    R lmax = R(0);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) lmax = fabs(lambda[i]) > lmax ? fabs(lambda[i]) : lmax;
+    from_face_frame(f, n, t1, t2, flux);
+    R stab[5];
+    stab[0] = R(0);
+    stab[1] = lmax * (t11 * n[0] + t12 * n[1] + t13 * n[2]);
+    stab[2] = lmax * (t12 * n[0] + t22 * n[1] + t23 * n[2]);
+    stab[3] = lmax * (t13 * n[0] + t23 * n[1] + t33 * n[2]);
+    stab[4] = lmax * ((u * t11 + v * t12 + w * t13) * n[0] + (u * t12 + v * t22 + w * t23) * n[1] +
+                      (u * t13 + v * t23 + w * t33) * n[2] + p.vns_kappa * (TR - TL));
+#pragma unroll
+    for (int q = 0; q < 5; ++q) flux[q] = flux[q] - p.lambda_stab * stab[q];
+}
+
+// NSGradientVariables_ENTROPY (VariableConversion_NS.f90:211-237) with the absolute pressure.
+template <typename R>
+__device__ __forceinline__ void entropy_variables(const PhysR<R>& p, const R* Q, R* U) {
+    const R irho = R(1) / Q[0];
+    const R rV2 = (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) * irho;
+    const R pr = p.gm1 * (Q[4] - R(0.5) * rV2) + p.p_ref;
+    const R ip = R(1) / pr;
+    U[0] = (p.gamma - (dlog(pr) - p.gamma * dlog(Q[0]))) * p.inv_gm1 - R(0.5) * rV2 * ip;
+    U[1] = Q[1] * ip;
+    U[2] = Q[2] * ip;
+    U[3] = Q[3] * ip;
+    U[4] = -Q[0] * ip;
+}
+
+// MatrixDissipationRiemannSolver (:578-719): the average minus the entropy-variable jump times
+// R |Lambda| T R^T / 2 of the logarithmic-mean states.
+template <typename R>
+__device__ __forceinline__ void matrix_diss_flux(const PhysR<R>& p, const R* QL, const R* QR, const R* n, const R* t1,
+                                                 const R* t2, R* flux) {
+    R L[5], Rt[5], EVL[5], EVR[5];
+    to_face_frame(QL, n, t1, t2, L);
+    to_face_frame(QR, n, t1, t2, Rt);
+    entropy_variables(p, L, EVL);
+    entropy_variables(p, Rt, EVR);
+    const R iL = R(1) / L[0], iR = R(1) / Rt[0];
+    const R uL = L[1] * iL, uR = Rt[1] * iR, vL = L[2] * iL, vR = Rt[2] * iR, wL = L[3] * iL, wR = Rt[3] * iR;
+    const R vtL = uL * uL + vL * vL + wL * wL, vtR = uR * uR + vR * vR + wR * wR;
+    const R pL = p.gm1 * (L[4] - R(0.5) * L[0] * vtL), pR = p.gm1 * (Rt[4] - R(0.5) * Rt[0] * vtR);
+    const R betaL = R(-0.5) * EVL[4], betaR = R(-0.5) * EVR[4];
+    const R betaLog = log_mean(betaL, betaR), rhoLog = log_mean(L[0], Rt[0]);
+    const R pMean = R(0.5) * (L[0] + Rt[0]) / (betaL + betaR);
+    const R a = dsqrt(p.gamma * pMean / rhoLog);
+    const R u = R(0.5) * (uL + uR), v = R(0.5) * (vL + vR), w = R(0.5) * (wL + wR);
+    const R V2 = R(2) * (u * u + v * v + w * w) - R(0.5) * (vtL + vtR);
+    const R h = R(0.5) * (p.g_over_gm1 / betaLog + V2);
+    R lambda[5] = {fabs(u - a), fabs(u), fabs(u), fabs(u), fabs(u + a)};
+    const R Rm[5][5] = {{R(1), u - a, v, w, h - u * a},
+                        {R(1), u, v, w, R(0.5) * V2},
+                        {R(0), R(0), R(1), R(0), v},
+                        {R(0), R(0), R(0), R(1), w},
+                        {R(1), u + a, v, w, h + u * a}};  // Rm[j][i] = R1(i, j)
+    const R T1 = R(0.5) * rhoLog * p.inv_gamma;
+    const R T[5] = {T1, R(2) * p.gm1_over_2g * rhoLog, pMean, pMean, T1};
+    R f[5];
+    averaged_states(p, L, Rt, pL, pR, iL, iR, f);
+    if (p.averaging == 1 || p.averaging == 4) lambda[0] = lambda[4];
+    R dEV[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) dEV[k] = EVR[k] - EVL[k];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        R st = R(0);
+#pragma unroll
+        for (int j = 0; j < 5; ++j)
+#pragma unroll
+            for (int k = 0; k < 5; ++k) st = st + R(0.5) * Rm[j][i] * lambda[j] * T[j] * Rm[j][k] * dEV[k];
+        f[i] = f[i] - p.lambda_stab * st;
+    }
+    from_face_frame(f, n, t1, t2, flux);
+}
+
+// The interface flux of the chosen solver: Roe (0), LxF (1), central (2), Rusanov (3), standard Roe
+// (4), Roe-Pike (5), low-dissipation Roe (6), matrix dissipation (7), viscous NS (8), u-diss (9).
 template <typename R>
 __device__ __forceinline__ void riemann_flux(const PhysR<R>& p, const R* QL, const R* QR, const R* n, const R* t1,
                                              const R* t2, R* flux) {
-    if (p.riemann == 0) roe_flux(p, QL, QR, n, flux);
-    else if (p.riemann == 3) rusanov_flux(p, QL, QR, n, flux);
-    else lxf_flux(p, QL, QR, n, t1, t2, flux);
+    switch (p.riemann) {
+        case 0: roe_flux(p, QL, QR, n, flux); break;
+        case 3: rusanov_flux(p, QL, QR, n, flux); break;
+        case 4: std_roe_flux(p, false, QL, QR, n, t1, t2, flux); break;
+        case 5: std_roe_flux(p, true, QL, QR, n, t1, t2, flux); break;
+        case 6: low_diss_roe_flux(p, QL, QR, n, t1, t2, flux); break;
+        case 7: matrix_diss_flux(p, QL, QR, n, t1, t2, flux); break;
+        case 8: viscous_ns_flux(p, QL, QR, n, t1, t2, flux); break;
+        default: lxf_flux(p, QL, QR, n, t1, t2, flux); break;
+    }
 }
 
 // Two-point fluxes of the split form, contracted with the averaged metric vector:
 // StandardDG_TwoPointFlux (RiemannSolvers_NS.f90:2085-2145), Morinishi_TwoPointFlux (:2147-2229),
 // Ducros_TwoPointFlux (:2231-2294), KennedyGruber_TwoPointFlux (:2296-2367), Pirozzoli_TwoPointFlux
-// (:2369-2437).
+// (:2369-2437), EntropyConserving_TwoPointFlux (:2439-2558), Chandrasekar_TwoPointFlux (:2560-2641).
 template <typename R>
 __device__ __forceinline__ void two_point_flux(const PhysR<R>& p, const R* QL, const R* QR, const R* JaL, const R* JaR,
                                                R* fs) {
@@ -369,6 +720,18 @@ __device__ __forceinline__ void two_point_flux(const PhysR<R>& p, const R* QL, c
             F[d][3] = ru * w + (d == 2 ? pp : R(0));
             F[d][4] = ru * e + pa * um[d];
         }
+    } else if (p.averaging == 5 || p.averaging == 6) {  // entropy conserving, Chandrasekar
+        R rho, u, v, w, pm, h;
+        log_mean_state(p, p.averaging == 5, QL[0], QR[0], uL, uR, vL, vR, wL, wR, pL + p.p_ref, pR + p.p_ref, rho, u, v,
+                       w, pm, h, true);
+        const R pp = pm - p.p_ref;
+        const R ru = rho * u, rv = rho * v, rw = rho * w;
+        fs[0] = ru * J0 + rv * J1 + rw * J2;
+        fs[1] = (ru * u + pp) * J0 + (rv * u) * J1 + (rw * u) * J2;
+        fs[2] = (ru * v) * J0 + (rv * v + pp) * J1 + (rw * v) * J2;
+        fs[3] = (ru * w) * J0 + (rv * w) * J1 + (rw * w + pp) * J2;
+        fs[4] = (ru * h) * J0 + (rv * h) * J1 + (rw * h) * J2;
+        return;
     } else {  // Pirozzoli
         const R rho = R(0.5) * (QL[0] + QR[0]), u = R(0.5) * (uL + uR), v = R(0.5) * (vL + vR), w = R(0.5) * (wL + wR);
         const R pp = R(0.5) * (pL + pR);

@@ -548,7 +548,7 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS) kv_face(VArgs<R> a)
             } else {
                 const R t1[3] = {a.ft1[3 * gp], a.ft1[3 * gp + 1], a.ft1[3 * gp + 2]};
                 const R t2[3] = {a.ft2[3 * gp], a.ft2[3 * gp + 1], a.ft2[3 * gp + 2]};
-                lxf_flux(ph, QL, QR, n, t1, t2, inv);
+                riemann_flux(ph, QL, QR, n, t1, t2, inv);  // the solvers that need the tangents
             }
             R visc[5] = {0, 0, 0, 0, 0};
             if (MODE == kFluxNS) {
@@ -714,7 +714,7 @@ __global__ void __launch_bounds__(128) kv_face_direct(VArgs<R> a) {
     } else {
         const R t1[3] = {a.ft1[3 * gpt], a.ft1[3 * gpt + 1], a.ft1[3 * gpt + 2]};
         const R t2[3] = {a.ft2[3 * gpt], a.ft2[3 * gpt + 1], a.ft2[3 * gpt + 2]};
-        lxf_flux(ph, QL, QR, n, t1, t2, inv);
+        riemann_flux(ph, QL, QR, n, t1, t2, inv);  // the solvers that need the tangents
     }
     R visc[5] = {0, 0, 0, 0, 0};
     if (MODE == kFluxNS) {

@@ -92,6 +92,7 @@ dg::PhysConst phys_const(const dg_physics* ph, const dg_options* op) {
     pc.S_div_TRef = (198.6 * 5.0 / 9.0) / TRef;
     pc.TReNorm = TRef / TRef;
     pc.lambda_stab = op->riemann == DG_RIEMANN_CENTRAL ? 0.0 : op->lambda_stab;  // SetRiemannSolver
+    pc.vns_kappa = 1.0 / (3.0 / 4.0 * pc.gm1 * (ph->mach * ph->mach));              // FluidData_NS.f90:173-181
     pc.riemann = op->riemann;
     pc.averaging = op->averaging;
     pc.inviscid = op->inviscid;
@@ -355,8 +356,8 @@ int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, cons
     if (n_cases < 1 || !meshes || !phys || !op) return h3d::fail(DG_ERR_INVALID, "null argument or no case");
     if (op->inviscid != DG_INVISCID_STANDARD)
         return h3d::fail(DG_ERR_UNSUPPORTED, "the variable-order path implements the standard (weak) volume form");
-    if (op->riemann < DG_RIEMANN_ROE || op->riemann > DG_RIEMANN_RUSANOV) return h3d::fail(DG_ERR_UNSUPPORTED, "riemann solver");
-    if (op->averaging < DG_AVG_STANDARD || op->averaging > DG_AVG_KENNEDY_GRUBER)
+    if (op->riemann < DG_RIEMANN_ROE || op->riemann > DG_RIEMANN_U_DISS) return h3d::fail(DG_ERR_UNSUPPORTED, "riemann solver");
+    if (op->averaging < DG_AVG_STANDARD || op->averaging > DG_AVG_CHANDRASEKAR)
         return h3d::fail(DG_ERR_UNSUPPORTED, "averaging");
     if (op->precision != DG_PRECISION_FP64 && op->precision != DG_PRECISION_MIXED)
         return h3d::fail(DG_ERR_UNSUPPORTED, "precision");

@@ -48,10 +48,15 @@ extern "C" {
 enum { DG_NODES_GAUSS = 0, DG_NODES_GAUSS_LOBATTO = 1 };          /* "discretization nodes" */
 enum { DG_INVISCID_STANDARD = 0, DG_INVISCID_SPLIT = 1 };          /* "inviscid discretization" */
 enum { DG_RIEMANN_ROE = 0, DG_RIEMANN_LXF = 1,                    /* "riemann solver" */
-       DG_RIEMANN_CENTRAL = 2, DG_RIEMANN_RUSANOV = 3 };
-enum { DG_AVG_STANDARD = 0, DG_AVG_PIROZZOLI = 1,                  /* "averaging" (LxF, central and */
-       DG_AVG_DUCROS = 2, DG_AVG_MORINISHI = 3,                    /*  the split form's two-point */
-       DG_AVG_KENNEDY_GRUBER = 4 };                                /*  fluxes) */
+       DG_RIEMANN_CENTRAL = 2, DG_RIEMANN_RUSANOV = 3,
+       DG_RIEMANN_STD_ROE = 4, DG_RIEMANN_ROE_PIKE = 5,            /* "standard roe", "roe-pike" */
+       DG_RIEMANN_LOW_DISS_ROE = 6,                                /* "low dissipation roe" */
+       DG_RIEMANN_MATRIX_DISS = 7, DG_RIEMANN_VISCOUS_NS = 8,      /* "matrix dissipation", "viscous ns" */
+       DG_RIEMANN_U_DISS = 9 };                                    /* "u-diss" */
+enum { DG_AVG_STANDARD = 0, DG_AVG_PIROZZOLI = 1,                  /* "averaging" (the averaged */
+       DG_AVG_DUCROS = 2, DG_AVG_MORINISHI = 3,                    /*  states of every solver but */
+       DG_AVG_KENNEDY_GRUBER = 4,                                  /*  Roe and Rusanov, and the */
+       DG_AVG_ENTROPY_CONSERVING = 5, DG_AVG_CHANDRASEKAR = 6 };   /*  split form's two-point fluxes) */
 enum { DG_PRECISION_FP64 = 0, DG_PRECISION_MIXED = 1 };            /* plain FP64 / FP32 flux form */
 enum { DG_SOURCE_NONE = 0,                                         /* UserDefinedSourceTermNS of */
        DG_SOURCE_MMS_CONVERGENCE = 1,                              /*  NavierStokes/Convergence */

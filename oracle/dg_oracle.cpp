@@ -197,7 +197,7 @@ static void l2r(int i, int j, int Nx, int Ny, int rot, int& ii, int& jj) {
 
 // ---------------------------------------------------------------- physics --------------------
 struct Phys {
-    double gamma = 1.4, gm1 = 0.4, Mach, Re, Pr, mu, kappa, mu_to_kappa, gammaM2;
+    double gamma = 1.4, gm1 = 1.4 - 1.0, Mach, Re, Pr, mu, kappa, mu_to_kappa, gammaM2;  // PhysicsStorage_NS.f90:115-133
     double S_div_TRef, TReNorm;
     bool ns;
 };
@@ -311,9 +311,51 @@ static void roe(const Phys& p, const double* QL, const double* QR, const double*
 // Averaged states of the rotated (normal, t1, t2) frame: RiemannSolvers_NS.f90:1784-1819 StandardAverage,
 // :1821-1848 DucrosAverage, :1850-1886 MorinishiAverage, :1888-1925 KennedyGruberAverage,
 // :1927-1962 PirozzoliAverage.
+// Utilities.f90:269-301 logarithmicMean (Ismail and Roe).
+static double log_mean(double aL, double aR) {
+    const double xi = aL / aR;
+    const double f = (xi - 1.0) / (xi + 1.0);
+    const double u = f * f;
+    double FF;
+    if (u < 0.01) FF = 1.0 + (1.0 / 3.0) * u + (1.0 / 5.0) * (u * u) + (1.0 / 7.0) * ((u * u) * u);
+    else FF = std::log(xi) / (2.0 * f);
+    return 0.5 * (aL + aR) / FF;
+}
+
 static void average(const Phys& ph, int avg, const double* L, const double* R, double pL, double pR, double iL,
                     double iR, double* f) {
     const double uL = iL * L[1], uR = iR * R[1], vL = iL * L[2], vR = iR * R[2], wL = iL * L[3], wR = iR * R[3];
+    if (avg == DG_AVG_ENTROPY_CONSERVING) {  // :1964-2026 EntropyConservingAverage (Ismail and Roe)
+        const double rhoL = L[0], rhoR = R[0];
+        double zL[5], zR[5], zS[5];
+        zL[4] = std::sqrt(rhoL * pL); zR[4] = std::sqrt(rhoR * pR);
+        zL[0] = rhoL / zL[4]; zR[0] = rhoR / zR[4];
+        zL[1] = zL[0] * uL; zR[1] = zR[0] * uR;
+        zL[2] = zL[0] * vL; zR[2] = zR[0] * vR;
+        zL[3] = zL[0] * wL; zR[3] = zR[0] * wR;
+        for (int q = 0; q < 5; ++q) zS[q] = zL[q] + zR[q];
+        const double inv1 = 1.0 / zS[0];
+        const double z1Log = log_mean(zL[0], zR[0]), z5Log = log_mean(zL[4], zR[4]);
+        const double rho = 0.5 * zS[0] * z5Log;
+        const double u = zS[1] * inv1, v = zS[2] * inv1, w = zS[3] * inv1, p = zS[4] * inv1;
+        const double p2 = ((ph.gamma + 1.0) / 2.0 * z5Log / z1Log + (ph.gamma - 1.0) / 2.0 * p) * (1.0 / ph.gamma);
+        const double h = ph.gamma / ph.gm1 * p2 / rho + 0.5 * (u * u + v * v + w * w);
+        f[0] = rho * u; f[1] = rho * u * u + p; f[2] = rho * u * v; f[3] = rho * u * w; f[4] = rho * u * h;
+        return;
+    }
+    if (avg == DG_AVG_CHANDRASEKAR) {  // :2028-2077 ChandrasekarAverage
+        const double rhoL = L[0], rhoR = R[0];
+        const double betaL = 0.5 * rhoL / pL, betaR = 0.5 * rhoR / pR;
+        const double betaLog = log_mean(betaL, betaR);
+        const double rho = log_mean(rhoL, rhoR);
+        const double u = 0.5 * (uL + uR), v = 0.5 * (vL + vR), w = 0.5 * (wL + wR);
+        const double p = 0.5 * (rhoL + rhoR) / (betaL + betaR);
+        const double h = 0.5 / (betaLog * ph.gm1) -
+                         0.5 * (0.5 * ((uL * uL + vL * vL + wL * wL) + (uR * uR + vR * vR + wR * wR))) + p / rho +
+                         u * u + v * v + w * w;
+        f[0] = rho * u; f[1] = rho * u * u + p; f[2] = rho * u * v; f[3] = rho * u * w; f[4] = rho * u * h;
+        return;
+    }
     if (avg == DG_AVG_STANDARD) {
         f[0] = 0.5 * (L[1] + R[1]);
         f[1] = 0.5 * (L[1] * uL + R[1] * uR + pL + pR);
@@ -401,6 +443,269 @@ static void rusanov(const Phys& p, const double* QL, const double* QR, const dou
     for (int v = 0; v < 5; ++v) flux[v] = (f[v] - smax * (QR[v] - QL[v])) / 2.0;
 }
 
+// ---- the Roe family, matrix dissipation, viscous-NS and u-diss solvers (RiemannSolvers_NS.f90) ----
+static void rotate_in(const double* Q, const double* n, const double* t1, const double* t2, double* r) {
+    r[0] = Q[0];
+    r[1] = Q[1] * n[0] + Q[2] * n[1] + Q[3] * n[2];
+    r[2] = Q[1] * t1[0] + Q[2] * t1[1] + Q[3] * t1[2];
+    r[3] = Q[1] * t2[0] + Q[2] * t2[1] + Q[3] * t2[2];
+    r[4] = Q[4];
+}
+static void rotate_out(const double* f, const double* n, const double* t1, const double* t2, double* flux) {
+    flux[0] = f[0];
+    for (int c = 0; c < 3; ++c) flux[1 + c] = n[c] * f[1] + t1[c] * f[2] + t2[c] * f[3];
+    flux[4] = f[4];
+}
+
+// VariableConversion_NS.f90:266-294 getPrimitiveVariables: [1/rho, u, v, w, p, T, a^2].
+struct Prim {
+    double irho, u, v, w, p, T, a2;
+};
+static Prim primitive(const Phys& ph, const double* U) {
+    Prim V;
+    V.irho = 1.0 / U[0];
+    V.u = U[1] * V.irho; V.v = U[2] * V.irho; V.w = U[3] * V.irho;
+    V.p = ph.gm1 * (U[4] - 0.5 * (V.u * U[1] + V.v * U[2] + V.w * U[3]));
+    V.T = V.p * ph.gammaM2 * V.irho;
+    V.a2 = ph.gamma * V.p * V.irho;
+    return V;
+}
+
+// Van Leer's modification of Harten's entropy fix of the acoustic waves (RiemannSolvers_NS.f90:507-530).
+static double entropy_fix(double lambda, double sL, double sR) {
+    const double dl = std::fmax(sR - sL, 0.0);
+    if (std::fabs(lambda) >= 2.0 * dl) return std::fabs(lambda);
+    return lambda * lambda / (4.0 * dl) + dl;
+}
+
+// stab = sum_i 1/2 alpha_i |lambda_i| K_i with the Roe eigenvectors of (u, v, w, H, a), then
+// flux = average - lambdaStab * stab in the face frame.
+static void roe_stabilised(const Phys& ph, int avg, double lambdaStab, const double* L, const double* R, double pL,
+                           double pR, double iL, double iR, double u, double v, double w, double V2, double H,
+                           double a, const double* alpha, double* lambda, double* f) {
+    (void)ph;
+    const double K[5][5] = {{1.0, u - a, v, w, H - u * a},
+                            {1.0, u, v, w, 0.5 * V2},
+                            {0.0, 0.0, 1.0, 0.0, v},
+                            {0.0, 0.0, 0.0, 1.0, w},
+                            {1.0, u + a, v, w, H + u * a}};
+    average(ph, avg, L, R, pL, pR, iL, iR, f);
+    if (avg == DG_AVG_PIROZZOLI || avg == DG_AVG_KENNEDY_GRUBER) lambda[0] = lambda[4];
+    double stab[5] = {0, 0, 0, 0, 0};
+    for (int i = 0; i < 5; ++i)
+        for (int c = 0; c < 5; ++c) stab[c] = stab[c] + 0.5 * alpha[i] * std::fabs(lambda[i]) * K[i][c];
+    for (int c = 0; c < 5; ++c) f[c] = f[c] - lambdaStab * stab[c];
+}
+
+// :430-576 StdRoeRiemannSolver and :721-861 RoePikeRiemannSolver (Roe averages of getRoeVariables,
+// VariableConversion_NS.f90:323-365; the projections differ).
+static void std_roe(const Phys& ph, int avg, double lambdaStab, bool pike, const double* QL, const double* QR,
+                    const double* n, const double* t1, const double* t2, double* flux) {
+    double L[5], R[5];
+    rotate_in(QL, n, t1, t2, L);
+    rotate_in(QR, n, t1, t2, R);
+    const Prim VL = primitive(ph, L), VR = primitive(ph, R);
+    const double aL = std::sqrt(VL.a2), aR = std::sqrt(VR.a2);
+    const double sL = std::sqrt(L[0]), sR = std::sqrt(R[0]);
+    const double inv = 1.0 / (sL + sR);
+    const double HL = (VL.p + L[4]) * VL.irho, HR = (VR.p + R[4]) * VR.irho;
+    const double rho = sL * sR;
+    const double u = (sL * VL.u + sR * VR.u) * inv, v = (sL * VL.v + sR * VR.v) * inv, w = (sL * VL.w + sR * VR.w) * inv;
+    const double H = (sL * HL + sR * HR) * inv;
+    const double V2 = u * u + v * v + w * w;
+    const double a = std::sqrt(ph.gm1 * (H - 0.5 * V2));
+    double lambda[5] = {u - a, u, u, u, u + a};
+    double alpha[5];
+    if (!pike) {
+        double dQ[5];
+        for (int q = 0; q < 5; ++q) dQ[q] = R[q] - L[q];
+        alpha[2] = dQ[2] - v * dQ[0];
+        alpha[3] = dQ[3] - w * dQ[0];
+        dQ[4] = dQ[4] - alpha[2] * v - alpha[3] * w;
+        alpha[1] = ph.gm1 * (dQ[0] * (H - u * u) + u * dQ[1] - dQ[4]) / (a * a);
+        alpha[0] = 0.5 * (dQ[0] * lambda[4] - dQ[1] - a * alpha[1]) / a;
+        alpha[4] = dQ[0] - alpha[0] - alpha[1];
+    } else {
+        const double dp = VR.p - VL.p, du = VR.u - VL.u;
+        alpha[0] = (dp - rho * a * du) / (2.0 * a * a);
+        alpha[1] = (QR[0] - QL[0]) - dp / (a * a);
+        alpha[2] = rho * (VR.v - VL.v);
+        alpha[3] = rho * (VR.w - VL.w);
+        alpha[4] = (dp + rho * a * du) / (2.0 * a * a);
+    }
+    lambda[0] = entropy_fix(lambda[0], VL.u - aL, VR.u - aR);
+    lambda[4] = entropy_fix(lambda[4], VL.u + aL, VR.u + aR);
+    double f[5];
+    roe_stabilised(ph, avg, lambdaStab, L, R, VL.p, VR.p, VL.irho, VR.irho, u, v, w, V2, H, a, alpha, lambda, f);
+    rotate_out(f, n, t1, t2, flux);
+}
+
+// Face-frame states and Roe-Pike averages written with 1/sqrt(rho) (the form of :863-1058 and
+// :1060-1247).
+struct RoePikeState {
+    double L[5], R[5], iL, iR, uL, vL, wL, uR, vR, wR, pL, pR, aL, aR, rho, u, v, w, H, V2, a;
+};
+static RoePikeState roe_pike_state(const Phys& ph, const double* QL, const double* QR, const double* n,
+                                   const double* t1, const double* t2) {
+    RoePikeState s;
+    rotate_in(QL, n, t1, t2, s.L);
+    rotate_in(QR, n, t1, t2, s.R);
+    const double rhoL = s.L[0], rhoR = s.R[0];
+    s.iL = 1.0 / rhoL; s.iR = 1.0 / rhoR;
+    const double sL = std::sqrt(rhoL), sR = std::sqrt(rhoR);
+    const double isL = 1.0 / sL, isR = 1.0 / sR;
+    const double inv = 1.0 / (sL + sR);
+    s.uL = s.L[1] * s.iL; s.uR = s.R[1] * s.iR;
+    s.vL = s.L[2] * s.iL; s.vR = s.R[2] * s.iR;
+    s.wL = s.L[3] * s.iL; s.wR = s.R[3] * s.iR;
+    const double rV2L = (s.uL * s.uL + s.vL * s.vL + s.wL * s.wL) * rhoL;
+    const double rV2R = (s.uR * s.uR + s.vR * s.vR + s.wR * s.wR) * rhoR;
+    const double rHL = ph.gamma * s.L[4] - 0.5 * ph.gm1 * rV2L, rHR = ph.gamma * s.R[4] - 0.5 * ph.gm1 * rV2R;
+    s.pL = ph.gm1 * (s.L[4] - 0.5 * rV2L);
+    s.pR = ph.gm1 * (s.R[4] - 0.5 * rV2R);
+    s.aL = std::sqrt(ph.gamma * s.pL * s.iL);
+    s.aR = std::sqrt(ph.gamma * s.pR * s.iR);
+    s.rho = sL * sR;
+    s.u = (isL * s.L[1] + isR * s.R[1]) * inv;
+    s.v = (isL * s.L[2] + isR * s.R[2]) * inv;
+    s.w = (isL * s.L[3] + isR * s.R[3]) * inv;
+    s.H = (isL * rHL + isR * rHR) * inv;
+    s.V2 = s.u * s.u + s.v * s.v + s.w * s.w;
+    s.a = std::sqrt(ph.gm1 * (s.H - 0.5 * s.V2));
+    return s;
+}
+
+// :863-1058 LowDissipationRoeRiemannSolver (L2Roe: velocity jumps scaled by min(1, max(ML, MR))).
+static void low_diss_roe(const Phys& ph, int avg, double lambdaStab, const double* QL, const double* QR,
+                         const double* n, const double* t1, const double* t2, double* flux) {
+    const RoePikeState s = roe_pike_state(ph, QL, QR, n, t1, t2);
+    const double u = s.u, a = s.a, rho = s.rho;
+    double lambda[5] = {u - a, u, u, u, u + a};
+    const double ML = std::fabs(s.uL) / s.aL, MR = std::fabs(s.uR) / s.aR;
+    const double z = std::fmin(1.0, std::fmax(ML, MR));
+    const double du = z * (s.uR - s.uL), dv = z * (s.vR - s.vL), dw = z * (s.wR - s.wL), dp = s.pR - s.pL;
+    double alpha[5];
+    alpha[0] = (dp - rho * a * du) / (2.0 * a * a);
+    alpha[1] = (s.R[0] - s.L[0]) - dp / (a * a);
+    alpha[2] = rho * dv;
+    alpha[3] = rho * dw;
+    alpha[4] = (dp + rho * a * du) / (2.0 * a * a);
+    lambda[0] = entropy_fix(lambda[0], s.uL - s.aL, s.uR - s.aR);
+    lambda[4] = entropy_fix(lambda[4], s.uL + s.aL, s.uR + s.aR);
+    double f[5];
+    roe_stabilised(ph, avg, lambdaStab, s.L, s.R, s.pL, s.pR, s.iL, s.iR, s.u, s.v, s.w, s.V2, s.H, a, alpha, lambda,
+                   f);
+    rotate_out(f, n, t1, t2, flux);
+}
+
+// :1060-1247 ViscousNSRiemannSolver: the average plus a dissipation shaped like the NS viscous terms
+// of the velocity and temperature jumps, scaled by the largest wave speed (added in the Cartesian frame).
+static void viscous_ns(const Phys& ph, int avg, double lambdaStab, const double* QL, const double* QR, const double* n,
+                       const double* t1, const double* t2, double* flux) {
+    const RoePikeState s = roe_pike_state(ph, QL, QR, n, t1, t2);
+    double lambda[5] = {s.u - s.a, s.u, s.u, s.u, s.u + s.a};
+    lambda[0] = entropy_fix(lambda[0], s.uL - s.aL, s.uR - s.aR);
+    lambda[4] = entropy_fix(lambda[4], s.uL + s.aL, s.uR + s.aR);
+    double f[5];
+    average(ph, avg, s.L, s.R, s.pL, s.pR, s.iL, s.iR, f);
+    if (avg == DG_AVG_PIROZZOLI || avg == DG_AVG_KENNEDY_GRUBER) lambda[0] = lambda[4];
+    const double uL = QL[1] / QL[0], uR = QR[1] / QR[0];
+    const double vL = QL[2] / QL[0], vR = QR[2] / QR[0];
+    const double wL = QL[3] / QL[0], wR = QR[3] / QR[0];
+    const double u = 0.5 * (uL + uR), v = 0.5 * (vL + vR), w = 0.5 * (wL + wR);
+    const double divV = (uR - uL) * n[0] + (vR - vL) * n[1] + (wR - wL) * n[2];
+    double tau[3][3];
+    tau[0][0] = 2.0 * (uR - uL) * n[0] - (1.0 / 3.0) * divV;
+    tau[1][1] = 2.0 * (vR - vL) * n[1] - (1.0 / 3.0) * divV;
+    tau[2][2] = 2.0 * (wR - wL) * n[2] - (1.0 / 3.0) * divV;
+    tau[0][1] = (uR - uL) * n[1] + (vR - vL) * n[0];
+    tau[0][2] = (uR - uL) * n[2] + (wR - wL) * n[0];
+    tau[1][2] = (vR - vL) * n[2] + (wR - wL) * n[1];
+    tau[1][0] = tau[0][1]; tau[2][0] = tau[0][2]; tau[2][1] = tau[1][2];
+    const double kappa = 1.0 / (3.0 / 4.0 * ph.gm1 * (ph.Mach * ph.Mach));  // FluidData_NS.f90:173-181, Pr = 3/4
+    const double TL = s.pL * ph.gammaM2 / s.L[0], TR = s.pR * ph.gammaM2 / s.R[0];  // :156-164
+    double lmax = 0.0;
+    for (int i = 0; i < 5; ++i) lmax = std::fmax(lmax, std::fabs(lambda[i]));
+    double stab[5];
+    stab[0] = 0.0;
+    for (int r = 0; r < 3; ++r) stab[1 + r] = lmax * (tau[r][0] * n[0] + tau[r][1] * n[1] + tau[r][2] * n[2]);
+    stab[4] = lmax * ((u * tau[0][0] + v * tau[0][1] + w * tau[0][2]) * n[0] +
+                      (u * tau[1][0] + v * tau[1][1] + w * tau[1][2]) * n[1] +
+                      (u * tau[2][0] + v * tau[2][1] + w * tau[2][2]) * n[2] + kappa * (TR - TL));
+    rotate_out(f, n, t1, t2, flux);
+    for (int c = 0; c < 5; ++c) flux[c] = flux[c] - lambdaStab * stab[c];
+}
+
+// VariableConversion_NS.f90:211-237 NSGradientVariables_ENTROPY.
+static void entropy_variables(const Phys& ph, const double* Q, double* U) {
+    const double irho = 1.0 / Q[0];
+    const double rV2 = (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) * irho;
+    const double p = ph.gm1 * (Q[4] - 0.5 * rV2);
+    const double ip = 1.0 / p;
+    U[0] = (ph.gamma - (std::log(p) - ph.gamma * std::log(Q[0]))) * (1.0 / (1.4 - 1.0)) - 0.5 * rV2 * ip;
+    U[1] = Q[1] * ip;
+    U[2] = Q[2] * ip;
+    U[3] = Q[3] * ip;
+    U[4] = -Q[0] * ip;
+}
+
+// :578-719 MatrixDissipationRiemannSolver: dissipation of the entropy-variable jump with the
+// eigenvectors and scalings of the logarithmic-mean states.
+static void matrix_diss(const Phys& ph, int avg, double lambdaStab, const double* QL, const double* QR,
+                        const double* n, const double* t1, const double* t2, double* flux) {
+    double L[5], R[5], EVL[5], EVR[5];
+    rotate_in(QL, n, t1, t2, L);
+    rotate_in(QR, n, t1, t2, R);
+    entropy_variables(ph, L, EVL);
+    entropy_variables(ph, R, EVR);
+    const double iL = 1.0 / L[0], iR = 1.0 / R[0];
+    const double uL = L[1] * iL, uR = R[1] * iR, vL = L[2] * iL, vR = R[2] * iR, wL = L[3] * iL, wR = R[3] * iR;
+    const double vtL = uL * uL + vL * vL + wL * wL, vtR = uR * uR + vR * vR + wR * wR;
+    const double pL = ph.gm1 * (L[4] - 0.5 * L[0] * vtL), pR = ph.gm1 * (R[4] - 0.5 * R[0] * vtR);
+    const double betaL = -0.5 * EVL[4], betaR = -0.5 * EVR[4];
+    const double betaLog = log_mean(betaL, betaR), rhoLog = log_mean(L[0], R[0]);
+    const double pMean = 0.5 * (L[0] + R[0]) / (betaL + betaR);
+    const double a = std::sqrt(ph.gamma * pMean / rhoLog);
+    const double u = 0.5 * (uL + uR), v = 0.5 * (vL + vR), w = 0.5 * (wL + wR);
+    const double V2 = 2.0 * (u * u + v * v + w * w) - 0.5 * (vtL + vtR);
+    const double h = 0.5 * (ph.gamma / ph.gm1 / betaLog + V2);
+    double lambda[5] = {std::fabs(u - a), std::fabs(u), std::fabs(u), std::fabs(u), std::fabs(u + a)};
+    const double Rm[5][5] = {{1.0, u - a, v, w, h - u * a},
+                             {1.0, u, v, w, 0.5 * V2},
+                             {0.0, 0.0, 1.0, 0.0, v},
+                             {0.0, 0.0, 0.0, 1.0, w},
+                             {1.0, u + a, v, w, h + u * a}};  // Rm[j][i] = R1(i, j)
+    const double T1 = 0.5 * rhoLog * (1.0 / ph.gamma);
+    const double T[5] = {T1, 2.0 * ((1.4 - 1.0) / (2.0 * 1.4)) * rhoLog, pMean, pMean, T1};
+    double f[5];
+    average(ph, avg, L, R, pL, pR, iL, iR, f);
+    if (avg == DG_AVG_PIROZZOLI || avg == DG_AVG_KENNEDY_GRUBER) lambda[0] = lambda[4];
+    double stab[5] = {0, 0, 0, 0, 0};
+    for (int i = 0; i < 5; ++i)
+        for (int j = 0; j < 5; ++j)
+            for (int k = 0; k < 5; ++k)
+                stab[i] = stab[i] + 0.5 * Rm[j][i] * lambda[j] * T[j] * Rm[j][k] * (EVR[k] - EVL[k]);
+    for (int c = 0; c < 5; ++c) f[c] = f[c] - lambdaStab * stab[c];
+    rotate_out(f, n, t1, t2, flux);
+}
+
+// :1336-1425 u_dissRiemannSolver: the LxF form with lambda = max(|u_L|, |u_R|) (no sound speed).
+static void u_diss(const Phys& p, int avg, double lambdaStab, const double* QL, const double* QR, const double* n,
+                   const double* t1, const double* t2, double* flux) {
+    double L[5], R[5];
+    rotate_in(QL, n, t1, t2, L);
+    rotate_in(QR, n, t1, t2, R);
+    const double iL = 1.0 / L[0], iR = 1.0 / R[0];
+    const double V2L = (L[1] * L[1] + L[2] * L[2] + L[3] * L[3]) * iL;
+    const double V2R = (R[1] * R[1] + R[2] * R[2] + R[3] * R[3]) * iR;
+    const double pL = p.gm1 * (L[4] - 0.5 * V2L), pR = p.gm1 * (R[4] - 0.5 * V2R);
+    const double lambda = std::fmax(std::fabs(L[1] * iL), std::fabs(R[1] * iR));
+    double f[5];
+    average(p, avg, L, R, pL, pR, iL, iR, f);
+    for (int v = 0; v < 5; ++v) f[v] = f[v] - lambdaStab * (0.5 * lambda * (R[v] - L[v]));
+    rotate_out(f, n, t1, t2, flux);
+}
+
 // RiemannSolvers_NS.f90:2085-2145 StandardDG_TwoPointFlux and :2369-2437 Pirozzoli_TwoPointFlux.
 static void two_point(const Phys& p, int avg, const double* QL, const double* QR, const double* JaL, const double* JaR,
                       double* fs) {
@@ -461,6 +766,38 @@ static void two_point(const Phys& p, int avg, const double* QL, const double* QR
             F[d][1 + d] += pp;
             F[d][4] = rho * um[d] * e + pp * um[d];
         }
+    } else if (avg == DG_AVG_ENTROPY_CONSERVING || avg == DG_AVG_CHANDRASEKAR) {
+        // :2439-2558 EntropyConserving_TwoPointFlux, :2560-2641 Chandrasekar_TwoPointFlux: the averaged
+        // states of the two-point average, fluxes in all three directions.
+        double rho, u, v, w, pp, hh;
+        if (avg == DG_AVG_ENTROPY_CONSERVING) {
+            double zL[5], zR[5], zA[5];
+            zL[4] = std::sqrt(QL[0] * pL); zR[4] = std::sqrt(QR[0] * pR);
+            zL[0] = QL[0] / zL[4]; zR[0] = QR[0] / zR[4];
+            zL[1] = zL[0] * uL; zR[1] = zR[0] * uR;
+            zL[2] = zL[0] * vL; zR[2] = zR[0] * vR;
+            zL[3] = zL[0] * wL; zR[3] = zR[0] * wR;
+            for (int q = 0; q < 5; ++q) zA[q] = 0.5 * (zL[q] + zR[q]);
+            const double inv1 = 1.0 / zA[0];
+            const double z1Log = log_mean(zL[0], zR[0]), z5Log = log_mean(zL[4], zR[4]);
+            rho = zA[0] * z5Log;
+            u = zA[1] * inv1; v = zA[2] * inv1; w = zA[3] * inv1; pp = zA[4] * inv1;
+            const double p2 = ((p.gamma + 1.0) / 2.0 * z5Log / z1Log + (p.gamma - 1.0) / 2.0 * pp) * (1.0 / p.gamma);
+            hh = p.gamma / p.gm1 * p2 / rho + 0.5 * (u * u + v * v + w * w);
+        } else {
+            const double betaL = 0.5 * QL[0] / pL, betaR = 0.5 * QR[0] / pR;
+            const double betaLog = log_mean(betaL, betaR);
+            rho = log_mean(QL[0], QR[0]);
+            u = 0.5 * (uL + uR); v = 0.5 * (vL + vR); w = 0.5 * (wL + wR);
+            pp = 0.5 * (QL[0] + QR[0]) / (betaL + betaR);
+            hh = 0.5 / (betaLog * p.gm1) - 0.5 * (0.5 * ((uL * uL + vL * vL + wL * wL) + (uR * uR + vR * vR + wR * wR))) +
+                 pp / rho + u * u + v * v + w * w;
+        }
+        const double ff[5] = {rho * u, rho * u * u + pp, rho * u * v, rho * u * w, rho * u * hh};
+        const double gg[5] = {rho * v, rho * v * u, rho * v * v + pp, rho * v * w, rho * v * hh};
+        const double hhh[5] = {rho * w, rho * w * u, rho * w * v, rho * w * w + pp, rho * w * hh};
+        for (int q = 0; q < 5; ++q) fs[q] = ff[q] * Ja[0] + gg[q] * Ja[1] + hhh[q] * Ja[2];
+        return;
     } else {  // Pirozzoli, :2369-2437
         const double rho = 0.5 * (QL[0] + QR[0]), u = 0.5 * (uL + uR), v = 0.5 * (vL + vR), w = 0.5 * (wL + wR);
         const double pp = 0.5 * (pL + pR);
@@ -985,11 +1322,25 @@ static void compute_rhs(Solver& s, double t) {
                 }
             }
             double inv[5];
-            if (s.opt.riemann == DG_RIEMANN_ROE) roe(s.ph, &f.Q[0][5 * p], &f.Q[1][5 * p], n, inv);
-            else if (s.opt.riemann == DG_RIEMANN_RUSANOV) rusanov(s.ph, &f.Q[0][5 * p], &f.Q[1][5 * p], n, inv);
-            else  // LxF, or central = LxF with lambdaStab = 0 (RiemannSolvers_NS.f90:224)
-                lxf(s.ph, s.opt.averaging, s.opt.riemann == DG_RIEMANN_CENTRAL ? 0.0 : s.opt.lambda_stab,
-                    &f.Q[0][5 * p], &f.Q[1][5 * p], n, &s.ft1[3 * (f.off + p)], &s.ft2[3 * (f.off + p)], inv);
+            const double* QL = &f.Q[0][5 * p];
+            const double* QR = &f.Q[1][5 * p];
+            const double* t1 = &s.ft1[3 * (f.off + p)];
+            const double* t2 = &s.ft2[3 * (f.off + p)];
+            const int avg = s.opt.averaging;
+            const double ls = s.opt.lambda_stab;
+            switch (s.opt.riemann) {
+                case DG_RIEMANN_ROE: roe(s.ph, QL, QR, n, inv); break;
+                case DG_RIEMANN_RUSANOV: rusanov(s.ph, QL, QR, n, inv); break;
+                case DG_RIEMANN_STD_ROE: std_roe(s.ph, avg, ls, false, QL, QR, n, t1, t2, inv); break;
+                case DG_RIEMANN_ROE_PIKE: std_roe(s.ph, avg, ls, true, QL, QR, n, t1, t2, inv); break;
+                case DG_RIEMANN_LOW_DISS_ROE: low_diss_roe(s.ph, avg, ls, QL, QR, n, t1, t2, inv); break;
+                case DG_RIEMANN_MATRIX_DISS: matrix_diss(s.ph, avg, ls, QL, QR, n, t1, t2, inv); break;
+                case DG_RIEMANN_VISCOUS_NS: viscous_ns(s.ph, avg, ls, QL, QR, n, t1, t2, inv); break;
+                case DG_RIEMANN_U_DISS: u_diss(s.ph, avg, ls, QL, QR, n, t1, t2, inv); break;
+                default:  // LxF, or central = LxF with lambdaStab = 0 (RiemannSolvers_NS.f90:224)
+                    lxf(s.ph, avg, s.opt.riemann == DG_RIEMANN_CENTRAL ? 0.0 : ls, QL, QR, n, t1, t2, inv);
+                    break;
+            }
             for (int v = 0; v < 5; ++v) flux[5 * p + v] = (inv[v] - visc[v]) * s.fj[f.off + p];
         }
         project_to_side(f, 1, 5, flux, f.fStar[0], -1.0, s.nodes);

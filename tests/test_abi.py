@@ -47,7 +47,8 @@ def test_create_validates_before_touching_the_device():
     # split form needs Gauss-Lobatto nodes
     assert _ctx_create(mesh, Config(inviscid=_abi.DG_INVISCID_SPLIT)) == _abi.DG_ERR_INVALID
     assert _ctx_create(mesh, Config(mach=-1.0)) == _abi.DG_ERR_INVALID
-    assert _ctx_create(mesh, Config(riemann=7)) == _abi.DG_ERR_UNSUPPORTED
+    assert _ctx_create(mesh, Config(riemann=10)) == _abi.DG_ERR_UNSUPPORTED
+    assert _ctx_create(mesh, Config(averaging=7)) == _abi.DG_ERR_UNSUPPORTED
     big = HexMesh.box(1, [0, 0, 0], [1, 1, 1], 8, node_type=_abi.DG_NODES_GAUSS)
     assert _ctx_create(big, Config()) == _abi.DG_ERR_UNSUPPORTED
 
@@ -159,7 +160,7 @@ def test_control_file_keys():
     with pytest.raises(UnsupportedOption):
         parse_control("viscous discretization = BR2\nreynolds number = 1\n")
     with pytest.raises(UnsupportedOption):
-        parse_control("riemann solver = roe-pike\nreynolds number = 1\n")
+        parse_control("riemann solver = hllc\nreynolds number = 1\n")
 
 
 def test_riemann_and_averaging_keys():
@@ -168,6 +169,13 @@ def test_riemann_and_averaging_keys():
     c = parse_control("riemann solver = central\naveraging = ducros\nreynolds number = 1\n")
     assert c.riemann == _abi.DG_RIEMANN_CENTRAL and c.averaging == _abi.DG_AVG_DUCROS
     assert parse_control("averaging = morinishi\nreynolds number = 1\n").averaging == _abi.DG_AVG_MORINISHI
+    names = {"standard roe": _abi.DG_RIEMANN_STD_ROE, "Roe-Pike": _abi.DG_RIEMANN_ROE_PIKE,
+             "low dissipation roe": _abi.DG_RIEMANN_LOW_DISS_ROE, "matrix dissipation": _abi.DG_RIEMANN_MATRIX_DISS,
+             "viscous NS": _abi.DG_RIEMANN_VISCOUS_NS, "u-diss": _abi.DG_RIEMANN_U_DISS}
+    for k, v in names.items():
+        assert parse_control(f"riemann solver = {k}\nreynolds number = 1\n").riemann == v
+    for k, v in (("entropy conserving", _abi.DG_AVG_ENTROPY_CONSERVING), ("Chandrasekar", _abi.DG_AVG_CHANDRASEKAR)):
+        assert parse_control(f"averaging = {k}\nreynolds number = 1\n").averaging == v
 
 
 def test_anisotropic_order_keys(tmp_path):

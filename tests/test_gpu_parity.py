@@ -216,13 +216,19 @@ def test_max_dt_filter_ties_and_high_mach(precision):
 
 SOLVERS = [(_abi.DG_RIEMANN_LXF, _abi.DG_AVG_DUCROS), (_abi.DG_RIEMANN_LXF, _abi.DG_AVG_MORINISHI),
            (_abi.DG_RIEMANN_LXF, _abi.DG_AVG_KENNEDY_GRUBER), (_abi.DG_RIEMANN_CENTRAL, _abi.DG_AVG_STANDARD),
-           (_abi.DG_RIEMANN_CENTRAL, _abi.DG_AVG_KENNEDY_GRUBER), (_abi.DG_RIEMANN_RUSANOV, _abi.DG_AVG_STANDARD)]
+           (_abi.DG_RIEMANN_CENTRAL, _abi.DG_AVG_KENNEDY_GRUBER), (_abi.DG_RIEMANN_RUSANOV, _abi.DG_AVG_STANDARD),
+           (_abi.DG_RIEMANN_STD_ROE, _abi.DG_AVG_STANDARD), (_abi.DG_RIEMANN_STD_ROE, _abi.DG_AVG_PIROZZOLI),
+           (_abi.DG_RIEMANN_ROE_PIKE, _abi.DG_AVG_KENNEDY_GRUBER), (_abi.DG_RIEMANN_ROE_PIKE, _abi.DG_AVG_MORINISHI),
+           (_abi.DG_RIEMANN_LOW_DISS_ROE, _abi.DG_AVG_STANDARD), (_abi.DG_RIEMANN_MATRIX_DISS, _abi.DG_AVG_STANDARD),
+           (_abi.DG_RIEMANN_MATRIX_DISS, _abi.DG_AVG_CHANDRASEKAR), (_abi.DG_RIEMANN_VISCOUS_NS, _abi.DG_AVG_PIROZZOLI),
+           (_abi.DG_RIEMANN_U_DISS, _abi.DG_AVG_DUCROS), (_abi.DG_RIEMANN_LXF, _abi.DG_AVG_ENTROPY_CONSERVING),
+           (_abi.DG_RIEMANN_CENTRAL, _abi.DG_AVG_CHANDRASEKAR)]
 
 
 @pytest.mark.parametrize("riemann,averaging", SOLVERS)
 def test_more_riemann_solvers_and_averages(riemann, averaging):
-    """Central, Rusanov and the Ducros / Morinishi / Kennedy-Gruber averages (RiemannSolvers_NS.f90),
-    plain form against the oracle and mixed form within 1e-6 of it."""
+    """Every Riemann solver and average of RiemannSolvers_NS.f90 beyond Roe/LxF: plain form against the
+    oracle (RHS 1e-10, state 1e-12) and mixed form within 1e-6 of it."""
     mesh, cfg, q0 = cases.tgv_case(n=3, order=4, nodes=_abi.DG_NODES_GAUSS, riemann=riemann, averaging=averaging,
                                    warp=0.1, mach=0.3, perturbation=0.02, seed=3)
     _check_rhs(mesh, cfg, q0)
@@ -233,9 +239,11 @@ def test_more_riemann_solvers_and_averages(riemann, averaging):
     _check_steps(mesh, mixed, q0, steps=2, dt=2e-3, tol=MIXED_TOL)
 
 
-@pytest.mark.parametrize("averaging", [_abi.DG_AVG_DUCROS, _abi.DG_AVG_MORINISHI, _abi.DG_AVG_KENNEDY_GRUBER])
+@pytest.mark.parametrize("averaging", [_abi.DG_AVG_DUCROS, _abi.DG_AVG_MORINISHI, _abi.DG_AVG_KENNEDY_GRUBER,
+                                       _abi.DG_AVG_ENTROPY_CONSERVING, _abi.DG_AVG_CHANDRASEKAR])
 def test_split_form_two_point_fluxes(averaging):
-    """Split form with the Ducros, Morinishi and Kennedy-Gruber two-point fluxes."""
+    """Split form with the Ducros, Morinishi, Kennedy-Gruber, entropy-conserving (Ismail-Roe) and
+    Chandrasekar two-point fluxes."""
     mesh, cfg, q0 = cases.tgv_case(n=3, order=4, nodes=_abi.DG_NODES_GAUSS_LOBATTO, riemann=_abi.DG_RIEMANN_LXF,
                                    inviscid=_abi.DG_INVISCID_SPLIT, averaging=averaging, perturbation=0.01, seed=5)
     _check_rhs(mesh, cfg, q0)

@@ -245,7 +245,11 @@ def test_autotune_keeps_results_and_persists(tmp_path, monkeypatch):
 
 @pytest.mark.parametrize("riemann,averaging", [(_abi.DG_RIEMANN_RUSANOV, _abi.DG_AVG_STANDARD),
                                                (_abi.DG_RIEMANN_CENTRAL, _abi.DG_AVG_DUCROS),
-                                               (_abi.DG_RIEMANN_LXF, _abi.DG_AVG_KENNEDY_GRUBER)])
+                                               (_abi.DG_RIEMANN_LXF, _abi.DG_AVG_KENNEDY_GRUBER),
+                                               (_abi.DG_RIEMANN_ROE_PIKE, _abi.DG_AVG_ENTROPY_CONSERVING),
+                                               (_abi.DG_RIEMANN_MATRIX_DISS, _abi.DG_AVG_STANDARD),
+                                               (_abi.DG_RIEMANN_VISCOUS_NS, _abi.DG_AVG_CHANDRASEKAR),
+                                               (_abi.DG_RIEMANN_LOW_DISS_ROE, _abi.DG_AVG_PIROZZOLI)])
 def test_anisotropic_more_solvers(riemann, averaging):
     mesh, cfg, q0 = cases.aniso_tgv_case(n=3, lo=1, hi=4, seed=31, riemann=riemann)
     import dataclasses

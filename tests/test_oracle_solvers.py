@@ -1,0 +1,51 @@
+"""Properties of every Riemann solver and average of the oracle (no GPU): free-stream preservation on
+a curvilinear mesh and discrete conservation on a periodic one."""
+import numpy as np
+import pytest
+
+import cases
+import oracle
+from horses3d_gb300 import _abi
+from horses3d_gb300.mesh import HexMesh
+
+ALL_RIEMANN = [_abi.DG_RIEMANN_ROE, _abi.DG_RIEMANN_LXF, _abi.DG_RIEMANN_CENTRAL, _abi.DG_RIEMANN_RUSANOV,
+               _abi.DG_RIEMANN_STD_ROE, _abi.DG_RIEMANN_ROE_PIKE, _abi.DG_RIEMANN_LOW_DISS_ROE,
+               _abi.DG_RIEMANN_MATRIX_DISS, _abi.DG_RIEMANN_VISCOUS_NS, _abi.DG_RIEMANN_U_DISS]
+ALL_AVERAGES = [_abi.DG_AVG_STANDARD, _abi.DG_AVG_PIROZZOLI, _abi.DG_AVG_DUCROS, _abi.DG_AVG_MORINISHI,
+                _abi.DG_AVG_KENNEDY_GRUBER, _abi.DG_AVG_ENTROPY_CONSERVING, _abi.DG_AVG_CHANDRASEKAR]
+
+
+def _warped():
+    return HexMesh.box(2, [0, 0, 0], [2 * np.pi] * 3, 4, node_type=_abi.DG_NODES_GAUSS, warp=0.1, patch_order=4)
+
+
+@pytest.mark.parametrize("riemann", ALL_RIEMANN)
+def test_every_solver_preserves_a_uniform_flow(riemann):
+    """A uniform state has zero right-hand side: every numerical flux is consistent (F*(Q, Q) = F(Q).n)
+    and the metric terms are discretely free-stream preserving."""
+    mesh = _warped()
+    cfg = cases.Config(order=4, nodes=_abi.DG_NODES_GAUSS, mach=0.3, reynolds=100.0, riemann=riemann,
+                       averaging=_abi.DG_AVG_CHANDRASEKAR if riemann == _abi.DG_RIEMANN_MATRIX_DISS else 0)
+    o = oracle.Oracle(mesh, cfg.physics(), cfg.options())
+    q = np.tile([1.2, 0.3 * 1.2, -0.2 * 1.2, 0.1 * 1.2, 1.0 / (0.4 * 1.4 * 0.09) + 0.5 * 1.2 * 0.14],
+                mesh.ndof)
+    o.set_state(q)
+    assert np.max(np.abs(o.rhs(0.0))) < 1e-9
+
+
+@pytest.mark.parametrize("averaging", ALL_AVERAGES)
+@pytest.mark.parametrize("inviscid", [_abi.DG_INVISCID_STANDARD, _abi.DG_INVISCID_SPLIT])
+def test_every_average_conserves_mass_momentum_energy(averaging, inviscid):
+    """On a periodic mesh sum_nodes w J QDot = 0 for every conserved variable: the face fluxes are
+    single-valued and the volume terms telescope (standard and split form)."""
+    if inviscid == _abi.DG_INVISCID_SPLIT and averaging == _abi.DG_AVG_PIROZZOLI:
+        pytest.skip("covered by the split-form parity tests")
+    mesh, cfg, q0 = cases.tgv_case(n=2, order=3, nodes=_abi.DG_NODES_GAUSS_LOBATTO, riemann=_abi.DG_RIEMANN_LXF,
+                                   inviscid=inviscid, averaging=averaging, mach=0.3, perturbation=0.05, seed=4)
+    o = oracle.Oracle(mesh, cfg.physics(), cfg.options())
+    o.set_state(q0)
+    qd = o.rhs(0.0).reshape(-1, 5)
+    w = cases.quadrature_weights(mesh)
+    total = np.einsum("n,nv->v", w, qd)
+    scale = np.einsum("n,nv->v", w, np.abs(qd))
+    assert np.all(np.abs(total) <= 1e-12 * scale + 1e-14), total / scale
