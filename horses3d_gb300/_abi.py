@@ -34,6 +34,7 @@ DG_AVG_STANDARD, DG_AVG_PIROZZOLI, DG_AVG_DUCROS, DG_AVG_MORINISHI, DG_AVG_KENNE
 DG_AVG_ENTROPY_CONSERVING, DG_AVG_CHANDRASEKAR = 5, 6
 DG_PRECISION_FP64, DG_PRECISION_MIXED = 0, 1
 DG_SOURCE_NONE, DG_SOURCE_MMS_CONVERGENCE, DG_SOURCE_MMS_LAMB_VECTOR = 0, 1, 2
+DG_GRADVARS_STATE, DG_GRADVARS_ENTROPY, DG_GRADVARS_ENERGY = 0, 1, 2
 DG_FIELD_Q, DG_FIELD_QDOT, DG_FIELD_G, DG_FIELD_UX, DG_FIELD_UY, DG_FIELD_UZ = range(6)
 
 _i32p = C.POINTER(C.c_int32)
@@ -80,6 +81,7 @@ class DgOptions(C.Structure):
         ("lambda_stab", C.c_double),
         ("precision", C.c_int32),
         ("source", C.c_int32),
+        ("gradient_variables", C.c_int32),
     ]
 
 

@@ -37,6 +37,7 @@ class Config:
     lambda_stab: float = 1.0
     precision: int = _abi.DG_PRECISION_FP64
     source: int = _abi.DG_SOURCE_NONE
+    gradient_variables: int = _abi.DG_GRADVARS_STATE
     cfl: float | None = None
     dcfl: float | None = None
     dt: float | None = None
@@ -60,11 +61,14 @@ class Config:
 
     def options(self) -> _abi.DgOptions:
         return _abi.DgOptions(self.inviscid, self.riemann, self.averaging, self.lambda_stab, self.precision,
-                              self.source)
+                              self.source, self.gradient_variables)
 
     def periodic_spec(self) -> str:
         return ",".join(f"{a}:{b}" for a, b in self.periodic)
 
+
+# SpatialDiscretization.f90:106-148 "gradient variables"
+_GRADVARS = {"state": _abi.DG_GRADVARS_STATE, "entropy": _abi.DG_GRADVARS_ENTROPY, "energy": _abi.DG_GRADVARS_ENERGY}
 
 # RiemannSolvers_NS.f90:5-40 keyword values
 _RIEMANN = {"roe": _abi.DG_RIEMANN_ROE, "lax-friedrichs": _abi.DG_RIEMANN_LXF, "central": _abi.DG_RIEMANN_CENTRAL,
@@ -154,8 +158,9 @@ def parse_control(text: str) -> Config:
     if vd != "br1":
         raise UnsupportedOption(f"viscous discretization '{vd}'")
     gv = (get("gradient variables", "state") or "state").lower()
-    if gv != "state":
+    if gv not in _GRADVARS:
         raise UnsupportedOption(f"gradient variables '{gv}'")
+    cfg.gradient_variables = _GRADVARS[gv]
     em = (get("explicit method", "rk3") or "rk3").lower()
     if em not in ("rk3", "williamson rk3"):
         raise UnsupportedOption(f"explicit method '{em}'")

@@ -252,6 +252,8 @@ int validate(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op) 
         return h3d::fail(DG_ERR_UNSUPPORTED, "precision");
     if (op->source < DG_SOURCE_NONE || op->source > DG_SOURCE_MMS_LAMB_VECTOR)
         return h3d::fail(DG_ERR_UNSUPPORTED, "source");
+    if (op->gradient_variables < DG_GRADVARS_STATE || op->gradient_variables > DG_GRADVARS_ENERGY)
+        return h3d::fail(DG_ERR_UNSUPPORTED, "gradient variables");
     return DG_OK;
 }
 
@@ -304,6 +306,7 @@ int dg_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op,
     pc.averaging = op->averaging;
     pc.inviscid = op->inviscid;
     pc.source = op->source;
+    pc.grad_vars = pc.ns ? op->gradient_variables : 0;
     const h3d::NodalStorage& nsx = h3d::nodal_storage(c->nodes, c->P - 1);
     for (int d = 0; d < 3; ++d) c->dxi[d] = 1.0 / std::fabs(nsx.x[1] - nsx.x[0]);
 

@@ -117,6 +117,7 @@ struct dg_ctx {
     h3dctx::DevBuf<long long> eoff, soff, foff;
     h3dctx::DevBuf<dg::CaseConst> cc;
     h3dctx::DevBuf<double> dxi_table, gamma_M2;
+    h3dctx::DevBuf<double> pstat;  // mixed form: momentum residual of the state at rest per unit pressure
     h3dctx::VStore<double> v64;
     h3dctx::VStore<float> v32;
     int n_items = 0;

@@ -327,6 +327,20 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
     __syncthreads();
 
     R U[3][5];
+    // gradient variables other than the state are formed per node into the (still unused) gradient
+    // space, read with the stride of its 3-direction layout
+    const bool gv = ns && a.ph.grad_vars != 0;
+    if (gv) {
+        if (active) {
+            R u[5];
+            gradient_variables(a.ph, q, u);
+            st5(G4, n * 3, G1, n, u);
+        }
+        __syncthreads();
+    }
+    const R* X4 = gv ? G4 : Q4;
+    const R* X1 = gv ? G1 : Q1;
+    const int xs = gv ? 3 : 1;
     if (ns) {
         if (active) {
             // local gradient: U_x = (U_xi Ja^xi_x + U_eta Ja^eta_x + U_zeta Ja^zeta_x) / J
@@ -336,7 +350,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
                 const R w = a.ops.D[i * kMaxP + l];
                 const int m = l + P * (j + P * k);
                 R x[5];
-                ld5(Q4, m, Q1, m, x);
+                ld5(X4, m * xs, X1, m, x);
 #pragma unroll
                 for (int v = 0; v < 5; ++v) uxi[v] = uxi[v] + x[v] * w;
             }
@@ -345,7 +359,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
                 const R w = a.ops.D[j * kMaxP + l];
                 const int m = i + P * (l + P * k);
                 R x[5];
-                ld5(Q4, m, Q1, m, x);
+                ld5(X4, m * xs, X1, m, x);
 #pragma unroll
                 for (int v = 0; v < 5; ++v) ueta[v] = ueta[v] + x[v] * w;
             }
@@ -354,7 +368,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
                 const R w = a.ops.D[k * kMaxP + l];
                 const int m = i + P * (j + P * l);
                 R x[5];
-                ld5(Q4, m, Q1, m, x);
+                ld5(X4, m * xs, X1, m, x);
 #pragma unroll
                 for (int v = 0; v < 5; ++v) uzeta[v] = uzeta[v] + x[v] * w;
             }
@@ -380,9 +394,12 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
                 const R nn[3] = {sg[0], sg[P2], sg[2 * P2]};
                 const R J = sg[3 * P2];
                 const bool left = (map >> 3) == 1;
+                R uo[5], un[5];
+                gradient_variables(a.ph, own[0], uo);
+                gradient_variables(a.ph, nbr, un);
                 R u[5];
 #pragma unroll
-                for (int v = 0; v < 5; ++v) u[v] = R(0.5) * (left ? (nbr[v] - own[0][v]) : (own[0][v] - nbr[v])) * J;
+                for (int v = 0; v < 5; ++v) u[v] = R(0.5) * (left ? (un[v] - uo[v]) : (uo[v] - un[v])) * J;
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
                     R x[5];

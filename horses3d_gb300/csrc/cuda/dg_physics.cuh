@@ -11,7 +11,7 @@ struct PhysConst {
     double gamma, gm1, gammaM2, mu, kappa, mu_to_kappa, S_div_TRef, TReNorm;
     double vns_kappa;  // conductivity of the viscous-NS Riemann solver, 1 / (3/4 (gamma-1) M^2)
     double lambda_stab;
-    int ns, riemann, averaging, inviscid, source;
+    int ns, riemann, averaging, inviscid, source, grad_vars;
 };
 
 // The mixed form stores the energy relative to a constant reference E_ref (Q5' = E - E_ref, formed in
@@ -26,7 +26,7 @@ struct PhysR {
     R g_over_gm1, gp1_over_4, gm1_gammaM2;
     R gp1_over_2, gm1_over_2, inv_gamma, inv_gm1, gm1_over_2g, vns_kappa;
     R e_ref, p_ref, h_ref;
-    int ns, riemann, averaging;
+    int ns, riemann, averaging, grad_vars;
 };
 
 template <typename R>
@@ -47,7 +47,7 @@ PhysR<R> make_phys(const PhysConst& c) {
     p.gm1_over_2g = R(c.gm1 / (2.0 * c.gamma));
     p.vns_kappa = R(c.vns_kappa);
     p.e_ref = R(0); p.p_ref = R(0); p.h_ref = R(0);
-    p.ns = c.ns; p.riemann = c.riemann; p.averaging = c.averaging;
+    p.ns = c.ns; p.riemann = c.riemann; p.averaging = c.averaging; p.grad_vars = c.grad_vars;
     return p;
 }
 
@@ -107,25 +107,81 @@ __device__ __forceinline__ void euler_contravariant(const PhysR<R>& p, const R* 
         for (int q = 0; q < 5; ++q) F[d][q] = f[q] * ja[d][0] + g[q] * ja[d][1] + h[q] * ja[d][2];
 }
 
-// Physics_NS.f90:246-303 ViscousFlux_STATE (beta = 0): F[c][v] cartesian component c.
+// BR1's gradient variables U(Q) (VariableConversion_NS.f90:196-262): the state itself, the entropy
+// variables or (rho, u, v, w, T). The entropy and energy variables take the absolute pressure.
+template <typename R>
+__device__ __forceinline__ void gradient_variables(const PhysR<R>& p, const R* Q, R* U) {
+    if (p.grad_vars == 0) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) U[v] = Q[v];
+        return;
+    }
+    const R irho = R(1) / Q[0];
+    const R rV2 = (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) * irho;
+    const R pr = p.gm1 * (Q[4] - R(0.5) * rV2) + p.p_ref;
+    if (p.grad_vars == 1) {
+        const R ip = R(1) / pr;
+        U[0] = (p.gamma - (dlog(pr) - p.gamma * dlog(Q[0]))) * p.inv_gm1 - R(0.5) * rV2 * ip;
+        U[1] = Q[1] * ip;
+        U[2] = Q[2] * ip;
+        U[3] = Q[3] * ip;
+        U[4] = -Q[0] * ip;
+    } else {
+        U[0] = Q[0];
+        U[1] = Q[1] * irho;
+        U[2] = Q[2] * irho;
+        U[3] = Q[3] * irho;
+        U[4] = p.gammaM2 * pr * irho;
+    }
+}
+
+// Physics_NS.f90:246-414 ViscousFlux_STATE / _ENTROPY / _ENERGY (beta = 0): F[c][v] cartesian
+// component c, from the gradients Ux, Uy, Uz of the gradient variables.
 template <typename R>
 __device__ __forceinline__ void viscous_flux(const PhysR<R>& p, const R* Q, const R* Ux, const R* Uy, const R* Uz,
                                              R mu, R kappa, R F[3][5]) {
     const R invRho = R(1) / Q[0];
     const R u = Q[1] * invRho, v = Q[2] * invRho, w = Q[3] * invRho;
-    const R ud[3] = {u * invRho, v * invRho, w * invRho};
     R ux[3], uy[3], uz[3];
+    R nTx, nTy, nTz;
+    if (p.grad_vars == 0) {
+        const R ud[3] = {u * invRho, v * invRho, w * invRho};
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        ux[c] = invRho * Ux[1 + c] - ud[c] * Ux[0];
-        uy[c] = invRho * Uy[1 + c] - ud[c] * Uy[0];
-        uz[c] = invRho * Uz[1 + c] - ud[c] * Uz[0];
+        for (int c = 0; c < 3; ++c) {
+            ux[c] = invRho * Ux[1 + c] - ud[c] * Ux[0];
+            uy[c] = invRho * Uy[1 + c] - ud[c] * Uy[0];
+            uz[c] = invRho * Uz[1 + c] - ud[c] * Uz[0];
+        }
+        const R g = p.gm1_gammaM2;
+        const R e2 = (Q[4] + p.e_ref) * invRho * invRho;
+        nTx = g * (invRho * Ux[4] - e2 * Ux[0] - u * ux[0] - v * ux[1] - w * ux[2]);
+        nTy = g * (invRho * Uy[4] - e2 * Uy[0] - u * uy[0] - v * uy[1] - w * uy[2]);
+        nTz = g * (invRho * Uz[4] - e2 * Uz[0] - u * uz[0] - v * uz[1] - w * uz[2]);
+    } else if (p.grad_vars == 1) {
+        const R pdr = p.gm1 * invRho * (Q[4] - R(0.5) * (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) * invRho) +
+                      p.p_ref * invRho;
+        const R um[3] = {u, v, w};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            ux[c] = pdr * (Ux[1 + c] + um[c] * Ux[4]);
+            uy[c] = pdr * (Uy[1 + c] + um[c] * Uy[4]);
+            uz[c] = pdr * (Uz[1 + c] + um[c] * Uz[4]);
+        }
+        const R g = p.gammaM2 * (pdr * pdr);
+        nTx = g * Ux[4];
+        nTy = g * Uy[4];
+        nTz = g * Uz[4];
+    } else {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            ux[c] = Ux[1 + c];
+            uy[c] = Uy[1 + c];
+            uz[c] = Uz[1 + c];
+        }
+        nTx = Ux[4];
+        nTy = Uy[4];
+        nTz = Uz[4];
     }
-    const R g = p.gm1_gammaM2;
-    const R e2 = (Q[4] + p.e_ref) * invRho * invRho;
-    const R nTx = g * (invRho * Ux[4] - e2 * Ux[0] - u * ux[0] - v * ux[1] - w * ux[2]);
-    const R nTy = g * (invRho * Uy[4] - e2 * Uy[0] - u * uy[0] - v * uy[1] - w * uy[2]);
-    const R nTz = g * (invRho * Uz[4] - e2 * Uz[0] - u * uz[0] - v * uz[1] - w * uz[2]);
     const R divV = ux[0] + uy[1] + uz[2];
     const R tt = R(2) / R(3) * divV;
     const R txx = mu * (R(2) * ux[0] - tt);

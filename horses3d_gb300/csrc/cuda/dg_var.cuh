@@ -91,6 +91,10 @@ struct VArgs {
     const R* jac;
     const R* inv_jac;
     const double* x;
+    // Mixed form on geometries that are not free-stream preserving: per node, the momentum residual
+    // of the state at rest with unit pressure (3 values), added times p_ref in the update; null when
+    // the geometry preserves a uniform state to round-off.
+    const double* pstat;
     const R* fn;                // face points, 3 per point
     const R* ft1;
     const R* ft2;
@@ -240,12 +244,25 @@ __global__ void __launch_bounds__(256) kv_volume(VArgs<R> a, int store_grad) {
     load_ops(a.ops, sO, px, py, pz);
     const PhysR<R> ph = a.ph[d.kase];
     const double eref = a.cc[d.kase].e_ref;
+    // sQ holds the gradient variables while the gradient is formed: the state itself, or U(Q) for
+    // the entropy and energy variables (then the fluxes below read the state from global memory)
+    const bool gv = a.ns && ph.grad_vars != 0;
     for (int t = threadIdx.x; t < ntot; t += blockDim.x) {
         const int le = t / np, n = t - le * np;
         const long long g = a.eoff[a.item_elems[d.first + le]] + n;
+        R x[5];
 #pragma unroll
-        for (int v = 0; v < 4; ++v) sQ[v * ntot + t] = R(a.Q[5 * g + v]);
-        sQ[4 * ntot + t] = R(a.Q[5 * g + 4] - eref);
+        for (int v = 0; v < 4; ++v) x[v] = R(a.Q[5 * g + v]);
+        x[4] = R(a.Q[5 * g + 4] - eref);
+        if (gv) {
+            R u[5];
+            gradient_variables(ph, x, u);
+#pragma unroll
+            for (int v = 0; v < 5; ++v) sQ[v * ntot + t] = u[v];
+        } else {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) sQ[v * ntot + t] = x[v];
+        }
     }
     __syncthreads();
     if (a.ns) {
@@ -335,8 +352,14 @@ __global__ void __launch_bounds__(256) kv_volume(VArgs<R> a, int store_grad) {
         const int le = t / np, n = t - le * np;
         const long long g = a.eoff[a.item_elems[d.first + le]] + n;
         R q[5], jx[3], je[3], jz[3];
+        if (gv) {
 #pragma unroll
-        for (int v = 0; v < 5; ++v) q[v] = sQ[v * ntot + t];
+            for (int v = 0; v < 4; ++v) q[v] = R(a.Q[5 * g + v]);
+            q[4] = R(a.Q[5 * g + 4] - eref);
+        } else {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) q[v] = sQ[v * ntot + t];
+        }
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             jx[c] = a.ja_xi[3 * g + c];
@@ -526,9 +549,18 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS) kv_face(VArgs<R> a)
         const R n[3] = {a.fn[3 * gp], a.fn[3 * gp + 1], a.fn[3 * gp + 2]};
         const R J = a.fj[gp];
         if (MODE == kJump) {
+            const PhysR<R> ph = a.ph[kase];
+            R QL[5], QR[5], UL[5], UR[5];
 #pragma unroll
             for (int v = 0; v < 5; ++v) {
-                const R u = R(0.5) * (XR[v * NP + lane] - XL[v * NP + lane]) * J;
+                QL[v] = XL[v * NP + lane];
+                QR[v] = XR[v * NP + lane];
+            }
+            gradient_variables(ph, QL, UL);
+            gradient_variables(ph, QR, UR);
+#pragma unroll
+            for (int v = 0; v < 5; ++v) {
+                const R u = R(0.5) * (UR[v] - UL[v]) * J;
                 out[v] = u * n[0];
                 out[5 + v] = u * n[1];
                 out[10 + v] = u * n[2];
@@ -689,9 +721,12 @@ __global__ void __launch_bounds__(128) kv_face_direct(VArgs<R> a) {
     }
     R out[NVOUT];
     if (MODE == kJump) {
+        R UL[5], UR[5];
+        gradient_variables(a.ph[fd.w], QL, UL);
+        gradient_variables(a.ph[fd.w], QR, UR);
 #pragma unroll
         for (int v = 0; v < 5; ++v) {
-            const R u = R(0.5) * (QR[v] - QL[v]) * J;
+            const R u = R(0.5) * (UR[v] - UL[v]) * J;
             out[v] = u * n[0];
             out[5 + v] = u * n[1];
             out[10 + v] = u * n[2];
@@ -794,6 +829,11 @@ __global__ void __launch_bounds__(256) kv_update(VArgs<R> a, int stage, double t
                                 cc.kappa, S);
 #pragma unroll
             for (int v = 0; v < 5; ++v) qd[v] = R(double(qd[v]) + S[v]);
+        }
+        if (a.pstat) {
+            const double pr = cc.gm1 * cc.e_ref;  // the pressure the momentum fluxes leave out
+#pragma unroll
+            for (int c = 0; c < 3; ++c) qd[1 + c] = R(double(qd[1 + c]) + pr * a.pstat[3 * g + c]);
         }
         if (write_qdot) {
 #pragma unroll

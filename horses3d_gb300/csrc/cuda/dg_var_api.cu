@@ -97,6 +97,7 @@ dg::PhysConst phys_const(const dg_physics* ph, const dg_options* op) {
     pc.averaging = op->averaging;
     pc.inviscid = op->inviscid;
     pc.source = op->source;
+    pc.grad_vars = pc.ns ? op->gradient_variables : 0;
     return pc;
 }
 
@@ -337,6 +338,66 @@ ItemTable build_items(const std::vector<int>& eord, const std::vector<int>& ecas
     return t;
 }
 
+// The reference's discretisation is not free-stream preserving where curved faces join elements of
+// different orders: the two sides' metric terms, interpolated to the face points with Tset, do not
+// match, and a fluid at rest at pressure p gets the momentum residual p G(x). The mixed form leaves
+// the constant p_ref out of its FP32 momentum fluxes (exact where G = 0), so it adds p_ref G back in
+// the update. G is the FP64 right-hand side of the state at rest with unit pressure (no source),
+// computed once here with the FP64 kernels and FP64 item sizes; where its largest value is round-off
+// (straight or conforming meshes) nothing is added.
+int static_pressure_residual(dg_ctx* c, const Gathered& h) {
+    cudaStream_t s = c->stream;
+    const size_t nd = static_cast<size_t>(c->ndof);
+    const ItemTable t = build_items(c->h_eord, c->h_ecase, -1, false, c->pc.ns != 0, c->nodes);
+    h3dctx::DevBuf<int4> items;
+    h3dctx::DevBuf<int> elems;
+    h3dctx::VStore<double> st;
+    auto done = [&](int rc) {
+        st.free();
+        items.free();
+        elems.free();
+        return rc;
+    };
+    cudaError_t e;
+    if ((e = items.upload(t.items.data(), t.items.size(), s)) || (e = elems.upload(t.elems.data(), t.elems.size(), s)))
+        return done(cuda_fail(e, "static pressure items"));
+    int rc = setup_vstore(c, st, h);
+    if (rc) return done(rc);
+    dg::VArgs<double>& a = st.args;
+    a.items = items.p;
+    a.item_elems = elems.p;
+    a.n_items = static_cast<int>(t.items.size());
+    a.cap = t.cap;
+    for (int q = 0; q <= dg::kItemClasses; ++q) a.cls[q] = t.cls[q];
+    for (int q = 0; q < dg::kItemClasses; ++q) a.ccap[q] = t.ccap[q];
+    a.source = DG_SOURCE_NONE;
+    const dg::VStageFn<double> fn = dg::vstage_fn_fp64();
+    std::vector<double> q(5 * nd);
+    for (size_t g = 0; g < nd; ++g) {
+        q[5 * g] = 1.0;
+        q[5 * g + 1] = q[5 * g + 2] = q[5 * g + 3] = 0.0;
+        q[5 * g + 4] = 1.0 / c->pc.gm1;
+    }
+    if ((e = cudaMemcpyAsync(c->Q.p, q.data(), sizeof(double) * q.size(), cudaMemcpyHostToDevice, s)) ||
+        (e = fn(a, dg::kPrepare, 0.0, 0, s)) || (e = fn(a, dg::kTraces, 0.0, 0, s)) ||
+        (e = fn(a, -1, 0.0, dg::kWriteQDot, s)) ||
+        (e = cudaMemcpyAsync(q.data(), st.QDot.p, sizeof(double) * q.size(), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaMemsetAsync(c->Q.p, 0, sizeof(double) * q.size(), s)) || (e = cudaStreamSynchronize(s)))
+        return done(cuda_fail(e, "static pressure residual"));
+    std::vector<double> g3(3 * nd);
+    double mx = 0.0;
+    for (size_t g = 0; g < nd; ++g)
+        for (int d = 0; d < 3; ++d) {
+            g3[3 * g + d] = q[5 * g + 1 + d];
+            mx = std::max(mx, std::fabs(g3[3 * g + d]));
+        }
+    if (mx > 1e-10) {
+        if ((e = c->pstat.upload(g3.data(), g3.size(), s)) != cudaSuccess)
+            return done(cuda_fail(e, "static pressure upload"));
+    }
+    return done(DG_OK);
+}
+
 }  // namespace
 
 namespace h3dvar {
@@ -363,6 +424,8 @@ int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, cons
         return h3d::fail(DG_ERR_UNSUPPORTED, "precision");
     if (op->source < DG_SOURCE_NONE || op->source > DG_SOURCE_MMS_LAMB_VECTOR)
         return h3d::fail(DG_ERR_UNSUPPORTED, "source");
+    if (op->gradient_variables < DG_GRADVARS_STATE || op->gradient_variables > DG_GRADVARS_ENERGY)
+        return h3d::fail(DG_ERR_UNSUPPORTED, "gradient variables");
     for (int k = 0; k < n_cases; ++k) {
         int rc = validate_case(&meshes[k], &phys[k], k);
         if (rc) return rc;
@@ -553,7 +616,9 @@ int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, cons
     }
     int rc;
     if (c->mixed) {
+        if ((rc = static_pressure_residual(c, h))) return bail(rc);
         if ((rc = setup_vstore(c, c->v32, h))) return bail(rc);
+        c->v32.args.pstat = c->pstat.p;
         c->v32.args.cap = cap;
         c->v32.stage = dg::vstage_fn_fp32();
         c->v32.times = dg::vtimes_fn_fp32();
@@ -578,6 +643,7 @@ void release(dg_ctx* c) {
     for (auto* b : {&c->item_elems, &c->eord, &c->vnan, &c->nc_faces, &c->direct_faces}) b->free();
     for (auto* b : {&c->eoff, &c->soff, &c->foff}) b->free();
     c->cc.free();
+    c->pstat.free();
     c->dxi_table.free();
     c->gamma_M2.free();
 }

@@ -58,6 +58,8 @@ enum { DG_AVG_STANDARD = 0, DG_AVG_PIROZZOLI = 1,                  /* "averaging
        DG_AVG_KENNEDY_GRUBER = 4,                                  /*  Roe and Rusanov, and the */
        DG_AVG_ENTROPY_CONSERVING = 5, DG_AVG_CHANDRASEKAR = 6 };   /*  split form's two-point fluxes) */
 enum { DG_PRECISION_FP64 = 0, DG_PRECISION_MIXED = 1 };            /* plain FP64 / FP32 flux form */
+enum { DG_GRADVARS_STATE = 0, DG_GRADVARS_ENTROPY = 1,             /* "gradient variables" of BR1 */
+       DG_GRADVARS_ENERGY = 2 };
 enum { DG_SOURCE_NONE = 0,                                         /* UserDefinedSourceTermNS of */
        DG_SOURCE_MMS_CONVERGENCE = 1,                              /*  NavierStokes/Convergence */
        DG_SOURCE_MMS_LAMB_VECTOR = 2 };                            /*  NavierStokes/LambVector */
@@ -106,6 +108,7 @@ typedef struct dg_options {
     double lambda_stab;             /* LxF stabilisation factor, reference default 1.0 */
     int32_t precision;              /* DG_PRECISION_* */
     int32_t source;                 /* DG_SOURCE_* */
+    int32_t gradient_variables;     /* DG_GRADVARS_* (SpatialDiscretization.f90:106-148) */
 } dg_options;
 
 typedef struct dg_ctx dg_ctx;

@@ -200,6 +200,7 @@ struct Phys {
     double gamma = 1.4, gm1 = 1.4 - 1.0, Mach, Re, Pr, mu, kappa, mu_to_kappa, gammaM2;  // PhysicsStorage_NS.f90:115-133
     double S_div_TRef, TReNorm;
     bool ns;
+    int grad_vars = DG_GRADVARS_STATE;
 };
 
 static inline double pressure(const Phys& p, const double* Q) {  // VariableConversion_NS.f90:44-57
@@ -225,22 +226,69 @@ static void euler_flux(const Phys& p, const double* Q, double* F) {
     F[10] = Q[3]; F[11] = F[3]; F[12] = F[8]; F[13] = Q[3] * w + pr; F[14] = (Q[4] + pr) * w;
 }
 
-// Physics_NS.f90:246-303 ViscousFlux_STATE.
+// VariableConversion_NS.f90:196-262 NSGradientVariables_STATE / _ENTROPY / _ENERGY.
+static void gradient_variables(const Phys& p, const double* Q, double* U) {
+    if (p.grad_vars == DG_GRADVARS_STATE) {
+        for (int v = 0; v < 5; ++v) U[v] = Q[v];
+        return;
+    }
+    const double invRho = 1.0 / Q[0];
+    const double rhoV2 = (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) * invRho;
+    const double pr = p.gm1 * (Q[4] - 0.5 * rhoV2);
+    if (p.grad_vars == DG_GRADVARS_ENTROPY) {
+        const double invP = 1.0 / pr;
+        U[0] = (p.gamma - (std::log(pr) - p.gamma * std::log(Q[0]))) * (1.0 / (1.4 - 1.0)) - 0.5 * rhoV2 * invP;
+        U[1] = Q[1] * invP;
+        U[2] = Q[2] * invP;
+        U[3] = Q[3] * invP;
+        U[4] = -Q[0] * invP;
+    } else {
+        U[0] = Q[0];
+        U[1] = Q[1] * invRho;
+        U[2] = Q[2] * invRho;
+        U[3] = Q[3] * invRho;
+        U[4] = p.gammaM2 * pr * invRho;
+    }
+}
+
+// Physics_NS.f90:246-414 ViscousFlux_STATE, ViscousFlux_ENTROPY, ViscousFlux_ENERGY.
 static void viscous_flux(const Phys& p, const double* Q, const double* Ux, const double* Uy, const double* Uz,
                          double mu, double beta, double kappa, double* F) {
     const double invRho = 1.0 / Q[0];
     const double u = Q[1] * invRho, v = Q[2] * invRho, w = Q[3] * invRho;
-    const double ud[3] = {u * invRho, v * invRho, w * invRho};
-    double ux[3], uy[3], uz[3];
-    for (int c = 0; c < 3; ++c) {
-        ux[c] = invRho * Ux[1 + c] - ud[c] * Ux[0];
-        uy[c] = invRho * Uy[1 + c] - ud[c] * Uy[0];
-        uz[c] = invRho * Uz[1 + c] - ud[c] * Uz[0];
+    double ux[3], uy[3], uz[3], nTx, nTy, nTz;
+    if (p.grad_vars == DG_GRADVARS_STATE) {
+        const double ud[3] = {u * invRho, v * invRho, w * invRho};
+        for (int c = 0; c < 3; ++c) {
+            ux[c] = invRho * Ux[1 + c] - ud[c] * Ux[0];
+            uy[c] = invRho * Uy[1 + c] - ud[c] * Uy[0];
+            uz[c] = invRho * Uz[1 + c] - ud[c] * Uz[0];
+        }
+        const double g = p.gm1 * p.gammaM2;
+        nTx = g * (invRho * Ux[4] - Q[4] * invRho * invRho * Ux[0] - u * ux[0] - v * ux[1] - w * ux[2]);
+        nTy = g * (invRho * Uy[4] - Q[4] * invRho * invRho * Uy[0] - u * uy[0] - v * uy[1] - w * uy[2]);
+        nTz = g * (invRho * Uz[4] - Q[4] * invRho * invRho * Uz[0] - u * uz[0] - v * uz[1] - w * uz[2]);
+    } else if (p.grad_vars == DG_GRADVARS_ENTROPY) {
+        const double pdr = p.gm1 * invRho * (Q[4] - 0.5 * (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) * invRho);
+        const double um[3] = {u, v, w};
+        for (int c = 0; c < 3; ++c) {
+            ux[c] = pdr * (Ux[1 + c] + um[c] * Ux[4]);
+            uy[c] = pdr * (Uy[1 + c] + um[c] * Uy[4]);
+            uz[c] = pdr * (Uz[1 + c] + um[c] * Uz[4]);
+        }
+        nTx = p.gammaM2 * (pdr * pdr) * Ux[4];
+        nTy = p.gammaM2 * (pdr * pdr) * Uy[4];
+        nTz = p.gammaM2 * (pdr * pdr) * Uz[4];
+    } else {
+        for (int c = 0; c < 3; ++c) {
+            ux[c] = Ux[1 + c];
+            uy[c] = Uy[1 + c];
+            uz[c] = Uz[1 + c];
+        }
+        nTx = Ux[4];
+        nTy = Uy[4];
+        nTz = Uz[4];
     }
-    const double g = p.gm1 * p.gammaM2;
-    const double nTx = g * (invRho * Ux[4] - Q[4] * invRho * invRho * Ux[0] - u * ux[0] - v * ux[1] - w * ux[2]);
-    const double nTy = g * (invRho * Uy[4] - Q[4] * invRho * invRho * Uy[0] - u * uy[0] - v * uy[1] - w * uy[2]);
-    const double nTz = g * (invRho * Uz[4] - Q[4] * invRho * invRho * Uz[0] - u * uz[0] - v * uz[1] - w * uz[2]);
     const double divV = ux[0] + uy[1] + uz[2];
     F[0] = 0.0;
     F[1] = mu * (2.0 * ux[0] - 2.0 / 3.0 * divV) + beta * divV;
@@ -1113,7 +1161,9 @@ static void compute_rhs(Solver& s, double t) {
             const Nodal& sy = nodal(s.nodes, e.N[1]);
             const Nodal& sz = nodal(s.nodes, e.N[2]);
             const int px = e.P[0], py = e.P[1], pz = e.P[2], np = px * py * pz;
-            const double* U = &s.Q[5 * e.off];
+            std::vector<double> Uv(5 * np);  // GetGradients at the nodes (HexElementClass.f90:463-470)
+            for (int q = 0; q < np; ++q) gradient_variables(s.ph, &s.Q[5 * (e.off + q)], &Uv[5 * q]);
+            const double* U = Uv.data();
             std::vector<double> Uxi(5 * np, 0.0), Ueta(5 * np, 0.0), Uzeta(5 * np, 0.0);
             auto n = [&](int i, int j, int k) { return i + px * (j + py * k); };
             for (int k = 0; k < pz; ++k) for (int j = 0; j < py; ++j) for (int l = 0; l < px; ++l) for (int i = 0; i < px; ++i)
@@ -1145,8 +1195,11 @@ static void compute_rhs(Solver& s, double t) {
                     const int p = i + q1 * j;
                     const double J = s.fj[f.off + p];
                     const double* n = &s.fn[3 * (f.off + p)];
+                    double UL[5], UR[5];
+                    gradient_variables(s.ph, &f.Q[0][5 * p], UL);
+                    gradient_variables(s.ph, &f.Q[1][5 * p], UR);
                     for (int v = 0; v < 5; ++v) {
-                        const double u = 0.5 * (f.Q[1][5 * p + v] - f.Q[0][5 * p + v]) * J;
+                        const double u = 0.5 * (UR[v] - UL[v]) * J;
                         us[15 * p + v] = u * n[0];
                         us[15 * p + 5 + v] = u * n[1];
                         us[15 * p + 10 + v] = u * n[2];
@@ -1445,6 +1498,7 @@ void* orc_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* 
     s->ph.Re = ph->reynolds;
     s->ph.Pr = ph->prandtl;
     s->ph.ns = ph->navier_stokes != 0;
+    s->ph.grad_vars = s->ph.ns ? op->gradient_variables : DG_GRADVARS_STATE;
     // PhysicsStorage_NS.f90:186-290,413-429
     s->ph.gammaM2 = s->ph.gamma * (ph->mach * ph->mach);
     if (s->ph.ns) {

@@ -40,6 +40,39 @@ def convergence_case(order=7, precision=_abi.DG_PRECISION_FP64):
     return mesh, cfg, q0
 
 
+def convergence_variant_case(variant, precision=_abi.DG_PRECISION_FP64):
+    """NavierStokes/Convergence_energy and Convergence_entropy: the Convergence case on Gauss-Lobatto
+    nodes in split form at CFL 1, with the energy gradient variables (Roe, Pirozzoli) or the entropy
+    gradient variables (matrix dissipation, Chandrasekar) (Convergence_*/Convergence.control)."""
+    mesh = HexMesh.box(4, [-1, 0, -1], [1, 2, 1], 7, node_type=_abi.DG_NODES_GAUSS_LOBATTO)
+    if variant == "energy":
+        riemann, avg, gv = _abi.DG_RIEMANN_ROE, _abi.DG_AVG_PIROZZOLI, _abi.DG_GRADVARS_ENERGY
+    else:
+        riemann, avg, gv = _abi.DG_RIEMANN_MATRIX_DISS, _abi.DG_AVG_CHANDRASEKAR, _abi.DG_GRADVARS_ENTROPY
+    cfg = Config(order=7, nodes=_abi.DG_NODES_GAUSS_LOBATTO, mach=0.3, reynolds=10.0, riemann=riemann,
+                 inviscid=_abi.DG_INVISCID_SPLIT, averaging=avg, gradient_variables=gv, precision=precision,
+                 source=_abi.DG_SOURCE_MMS_CONVERGENCE, cfl=1.0, dcfl=1.0e5, t_final=1.0, n_steps=1000000)
+    q0, _ = problems.mms_convergence_state(mesh.x, 0.0)
+    return mesh, cfg, q0
+
+
+# Goldens of Convergence_energy and Convergence_entropy (SETUP/ProblemFile.f90:618-633, tol 1e-11 on x+1).
+CONVERGENCE_VARIANT_GOLDENS = {
+    "energy": (np.array([6.2838924111412731E-01, 1.8880402299553984E+00, 2.5257816906017094E+00,
+                         4.4137338696617938E+00, 2.5153751482782658E+00]),
+               np.array([6.7174769052792914E-06, 7.8936751849804373E-06, 2.8203611177044557E-06,
+                         6.6884144365250127E-06, 1.4116624697295942E-05]),
+               np.array([1.2370219075207763E-04, 1.1813999720732922E-04, 4.0653170754839378E-05,
+                         1.2358578587070169E-04, 2.1723315094097264E-04])),
+    "entropy": (np.array([6.2929844029491377E-01, 1.8894710750845625E+00, 2.5264755519384234E+00,
+                          4.4146672499485859E+00, 2.5157533917446182E+00]),
+                np.array([3.3102799903292017E-05, 3.6405407003671022E-05, 1.5957629488942332E-05,
+                          3.4132613560424396E-05, 6.6811198249671421E-05]),
+                np.array([9.2273153574772720E-04, 9.6259031804949867E-04, 3.8474183309141608E-04,
+                          8.7717012428247660E-04, 1.6750805236722724E-03])),
+}
+
+
 # Goldens of Solver/test/NavierStokes/Convergence/SETUP/ProblemFile.f90:617-635 (tol 1e-11 on x+1).
 CONVERGENCE_RESIDUALS = np.array([6.2801762330611588E-01, 1.8889640334957627E+00, 2.5256897695536247E+00,
                                   4.4142472296503827E+00, 2.5163928650671146E+00])

@@ -49,6 +49,7 @@ def test_create_validates_before_touching_the_device():
     assert _ctx_create(mesh, Config(mach=-1.0)) == _abi.DG_ERR_INVALID
     assert _ctx_create(mesh, Config(riemann=10)) == _abi.DG_ERR_UNSUPPORTED
     assert _ctx_create(mesh, Config(averaging=7)) == _abi.DG_ERR_UNSUPPORTED
+    assert _ctx_create(mesh, Config(gradient_variables=3)) == _abi.DG_ERR_UNSUPPORTED
     big = HexMesh.box(1, [0, 0, 0], [1, 1, 1], 8, node_type=_abi.DG_NODES_GAUSS)
     assert _ctx_create(big, Config()) == _abi.DG_ERR_UNSUPPORTED
 
@@ -176,6 +177,11 @@ def test_riemann_and_averaging_keys():
         assert parse_control(f"riemann solver = {k}\nreynolds number = 1\n").riemann == v
     for k, v in (("entropy conserving", _abi.DG_AVG_ENTROPY_CONSERVING), ("Chandrasekar", _abi.DG_AVG_CHANDRASEKAR)):
         assert parse_control(f"averaging = {k}\nreynolds number = 1\n").averaging == v
+    for k, v in (("state", _abi.DG_GRADVARS_STATE), ("Entropy", _abi.DG_GRADVARS_ENTROPY),
+                 ("energy", _abi.DG_GRADVARS_ENERGY)):
+        assert parse_control(f"gradient variables = {k}\nreynolds number = 1\n").gradient_variables == v
+    with pytest.raises(UnsupportedOption):
+        parse_control("gradient variables = primitive\nreynolds number = 1\n")
 
 
 def test_anisotropic_order_keys(tmp_path):

@@ -314,3 +314,34 @@ def test_lamb_vector_source_on_per_element_orders():
     q0 = cases.problems.mms_lamb_vector_state(mesh.x, 0.0)
     _check_rhs(mesh, cfg, q0, t=0.03)
     _check_steps(mesh, cfg, q0, 5, 0.005)
+
+
+@pytest.mark.parametrize("variant", ["energy", "entropy"])
+def test_convergence_variants_on_gpu_reach_the_reference_goldens(variant):
+    """Convergence_energy / Convergence_entropy on the GPU: split form on Gauss-Lobatto nodes with the
+    energy or entropy gradient variables (Roe + Pirozzoli, matrix dissipation + Chandrasekar)."""
+    mesh, cfg, q0 = cases.convergence_variant_case(variant)
+    g = NavierStokesDG(mesh, cfg)
+    g.set_state(q0)
+    rep = g.integrate_in_time(t0=0.0, compute_after_steps=True)
+    assert rep.iterations == 137
+    err, qerr = cases.convergence_errors(mesh, g.Q, g.QDot, rep.time)
+    gres, gerr, gqerr = cases.CONVERGENCE_VARIANT_GOLDENS[variant]
+    assert cases.ftassert_close(gres, rep.residuals), rep.residuals - gres
+    assert cases.ftassert_close(gerr, err), err - gerr
+    assert cases.ftassert_close(gqerr, qerr), qerr - gqerr
+
+
+@pytest.mark.parametrize("gv", [_abi.DG_GRADVARS_ENTROPY, _abi.DG_GRADVARS_ENERGY])
+@pytest.mark.parametrize("nodes", [_abi.DG_NODES_GAUSS, _abi.DG_NODES_GAUSS_LOBATTO])
+def test_gradient_variables(gv, nodes):
+    """BR1 with the entropy and energy gradient variables (VariableConversion_NS.f90:211-262,
+    Physics_NS.f90:306-414) on a curvilinear mesh: RHS and lifted gradients, steps, mixed form."""
+    import dataclasses
+
+    mesh, cfg, q0 = cases.tgv_case(n=3, order=4, nodes=nodes, warp=0.1, mach=0.3, perturbation=0.02, seed=8)
+    cfg = dataclasses.replace(cfg, gradient_variables=gv)
+    _check_rhs(mesh, cfg, q0)
+    _check_steps(mesh, cfg, q0, steps=2, dt=2e-3)
+    mixed = dataclasses.replace(cfg, precision=_abi.DG_PRECISION_MIXED)
+    _check_steps(mesh, mixed, q0, steps=2, dt=2e-3, tol=MIXED_TOL)

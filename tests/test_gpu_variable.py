@@ -283,3 +283,18 @@ def test_batch_save_and_restart_one_case(tmp_path):
     c2.set_clock(np.array([0.0, t1, 0.0]), dts)
     c2.run_steps(2)
     assert np.array_equal(c2.get()[1], b.get()[1])
+
+
+@pytest.mark.parametrize("gv", [_abi.DG_GRADVARS_STATE, _abi.DG_GRADVARS_ENTROPY, _abi.DG_GRADVARS_ENERGY])
+def test_anisotropic_gradient_variables(gv):
+    """State, entropy and energy gradient variables on per-element orders of a curvilinear mesh: the
+    BR1 jumps are formed from the face-point states of both sides after the Tset interpolation. The
+    mixed form includes the static-pressure residual of this non-free-stream-preserving geometry."""
+    import dataclasses
+
+    mesh, cfg, q0 = cases.aniso_tgv_case(n=3, lo=1, hi=4, seed=41, warp=0.1, riemann=_abi.DG_RIEMANN_LXF)
+    cfg = dataclasses.replace(cfg, gradient_variables=gv)
+    _check_rhs(mesh, cfg, q0)
+    _check_steps(mesh, cfg, q0, steps=2, dt=2e-3)
+    mixed = dataclasses.replace(cfg, precision=_abi.DG_PRECISION_MIXED)
+    _check_steps(mesh, mixed, q0, steps=2, dt=2e-3, tol=MIXED_TOL)

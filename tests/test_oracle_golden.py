@@ -44,6 +44,19 @@ def test_convergence_goldens_generated_mesh():
     assert cases.ftassert_close(cases.CONVERGENCE_QDOT_ERRORS, qerr), qerr - cases.CONVERGENCE_QDOT_ERRORS
 
 
+@pytest.mark.parametrize("variant", ["energy", "entropy"])
+def test_convergence_variant_goldens(variant):
+    """Convergence_energy (split form, Pirozzoli, Roe, energy gradient variables) and
+    Convergence_entropy (split form, Chandrasekar, matrix dissipation, entropy gradient variables)."""
+    mesh, cfg, _ = cases.convergence_variant_case(variant)
+    it, res, err, qerr, nan = _run_convergence(mesh, cfg)
+    assert not nan
+    gres, gerr, gqerr = cases.CONVERGENCE_VARIANT_GOLDENS[variant]
+    assert cases.ftassert_close(gres, res), res - gres
+    assert cases.ftassert_close(gerr, err), err - gerr
+    assert cases.ftassert_close(gqerr, qerr), qerr - gqerr
+
+
 @pytest.mark.skipif(not REF_MESH.exists(), reason="reference mesh file not mounted")
 def test_convergence_goldens_reference_mesh_file():
     _, cfg, _ = cases.convergence_case()
