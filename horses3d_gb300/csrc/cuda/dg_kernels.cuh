@@ -604,7 +604,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
 // ------------------------------------------------------------------------------------------------
 // k_flux: f* = (F_inv(QL,QR) - 1/2 (Fv_L.n + Fv_R.n)) Jf; side 1 gets f*, side 2 gets -f*.
 // ------------------------------------------------------------------------------------------------
-template <int P, typename R>
+template <int P, typename R, bool GEN>
 __global__ void __launch_bounds__(128) k_flux(Args<R> a) {
     constexpr int P2 = P * P;
     const int64_t nfp = static_cast<int64_t>(a.F) * P2;
@@ -622,14 +622,18 @@ __global__ void __launch_bounds__(128) k_flux(Args<R> a) {
     const R n[3] = {a.fn[gid], a.fn[nfp + gid], a.fn[2 * nfp + gid]};
     const R J = a.fj[gid];
     R inv[5];
-    if (a.ph.riemann == 0) {
+    if (GEN) {  // standard Roe, Roe-Pike, low-dissipation Roe, matrix dissipation, viscous NS
+        const R t1[3] = {a.ft1[gid], a.ft1[nfp + gid], a.ft1[2 * nfp + gid]};
+        const R t2[3] = {a.ft2[gid], a.ft2[nfp + gid], a.ft2[2 * nfp + gid]};
+        riemann_flux(a.ph, QL, QR, n, t1, t2, inv);
+    } else if (a.ph.riemann == 0) {
         roe_flux(a.ph, QL, QR, n, inv);
     } else if (a.ph.riemann == 3) {
         rusanov_flux(a.ph, QL, QR, n, inv);
-    } else {
+    } else {  // LxF, central, u-diss
         const R t1[3] = {a.ft1[gid], a.ft1[nfp + gid], a.ft1[2 * nfp + gid]};
         const R t2[3] = {a.ft2[gid], a.ft2[nfp + gid], a.ft2[2 * nfp + gid]};
-        riemann_flux(a.ph, QL, QR, n, t1, t2, inv);  // the solvers that need the tangents
+        lxf_flux<R, false>(a.ph, QL, QR, n, t1, t2, inv);
     }
     R vL[5] = {0, 0, 0, 0, 0}, vR[5] = {0, 0, 0, 0, 0};
     if (a.ph.ns) {

@@ -34,6 +34,14 @@ void launch_update(const Args<R>& a, int blocks, int stage, double tshift, int w
     else k_update<P, GL, SRC, R><<<blocks, Geo<P>::THREADS, 0, s>>>(a, stage, tshift, wq);
 }
 
+// The interface-flux kernel in its common variant (Roe, LxF, central, Rusanov, u-diss with the
+// averages 0-4) or the generic one with the other solvers and the logarithmic-mean averages.
+template <int P, typename R>
+void launch_flux(const Args<R>& a, int blocks, cudaStream_t s) {
+    if ((a.ph.riemann >= 4 && a.ph.riemann <= 8) || a.ph.averaging >= 5) k_flux<P, R, true><<<blocks, 128, 0, s>>>(a);
+    else k_flux<P, R, false><<<blocks, 128, 0, s>>>(a);
+}
+
 template <int P, bool GL, typename R>
 cudaError_t run_stage(const Args<R>& a, int stage, double tshift, int flags, cudaStream_t s) {
     constexpr int EPB = Geo<P>::EPB, THREADS = Geo<P>::THREADS;
@@ -48,7 +56,7 @@ cudaError_t run_stage(const Args<R>& a, int stage, double tshift, int flags, cud
         return cudaGetLastError();
     }
     k_volume<P, GL, R><<<eblocks, THREADS, volume_smem_bytes<P, R>(a.inviscid), s>>>(a, flags & kStoreGrad);
-    k_flux<P, R><<<fblocks, 128, 0, s>>>(a);
+    launch_flux<P, R>(a, fblocks, s);
     if (a.source) launch_update<P, GL, true>(a, eblocks, stage, tshift, (flags & kWriteQDot) ? 1 : 0, s);
     else launch_update<P, GL, false>(a, eblocks, stage, tshift, (flags & kWriteQDot) ? 1 : 0, s);
     return cudaGetLastError();
@@ -77,7 +85,7 @@ cudaError_t kernel_times(const Args<R>& a, int reps, cudaStream_t s, double* ms)
         for (int r = 0; r < reps; ++r) {
             switch (kk) {
                 case 0: k_volume<P, GL, R><<<eblocks, THREADS, volume_smem_bytes<P, R>(a.inviscid), s>>>(a, 0); break;
-                case 1: k_flux<P, R><<<fblocks, 128, 0, s>>>(a); break;
+                case 1: launch_flux<P, R>(a, fblocks, s); break;
                 case 2: launch_update<P, GL, false>(a, eblocks, 1, 1.0 / 3.0, 0, s); break;
                 default: k_traces<P, GL, R><<<eblocks, THREADS, 0, s>>>(a); break;
             }

@@ -290,11 +290,13 @@ __device__ __forceinline__ void log_mean_state(const PhysR<R>& p, bool entropy_c
 // MorinishiAverage (:1850-1886), KennedyGruberAverage (:1888-1925), PirozzoliAverage (:1927-1962),
 // EntropyConservingAverage (:1964-2026), ChandrasekarAverage (:2028-2077).
 // Absolute energies and pressures are E' + e_ref, p' + p_ref; momentum fluxes carry p' only.
-template <typename R>
+// LM = false compiles the averages without the logarithmic means (callers that never see averages
+// 5 and 6 keep a smaller register footprint).
+template <typename R, bool LM = true>
 __device__ __forceinline__ void averaged_states(const PhysR<R>& p, const R* L, const R* Rt, R pL, R pR, R iL, R iR,
                                                 R* f) {
     const R uL = iL * L[1], uR = iR * Rt[1], vL = iL * L[2], vR = iR * Rt[2], wL = iL * L[3], wR = iR * Rt[3];
-    switch (p.averaging) {
+    switch (LM ? p.averaging : (p.averaging >= 5 ? 0 : p.averaging)) {
         case 5:
         case 6: {  // entropy conserving, Chandrasekar
             R rho, u, v, w, pm, h;
@@ -360,7 +362,7 @@ __device__ __forceinline__ void averaged_states(const PhysR<R>& p, const R* L, c
 
 // RiemannSolvers_NS.f90:1251-1334 LxFRiemannSolver (the averaging of the control file) and :375-428
 // CentralRiemannSolver, which is the same average with lambda_stab = 0 (SetRiemannSolver, :224).
-template <typename R>
+template <typename R, bool LM = true>
 __device__ __forceinline__ void lxf_flux(const PhysR<R>& p, const R* QL, const R* QR, const R* n, const R* t1,
                                          const R* t2, R* flux) {
     const R iL = R(1) / QL[0], iR = R(1) / QR[0];
@@ -375,7 +377,7 @@ __device__ __forceinline__ void lxf_flux(const PhysR<R>& p, const R* QL, const R
     const R Lr[5] = {QL[0], ruL, rvL, rwL, QL[4]};
     const R Rr[5] = {QR[0], ruR, rvR, rwR, QR[4]};
     R f[5];
-    averaged_states(p, Lr, Rr, pL, pR, iL, iR, f);
+    averaged_states<R, LM>(p, Lr, Rr, pL, pR, iL, iR, f);
     if (p.riemann != 2) {  // central fluxes carry no dissipation
         // u-diss (RiemannSolvers_NS.f90:1336-1425) drops the sound speeds
         const R aL = p.riemann == 9 ? R(0) : dsqrt(p.gamma * (pL + p.p_ref) * iL);

@@ -57,6 +57,7 @@ template <typename R>
 struct VArgs {
     int n_items, n_faces, cap;  // cap: largest node count of an item
     int ns, source;
+    int riemann, averaging, grad_vars;  // the host's copies of the solver, average and gradient variables
     int item0;                     // first item of the launch (the grid covers one class)
     int cls[kItemClasses + 1];     // class c holds items [cls[c], cls[c+1])
     int ccap[kItemClasses];        // largest node count of an item of class c (its shared memory)
@@ -482,7 +483,11 @@ __device__ __forceinline__ R* to_face_points(const R* tset, R* S, R* A, int s1, 
     return d2 ? nxt : cur;
 }
 
-template <typename R, int MODE>
+// V selects the compiled variant: for kJump, gradient variables other than the state (V = 1); for
+// the flux modes, the Riemann solvers beyond Roe / LxF / central / Rusanov / u-diss or the
+// logarithmic-mean averages (V = 1). The common variants (V = 0) keep the short code and register
+// footprint.
+template <typename R, int MODE, int V>
 __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS) kv_face(VArgs<R> a) {
     using Cfg = FaceCfg<R, MODE>;
     constexpr int NVIN = Cfg::NVIN, NVOUT = Cfg::NVOUT, NVB = Cfg::NVB, NP = kFacePts;
@@ -556,8 +561,16 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS) kv_face(VArgs<R> a)
                 QL[v] = XL[v * NP + lane];
                 QR[v] = XR[v * NP + lane];
             }
-            gradient_variables(ph, QL, UL);
-            gradient_variables(ph, QR, UR);
+            if (V) {
+                gradient_variables(ph, QL, UL);
+                gradient_variables(ph, QR, UR);
+            } else {
+#pragma unroll
+                for (int v = 0; v < 5; ++v) {
+                    UL[v] = QL[v];
+                    UR[v] = QR[v];
+                }
+            }
 #pragma unroll
             for (int v = 0; v < 5; ++v) {
                 const R u = R(0.5) * (UR[v] - UL[v]) * J;
@@ -573,14 +586,18 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS) kv_face(VArgs<R> a)
                 QL[v] = XL[v * NP + lane];
                 QR[v] = XR[v * NP + lane];
             }
-            if (ph.riemann == 0) {
+            if (V) {
+                const R t1[3] = {a.ft1[3 * gp], a.ft1[3 * gp + 1], a.ft1[3 * gp + 2]};
+                const R t2[3] = {a.ft2[3 * gp], a.ft2[3 * gp + 1], a.ft2[3 * gp + 2]};
+                riemann_flux(ph, QL, QR, n, t1, t2, inv);
+            } else if (ph.riemann == 0) {
                 roe_flux(ph, QL, QR, n, inv);
             } else if (ph.riemann == 3) {
                 rusanov_flux(ph, QL, QR, n, inv);
-            } else {
+            } else {  // LxF, central, u-diss
                 const R t1[3] = {a.ft1[3 * gp], a.ft1[3 * gp + 1], a.ft1[3 * gp + 2]};
                 const R t2[3] = {a.ft2[3 * gp], a.ft2[3 * gp + 1], a.ft2[3 * gp + 2]};
-                riemann_flux(ph, QL, QR, n, t1, t2, inv);  // the solvers that need the tangents
+                lxf_flux<R, false>(ph, QL, QR, n, t1, t2, inv);
             }
             R visc[5] = {0, 0, 0, 0, 0};
             if (MODE == kFluxNS) {
@@ -689,7 +706,7 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS) kv_face(VArgs<R> a)
 // one thread per face point reads both sides' traces in place, the right side re-indexed by
 // leftIndexes2Right, and writes both sides' results.
 // ------------------------------------------------------------------------------------------------
-template <typename R, int MODE>
+template <typename R, int MODE, int V>
 __global__ void __launch_bounds__(128) kv_face_direct(VArgs<R> a) {
     using Cfg = FaceCfg<R, MODE>;
     constexpr int NVOUT = Cfg::NVOUT;
@@ -722,8 +739,16 @@ __global__ void __launch_bounds__(128) kv_face_direct(VArgs<R> a) {
     R out[NVOUT];
     if (MODE == kJump) {
         R UL[5], UR[5];
-        gradient_variables(a.ph[fd.w], QL, UL);
-        gradient_variables(a.ph[fd.w], QR, UR);
+        if (V) {
+            gradient_variables(a.ph[fd.w], QL, UL);
+            gradient_variables(a.ph[fd.w], QR, UR);
+        } else {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) {
+                UL[v] = QL[v];
+                UR[v] = QR[v];
+            }
+        }
 #pragma unroll
         for (int v = 0; v < 5; ++v) {
             const R u = R(0.5) * (UR[v] - UL[v]) * J;
@@ -742,14 +767,18 @@ __global__ void __launch_bounds__(128) kv_face_direct(VArgs<R> a) {
     }
     const PhysR<R> ph = a.ph[fd.w];
     R inv[5];
-    if (ph.riemann == 0) {
+    if (V) {
+        const R t1[3] = {a.ft1[3 * gpt], a.ft1[3 * gpt + 1], a.ft1[3 * gpt + 2]};
+        const R t2[3] = {a.ft2[3 * gpt], a.ft2[3 * gpt + 1], a.ft2[3 * gpt + 2]};
+        riemann_flux(ph, QL, QR, n, t1, t2, inv);
+    } else if (ph.riemann == 0) {
         roe_flux(ph, QL, QR, n, inv);
     } else if (ph.riemann == 3) {
         rusanov_flux(ph, QL, QR, n, inv);
-    } else {
+    } else {  // LxF, central, u-diss
         const R t1[3] = {a.ft1[3 * gpt], a.ft1[3 * gpt + 1], a.ft1[3 * gpt + 2]};
         const R t2[3] = {a.ft2[3 * gpt], a.ft2[3 * gpt + 1], a.ft2[3 * gpt + 2]};
-        riemann_flux(ph, QL, QR, n, t1, t2, inv);  // the solvers that need the tangents
+        lxf_flux<R, false>(ph, QL, QR, n, t1, t2, inv);
     }
     R visc[5] = {0, 0, 0, 0, 0};
     if (MODE == kFluxNS) {
@@ -998,21 +1027,27 @@ using VStageFn = cudaError_t (*)(const VArgs<R>& a, int stage, double tshift, in
 template <typename R>
 using VTimesFn = cudaError_t (*)(const VArgs<R>& a, int reps, cudaStream_t s, double* ms);
 
-template <typename R, int MODE>
-cudaError_t launch_face(const VArgs<R>& a, cudaStream_t s) {
+template <typename R, int MODE, int V>
+cudaError_t launch_face_variant(const VArgs<R>& a, cudaStream_t s) {
     using Cfg = FaceCfg<R, MODE>;
     if (a.n_nc > 0) {
         const int blocks = (a.n_nc + Cfg::FPB - 1) / Cfg::FPB;
-        kv_face<R, MODE><<<blocks, Cfg::THREADS, Cfg::SMEM, s>>>(a);
+        kv_face<R, MODE, V><<<blocks, Cfg::THREADS, Cfg::SMEM, s>>>(a);
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
     const int npts = a.gp0[a.n_groups];
     if (npts > 0) {
-        kv_face_direct<R, MODE><<<(npts + 127) / 128, 128, 0, s>>>(a);
+        kv_face_direct<R, MODE, V><<<(npts + 127) / 128, 128, 0, s>>>(a);
         return cudaGetLastError();
     }
     return cudaSuccess;
+}
+
+template <typename R, int MODE>
+cudaError_t launch_face(const VArgs<R>& a, cudaStream_t s) {
+    const bool v = MODE == kJump ? a.grad_vars != 0 : ((a.riemann >= 4 && a.riemann <= 8) || a.averaging >= 5);
+    return v ? launch_face_variant<R, MODE, 1>(a, s) : launch_face_variant<R, MODE, 0>(a, s);
 }
 
 // Item kernels of one class: 0 traces, 1 volume, 2 update, 3 update with the manufactured source.
@@ -1098,11 +1133,17 @@ cudaError_t vrun_stage(const VArgs<R>& a, int stage, double tshift, int flags, c
             (e = set_item_attributes<R, 3>(vol, upd)) || (e = set_item_attributes<R, 4>(vol, upd)) ||
             (e = set_item_attributes<R, 5>(vol, upd)) || (e = set_item_attributes<R, 6>(vol, upd)) ||
             (e = set_item_attributes<R, 7>(vol, upd)) || (e = set_item_attributes<R, 8>(vol, upd)) ||
-            (e = cudaFuncSetAttribute(kv_face<R, kJump>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            (e = cudaFuncSetAttribute(kv_face<R, kJump, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       static_cast<int>(FaceCfg<R, kJump>::SMEM))) ||
-            (e = cudaFuncSetAttribute(kv_face<R, kFluxEuler>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            (e = cudaFuncSetAttribute(kv_face<R, kJump, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(FaceCfg<R, kJump>::SMEM))) ||
+            (e = cudaFuncSetAttribute(kv_face<R, kFluxEuler, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       static_cast<int>(FaceCfg<R, kFluxEuler>::SMEM))) ||
-            (e = cudaFuncSetAttribute(kv_face<R, kFluxNS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            (e = cudaFuncSetAttribute(kv_face<R, kFluxEuler, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(FaceCfg<R, kFluxEuler>::SMEM))) ||
+            (e = cudaFuncSetAttribute(kv_face<R, kFluxNS, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(FaceCfg<R, kFluxNS>::SMEM))) ||
+            (e = cudaFuncSetAttribute(kv_face<R, kFluxNS, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       static_cast<int>(FaceCfg<R, kFluxNS>::SMEM))))
             return e;
         return cudaSuccess;

@@ -189,6 +189,9 @@ int setup_vstore(dg_ctx* c, h3dctx::VStore<R>& st, const Gathered& h) {
     for (int q = 0; q < dg::kItemClasses; ++q) a.ccap[q] = c->ccap[q];
     a.ns = c->pc.ns;
     a.source = c->opt.source;
+    a.riemann = c->pc.riemann;
+    a.averaging = c->pc.averaging;
+    a.grad_vars = c->pc.grad_vars;
     a.items = c->items.p;
     a.item_elems = c->item_elems.p;
     a.eord = c->eord.p;
