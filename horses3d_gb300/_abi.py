@@ -35,10 +35,26 @@ DG_AVG_ENTROPY_CONSERVING, DG_AVG_CHANDRASEKAR = 5, 6
 DG_PRECISION_FP64, DG_PRECISION_MIXED = 0, 1
 DG_SOURCE_NONE, DG_SOURCE_MMS_CONVERGENCE, DG_SOURCE_MMS_LAMB_VECTOR = 0, 1, 2
 DG_GRADVARS_STATE, DG_GRADVARS_ENTROPY, DG_GRADVARS_ENERGY = 0, 1, 2
+DG_BC_NO_SLIP_WALL, DG_BC_FREE_SLIP_WALL, DG_BC_INFLOW, DG_BC_OUTFLOW = 1, 2, 3, 4
 DG_FIELD_Q, DG_FIELD_QDOT, DG_FIELD_G, DG_FIELD_UX, DG_FIELD_UY, DG_FIELD_UZ = range(6)
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
+
+
+class DgBoundary(C.Structure):
+    _fields_ = [
+        ("type", C.c_int32),
+        ("isothermal", C.c_int32),
+        ("wall_temperature", C.c_double),
+        ("wall_velocity", C.c_double * 3),
+        ("rho", C.c_double),
+        ("u", C.c_double),
+        ("v", C.c_double),
+        ("w", C.c_double),
+        ("p", C.c_double),
+        ("pressure", C.c_double),
+    ]
 
 
 class DgMeshDesc(C.Structure):
@@ -61,6 +77,9 @@ class DgMeshDesc(C.Structure):
         ("face_t1", _f64p),
         ("face_t2", _f64p),
         ("face_jacobian", _f64p),
+        ("face_boundary", _i32p),
+        ("n_boundaries", C.c_int32),
+        ("boundaries", C.POINTER(DgBoundary)),
     ]
 
 
@@ -132,7 +151,11 @@ SIGNATURES = [
     ("h3d_mesh_read_specmesh", C.c_int, [C.c_char_p, C.c_int, C.c_int, _i32p, C.c_char_p, C.POINTER(C.c_void_p)]),
     ("h3d_mesh_box", C.c_int, [C.c_int, C.c_int, C.c_int, _f64p, _f64p, C.c_double, C.c_int, C.c_int, C.c_int,
                                _i32p, C.POINTER(C.c_void_p)]),
+    ("h3d_mesh_box_zones", C.c_int, [C.c_int, C.c_int, C.c_int, _f64p, _f64p, C.c_double, C.c_int, C.c_int,
+                                     C.c_int, _i32p, C.c_char_p, C.POINTER(C.c_void_p)]),
     ("h3d_mesh_describe", C.c_int, [C.c_void_p, C.POINTER(DgMeshDesc)]),
+    ("h3d_mesh_zone_count", C.c_int, [C.c_void_p]),
+    ("h3d_mesh_zone_name", C.c_char_p, [C.c_void_p, C.c_int]),
     ("h3d_mesh_volume", C.c_double, [C.c_void_p]),
     ("h3d_mesh_free", None, [C.c_void_p]),
     ("h3d_nodal_storage", C.c_int, [C.c_int, C.c_int, _f64p, _f64p, _f64p]),

@@ -23,7 +23,9 @@ class CaseBatch:
         self.meshes = list(meshes)
         self.configs = list(configs)
         self.n_cases = len(meshes)
-        descs = (_abi.DgMeshDesc * self.n_cases)(*[m.desc for m in meshes])
+        self._bcs = [c.boundary_table(m.zone_names) if m.n_boundary_faces else None for m, c in zip(meshes, configs)]
+        descs = (_abi.DgMeshDesc * self.n_cases)(*[m.with_boundaries(b) if b is not None else m.desc
+                                                   for m, b in zip(meshes, self._bcs)])
         phys = (_abi.DgPhysics * self.n_cases)(*[c.physics() for c in configs])
         self._keep = (descs, phys)
         opts = configs[0].options()

@@ -45,6 +45,9 @@ class Config:
     t_final: float | None = None
     periodic: list = field(default_factory=list)
     order_file: str | None = None
+    aoa_theta: float = 0.0  # degrees ("AOA theta", PhysicsStorage_NS.f90)
+    aoa_phi: float = 0.0    # degrees ("AOA phi")
+    boundaries: dict = field(default_factory=dict)  # zone name -> {"type": ..., block keys}
 
     def element_orders(self, base_dir=None):
         """(Nx, Ny, Nz) per element from "polynomial order file" (ReadInputFile.f90:132-153: the element
@@ -65,6 +68,70 @@ class Config:
 
     def periodic_spec(self) -> str:
         return ",".join(f"{a}:{b}" for a, b in self.periodic)
+
+    # -- reference values (PhysicsStorage_NS.f90:284-318; air, T_ref = 520*5/9 K, p_ref = 101325 Pa) --
+    def _ref(self):
+        R, gamma = 287.15, 1.4
+        T = 520.0 * 5.0 / 9.0
+        rho = 101325.0 / (R * T)
+        V = self.mach * np.sqrt(gamma * R * T)
+        return {"T": T, "rho": rho, "V": V, "p": rho * V * V}
+
+    def free_stream(self):
+        """(rho, u, v, w, p) of the free stream: unit density and speed along the angles of attack,
+        p = 1/(gamma M^2) (the reference's uniform initial state and inflow defaults)."""
+        th, ph = np.radians(self.aoa_theta), np.radians(self.aoa_phi)
+        return (1.0, np.cos(th) * np.cos(ph), np.sin(th) * np.cos(ph), np.sin(ph), 1.0 / (1.4 * self.mach ** 2))
+
+    def boundary(self, zone: str) -> _abi.DgBoundary:
+        """The DgBoundary of a zone from its "#define boundary" block (NoSlipWallBC.f90:80-216,
+        FreeSlipWallBC.f90:80-200, InflowBC.f90:112-290, OutflowBC.f90:85-188), dimensionless."""
+        spec = self.boundaries.get(zone.lower())
+        if spec is None:
+            raise ValueError(f"no boundary condition for zone '{zone}'")
+        kind = spec["type"].replace(" ", "").lower()
+        b = _abi.DgBoundary()
+        ref = self._ref()
+        gM2 = 1.4 * self.mach ** 2
+        if kind in ("noslipwall", "freeslipwall"):
+            b.type = _abi.DG_BC_NO_SLIP_WALL if kind == "noslipwall" else _abi.DG_BC_FREE_SLIP_WALL
+            wt = str(spec.get("wall type (adiabatic/isothermal)", "adiabatic")).lower()
+            b.isothermal = 1 if wt == "isothermal" else 0
+            b.wall_temperature = float(spec.get("wall temperature", ref["T"])) / ref["T"]
+            if kind == "noslipwall" and "wall velocity" in spec:
+                vw = [float(x) for x in str(spec["wall velocity"]).strip("[]() ").replace(",", " ").split()]
+                for c in range(3):
+                    b.wall_velocity[c] = vw[c]
+        elif kind == "inflow":
+            b.type = _abi.DG_BC_INFLOW
+            if float(spec.get("turbintensity", 0.0)) != 0.0:
+                raise UnsupportedOption("inflow turbulence intensity (random fluctuations)")
+            p = float(spec.get("pressure", ref["p"] / gM2)) / ref["p"]
+            rho = float(spec.get("density", ref["rho"])) / ref["rho"]
+            v = float(spec.get("mach", self.mach)) * np.sqrt(1.4 * p / rho)
+            th = np.radians(float(spec.get("aoatheta", self.aoa_theta)))
+            ph = np.radians(float(spec.get("aoaphi", self.aoa_phi)))
+            b.rho, b.p = rho, p
+            b.u, b.v, b.w = v * np.cos(th) * np.cos(ph), v * np.sin(th) * np.cos(ph), v * np.sin(ph)
+        elif kind == "outflow":
+            b.type = _abi.DG_BC_OUTFLOW
+            if "pressure" in spec:
+                pext = float(spec["pressure"])
+            elif "dp" in spec:
+                pext = ref["p"] / gM2 - float(spec["dp"])
+            else:
+                pext = ref["p"] / gM2
+            b.pressure = pext / ref["p"]
+        else:
+            raise UnsupportedOption(f"boundary '{zone}' of type '{spec['type']}'")
+        return b
+
+    def boundary_table(self, zone_names):
+        """One DgBoundary per mesh zone, in the mesh's zone order (a ctypes array)."""
+        arr = (_abi.DgBoundary * max(1, len(zone_names)))()
+        for z, name in enumerate(zone_names):
+            arr[z] = self.boundary(name)
+        return arr
 
 
 # SpatialDiscretization.f90:106-148 "gradient variables"
@@ -178,13 +245,21 @@ def parse_control(text: str) -> Config:
     cfg.n_steps = int(float(get("number of time steps", 1)))
     if "final time" in keys:
         cfg.t_final = float(keys["final time"])
+    cfg.aoa_theta = float(get("aoa theta", 0.0))
+    cfg.aoa_phi = float(get("aoa phi", 0.0))
     pairs = []
     for b in blocks:
         if b.get("kind") != "boundary":
             continue
-        if b.get("type", "").lower() != "periodic":
+        kind = str(b.get("type", "")).replace(" ", "").lower()
+        names = b["name"].split()  # "#define boundary a b c" applies to every name
+        if kind == "periodic":
+            pairs.append((b["name"].strip(), str(b.get("coupled boundary", "")).lower().strip()))
+        elif kind in ("noslipwall", "freeslipwall", "inflow", "outflow"):
+            for nm in names:
+                cfg.boundaries[nm.lower()] = dict(b, type=kind)
+        else:
             raise UnsupportedOption(f"boundary '{b.get('name')}' of type '{b.get('type')}'")
-        pairs.append((b["name"].strip(), b.get("coupled boundary", "").lower().strip()))
     seen = set()
     for a, b in pairs:
         if (b, a) in seen:

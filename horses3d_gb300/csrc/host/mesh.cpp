@@ -696,31 +696,41 @@ bool build_mesh(const MeshSource& src, int node_type, const std::vector<int32_t>
     }
 
     // ---- compact, element -> face tables (DeletePeriodicMinusFaces, GetElementsFaceIDs) ----
+    // Faces left without a partner are boundary faces of their zone (HexMesh.f90:433-480,
+    // ConstructZones): one element, normal pointing out of the domain.
     std::vector<F> kept;
     for (auto& f : faces)
         if (!f.deleted) kept.push_back(f);
-    int nb = 0;
-    for (auto& f : kept)
-        if (!f.interior) ++nb;
-    if (nb > 0) {
-        err = "mesh has " + std::to_string(nb) + " boundary faces; only periodic/interior faces are supported";
-        return false;
-    }
     out.F = static_cast<int>(kept.size());
     out.face_elem.resize(2 * out.F);
     out.face_side.resize(2 * out.F);
     out.face_rot.resize(out.F);
     out.face_nf.resize(2 * out.F);
+    out.face_zone.assign(out.F, -1);
     out.elem_face.assign(6 * K, -1);
     out.elem_face_side.assign(6 * K, 0);
+    out.n_boundary_faces = 0;
     for (int f = 0; f < out.F; ++f) {
         for (int s = 0; s < 2; ++s) {
             out.face_elem[2 * f + s] = kept[f].elem[s];
             out.face_side[2 * f + s] = kept[f].side[s];
+            if (kept[f].elem[s] < 0) continue;
             out.elem_face[6 * kept[f].elem[s] + kept[f].side[s] - 1] = f;
             out.elem_face_side[6 * kept[f].elem[s] + kept[f].side[s] - 1] = s + 1;
         }
         out.face_rot[f] = kept[f].rot;
+        if (!kept[f].interior) {
+            const std::string& name = kept[f].bname;
+            if (name.empty() || name == "---") {
+                err = "a boundary face of element " + std::to_string(kept[f].elem[0] + 1) + " has no zone name";
+                return false;
+            }
+            int z = 0;
+            while (z < static_cast<int>(out.zone_names.size()) && out.zone_names[z] != name) ++z;
+            if (z == static_cast<int>(out.zone_names.size())) out.zone_names.push_back(name);
+            out.face_zone[f] = z;
+            ++out.n_boundary_faces;
+        }
     }
 
     // ---- face orders (HexMesh.f90:2420-2480, FaceClass.f90:187-276 Face_LinkWithElements) ----
@@ -731,9 +741,15 @@ bool build_mesh(const MeshSource& src, int node_type, const std::vector<int32_t>
         int NelL[2], NelR[2];
         for (int a = 0; a < 2; ++a) {
             NelL[a] = orders[3 * eL + kAxisMap[sL][a] - 1];
-            NelR[a] = orders[3 * eR + kAxisMap[sR][a] - 1];
+            NelR[a] = eR >= 0 ? orders[3 * eR + kAxisMap[sR][a] - 1] : NelL[a];
         }
         NfLeft[2 * f] = NelL[0]; NfLeft[2 * f + 1] = NelL[1];
+        if (eR < 0) {  // boundary faces keep their element's face orders
+            NfRight[2 * f] = NelL[0]; NfRight[2 * f + 1] = NelL[1];
+            out.face_nf[2 * f] = NelL[0];
+            out.face_nf[2 * f + 1] = NelL[1];
+            continue;
+        }
         switch (out.face_rot[f]) {
             case 0: case 2: case 5: case 7:
                 NfRight[2 * f] = NelR[0]; NfRight[2 * f + 1] = NelR[1]; break;
@@ -762,6 +778,15 @@ bool build_mesh(const MeshSource& src, int node_type, const std::vector<int32_t>
     for (int f = 0; f < out.F; ++f) {
         const int eL = out.face_elem[2 * f], eR = out.face_elem[2 * f + 1];
         const int sL = out.face_side[2 * f] - 1, sR = out.face_side[2 * f + 1] - 1;
+        if (eR < 0) {  // boundary face: the patch is adapted to the element's face orders
+            HexMap& m = maps[eL];
+            if (m.hex8) continue;
+            const int nL[2] = {m.faces[sL].nu - 1, m.faces[sL].nv - 1};
+            if (nL[0] == 1 && nL[1] == 1) continue;
+            const int CLN[2] = {NfLeft[2 * f], NfLeft[2 * f + 1]};
+            if (CLN[0] < nL[0] || CLN[1] < nL[1]) adapt(m, sL, CLN[0], CLN[1]);
+            continue;
+        }
         HexMap& mL = maps[eL];
         HexMap& mR = maps[eR];
         if (mL.hex8 && mR.hex8) continue;

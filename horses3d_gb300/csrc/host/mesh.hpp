@@ -57,6 +57,8 @@ struct Mesh {
     std::vector<double> face_normal, face_t1, face_t2, face_jac, face_x;
     std::vector<int32_t> elem_face, elem_face_side;  // 6 per element (face id, 1 or 2)
     int n_boundary_faces = 0;
+    std::vector<std::string> zone_names;        // non-periodic boundary zones
+    std::vector<int32_t> face_zone;             // [F] zone of a boundary face, -1 for interior faces
     double volume = 0.0;
 };
 

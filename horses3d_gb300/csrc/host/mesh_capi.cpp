@@ -58,6 +58,19 @@ int h3d_mesh_box(int nx, int ny, int nz, const double lo[3], const double hi[3],
     return finish(src, node_type, uniform_n, orders, "front:back,bottom:top,left:right", out);
 }
 
+int h3d_mesh_box_zones(int nx, int ny, int nz, const double lo[3], const double hi[3], double warp,
+                       int patch_order, int node_type, int uniform_n, const int32_t* orders,
+                       const char* periodic, h3d_mesh** out) {
+    if (!lo || !hi || !out || nx < 1 || ny < 1 || nz < 1) return h3d::fail(DG_ERR_INVALID, "bad box arguments");
+    if (node_type != DG_NODES_GAUSS && node_type != DG_NODES_GAUSS_LOBATTO)
+        return h3d::fail(DG_ERR_INVALID, "unknown node type");
+    if (warp != 0.0 && patch_order < 2)
+        return h3d::fail(DG_ERR_INVALID, "a warped box needs curved face patches (patch_order >= 2)");
+    h3d::MeshSource src;
+    h3d::box_source(nx, ny, nz, lo, hi, warp, patch_order, src);
+    return finish(src, node_type, uniform_n, orders, periodic ? periodic : "", out);
+}
+
 int h3d_mesh_describe(const h3d_mesh* mesh, dg_mesh_desc* d) {
     if (!mesh || !d) return h3d::fail(DG_ERR_INVALID, "null argument");
     const h3d::Mesh& m = mesh->m;
@@ -80,7 +93,17 @@ int h3d_mesh_describe(const h3d_mesh* mesh, dg_mesh_desc* d) {
     d->face_t1 = m.face_t1.data();
     d->face_t2 = m.face_t2.data();
     d->face_jacobian = m.face_jac.data();
+    d->face_boundary = m.n_boundary_faces > 0 ? m.face_zone.data() : nullptr;
+    d->n_boundaries = static_cast<int32_t>(m.zone_names.size());
+    d->boundaries = nullptr;
     return DG_OK;
+}
+
+int h3d_mesh_zone_count(const h3d_mesh* mesh) { return mesh ? static_cast<int>(mesh->m.zone_names.size()) : 0; }
+
+const char* h3d_mesh_zone_name(const h3d_mesh* mesh, int zone) {
+    if (!mesh || zone < 0 || zone >= static_cast<int>(mesh->m.zone_names.size())) return nullptr;
+    return mesh->m.zone_names[zone].c_str();
 }
 
 double h3d_mesh_volume(const h3d_mesh* mesh) { return mesh ? mesh->m.volume : 0.0; }

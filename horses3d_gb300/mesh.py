@@ -30,6 +30,23 @@ class HexMesh:
         self.n_faces = int(d.n_faces)
         nf = np.ctypeslib.as_array(d.face_nf, shape=(self.n_faces, 2)) if self.n_faces else np.zeros((0, 2), np.int32)
         self.face_points = int(np.sum((nf[:, 0] + 1) * (nf[:, 1] + 1)))
+        L = _abi.lib()
+        self.zone_names = [L.h3d_mesh_zone_name(self._h, z).decode() for z in range(L.h3d_mesh_zone_count(self._h))]
+        self.n_boundary_faces = 0
+        if d.face_boundary:
+            fb = np.ctypeslib.as_array(d.face_boundary, shape=(self.n_faces,))
+            self.n_boundary_faces = int(np.count_nonzero(fb >= 0))
+
+    def with_boundaries(self, table) -> _abi.DgMeshDesc:
+        """A copy of the mesh description whose `boundaries` points at `table` (one DgBoundary per
+        zone, in zone_names order). The caller keeps `table` alive while the description is used."""
+        if len(table) != len(self.zone_names):
+            raise ValueError(f"{len(table)} boundary conditions for {len(self.zone_names)} zones")
+        d = _abi.DgMeshDesc()
+        C.pointer(d)[0] = self.desc
+        d.n_boundaries = len(table)
+        d.boundaries = C.cast(table, C.POINTER(_abi.DgBoundary)) if len(table) else None
+        return d
 
     # -- construction -------------------------------------------------------------------------
     @classmethod
@@ -52,18 +69,22 @@ class HexMesh:
 
     @classmethod
     def box(cls, n, lo, hi, order, node_type: int = _abi.DG_NODES_GAUSS, warp: float = 0.0,
-            patch_order: int = 0) -> "HexMesh":
+            patch_order: int = 0, periodic: str | None = None) -> "HexMesh":
+        """Box of n^3 (or nx*ny*nz) hexahedra. periodic: the periodic zone pairs over left/right (x),
+        front/back (y), bottom/top (z); None makes all three directions periodic, the zones left out
+        are boundary zones."""
         nx, ny, nz = (n, n, n) if np.ndim(n) == 0 else n
         lo = np.ascontiguousarray(lo, dtype=np.float64)
         hi = np.ascontiguousarray(hi, dtype=np.float64)
         h = C.c_void_p()
+        spec = "front:back,bottom:top,left:right" if periodic is None else periodic
         if np.ndim(order) == 0:
-            rc = _abi.lib().h3d_mesh_box(nx, ny, nz, _abi.f64ptr(lo), _abi.f64ptr(hi), float(warp), int(patch_order),
-                                         node_type, int(order), None, C.byref(h))
+            uniform, optr = int(order), None
         else:
             o = np.ascontiguousarray(order, dtype=np.int32).reshape(-1)
-            rc = _abi.lib().h3d_mesh_box(nx, ny, nz, _abi.f64ptr(lo), _abi.f64ptr(hi), float(warp), int(patch_order),
-                                         node_type, 0, _abi.i32ptr(o), C.byref(h))
+            uniform, optr = 0, _abi.i32ptr(o)
+        rc = _abi.lib().h3d_mesh_box_zones(nx, ny, nz, _abi.f64ptr(lo), _abi.f64ptr(hi), float(warp), int(patch_order),
+                                           node_type, uniform, optr, spec.encode(), C.byref(h))
         _abi.check(rc, "h3d_mesh_box")
         return cls(h)
 

@@ -32,8 +32,13 @@ class NavierStokesDG:
         self.config = config
         self.physics = config.physics()
         self.options = config.options()
+        desc = mesh.desc
+        if mesh.n_boundary_faces:  # the zones' boundary conditions from the configuration
+            self._bc = config.boundary_table(mesh.zone_names)
+            desc = mesh.with_boundaries(self._bc)
+        self._desc = desc
         h = C.c_void_p()
-        _abi.check(_abi.lib().dg_create(C.byref(mesh.desc), C.byref(self.physics), C.byref(self.options), C.byref(h)),
+        _abi.check(_abi.lib().dg_create(C.byref(desc), C.byref(self.physics), C.byref(self.options), C.byref(h)),
                    "dg_create")
         self._h = h
         self.ndof = int(_abi.lib().dg_ndof(self._h))

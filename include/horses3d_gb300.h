@@ -69,8 +69,27 @@ enum { DG_FIELD_Q = 0, DG_FIELD_QDOT = 1, DG_FIELD_G = 2,
 /* Face-local element sides, numbered as the reference (HexElementConnectivityDefinitions.f90:69-77):
  * 1 FRONT (eta=-1), 2 BACK (eta=+1), 3 BOTTOM (zeta=-1), 4 RIGHT (xi=+1), 5 TOP (zeta=+1), 6 LEFT (xi=-1). */
 
+/* Boundary conditions of non-periodic boundary zones (physics/common/*BC.f90, NAVIERSTOKES parts),
+ * in the solver's dimensionless variables:
+ *   NO_SLIP_WALL   NoSlipWallBC.f90:265-372   (wall velocity; adiabatic or isothermal)
+ *   FREE_SLIP_WALL FreeSlipWallBC.f90:249-351 (adiabatic or isothermal)
+ *   INFLOW         InflowBC.f90:363-414        (imposed rho, u, v, w, p; no turbulence intensity)
+ *   OUTFLOW        OutflowBC.f90:226-304       (subsonic characteristic outflow at pressure p) */
+enum { DG_BC_NO_SLIP_WALL = 1, DG_BC_FREE_SLIP_WALL = 2, DG_BC_INFLOW = 3, DG_BC_OUTFLOW = 4 };
+typedef struct dg_boundary {
+    int32_t type;                   /* DG_BC_* */
+    int32_t isothermal;             /* walls: 0 adiabatic (reference default), 1 isothermal */
+    double wall_temperature;        /* isothermal walls: T_wall / T_ref (reference default 1) */
+    double wall_velocity[3];        /* no-slip walls (default 0) */
+    double rho, u, v, w, p;         /* inflow state (defaults 1, the free stream at the AoA, 1/(gamma M^2)) */
+    double pressure;                /* outflow pressure (default 1/(gamma M^2)) */
+} dg_boundary;
+
 /* Mesh description: geometry and connectivity as HexMesh holds them after ConstructGeometry.
- * Only interior faces (periodic faces count as interior, HexMesh.f90:519-736) are supported. */
+ * Periodic faces count as interior faces (HexMesh.f90:519-736). A boundary face has a single
+ * element: face_elem[2f+1] = -1, face_side[2f+1] = 0, face_rotation 0, face orders those of its
+ * element side, its normal pointing out of the domain, and face_boundary[f] >= 0 naming its entry
+ * of `boundaries`. */
 typedef struct dg_mesh_desc {
     int32_t n_elements;
     int32_t node_type;              /* DG_NODES_* */
@@ -90,6 +109,10 @@ typedef struct dg_mesh_desc {
     const double* face_t1;          /* [3*sum(Pf)] */
     const double* face_t2;          /* [3*sum(Pf)] */
     const double* face_jacobian;    /* [sum(Pf)] surface Jacobian Jf */
+    const int32_t* face_boundary;   /* [F] boundary condition of each boundary face, -1 for interior
+                                       faces; NULL when every face is interior */
+    int32_t n_boundaries;
+    const dg_boundary* boundaries;  /* [n_boundaries] */
 } dg_mesh_desc;
 
 /* Physics constants (PhysicsStorage_NS.f90:186-429). gamma=1.4 (air) and Sutherland's law with
@@ -260,7 +283,18 @@ int h3d_mesh_read_specmesh(const char* path, int node_type, int uniform_n, const
  * patch_order (patch_order < 2 and warp == 0 gives straight-sided hex8 elements). */
 int h3d_mesh_box(int nx, int ny, int nz, const double lo[3], const double hi[3], double warp,
                  int patch_order, int node_type, int uniform_n, const int32_t* orders, h3d_mesh** out);
+/* The same box with a chosen periodic-pair list ("left:right,..." over the zone names left/right
+ * (x), front/back (y), bottom/top (z)); the other zones become boundary zones. */
+int h3d_mesh_box_zones(int nx, int ny, int nz, const double lo[3], const double hi[3], double warp,
+                       int patch_order, int node_type, int uniform_n, const int32_t* orders,
+                       const char* periodic, h3d_mesh** out);
+/* Fills out with the mesh's arrays. Boundary faces get face_boundary = the index of their zone
+ * (h3d_mesh_zone_name) and n_boundaries = the number of zones; `boundaries` is left NULL for the
+ * caller to point at one dg_boundary per zone. */
 int h3d_mesh_describe(const h3d_mesh* mesh, dg_mesh_desc* out);
+/* Non-periodic boundary zones of the mesh (SpecMesh boundary names, lower case). */
+int h3d_mesh_zone_count(const h3d_mesh* mesh);
+const char* h3d_mesh_zone_name(const h3d_mesh* mesh, int zone);
 /* Total quadrature volume sum_e sum_ijk w_i w_j w_k J (MappedGeometry.f90:132-135). */
 double h3d_mesh_volume(const h3d_mesh* mesh);
 void h3d_mesh_free(h3d_mesh* mesh);

@@ -980,6 +980,120 @@ static void lamb_point(double x, double y, double z, double t, double gm1, doubl
     for (int q = 0; q < 5; ++q) S[q] = dQ[q] + dF[q] - dG[q] / Re;
 }
 
+// ---------------------------------------------------------------- boundary conditions --------
+// physics/common/{NoSlipWallBC,FreeSlipWallBC,InflowBC,OutflowBC}.f90 (NAVIERSTOKES parts) and
+// GenericBoundaryConditionClass.f90:243-291 (the default gradient variables and Neumann flux).
+static double wall_type(const dg_boundary& b) { return b.isothermal ? 1.0 : 0.0; }
+
+// FlowState: the external state of the Riemann problem at a boundary point.
+static void bc_state(const Phys& p, const dg_boundary& b, const double* n, double* Q) {
+    switch (b.type) {
+        case DG_BC_NO_SLIP_WALL: {  // NoSlipWallBC.f90:265-296
+            for (int c = 0; c < 3; ++c) Q[1 + c] = 2.0 * Q[0] * b.wall_velocity[c] - Q[1 + c];
+            Q[4] = Q[4] + wall_type(b) * (Q[0] * b.wall_temperature / (p.gammaM2 * p.gm1) - Q[4]);
+            break;
+        }
+        case DG_BC_FREE_SLIP_WALL: {  // FreeSlipWallBC.f90:249-286
+            const double qn = n[0] * Q[1] + n[1] * Q[2] + n[2] * Q[3];
+            for (int c = 0; c < 3; ++c) Q[1 + c] = Q[1 + c] - 2.0 * qn * n[c];
+            const double pa = Q[0] * b.wall_temperature / p.gammaM2;
+            Q[4] = Q[4] + wall_type(b) * (pa / p.gm1 + 0.5 * (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) / Q[0] - Q[4]);
+            break;
+        }
+        case DG_BC_INFLOW: {  // InflowBC.f90:363-406 (no turbulence intensity)
+            Q[0] = b.rho;
+            Q[1] = Q[0] * b.u;
+            Q[2] = Q[0] * b.v;
+            Q[3] = Q[0] * b.w;
+            Q[4] = b.p / (p.gamma - 1.0) + 0.5 * Q[0] * (b.u * b.u + b.v * b.v + b.w * b.w);
+            break;
+        }
+        default: {  // OutflowBC.f90:226-288
+            double qn = (n[0] * Q[1] + n[1] * Q[2] + n[2] * Q[3]) / Q[0];
+            const double tx = Q[1] / Q[0] - qn * n[0], ty = Q[2] / Q[0] - qn * n[1], tz = Q[3] / Q[0] - qn * n[2];
+            const double pr = p.gm1 * (Q[4] - 0.5 * (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) / Q[0]);
+            const double a2 = p.gamma * pr / Q[0];
+            double a = std::sqrt(a2);
+            if (std::fabs(qn / a) <= 1.0) {
+                const double rPlus = qn + 2.0 * a / p.gm1;
+                const double ent = pr - a2 * Q[0];
+                const double rho = -(ent - b.pressure) / a2;
+                a = std::sqrt(p.gamma * b.pressure / rho);
+                qn = rPlus - 2.0 * a / p.gm1;
+                const double u = tx + qn * n[0], v = ty + qn * n[1], w = tz + qn * n[2];
+                Q[0] = rho;
+                Q[1] = rho * u;
+                Q[2] = rho * v;
+                Q[3] = rho * w;
+                Q[4] = b.pressure / p.gm1 + 0.5 * rho * (u * u + v * v + w * w);
+            }
+            break;
+        }
+    }
+}
+
+// FlowGradVars: U (in: the interior gradient variables, out: U* at the boundary).
+static void bc_gradvars(const Phys& p, const dg_boundary& b, const double* n, const double* Q, double* U) {
+    double Qa[5];
+    switch (b.type) {
+        case DG_BC_NO_SLIP_WALL: {  // NoSlipWallBC.f90:298-337
+            const double invRho = 1.0 / Q[0];
+            const double e_int = invRho * (Q[4] - 0.5 * invRho * (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]));
+            const double ewall = b.wall_temperature / (p.gm1 * p.gammaM2);
+            const double wt = wall_type(b);
+            const double* vw = b.wall_velocity;
+            Qa[0] = Q[0];
+            for (int c = 0; c < 3; ++c) Qa[1 + c] = Q[0] * vw[c];
+            Qa[4] = Q[0] * ((1.0 - wt) * e_int + wt * ewall + 0.5 * (vw[0] * vw[0] + vw[1] * vw[1] + vw[2] * vw[2]));
+            const double U1 = U[0];
+            gradient_variables(p, Qa, U);
+            U[0] = U1;
+            return;
+        }
+        case DG_BC_FREE_SLIP_WALL: {  // FreeSlipWallBC.f90:288-318
+            const double ewall = b.wall_temperature / (p.gm1 * p.gammaM2);
+            for (int c = 0; c < 4; ++c) Qa[c] = Q[c];
+            Qa[4] = Q[4] + wall_type(b) * (Q[0] * ewall + 0.5 * (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) / Q[0] - Q[4]);
+            gradient_variables(p, Qa, U);
+            return;
+        }
+        default: {  // GenericBC_FlowGradVars: U* = (U(FlowState(Q)) + U) / 2
+            for (int c = 0; c < 5; ++c) Qa[c] = Q[c];
+            bc_state(p, b, n, Qa);
+            double Ua[5];
+            gradient_variables(p, Qa, Ua);
+            for (int c = 0; c < 5; ++c) U[c] = 0.5 * (Ua[c] + U[c]);
+            return;
+        }
+    }
+}
+
+// FlowNeumann: the boundary's viscous normal flux from the interior one.
+static void bc_neumann(const dg_boundary& b, const double* Q, double* f) {
+    switch (b.type) {
+        case DG_BC_NO_SLIP_WALL: {  // NoSlipWallBC.f90:339-372
+            const double invRho = 1.0 / Q[0];
+            const double u = invRho * Q[1], v = invRho * Q[2], w = invRho * Q[3];
+            const double work = u * f[1] + v * f[2] + w * f[3];
+            const double heat = f[4] - work;
+            f[0] = 0.0;
+            f[4] = (b.wall_velocity[0] * f[1] + b.wall_velocity[1] * f[2] + b.wall_velocity[2] * f[3]) +
+                   wall_type(b) * heat;
+            return;
+        }
+        case DG_BC_FREE_SLIP_WALL: {  // FreeSlipWallBC.f90:320-351
+            const double work = (f[1] * Q[1] + f[2] * Q[2] + f[3] * Q[3]) / Q[0];
+            const double heat = f[4] - work;
+            f[0] = f[1] = f[2] = f[3] = 0.0;
+            f[4] = wall_type(b) * heat;
+            return;
+        }
+        default:  // InflowBC.f90:408-414, OutflowBC.f90:290-304
+            for (int c = 0; c < 5; ++c) f[c] = 0.0;
+            return;
+    }
+}
+
 // ---------------------------------------------------------------- solver state ---------------
 struct Elem {
     int N[3];
@@ -989,6 +1103,7 @@ struct Elem {
 };
 struct Face {
     int elem[2], side[2], rot;
+    int bc = -1;  // boundary condition of a boundary face (elem[1] == -1)
     int Nf[2], NelL[2], NelR[2], NfL[2], NfR[2], proj[2];
     int64_t off;  // face point offset in the geometry arrays
     std::vector<double> Q[2], Ux[2], Uy[2], Uz[2], mu[2];  // at Nf
@@ -998,6 +1113,7 @@ struct Face {
 
 struct Solver {
     Phys ph;
+    std::vector<dg_boundary> bcs;
     dg_options opt;
     int nodes;
     int K;
@@ -1190,6 +1306,7 @@ static void compute_rhs(Solver& s, double t) {
             Face& f = s.fa[fid];
             const int q1 = f.Nf[0] + 1, q2 = f.Nf[1] + 1;
             std::vector<double> us(15 * q1 * q2);
+            const bool boundary = f.elem[1] < 0;
             for (int j = 0; j < q2; ++j)
                 for (int i = 0; i < q1; ++i) {
                     const int p = i + q1 * j;
@@ -1197,6 +1314,18 @@ static void compute_rhs(Solver& s, double t) {
                     const double* n = &s.fn[3 * (f.off + p)];
                     double UL[5], UR[5];
                     gradient_variables(s.ph, &f.Q[0][5 * p], UL);
+                    if (boundary) {  // BR1_ComputeBoundaryFlux (EllipticBR1.f90:686-736): (U* - U) Jf n
+                        double Us[5];
+                        for (int v = 0; v < 5; ++v) Us[v] = UL[v];
+                        bc_gradvars(s.ph, s.bcs[f.bc], n, &f.Q[0][5 * p], Us);
+                        for (int v = 0; v < 5; ++v) {
+                            const double u = (Us[v] - UL[v]) * J;
+                            us[15 * p + v] = u * n[0];
+                            us[15 * p + 5 + v] = u * n[1];
+                            us[15 * p + 10 + v] = u * n[2];
+                        }
+                        continue;
+                    }
                     gradient_variables(s.ph, &f.Q[1][5 * p], UR);
                     for (int v = 0; v < 5; ++v) {
                         const double u = 0.5 * (UR[v] - UL[v]) * J;
@@ -1206,7 +1335,7 @@ static void compute_rhs(Solver& s, double t) {
                     }
                 }
             project_to_side(f, 1, 15, us, f.unStar[0], 1.0, s.nodes);
-            project_to_side(f, 2, 15, us, f.unStar[1], 1.0, s.nodes);
+            if (!boundary) project_to_side(f, 2, 15, us, f.unStar[1], 1.0, s.nodes);
         }
         // BR1_GradientFaceLoop + ProlongGradientsToFaces (EllipticBR1.f90:531-569; DGIntegrals.f90:365-443)
 #pragma omp parallel for schedule(static)
@@ -1261,6 +1390,7 @@ static void compute_rhs(Solver& s, double t) {
             Face& f = s.fa[fid];
             const int np = (f.Nf[0] + 1) * (f.Nf[1] + 1);
             for (int side = 0; side < 2; ++side) {
+                if (f.elem[side] < 0) continue;
                 f.mu[side].resize(2 * np);
                 for (int p = 0; p < np; ++p) mu_kappa(s.ph, &f.Q[side][5 * p], f.mu[side][2 * p], f.mu[side][2 * p + 1]);
             }
@@ -1360,10 +1490,23 @@ static void compute_rhs(Solver& s, double t) {
         Face& f = s.fa[fid];
         const int q1 = f.Nf[0] + 1, q2 = f.Nf[1] + 1, np = q1 * q2;
         std::vector<double> flux(5 * np);
+        const bool boundary = f.elem[1] < 0;
         for (int p = 0; p < np; ++p) {
             double visc[5] = {0, 0, 0, 0, 0};
             const double* n = &s.fn[3 * (f.off + p)];
-            if (ns) {  // BR1_RiemannSolver (EllipticBR1.f90:816-868)
+            double Qb[5];
+            if (boundary) {  // computeBoundaryFlux (SpatialDiscretization.f90:1896-2028)
+                const dg_boundary& b = s.bcs[f.bc];
+                for (int v = 0; v < 5; ++v) Qb[v] = f.Q[0][5 * p + v];
+                bc_state(s.ph, b, n, Qb);
+                if (ns) {
+                    double fL[15];
+                    viscous_flux(s.ph, &f.Q[0][5 * p], &f.Ux[0][5 * p], &f.Uy[0][5 * p], &f.Uz[0][5 * p],
+                                 f.mu[0][2 * p], 0.0, f.mu[0][2 * p + 1], fL);
+                    for (int v = 0; v < 5; ++v) visc[v] = fL[v] * n[0] + fL[v + 5] * n[1] + fL[v + 10] * n[2];
+                    bc_neumann(b, &f.Q[0][5 * p], visc);
+                }
+            } else if (ns) {  // BR1_RiemannSolver (EllipticBR1.f90:816-868)
                 double fL[15], fR[15];
                 viscous_flux(s.ph, &f.Q[0][5 * p], &f.Ux[0][5 * p], &f.Uy[0][5 * p], &f.Uz[0][5 * p], f.mu[0][2 * p], 0.0,
                              f.mu[0][2 * p + 1], fL);
@@ -1376,7 +1519,7 @@ static void compute_rhs(Solver& s, double t) {
             }
             double inv[5];
             const double* QL = &f.Q[0][5 * p];
-            const double* QR = &f.Q[1][5 * p];
+            const double* QR = boundary ? Qb : &f.Q[1][5 * p];
             const double* t1 = &s.ft1[3 * (f.off + p)];
             const double* t2 = &s.ft2[3 * (f.off + p)];
             const int avg = s.opt.averaging;
@@ -1397,7 +1540,7 @@ static void compute_rhs(Solver& s, double t) {
             for (int v = 0; v < 5; ++v) flux[5 * p + v] = (inv[v] - visc[v]) * s.fj[f.off + p];
         }
         project_to_side(f, 1, 5, flux, f.fStar[0], -1.0, s.nodes);
-        project_to_side(f, 2, 5, flux, f.fStar[1], -1.0, s.nodes);
+        if (!boundary) project_to_side(f, 2, 5, flux, f.fStar[1], -1.0, s.nodes);
     }
     // Surface integrals, 1/J, source (SpatialDiscretization.f90:483-494, 1686-1701, 564-639)
     const double mms_mu = s.ph.mu, mms_kap = s.ph.kappa;
@@ -1526,19 +1669,23 @@ void* orc_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* 
     s->jac = cp(m->jacobian, off); s->invJac = cp(m->inv_jacobian, off);
     s->fa.resize(m->n_faces);
     int64_t foff = 0;
+    if (m->n_boundaries > 0 && m->boundaries) s->bcs.assign(m->boundaries, m->boundaries + m->n_boundaries);
     for (int f = 0; f < m->n_faces; ++f) {
         auto& F = s->fa[f];
         for (int q = 0; q < 2; ++q) {
             F.elem[q] = m->face_elem[2 * f + q];
             F.side[q] = m->face_side[2 * f + q];
             F.Nf[q] = m->face_nf[2 * f + q];
+            if (F.elem[q] < 0) continue;  // boundary face: no second element
             s->el[F.elem[q]].face[F.side[q] - 1] = f;
             s->el[F.elem[q]].fside[F.side[q] - 1] = q + 1;
         }
         F.rot = m->face_rotation[f];
+        const bool boundary = F.elem[1] < 0;
+        if (boundary) F.bc = m->face_boundary ? m->face_boundary[f] : -1;
         for (int a = 0; a < 2; ++a) {
             F.NelL[a] = s->el[F.elem[0]].N[orc::axis_of(F.side[0], a)];
-            F.NelR[a] = s->el[F.elem[1]].N[orc::axis_of(F.side[1], a)];
+            F.NelR[a] = boundary ? F.NelL[a] : s->el[F.elem[1]].N[orc::axis_of(F.side[1], a)];
             F.NfL[a] = F.NelL[a];
         }
         switch (F.rot) {

@@ -58,11 +58,20 @@ def set_threads(n: int) -> None:
 class Oracle:
     """One oracle solver on a mesh (a HexMesh or anything with a ``desc`` dg_mesh_desc)."""
 
-    def __init__(self, mesh, physics, options):
+    def __init__(self, mesh, physics, options, boundaries=None):
+        """boundaries: one DgBoundary per mesh zone (Config.boundary_table), required when the mesh
+        has non-periodic boundary faces."""
         self.mesh = mesh
         self.physics = physics
         self.options = options
-        self._h = lib().orc_create(C.byref(mesh.desc), C.byref(physics), C.byref(options))
+        desc = mesh.desc
+        if getattr(mesh, "n_boundary_faces", 0):
+            if boundaries is None:
+                raise ValueError("the mesh has boundary faces: pass the boundary conditions")
+            self._bc = boundaries
+            desc = mesh.with_boundaries(boundaries)
+        self._desc = desc
+        self._h = lib().orc_create(C.byref(desc), C.byref(physics), C.byref(options))
         self.ndof = int(lib().orc_ndof(self._h))
 
     def __del__(self):

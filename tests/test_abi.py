@@ -104,11 +104,15 @@ def test_mesh_builder_rejects_bad_input(tmp_path):
     assert L.h3d_mesh_read_specmesh(str(bad).encode(), 0, 3, None, b"", C.byref(h)) == _abi.DG_ERR_IO
 
 
-def test_non_periodic_mesh_is_rejected(tmp_path):
-    L = _abi.lib()
-    h = C.c_void_p()
+def test_non_periodic_mesh_has_boundary_zones(tmp_path):
+    m = HexMesh.from_specmesh(_write_single_hex(tmp_path), 2, periodic="")
+    assert m.n_faces == 6 and m.n_boundary_faces == 6
+    assert sorted(m.zone_names) == ["back", "bottom", "front", "left", "right", "top"]
+    # a boundary face without a zone name is an error
+    p = tmp_path / "one.mesh"
+    p.write_text(p.read_text().replace("front back", "--- back"))
     with pytest.raises(_abi.DgError):
-        HexMesh.from_specmesh(_write_single_hex(tmp_path), 2, periodic="")
+        HexMesh.from_specmesh(p, 2, periodic="")
 
 
 def _write_single_hex(tmp_path):
@@ -192,3 +196,44 @@ def test_anisotropic_order_keys(tmp_path):
     (tmp_path / "orders.omesh").write_text("3\n1 2 3\n4 5 6\n7 1 2\n")
     f = parse_control("polynomial order = 5\npolynomial order file = orders.omesh\nreynolds number = 1\n")
     assert f.element_orders(tmp_path).tolist() == [[1, 2, 3], [4, 5, 6], [7, 1, 2]]
+
+
+def test_boundary_blocks_of_a_control_file():
+    text = """mach number = 0.3
+reynolds number = 200
+AOA theta = 0.0
+AOA phi = 90.0
+#define boundary InnerCylinder
+  type = NoSlipWall
+#end
+#define boundary inlet
+  type = Inflow
+#end
+#define boundary outlet
+  type = Outflow
+  pressure = 50000
+#end
+#define boundary hot
+  type = NoSlipWall
+  wall type (adiabatic/isothermal) = isothermal
+  wall temperature = 400
+#end
+#define boundary bottom
+  type = periodic
+  coupled boundary = top
+#end
+"""
+    c = parse_control(text)
+    assert c.periodic == [("bottom", "top")] and c.aoa_phi == 90.0
+    wall = c.boundary("InnerCylinder")
+    assert wall.type == _abi.DG_BC_NO_SLIP_WALL and wall.isothermal == 0
+    hot = c.boundary("hot")
+    assert hot.isothermal == 1 and abs(hot.wall_temperature - 400.0 / (520.0 * 5.0 / 9.0)) < 1e-15
+    inflow = c.boundary("inlet")  # the free stream: unit density and speed along z
+    assert inflow.type == _abi.DG_BC_INFLOW and abs(inflow.rho - 1.0) < 1e-15 and abs(inflow.w - 1.0) < 1e-12
+    assert abs(inflow.p - 1.0 / (1.4 * 0.09)) < 1e-12
+    out = c.boundary("outlet")
+    ref = c._ref()
+    assert out.type == _abi.DG_BC_OUTFLOW and abs(out.pressure - 50000.0 / ref["p"]) < 1e-12
+    with pytest.raises(ValueError):
+        c.boundary("nowhere")

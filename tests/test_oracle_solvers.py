@@ -69,3 +69,35 @@ def test_rest_state_residual_on_nonconforming_curved_faces_is_linear_in_pressure
     o2 = oracle.Oracle(straight, cfg2.physics(), cfg2.options())
     o2.set_state(np.tile([1.0, 0.0, 0.0, 0.0, 1.0 / 0.4], straight.ndof))
     assert np.max(np.abs(o2.rhs(0.0))) < 1e-11
+
+
+def _channel(kind_y="noslipwall", n=(3, 2, 2), order=3, nodes=_abi.DG_NODES_GAUSS):
+    mesh = HexMesh.box(n, [0, 0, 0], [2.0, 1.0, 1.0], order, node_type=nodes, periodic="left:right,bottom:top")
+    cfg = cases.Config(order=order, nodes=nodes, mach=0.3, reynolds=100.0, riemann=_abi.DG_RIEMANN_LXF)
+    cfg.boundaries = {"front": {"type": kind_y}, "back": {"type": kind_y}}
+    return mesh, cfg
+
+
+@pytest.mark.parametrize("kind", ["noslipwall", "freeslipwall"])
+def test_walls_conserve_mass(kind):
+    """A channel with walls at y = 0, 1 (periodic in x and z): the mirrored ghost state carries no
+    mass through the walls, so sum w J dRho/dt = 0 for any state."""
+    mesh, cfg = _channel(kind)
+    assert mesh.n_boundary_faces == 2 * 3 * 2 and sorted(mesh.zone_names) == ["back", "front"]
+    o = oracle.Oracle(mesh, cfg.physics(), cfg.options(), cfg.boundary_table(mesh.zone_names))
+    rng = np.random.default_rng(3)
+    q = np.tile([1.0, 0.3, 0.0, 0.1, 1.0 / (0.4 * 1.4 * 0.09) + 0.05], mesh.ndof).reshape(-1, 5)
+    q = q * (1.0 + 0.02 * rng.standard_normal(q.shape))
+    o.set_state(q.reshape(-1))
+    qd = o.rhs(0.0).reshape(-1, 5)
+    w = cases.quadrature_weights(mesh)
+    assert abs(np.dot(w, qd[:, 0])) <= 1e-12 * np.dot(w, np.abs(qd[:, 0]))
+
+
+def test_free_slip_channel_keeps_a_uniform_axial_flow():
+    """Uniform flow along x between free-slip walls: the ghost state mirrors a zero normal velocity,
+    so the state is steady."""
+    mesh, cfg = _channel("freeslipwall")
+    o = oracle.Oracle(mesh, cfg.physics(), cfg.options(), cfg.boundary_table(mesh.zone_names))
+    o.set_state(np.tile([1.0, 0.4, 0.0, 0.0, 1.0 / (0.4 * 1.4 * 0.09) + 0.08], mesh.ndof))
+    assert np.max(np.abs(o.rhs(0.0))) < 1e-10
