@@ -81,6 +81,7 @@ int setup_store(dg_ctx* c, Store<R>& st, const dg_mesh_desc* m) {
         std::vector<double> sg(4 * nslot * P2);
         for (int f = 0; f < c->F; ++f)
             for (int side = 0; side < 2; ++side) {
+                if (m->face_elem[2 * f + side] < 0) continue;  // boundary face: one side
                 const size_t sl = 6 * static_cast<size_t>(m->face_elem[2 * f + side]) + (m->face_side[2 * f + side] - 1);
                 for (int cb = 0; cb < P; ++cb)
                     for (int ca = 0; ca < P; ++ca) {
@@ -94,6 +95,11 @@ int setup_store(dg_ctx* c, Store<R>& st, const dg_mesh_desc* m) {
             }
         if ((rc = upload_convert(st.sgeo, sg.data(), 4 * nslot * P2, c->stream))) return rc;
         CK(cudaStreamSynchronize(c->stream));
+    }
+    {  // boundary conditions in this precision
+        std::vector<dg::BoundaryR<R>> b(c->bcs.size());
+        for (size_t k = 0; k < c->bcs.size(); ++k) b[k] = dg::make_boundary<R>(c->bcs[k], c->pc);
+        CK(st.bcs.upload(b.data(), b.size(), c->stream));
     }
     CK(st.QDot.alloc(5 * nd));
     CK(cudaMemsetAsync(st.QDot.p, 0, sizeof(R) * 5 * nd, c->stream));
@@ -142,6 +148,7 @@ int setup_store(dg_ctx* c, Store<R>& st, const dg_mesh_desc* m) {
     dg::source_constants(c->opt.source, c->phys.mach, c->phys.reynolds, c->phys.prandtl, c->pc.ns, &a.src_mu,
                          &a.src_kappa);
     a.err = c->err_flag.p;
+    a.bc = st.bcs.p;
     return DG_OK;
 }
 
@@ -212,6 +219,29 @@ int set_scalars(dg_ctx* c, double t, double dt) {
     return DG_OK;
 }
 
+}  // namespace
+
+namespace h3dctx {
+
+// A boundary face (face_elem[2f+1] == -1) of a mesh description: one element side, a valid
+// condition index and a supported condition type.
+int validate_boundary_face(const dg_mesh_desc* m, int f) {
+    if (!m->face_boundary || !m->boundaries)
+        return h3d::fail(DG_ERR_INVALID, "a boundary face needs face_boundary and the boundaries table");
+    const int b = m->face_boundary[f];
+    if (b < 0 || b >= m->n_boundaries) return h3d::fail(DG_ERR_INVALID, "face_boundary outside 0..n_boundaries-1");
+    const int t = m->boundaries[b].type;
+    if (t < DG_BC_NO_SLIP_WALL || t > DG_BC_OUTFLOW) return h3d::fail(DG_ERR_UNSUPPORTED, "boundary condition type");
+    if (m->face_rotation[f] != 0) return h3d::fail(DG_ERR_INVALID, "a boundary face has rotation 0");
+    return DG_OK;
+}
+
+}  // namespace h3dctx
+
+namespace {
+
+using h3dctx::validate_boundary_face;
+
 int validate(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op) {
     if (!m || !ph || !op) return h3d::fail(DG_ERR_INVALID, "null argument");
     if (m->n_elements < 1 || m->n_faces < 1) return h3d::fail(DG_ERR_INVALID, "empty mesh");
@@ -227,18 +257,25 @@ int validate(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op) 
             if (m->order[3 * e + d] != N)
                 return h3d::fail(DG_ERR_UNSUPPORTED, "the GPU path needs one isotropic order on every element");
     if (N + 1 < 2 || N + 1 > dg::kMaxP) return h3d::fail(DG_ERR_UNSUPPORTED, "polynomial order outside 1..7");
-    if (2 * static_cast<int64_t>(m->n_faces) != 6 * static_cast<int64_t>(m->n_elements))
-        return h3d::fail(DG_ERR_UNSUPPORTED, "boundary faces are not supported (periodic/interior meshes only)");
+    int64_t sides = 0;
     for (int f = 0; f < m->n_faces; ++f) {
         if (m->face_nf[2 * f] != N || m->face_nf[2 * f + 1] != N)
             return h3d::fail(DG_ERR_INVALID, "face order differs from the element order");
         if (m->face_rotation[f] < 0 || m->face_rotation[f] > 7) return h3d::fail(DG_ERR_INVALID, "face rotation outside 0..7");
-        for (int s = 0; s < 2; ++s) {
+        const bool boundary = m->face_elem[2 * f + 1] < 0;
+        if (boundary) {
+            int rc = validate_boundary_face(m, f);
+            if (rc) return rc;
+        }
+        for (int s = 0; s < (boundary ? 1 : 2); ++s) {
             const int e = m->face_elem[2 * f + s], side = m->face_side[2 * f + s];
             if (e < 0 || e >= m->n_elements || side < 1 || side > 6)
                 return h3d::fail(DG_ERR_INVALID, "face connectivity out of range");
+            ++sides;
         }
     }
+    if (sides != 6 * static_cast<int64_t>(m->n_elements))
+        return h3d::fail(DG_ERR_INVALID, "the faces do not cover every element side once");
     if (ph->mach <= 0.0) return h3d::fail(DG_ERR_INVALID, "Mach number must be positive");
     if (ph->navier_stokes && ph->reynolds <= 0.0) return h3d::fail(DG_ERR_INVALID, "Reynolds number must be positive");
     if (op->inviscid != DG_INVISCID_STANDARD && op->inviscid != DG_INVISCID_SPLIT)
@@ -280,6 +317,7 @@ int dg_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op,
     auto* c = new dg_ctx();
     c->phys = *ph;
     c->opt = *op;
+    if (m->n_boundaries > 0 && m->boundaries) c->bcs.assign(m->boundaries, m->boundaries + m->n_boundaries);
     c->K = m->n_elements;
     c->F = m->n_faces;
     c->P = m->order[0] + 1;
@@ -347,23 +385,35 @@ int dg_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op,
     if ((e = c->face_elem.alloc(2 * c->F)) != cudaSuccess) return bail(cuda_fail(e, "alloc faces"));
     if ((e = c->face_side.alloc(2 * c->F)) != cudaSuccess) return bail(cuda_fail(e, "alloc faces"));
     if ((e = c->face_rot.alloc(c->F)) != cudaSuccess) return bail(cuda_fail(e, "alloc faces"));
+    std::vector<int> fside(m->face_side, m->face_side + 2 * c->F);
+    for (int f = 0; f < c->F; ++f)  // a boundary face's second entry holds its condition index on the device
+        if (m->face_elem[2 * f + 1] < 0) fside[2 * f + 1] = m->face_boundary[f];
     if ((e = cudaMemcpyAsync(c->face_elem.p, m->face_elem, sizeof(int) * 2 * c->F, cudaMemcpyHostToDevice, c->stream)) ||
-        (e = cudaMemcpyAsync(c->face_side.p, m->face_side, sizeof(int) * 2 * c->F, cudaMemcpyHostToDevice, c->stream)) ||
-        (e = cudaMemcpyAsync(c->face_rot.p, m->face_rotation, sizeof(int) * c->F, cudaMemcpyHostToDevice, c->stream)))
+        (e = cudaMemcpyAsync(c->face_side.p, fside.data(), sizeof(int) * 2 * c->F, cudaMemcpyHostToDevice, c->stream)) ||
+        (e = cudaMemcpyAsync(c->face_rot.p, m->face_rotation, sizeof(int) * c->F, cudaMemcpyHostToDevice, c->stream)) ||
+        (e = cudaStreamSynchronize(c->stream)))
         return bail(cuda_fail(e, "copy faces"));
     {  // slot neighbour tables: the other side's slot and (rotation | own side << 3)
         const size_t nslot = 6 * static_cast<size_t>(c->K);
         std::vector<int> nbs(nslot, -1), nbm(nslot, 0);
+        std::vector<char> seen(nslot, 0);
         for (int f = 0; f < c->F; ++f)
             for (int side = 0; side < 2; ++side) {
+                if (m->face_elem[2 * f + side] < 0) continue;
                 const size_t sl = 6 * static_cast<size_t>(m->face_elem[2 * f + side]) + (m->face_side[2 * f + side] - 1);
+                if (seen[sl]) return bail(h3d::fail(DG_ERR_INVALID, "an element side belongs to two faces"));
+                seen[sl] = 1;
+                if (m->face_elem[2 * f + 1] < 0) {  // boundary: -1 - condition index, own side 1
+                    nbs[sl] = -1 - m->face_boundary[f];
+                    nbm[sl] = 1 << 3;
+                    continue;
+                }
                 const size_t so = 6 * static_cast<size_t>(m->face_elem[2 * f + 1 - side]) + (m->face_side[2 * f + 1 - side] - 1);
-                if (nbs[sl] != -1) return bail(h3d::fail(DG_ERR_INVALID, "an element side belongs to two faces"));
                 nbs[sl] = static_cast<int>(so);
                 nbm[sl] = m->face_rotation[f] | ((side + 1) << 3);
             }
         for (size_t sl = 0; sl < nslot; ++sl)
-            if (nbs[sl] < 0) return bail(h3d::fail(DG_ERR_INVALID, "an element side has no face"));
+            if (!seen[sl]) return bail(h3d::fail(DG_ERR_INVALID, "an element side has no face"));
         if ((e = c->nb_slot.alloc(nslot)) != cudaSuccess || (e = c->nb_map.alloc(nslot)) != cudaSuccess)
             return bail(cuda_fail(e, "alloc slot tables"));
         if ((e = cudaMemcpy(c->nb_slot.p, nbs.data(), sizeof(int) * nslot, cudaMemcpyHostToDevice)) != cudaSuccess ||

@@ -51,6 +51,7 @@ template <typename R>
 struct Store {
     DevBuf<R> ja_xi, ja_eta, ja_zeta, jac, inv_jac, fn, ft1, ft2, fj, sgeo;
     DevBuf<R> QDot, Ux, Uy, Uz, QF, FV, FS;
+    DevBuf<dg::BoundaryR<R>> bcs;
     dg::Args<R> args;
     dg::StageFn<R> stage = nullptr;
     dg::KernelTimesFn<R> times = nullptr;
@@ -58,6 +59,7 @@ struct Store {
         for (DevBuf<R>* b : {&ja_xi, &ja_eta, &ja_zeta, &jac, &inv_jac, &fn, &ft1, &ft2, &fj, &sgeo, &QDot, &Ux, &Uy,
                              &Uz, &QF, &FV, &FS})
             b->free();
+        bcs.free();
     }
 };
 
@@ -90,6 +92,7 @@ struct dg_ctx {
     int64_t ndof = 0;
     dg_physics phys{};
     dg_options opt{};
+    std::vector<dg_boundary> bcs;  // boundary conditions of the (first) case's zones
     dg::PhysConst pc{};
     bool mixed = false;
     double dxi[3] = {0, 0, 0};

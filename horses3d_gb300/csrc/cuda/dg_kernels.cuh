@@ -79,6 +79,7 @@ struct Args {
     const double* time;  // device scalars: step start time and dt
     const double* dt;
     double e_ref;        // energy reference of the mixed form (0 for the plain form)
+    const BoundaryR<R>* bc;  // boundary conditions (a boundary slot has nb_slot = -1 - its index)
     int* err;            // set by a kernel whose bounded wait on a bulk copy gave up
     uint32_t extra_tx;   // bytes the update kernel's mbarrier expects beyond its copies (fault injection; 0)
     // manufactured-solution source constants
@@ -388,18 +389,26 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
                 trace5<P, GL, 1>(a.ops, Q4, Q1, P3, side, ca, cb, own);
                 st5(T4, t, T1, t, own[0]);
                 const int map = a.nb_map[s];
-                const int pn = neighbour_point<P>(map, ca, cb);
-                gld5(a.QF, a.nsp, static_cast<int64_t>(a.nb_slot[s]) * P2 + pn, nbr);
+                const int nb = a.nb_slot[s];
                 const R* sg = a.sgeo + s * 4 * P2 + p;
                 const R nn[3] = {sg[0], sg[P2], sg[2 * P2]};
                 const R J = sg[3 * P2];
-                const bool left = (map >> 3) == 1;
-                R uo[5], un[5];
+                R uo[5], u[5];
                 gradient_variables(a.ph, own[0], uo);
-                gradient_variables(a.ph, nbr, un);
-                R u[5];
+                if (nb < 0) {  // boundary: (U* - U) Jf n (EllipticBR1.f90:686-736)
+                    R us[5];
+                    bc_gradvars(a.ph, a.bc[-1 - nb], nn, own[0], uo, us);
 #pragma unroll
-                for (int v = 0; v < 5; ++v) u[v] = R(0.5) * (left ? (un[v] - uo[v]) : (uo[v] - un[v])) * J;
+                    for (int v = 0; v < 5; ++v) u[v] = (us[v] - uo[v]) * J;
+                } else {
+                    const int pn = neighbour_point<P>(map, ca, cb);
+                    gld5(a.QF, a.nsp, static_cast<int64_t>(nb) * P2 + pn, nbr);
+                    const bool left = (map >> 3) == 1;
+                    R un[5];
+                    gradient_variables(a.ph, nbr, un);
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) u[v] = R(0.5) * (left ? (un[v] - uo[v]) : (uo[v] - un[v])) * J;
+                }
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
                     R x[5];
@@ -614,13 +623,21 @@ __global__ void __launch_bounds__(128) k_flux(Args<R> a) {
     int ii, jj;
     left2right(p % P, p / P, P - 1, P - 1, a.face_rot[f], ii, jj);
     const int pr = ii + P * jj;
+    const int eR = a.face_elem[2 * f + 1];
+    const bool boundary = eR < 0;  // a boundary face: its condition's ghost state is the right side
     const int64_t iL = slot(a.face_elem[2 * f], a.face_side[2 * f]) * P2 + p;
-    const int64_t iR = slot(a.face_elem[2 * f + 1], a.face_side[2 * f + 1]) * P2 + pr;
-    R QL[5], QR[5];
-    gld5(a.QF, a.nsp, iL, QL);
-    gld5(a.QF, a.nsp, iR, QR);
+    const int64_t iR = boundary ? iL : slot(eR, a.face_side[2 * f + 1]) * P2 + pr;
     const R n[3] = {a.fn[gid], a.fn[nfp + gid], a.fn[2 * nfp + gid]};
     const R J = a.fj[gid];
+    R QL[5], QR[5];
+    gld5(a.QF, a.nsp, iL, QL);
+    if (boundary) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) QR[v] = QL[v];
+        bc_state(a.ph, a.bc[a.face_side[2 * f + 1]], n, QR);
+    } else {
+        gld5(a.QF, a.nsp, iR, QR);
+    }
     R inv[5];
     if (GEN) {  // standard Roe, Roe-Pike, low-dissipation Roe, matrix dissipation, viscous NS
         const R t1[3] = {a.ft1[gid], a.ft1[nfp + gid], a.ft1[2 * nfp + gid]};
@@ -638,7 +655,13 @@ __global__ void __launch_bounds__(128) k_flux(Args<R> a) {
     R vL[5] = {0, 0, 0, 0, 0}, vR[5] = {0, 0, 0, 0, 0};
     if (a.ph.ns) {
         gld5(a.FV, a.nsp, iL, vL);
-        gld5(a.FV, a.nsp, iR, vR);
+        if (boundary) {  // the interior viscous flux through the condition's Neumann rule
+            bc_neumann(a.bc[a.face_side[2 * f + 1]], QL, vL);
+#pragma unroll
+            for (int v = 0; v < 5; ++v) vR[v] = vL[v];
+        } else {
+            gld5(a.FV, a.nsp, iR, vR);
+        }
     }
     R fl[5], fr[5];
 #pragma unroll
@@ -648,7 +671,7 @@ __global__ void __launch_bounds__(128) k_flux(Args<R> a) {
         fr[v] = -fl[v];
     }
     gst5(a.FS, a.nsp, iL, fl);
-    gst5(a.FS, a.nsp, iR, fr);
+    if (!boundary) gst5(a.FS, a.nsp, iR, fr);
 }
 
 // Surface integral in the reference's order (left, right, front, back, bottom, top), division by J

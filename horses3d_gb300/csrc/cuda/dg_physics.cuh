@@ -4,6 +4,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "horses3d_gb300.h"
+
 namespace dg {
 
 // Derived physics constants (PhysicsStorage_NS.f90:186-429), host-filled.
@@ -925,6 +927,129 @@ inline void source_constants(int kind, double mach, double reynolds, double pran
     } else {
         *mu = 1.0 / reynolds;
         *kap = 1.0 / (gm1 * (mach * mach) * reynolds * prandtl);
+    }
+}
+
+// ---- boundary conditions (physics/common/*BC.f90, NAVIERSTOKES parts) ----------------------------
+// The energies of the state vectors are the stored ones (E' = E - e_ref in the mixed form); the
+// formulas are arranged so that the reference energy cancels where it does in exact arithmetic.
+template <typename R>
+struct BoundaryR {
+    int type;
+    R wt;          // 1 isothermal, 0 adiabatic (wallType)
+    R ewall;       // T_w/T_ref / ((gamma-1) gamma M^2): wall internal energy
+    R pwall;       // T_w/T_ref / (gamma M^2): wall pressure per unit density
+    R vw[3];       // no-slip wall velocity
+    R rho, u, v, w, E;  // inflow state (absolute total energy)
+    R pext;        // outflow pressure
+};
+
+template <typename R>
+BoundaryR<R> make_boundary(const dg_boundary& b, const PhysConst& c) {
+    BoundaryR<R> r;
+    r.type = b.type;
+    r.wt = R(b.isothermal ? 1.0 : 0.0);
+    r.ewall = R(b.wall_temperature / (c.gammaM2 * c.gm1));
+    r.pwall = R(b.wall_temperature / c.gammaM2);
+    for (int k = 0; k < 3; ++k) r.vw[k] = R(b.wall_velocity[k]);
+    r.rho = R(b.rho); r.u = R(b.u); r.v = R(b.v); r.w = R(b.w);
+    r.E = R(b.p / (c.gamma - 1.0) + 0.5 * b.rho * (b.u * b.u + b.v * b.v + b.w * b.w));
+    r.pext = R(b.pressure);
+    return r;
+}
+
+// FlowState: the external state of the Riemann problem (NoSlipWallBC.f90:265-296,
+// FreeSlipWallBC.f90:249-286, InflowBC.f90:363-406, OutflowBC.f90:226-288).
+template <typename R>
+__device__ __forceinline__ void bc_state(const PhysR<R>& p, const BoundaryR<R>& b, const R* n, R* Q) {
+    if (b.type == 1) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) Q[1 + c] = R(2) * Q[0] * b.vw[c] - Q[1 + c];
+        Q[4] = Q[4] + b.wt * (Q[0] * b.ewall - p.e_ref - Q[4]);
+    } else if (b.type == 2) {
+        const R qn = n[0] * Q[1] + n[1] * Q[2] + n[2] * Q[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) Q[1 + c] = Q[1 + c] - R(2) * qn * n[c];
+        const R pa = Q[0] * b.pwall;
+        Q[4] = Q[4] + b.wt * (pa / p.gm1 + R(0.5) * (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) / Q[0] - p.e_ref - Q[4]);
+    } else if (b.type == 3) {
+        Q[0] = b.rho;
+        Q[1] = b.rho * b.u;
+        Q[2] = b.rho * b.v;
+        Q[3] = b.rho * b.w;
+        Q[4] = b.E - p.e_ref;
+    } else {
+        R qn = (n[0] * Q[1] + n[1] * Q[2] + n[2] * Q[3]) / Q[0];
+        const R tx = Q[1] / Q[0] - qn * n[0], ty = Q[2] / Q[0] - qn * n[1], tz = Q[3] / Q[0] - qn * n[2];
+        const R pr = p.gm1 * (Q[4] - R(0.5) * (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) / Q[0]) + p.p_ref;
+        const R a2 = p.gamma * pr / Q[0];
+        R a = dsqrt(a2);
+        if (fabs(qn / a) <= R(1)) {
+            const R rPlus = qn + R(2) * a / p.gm1;
+            const R ent = pr - a2 * Q[0];
+            const R rho = -(ent - b.pext) / a2;
+            a = dsqrt(p.gamma * b.pext / rho);
+            qn = rPlus - R(2) * a / p.gm1;
+            const R u = tx + qn * n[0], v = ty + qn * n[1], w = tz + qn * n[2];
+            Q[0] = rho;
+            Q[1] = rho * u;
+            Q[2] = rho * v;
+            Q[3] = rho * w;
+            Q[4] = b.pext / p.gm1 + R(0.5) * rho * (u * u + v * v + w * w) - p.e_ref;
+        }
+    }
+}
+
+// FlowGradVars: U* at the boundary from the interior state Q and its gradient variables U
+// (NoSlipWallBC.f90:298-337, FreeSlipWallBC.f90:288-318, GenericBC_FlowGradVars for in/outflow).
+template <typename R>
+__device__ __forceinline__ void bc_gradvars(const PhysR<R>& p, const BoundaryR<R>& b, const R* n, const R* Q,
+                                            const R* U, R* Us) {
+    R Qa[5];
+    if (b.type == 1) {
+        const R m2 = (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) / Q[0];
+        const R kw = R(0.5) * Q[0] * (b.vw[0] * b.vw[0] + b.vw[1] * b.vw[1] + b.vw[2] * b.vw[2]);
+        Qa[0] = Q[0];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) Qa[1 + c] = Q[0] * b.vw[c];
+        // rho ((1 - wt) e_int + wt e_wall + |v_w|^2 / 2), relative to e_ref
+        Qa[4] = (R(1) - b.wt) * (Q[4] - R(0.5) * m2) + b.wt * (Q[0] * b.ewall - p.e_ref) + kw;
+        gradient_variables(p, Qa, Us);
+        Us[0] = U[0];
+    } else if (b.type == 2) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) Qa[c] = Q[c];
+        Qa[4] = Q[4] + b.wt * (Q[0] * b.ewall + R(0.5) * (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) / Q[0] - p.e_ref - Q[4]);
+        gradient_variables(p, Qa, Us);
+    } else {
+#pragma unroll
+        for (int c = 0; c < 5; ++c) Qa[c] = Q[c];
+        bc_state(p, b, n, Qa);
+        R Ua[5];
+        gradient_variables(p, Qa, Ua);
+#pragma unroll
+        for (int c = 0; c < 5; ++c) Us[c] = R(0.5) * (Ua[c] + U[c]);
+    }
+}
+
+// FlowNeumann: the boundary's viscous normal flux from the interior one (NoSlipWallBC.f90:339-372,
+// FreeSlipWallBC.f90:320-351; inflow and outflow cancel it).
+template <typename R>
+__device__ __forceinline__ void bc_neumann(const BoundaryR<R>& b, const R* Q, R* f) {
+    if (b.type == 1) {
+        const R ir = R(1) / Q[0];
+        const R work = (ir * Q[1]) * f[1] + (ir * Q[2]) * f[2] + (ir * Q[3]) * f[3];
+        const R heat = f[4] - work;
+        f[0] = R(0);
+        f[4] = (b.vw[0] * f[1] + b.vw[1] * f[2] + b.vw[2] * f[3]) + b.wt * heat;
+    } else if (b.type == 2) {
+        const R work = (f[1] * Q[1] + f[2] * Q[2] + f[3] * Q[3]) / Q[0];
+        const R heat = f[4] - work;
+        f[0] = f[1] = f[2] = f[3] = R(0);
+        f[4] = b.wt * heat;
+    } else {
+#pragma unroll
+        for (int c = 0; c < 5; ++c) f[c] = R(0);
     }
 }
 

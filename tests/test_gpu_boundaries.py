@@ -1,0 +1,133 @@
+"""Non-periodic boundary conditions on the GPU against the oracle, through the C ABI: no-slip and
+free-slip walls (adiabatic and isothermal, moving), inflow and outflow, on uniform orders (plain
+and mixed form)."""
+import dataclasses
+
+import numpy as np
+import pytest
+
+import cases
+import oracle
+from horses3d_gb300 import _abi
+from horses3d_gb300.mesh import HexMesh
+from horses3d_gb300.problems import rel_l2
+from horses3d_gb300.solver import NavierStokesDG
+
+pytestmark = pytest.mark.gpu
+
+STATE_TOL = 1e-12
+RHS_TOL = 1e-10
+MIXED_TOL = 1e-6
+
+
+def _state(mesh, mach, seed=0, amp=0.02, u0=(0.3, 0.0, 0.1)):
+    rng = np.random.default_rng(seed)
+    x = mesh.x
+    rho = 1.0 + amp * np.sin(x[:, 0]) * np.cos(x[:, 1] + 0.3) + amp * rng.standard_normal(mesh.ndof) * 0.1
+    u = u0[0] + amp * np.cos(x[:, 2])
+    v = u0[1] + amp * np.sin(x[:, 0] + x[:, 2])
+    w = u0[2] + amp * np.cos(x[:, 1])
+    p = 1.0 / (1.4 * mach ** 2) * (1.0 + amp * np.sin(x[:, 1]))
+    q = np.stack([rho, rho * u, rho * v, rho * w, p / 0.4 + 0.5 * rho * (u * u + v * v + w * w)], axis=1)
+    return q.reshape(-1)
+
+
+def _channel(y_kind, x_kinds=None, order=3, nodes=_abi.DG_NODES_GAUSS, n=(3, 2, 2), warp=0.0, **bc):
+    """[0, 2 pi] x [0, 2 pi] x [0, 2 pi]: walls of y_kind at y = 0, 2 pi; x periodic unless x_kinds
+    gives (left, right) conditions; z periodic."""
+    periodic = "bottom:top" + ("" if x_kinds else ",left:right")
+    mesh = HexMesh.box(n, [0, 0, 0], [2 * np.pi] * 3, order, node_type=nodes, warp=warp,
+                       patch_order=order if warp else 0, periodic=periodic)
+    cfg = cases.Config(order=order, nodes=nodes, mach=0.3, reynolds=150.0, riemann=_abi.DG_RIEMANN_ROE)
+    cfg.boundaries = {"front": dict({"type": y_kind}, **bc), "back": dict({"type": y_kind}, **bc)}
+    if x_kinds:
+        cfg.boundaries["left"] = {"type": x_kinds[0]}
+        cfg.boundaries["right"] = {"type": x_kinds[1]}
+    return mesh, cfg
+
+
+def _pair(mesh, cfg, q0):
+    o = oracle.Oracle(mesh, cfg.physics(), cfg.options(), cfg.boundary_table(mesh.zone_names))
+    o.set_state(q0)
+    g = NavierStokesDG(mesh, cfg)
+    g.set_state(q0)
+    return o, g
+
+
+def _check(mesh, cfg, q0, steps=2, dt=1e-3):
+    o, g = _pair(mesh, cfg, q0)
+    ref = o.rhs(0.0)
+    g.compute_time_derivative(0.0)
+    err = rel_l2(g.QDot, ref)
+    assert np.all(err <= RHS_TOL), err
+    if cfg.flow == "ns":
+        for f in (_abi.DG_FIELD_UX, _abi.DG_FIELD_UY, _abi.DG_FIELD_UZ):
+            gr = o.get(f)
+            e2 = np.max(np.abs(g.get(f) - gr)) / max(np.max(np.abs(gr)), 1e-300)
+            assert e2 <= RHS_TOL, (f, e2)
+    o, g = _pair(mesh, cfg, q0)
+    t = 0.0
+    for _ in range(steps):
+        o.rk3_step(t, dt)
+        g.take_rk3_step(t, dt)
+        t += dt
+    w = cases.quadrature_weights(mesh)
+    err = rel_l2(g.Q, o.get(0), w)
+    assert np.all(err <= STATE_TOL), err
+    mixed = dataclasses.replace(cfg, precision=_abi.DG_PRECISION_MIXED)
+    o, gm = _pair(mesh, mixed, q0)
+    t = 0.0
+    for _ in range(steps):
+        o.rk3_step(t, dt)
+        gm.take_rk3_step(t, dt)
+        t += dt
+    err = rel_l2(gm.Q, o.get(0), w)
+    assert np.all(err <= MIXED_TOL), err
+
+
+@pytest.mark.parametrize("nodes", [_abi.DG_NODES_GAUSS, _abi.DG_NODES_GAUSS_LOBATTO])
+def test_no_slip_walls(nodes):
+    mesh, cfg = _channel("noslipwall", nodes=nodes)
+    _check(mesh, cfg, _state(mesh, cfg.mach))
+
+
+def test_isothermal_moving_no_slip_walls():
+    mesh, cfg = _channel("noslipwall", **{"wall type (adiabatic/isothermal)": "isothermal",
+                                          "wall temperature": 310.0, "wall velocity": "[0.2, 0.0, -0.1]"})
+    _check(mesh, cfg, _state(mesh, cfg.mach, seed=1))
+
+
+@pytest.mark.parametrize("wt", ["adiabatic", "isothermal"])
+def test_free_slip_walls(wt):
+    mesh, cfg = _channel("freeslipwall", **{"wall type (adiabatic/isothermal)": wt})
+    _check(mesh, cfg, _state(mesh, cfg.mach, seed=2))
+
+
+@pytest.mark.parametrize("riemann", [_abi.DG_RIEMANN_ROE, _abi.DG_RIEMANN_LXF, _abi.DG_RIEMANN_MATRIX_DISS])
+def test_inflow_outflow_channel(riemann):
+    mesh, cfg = _channel("noslipwall", x_kinds=("inflow", "outflow"), order=4)
+    cfg = dataclasses.replace(cfg, riemann=riemann, aoa_theta=0.0, aoa_phi=0.0)
+    _check(mesh, cfg, _state(mesh, cfg.mach, seed=3, u0=(1.0, 0.0, 0.0)))
+
+
+def test_split_form_walls_entropy_variables():
+    mesh, cfg = _channel("noslipwall", nodes=_abi.DG_NODES_GAUSS_LOBATTO, order=4, warp=0.1)
+    cfg = dataclasses.replace(cfg, inviscid=_abi.DG_INVISCID_SPLIT, averaging=_abi.DG_AVG_CHANDRASEKAR,
+                              riemann=_abi.DG_RIEMANN_CENTRAL, gradient_variables=_abi.DG_GRADVARS_ENTROPY)
+    _check(mesh, cfg, _state(mesh, cfg.mach, seed=4))
+
+
+def test_euler_walls_and_graph_replay():
+    """Euler equations between free-slip walls; graph-replayed steps equal single steps bit for bit."""
+    mesh, cfg = _channel("freeslipwall", order=3)
+    cfg = dataclasses.replace(cfg, flow="euler")
+    q0 = _state(mesh, cfg.mach, seed=5)
+    _check(mesh, cfg, q0)
+    g1 = NavierStokesDG(mesh, cfg)
+    g1.set_state(q0)
+    for k in range(3):
+        g1.take_rk3_step(k * 1e-3, 1e-3)
+    g2 = NavierStokesDG(mesh, cfg)
+    g2.set_state(q0)
+    g2.run_steps(3, 0.0, dt=1e-3)
+    assert np.array_equal(g1.Q, g2.Q)
