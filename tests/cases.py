@@ -123,6 +123,47 @@ def lamb_vector_l2_error(mesh, q, t):
     return float(np.sqrt(np.sum(J * w3[None, :] * d2) / mesh.n_elements))
 
 
+GOLDEN_DIR = __import__("pathlib").Path(__file__).resolve().parent / "golden"
+
+# Solver/test/NavierStokes/{Energy,Entropy}ConservingTest/SETUP/ProblemFile.f90:555-561 (tol 1e-11 on
+# x+1, 1e-10 for the y-momentum)
+CONSERVING_GOLDENS = {
+    "EnergyConservingTest": np.array([8.4536070422136675E+01, 2.1762123673954497E+02, 6.4602872675548434E-11,
+                                      4.0133134577655784E+02, 2.3743041720710371E+03]),
+    "EntropyConservingTest": np.array([8.2631424496364474E+01, 2.2430272815501075E+02, 6.4161760571618557E-11,
+                                       4.1620680221184398E+02, 2.3047571785589912E+03]),
+}
+
+
+def conserving_cylinder_config(test):
+    """The configuration of {Energy,Entropy}ConservingTest.control: N=5 on Gauss-Lobatto nodes (split
+    form), central fluxes, Pirozzoli + energy / Chandrasekar + entropy gradient variables, M=0.3,
+    Re=200, AoA phi 90, CFL 0.3 for 10 steps, no-slip walls on the cylinder and the side walls."""
+    energy = test == "EnergyConservingTest"
+    cfg = Config(order=5, nodes=_abi.DG_NODES_GAUSS_LOBATTO, mach=0.3, reynolds=200.0, riemann=_abi.DG_RIEMANN_CENTRAL,
+                 inviscid=_abi.DG_INVISCID_SPLIT,
+                 averaging=_abi.DG_AVG_PIROZZOLI if energy else _abi.DG_AVG_CHANDRASEKAR,
+                 gradient_variables=_abi.DG_GRADVARS_ENERGY if energy else _abi.DG_GRADVARS_ENTROPY,
+                 cfl=0.3, dcfl=0.3, n_steps=10, aoa_theta=0.0, aoa_phi=90.0)
+    cfg.periodic = [("bottom", "top"), ("back", "front")]
+    cfg.boundaries = {z: {"type": "noslipwall"} for z in ("innercylinder", "left", "right")}
+    return cfg
+
+
+def cylinder_mesh(cfg, tmp_dir):
+    """CylinderNSpol3.mesh from the committed fixture (tests/golden/make_fixtures.py)."""
+    import gzip
+
+    path = __import__("pathlib").Path(tmp_dir) / "CylinderNSpol3.mesh"
+    path.write_bytes(gzip.decompress((GOLDEN_DIR / "CylinderNSpol3.mesh.gz").read_bytes()))
+    return HexMesh.from_specmesh(path, cfg.order, node_type=cfg.nodes, periodic=cfg.periodic_spec())
+
+
+def free_stream_state(cfg, mesh):
+    rho, u, v, w, p = cfg.free_stream()
+    return np.tile([rho, rho * u, rho * v, rho * w, p / 0.4 + 0.5 * rho * (u * u + v * v + w * w)], mesh.ndof)
+
+
 def ftassert_equal(expected, actual, tol):
     """FTAssertEqual of two reals (ftobject/Comparisons.f90:238-255): relative tolerance, absolute
     below tol."""

@@ -131,3 +131,19 @@ def test_euler_walls_and_graph_replay():
     g2.set_state(q0)
     g2.run_steps(3, 0.0, dt=1e-3)
     assert np.array_equal(g1.Q, g2.Q)
+
+
+@pytest.mark.parametrize("test", ["EnergyConservingTest", "EntropyConservingTest"])
+def test_conserving_cylinder_cases_reach_the_reference_goldens(test, tmp_path):
+    """{Energy,Entropy}ConservingTest on the GPU through the reference-shaped driver: the five
+    residuals after 10 CFL steps equal the goldens (tol 1e-11 on x+1, 1e-10 for the y-momentum)."""
+    cfg = cases.conserving_cylinder_config(test)
+    mesh = cases.cylinder_mesh(cfg, tmp_path)
+    g = NavierStokesDG(mesh, cfg)
+    g.set_state(cases.free_stream_state(cfg, mesh))
+    rep = g.integrate_in_time(t0=0.0, compute_after_steps=True)
+    assert rep.iterations == 10
+    gold = cases.CONSERVING_GOLDENS[test]
+    res = rep.residuals
+    assert cases.ftassert_close(gold[[0, 1, 3, 4]], res[[0, 1, 3, 4]], 1e-11), res - gold
+    assert cases.ftassert_close(gold[2], res[2], 1e-10), res - gold

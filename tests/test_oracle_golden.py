@@ -109,33 +109,30 @@ def test_lamb_vector_golden_reference_mesh_file():
     assert cases.ftassert_equal(cases.LAMB_VECTOR_L2, err, 1e-7), err - cases.LAMB_VECTOR_L2
 
 
-CYL_MESH = Path("/root/reference/Solver/test/TestMeshes/CylinderNSpol3.mesh")
 CONSERVING_TESTS = Path("/root/reference/Solver/test/NavierStokes")
-# Solver/test/NavierStokes/{Energy,Entropy}ConservingTest/SETUP/ProblemFile.f90:555-561 (tol 1e-11 on
-# x+1, 1e-10 for the y-momentum)
-CONSERVING_GOLDENS = {
-    "EnergyConservingTest": np.array([8.4536070422136675E+01, 2.1762123673954497E+02, 6.4602872675548434E-11,
-                                      4.0133134577655784E+02, 2.3743041720710371E+03]),
-    "EntropyConservingTest": np.array([8.2631424496364474E+01, 2.2430272815501075E+02, 6.4161760571618557E-11,
-                                       4.1620680221184398E+02, 2.3047571785589912E+03]),
-}
 
 
-@pytest.mark.skipif(not CYL_MESH.exists(), reason="reference mesh and control files not mounted")
 @pytest.mark.parametrize("test", ["EnergyConservingTest", "EntropyConservingTest"])
-def test_conserving_cylinder_goldens(test):
+def test_conserving_cylinder_goldens(test, tmp_path):
     """Flow past a cylinder (CylinderNSpol3.mesh, curved N=3 boundary patches) with no-slip walls on
     the cylinder and the side walls, periodic elsewhere: split form (Pirozzoli / Chandrasekar),
     central fluxes, energy / entropy gradient variables, N=5, 10 CFL steps from the free stream.
-    The reference's own control file drives the case; the five residuals are the goldens."""
-    from horses3d_gb300.control import read_control
+    The five residuals are the goldens. Where the reference is mounted, its own control file must
+    give the same configuration."""
+    cfg = cases.conserving_cylinder_config(test)
+    control = CONSERVING_TESTS / test / f"{test}.control"
+    if control.exists():
+        from horses3d_gb300.control import read_control
 
-    cfg = read_control(CONSERVING_TESTS / test / f"{test}.control")
-    mesh = HexMesh.from_specmesh(CYL_MESH, cfg.order, node_type=cfg.nodes, periodic=cfg.periodic_spec())
+        rc = read_control(control)
+        for k in ("order", "nodes", "mach", "reynolds", "riemann", "inviscid", "averaging", "gradient_variables",
+                  "cfl", "dcfl", "n_steps", "aoa_theta", "aoa_phi", "periodic"):
+            assert getattr(rc, k) == getattr(cfg, k), k
+        assert {z: b["type"] for z, b in rc.boundaries.items()} == {z: b["type"] for z, b in cfg.boundaries.items()}
+    mesh = cases.cylinder_mesh(cfg, tmp_path)
     assert mesh.n_boundary_faces == 168 and set(mesh.zone_names) == {"innercylinder", "left", "right"}
     o = oracle.Oracle(mesh, cfg.physics(), cfg.options(), cfg.boundary_table(mesh.zone_names))
-    rho, u, v, w, p = cfg.free_stream()
-    o.set_state(np.tile([rho, rho * u, rho * v, rho * w, p / 0.4 + 0.5 * rho * (u * u + v * v + w * w)], mesh.ndof))
+    o.set_state(cases.free_stream_state(cfg, mesh))
     t = 0.0
     for _ in range(cfg.n_steps):
         dt = o.max_dt(cfg.cfl, cfg.dcfl)
@@ -143,7 +140,7 @@ def test_conserving_cylinder_goldens(test):
         t += dt
     o.rhs(t)  # "compute time derivative after timestep = .true."
     res, nan = o.residuals()
-    g = CONSERVING_GOLDENS[test]
+    g = cases.CONSERVING_GOLDENS[test]
     assert not nan
     assert cases.ftassert_close(g[[0, 1, 3, 4]], res[[0, 1, 3, 4]], 1e-11), res - g
     assert cases.ftassert_close(g[2], res[2], 1e-10), res - g
