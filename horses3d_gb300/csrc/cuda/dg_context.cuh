@@ -70,6 +70,7 @@ struct VStore {
     DevBuf<R> QDot, Ux, Uy, Uz, QF, GF, UJ, FS;
     DevBuf<dg::OpsP<R>> ops;
     DevBuf<dg::PhysR<R>> ph;
+    DevBuf<dg::BoundaryR<R>> bcs;
     dg::VArgs<R> args;
     dg::VStageFn<R> stage = nullptr;
     dg::VTimesFn<R> times = nullptr;
@@ -80,6 +81,7 @@ struct VStore {
             b->free();
         ops.free();
         ph.free();
+        bcs.free();
     }
 };
 
@@ -92,7 +94,8 @@ struct dg_ctx {
     int64_t ndof = 0;
     dg_physics phys{};
     dg_options opt{};
-    std::vector<dg_boundary> bcs;  // boundary conditions of the (first) case's zones
+    std::vector<dg_boundary> bcs;  // boundary conditions (variable-order path: of all cases, appended)
+    std::vector<int> bc_case;      // variable-order path: the case of each boundary condition
     dg::PhysConst pc{};
     bool mixed = false;
     double dxi[3] = {0, 0, 0};
@@ -138,6 +141,10 @@ struct dg_ctx {
 };
 
 // Variable-order / multi-case path (dg_var_api.cu).
+namespace h3dctx {
+int validate_boundary_face(const dg_mesh_desc* m, int f);  // dg_api.cu
+}
+
 namespace h3dvar {
 bool needs_variable_path(const dg_mesh_desc* m);
 int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, const dg_options* opt, dg_ctx** out);

@@ -96,6 +96,7 @@ struct VArgs {
     // of the state at rest with unit pressure (3 values), added times p_ref in the update; null when
     // the geometry preserves a uniform state to round-off.
     const double* pstat;
+    const BoundaryR<R>* bc;  // boundary conditions of all cases (a boundary face's record holds its index)
     const R* fn;                // face points, 3 per point
     const R* ft1;
     const R* ft2;
@@ -721,12 +722,14 @@ __global__ void __launch_bounds__(128) kv_face_direct(VArgs<R> a) {
     const int i = p % q1, j = p / q1;
     const int4 fd = a.faces[f];
     const int eL = fd.x, eR = fd.y, sL = fd.z & 15, sR = (fd.z >> 4) & 15, rot = (fd.z >> 8) & 15;
-    int r1, r2;
-    side_dims(sR, a.eord[eR], r1, r2);
-    int ii, jj;
-    left2right(i, j, q1 - 1, q2 - 1, rot, ii, jj);
+    const bool boundary = eR < 0;  // one element side; the condition index sits in bits 20.. of z
+    int r1 = q1, r2 = q2;
+    if (!boundary) side_dims(sR, a.eord[eR], r1, r2);
+    int ii = i, jj = j;
+    if (!boundary) left2right(i, j, q1 - 1, q2 - 1, rot, ii, jj);
     const int pr = ii + r1 * jj;
-    const long long offL = a.soff[6LL * eL + sL - 1], offR = a.soff[6LL * eR + sR - 1];
+    const long long offL = a.soff[6LL * eL + sL - 1];
+    const long long offR = boundary ? offL : a.soff[6LL * eR + sR - 1];
     const long long gpt = a.foff[f] + p;
     const R n[3] = {a.fn[3 * gpt], a.fn[3 * gpt + 1], a.fn[3 * gpt + 2]};
     const R J = a.fj[gpt];
@@ -737,6 +740,26 @@ __global__ void __launch_bounds__(128) kv_face_direct(VArgs<R> a) {
         QR[v] = a.QF[offR * 5 + v * np + pr];
     }
     R out[NVOUT];
+    if (MODE == kJump && boundary) {  // (U* - U) Jf n (EllipticBR1.f90:686-736)
+        const PhysR<R> ph = a.ph[fd.w];
+        R UL[5], us[5];
+        gradient_variables(ph, QL, UL);
+        bc_gradvars(ph, a.bc[static_cast<unsigned>(fd.z) >> 20], n, QL, UL, us);
+        R* dL = a.UJ + offL * 15 + p;
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+            const R u = (us[v] - UL[v]) * J;
+            dL[v * np] = u * n[0];
+            dL[(5 + v) * np] = u * n[1];
+            dL[(10 + v) * np] = u * n[2];
+        }
+        return;
+    }
+    if (MODE != kJump && boundary) {  // the condition's external state (computeBoundaryFlux)
+#pragma unroll
+        for (int v = 0; v < 5; ++v) QR[v] = QL[v];
+        bc_state(a.ph[fd.w], a.bc[static_cast<unsigned>(fd.z) >> 20], n, QR);
+    }
     if (MODE == kJump) {
         R UL[5], UR[5];
         if (V) {
@@ -781,7 +804,17 @@ __global__ void __launch_bounds__(128) kv_face_direct(VArgs<R> a) {
         lxf_flux<R, false>(ph, QL, QR, n, t1, t2, inv);
     }
     R visc[5] = {0, 0, 0, 0, 0};
-    if (MODE == kFluxNS) {
+    if (MODE == kFluxNS && boundary) {  // the interior viscous flux through the Neumann rule
+        R gl[15];
+#pragma unroll
+        for (int c = 0; c < 15; ++c) gl[c] = a.GF[offL * 15 + c * np + p];
+        R mu, kap, FL[3][5];
+        mu_kappa(ph, QL, mu, kap);
+        viscous_flux(ph, QL, gl, gl + 5, gl + 10, mu, kap, FL);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) visc[v] = FL[0][v] * n[0] + FL[1][v] * n[1] + FL[2][v] * n[2];
+        bc_neumann(a.bc[static_cast<unsigned>(fd.z) >> 20], QL, visc);
+    } else if (MODE == kFluxNS) {
         R gl[15], gr[15];
 #pragma unroll
         for (int c = 0; c < 15; ++c) {
@@ -804,7 +837,7 @@ __global__ void __launch_bounds__(128) kv_face_direct(VArgs<R> a) {
     for (int v = 0; v < 5; ++v) {
         const R fl = (inv[v] - visc[v]) * J;
         dL[v * np] = fl;
-        dR[v * np] = -fl;
+        if (!boundary) dR[v * np] = -fl;
     }
 }
 

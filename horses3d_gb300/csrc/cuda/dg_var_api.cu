@@ -53,12 +53,24 @@ int validate_case(const dg_mesh_desc* m, const dg_physics* ph, int c) {
         for (int d = 0; d < 3; ++d)
             if (m->order[3 * e + d] < 1 || m->order[3 * e + d] + 1 > dg::kMaxP)
                 return h3d::fail(DG_ERR_UNSUPPORTED, tag + "polynomial order outside 1..7");
-    if (2 * static_cast<int64_t>(m->n_faces) != 6 * static_cast<int64_t>(m->n_elements))
-        return h3d::fail(DG_ERR_UNSUPPORTED, tag + "boundary faces are not supported (periodic/interior meshes only)");
+    int64_t sides = 0;
     for (int f = 0; f < m->n_faces; ++f) {
         if (m->face_rotation[f] < 0 || m->face_rotation[f] > 7)
             return h3d::fail(DG_ERR_INVALID, tag + "face rotation outside 0..7");
         int dims[2][2];
+        if (m->face_elem[2 * f + 1] < 0) {  // boundary face: one side, face orders its own
+            int rc = h3dctx::validate_boundary_face(m, f);
+            if (rc) return rc;
+            const int e = m->face_elem[2 * f], side = m->face_side[2 * f];
+            if (e < 0 || e >= m->n_elements || side < 1 || side > 6)
+                return h3d::fail(DG_ERR_INVALID, tag + "face connectivity out of range");
+            side_orders(side, m->order + 3 * e, dims[0][0], dims[0][1]);
+            if (m->face_nf[2 * f] != dims[0][0] || m->face_nf[2 * f + 1] != dims[0][1])
+                return h3d::fail(DG_ERR_INVALID, tag + "a boundary face's orders are not its element side's");
+            ++sides;
+            continue;
+        }
+        sides += 2;
         for (int s = 0; s < 2; ++s) {
             const int e = m->face_elem[2 * f + s], side = m->face_side[2 * f + s];
             if (e < 0 || e >= m->n_elements || side < 1 || side > 6)
@@ -71,6 +83,8 @@ int validate_case(const dg_mesh_desc* m, const dg_physics* ph, int c) {
             if (m->face_nf[2 * f + a] != std::max(dims[0][a], dims[1][a]))
                 return h3d::fail(DG_ERR_INVALID, tag + "face order is not the larger of its two sides' orders");
     }
+    if (sides != 6 * static_cast<int64_t>(m->n_elements))
+        return h3d::fail(DG_ERR_INVALID, tag + "the faces do not cover every element side once");
     if (ph->mach <= 0.0) return h3d::fail(DG_ERR_INVALID, tag + "Mach number must be positive");
     if (ph->navier_stokes && ph->reynolds <= 0.0) return h3d::fail(DG_ERR_INVALID, tag + "Reynolds number must be positive");
     return DG_OK;
@@ -157,6 +171,11 @@ int setup_vstore(dg_ctx* c, h3dctx::VStore<R>& st, const Gathered& h) {
     std::vector<dg::PhysR<R>> ph(c->n_cases);
     for (int k = 0; k < c->n_cases; ++k) ph[k] = dg::make_phys<R>(c->case_pc[k]);
     CK(st.ph.upload(ph.data(), ph.size(), s));
+    {  // boundary conditions of all cases in this precision
+        std::vector<dg::BoundaryR<R>> b(c->bcs.size());
+        for (size_t i = 0; i < c->bcs.size(); ++i) b[i] = dg::make_boundary<R>(c->bcs[i], c->case_pc[c->bc_case[i]]);
+        CK(st.bcs.upload(b.data(), b.size(), s));
+    }
     const bool ns = c->pc.ns != 0;
     CK(st.QDot.alloc(5 * nd));
     CK(cudaMemsetAsync(st.QDot.p, 0, sizeof(R) * 5 * nd, s));
@@ -201,6 +220,7 @@ int setup_vstore(dg_ctx* c, h3dctx::VStore<R>& st, const Gathered& h) {
     a.foff = c->foff.p;
     a.ops = st.ops.p;
     a.tset = st.tset.p;
+    a.bc = st.bcs.p;
     a.ph = st.ph.p;
     a.cc = c->cc.p;
     a.time = c->scal.p;
@@ -366,6 +386,19 @@ int static_pressure_residual(dg_ctx* c, const Gathered& h) {
         return done(cuda_fail(e, "static pressure items"));
     int rc = setup_vstore(c, st, h);
     if (rc) return done(rc);
+    {  // every boundary as an adiabatic free-slip wall: its external state is the state at rest itself,
+       // so the residual below is that of a constant pressure (the part the mixed fluxes leave out)
+        std::vector<dg::BoundaryR<double>> b(c->bcs.size());
+        for (size_t i = 0; i < c->bcs.size(); ++i) {
+            dg_boundary w{};
+            w.type = DG_BC_FREE_SLIP_WALL;
+            w.wall_temperature = 1.0;
+            b[i] = dg::make_boundary<double>(w, c->case_pc[c->bc_case[i]]);
+        }
+        if (!b.empty() &&
+            (e = cudaMemcpyAsync(st.bcs.p, b.data(), sizeof(b[0]) * b.size(), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+            return done(cuda_fail(e, "static pressure boundaries"));
+    }
     dg::VArgs<double>& a = st.args;
     a.items = items.p;
     a.item_elems = elems.p;
@@ -497,17 +530,26 @@ int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, cons
         append(h.x, m.x, 3 * case_nodes);
         int64_t case_fpts = 0;
         std::vector<int> seen(6 * static_cast<size_t>(m.n_elements), 0);
+        const int bc_base = static_cast<int>(c->bcs.size());
+        if (m.n_boundaries > 0 && m.boundaries)
+            for (int b = 0; b < m.n_boundaries; ++b) {
+                c->bcs.push_back(m.boundaries[b]);
+                c->bc_case.push_back(k);
+            }
+        if (c->bcs.size() >= (1u << 11)) return bail(h3d::fail(DG_ERR_UNSUPPORTED, "more than 2047 boundary conditions"));
         for (int f = 0; f < m.n_faces; ++f) {
             const int q1 = m.face_nf[2 * f] + 1, q2 = m.face_nf[2 * f + 1] + 1;
-            for (int s = 0; s < 2; ++s) {
+            const bool boundary = m.face_elem[2 * f + 1] < 0;
+            for (int s = 0; s < (boundary ? 1 : 2); ++s) {
                 int& mark = seen[6 * static_cast<size_t>(m.face_elem[2 * f + s]) + m.face_side[2 * f + s] - 1];
                 if (mark) return bail(h3d::fail(DG_ERR_INVALID, "an element side belongs to two faces"));
                 mark = 1;
             }
             int4 fd;
             fd.x = kbase + m.face_elem[2 * f];
-            fd.y = kbase + m.face_elem[2 * f + 1];
-            fd.z = m.face_side[2 * f] | (m.face_side[2 * f + 1] << 4) | (m.face_rotation[f] << 8) | (q1 << 12) | (q2 << 16);
+            fd.y = boundary ? -1 : kbase + m.face_elem[2 * f + 1];
+            fd.z = m.face_side[2 * f] | ((boundary ? 0 : m.face_side[2 * f + 1]) << 4) | (m.face_rotation[f] << 8) |
+                   (q1 << 12) | (q2 << 16) | (boundary ? (bc_base + m.face_boundary[f]) << 20 : 0);
             fd.w = k;
             faces.push_back(fd);
             foff.push_back(fpts + case_fpts);
@@ -536,6 +578,10 @@ int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, cons
         for (int f = 0; f < c->F; ++f) {
             const int4& fd = faces[f];
             const int q1 = (fd.z >> 12) & 15, q2 = (fd.z >> 16) & 15;
+            if (fd.y < 0) {  // boundary faces carry their element side's orders
+                groups[{q1, q2}].push_back(f);
+                continue;
+            }
             const int oL = eord[fd.x], oR = eord[fd.y];
             const int32_t ordL[3] = {(oL & 255) - 1, ((oL >> 8) & 255) - 1, ((oL >> 16) & 255) - 1};
             const int32_t ordR[3] = {(oR & 255) - 1, ((oR >> 8) & 255) - 1, ((oR >> 16) & 255) - 1};

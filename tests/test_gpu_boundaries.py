@@ -147,3 +147,55 @@ def test_conserving_cylinder_cases_reach_the_reference_goldens(test, tmp_path):
     res = rep.residuals
     assert cases.ftassert_close(gold[[0, 1, 3, 4]], res[[0, 1, 3, 4]], 1e-11), res - gold
     assert cases.ftassert_close(gold[2], res[2], 1e-10), res - gold
+
+
+def _aniso_channel(y_kind, x_kinds=None, seed=21, lo=1, hi=4, warp=0.0, nodes=_abi.DG_NODES_GAUSS, **bc):
+    orders = cases.random_orders(27, lo, hi, seed)
+    periodic = "bottom:top" + ("" if x_kinds else ",left:right")
+    mesh = HexMesh.box(3, [0, 0, 0], [2 * np.pi] * 3, orders, node_type=nodes, warp=warp,
+                       patch_order=hi if warp else 0, periodic=periodic)
+    cfg = cases.Config(order=hi, nodes=nodes, mach=0.3, reynolds=150.0, riemann=_abi.DG_RIEMANN_LXF)
+    cfg.boundaries = {"front": dict({"type": y_kind}, **bc), "back": dict({"type": y_kind}, **bc)}
+    if x_kinds:
+        cfg.boundaries["left"] = {"type": x_kinds[0]}
+        cfg.boundaries["right"] = {"type": x_kinds[1]}
+    return mesh, cfg
+
+
+@pytest.mark.parametrize("warp", [0.0, 0.1])
+def test_anisotropic_orders_no_slip_walls(warp):
+    """Per-element orders 1..4 between no-slip walls (variable-order kernels; the walls' faces are
+    direct faces at their element side's orders); curved interior with warp."""
+    mesh, cfg = _aniso_channel("noslipwall", warp=warp)
+    _check(mesh, cfg, _state(mesh, cfg.mach, seed=6))
+
+
+def test_anisotropic_orders_inflow_outflow_isothermal_walls():
+    mesh, cfg = _aniso_channel("noslipwall", x_kinds=("inflow", "outflow"), seed=22, lo=2, hi=5,
+                               **{"wall type (adiabatic/isothermal)": "isothermal", "wall temperature": 300.0})
+    cfg = dataclasses.replace(cfg, aoa_theta=0.0, aoa_phi=0.0, gradient_variables=_abi.DG_GRADVARS_ENERGY)
+    _check(mesh, cfg, _state(mesh, cfg.mach, seed=7, u0=(1.0, 0.0, 0.0)))
+
+
+def test_batch_with_walled_and_periodic_cases():
+    """A batch of a walled channel (anisotropic orders) and a periodic TGV box: each case equals the
+    oracle run on it alone."""
+    from horses3d_gb300.batch import CaseBatch
+
+    m1, c1 = _aniso_channel("freeslipwall", seed=23)
+    q1 = _state(m1, c1.mach, seed=8)
+    m2, c2, q2 = cases.tgv_case(n=2, order=3, nodes=_abi.DG_NODES_GAUSS, mach=0.3, reynolds=150.0, perturbation=0.01,
+                                seed=9, riemann=_abi.DG_RIEMANN_LXF)
+    b = CaseBatch([m1, m2], [c1, c2])
+    b.set_state([q1, q2])
+    dt = 1e-3
+    b.set_clock(np.zeros(2), np.full(2, dt))
+    b.run_steps(2)
+    got = b.get()
+    for (m, c, q), g in zip(((m1, c1, q1), (m2, c2, q2)), got):
+        o = oracle.Oracle(m, c.physics(), c.options(), c.boundary_table(m.zone_names) if m.n_boundary_faces else None)
+        o.set_state(q)
+        for s in range(2):
+            o.rk3_step(s * dt, dt)
+        err = rel_l2(g, o.get(0), cases.quadrature_weights(m))
+        assert np.all(err <= STATE_TOL), err
