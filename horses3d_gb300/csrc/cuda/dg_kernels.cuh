@@ -230,6 +230,24 @@ __host__ __device__ constexpr int volume_smem_values(bool split) {
     return VolLayout<P, R>::values(split);
 }
 
+// Work item tt of the 6 P^2 face points of an element -> (side, point). For Gauss nodes the two ends
+// of a line are adjacent items (lanes 2q and 2q+1): their traces read the same shared-memory words in
+// the same instructions, which the hardware serves as one broadcast; Gauss-Lobatto traces read one
+// end node only and keep the side-major order.
+template <int P, bool GL>
+__device__ __forceinline__ void face_point_of(int tt, int& side, int& p) {
+    constexpr int P2 = P * P;
+    if (GL) {
+        side = 1 + tt / P2;
+        p = tt - (side - 1) * P2;
+        return;
+    }
+    const int q = tt >> 1, axis = q / P2;
+    p = q - axis * P2;
+    const bool hi = (tt & 1) != 0;
+    side = axis == 0 ? (hi ? 2 : 1) : axis == 1 ? (hi ? 5 : 3) : (hi ? 4 : 6);
+}
+
 // Trace at face point (ca,cb) of a side of D 5-vectors per entry (entry m, direction d at
 // v4[(m*D+d)*4], v1[d*n+m]): sum_l v(l) s(line node l) in line order (HexElementClass.f90:233-372);
 // the Gauss-Lobatto end weights are unit vectors, so the end node is picked.
@@ -381,8 +399,10 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
                 U[2][v] = (uxi[v] * jxs[2] + ueta[v] * jes[2] + uzeta[v] * jzs[2]) * ij;
             }
             // BR1 jumps at the six sides: 1/2 (U_R - U_L) Jf n in the face's orientation (left -> right)
-            for (int t = n; t < F6; t += P3) {
-                const int side = 1 + t / P2, p = t - (side - 1) * P2;
+            for (int tt = n; tt < F6; tt += P3) {
+                int side, p;
+                face_point_of<P, GL>(tt, side, p);
+                const int t = (side - 1) * P2 + p;
                 const int ca = p % P, cb = p / P;
                 const int64_t s = slot(e, side);
                 R own[1][5], nbr[5];
@@ -470,8 +490,10 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
         __syncthreads();
         if (active) {
             // viscous normal flux of this side at its face points: Fv(Q, grad U, mu(Q)) . n
-            for (int t = n; t < F6; t += P3) {
-                const int side = 1 + t / P2, p = t - (side - 1) * P2;
+            for (int tt = n; tt < F6; tt += P3) {
+                int side, p;
+                face_point_of<P, GL>(tt, side, p);
+                const int t = (side - 1) * P2 + p;
                 const int ca = p % P, cb = p / P;
                 const int64_t s = slot(e, side);
                 R tq[5], tg[3][5];
