@@ -146,6 +146,9 @@ SIGNATURES = [
     ("h3d_read_solution_header", C.c_int, [C.c_char_p, C.POINTER(SolutionHeader)]),
     ("h3d_read_solution", C.c_int, [C.c_char_p, C.c_int32, _i32p, _f64p, _f64p]),
     ("h3d_write_solution", C.c_int, [C.c_char_p, C.POINTER(SolutionHeader), _i32p, _f64p, _f64p]),
+    ("dg_batch_integrate", C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, _f64p, C.POINTER(C.c_int)]),
+    ("dg_integrate", C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                               C.POINTER(C.c_double), _f64p, C.POINTER(C.c_int)]),
     ("dg_save_solution", C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.c_int, C.c_double, C.c_int]),
     ("dg_load_solution", C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     ("h3d_mesh_read_specmesh", C.c_int, [C.c_char_p, C.c_int, C.c_int, _i32p, C.c_char_p, C.POINTER(C.c_void_p)]),

@@ -89,6 +89,18 @@ class CaseBatch:
                    "dg_batch_run_steps")
         return ms.value
 
+    def integrate_on_device(self, n: int, cfl: float = 0.0, dcfl: float = 0.0) -> np.ndarray:
+        """n steps of every case from its clock with the residual monitor (dg_batch_integrate); returns
+        the residual history [n, n_cases, 5]."""
+        hist = np.zeros((max(1, n), self.n_cases, 5))
+        nan_step = C.c_int()
+        rc = _abi.lib().dg_batch_integrate(self._h, int(n), float(cfl), float(dcfl), _abi.f64ptr(hist),
+                                           C.byref(nan_step))
+        if rc == _abi.DG_ERR_NAN:
+            raise FloatingPointError(f"NaN or Inf after step {nan_step.value}")
+        _abi.check(rc, "dg_batch_integrate")
+        return hist[:n]
+
     def compute_max_residuals(self):
         r = np.zeros(5 * self.n_cases)
         nan = np.zeros(self.n_cases, dtype=np.int32)

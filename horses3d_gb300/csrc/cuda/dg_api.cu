@@ -182,17 +182,19 @@ cudaError_t enqueue_max_dt(dg_ctx* c, double cfl, double dcfl) {
     d.Q = c->Q.p;
     d.red = c->red.p;
     const dg::DtConst32 c32 = dg::dt_const32(cfl, dcfl, c->dxi, d.gamma, d.gm1, d.gammaM2, d.S_div_TRef, d.TReNorm, d.ns);
-    const int blocks = 2 * 152 * 4;
+    const int blocks = dg::kDtBlocks;
     if (c->mixed) {
         const Store<float>& st = c->s32;
         dg::k_dt_estimate<float><<<blocks, 256, 0, c->stream>>>(c32, c->ndof, c->Q.p, st.ja_xi.p, st.ja_eta.p,
-                                                                 st.ja_zeta.p, st.jac.p, c->red.p);
-        dg::k_dt_exact<float><<<blocks, 256, 0, c->stream>>>(d, c32, st.ja_xi.p, st.ja_eta.p, st.ja_zeta.p, st.jac.p);
+                                                                 st.ja_zeta.p, st.jac.p, c->red.p, c->dt_bmin.p);
+        dg::k_dt_exact<float><<<blocks, 256, 0, c->stream>>>(d, c32, st.ja_xi.p, st.ja_eta.p, st.ja_zeta.p, st.jac.p,
+                                                             c->dt_bmin.p);
     } else {
         const Store<double>& st = c->s64;
         dg::k_dt_estimate<double><<<blocks, 256, 0, c->stream>>>(c32, c->ndof, c->Q.p, st.ja_xi.p, st.ja_eta.p,
-                                                                  st.ja_zeta.p, st.jac.p, c->red.p);
-        dg::k_dt_exact<double><<<blocks, 256, 0, c->stream>>>(d, c32, st.ja_xi.p, st.ja_eta.p, st.ja_zeta.p, st.jac.p);
+                                                                  st.ja_zeta.p, st.jac.p, c->red.p, c->dt_bmin.p);
+        dg::k_dt_exact<double><<<blocks, 256, 0, c->stream>>>(d, c32, st.ja_xi.p, st.ja_eta.p, st.ja_zeta.p, st.jac.p,
+                                                              c->dt_bmin.p);
     }
     dg::k_dt_final<<<1, 1, 0, c->stream>>>(c->red.p, c->scal.p + 1);
     return cudaGetLastError();
@@ -382,6 +384,7 @@ int dg_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op,
         if ((e = cudaMemcpy(c->red.p, init, sizeof(init), cudaMemcpyHostToDevice)) != cudaSuccess)
             return bail(cuda_fail(e, "init reductions"));
     }
+    if ((e = c->dt_bmin.alloc(2 * dg::kDtBlocks)) != cudaSuccess) return bail(cuda_fail(e, "alloc dt chunks"));
     if ((e = c->face_elem.alloc(2 * c->F)) != cudaSuccess) return bail(cuda_fail(e, "alloc faces"));
     if ((e = c->face_side.alloc(2 * c->F)) != cudaSuccess) return bail(cuda_fail(e, "alloc faces"));
     if ((e = c->face_rot.alloc(c->F)) != cudaSuccess) return bail(cuda_fail(e, "alloc faces"));
@@ -438,12 +441,13 @@ int dg_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op,
 void dg_destroy(dg_ctx* c) {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
-    if (c->graph) cudaGraphExecDestroy(c->graph);
+    h3dctx::drop_graphs(c);
     if (c->var) h3dvar::release(c);
     c->s64.free();
     c->s32.free();
     c->Q.free(); c->G.free(); c->x.free(); c->scal.free(); c->red.free(); c->nan_flag.free(); c->err_flag.free();
     c->face_elem.free(); c->face_side.free(); c->face_rot.free(); c->nb_slot.free(); c->nb_map.free();
+    c->mon.free(); c->mon_count.free(); c->esum.free(); c->dt_bmin.free();
     if (c->h_scal) cudaFreeHost(c->h_scal);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -454,20 +458,19 @@ int64_t dg_ndof(const dg_ctx* c) { return c ? c->ndof : 0; }
 int dg_upload_state(dg_ctx* c, const double* q) {
     if (!c || !q) return h3d::fail(DG_ERR_INVALID, "null argument");
     if (c->var) return h3dvar::upload(c, q);  // per-case constants live in device memory: graphs stay valid
+    CK(cudaMemcpyAsync(c->Q.p, q, sizeof(double) * 5 * c->ndof, cudaMemcpyHostToDevice, c->stream));
     if (c->mixed) {
-        // energy reference of the mixed form: the mean energy of the uploaded state
-        double sum = 0.0;
-        for (int64_t g = 0; g < c->ndof; ++g) sum += q[5 * g + 4];
-        const double e_ref = sum / static_cast<double>(c->ndof);
+        // energy reference of the mixed form: the mean energy of the uploaded state (device sum)
+        double e_ref = 0.0;
+        int rc = h3dctx::device_mean_energy(c, 0, c->ndof, &e_ref);
+        if (rc) return rc;
         if (!std::isfinite(e_ref)) return h3d::fail(DG_ERR_NAN, "NaN or Inf in the uploaded state");
         if (e_ref != c->s32.args.e_ref) {
             c->s32.args.e_ref = e_ref;
             dg::set_reference_energy(c->s32.args.ph, c->pc.gm1, e_ref);
-            if (c->graph) cudaGraphExecDestroy(c->graph);  // kernel arguments changed
-            c->graph = nullptr;
+            h3dctx::drop_graphs(c);  // kernel arguments changed
         }
     }
-    CK(cudaMemcpyAsync(c->Q.p, q, sizeof(double) * 5 * c->ndof, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemsetAsync(c->G.p, 0, sizeof(double) * 5 * c->ndof, c->stream));
     CK(run_stage(c, dg::kTraces, 0.0, 0));  // face traces of the new state
     CK(cudaStreamSynchronize(c->stream));
@@ -580,6 +583,65 @@ int prepare_graph(dg_ctx* c, int mode, double cfl, double dcfl) {
     return DG_OK;
 }
 
+// The step graph of dg_integrate: prepare_graph's step followed by ComputeMaxResiduals / checkForNan
+// into the history row of the step (captured once per mode, cfl, dcfl and history buffer).
+int prepare_monitor_graph(dg_ctx* c, int mode, double cfl, double dcfl) {
+    const bool stale = !c->mgraph || c->mgraph_mode != mode || c->mgraph_key[1] != cfl || c->mgraph_key[2] != dcfl;
+    if (!stale) return DG_OK;
+    if (c->mgraph) cudaGraphExecDestroy(c->mgraph);
+    c->mgraph = nullptr;
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    if (mode == 1) e = enqueue_max_dt(c, cfl, dcfl);
+    if (e == cudaSuccess) e = enqueue_step(c);
+    if (e == cudaSuccess) {
+        if (c->var) {
+            e = h3dvar::enqueue_advance_time(c);
+        } else {
+            dg::k_advance_time<<<1, 1, 0, c->stream>>>(c->scal.p, c->scal.p + 1);
+            e = cudaGetLastError();
+        }
+    }
+    if (e == cudaSuccess) {
+        if (c->var) {
+            e = h3dvar::enqueue_residuals(c);
+            if (e == cudaSuccess) {
+                dg::k_record_monitor<<<1, 1, 0, c->stream>>>(c->red.p, 8, c->vnan.p, c->n_cases, c->mon.p,
+                                                             c->mon_count.p, c->mon_rows);
+                e = cudaGetLastError();
+            }
+        } else {
+            e = cudaMemsetAsync(c->red.p + 2, 0, 5 * sizeof(unsigned long long), c->stream);
+            if (e == cudaSuccess) e = cudaMemsetAsync(c->nan_flag.p, 0, sizeof(int), c->stream);
+            if (e == cudaSuccess) {
+                if (c->mixed)
+                    dg::k_residuals<float><<<152 * 4, 256, 0, c->stream>>>(c->ndof, c->s32.QDot.p, c->Q.p, c->red.p + 2,
+                                                                           c->nan_flag.p);
+                else
+                    dg::k_residuals<double><<<152 * 4, 256, 0, c->stream>>>(c->ndof, c->s64.QDot.p, c->Q.p,
+                                                                            c->red.p + 2, c->nan_flag.p);
+                dg::k_record_monitor<<<1, 1, 0, c->stream>>>(c->red.p, 0, c->nan_flag.p, 1, c->mon.p, c->mon_count.p,
+                                                             c->mon_rows);
+                e = cudaGetLastError();
+            }
+        }
+    }
+    cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+    if (e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return cuda_fail(e, "capture monitored RK3 step");
+    }
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&c->mgraph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    c->mgraph_mode = mode;
+    c->mgraph_key[1] = cfl;
+    c->mgraph_key[2] = dcfl;
+    return DG_OK;
+}
+
 // n graph launches of one RK3 step (mode 0: the dt on the device; mode 1: MaxTimeStep first).
 int run_graph(dg_ctx* c, int n, int mode, double cfl, double dcfl, double* ms) {
     int rc = prepare_graph(c, mode, cfl, dcfl);
@@ -626,6 +688,65 @@ extern "C" {
 
 int dg_run_steps(dg_ctx* c, int n, double t0, double dt, double cfl, double dcfl, double* t_end) {
     return steps_common(c, n, t0, dt, cfl, dcfl, t_end, nullptr);
+}
+
+}  // extern "C"
+
+namespace {
+
+// dg_integrate / dg_batch_integrate from the current device clock (mode 0: each case's dt, mode 1:
+// MaxTimeStep each step). t_end receives case 0's final time.
+int integrate_core(dg_ctx* c, int n, int mode, double cfl, double dcfl, double* t_end, double* residuals,
+                   int* nan_step) {
+    if (nan_step) *nan_step = 0;
+    if (n == 0) return DG_OK;
+    const int nc = c->n_cases;
+    if (n > c->mon_rows) {  // grow the history; the captured graph points at the old buffer
+        c->mon.free();
+        c->mon_rows = 0;
+        CK(c->mon.alloc(static_cast<size_t>(n) * 6 * nc));
+        if (!c->mon_count.p) CK(c->mon_count.alloc(1));
+        c->mon_rows = n;
+        if (c->mgraph) cudaGraphExecDestroy(c->mgraph);
+        c->mgraph = nullptr;
+    }
+    int rc = prepare_monitor_graph(c, mode, cfl, dcfl);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(c->mon_count.p, 0, sizeof(int), c->stream));
+    for (int s = 0; s < n; ++s) CK(cudaGraphLaunch(c->mgraph, c->stream));
+    std::vector<double> rows(static_cast<size_t>(n) * 6 * nc);
+    CK(cudaMemcpyAsync(rows.data(), c->mon.p, sizeof(double) * rows.size(), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(c->h_scal, c->scal.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (t_end) *t_end = c->h_scal[0];
+    rc = check_device_error(c);
+    if (rc) return rc;
+    int first = 0;
+    for (int s = 0; s < n && !first; ++s)
+        for (int k = 0; k < nc; ++k)
+            if (rows[(static_cast<size_t>(s) * nc + k) * 6 + 5] != 0.0) first = s + 1;
+    if (residuals)
+        for (int s = 0; s < n; ++s)
+            for (int k = 0; k < nc; ++k)
+                for (int v = 0; v < 5; ++v)
+                    residuals[(static_cast<size_t>(s) * nc + k) * 5 + v] = rows[(static_cast<size_t>(s) * nc + k) * 6 + v];
+    if (nan_step) *nan_step = first;
+    return first ? h3d::fail(DG_ERR_NAN, "NaN or Inf in Q after step " + std::to_string(first)) : DG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dg_integrate(dg_ctx* c, int n, double t0, double dt, double cfl, double dcfl, double* t_end,
+                 double* residuals, int* nan_step) {
+    if (!c || n < 0) return h3d::fail(DG_ERR_INVALID, "bad arguments");
+    const int mode = dt > 0.0 ? 0 : 1;
+    if (mode == 1 && !(cfl > 0.0)) return h3d::fail(DG_ERR_INVALID, "CFL stepping needs cfl > 0");
+    if (n == 0 && t_end) *t_end = t0;
+    int rc = set_scalars(c, t0, mode == 0 ? dt : 0.0);
+    if (rc) return rc;
+    return integrate_core(c, n, mode, cfl, dcfl, t_end, residuals, nan_step);
 }
 
 int dg_time_steps(dg_ctx* c, int n, double t0, double dt, double cfl, double dcfl, double* ms) {
@@ -760,10 +881,7 @@ int dg_inject_fault(dg_ctx* c, int kind) {
     const uint32_t extra = kind == DG_FAULT_TMA_WAIT ? 16u : 0u;
     c->s32.args.extra_tx = extra;
     c->s64.args.extra_tx = extra;
-    if (c->graph) {  // the captured launches carry the old arguments
-        cudaGraphExecDestroy(c->graph);
-        c->graph = nullptr;
-    }
+    h3dctx::drop_graphs(c);  // the captured launches carry the old arguments
     return DG_OK;
 }
 
@@ -776,6 +894,11 @@ int dg_autotune(dg_ctx* c, int reps) {
 int dg_batch_run_steps(dg_ctx* c, int n, double cfl, double dcfl, double* ms) {
     if (!c || n < 0) return h3d::fail(DG_ERR_INVALID, "bad arguments");
     return run_graph(c, n, cfl > 0.0 ? 1 : 0, cfl, dcfl, ms);
+}
+
+int dg_batch_integrate(dg_ctx* c, int n, double cfl, double dcfl, double* residuals, int* nan_step) {
+    if (!c || n < 0) return h3d::fail(DG_ERR_INVALID, "bad arguments");
+    return integrate_core(c, n, cfl > 0.0 ? 1 : 0, cfl, dcfl, nullptr, residuals, nan_step);
 }
 
 }  // extern "C"

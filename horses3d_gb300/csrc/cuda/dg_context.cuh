@@ -103,12 +103,22 @@ struct dg_ctx {
     h3dctx::DevBuf<unsigned long long> red;  // uniform: [0..1] dt, [2..6] residuals; variable: 8 per case
     h3dctx::DevBuf<int> face_elem, face_side, face_rot, nan_flag, nb_slot, nb_map;
     h3dctx::DevBuf<int> err_flag;  // set by kernels whose bounded waits gave up
+    h3dctx::DevBuf<double> esum;   // energy sums of the mixed form's reference (partials, then per case)
+    h3dctx::DevBuf<float> dt_bmin;  // per-chunk minima of the MaxTimeStep estimate pass
     h3dctx::Store<double> s64;
     h3dctx::Store<float> s32;
     double* h_scal = nullptr;  // pinned staging for the per-case scalars (4 * n_cases doubles)
     cudaGraphExec_t graph = nullptr;
     double graph_key[3] = {0, 0, 0};  // (mode, cfl, dcfl) the graph was captured for
     int graph_mode = -1;
+    // IntegrateInTime on the device (dg_integrate): the step graph with residual monitoring, and the
+    // per-step history rows (per case: 5 residuals and a NaN flag) with their device row counter
+    cudaGraphExec_t mgraph = nullptr;
+    double mgraph_key[3] = {0, 0, 0};
+    int mgraph_mode = -1;
+    h3dctx::DevBuf<double> mon;
+    h3dctx::DevBuf<int> mon_count;
+    int mon_rows = 0;
 
     // variable-order / multi-case path
     bool var = false;
@@ -140,10 +150,33 @@ struct dg_ctx {
     unsigned char gq2[dg::kMaxP * dg::kMaxP] = {};
 };
 
-// Variable-order / multi-case path (dg_var_api.cu).
 namespace h3dctx {
-int validate_boundary_face(const dg_mesh_desc* m, int f);  // dg_api.cu
+// Mean of Q[5g+4] over [g0, g1) of the device state, summed in a fixed order (same bits for the same
+// state), into *mean on the host.
+inline int device_mean_energy(dg_ctx* c, int64_t g0, int64_t g1, double* mean) {
+    if (!c->esum.p) CK(c->esum.alloc(dg::kSumBlocks + 1));
+    dg::k_energy_partial<<<dg::kSumBlocks, 256, 0, c->stream>>>(g0, g1, c->Q.p, c->esum.p);
+    dg::k_energy_final<<<1, 256, 0, c->stream>>>(c->esum.p, c->esum.p + dg::kSumBlocks);
+    CK(cudaGetLastError());
+    double sum = 0.0;
+    CK(cudaMemcpyAsync(&sum, c->esum.p + dg::kSumBlocks, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    *mean = sum / static_cast<double>(g1 - g0);
+    return DG_OK;
 }
+
+// Drops the captured step graphs (their kernel arguments or buffers changed).
+inline void drop_graphs(dg_ctx* c) {
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+    if (c->mgraph) cudaGraphExecDestroy(c->mgraph);
+    c->mgraph = nullptr;
+}
+
+int validate_boundary_face(const dg_mesh_desc* m, int f);  // dg_api.cu
+}  // namespace h3dctx
+
+// Variable-order / multi-case path (dg_var_api.cu).
 
 namespace h3dvar {
 bool needs_variable_path(const dg_mesh_desc* m);
@@ -154,6 +187,7 @@ cudaError_t stage(dg_ctx* c, int stage, double tshift, int flags);
 cudaError_t enqueue_max_dt(dg_ctx* c, double cfl, double dcfl);
 cudaError_t enqueue_advance_time(dg_ctx* c);
 int residuals(dg_ctx* c, double* maxres, int* nan_case);  // maxres [5*n_cases], nan_case [n_cases]
+cudaError_t enqueue_residuals(dg_ctx* c);                  // into red[8k+2..6] and vnan[k], no sync
 int kernel_times(dg_ctx* c, int reps, double* ms);
 int autotune(dg_ctx* c, int reps);
 }  // namespace h3dvar

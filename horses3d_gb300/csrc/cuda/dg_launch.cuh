@@ -113,6 +113,18 @@ KernelTimesFn<float> times_fn_fp32(int P, bool gl);
 // implement min/max reductions exactly.
 __device__ __forceinline__ unsigned long long dbits(double x) { return static_cast<unsigned long long>(__double_as_longlong(x)); }
 
+// |x| as its bit pattern (float: 31 bits, double: 63 bits); the maximum of such patterns is the
+// pattern of the maximum |x|.
+__device__ __forceinline__ unsigned long long abs_bits(float x) { return __float_as_uint(x) & 0x7fffffffu; }
+__device__ __forceinline__ unsigned long long abs_bits(double x) { return dbits(x) & 0x7fffffffffffffffull; }
+// The double image (for the FP64 reduction slots) of a maximum pattern of the element type.
+__device__ __forceinline__ unsigned long long abs_bits_as_double(unsigned long long m, const float*) {
+    return dbits(static_cast<double>(__uint_as_float(static_cast<unsigned>(m))));
+}
+__device__ __forceinline__ unsigned long long abs_bits_as_double(unsigned long long m, const double*) { return m; }
+// NaN or Inf: all exponent bits set.
+__device__ __forceinline__ int nonfinite(double x) { return (dbits(x) & 0x7ff0000000000000ull) == 0x7ff0000000000000ull; }
+
 struct DtArgs {
     long long ndof;
     double cfl, dcfl, dxi[3], dxi2[3];
@@ -239,12 +251,22 @@ __device__ __forceinline__ void block_min2(T a, T b, T* slot_a_out, T* slot_b_ou
     }
 }
 
+// Each block takes one contiguous chunk of nodes in both passes, and the estimate pass records the
+// chunk's minima (bmin[2b], bmin[2b+1]), so that the exact pass skips every chunk without a node in
+// the window of the global minimum.
+__device__ __forceinline__ void dt_chunk(long long ndof, long long& g0, long long& g1) {
+    const long long chunk = (ndof + gridDim.x - 1) / gridDim.x;
+    g0 = blockIdx.x * chunk;
+    g1 = g0 + chunk < ndof ? g0 + chunk : ndof;
+}
+
 template <typename R>
 __global__ void k_dt_estimate(DtConst32 c, long long ndof, const double* Q, const R* ja_xi, const R* ja_eta,
-                              const R* ja_zeta, const R* jac, unsigned long long* red) {
+                              const R* ja_zeta, const R* jac, unsigned long long* red, float* bmin) {
     float conv = 3.0e38f, visc = 3.0e38f;
-    for (long long g = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; g < ndof;
-         g += static_cast<long long>(gridDim.x) * blockDim.x) {
+    long long g0, g1;
+    dt_chunk(ndof, g0, g1);
+    for (long long g = g0 + threadIdx.x; g < g1; g += blockDim.x) {
         float cv, vs;
         dt_estimate(c, Q + 5 * g, ja_xi + 3 * g, ja_eta + 3 * g, ja_zeta + 3 * g, jac[g], cv, vs);
         conv = fminf(conv, cv);
@@ -256,17 +278,23 @@ __global__ void k_dt_estimate(DtConst32 c, long long ndof, const double* Q, cons
         unsigned int* s32 = reinterpret_cast<unsigned int*>(red + 7);
         atomicMin(&s32[0], fbits(bc));
         atomicMin(&s32[1], fbits(bv));
+        bmin[2 * blockIdx.x] = bc;
+        bmin[2 * blockIdx.x + 1] = bv;
     }
 }
 
 template <typename R>
-__global__ void k_dt_exact(DtArgs d, DtConst32 c, const R* ja_xi, const R* ja_eta, const R* ja_zeta, const R* jac) {
+__global__ void k_dt_exact(DtArgs d, DtConst32 c, const R* ja_xi, const R* ja_eta, const R* ja_zeta, const R* jac,
+                           const float* bmin) {
     const unsigned int* s32 = reinterpret_cast<const unsigned int*>(d.red + 7);
     const float thr_c = __uint_as_float(s32[0]) * (1.0f + kDtWindow);
     const float thr_v = __uint_as_float(s32[1]) * (1.0f + kDtWindow);
+    // no node of this chunk is a candidate: nothing to add (a block-uniform exit, before any barrier)
+    if (bmin[2 * blockIdx.x] > thr_c && !(d.ns && !(bmin[2 * blockIdx.x + 1] > thr_v))) return;
     double conv = 1.0e300, visc = 1.0e300;
-    for (long long g = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; g < d.ndof;
-         g += static_cast<long long>(gridDim.x) * blockDim.x) {
+    long long g0, g1;
+    dt_chunk(d.ndof, g0, g1);
+    for (long long g = g0 + threadIdx.x; g < g1; g += blockDim.x) {
         const double* Q = d.Q + 5 * g;
         float cv, vs;
         dt_estimate(c, Q, ja_xi + 3 * g, ja_eta + 3 * g, ja_zeta + 3 * g, jac[g], cv, vs);
@@ -301,25 +329,75 @@ static __global__ void k_advance_time(double* t, const double* dt) { *t = *t + *
 // ComputeMaxResiduals (DGSEMClass.f90:770-868) and the NaN test of checkForNan.
 template <typename R>
 __global__ void k_residuals(long long ndof, const R* qdot, const double* Q, unsigned long long* red, int* nan_flag) {
-    double m[5] = {0, 0, 0, 0, 0};
+    // max |QDot| and the NaN/Inf test on bit patterns (non-negative IEEE numbers order as their bits),
+    // so that the pass runs on the integer pipe instead of the slow FP64 one
+    unsigned long long m[5] = {0, 0, 0, 0, 0};
     int bad = 0;
     for (long long g = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; g < ndof;
          g += static_cast<long long>(gridDim.x) * blockDim.x) {
 #pragma unroll
         for (int v = 0; v < 5; ++v) {
-            m[v] = fmax(m[v], fabs(double(qdot[5 * g + v])));
-            const double q = Q[5 * g + v];
-            if (!(q == q) || fabs(q) > 1.7976931348623157e308) bad = 1;
+            const unsigned long long a = abs_bits(qdot[5 * g + v]);
+            m[v] = a > m[v] ? a : m[v];
+            bad |= nonfinite(Q[5 * g + v]);
         }
     }
 #pragma unroll
     for (int v = 0; v < 5; ++v)
-        for (int o = 16; o > 0; o >>= 1) m[v] = fmax(m[v], __shfl_down_sync(0xffffffffu, m[v], o));
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long x = __shfl_down_sync(0xffffffffu, m[v], o);
+            m[v] = x > m[v] ? x : m[v];
+        }
     if ((threadIdx.x & 31) == 0) {
 #pragma unroll
-        for (int v = 0; v < 5; ++v) atomicMax(&red[v], dbits(m[v]));
+        for (int v = 0; v < 5; ++v) atomicMax(&red[v], abs_bits_as_double(m[v], qdot));
     }
     if (bad) atomicOr(nan_flag, 1);
+}
+
+// Deterministic FP64 sum of Q[5g+4] over g in [g0, g1): a fixed grid (kSumBlocks blocks, grid-stride,
+// fixed-order tree per block) writes per-block partial sums, one block adds them in order. The mixed
+// form's energy reference is this sum over the node count.
+constexpr int kSumBlocks = 512;
+constexpr int kDtBlocks = 2 * 152 * 4;  // MaxTimeStep passes: one contiguous chunk of nodes per block
+__global__ static void __launch_bounds__(256) k_energy_partial(long long g0, long long g1, const double* Q,
+                                                               double* partial) {
+    __shared__ double sh[256];
+    double acc = 0.0;
+    for (long long g = g0 + blockIdx.x * 256LL + threadIdx.x; g < g1; g += kSumBlocks * 256LL) acc += Q[5 * g + 4];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+__global__ static void __launch_bounds__(256) k_energy_final(const double* partial, double* out) {
+    __shared__ double sh[256];
+    double acc = 0.0;
+    for (int b = threadIdx.x; b < kSumBlocks; b += 256) acc += partial[b];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sh[0];
+}
+
+// One history row per step (dg_integrate): per case the five residuals (bit images in red at
+// red_stride * k + 2) and the NaN flag, at row *count, then ++*count. One thread.
+__global__ static void k_record_monitor(const unsigned long long* red, int red_stride, const int* nan_flag,
+                                        int n_cases, double* rows, int* count, int capacity) {
+    const int r = *count;
+    if (r >= capacity) return;
+    double* row = rows + static_cast<long long>(r) * 6 * n_cases;
+    for (int k = 0; k < n_cases; ++k) {
+        for (int v = 0; v < 5; ++v) row[6 * k + v] = __longlong_as_double(static_cast<long long>(red[red_stride * k + 2 + v]));
+        row[6 * k + 5] = nan_flag[k] ? 1.0 : 0.0;
+    }
+    *count = r + 1;
 }
 
 }  // namespace dg

@@ -1024,24 +1024,27 @@ __global__ void __launch_bounds__(256) kv_residuals(const int4* items, const int
                                                     const R* qdot, const double* Q, unsigned long long* red,
                                                     int* nan_flag) {
     const ItemDims it = item_dims(items[blockIdx.x]);
-    double m[5] = {0, 0, 0, 0, 0};
+    unsigned long long m[5] = {0, 0, 0, 0, 0};  // bit patterns, as k_residuals
     int bad = 0;
     for (int t = threadIdx.x; t < it.ntot; t += blockDim.x) {
         const int le = t / it.np, n = t - le * it.np;
         const long long g = eoff[item_elems[it.first + le]] + n;
 #pragma unroll
         for (int v = 0; v < 5; ++v) {
-            m[v] = fmax(m[v], fabs(double(qdot[5 * g + v])));
-            const double q = Q[5 * g + v];
-            if (!(q == q) || fabs(q) > 1.7976931348623157e308) bad = 1;
+            const unsigned long long a = abs_bits(qdot[5 * g + v]);
+            m[v] = a > m[v] ? a : m[v];
+            bad |= nonfinite(Q[5 * g + v]);
         }
     }
 #pragma unroll
     for (int v = 0; v < 5; ++v)
-        for (int o = 16; o > 0; o >>= 1) m[v] = fmax(m[v], __shfl_down_sync(0xffffffffu, m[v], o));
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long x = __shfl_down_sync(0xffffffffu, m[v], o);
+            m[v] = x > m[v] ? x : m[v];
+        }
     if ((threadIdx.x & 31) == 0) {
 #pragma unroll
-        for (int v = 0; v < 5; ++v) atomicMax(&red[8 * it.kase + 2 + v], dbits(m[v]));
+        for (int v = 0; v < 5; ++v) atomicMax(&red[8 * it.kase + 2 + v], abs_bits_as_double(m[v], qdot));
     }
     if (bad) atomicOr(&nan_flag[it.kase], 1);
 }

@@ -693,18 +693,20 @@ void release(dg_ctx* c) {
     for (auto* b : {&c->eoff, &c->soff, &c->foff}) b->free();
     c->cc.free();
     c->pstat.free();
+    c->esum.free();
     c->dxi_table.free();
     c->gamma_M2.free();
 }
 
 int upload(dg_ctx* c, const double* q) {
     bool changed = false;
+    CK(cudaMemcpyAsync(c->Q.p, q, sizeof(double) * 5 * c->ndof, cudaMemcpyHostToDevice, c->stream));
     if (c->mixed) {  // energy reference of every case: the mean energy of its uploaded state
         for (int k = 0; k < c->n_cases; ++k) {
             const int64_t g0 = c->case_ndof_off[k], g1 = c->case_ndof_off[k + 1];
-            double sum = 0.0;
-            for (int64_t g = g0; g < g1; ++g) sum += q[5 * g + 4];
-            const double e_ref = sum / static_cast<double>(g1 - g0);
+            double e_ref = 0.0;
+            int rc = h3dctx::device_mean_energy(c, g0, g1, &e_ref);
+            if (rc) return rc;
             if (!std::isfinite(e_ref)) return h3d::fail(DG_ERR_NAN, "NaN or Inf in the uploaded state");
             if (e_ref != c->case_const[k].e_ref) {
                 c->case_const[k].e_ref = e_ref;
@@ -723,7 +725,6 @@ int upload(dg_ctx* c, const double* q) {
             CK(cudaStreamSynchronize(c->stream));
         }
     }
-    CK(cudaMemcpyAsync(c->Q.p, q, sizeof(double) * 5 * c->ndof, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemsetAsync(c->G.p, 0, sizeof(double) * 5 * c->ndof, c->stream));
     CK(stage(c, dg::kTraces, 0.0, 0));
     CK(cudaStreamSynchronize(c->stream));
@@ -768,17 +769,23 @@ cudaError_t enqueue_advance_time(dg_ctx* c) {
     return cudaGetLastError();
 }
 
-int residuals(dg_ctx* c, double* maxres, int* nan_case) {
+cudaError_t enqueue_residuals(dg_ctx* c) {
+    cudaError_t e;
     for (int k = 0; k < c->n_cases; ++k)
-        CK(cudaMemsetAsync(c->red.p + 8 * k + 2, 0, 5 * sizeof(unsigned long long), c->stream));
-    CK(cudaMemsetAsync(c->vnan.p, 0, sizeof(int) * c->n_cases, c->stream));
+        if ((e = cudaMemsetAsync(c->red.p + 8 * k + 2, 0, 5 * sizeof(unsigned long long), c->stream)) != cudaSuccess)
+            return e;
+    if ((e = cudaMemsetAsync(c->vnan.p, 0, sizeof(int) * c->n_cases, c->stream)) != cudaSuccess) return e;
     if (c->mixed)
         dg::kv_residuals<float><<<c->n_items, 256, 0, c->stream>>>(c->items.p, c->item_elems.p, c->eoff.p,
                                                                     c->v32.QDot.p, c->Q.p, c->red.p, c->vnan.p);
     else
         dg::kv_residuals<double><<<c->n_items, 256, 0, c->stream>>>(c->items.p, c->item_elems.p, c->eoff.p,
                                                                      c->v64.QDot.p, c->Q.p, c->red.p, c->vnan.p);
-    CK(cudaGetLastError());
+    return cudaGetLastError();
+}
+
+int residuals(dg_ctx* c, double* maxres, int* nan_case) {
+    CK(enqueue_residuals(c));
     std::vector<unsigned long long> bits(8 * static_cast<size_t>(c->n_cases));
     std::vector<int> flags(c->n_cases);
     CK(cudaMemcpyAsync(bits.data(), c->red.p, sizeof(unsigned long long) * bits.size(), cudaMemcpyDeviceToHost, c->stream));
@@ -820,10 +827,7 @@ int apply_items(dg_ctx* c, h3dctx::VStore<R>& st, const ItemTable& t) {
     for (int q = 0; q <= dg::kItemClasses; ++q) a.cls[q] = t.cls[q];
     for (int q = 0; q < dg::kItemClasses; ++q) a.ccap[q] = t.ccap[q];
     CK(st.stage(a, dg::kPrepare, 0.0, 0, c->stream));
-    if (c->graph) {
-        cudaGraphExecDestroy(c->graph);
-        c->graph = nullptr;
-    }
+    h3dctx::drop_graphs(c);
     return DG_OK;
 }
 

@@ -106,6 +106,21 @@ class NavierStokesDG:
                                            C.byref(t_end)), "dg_run_steps")
         return t_end.value
 
+    def integrate_on_device(self, n_steps: int, t0: float = 0.0, dt: float = 0.0, cfl: float = 0.0,
+                            dcfl: float = 0.0):
+        """IntegrateInTime's explicit loop in one call (dg_integrate): n steps of MaxTimeStep (when
+        dt is 0) + TakeRK3Step + ComputeMaxResiduals from one CUDA graph. Returns (t_end, residual
+        history [n_steps, 5]); raises FloatingPointError naming the first step with a NaN/Inf."""
+        t_end = C.c_double()
+        hist = np.zeros((max(1, n_steps), 5))
+        nan_step = C.c_int()
+        rc = _abi.lib().dg_integrate(self._h, int(n_steps), float(t0), float(dt), float(cfl), float(dcfl),
+                                     C.byref(t_end), _abi.f64ptr(hist), C.byref(nan_step))
+        if rc == _abi.DG_ERR_NAN:
+            raise FloatingPointError(f"NaN or Inf in the solution after step {nan_step.value} (checkForNan)")
+        _abi.check(rc, "dg_integrate")
+        return t_end.value, hist[:n_steps]
+
     def synchronize(self):
         _abi.check(_abi.lib().dg_synchronize(self._h), "dg_synchronize")
 

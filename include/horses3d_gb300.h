@@ -166,6 +166,15 @@ int dg_rk3_step(dg_ctx* ctx, double t, double dt);
  * time (this synchronises). */
 int dg_run_steps(dg_ctx* ctx, int n, double t0, double dt, double cfl, double dcfl, double* t_end);
 
+/* IntegrateInTime's explicit loop on the device (TimeIntegrator.f90:737-890 without output): n steps
+ * from t0, each MaxTimeStep (when dt <= 0, with cfl/dcfl) + TakeRK3Step + t += dt +
+ * ComputeMaxResiduals / checkForNan, replayed from one CUDA graph with a single host synchronization at
+ * the end. residuals (optional) receives [n][n_cases][5] maximum |QDot| after each step; *nan_step the
+ * first step (1-based) whose state held a NaN/Inf, then DG_ERR_NAN is returned (the steps after it
+ * ran on the non-finite state; the reference would have stopped there). */
+int dg_integrate(dg_ctx* ctx, int n, double t0, double dt, double cfl, double dcfl, double* t_end,
+                 double* residuals, int* nan_step);
+
 /* dg_run_steps timed with CUDA events recorded on the context's stream around the graph
  * launches; *ms receives the elapsed device time. Measurement helper, no reference counterpart. */
 int dg_time_steps(dg_ctx* ctx, int n, double t0, double dt, double cfl, double dcfl, double* ms);
@@ -238,6 +247,9 @@ int dg_inject_fault(dg_ctx* ctx, int kind);
  * each case's MaxTimeStep(cfl, dcfl); otherwise each case's current dt. ms (may be NULL) receives
  * the device time measured with events on the context's stream. */
 int dg_batch_run_steps(dg_ctx* ctx, int n, double cfl, double dcfl, double* ms);
+/* dg_integrate for a batch from each case's own clock (dg_batch_set_clock): MaxTimeStep per case
+ * each step when cfl > 0, else each case's dt; residuals [n][n_cases][5]. */
+int dg_batch_integrate(dg_ctx* ctx, int n, double cfl, double dcfl, double* residuals, int* nan_step);
 
 /* HORSES3D solution files (.hsol; io/SolutionFile.f90, HexMesh_SaveSolution/LoadSolution in
  * HexMesh.f90:3376-3555,4708-). Host functions, no device needed. The gradient array of a type-3

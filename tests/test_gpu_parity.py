@@ -345,3 +345,40 @@ def test_gradient_variables(gv, nodes):
     _check_steps(mesh, cfg, q0, steps=2, dt=2e-3)
     mixed = dataclasses.replace(cfg, precision=_abi.DG_PRECISION_MIXED)
     _check_steps(mesh, mixed, q0, steps=2, dt=2e-3, tol=MIXED_TOL)
+
+
+@pytest.mark.parametrize("precision", [_abi.DG_PRECISION_FP64, _abi.DG_PRECISION_MIXED])
+def test_integrate_on_device_equals_the_step_loop(precision):
+    """dg_integrate (IntegrateInTime on the device, one graph per step with the residual monitor)
+    gives the state, time and per-step residuals of the host loop MaxTimeStep + TakeRK3Step +
+    ComputeMaxResiduals bit for bit."""
+    mesh, cfg, q0 = cases.tgv_case(n=3, order=3, nodes=_abi.DG_NODES_GAUSS, perturbation=0.02, seed=12,
+                                   precision=precision)
+    g1 = NavierStokesDG(mesh, cfg)
+    g1.set_state(q0)
+    t, hist = 0.0, []
+    for _ in range(4):
+        dt = g1.max_time_step(0.4, 0.4)
+        g1.take_rk3_step(t, dt)
+        t += dt
+        hist.append(g1.compute_max_residuals()[0])
+    g2 = NavierStokesDG(mesh, cfg)
+    g2.set_state(q0)
+    t2, hist2 = g2.integrate_on_device(4, 0.0, cfl=0.4, dcfl=0.4)
+    assert t2 == t
+    assert np.array_equal(g1.Q, g2.Q)
+    assert np.array_equal(np.array(hist), hist2)
+    # the same again (the graph is reused) from a fresh upload
+    g2.set_state(q0)
+    t3, hist3 = g2.integrate_on_device(4, 0.0, cfl=0.4, dcfl=0.4)
+    assert t3 == t and np.array_equal(hist3, hist2)
+
+
+def test_integrate_on_device_reports_the_first_nan_step():
+    mesh, cfg, q0 = cases.tgv_case(n=2, order=2, nodes=_abi.DG_NODES_GAUSS)
+    g = NavierStokesDG(mesh, cfg)
+    q = q0.copy()
+    q[7] = np.nan
+    g.set_state(q)
+    with pytest.raises(FloatingPointError, match="after step 1"):
+        g.integrate_on_device(3, 0.0, dt=1e-3)

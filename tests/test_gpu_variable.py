@@ -298,3 +298,24 @@ def test_anisotropic_gradient_variables(gv):
     _check_steps(mesh, cfg, q0, steps=2, dt=2e-3)
     mixed = dataclasses.replace(cfg, precision=_abi.DG_PRECISION_MIXED)
     _check_steps(mesh, mixed, q0, steps=2, dt=2e-3, tol=MIXED_TOL)
+
+
+def test_batch_integrate_on_device():
+    """dg_batch_integrate: per-case clocks and residual history, state equal to run_steps."""
+    cs = _batch_cases()
+    b = CaseBatch([m for m, _, _ in cs], [c for _, c, _ in cs])
+    b.set_state([q for _, _, q in cs])
+    dts = b.max_time_steps(0.4, 0.4)
+    b.set_clock(np.zeros(3), dts)
+    b.run_steps(3)
+    ref = b.get()
+    b.set_state([q for _, _, q in cs])
+    b.set_clock(np.zeros(3), dts)
+    hist = b.integrate_on_device(3)
+    t, _ = b.clock()
+    assert np.allclose(t, 3 * dts, rtol=1e-14, atol=0)
+    for k in range(3):
+        assert np.array_equal(b.get()[k], ref[k])
+        assert np.all(hist[:, k, :] > 0)
+    res, _ = b.compute_max_residuals()
+    assert np.array_equal(hist[-1], res)
