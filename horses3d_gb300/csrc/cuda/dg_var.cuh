@@ -843,8 +843,10 @@ __global__ void __launch_bounds__(128) kv_face_direct(VArgs<R> a) {
 
 // ------------------------------------------------------------------------------------------------
 // kv_update: surface integral, 1/J, source, RK3 stage update (per-case dt), traces of the new Q.
+// SRC adds the manufactured source, PST the static-pressure residual of the mixed form; both are
+// compile-time so that the common kernel carries neither (40 registers instead of 48).
 // ------------------------------------------------------------------------------------------------
-template <typename R, int PC, bool SRC>
+template <typename R, int PC, bool SRC, bool PST>
 __global__ void __launch_bounds__(256) kv_update(VArgs<R> a, int stage, double tshift, int write_qdot) {
     extern __shared__ __align__(16) unsigned char vsm[];
     const ItemDims d = item_dims<PC>(a.items[a.item0 + blockIdx.x]);
@@ -892,7 +894,7 @@ __global__ void __launch_bounds__(256) kv_update(VArgs<R> a, int stage, double t
 #pragma unroll
             for (int v = 0; v < 5; ++v) qd[v] = R(double(qd[v]) + S[v]);
         }
-        if (a.pstat) {
+        if (PST) {
             const double pr = cc.gm1 * cc.e_ref;  // the pressure the momentum fluxes leave out
 #pragma unroll
             for (int c = 0; c < 3; ++c) qd[1 + c] = R(double(qd[1 + c]) + pr * a.pstat[3 * g + c]);
@@ -1101,16 +1103,24 @@ cudaError_t launch_item_class(const VArgs<R>& a, int which, int n, size_t smem, 
         case 0: kv_traces<R, PC><<<n, 256, smem, s>>>(a); break;
         case 1: kv_volume<R, PC><<<n, 256, smem, s>>>(a, store_grad); break;
         // the update kernel is bound by its memory traffic; compile-time orders only lengthen it
-        case 2: kv_update<R, 0, false><<<n, 256, smem, s>>>(a, stage, tshift, wq); break;
-        default: kv_update<R, 0, true><<<n, 256, smem, s>>>(a, stage, tshift, wq); break;
+        case 2:
+            if (a.pstat) kv_update<R, 0, false, true><<<n, 256, smem, s>>>(a, stage, tshift, wq);
+            else kv_update<R, 0, false, false><<<n, 256, smem, s>>>(a, stage, tshift, wq);
+            break;
+        default:
+            if (a.pstat) kv_update<R, 0, true, true><<<n, 256, smem, s>>>(a, stage, tshift, wq);
+            else kv_update<R, 0, true, false><<<n, 256, smem, s>>>(a, stage, tshift, wq);
+            break;
     }
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         cudaFuncAttributes fa{};
         const void* fn = which == 0 ? reinterpret_cast<const void*>(kv_traces<R, PC>)
                          : which == 1 ? reinterpret_cast<const void*>(kv_volume<R, PC>)
-                         : which == 2 ? reinterpret_cast<const void*>(kv_update<R, 0, false>)
-                                      : reinterpret_cast<const void*>(kv_update<R, 0, true>);
+                         : which == 2 ? (a.pstat ? reinterpret_cast<const void*>(kv_update<R, 0, false, true>)
+                                                 : reinterpret_cast<const void*>(kv_update<R, 0, false, false>))
+                         : (a.pstat ? reinterpret_cast<const void*>(kv_update<R, 0, true, true>)
+                                    : reinterpret_cast<const void*>(kv_update<R, 0, true, false>));
         cudaFuncGetAttributes(&fa, fn);
         snprintf(failed_launch(), 160, "item kernel %d class %d grid %d smem %zu (limit %d, static %zu, regs %d)", which,
                  PC, n, smem, fa.maxDynamicSharedSizeBytes, fa.sharedSizeBytes, fa.numRegs);
@@ -1151,9 +1161,13 @@ template <typename R, int PC>
 cudaError_t set_item_attributes(size_t vol, size_t upd) {
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(kv_volume<R, PC>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(vol))) ||
-        (e = cudaFuncSetAttribute(kv_update<R, 0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (e = cudaFuncSetAttribute(kv_update<R, 0, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(upd))) ||
-        (e = cudaFuncSetAttribute(kv_update<R, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (e = cudaFuncSetAttribute(kv_update<R, 0, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(upd))) ||
+        (e = cudaFuncSetAttribute(kv_update<R, 0, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(upd))) ||
+        (e = cudaFuncSetAttribute(kv_update<R, 0, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(upd))) ||
         (e = cudaFuncSetAttribute(kv_traces<R, PC>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(upd))))
         return e;

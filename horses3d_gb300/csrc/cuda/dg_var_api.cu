@@ -367,7 +367,7 @@ ItemTable build_items(const std::vector<int>& eord, const std::vector<int>& ecas
 // the constant p_ref out of its FP32 momentum fluxes (exact where G = 0), so it adds p_ref G back in
 // the update. G is the FP64 right-hand side of the state at rest with unit pressure (no source),
 // computed once here with the FP64 kernels and FP64 item sizes; where its largest value is round-off
-// (straight or conforming meshes) nothing is added.
+// (straight or conforming meshes, below 1e-8) nothing is added.
 int static_pressure_residual(dg_ctx* c, const Gathered& h) {
     cudaStream_t s = c->stream;
     const size_t nd = static_cast<size_t>(c->ndof);
@@ -427,7 +427,7 @@ int static_pressure_residual(dg_ctx* c, const Gathered& h) {
             g3[3 * g + d] = q[5 * g + 1 + d];
             mx = std::max(mx, std::fabs(g3[3 * g + d]));
         }
-    if (mx > 1e-10) {
+    if (mx > 1e-8) {  // round-off of straight or conforming meshes stays far below; curved p-nonconforming ~0.1
         if ((e = c->pstat.upload(g3.data(), g3.size(), s)) != cudaSuccess)
             return done(cuda_fail(e, "static pressure upload"));
     }
