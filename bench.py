@@ -136,8 +136,8 @@ def build_case(n_elem: int = N_ELEM):
 
 
 # DRAM bytes per DOF of one k_volume<6, gauss, float> launch, measured with ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum = 445.2 MB over 2,985,984 DOF, 24^3 elements, N=5).
-VOLUME_DRAM_BYTES_PER_DOF = 149.1
+# (dram__bytes_read.sum + dram__bytes_write.sum = 444.8 MB over 2,985,984 DOF, 24^3 elements, N=5).
+VOLUME_DRAM_BYTES_PER_DOF = 149.0
 
 
 def volume_bytes(P: int, word: int) -> float:
@@ -203,7 +203,7 @@ def run_gpu_arm(args, rank, world, local, case):
                 "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / hbm, 4),
                 "traffic": traffic, "alg_bytes_per_launch": alg,
                 "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_volume launch on the "
-                                "24^3-element case (149.1 B/DOF), scaled by the DOF count"}
+                                "24^3-element case (149.0 B/DOF), scaled by the DOF count"}
 
     # e2e through the C ABI with host buffers (IntegrateInTime-shaped loop)
     import torch
