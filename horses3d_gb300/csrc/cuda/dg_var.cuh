@@ -27,6 +27,7 @@
 // Slot data (slot = 6e + side - 1) are stored per slot and variable: value(slot, v, p) at
 // [soff[slot]*NV + v*n_slot + p], n_slot the side's point count at the element's own orders.
 #pragma once
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 
@@ -841,20 +842,61 @@ __global__ void __launch_bounds__(128) kv_face_direct(VArgs<R> a) {
     }
 }
 
+// Shared memory of kv_update: the operators, sQ (5 R per node: the new Q for the traces) and, for
+// items of up to kStageNodes nodes, the updated G and Q (5 doubles per node each, stored back as flat
+// arrays) and the elements' value offsets. Larger items store G and Q per node: their staging space
+// would cut the resident blocks below the six that the kernel's 40 registers allow, and the kernel
+// is bound by the latency of its loads.
+constexpr int kStageNodes = 256;
+__host__ __device__ constexpr bool vupdate_staged(int cap) { return cap <= kStageNodes; }
+template <typename R>
+__host__ __device__ constexpr size_t vupdate_stage_offset(int cap) {
+    return (3 * sizeof(OpsP<R>) + static_cast<size_t>(5) * cap * sizeof(R) + 15) / 16 * 16;
+}
+
+// Elements of an item: each has at least 8 nodes (P >= 2 per direction), so at most cap/8 + 1.
+__host__ __device__ constexpr int vupdate_max_elems(int cap) { return cap / 8 + 1; }
+
+template <typename R>
+size_t vupdate_smem(int cap) {
+    if (!vupdate_staged(cap)) return 3 * sizeof(OpsP<R>) + static_cast<size_t>(5) * cap * sizeof(R);
+    return vupdate_stage_offset<R>(cap) + static_cast<size_t>(10) * cap * sizeof(double) +
+           static_cast<size_t>(vupdate_max_elems(cap)) * sizeof(long long);
+}
+
+// Flat store of the item's element blocks (W values per element, element le's block at global value
+// index base[le]) from shared memory: consecutive lanes write consecutive values. inv_w = 1/W as a
+// float gives the exact element of every index (f + 0.5 stays at least 0.5/W from a multiple of W).
+__device__ __forceinline__ void vupdate_store(const double* shared, double* global, const long long* base, int W, int n,
+                                              float inv_w) {
+    for (int f = threadIdx.x; f < n; f += blockDim.x) {
+        const int le = static_cast<int>((static_cast<float>(f) + 0.5f) * inv_w);
+        global[base[le] + (f - le * W)] = shared[f];
+    }
+}
+
 // ------------------------------------------------------------------------------------------------
 // kv_update: surface integral, 1/J, source, RK3 stage update (per-case dt), traces of the new Q.
 // SRC adds the manufactured source, PST the static-pressure residual of the mixed form; both are
-// compile-time so that the common kernel carries neither (40 registers instead of 48).
+// compile-time so that the common kernel carries neither (40 registers instead of 48). FP32 <-> FP64
+// conversions use the integer pipe (bit-exact with the hardware conversion, which runs on the FP64
+// pipe beside the update's FP64 multiply-adds).
 // ------------------------------------------------------------------------------------------------
 template <typename R, int PC, bool SRC, bool PST>
-__global__ void __launch_bounds__(256) kv_update(VArgs<R> a, int stage, double tshift, int write_qdot) {
+__global__ void __launch_bounds__(256, sizeof(R) == 4 && !SRC && !PST ? 6 : 0)
+    kv_update(VArgs<R> a, int stage, double tshift, int write_qdot, int cap) {
     extern __shared__ __align__(16) unsigned char vsm[];
     const ItemDims d = item_dims<PC>(a.items[a.item0 + blockIdx.x]);
     const int px = d.px, py = d.py, np = d.np, ntot = d.ntot;
     OpsP<R>* sO = reinterpret_cast<OpsP<R>*>(vsm);
     R* sQ = reinterpret_cast<R*>(sO + 3);
+    const bool staged = vupdate_staged(cap);
+    double* sG = reinterpret_cast<double*>(vsm + vupdate_stage_offset<R>(cap));
+    double* sQd = sG + 5 * cap;
+    long long* sE = reinterpret_cast<long long*>(sQd + 5 * cap);
+    // the operators in shared memory serve the traces at the end (after the barrier there); the
+    // surface integral reads its six weights through the cache, so no barrier precedes the node loads
     load_ops(a.ops, sO, px, py, d.pz);
-    __syncthreads();
     const CaseConst cc = a.cc[d.kase];
     const double dt = stage >= 0 ? a.dt[d.kase] : 0.0;
     const double ak = stage == 0 ? 0.0 : (stage == 1 ? -5.0 / 9.0 : -153.0 / 128.0);
@@ -872,8 +914,9 @@ __global__ void __launch_bounds__(256) kv_update(VArgs<R> a, int stage, double t
         const R* FR = a.FS + a.soff[s0 + 3] * 5 + (j + py * k);
         const R* FT = a.FS + a.soff[s0 + 4] * 5 + (i + px * j);
         const R* FL = a.FS + a.soff[s0 + 5] * 5 + (j + py * k);
-        const R bxl = sO[0].bL[i], bxr = sO[0].bR[i], byl = sO[1].bL[j], byr = sO[1].bR[j];
-        const R bzl = sO[2].bL[k], bzr = sO[2].bR[k];
+        const R bxl = __ldg(&a.ops[px].bL[i]), bxr = __ldg(&a.ops[px].bR[i]);
+        const R byl = __ldg(&a.ops[py].bL[j]), byr = __ldg(&a.ops[py].bR[j]);
+        const R bzl = __ldg(&a.ops[d.pz].bL[k]), bzr = __ldg(&a.ops[d.pz].bR[k]);
         const R J = a.jac[g];
         R qd[5];
 #pragma unroll
@@ -892,12 +935,12 @@ __global__ void __launch_bounds__(256) kv_update(VArgs<R> a, int stage, double t
             manufactured_source(a.source, a.x[3 * g], a.x[3 * g + 1], a.x[3 * g + 2], tt, cc.gm1, cc.gM2, cc.mu,
                                 cc.kappa, S);
 #pragma unroll
-            for (int v = 0; v < 5; ++v) qd[v] = R(double(qd[v]) + S[v]);
+            for (int v = 0; v < 5; ++v) qd[v] = from_f64<R>(widen(qd[v]) + S[v]);
         }
         if (PST) {
             const double pr = cc.gm1 * cc.e_ref;  // the pressure the momentum fluxes leave out
 #pragma unroll
-            for (int c = 0; c < 3; ++c) qd[1 + c] = R(double(qd[1 + c]) + pr * a.pstat[3 * g + c]);
+            for (int c = 0; c < 3; ++c) qd[1 + c] = from_f64<R>(widen(qd[1 + c]) + pr * a.pstat[3 * g + c]);
         }
         if (write_qdot) {
 #pragma unroll
@@ -908,18 +951,30 @@ __global__ void __launch_bounds__(256) kv_update(VArgs<R> a, int stage, double t
             double qq[5];
 #pragma unroll
             for (int v = 0; v < 5; ++v) {
-                const double gq = ak * a.G[5 * g + v] + double(qd[v]);
+                const double gq = ak * a.G[5 * g + v] + widen(qd[v]);
                 qq[v] = a.Q[5 * g + v] + cdt * gq;
-                a.G[5 * g + v] = gq;
-                a.Q[5 * g + v] = qq[v];
+                if (staged) {
+                    sG[5 * t + v] = gq;
+                    sQd[5 * t + v] = qq[v];
+                } else {
+                    a.G[5 * g + v] = gq;
+                    a.Q[5 * g + v] = qq[v];
+                }
             }
+            if (staged && n == 0) sE[le] = 5 * g;
 #pragma unroll
-            for (int v = 0; v < 4; ++v) sQ[v * ntot + t] = R(qq[v]);
-            sQ[4 * ntot + t] = R(qq[4] - cc.e_ref);
+            for (int v = 0; v < 4; ++v) sQ[v * ntot + t] = from_f64<R>(qq[v]);
+            sQ[4 * ntot + t] = from_f64<R>(qq[4] - cc.e_ref);
         }
     }
     if (stage < 0) return;
     __syncthreads();
+    if (staged) {
+        const int W = 5 * np;
+        const float inv_w = 1.0f / static_cast<float>(W);
+        vupdate_store(sG, a.G, sE, W, 5 * ntot, inv_w);
+        vupdate_store(sQd, a.Q, sE, W, 5 * ntot, inv_w);
+    }
     write_traces<R, 5, PC>(a, d, sO, sQ, a.QF);
 }
 
@@ -1098,18 +1153,18 @@ inline char* failed_launch() {
 
 template <typename R, int PC>
 cudaError_t launch_item_class(const VArgs<R>& a, int which, int n, size_t smem, cudaStream_t s, int store_grad,
-                              int stage, double tshift, int wq) {
+                              int stage, double tshift, int wq, int cap) {
     switch (which) {
         case 0: kv_traces<R, PC><<<n, 256, smem, s>>>(a); break;
         case 1: kv_volume<R, PC><<<n, 256, smem, s>>>(a, store_grad); break;
         // the update kernel is bound by its memory traffic; compile-time orders only lengthen it
         case 2:
-            if (a.pstat) kv_update<R, 0, false, true><<<n, 256, smem, s>>>(a, stage, tshift, wq);
-            else kv_update<R, 0, false, false><<<n, 256, smem, s>>>(a, stage, tshift, wq);
+            if (a.pstat) kv_update<R, 0, false, true><<<n, 256, smem, s>>>(a, stage, tshift, wq, cap);
+            else kv_update<R, 0, false, false><<<n, 256, smem, s>>>(a, stage, tshift, wq, cap);
             break;
         default:
-            if (a.pstat) kv_update<R, 0, true, true><<<n, 256, smem, s>>>(a, stage, tshift, wq);
-            else kv_update<R, 0, true, false><<<n, 256, smem, s>>>(a, stage, tshift, wq);
+            if (a.pstat) kv_update<R, 0, true, true><<<n, 256, smem, s>>>(a, stage, tshift, wq, cap);
+            else kv_update<R, 0, true, false><<<n, 256, smem, s>>>(a, stage, tshift, wq, cap);
             break;
     }
     const cudaError_t e = cudaGetLastError();
@@ -1139,17 +1194,18 @@ cudaError_t launch_items(const VArgs<R>& a0, int which, cudaStream_t s, int stor
         if (n <= 0) continue;
         VArgs<R> a = a0;
         a.item0 = a0.cls[c];
-        const size_t smem = vitem_smem<R>(a0.ccap[c], which == 1 ? 20 : 5);
+        const int cap = a0.ccap[c];
+        const size_t smem = which >= 2 ? vupdate_smem<R>(cap) : vitem_smem<R>(cap, which == 1 ? 20 : 5);
         cudaError_t e;
         switch (c) {
-            case 0: e = launch_item_class<R, 0>(a, which, n, smem, s, store_grad, stage, tshift, wq); break;
-            case 2: e = launch_item_class<R, 2>(a, which, n, smem, s, store_grad, stage, tshift, wq); break;
-            case 3: e = launch_item_class<R, 3>(a, which, n, smem, s, store_grad, stage, tshift, wq); break;
-            case 4: e = launch_item_class<R, 4>(a, which, n, smem, s, store_grad, stage, tshift, wq); break;
-            case 5: e = launch_item_class<R, 5>(a, which, n, smem, s, store_grad, stage, tshift, wq); break;
-            case 6: e = launch_item_class<R, 6>(a, which, n, smem, s, store_grad, stage, tshift, wq); break;
-            case 7: e = launch_item_class<R, 7>(a, which, n, smem, s, store_grad, stage, tshift, wq); break;
-            case 8: e = launch_item_class<R, 8>(a, which, n, smem, s, store_grad, stage, tshift, wq); break;
+            case 0: e = launch_item_class<R, 0>(a, which, n, smem, s, store_grad, stage, tshift, wq, cap); break;
+            case 2: e = launch_item_class<R, 2>(a, which, n, smem, s, store_grad, stage, tshift, wq, cap); break;
+            case 3: e = launch_item_class<R, 3>(a, which, n, smem, s, store_grad, stage, tshift, wq, cap); break;
+            case 4: e = launch_item_class<R, 4>(a, which, n, smem, s, store_grad, stage, tshift, wq, cap); break;
+            case 5: e = launch_item_class<R, 5>(a, which, n, smem, s, store_grad, stage, tshift, wq, cap); break;
+            case 6: e = launch_item_class<R, 6>(a, which, n, smem, s, store_grad, stage, tshift, wq, cap); break;
+            case 7: e = launch_item_class<R, 7>(a, which, n, smem, s, store_grad, stage, tshift, wq, cap); break;
+            case 8: e = launch_item_class<R, 8>(a, which, n, smem, s, store_grad, stage, tshift, wq, cap); break;
             default: e = cudaErrorInvalidValue; break;  // no item has a single node per direction
         }
         if (e != cudaSuccess) return e;
@@ -1158,7 +1214,7 @@ cudaError_t launch_items(const VArgs<R>& a0, int which, cudaStream_t s, int stor
 }
 
 template <typename R, int PC>
-cudaError_t set_item_attributes(size_t vol, size_t upd) {
+cudaError_t set_item_attributes(size_t vol, size_t upd, size_t trc) {
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(kv_volume<R, PC>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(vol))) ||
         (e = cudaFuncSetAttribute(kv_update<R, 0, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1169,20 +1225,21 @@ cudaError_t set_item_attributes(size_t vol, size_t upd) {
                                   static_cast<int>(upd))) ||
         (e = cudaFuncSetAttribute(kv_update<R, 0, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(upd))) ||
-        (e = cudaFuncSetAttribute(kv_traces<R, PC>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(upd))))
+        (e = cudaFuncSetAttribute(kv_traces<R, PC>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(trc))))
         return e;
     return cudaSuccess;
 }
 
 template <typename R>
 cudaError_t vrun_stage(const VArgs<R>& a, int stage, double tshift, int flags, cudaStream_t s) {
-    const size_t vol = vitem_smem<R>(a.cap, 20), upd = vitem_smem<R>(a.cap, 5);
+    const size_t vol = vitem_smem<R>(a.cap, 20), trc = vitem_smem<R>(a.cap, 5);
+    const size_t upd = std::max(vupdate_smem<R>(a.cap), vupdate_smem<R>(std::min(a.cap, kStageNodes)));
     if (stage == kPrepare) {
         cudaError_t e;
-        if ((e = set_item_attributes<R, 0>(vol, upd)) || (e = set_item_attributes<R, 2>(vol, upd)) ||
-            (e = set_item_attributes<R, 3>(vol, upd)) || (e = set_item_attributes<R, 4>(vol, upd)) ||
-            (e = set_item_attributes<R, 5>(vol, upd)) || (e = set_item_attributes<R, 6>(vol, upd)) ||
-            (e = set_item_attributes<R, 7>(vol, upd)) || (e = set_item_attributes<R, 8>(vol, upd)) ||
+        if ((e = set_item_attributes<R, 0>(vol, upd, trc)) || (e = set_item_attributes<R, 2>(vol, upd, trc)) ||
+            (e = set_item_attributes<R, 3>(vol, upd, trc)) || (e = set_item_attributes<R, 4>(vol, upd, trc)) ||
+            (e = set_item_attributes<R, 5>(vol, upd, trc)) || (e = set_item_attributes<R, 6>(vol, upd, trc)) ||
+            (e = set_item_attributes<R, 7>(vol, upd, trc)) || (e = set_item_attributes<R, 8>(vol, upd, trc)) ||
             (e = cudaFuncSetAttribute(kv_face<R, kJump, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       static_cast<int>(FaceCfg<R, kJump>::SMEM))) ||
             (e = cudaFuncSetAttribute(kv_face<R, kJump, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
