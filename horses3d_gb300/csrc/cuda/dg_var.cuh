@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(256) kv_traces(VArgs<R> a) {
 // kv_volume: gradient + lifting + gradient traces (Navier-Stokes), fluxes, weak volume integral.
 // ------------------------------------------------------------------------------------------------
 template <typename R, int PC>
-__global__ void __launch_bounds__(256) kv_volume(VArgs<R> a, int store_grad) {
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 0) kv_volume(VArgs<R> a, int store_grad) {
     extern __shared__ __align__(16) unsigned char vsm[];
     const ItemDims d = item_dims<PC>(a.items[a.item0 + blockIdx.x]);
     const int px = d.px, py = d.py, pz = d.pz, np = d.np, ntot = d.ntot;
