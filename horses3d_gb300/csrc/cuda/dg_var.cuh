@@ -490,7 +490,8 @@ __device__ __forceinline__ R* to_face_points(const R* tset, R* S, R* A, int s1, 
 // logarithmic-mean averages (V = 1). The common variants (V = 0) keep the short code and register
 // footprint.
 template <typename R, int MODE, int V>
-__global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS) kv_face(VArgs<R> a) {
+__global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS, (sizeof(R) == 4 && MODE == kFluxEuler && V == 0) ? 5 : 0)
+    kv_face(VArgs<R> a) {
     using Cfg = FaceCfg<R, MODE>;
     constexpr int NVIN = Cfg::NVIN, NVOUT = Cfg::NVOUT, NVB = Cfg::NVB, NP = kFacePts;
     extern __shared__ __align__(16) unsigned char fsm[];
