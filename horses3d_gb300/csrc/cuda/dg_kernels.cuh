@@ -94,13 +94,15 @@ struct Geo {
 };
 
 // Minimum resident blocks per SM requested from the register allocator: the kernels are latency
-// bound at one element per block, so occupancy is bought with a register budget per thread.
+// bound at one element per block, so occupancy is bought with a register budget per thread. The
+// FP32 volume budgets are measured: 64 registers (4 blocks) for P = 5 (the split-form workload,
+// +6 %), 72 elsewhere (P = 6: 64 spills; P = 4: 64 measured 8 % slower).
 template <int P, typename R>
 struct Occupancy {
     static constexpr int blocks(int regs) {
         return (65536 / (Geo<P>::THREADS * regs)) > 0 ? (65536 / (Geo<P>::THREADS * regs)) : 1;
     }
-    static constexpr int volume = blocks(sizeof(R) == 4 ? 72 : 168);
+    static constexpr int volume = blocks(sizeof(R) == 4 ? (P == 5 ? 64 : 72) : 168);
     static constexpr int update = blocks(sizeof(R) == 4 ? 64 : 96);
 };
 
