@@ -319,3 +319,47 @@ def test_batch_integrate_on_device():
         assert np.all(hist[:, k, :] > 0)
     res, _ = b.compute_max_residuals()
     assert np.array_equal(hist[-1], res)
+
+
+_ITEM_SIZE_RUN = """
+import sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+import cases
+from horses3d_gb300 import _abi
+from horses3d_gb300.solver import NavierStokesDG
+mesh, cfg, q0 = cases.aniso_tgv_case(n=4, lo=3, hi=4, seed=21, precision=_abi.DG_PRECISION_MIXED)
+g = NavierStokesDG(mesh, cfg)
+g.set_state(q0)
+g.run_steps(3, 0.0, dt=1e-3)
+np.save(sys.argv[2], g.Q)
+"""
+
+
+def test_update_store_paths_agree_bit_for_bit(tmp_path):
+    """kv_update stores G and Q through shared memory as flat arrays for items of up to 256 nodes and
+    per node for larger ones; the item size changes only the grouping, so 64-node and 512-node items
+    (the tune file fixes them, one process each) give identical states."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    # 64 elements over 8 order triples (4..5 nodes per direction): 512-node items hold several
+    # elements (more than 256 nodes), 64-node items one
+    mesh, _, _ = cases.aniso_tgv_case(n=4, lo=3, hi=4, seed=21)
+    triples = {tuple(int(v) + 1 for v in o) for o in mesh.order}
+    assert len(triples) >= 4
+    tests_dir = str(Path(__file__).resolve().parent)
+    repo = str(Path(__file__).resolve().parent.parent)
+    out = {}
+    for cap in (64, 512):
+        tune = tmp_path / f"tune{cap}.txt"
+        # key: px py pz, FP32 (mixed) form, Navier-Stokes, Gauss nodes -> nodes per item
+        tune.write_text("".join(f"{px} {py} {pz} 1 1 {_abi.DG_NODES_GAUSS} {cap}\n" for px, py, pz in sorted(triples)))
+        env = dict(os.environ, HORSES3D_GB300_TUNE_FILE=str(tune))
+        dst = tmp_path / f"q{cap}.npy"
+        subprocess.run([sys.executable, "-c", _ITEM_SIZE_RUN, tests_dir, str(dst)], cwd=repo, env=env, check=True,
+                       timeout=600)
+        out[cap] = np.load(dst)
+    assert np.array_equal(out[64], out[512])
