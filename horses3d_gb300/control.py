@@ -43,6 +43,9 @@ class Config:
     dt: float | None = None
     n_steps: int = 1
     t_final: float | None = None
+    # steady-state runs stop when the maximum residual reaches it ("convergence tolerance",
+    # TimeIntegrator.f90:214,820-828); None runs the step count
+    convergence_tolerance: float | None = None
     periodic: list = field(default_factory=list)
     order_file: str | None = None
     aoa_theta: float = 0.0  # degrees ("AOA theta", PhysicsStorage_NS.f90)
@@ -155,6 +158,11 @@ def _value(v: str) -> str:
     return v.strip()
 
 
+def _fortran_real(v: str) -> float:
+    """A real in Fortran list-directed form (1.d-10, 1.0D0, 2.5e-3)."""
+    return float(v.strip().lower().replace("d", "e"))
+
+
 def parse_control(text: str) -> Config:
     cfg = Config()
     keys: dict[str, str] = {}
@@ -243,6 +251,8 @@ def parse_control(text: str) -> Config:
     if "dt" in keys:
         cfg.dt = float(keys["dt"])
     cfg.n_steps = int(float(get("number of time steps", 1)))
+    if "convergence tolerance" in keys:
+        cfg.convergence_tolerance = _fortran_real(keys["convergence tolerance"])
     if "final time" in keys:
         cfg.t_final = float(keys["final time"])
     cfg.aoa_theta = float(get("aoa theta", 0.0))
@@ -252,7 +262,9 @@ def parse_control(text: str) -> Config:
         if b.get("kind") != "boundary":
             continue
         kind = str(b.get("type", "")).replace(" ", "").lower()
-        names = b["name"].split()  # "#define boundary a b c" applies to every name
+        # the names of a "#define boundary" line are joined by "__"
+        # (GenericBoundaryConditionClass.f90:400-456, CheckIfBoundaryNameIsContained)
+        names = [n for part in b["name"].split("__") for n in part.split()]
         if kind == "periodic":
             pairs.append((b["name"].strip(), str(b.get("coupled boundary", "")).lower().strip()))
         elif kind in ("noslipwall", "freeslipwall", "inflow", "outflow"):

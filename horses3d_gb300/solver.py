@@ -145,13 +145,16 @@ class NavierStokesDG:
                           cfl: float | None = None, dcfl: float | None = None, dt: float | None = None,
                           compute_after_steps: bool = False) -> StepReport:
         """IntegrateInTime's explicit loop: MaxTimeStep (when cfl is given), CorrectDt, RKStep,
-        t += dt, ComputeMaxResiduals, stop at the final time or after n_steps."""
+        t += dt, ComputeMaxResiduals, stop at the final time or after n_steps; without a final time
+        (a steady-state run) also at the first step whose maximum residual is at most the
+        convergence tolerance (TimeIntegrator.f90:820-828)."""
         cfg = self.config
         cfl = cfg.cfl if cfl is None else cfl
         dcfl = cfg.dcfl if dcfl is None else dcfl
         dt_fixed = cfg.dt if dt is None else dt
         n_steps = cfg.n_steps if n_steps is None else n_steps
         t_final = cfg.t_final if t_final is None else t_final
+        tol = cfg.convergence_tolerance if t_final is None else None
         t = float(t0)
         it = 0
         eps = np.finfo(float).eps
@@ -169,5 +172,7 @@ class NavierStokesDG:
             if nan:
                 raise FloatingPointError(f"NaN or Inf in the solution at t={t} (checkForNan)")
             if t_final is not None and (t >= t_final or abs(t - t_final) <= 100.0 * eps):
+                break
+            if tol is not None and np.max(res) <= tol:
                 break
         return StepReport(it, t, res)

@@ -159,6 +159,41 @@ def cylinder_mesh(cfg, tmp_dir):
     return HexMesh.from_specmesh(path, cfg.order, node_type=cfg.nodes, periodic=cfg.periodic_spec())
 
 
+# Euler UniformFlow (Solver/test/Euler/UniformFlow/SETUP/ProblemFile.f90:320-323): per polynomial order,
+# the iterations to a maximum residual of 1e-10 (exact) and that final residual (FTAssertEqual, 1e-3).
+UNIFORM_FLOW_GOLDENS = {3: (1821, 9.7985624521602423e-11), 4: (3090, 9.7825050715404729e-11),
+                        5: (4164, 9.7454147241309180e-11)}
+
+
+def uniform_flow_config(order=5):
+    """UniformFlow.control: Euler, Box27.mesh, Gauss nodes, Rusanov, CFL 0.4, M=0.5, AoA 0, inflow on
+    every side (the six zones of one "#define boundary left__right__front__back__bottom__top" block),
+    steady state to a maximum residual of 1e-10 (at most 5000 steps)."""
+    cfg = Config(order=order, nodes=_abi.DG_NODES_GAUSS, flow="euler", mach=0.5, reynolds=0.0,
+                 riemann=_abi.DG_RIEMANN_RUSANOV, cfl=0.4, dcfl=0.4, n_steps=5000, aoa_theta=0.0, aoa_phi=0.0,
+                 convergence_tolerance=1e-10)
+    cfg.boundaries = {z: {"type": "inflow"} for z in ("left", "right", "front", "back", "bottom", "top")}
+    return cfg
+
+
+def box27_mesh(cfg, tmp_dir):
+    """Box27.mesh (27 unit cubes) from the committed fixture (tests/golden/make_fixtures.py)."""
+    import gzip
+
+    path = __import__("pathlib").Path(tmp_dir) / "Box27.mesh"
+    path.write_bytes(gzip.decompress((GOLDEN_DIR / "Box27.mesh.gz").read_bytes()))
+    return HexMesh.from_specmesh(path, cfg.order, node_type=cfg.nodes, periodic=cfg.periodic_spec())
+
+
+def uniform_flow_state(cfg, mesh):
+    """UserDefinedInitialCondition of UniformFlow (ProblemFile.f90:64-144): the free stream, with the
+    density of node (3,3,3) of every element raised by 5 % (energy unchanged)."""
+    q = free_stream_state(cfg, mesh).reshape(-1, 5)
+    P = cfg.order + 1
+    q[3 + P * (3 + P * 3)::P ** 3, 0] *= 1.05
+    return q.ravel()
+
+
 def free_stream_state(cfg, mesh):
     rho, u, v, w, p = cfg.free_stream()
     return np.tile([rho, rho * u, rho * v, rho * w, p / 0.4 + 0.5 * rho * (u * u + v * v + w * w)], mesh.ndof)

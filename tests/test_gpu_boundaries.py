@@ -199,3 +199,26 @@ def test_batch_with_walled_and_periodic_cases():
             o.rk3_step(s * dt, dt)
         err = rel_l2(g, o.get(0), cases.quadrature_weights(m))
         assert np.all(err <= STATE_TOL), err
+
+
+@pytest.mark.parametrize("order", [3, 5])
+def test_uniform_flow_reaches_the_reference_goldens(order, tmp_path):
+    """Euler UniformFlow on Box27.mesh (inflow on every side, Rusanov, CFL 0.4, M=0.5) on the GPU:
+    the steady-state loop stops at the reference's iteration count with its final residual (FTAssertEqual,
+    1e-3), and the state is the free stream within 1e-10. The host-driven loop (integrate_in_time) and
+    the device loop (dg_integrate) cross the tolerance at the same step."""
+    cfg = cases.uniform_flow_config(order)
+    mesh = cases.box27_mesh(cfg, tmp_path)
+    iters, golden_res = cases.UNIFORM_FLOW_GOLDENS[order]
+    g = NavierStokesDG(mesh, cfg)
+    g.set_state(cases.uniform_flow_state(cfg, mesh))
+    rep = g.integrate_in_time(t0=0.0)
+    assert rep.iterations == iters
+    assert cases.ftassert_equal(golden_res, np.max(rep.residuals), 1e-3), (np.max(rep.residuals), golden_res)
+    assert np.max(np.abs(g.Q - cases.free_stream_state(cfg, mesh))) <= 1e-10
+    d = NavierStokesDG(mesh, cfg)
+    d.set_state(cases.uniform_flow_state(cfg, mesh))
+    _, hist = d.integrate_on_device(iters, cfl=cfg.cfl, dcfl=cfg.dcfl)
+    m = hist.max(axis=1)
+    assert m[-1] <= cfg.convergence_tolerance and np.all(m[:-1] > cfg.convergence_tolerance)
+    assert np.array_equal(d.Q, g.Q)

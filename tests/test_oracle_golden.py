@@ -146,6 +146,48 @@ def test_conserving_cylinder_goldens(test, tmp_path):
     assert cases.ftassert_close(g[2], res[2], 1e-10), res - g
 
 
+UNIFORM_FLOW = Path("/root/reference/Solver/test/Euler/UniformFlow")
+
+
+@pytest.mark.parametrize("order", [3, 4, 5])
+def test_uniform_flow_goldens(order, tmp_path):
+    """Euler UniformFlow on Box27.mesh: inflow conditions on all six sides, Rusanov, CFL 0.4, M=0.5,
+    from the free stream with a 5 % density bump in every element, marched until the maximum
+    residual reaches 1e-10 (TimeIntegrator.f90:737-890, steady state). Goldens: the iteration count
+    (exact) and the final residual per order (FTAssertEqual, tol 1e-3), and the final state equal to
+    the free stream within 1e-10 (ProblemFile.f90:320-372). Where the reference is mounted, its
+    control file must give the same configuration."""
+    cfg = cases.uniform_flow_config(order)
+    control = UNIFORM_FLOW / "UniformFlow.control"
+    if control.exists():
+        from horses3d_gb300.control import read_control
+
+        rc = read_control(control)
+        for k in ("nodes", "mach", "riemann", "cfl", "aoa_theta", "aoa_phi", "flow", "n_steps", "convergence_tolerance"):
+            assert getattr(rc, k) == getattr(cfg, k), k
+        assert rc.order == 5 and rc.periodic == []
+        assert {z: b["type"] for z, b in rc.boundaries.items()} == {z: b["type"] for z, b in cfg.boundaries.items()}
+    mesh = cases.box27_mesh(cfg, tmp_path)
+    assert mesh.n_boundary_faces == 54 and set(mesh.zone_names) == set(cfg.boundaries)
+    o = oracle.Oracle(mesh, cfg.physics(), cfg.options(), cfg.boundary_table(mesh.zone_names))
+    o.set_state(cases.uniform_flow_state(cfg, mesh))
+    t, iters, res = 0.0, 0, None
+    for k in range(cfg.n_steps):
+        dt = o.max_dt(cfg.cfl, cfg.dcfl)
+        o.rk3_step(t, dt)
+        t += dt
+        res, nan = o.residuals()
+        assert not nan
+        if res.max() <= cfg.convergence_tolerance:
+            iters = k + 1
+            break
+    golden_iters, golden_res = cases.UNIFORM_FLOW_GOLDENS[order]
+    assert iters == golden_iters
+    assert cases.ftassert_equal(golden_res, res.max(), 1e-3), (res.max(), golden_res)
+    err = np.max(np.abs(o.get(0) - cases.free_stream_state(cfg, mesh)))
+    assert err <= 1e-10, err
+
+
 def test_nodal_storage_quadrature_and_derivative():
     # Solver/test/Components/NodalStorage/src/NodalStorageTests.f90:10-63 (N=8 Gauss, tol 1e-12)
     x, w, D = nodal_storage(_abi.DG_NODES_GAUSS, 8)
