@@ -159,6 +159,69 @@ def cylinder_mesh(cfg, tmp_dir):
     return HexMesh.from_specmesh(path, cfg.order, node_type=cfg.nodes, periodic=cfg.periodic_spec())
 
 
+# The NavierStokes Cylinder family (Solver/test/NavierStokes/<case>/SETUP/ProblemFile.f90): the five
+# residuals after 100 CFL steps from the free stream, FTAssertEqual on value + 1 with the case's
+# tolerance, and the mesh fixture of the case.
+CYLINDER_GOLDENS = {
+    # Cylinder/SETUP/ProblemFile.f90:556-560,572-595
+    "Cylinder": (np.array([8.8131248889811715e+00, 1.7608838068776613e+01, 1.9037533106262516e-01,
+                           2.4301352846288605e+01, 2.4063786464536835e+02]), 1e-11),
+    # CylinderDucros/SETUP/ProblemFile.f90:555-559,570-593
+    "CylinderDucros": (np.array([9.49419906221126, 24.2427358262976, 0.231929845707823, 27.3961550687737,
+                                 259.972329181719]), 1e-11),
+    # CylinderChandrasekarRoe/SETUP/ProblemFile.f90:538-542,548-571
+    "CylinderChandrasekarRoe": (np.array([9.292005572719354, 24.258016397589838, 0.2388511827572224,
+                                          28.435107391243378, 253.03319158649319]), 1e-7),
+    # CylinderDifferentOrders/SETUP/ProblemFile.f90:556-560,572-595
+    "CylinderDifferentOrders": (np.array([9.5806856005342933e+00, 2.0804408993372231e+01, 3.7668665836122439e-01,
+                                          2.8294964263463125e+01, 2.6470704194989690e+02]), 1e-11),
+}
+
+
+def cylinder_case_config(case):
+    """<case>.control of the Cylinder family: M=0.3, Re=200, AoA phi 90, CFL = dCFL = 0.3, 100 steps,
+    a no-slip wall on the cylinder, free-slip walls at bottom/top, inflow at back/left/front and
+    outflow at right. Cylinder: N=3 Gauss, Roe. CylinderDucros: split form (Gauss-Lobatto), standard
+    Roe, Ducros average. CylinderChandrasekarRoe: split form, Roe, Chandrasekar average.
+    CylinderDifferentOrders: Roe, Re=45, CFL = dCFL = 0.2, per-element (Nx, Ny, Nz) from
+    OrdersN2N3N4N5_anisotropy.csv. CylinderDucros sets the Roe dissipation scaling lambda to 0.9."""
+    split = case in ("CylinderDucros", "CylinderChandrasekarRoe")
+    cfg = Config(order=3, nodes=_abi.DG_NODES_GAUSS_LOBATTO if split else _abi.DG_NODES_GAUSS, mach=0.3,
+                 reynolds=200.0, riemann=_abi.DG_RIEMANN_STD_ROE if case == "CylinderDucros" else _abi.DG_RIEMANN_ROE,
+                 inviscid=_abi.DG_INVISCID_SPLIT if split else _abi.DG_INVISCID_STANDARD,
+                 averaging={"CylinderDucros": _abi.DG_AVG_DUCROS,
+                            "CylinderChandrasekarRoe": _abi.DG_AVG_CHANDRASEKAR}.get(case, _abi.DG_AVG_STANDARD),
+                 cfl=0.3, dcfl=0.3, n_steps=100, aoa_theta=0.0, aoa_phi=90.0, convergence_tolerance=1e-10)
+    if case == "CylinderDucros":
+        cfg.lambda_stab = 0.9
+    if case == "CylinderDifferentOrders":
+        cfg.order_file = "MESH/OrdersN2N3N4N5_anisotropy.csv"
+        cfg.reynolds = 45.0
+        cfg.cfl = cfg.dcfl = 0.2
+    cfg.boundaries = {"innercylinder": {"type": "noslipwall"}, "bottom": {"type": "freeslipwall"},
+                      "top": {"type": "freeslipwall"}, "back": {"type": "inflow"}, "left": {"type": "inflow"},
+                      "front": {"type": "inflow"}, "right": {"type": "outflow"}}
+    return cfg
+
+
+def cylinder_case_mesh(case, cfg, tmp_dir):
+    """The case's mesh (and orders) from the committed fixtures (tests/golden/make_fixtures.py)."""
+    import gzip
+    from pathlib import Path
+
+    from horses3d_gb300.control import read_order_file
+
+    name = "CylinderNSpol3_1elem_y.mesh" if case == "CylinderDifferentOrders" else "CylinderNSpol3.mesh"
+    path = Path(tmp_dir) / name
+    path.write_bytes(gzip.decompress((GOLDEN_DIR / f"{name}.gz").read_bytes()))
+    orders = cfg.order
+    if cfg.order_file is not None:
+        op = Path(tmp_dir) / Path(cfg.order_file).name
+        op.write_bytes(gzip.decompress((GOLDEN_DIR / f"{op.name}.gz").read_bytes()))
+        orders = read_order_file(op)
+    return HexMesh.from_specmesh(path, orders, node_type=cfg.nodes, periodic=cfg.periodic_spec())
+
+
 # Euler UniformFlow (Solver/test/Euler/UniformFlow/SETUP/ProblemFile.f90:320-323): per polynomial order,
 # the iterations to a maximum residual of 1e-10 (exact) and that final residual (FTAssertEqual, 1e-3).
 UNIFORM_FLOW_GOLDENS = {3: (1821, 9.7985624521602423e-11), 4: (3090, 9.7825050715404729e-11),

@@ -3,8 +3,13 @@
   CylinderNSpol3.mesh.gz  the SpecMesh file of Solver/test/TestMeshes/CylinderNSpol3.mesh (the mesh of
                           the EnergyConservingTest and EntropyConservingTest cases)
   Box27.mesh.gz           Solver/test/TestMeshes/Box27.mesh (the mesh of the Euler UniformFlow case)
+  CylinderNSpol3_1elem_y.mesh.gz
+                          Solver/test/TestMeshes/CylinderNSpol3_1elem_y.mesh and
+  OrdersN2N3N4N5_anisotropy.csv.gz
+                          Solver/test/NavierStokes/CylinderDifferentOrders/MESH/OrdersN2N3N4N5_anisotropy.csv
+                          (the mesh and per-element orders of the CylinderDifferentOrders case)
 
-Both gzip-compressed, so that the GPU tests can run those cases where the reference is absent.
+All gzip-compressed, so that the GPU tests can run those cases where the reference is absent.
 
 Usage: python tests/golden/make_fixtures.py [reference root]
 """
@@ -15,14 +20,16 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 
 
-MESHES = ("CylinderNSpol3.mesh", "Box27.mesh")
+FILES = ("Solver/test/TestMeshes/CylinderNSpol3.mesh", "Solver/test/TestMeshes/Box27.mesh",
+         "Solver/test/TestMeshes/CylinderNSpol3_1elem_y.mesh",
+         "Solver/test/NavierStokes/CylinderDifferentOrders/MESH/OrdersN2N3N4N5_anisotropy.csv")
 
 
 def main(root: str = "/root/reference") -> None:
-    for name in MESHES:
-        data = (Path(root) / "Solver/test/TestMeshes" / name).read_bytes()
-        with gzip.GzipFile(HERE / f"{name}.gz", "wb", mtime=0) as fh:
-            fh.write(data)
+    for rel in FILES:
+        src = Path(root) / rel
+        with gzip.GzipFile(HERE / f"{src.name}.gz", "wb", mtime=0) as fh:
+            fh.write(src.read_bytes())
 
 
 if __name__ == "__main__":

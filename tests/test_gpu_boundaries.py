@@ -222,3 +222,19 @@ def test_uniform_flow_reaches_the_reference_goldens(order, tmp_path):
     m = hist.max(axis=1)
     assert m[-1] <= cfg.convergence_tolerance and np.all(m[:-1] > cfg.convergence_tolerance)
     assert np.array_equal(d.Q, g.Q)
+
+
+@pytest.mark.parametrize("case", ["Cylinder", "CylinderDucros", "CylinderChandrasekarRoe", "CylinderDifferentOrders"])
+def test_cylinder_family_reaches_the_reference_goldens(case, tmp_path):
+    """The NavierStokes Cylinder cases on the GPU (FP64) through the reference-shaped driver: no-slip,
+    free-slip, inflow and outflow boundaries together; standard and split forms; per-element
+    anisotropic orders (variable-order kernels). The five residuals after 100 CFL steps equal the
+    goldens within each case's tolerance on value + 1."""
+    cfg = cases.cylinder_case_config(case)
+    mesh = cases.cylinder_case_mesh(case, cfg, tmp_path)
+    g = NavierStokesDG(mesh, cfg)
+    g.set_state(cases.free_stream_state(cfg, mesh))
+    rep = g.integrate_in_time(t0=0.0)
+    assert rep.iterations == cfg.n_steps
+    gold, tol = cases.CYLINDER_GOLDENS[case]
+    assert cases.ftassert_close(gold, rep.residuals, tol), rep.residuals - gold

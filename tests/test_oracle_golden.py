@@ -146,6 +146,46 @@ def test_conserving_cylinder_goldens(test, tmp_path):
     assert cases.ftassert_close(g[2], res[2], 1e-10), res - g
 
 
+CYLINDER_TESTS = Path("/root/reference/Solver/test/NavierStokes")
+
+
+@pytest.mark.parametrize("case", ["Cylinder", "CylinderDucros", "CylinderChandrasekarRoe", "CylinderDifferentOrders"])
+def test_cylinder_family_goldens(case, tmp_path):
+    """Flow past the cylinder with all four boundary kinds (no-slip cylinder, free-slip bottom/top,
+    inflow back/left/front, outflow right): standard form with Roe, split form with the Ducros and
+    Chandrasekar averages, and per-element anisotropic orders (N 2..5). The five residuals after
+    100 CFL steps from the free stream are the goldens. Where the reference is mounted, its control
+    file must give the same configuration."""
+    cfg = cases.cylinder_case_config(case)
+    control = CYLINDER_TESTS / case / f"{case}.control"
+    if control.exists():
+        from horses3d_gb300.control import read_control
+
+        rc = read_control(control)
+        for k in ("nodes", "mach", "reynolds", "prandtl", "riemann", "inviscid", "averaging", "lambda_stab", "cfl",
+                  "dcfl", "n_steps", "aoa_theta", "aoa_phi", "periodic", "flow", "gradient_variables", "source"):
+            assert getattr(rc, k) == getattr(cfg, k), k
+        assert (rc.order_file is None) == (cfg.order_file is None)
+        if cfg.order_file is None:
+            assert rc.order == cfg.order
+        else:
+            assert Path(rc.order_file).name == Path(cfg.order_file).name
+        assert {z: b["type"] for z, b in rc.boundaries.items()} == {z: b["type"] for z, b in cfg.boundaries.items()}
+    mesh = cases.cylinder_case_mesh(case, cfg, tmp_path)
+    assert set(mesh.zone_names) == set(cfg.boundaries)
+    o = oracle.Oracle(mesh, cfg.physics(), cfg.options(), cfg.boundary_table(mesh.zone_names))
+    o.set_state(cases.free_stream_state(cfg, mesh))
+    t = 0.0
+    for _ in range(cfg.n_steps):
+        dt = o.max_dt(cfg.cfl, cfg.dcfl)
+        o.rk3_step(t, dt)
+        t += dt
+    res, nan = o.residuals()
+    gold, tol = cases.CYLINDER_GOLDENS[case]
+    assert not nan
+    assert cases.ftassert_close(gold, res, tol), res - gold
+
+
 UNIFORM_FLOW = Path("/root/reference/Solver/test/Euler/UniformFlow")
 
 
