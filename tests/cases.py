@@ -222,6 +222,42 @@ def cylinder_case_mesh(case, cfg, tmp_dir):
     return HexMesh.from_specmesh(path, orders, node_type=cfg.nodes, periodic=cfg.periodic_spec())
 
 
+# Euler BoxAroundCircle and BoxAroundCirclePirozzoli (Solver/test/Euler/<case>/SETUP/ProblemFile.f90):
+# the five residuals after 1000 CFL steps from the free stream, FTAssertEqual on value + 1, tol 1e-11.
+BOX_AROUND_CIRCLE_GOLDENS = {
+    # BoxAroundCircle/SETUP/ProblemFile.f90:349-353,363-391
+    "BoxAroundCircle": np.array([3.9167069726447580e-03, 7.0027671589173224e-02, 3.6068228611380296e-13,
+                                 8.2231956082004870e-02, 0.10659815868258372]),
+    # BoxAroundCirclePirozzoli/SETUP/ProblemFile.f90:323-327,337-365
+    "BoxAroundCirclePirozzoli": np.array([3.2245412233756249e-03, 7.2948338786761158e-02, 7.8482433396760149e-12,
+                                          6.3956090995916370e-02, 9.8435366345196243e-02]),
+}
+
+
+def box_around_circle_config(case):
+    """<case>.control: Euler, N=3, standard Roe, CFL 0.7, M=0.3, AoA 0, 1000 steps; free-slip walls
+    on the cylinder, bottom and top, inflow on front, back, left and right. The Pirozzoli case runs
+    the split form (Gauss-Lobatto) with the Pirozzoli average."""
+    split = case == "BoxAroundCirclePirozzoli"
+    cfg = Config(order=3, nodes=_abi.DG_NODES_GAUSS_LOBATTO if split else _abi.DG_NODES_GAUSS, flow="euler",
+                 mach=0.3, reynolds=0.0, riemann=_abi.DG_RIEMANN_STD_ROE,
+                 inviscid=_abi.DG_INVISCID_SPLIT if split else _abi.DG_INVISCID_STANDARD,
+                 averaging=_abi.DG_AVG_PIROZZOLI if split else _abi.DG_AVG_STANDARD, cfl=0.7, dcfl=0.7,
+                 n_steps=1000, aoa_theta=0.0, aoa_phi=0.0, convergence_tolerance=1e-10)
+    cfg.boundaries = {z: {"type": "freeslipwall"} for z in ("innercylinder", "bottom", "top")}
+    cfg.boundaries.update({z: {"type": "inflow"} for z in ("front", "back", "left", "right")})
+    return cfg
+
+
+def box_around_circle_mesh(cfg, tmp_dir):
+    """BoxAroundCircle3D_extended_pol3.mesh from the committed fixture (tests/golden/make_fixtures.py)."""
+    import gzip
+
+    path = __import__("pathlib").Path(tmp_dir) / "BoxAroundCircle3D_extended_pol3.mesh"
+    path.write_bytes(gzip.decompress((GOLDEN_DIR / f"{path.name}.gz").read_bytes()))
+    return HexMesh.from_specmesh(path, cfg.order, node_type=cfg.nodes, periodic=cfg.periodic_spec())
+
+
 # Euler UniformFlow (Solver/test/Euler/UniformFlow/SETUP/ProblemFile.f90:320-323): per polynomial order,
 # the iterations to a maximum residual of 1e-10 (exact) and that final residual (FTAssertEqual, 1e-3).
 UNIFORM_FLOW_GOLDENS = {3: (1821, 9.7985624521602423e-11), 4: (3090, 9.7825050715404729e-11),

@@ -238,3 +238,18 @@ def test_cylinder_family_reaches_the_reference_goldens(case, tmp_path):
     assert rep.iterations == cfg.n_steps
     gold, tol = cases.CYLINDER_GOLDENS[case]
     assert cases.ftassert_close(gold, rep.residuals, tol), rep.residuals - gold
+
+
+@pytest.mark.parametrize("case", ["BoxAroundCircle", "BoxAroundCirclePirozzoli"])
+def test_box_around_circle_reaches_the_reference_goldens(case, tmp_path):
+    """Euler BoxAroundCircle (standard form) and BoxAroundCirclePirozzoli (split form) on the GPU
+    (FP64): free-slip walls and inflow, 1000 CFL steps; the five residuals equal the goldens within
+    1e-11 on value + 1."""
+    cfg = cases.box_around_circle_config(case)
+    mesh = cases.box_around_circle_mesh(cfg, tmp_path)
+    g = NavierStokesDG(mesh, cfg)
+    g.set_state(cases.free_stream_state(cfg, mesh))
+    rep = g.integrate_in_time(t0=0.0)
+    assert rep.iterations == cfg.n_steps
+    gold = cases.BOX_AROUND_CIRCLE_GOLDENS[case]
+    assert cases.ftassert_close(gold, rep.residuals, 1e-11), rep.residuals - gold

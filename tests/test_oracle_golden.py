@@ -186,6 +186,40 @@ def test_cylinder_family_goldens(case, tmp_path):
     assert cases.ftassert_close(gold, res, tol), res - gold
 
 
+EULER_TESTS = Path("/root/reference/Solver/test/Euler")
+
+
+@pytest.mark.parametrize("case", ["BoxAroundCircle", "BoxAroundCirclePirozzoli"])
+def test_box_around_circle_goldens(case, tmp_path):
+    """Euler flow around a cylinder in a box (BoxAroundCircle3D_extended_pol3.mesh, curved N=3
+    patches): free-slip walls on the cylinder, bottom and top, inflow on the other four sides,
+    standard Roe, standard form or split form with the Pirozzoli average. The five residuals after
+    1000 CFL steps (CFL 0.7) from the free stream are the goldens (tol 1e-11 on value + 1)."""
+    cfg = cases.box_around_circle_config(case)
+    control = EULER_TESTS / case / f"{case}.control"
+    if control.exists():
+        from horses3d_gb300.control import read_control
+
+        rc = read_control(control)
+        for k in ("order", "nodes", "mach", "riemann", "inviscid", "averaging", "lambda_stab", "cfl", "dcfl", "n_steps",
+                  "aoa_theta", "aoa_phi", "periodic", "flow", "convergence_tolerance"):
+            assert getattr(rc, k) == getattr(cfg, k), k
+        assert {z: b["type"] for z, b in rc.boundaries.items()} == {z: b["type"] for z, b in cfg.boundaries.items()}
+    mesh = cases.box_around_circle_mesh(cfg, tmp_path)
+    assert set(mesh.zone_names) == set(cfg.boundaries)
+    o = oracle.Oracle(mesh, cfg.physics(), cfg.options(), cfg.boundary_table(mesh.zone_names))
+    o.set_state(cases.free_stream_state(cfg, mesh))
+    t = 0.0
+    for _ in range(cfg.n_steps):
+        dt = o.max_dt(cfg.cfl, cfg.dcfl)
+        o.rk3_step(t, dt)
+        t += dt
+    res, nan = o.residuals()
+    gold = cases.BOX_AROUND_CIRCLE_GOLDENS[case]
+    assert not nan
+    assert cases.ftassert_close(gold, res, 1e-11), res - gold
+
+
 UNIFORM_FLOW = Path("/root/reference/Solver/test/Euler/UniformFlow")
 
 
