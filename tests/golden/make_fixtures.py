@@ -11,6 +11,7 @@
   BoxAroundCircle3D_extended_pol3.mesh.gz
                           Solver/test/TestMeshes/BoxAroundCircle3D_extended_pol3.mesh (the Euler
                           BoxAroundCircle and BoxAroundCirclePirozzoli cases)
+  CubeWithSphere5.mesh.gz Solver/test/TestMeshes/CubeWithSphere5.mesh (the MeshConsistency component test)
 
 All gzip-compressed, so that the GPU tests can run those cases where the reference is absent.
 
@@ -26,7 +27,8 @@ HERE = Path(__file__).resolve().parent
 FILES = ("Solver/test/TestMeshes/CylinderNSpol3.mesh", "Solver/test/TestMeshes/Box27.mesh",
          "Solver/test/TestMeshes/CylinderNSpol3_1elem_y.mesh",
          "Solver/test/NavierStokes/CylinderDifferentOrders/MESH/OrdersN2N3N4N5_anisotropy.csv",
-         "Solver/test/TestMeshes/BoxAroundCircle3D_extended_pol3.mesh")
+         "Solver/test/TestMeshes/BoxAroundCircle3D_extended_pol3.mesh",
+         "Solver/test/TestMeshes/CubeWithSphere5.mesh")
 
 
 def main(root: str = "/root/reference") -> None:

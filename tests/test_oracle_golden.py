@@ -262,6 +262,37 @@ def test_uniform_flow_goldens(order, tmp_path):
     assert err <= 1e-10, err
 
 
+def test_mesh_consistency_cube_with_sphere(tmp_path):
+    """MeshConsistencyTests.f90:50-112 (the MeshConsistency component test) on CubeWithSphere5.mesh,
+    a 5 x 5 x 5 cube with curved inner elements around a sphere, N=5 Gauss: the quadrature of the
+    Jacobian is the volume 125, and the surface of every boundary zone is 25 (tol 1e-13, relative)."""
+    import gzip
+
+    path = tmp_path / "CubeWithSphere5.mesh"
+    path.write_bytes(gzip.decompress((cases.GOLDEN_DIR / "CubeWithSphere5.mesh.gz").read_bytes()))
+    mesh = HexMesh.from_specmesh(path, 5, node_type=_abi.DG_NODES_GAUSS, periodic="")
+    vol = float(np.sum(mesh.quadrature_weights()))
+    assert cases.ftassert_equal(125.0, vol, 1e-13), vol - 125.0
+    assert cases.ftassert_equal(125.0, mesh.volume, 1e-13), mesh.volume - 125.0
+    d = mesh.desc
+    nf = np.ctypeslib.as_array(d.face_nf, shape=(mesh.n_faces, 2))
+    fj = np.ctypeslib.as_array(d.face_jacobian, shape=(mesh.face_points,))
+    zone = np.ctypeslib.as_array(d.face_boundary, shape=(mesh.n_faces,))
+    surface = np.zeros(len(mesh.zone_names))
+    off = 0
+    for f in range(mesh.n_faces):
+        n1, n2 = int(nf[f, 0]), int(nf[f, 1])
+        npt = (n1 + 1) * (n2 + 1)
+        if zone[f] >= 0:
+            w1 = nodal_storage(_abi.DG_NODES_GAUSS, n1)[1]
+            w2 = nodal_storage(_abi.DG_NODES_GAUSS, n2)[1]
+            surface[zone[f]] += np.sum(np.outer(w2, w1).ravel() * fj[off:off + npt])
+        off += npt
+    assert off == mesh.face_points and len(mesh.zone_names) == 6
+    for z, s in zip(mesh.zone_names, surface):
+        assert cases.ftassert_equal(25.0, s, 1e-13), (z, s - 25.0)
+
+
 def test_nodal_storage_quadrature_and_derivative():
     # Solver/test/Components/NodalStorage/src/NodalStorageTests.f90:10-63 (N=8 Gauss, tol 1e-12)
     x, w, D = nodal_storage(_abi.DG_NODES_GAUSS, 8)
