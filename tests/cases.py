@@ -258,6 +258,56 @@ def box_around_circle_mesh(cfg, tmp_dir):
     return HexMesh.from_specmesh(path, cfg.order, node_type=cfg.nodes, periodic=cfg.periodic_spec())
 
 
+# NavierStokes TaylorGreen (Solver/test/NavierStokes/TaylorGreen/SETUP/ProblemFile.f90:317-366): after 5
+# CFL steps the five residuals (tol 1e-7 on value + 1) and the volume monitors kinetic energy, its
+# rate (on value + 1) and enstrophy (tol 1e-11).
+TAYLOR_GREEN_GOLDENS = {
+    "residuals": np.array([1.6417830052388520e-05, 1.2677577061211545e-01, 1.2677577048633804e-01,
+                           2.4981129585617484e-01, 6.2174425106488129e-01]),
+    "kinetic_energy": 1.2499879367819486e-01,
+    "kinetic_energy_rate": -4.2807806718622574e-04,
+    "enstrophy": 3.7499683882517909e-01,
+}
+
+
+def taylor_green_reference_case(n=32):
+    """TaylorGreen.control: N=3 Gauss, Roe, BR1, CFL = dCFL = 0.4, M=0.08, Re=1600, 5 steps, periodic.
+    Its mesh, TaylorGreen32.mesh, is not in the reference tree; a generated periodic box of n^3 straight
+    elements on [0, 2 pi]^3 (the domain of the TaylorGreen8.mesh that is there) stands in for it. The
+    initial condition is the test's own (ProblemFile.f90:64-148): rho 1, the Taylor-Green velocity, and
+    p = 100 + (cos 2x cos 2z + 2 cos 2y + 2 cos 2x + cos 2y cos 2z) / 16."""
+    cfg = Config(order=3, nodes=_abi.DG_NODES_GAUSS, mach=0.08, reynolds=1600.0, riemann=_abi.DG_RIEMANN_ROE,
+                 cfl=0.4, dcfl=0.4, n_steps=5, convergence_tolerance=1e-10)
+    cfg.periodic = [("front", "back"), ("bottom", "top"), ("left", "right")]
+    mesh = HexMesh.box(n, [0, 0, 0], [TWO_PI] * 3, 3, node_type=_abi.DG_NODES_GAUSS)
+    x, y, z = mesh.x[:, 0], mesh.x[:, 1], mesh.x[:, 2]
+    u = np.sin(x) * np.cos(y) * np.cos(z)
+    v = -np.cos(x) * np.sin(y) * np.cos(z)
+    p = 100.0 + (np.cos(2 * x) * np.cos(2 * z) + 2 * np.cos(2 * y) + 2 * np.cos(2 * x) + np.cos(2 * y) * np.cos(2 * z)) / 16.0
+    q = np.stack([np.ones_like(u), u, v, np.zeros_like(u), p / 0.4 + 0.5 * (u * u + v * v)], axis=1).ravel()
+    return mesh, cfg, q
+
+
+def volume_monitors(mesh, q, qdot, ux=None, uy=None, uz=None):
+    """Kinetic energy, its rate and enstrophy per unit volume (VolumeMonitor.f90:298-310 with
+    VolumeIntegrals.f90:179-286): quadratures of 1/2 |rho V|^2 / rho, of u . d(rho V)/dt - |u|^2/2
+    d(rho)/dt, and of 1/2 |curl u|^2 with the velocity gradients of getVelocityGradients_State."""
+    w = mesh.quadrature_weights()
+    vol = np.sum(w)
+    Q = q.reshape(-1, 5)
+    D = qdot.reshape(-1, 5)
+    ke = np.sum(w * 0.5 * np.sum(Q[:, 1:4] ** 2, axis=1) / Q[:, 0]) / vol
+    vel = Q[:, 1:4] / Q[:, [0]]
+    rate = np.sum(w * (np.sum(vel * D[:, 1:4], axis=1) - 0.5 * np.sum(vel ** 2, axis=1) * D[:, 0])) / vol
+    if ux is None:
+        return ke, rate, None
+    inv = 1.0 / Q[:, 0]
+    ud = Q[:, 1:4] * (inv * inv)[:, None]
+    g = [inv[:, None] * G.reshape(-1, 5)[:, 1:4] - ud * G.reshape(-1, 5)[:, [0]] for G in (ux, uy, uz)]
+    om2 = (g[1][:, 2] - g[2][:, 1]) ** 2 + (g[2][:, 0] - g[0][:, 2]) ** 2 + (g[0][:, 1] - g[1][:, 0]) ** 2
+    return ke, rate, 0.5 * np.sum(w * om2) / vol
+
+
 # Euler UniformFlow (Solver/test/Euler/UniformFlow/SETUP/ProblemFile.f90:320-323): per polynomial order,
 # the iterations to a maximum residual of 1e-10 (exact) and that final residual (FTAssertEqual, 1e-3).
 UNIFORM_FLOW_GOLDENS = {3: (1821, 9.7985624521602423e-11), 4: (3090, 9.7825050715404729e-11),
