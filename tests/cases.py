@@ -260,32 +260,64 @@ def box_around_circle_mesh(cfg, tmp_dir):
 
 # NavierStokes TaylorGreen (Solver/test/NavierStokes/TaylorGreen/SETUP/ProblemFile.f90:317-366): after 5
 # CFL steps the five residuals (tol 1e-7 on value + 1) and the volume monitors kinetic energy, its
-# rate (on value + 1) and enstrophy (tol 1e-11).
+# rate (on value + 1) and enstrophy (tol 1e-11). Euler TaylorGreenKEPEC
+# (Solver/test/Euler/TaylorGreenKEPEC/SETUP/ProblemFile.f90:337-395): after 10 steps the residuals
+# (1e-7), kinetic energy (1e-11), its rate and the entropy rate (1e-11 on value + 1).
 TAYLOR_GREEN_GOLDENS = {
-    "residuals": np.array([1.6417830052388520e-05, 1.2677577061211545e-01, 1.2677577048633804e-01,
-                           2.4981129585617484e-01, 6.2174425106488129e-01]),
-    "kinetic_energy": 1.2499879367819486e-01,
-    "kinetic_energy_rate": -4.2807806718622574e-04,
-    "enstrophy": 3.7499683882517909e-01,
+    "TaylorGreen": {
+        "residuals": np.array([1.6417830052388520e-05, 1.2677577061211545e-01, 1.2677577048633804e-01,
+                               2.4981129585617484e-01, 6.2174425106488129e-01]),
+        "kinetic_energy": 1.2499879367819486e-01,
+        "kinetic_energy_rate": -4.2807806718622574e-04,
+        "enstrophy": 3.7499683882517909e-01,
+    },
+    "TaylorGreenKEPEC": {
+        "residuals": np.array([1.1131779208842484e-04, 0.12741606758485369, 0.12741606776695064,
+                               0.24998271835184718, 0.62461894702221510]),
+        "kinetic_energy": 0.12500000000766839,
+        "kinetic_energy_rate": 2.3284871259485850e-06,
+        "entropy_rate": 2.346803715467861e-08,
+    },
 }
 
 
-def taylor_green_reference_case(n=32):
+def taylor_green_reference_case(test="TaylorGreen", n=32):
     """TaylorGreen.control: N=3 Gauss, Roe, BR1, CFL = dCFL = 0.4, M=0.08, Re=1600, 5 steps, periodic.
-    Its mesh, TaylorGreen32.mesh, is not in the reference tree; a generated periodic box of n^3 straight
-    elements on [0, 2 pi]^3 (the domain of the TaylorGreen8.mesh that is there) stands in for it. The
-    initial condition is the test's own (ProblemFile.f90:64-148): rho 1, the Taylor-Green velocity, and
+    TaylorGreenKEPEC.control: Euler, split form with the Chandrasekar average (Gauss-Lobatto), central
+    flux, N=3, CFL 0.4, M=0.08, 10 steps. Their mesh, TaylorGreen32.mesh, is not in the reference tree;
+    a generated periodic box of n^3 straight elements on [0, 2 pi]^3 (the domain of the
+    TaylorGreen8.mesh that is there) stands in for it. The initial condition is the tests' own
+    (TaylorGreen ProblemFile.f90:64-148): rho 1, the Taylor-Green velocity, and
     p = 100 + (cos 2x cos 2z + 2 cos 2y + 2 cos 2x + cos 2y cos 2z) / 16."""
-    cfg = Config(order=3, nodes=_abi.DG_NODES_GAUSS, mach=0.08, reynolds=1600.0, riemann=_abi.DG_RIEMANN_ROE,
-                 cfl=0.4, dcfl=0.4, n_steps=5, convergence_tolerance=1e-10)
+    if test == "TaylorGreen":
+        cfg = Config(order=3, nodes=_abi.DG_NODES_GAUSS, mach=0.08, reynolds=1600.0, riemann=_abi.DG_RIEMANN_ROE,
+                     cfl=0.4, dcfl=0.4, n_steps=5, convergence_tolerance=1e-10)
+    else:
+        cfg = Config(order=3, nodes=_abi.DG_NODES_GAUSS_LOBATTO, flow="euler", mach=0.08, reynolds=0.0,
+                     riemann=_abi.DG_RIEMANN_CENTRAL, inviscid=_abi.DG_INVISCID_SPLIT,
+                     averaging=_abi.DG_AVG_CHANDRASEKAR, cfl=0.4, dcfl=0.4, n_steps=10, convergence_tolerance=1e-10)
     cfg.periodic = [("front", "back"), ("bottom", "top"), ("left", "right")]
-    mesh = HexMesh.box(n, [0, 0, 0], [TWO_PI] * 3, 3, node_type=_abi.DG_NODES_GAUSS)
+    mesh = HexMesh.box(n, [0, 0, 0], [TWO_PI] * 3, 3, node_type=cfg.nodes)
     x, y, z = mesh.x[:, 0], mesh.x[:, 1], mesh.x[:, 2]
     u = np.sin(x) * np.cos(y) * np.cos(z)
     v = -np.cos(x) * np.sin(y) * np.cos(z)
     p = 100.0 + (np.cos(2 * x) * np.cos(2 * z) + 2 * np.cos(2 * y) + 2 * np.cos(2 * x) + np.cos(2 * y) * np.cos(2 * z)) / 16.0
     q = np.stack([np.ones_like(u), u, v, np.zeros_like(u), p / 0.4 + 0.5 * (u * u + v * v)], axis=1).ravel()
     return mesh, cfg, q
+
+
+def entropy_rate(mesh, q, qdot):
+    """The entropy-rate volume monitor (VolumeIntegrals.f90:322-331 over the volume): the quadrature of
+    QDot . U with U the entropy variables of NSGradientVariables_ENTROPY."""
+    Q = q.reshape(-1, 5)
+    D = qdot.reshape(-1, 5)
+    rho = Q[:, 0]
+    rv2 = np.sum(Q[:, 1:4] ** 2, axis=1) / rho
+    p = 0.4 * (Q[:, 4] - 0.5 * rv2)
+    U = np.stack([(1.4 - (np.log(p) - 1.4 * np.log(rho))) / 0.4 - 0.5 * rv2 / p, Q[:, 1] / p, Q[:, 2] / p,
+                  Q[:, 3] / p, -rho / p], axis=1)
+    w = mesh.quadrature_weights()
+    return np.sum(w * np.sum(D * U, axis=1)) / np.sum(w)
 
 
 def volume_monitors(mesh, q, qdot, ux=None, uy=None, uz=None):

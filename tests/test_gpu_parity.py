@@ -384,19 +384,24 @@ def test_integrate_on_device_reports_the_first_nan_step():
         g.integrate_on_device(3, 0.0, dt=1e-3)
 
 
-def test_taylor_green_reaches_the_reference_goldens():
-    """NavierStokes TaylorGreen on the GPU (FP64, 32^3 elements, N=3): after 5 CFL steps through the
-    reference-shaped driver the five residuals (tol 1e-7 on value + 1), the kinetic energy (1e-11)
-    and its rate (1e-11 on value + 1) equal the goldens (ProblemFile.f90:317-366). The enstrophy
-    golden reads the gradients of the last stage, which the step kernels do not store; the oracle
-    test pins it."""
-    mesh, cfg, q0 = cases.taylor_green_reference_case()
+@pytest.mark.parametrize("test", ["TaylorGreen", "TaylorGreenKEPEC"])
+def test_taylor_green_reaches_the_reference_goldens(test):
+    """NavierStokes TaylorGreen and Euler TaylorGreenKEPEC on the GPU (FP64, 32^3 elements, N=3):
+    through the reference-shaped driver the five residuals (tol 1e-7 on value + 1), the kinetic
+    energy (1e-11), its rate and, for the Euler case, the entropy rate (1e-11 on value + 1) equal the
+    goldens. The enstrophy golden reads the gradients of the last stage, which the step kernels do
+    not store; the oracle test pins it."""
+    mesh, cfg, q0 = cases.taylor_green_reference_case(test)
     g = NavierStokesDG(mesh, cfg)
     g.set_state(q0)
     rep = g.integrate_in_time(t0=0.0)
-    gold = cases.TAYLOR_GREEN_GOLDENS
-    assert rep.iterations == 5
+    gold = cases.TAYLOR_GREEN_GOLDENS[test]
+    assert rep.iterations == cfg.n_steps
     assert cases.ftassert_close(gold["residuals"], rep.residuals, 1e-7), rep.residuals - gold["residuals"]
-    ke, rate, _ = cases.volume_monitors(mesh, g.Q, g.QDot)
+    q, qdot = g.Q, g.QDot
+    ke, rate, _ = cases.volume_monitors(mesh, q, qdot)
     assert cases.ftassert_equal(gold["kinetic_energy"], ke, 1e-11), ke - gold["kinetic_energy"]
     assert cases.ftassert_close(gold["kinetic_energy_rate"], rate, 1e-11), rate - gold["kinetic_energy_rate"]
+    if "entropy_rate" in gold:
+        er = cases.entropy_rate(mesh, q, qdot)
+        assert cases.ftassert_close(gold["entropy_rate"], er, 1e-11), er - gold["entropy_rate"]

@@ -293,13 +293,15 @@ def test_mesh_consistency_cube_with_sphere(tmp_path):
         assert cases.ftassert_equal(25.0, s, 1e-13), (z, s - 25.0)
 
 
-def test_taylor_green_goldens():
-    """NavierStokes TaylorGreen: N=3 Gauss, Roe, BR1, M=0.08, Re=1600, 5 CFL steps on a 32^3 periodic
-    box (a generated [0, 2 pi]^3 box in place of TaylorGreen32.mesh, which is not in the reference
-    tree). Goldens: the five residuals (tol 1e-7 on value + 1), kinetic energy and enstrophy (1e-11)
-    and the kinetic-energy rate (1e-11 on value + 1), the monitors read with the final Q and the QDot
-    and gradients of the last right-hand side (ProblemFile.f90:317-366)."""
-    mesh, cfg, q0 = cases.taylor_green_reference_case()
+@pytest.mark.parametrize("test", ["TaylorGreen", "TaylorGreenKEPEC"])
+def test_taylor_green_goldens(test):
+    """NavierStokes TaylorGreen (N=3 Gauss, Roe, BR1, M=0.08, Re=1600, 5 CFL steps) and Euler
+    TaylorGreenKEPEC (split form, Chandrasekar, central flux, 10 steps) on a 32^3 periodic box (a
+    generated [0, 2 pi]^3 box in place of TaylorGreen32.mesh, which is not in the reference tree).
+    Goldens: the five residuals (tol 1e-7 on value + 1), kinetic energy (1e-11), its rate (1e-11 on
+    value + 1), and enstrophy (NS, 1e-11) or the entropy rate (Euler, 1e-11 on value + 1), the
+    monitors read with the final Q and the QDot and gradients of the last right-hand side."""
+    mesh, cfg, q0 = cases.taylor_green_reference_case(test)
     o = oracle.Oracle(mesh, cfg.physics(), cfg.options())
     o.set_state(q0)
     t = 0.0
@@ -308,14 +310,20 @@ def test_taylor_green_goldens():
         o.rk3_step(t, dt)
         t += dt
     res, nan = o.residuals()
-    g = cases.TAYLOR_GREEN_GOLDENS
+    g = cases.TAYLOR_GREEN_GOLDENS[test]
     assert not nan
     assert cases.ftassert_close(g["residuals"], res, 1e-7), res - g["residuals"]
-    ke, rate, ens = cases.volume_monitors(mesh, o.get(_abi.DG_FIELD_Q), o.get(_abi.DG_FIELD_QDOT),
-                                          o.get(_abi.DG_FIELD_UX), o.get(_abi.DG_FIELD_UY), o.get(_abi.DG_FIELD_UZ))
+    q, qdot = o.get(_abi.DG_FIELD_Q), o.get(_abi.DG_FIELD_QDOT)
+    if cfg.flow == "ns":
+        ke, rate, ens = cases.volume_monitors(mesh, q, qdot, o.get(_abi.DG_FIELD_UX), o.get(_abi.DG_FIELD_UY),
+                                              o.get(_abi.DG_FIELD_UZ))
+        assert cases.ftassert_equal(g["enstrophy"], ens, 1e-11), ens - g["enstrophy"]
+    else:
+        ke, rate, _ = cases.volume_monitors(mesh, q, qdot)
+        er = cases.entropy_rate(mesh, q, qdot)
+        assert cases.ftassert_close(g["entropy_rate"], er, 1e-11), er - g["entropy_rate"]
     assert cases.ftassert_equal(g["kinetic_energy"], ke, 1e-11), ke - g["kinetic_energy"]
     assert cases.ftassert_close(g["kinetic_energy_rate"], rate, 1e-11), rate - g["kinetic_energy_rate"]
-    assert cases.ftassert_equal(g["enstrophy"], ens, 1e-11), ens - g["enstrophy"]
 
 
 def test_nodal_storage_quadrature_and_derivative():
