@@ -237,3 +237,25 @@ AOA phi = 90.0
     assert out.type == _abi.DG_BC_OUTFLOW and abs(out.pressure - 50000.0 / ref["p"]) < 1e-12
     with pytest.raises(ValueError):
         c.boundary("nowhere")
+
+
+def test_control_zone_lists_and_steady_state_tolerance():
+    """A "#define boundary" line names its zones joined by "__" (GenericBoundaryConditionClass.f90:
+    400-456); "convergence tolerance" is a Fortran real (1.d-10) that stops a steady-state run."""
+    text = """Flow equations = "Euler"
+mach number = 0.5
+Convergence tolerance = 1.d-10
+Number of time steps = 5000
+#define boundary left__right__front__back__bottom__top
+   type = Inflow
+#end
+"""
+    cfg = parse_control(text)
+    assert cfg.convergence_tolerance == 1e-10 and cfg.n_steps == 5000 and cfg.flow == "euler"
+    assert set(cfg.boundaries) == {"left", "right", "front", "back", "bottom", "top"}
+    assert all(b["type"] == "inflow" for b in cfg.boundaries.values())
+    two = parse_control("reynolds number = 1\n#define boundary InnerCylinder\n type = NoSlipWall\n#end\n"
+                        "#define boundary Bottom__Top\n type = FreeSlipWall\n#end\n")
+    assert {z: b["type"] for z, b in two.boundaries.items()} == {
+        "innercylinder": "noslipwall", "bottom": "freeslipwall", "top": "freeslipwall"}
+    assert two.convergence_tolerance is None
