@@ -104,7 +104,9 @@ __global__ void k_dt_fold(double* partials, int nblocks) {
 }
 
 // Device address of g_partials, looked up once per device (cudaGetSymbolAddress with the device
-// current); host code must never pass the symbol itself to a kernel.
+// current); host code must never pass the symbol itself to a kernel. The cached address belongs to
+// the device's context at the time of the lookup: after cudaDeviceReset it is stale, so a process
+// that resets a device must not call dg_max_dt_noalloc on it again.
 constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
 double* g_partials_addr[kMaxDevices] = {};
@@ -144,6 +146,20 @@ int dg_max_dt_noalloc(const double* q, const double* ja_xi, const double* ja_eta
     if (node_type != DG_NODES_GAUSS && node_type != DG_NODES_GAUSS_LOBATTO)
         return h3d::fail(DG_ERR_INVALID, "unknown node type");
     if (!(phys->mach > 0.0)) return h3d::fail(DG_ERR_INVALID, "Mach number must be positive");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // An error left by the caller's own earlier work is reported as such, not as a failure here.
+    cudaError_t e = cudaPeekAtLastError();
+    if (e != cudaSuccess)
+        return h3d::fail(DG_ERR_CUDA, std::string("dg_max_dt_noalloc: a CUDA error was pending before the call: ") +
+                                          cudaGetErrorString(e));
+    // The call synchronises the stream and copies dt to host memory, neither of which a stream
+    // capture allows.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(s, &cap);
+    if (e != cudaSuccess)
+        return h3d::fail(DG_ERR_CUDA, std::string("dg_max_dt_noalloc: cudaStreamIsCapturing: ") + cudaGetErrorString(e));
+    if (cap != cudaStreamCaptureStatusNone)
+        return h3d::fail(DG_ERR_UNSUPPORTED, "dg_max_dt_noalloc cannot be called while its stream is being captured");
     double* partials = nullptr;
     int rc = partials_address(&partials);
     if (rc) return rc;
@@ -164,10 +180,12 @@ int dg_max_dt_noalloc(const double* q, const double* ja_xi, const double* ja_eta
     d.S_div_TRef = (198.6 * 5.0 / 9.0) / TRef;
     d.TReNorm = TRef / TRef;
     const int nblocks = static_cast<int>((ndof + kNodesPerBlock - 1) / kNodesPerBlock);
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     k_dt_partials<<<nblocks, kThreads, 0, s>>>(d, q, ja_xi, ja_eta, ja_zeta, jacobian, partials);
-    k_dt_fold<<<1, kThreads, 0, s>>>(partials, nblocks);
-    cudaError_t e = cudaGetLastError();
+    e = cudaGetLastError();
+    if (e == cudaSuccess) {
+        k_dt_fold<<<1, kThreads, 0, s>>>(partials, nblocks);
+        e = cudaGetLastError();
+    }
     if (e == cudaSuccess) e = cudaMemcpyAsync(dt, partials, sizeof(double), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return h3d::fail(DG_ERR_CUDA, std::string("dg_max_dt_noalloc: ") + cudaGetErrorString(e));

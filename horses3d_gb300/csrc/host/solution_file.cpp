@@ -9,7 +9,9 @@
 //   byte 152  reference values gamma, R, V, rho, T, Mach (6 x float64)
 //   byte 200  88 (beginning of data)
 //   byte 204  per element: 4 (int32 rank), NCONS, Nx+1, Ny+1, Nz+1 (int32), Q(1:5,0:Nx,0:Ny,0:Nz)
-//             (float64, column-major); gradient files then add U_x, U_y, U_z (5 values per node each)
+//             (float64, column-major); gradient files (types 3, 10) then add U_x, U_y, U_z (5 values
+//             per node each); sensor files (types 9, 10) end the record with the element's sensor
+//             value (float64), HexMesh.f90:3522-3525, 4832
 //   end       99 (int32)
 // Little-endian, as the reference writes it on the platforms it runs on.
 #include <cstdint>
@@ -74,7 +76,13 @@ int h3d_read_solution(const char* path, int32_t n_elements, const int32_t* order
     if (h.n_elements != n_elements)
         return h3d::fail(DG_ERR_INVALID, std::string(path) + ": the file holds " + std::to_string(h.n_elements) +
                                              " elements, the mesh " + std::to_string(n_elements));
+    // The file types HexMesh_LoadSolution restarts from (HexMesh.f90:4744-4780): solution (2),
+    // solution and gradients (3), either with the per-element sensor value (9, 10).
+    if (h.file_type != 2 && h.file_type != 3 && h.file_type != 9 && h.file_type != 10)
+        return h3d::fail(DG_ERR_INVALID, std::string(path) + ": file type " + std::to_string(h.file_type) +
+                                             " is not a solution file (2, 3, 9 or 10)");
     const bool has_grad = h.file_type == 3 || h.file_type == 10;
+    const bool has_sensor = h.file_type == 9 || h.file_type == 10;
     if (gradients && !has_grad) return h3d::fail(DG_ERR_INVALID, std::string(path) + ": the file holds no gradients");
     const int padding = has_grad ? 20 : 5;  // values per node: Q (5) [+ U_x, U_y, U_z (5 each)]
     File fl;
@@ -97,7 +105,7 @@ int h3d_read_solution(const char* path, int32_t n_elements, const int32_t* order
                 if (std::fread(gradients + 15 * off + 5 * np * d, sizeof(double), 5 * np, fl.f) != 5 * np)
                     return h3d::fail(DG_ERR_IO, std::string(path) + ": truncated gradient data");
         }
-        pos += 20 + static_cast<long>(padding) * static_cast<long>(np) * 8;
+        pos += 20 + static_cast<long>(padding) * static_cast<long>(np) * 8 + (has_sensor ? 8 : 0);
         off += static_cast<int64_t>(np);
     }
     return DG_OK;

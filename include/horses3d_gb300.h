@@ -194,10 +194,13 @@ int dg_max_dt(dg_ctx* ctx, double cfl, double dcfl, double* dt);
  * q (5*ndof), ja_xi/ja_eta/ja_zeta (3*ndof), jacobian (ndof), for uniform order `order`. The only
  * scratch is a fixed 128 KiB file-scope device array that every GPU loading the library keeps until
  * exit; it bounds ndof to dg_max_dt_noalloc_max_dof() (67,108,864) and larger sizes are rejected
- * with DG_ERR_INVALID. The first call on a device looks up that array's address (make it before any
- * stream capture). Every call reuses the array, so calls that overlap on the GPU (other streams or
- * threads) race; each call overwrites the entries it reads. stream may be NULL (default stream);
- * the call synchronises it and writes dt to host memory. */
+ * with DG_ERR_INVALID. The first call on a device looks up that array's address in the device's
+ * current context and keeps it; after a cudaDeviceReset of that device the kept address is stale, so
+ * do not call this function on a device that the process has reset. Every call reuses the array, so
+ * calls that overlap on the GPU (other streams or threads) race; each call overwrites the entries it
+ * reads. stream may be NULL (default stream); the call synchronises it and writes dt to host memory,
+ * so it cannot run while the stream is being captured into a CUDA graph (DG_ERR_UNSUPPORTED). A
+ * CUDA error already pending when the call starts is returned as DG_ERR_CUDA without launching. */
 int dg_max_dt_noalloc(const double* q, const double* ja_xi, const double* ja_eta, const double* ja_zeta,
                       const double* jacobian, int64_t ndof, int order, int node_type, const dg_physics* phys,
                       double cfl, double dcfl, void* stream, double* dt);

@@ -125,6 +125,32 @@ def lamb_vector_l2_error(mesh, q, t):
 
 GOLDEN_DIR = __import__("pathlib").Path(__file__).resolve().parent / "golden"
 
+# Root of a reference source tree, when one is mounted (read only by the fallback below).
+REFERENCE_ENV = "HORSES3D_REFERENCE"
+
+
+def reference_file(rel: str, tmp_dir=None):
+    """A file of the reference tree by its path within the project (e.g.
+    "Solver/test/TestMeshes/UnitCube4x4.mesh"): the committed gzip fixture of that name
+    (tests/golden/make_fixtures.py) decompressed into tmp_dir (a temporary directory when None), else
+    the file under the root named by $HORSES3D_REFERENCE, else None (the caller skips)."""
+    import gzip
+    import os
+    import tempfile
+    from pathlib import Path
+
+    name = Path(rel).name
+    fixture = GOLDEN_DIR / f"{name}.gz"
+    if fixture.exists():
+        out = Path(tmp_dir if tmp_dir is not None else tempfile.mkdtemp(prefix="h3d_ref_")) / name
+        if not out.exists():
+            out.write_bytes(gzip.decompress(fixture.read_bytes()))
+        return out
+    root = os.environ.get(REFERENCE_ENV)
+    if root and (Path(root) / rel).exists():
+        return Path(root) / rel
+    return None
+
 # Solver/test/NavierStokes/{Energy,Entropy}ConservingTest/SETUP/ProblemFile.f90:555-561 (tol 1e-11 on
 # x+1, 1e-10 for the y-momentum)
 CONSERVING_GOLDENS = {

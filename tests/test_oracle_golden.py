@@ -9,8 +9,15 @@ import oracle
 from horses3d_gb300 import _abi
 from horses3d_gb300.mesh import HexMesh, nodal_storage
 
-REF_MESH = Path("/root/reference/Solver/test/TestMeshes/UnitCube4x4.mesh")
-TGV8_MESH = Path("/root/reference/Solver/test/TestMeshes/TaylorGreen8.mesh")
+REF_MESH = "Solver/test/TestMeshes/UnitCube4x4.mesh"
+TGV8_MESH = "Solver/test/TestMeshes/TaylorGreen8.mesh"
+
+
+def _reference_or_skip(rel, tmp_path):
+    path = cases.reference_file(rel, tmp_path)
+    if path is None:
+        pytest.skip(f"{rel}: no fixture and no reference tree (set ${cases.REFERENCE_ENV})")
+    return path
 
 
 def _run_convergence(mesh, cfg):
@@ -57,10 +64,9 @@ def test_convergence_variant_goldens(variant):
     assert cases.ftassert_close(gqerr, qerr), qerr - gqerr
 
 
-@pytest.mark.skipif(not REF_MESH.exists(), reason="reference mesh file not mounted")
-def test_convergence_goldens_reference_mesh_file():
+def test_convergence_goldens_reference_mesh_file(tmp_path):
     _, cfg, _ = cases.convergence_case()
-    mesh = HexMesh.from_specmesh(REF_MESH, 7, node_type=_abi.DG_NODES_GAUSS,
+    mesh = HexMesh.from_specmesh(_reference_or_skip(REF_MESH, tmp_path), 7, node_type=_abi.DG_NODES_GAUSS,
                                  periodic="front:back,bottom:top,left:right")
     it, res, err, qerr, nan = _run_convergence(mesh, cfg)
     assert it == 215
@@ -100,16 +106,15 @@ def test_lamb_vector_golden_generated_mesh():
     assert cases.ftassert_equal(cases.LAMB_VECTOR_L2, err, 1e-7), err - cases.LAMB_VECTOR_L2
 
 
-@pytest.mark.skipif(not TGV8_MESH.exists(), reason="reference mesh file not mounted")
-def test_lamb_vector_golden_reference_mesh_file():
-    mesh = HexMesh.from_specmesh(TGV8_MESH, 5, node_type=_abi.DG_NODES_GAUSS,
+def test_lamb_vector_golden_reference_mesh_file(tmp_path):
+    mesh = HexMesh.from_specmesh(_reference_or_skip(TGV8_MESH, tmp_path), 5, node_type=_abi.DG_NODES_GAUSS,
                                  periodic="front:back,bottom:top,left:right")
     it, t, err = _lamb_vector_on_oracle(mesh)
     assert it == 21
     assert cases.ftassert_equal(cases.LAMB_VECTOR_L2, err, 1e-7), err - cases.LAMB_VECTOR_L2
 
 
-CONSERVING_TESTS = Path("/root/reference/Solver/test/NavierStokes")
+CONSERVING_TESTS = "Solver/test/NavierStokes"
 
 
 @pytest.mark.parametrize("test", ["EnergyConservingTest", "EntropyConservingTest"])
@@ -117,11 +122,11 @@ def test_conserving_cylinder_goldens(test, tmp_path):
     """Flow past a cylinder (CylinderNSpol3.mesh, curved N=3 boundary patches) with no-slip walls on
     the cylinder and the side walls, periodic elsewhere: split form (Pirozzoli / Chandrasekar),
     central fluxes, energy / entropy gradient variables, N=5, 10 CFL steps from the free stream.
-    The five residuals are the goldens. Where the reference is mounted, its own control file must
+    The five residuals are the goldens. The reference's own control file (committed fixture) must
     give the same configuration."""
     cfg = cases.conserving_cylinder_config(test)
-    control = CONSERVING_TESTS / test / f"{test}.control"
-    if control.exists():
+    control = cases.reference_file(f"{CONSERVING_TESTS}/{test}/{test}.control", tmp_path)
+    if control is not None:
         from horses3d_gb300.control import read_control
 
         rc = read_control(control)
@@ -146,7 +151,7 @@ def test_conserving_cylinder_goldens(test, tmp_path):
     assert cases.ftassert_close(g[2], res[2], 1e-10), res - g
 
 
-CYLINDER_TESTS = Path("/root/reference/Solver/test/NavierStokes")
+CYLINDER_TESTS = "Solver/test/NavierStokes"
 
 
 @pytest.mark.parametrize("case", ["Cylinder", "CylinderDucros", "CylinderChandrasekarRoe", "CylinderDifferentOrders"])
@@ -154,11 +159,11 @@ def test_cylinder_family_goldens(case, tmp_path):
     """Flow past the cylinder with all four boundary kinds (no-slip cylinder, free-slip bottom/top,
     inflow back/left/front, outflow right): standard form with Roe, split form with the Ducros and
     Chandrasekar averages, and per-element anisotropic orders (N 2..5). The five residuals after
-    100 CFL steps from the free stream are the goldens. Where the reference is mounted, its control
-    file must give the same configuration."""
+    100 CFL steps from the free stream are the goldens. The reference's control file (committed
+    fixture) must give the same configuration."""
     cfg = cases.cylinder_case_config(case)
-    control = CYLINDER_TESTS / case / f"{case}.control"
-    if control.exists():
+    control = cases.reference_file(f"{CYLINDER_TESTS}/{case}/{case}.control", tmp_path)
+    if control is not None:
         from horses3d_gb300.control import read_control
 
         rc = read_control(control)
@@ -186,7 +191,7 @@ def test_cylinder_family_goldens(case, tmp_path):
     assert cases.ftassert_close(gold, res, tol), res - gold
 
 
-EULER_TESTS = Path("/root/reference/Solver/test/Euler")
+EULER_TESTS = "Solver/test/Euler"
 
 
 @pytest.mark.parametrize("case", ["BoxAroundCircle", "BoxAroundCirclePirozzoli"])
@@ -196,8 +201,8 @@ def test_box_around_circle_goldens(case, tmp_path):
     standard Roe, standard form or split form with the Pirozzoli average. The five residuals after
     1000 CFL steps (CFL 0.7) from the free stream are the goldens (tol 1e-11 on value + 1)."""
     cfg = cases.box_around_circle_config(case)
-    control = EULER_TESTS / case / f"{case}.control"
-    if control.exists():
+    control = cases.reference_file(f"{EULER_TESTS}/{case}/{case}.control", tmp_path)
+    if control is not None:
         from horses3d_gb300.control import read_control
 
         rc = read_control(control)
@@ -220,7 +225,7 @@ def test_box_around_circle_goldens(case, tmp_path):
     assert cases.ftassert_close(gold, res, 1e-11), res - gold
 
 
-UNIFORM_FLOW = Path("/root/reference/Solver/test/Euler/UniformFlow")
+UNIFORM_FLOW = "Solver/test/Euler/UniformFlow"
 
 
 @pytest.mark.parametrize("order", [3, 4, 5])
@@ -229,11 +234,11 @@ def test_uniform_flow_goldens(order, tmp_path):
     from the free stream with a 5 % density bump in every element, marched until the maximum
     residual reaches 1e-10 (TimeIntegrator.f90:737-890, steady state). Goldens: the iteration count
     (exact) and the final residual per order (FTAssertEqual, tol 1e-3), and the final state equal to
-    the free stream within 1e-10 (ProblemFile.f90:320-372). Where the reference is mounted, its
-    control file must give the same configuration."""
+    the free stream within 1e-10 (ProblemFile.f90:320-372). The reference's
+    control file (committed fixture) must give the same configuration."""
     cfg = cases.uniform_flow_config(order)
-    control = UNIFORM_FLOW / "UniformFlow.control"
-    if control.exists():
+    control = cases.reference_file(f"{UNIFORM_FLOW}/UniformFlow.control", tmp_path)
+    if control is not None:
         from horses3d_gb300.control import read_control
 
         rc = read_control(control)

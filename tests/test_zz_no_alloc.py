@@ -23,7 +23,8 @@ def _device(arr, torch):
     return torch.from_numpy(np.ascontiguousarray(arr, dtype=np.float64)).cuda()
 
 
-def _noalloc_dt(mesh, cfg, q, torch, cfl, dcfl):
+def _noalloc_dt(mesh, cfg, q, torch, cfl, dcfl, stream=None):
+    """stream: a torch.cuda.Stream to run on (None: the default stream)."""
     t = {name: _device(a, torch) for name, a in (
         ("q", q), ("xi", np.ctypeslib.as_array(mesh.desc.ja_xi, shape=(3 * mesh.ndof,))),
         ("eta", np.ctypeslib.as_array(mesh.desc.ja_eta, shape=(3 * mesh.ndof,))),
@@ -33,7 +34,8 @@ def _noalloc_dt(mesh, cfg, q, torch, cfl, dcfl):
     dt = C.c_double()
     rc = _abi.lib().dg_max_dt_noalloc(t["q"].data_ptr(), t["xi"].data_ptr(), t["eta"].data_ptr(),
                                       t["zeta"].data_ptr(), t["jac"].data_ptr(), mesh.ndof, cfg.order, cfg.nodes,
-                                      C.byref(cfg.physics()), cfl, dcfl, None, C.byref(dt))
+                                      C.byref(cfg.physics()), cfl, dcfl,
+                                      None if stream is None else stream.cuda_stream, C.byref(dt))
     _abi.check(rc, "dg_max_dt_noalloc")
     return dt.value
 
@@ -49,6 +51,20 @@ def test_noalloc_max_dt_matches_the_allocating_entry_point():
             g.set_state(q)
             ref = g.max_time_step(cfl, dcfl)
         got = _noalloc_dt(mesh, cfg, q, torch, cfl, dcfl)
+        assert abs(got - ref) <= TOL * ref, (got, ref)
+
+
+def test_noalloc_max_dt_euler_case_on_a_side_stream():
+    """The Euler path (no viscous limit) on a stream other than the default one, twice in a row."""
+    torch = pytest.importorskip("torch")
+    mesh, cfg, q = cases.vortex_case(n=5, order=4, nodes=_abi.DG_NODES_GAUSS)
+    assert cfg.physics().navier_stokes == 0
+    with NavierStokesDG(mesh, cfg) as g:
+        g.set_state(q)
+        ref = g.max_time_step(0.4, 0.4)
+    side = torch.cuda.Stream()
+    for _ in range(2):
+        got = _noalloc_dt(mesh, cfg, q, torch, 0.4, 0.4, stream=side)
         assert abs(got - ref) <= TOL * ref, (got, ref)
 
 
