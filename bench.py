@@ -18,7 +18,8 @@ cpu_baseline: the CPU FP64 oracle (port of the reference loops) on the host core
 
 --impl reference times the reference's CPU implementation of this path. The Fortran reference does
 not build on this image (no Fortran compiler), so the reference arm runs the oracle port with all
-host threads on a bounded sample of the same workload.
+host threads: W untimed and K timed RK3 steps of the same workload, on a mesh and geometry the
+oracle builds itself (oracle/geometry.cpp), so that arm loads no product library.
 """
 from __future__ import annotations
 
@@ -138,6 +139,12 @@ def build_case(n_elem: int = N_ELEM):
 # DRAM bytes per DOF of one k_volume<6, gauss, float> launch, measured with ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum = 444.8 MB over 2,985,984 DOF, 24^3 elements, N=5).
 VOLUME_DRAM_BYTES_PER_DOF = 149.0
+# The unit that binds k_volume<6, gauss, float> in the same ncu capture: the L1/shared-memory pipe
+# (l1tex__throughput.avg.pct_of_peak_sustained_elapsed), ahead of DRAM.
+VOLUME_L1TEX_FRAC = 0.80
+# Executed FP64 floating-point operations per DOF and RK stage of the plain form (ncu SASS counts
+# dadd + dmul + 2 dfma over one stage's kernels, per DOF); None until measured.
+FP64_FLOP_PER_DOF_STAGE = None
 
 
 def volume_bytes(P: int, word: int) -> float:
@@ -186,7 +193,8 @@ def run_gpu_arm(args, rank, world, local, case):
     value = world * dof_stage_per_step * args.steps / (ms_mixed * 1e-3)
     plain = world * dof_stage_per_step * args.steps / (ms_plain * 1e-3)
     # accuracy of the mixed form against the FP64 form after the same steps
-    acc = rel_l2(gm.Q, gp.Q)
+    q_mixed, q_fp64 = gm.Q.copy(), gp.Q.copy()  # after warm-up + timed steps (the kernel timing below moves Q)
+    acc = rel_l2(q_mixed, q_fp64)
 
     # per-kernel launch times of the mixed form (dominant kernel for the roofline)
     kt = np.zeros(5)
@@ -203,7 +211,19 @@ def run_gpu_arm(args, rank, world, local, case):
                 "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / hbm, 4),
                 "traffic": traffic, "alg_bytes_per_launch": alg,
                 "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_volume launch on the "
-                                "24^3-element case (149.0 B/DOF), scaled by the DOF count"}
+                                "24^3-element case (149.0 B/DOF), scaled by the DOF count",
+                "limiter": {"unit": "l1tex (shared-memory operand loads)", "throughput_frac": VOLUME_L1TEX_FRAC,
+                            "source": "ncu l1tex__throughput.avg.pct_of_peak_sustained_elapsed, same capture"}}
+
+    # the plain form's compute roofline: FP64 pipe (measured FMA rate of this GPU)
+    fp64_peak = C.c_double()
+    _abi.check(L.dg_measure_fp64_peak(C.byref(fp64_peak)), "dg_measure_fp64_peak")
+    plain_roof = {"bound": "fp64", "peak_tflops": round(fp64_peak.value, 3), "peak_kind": "measured (FMA chains)",
+                  "hbm_frac": round(plain * 1016.0 / 1e9 / hbm, 4), "hbm_bytes_per_dof_stage": 1016.0}
+    if FP64_FLOP_PER_DOF_STAGE:
+        ach = plain * FP64_FLOP_PER_DOF_STAGE / 1e12
+        plain_roof.update({"achieved_tflops": round(ach, 3), "fp64_frac": round(ach / fp64_peak.value, 4),
+                           "fp64_flop_per_dof_stage": FP64_FLOP_PER_DOF_STAGE})
 
     # e2e through the C ABI with host buffers (IntegrateInTime-shaped loop)
     import torch
@@ -211,7 +231,6 @@ def run_gpu_arm(args, rank, world, local, case):
     pinned = torch.empty(q0.size, dtype=torch.float64).pin_memory()
     pinned.numpy()[:] = q0
     out = torch.empty(q0.size, dtype=torch.float64).pin_memory()
-    ge = NavierStokesDG(mesh, Config(**base, precision=DG_PRECISION_MIXED))
     qp = C.cast(pinned.data_ptr(), C.POINTER(C.c_double))
     op = C.cast(out.data_ptr(), C.POINTER(C.c_double))
     e2e_steps = max(1, args.steps)
@@ -219,29 +238,39 @@ def run_gpu_arm(args, rank, world, local, case):
     nan = C.c_int()
     t_end = C.c_double()
 
-    def e2e_once():
-        # IntegrateInTime through the C ABI: every step MaxTimeStep (CFL) + TakeRK3Step + t += dt +
-        # ComputeMaxResiduals / checkForNan on the device (dg_integrate), one host synchronization
-        _abi.check(L.dg_upload_state(ge._h, qp), "dg_upload_state")
-        _abi.check(L.dg_integrate(ge._h, e2e_steps, 0.0, 0.0, CFL, CFL, C.byref(t_end), _abi.f64ptr(hist),
-                                  C.byref(nan)), "dg_integrate")
-        _abi.check(L.dg_download(ge._h, _abi.DG_FIELD_Q, op), "dg_download")
+    def e2e_rate(precision):
+        ge = NavierStokesDG(mesh, Config(**base, precision=precision))
 
-    e2e_once()  # warm-up
-    _barrier(world)
-    t0 = time.perf_counter()
-    e2e_once()
-    e2e_s = _allreduce_max(time.perf_counter() - t0, world)
-    e2e_value = world * dof_stage_per_step * e2e_steps / e2e_s
+        def once():
+            # IntegrateInTime through the C ABI: every step MaxTimeStep (CFL) + TakeRK3Step + t += dt +
+            # ComputeMaxResiduals / checkForNan on the device (dg_integrate), one host synchronization
+            _abi.check(L.dg_upload_state(ge._h, qp), "dg_upload_state")
+            _abi.check(L.dg_integrate(ge._h, e2e_steps, 0.0, 0.0, CFL, CFL, C.byref(t_end), _abi.f64ptr(hist),
+                                      C.byref(nan)), "dg_integrate")
+            _abi.check(L.dg_download(ge._h, _abi.DG_FIELD_Q, op), "dg_download")
+
+        once()  # warm-up
+        _barrier(world)
+        t0 = time.perf_counter()
+        once()
+        el = _allreduce_max(time.perf_counter() - t0, world)
+        ge.close()
+        return world * dof_stage_per_step * e2e_steps / el
+
+    e2e_value = e2e_rate(DG_PRECISION_MIXED)
+    e2e_fp64 = e2e_rate(DG_PRECISION_FP64)
     qbytes = 8 * q0.size
     e2e = {"value": e2e_value, "unit": "DOF*stage/s", "h2d_bytes_per_step": int(qbytes / e2e_steps + 16),
            "d2h_bytes_per_step": int(qbytes / e2e_steps + 48 + 8 / e2e_steps),
            "loop": "upload Q from pinned host memory; dg_integrate (per step: CFL dt, RK3 step, residuals and "
-                   "NaN check on the device, one graph per step); download Q and the residual history"}
+                   "NaN check on the device, one graph per step); download Q and the residual history",
+           "plain_fp64": {"value": e2e_fp64, "unit": "DOF*stage/s",
+                          "note": "the same loop with the plain FP64 form (same precision as the CPU reference)"}}
 
     return {
         "value": value, "ms_per_step": ms_mixed / args.steps, "plain": plain,
         "plain_ms_per_step": ms_plain / args.steps, "mixed_over_plain": value / plain,
+        "plain_roofline": plain_roof, "q_mixed": q_mixed, "q_fp64": q_fp64, "dt_fixed": dt,
         "rel_l2_mixed_vs_fp64": [float(v) for v in acc], "roofline": roofline, "e2e": e2e, "clocks": clocks,
         "kernel_ms_mixed": dict(zip(names, [round(float(v), 5) for v in kt])),
         "kernel_ms_fp64": dict(zip(names, [round(float(v), 5) for v in kt_plain])), "ndof": ndof, "dt": dt,
@@ -404,8 +433,9 @@ def run_secondary(name: str, args):
     print(json.dumps(line))
 
 
-def cpu_oracle_rate(case, steps: int = 1):
-    """Oracle FP64 throughput on the host cores (OpenMP, all threads) on RK3 steps of the workload."""
+def oracle_steps(case, steps: int, dt: float):
+    """The FP64 oracle on the host cores (OpenMP, all threads): `steps` RK3 steps of size dt from the
+    workload's initial state. Returns (DOF*stage/s, seconds, final Q)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
 
@@ -415,12 +445,41 @@ def cpu_oracle_rate(case, steps: int = 1):
     cfg = Config(**base)
     o = oracle.Oracle(mesh, cfg.physics(), cfg.options())
     o.set_state(q0)
-    dt = o.max_dt(CFL, CFL)
     t0 = time.perf_counter()
     for s in range(steps):
         o.rk3_step(s * dt, dt)
     el = time.perf_counter() - t0
-    return 3.0 * mesh.ndof * steps / el, el
+    return 3.0 * mesh.ndof * steps / el, el, o.get(0)
+
+
+def reference_arm(args):
+    """The CPU reference timing: the oracle (FP64, OpenMP on all host threads) on its own build of the
+    workload's mesh and geometry; W untimed then K timed RK3 steps with the fixed CFL dt at t=0. Only
+    oracle/ is loaded (the product modules imported here are ctypes declarations and numpy initial
+    conditions)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
+    from horses3d_gb300 import _abi, problems
+    from horses3d_gb300.control import Config
+
+    oracle.build()
+    mesh = oracle.BoxMesh(args.elements, [0.0] * 3, [2 * np.pi] * 3, ORDER, node_type=_abi.DG_NODES_GAUSS, warp=WARP,
+                          patch_order=ORDER)
+    cfg = Config(order=ORDER, nodes=_abi.DG_NODES_GAUSS, mach=MACH, reynolds=RE, riemann=_abi.DG_RIEMANN_LXF)
+    o = oracle.Oracle(mesh, cfg.physics(), cfg.options())
+    o.set_state(problems.taylor_green(mesh.x, MACH))
+    dt = o.max_dt(CFL, CFL)
+    t = 0.0
+    for _ in range(args.warmup):
+        o.rk3_step(t, dt)
+        t += dt
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.rk3_step(t, dt)
+        t += dt
+    el = time.perf_counter() - t0
+    return 3.0 * mesh.ndof * args.steps / el, el, mesh.ndof
 
 
 def main():
@@ -457,18 +516,17 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        from horses3d_gb300 import build as product_build
-
-        product_build.build()
-        rate, el = cpu_oracle_rate(build_case(args.elements), steps=1)
+        rate, el, ndof = reference_arm(args)
         line = {"impl": "reference", "metric": metric, "value": rate, "unit": "DOF*stage/s", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": config,
                 "cpu_baseline": {"value": rate, "unit": "DOF*stage/s", "cores": threads, "kind": "port",
-                                 "sample": "one RK3 step of the full 32^3 N=5 workload (7.08 M DOF)"},
+                                 "sample": f"{args.steps} timed RK3 steps (after {args.warmup} untimed) of the full "
+                                           f"{args.elements}^3 N={ORDER} workload ({ndof} DOF), {el:.1f} s"},
                 "e2e": {"value": rate, "unit": "DOF*stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                 "note": "Fortran reference not buildable here (no Fortran compiler); the oracle port of its "
-                        "loops runs on all host threads"}
+                        "loops runs on all host threads, on the oracle's own mesh and geometry"}
         print(json.dumps(line))
         return
     from horses3d_gb300 import build as product_build
@@ -496,17 +554,26 @@ def main():
         return
     r = run_gpu_arm(args, rank, world, local, case)
     cpu = None
+    vs_oracle = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        rate, el = cpu_oracle_rate(case, steps=1)
+        # the oracle over the same W+K fixed-dt steps from the same state: the CPU baseline's timing
+        # and the accuracy of both GPU forms against the FP64 oracle
+        rate, el, q_ref = oracle_steps(case, args.warmup + args.steps, r["dt_fixed"])
         cpu = {"value": rate, "unit": "DOF*stage/s", "cores": threads, "kind": "port",
-               "sample": f"one RK3 step of the full workload ({el:.1f} s)"}
+               "sample": f"{args.warmup + args.steps} RK3 steps of the full workload ({el:.1f} s)"}
+        from horses3d_gb300.problems import rel_l2
+
+        vs_oracle = {"steps": args.warmup + args.steps,
+                     "mixed": [float(v) for v in rel_l2(r["q_mixed"], q_ref)],
+                     "plain_fp64": [float(v) for v in rel_l2(r["q_fp64"], q_ref)]}
     if rank != 0:
         return
     line = {"metric": metric, "value": r["value"], "unit": "DOF*stage/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 fluxes / f64 state", "data": "synthetic", "config": config,
-            "plain_fp64": {"value": r["plain"], "ms_per_step": r["plain_ms_per_step"]},
+            "plain_fp64": {"value": r["plain"], "ms_per_step": r["plain_ms_per_step"], "roofline": r["plain_roofline"]},
             "mixed_over_plain": r["mixed_over_plain"], "rel_l2_mixed_vs_fp64": r["rel_l2_mixed_vs_fp64"],
+            "rel_l2_vs_oracle": vs_oracle,
             "roofline": r["roofline"], "cpu_baseline": cpu, "e2e": r["e2e"], "clocks": r["clocks"],
             "gpu_launches": r["gpu_launches"], "kernel_ms_mixed": r["kernel_ms_mixed"],
             "kernel_ms_fp64": r["kernel_ms_fp64"]}

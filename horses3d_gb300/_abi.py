@@ -130,6 +130,7 @@ SIGNATURES = [
     ("dg_max_dt_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int,
                                     C.c_int, C.POINTER(DgPhysics), C.c_double, C.c_double, C.c_void_p, _f64p]),
     ("dg_max_dt_noalloc_max_dof", C.c_int64, []),
+    ("dg_measure_fp64_peak", C.c_int, [_f64p]),
     ("dg_residuals", C.c_int, [C.c_void_p, _f64p, C.POINTER(C.c_int)]),
     ("dg_synchronize", C.c_int, [C.c_void_p]),
     ("dg_create_batch", C.c_int, [C.c_int, C.POINTER(DgMeshDesc), C.POINTER(DgPhysics), C.POINTER(DgOptions),

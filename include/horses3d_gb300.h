@@ -185,6 +185,11 @@ int dg_time_steps(dg_ctx* ctx, int n, double t0, double dt, double cfl, double d
  * of size dt. Measurement helper, no reference counterpart. */
 int dg_kernel_times(dg_ctx* ctx, int reps, double t0, double dt, double ms[5]);
 
+/* FP64 fused multiply-add throughput of the current device in TFLOP/s (2 flops per FMA), from
+ * independent FMA chains over a grid that fills every SM, timed with CUDA events: the denominator
+ * of the plain FP64 form's compute roofline. Measurement helper, no reference counterpart. */
+int dg_measure_fp64_peak(double* tflops);
+
 /* MaxTimeStep (DGSEMClass.f90:870-1038) on the device. */
 int dg_max_dt(dg_ctx* ctx, double cfl, double dcfl, double* dt);
 

@@ -47,6 +47,12 @@ def lib():
         L.orc_residuals.restype = C.c_int
         L.orc_residuals.argtypes = [C.c_void_p, _f64p]
         L.orc_mms_state.argtypes = [C.c_void_p, C.c_double, _f64p, _f64p]
+        L.orc_box_mesh_create.restype = C.c_void_p
+        L.orc_box_mesh_create.argtypes = [C.c_int, C.c_int, C.c_int, _f64p, _f64p, C.c_double, C.c_int, C.c_int,
+                                          C.c_int]
+        L.orc_box_mesh_describe.restype = C.c_int
+        L.orc_box_mesh_describe.argtypes = [C.c_void_p, C.c_void_p]
+        L.orc_box_mesh_free.argtypes = [C.c_void_p]
         _lib = L
     return _lib
 
@@ -109,3 +115,37 @@ class Oracle:
         qd = np.empty(5 * self.ndof)
         lib().orc_mms_state(self._h, t, q.ctypes.data_as(_f64p), qd.ctypes.data_as(_f64p))
         return q, qd
+
+
+class BoxMesh:
+    """The oracle's own periodic box mesh (oracle/geometry.cpp): [lo,hi]^3 in n^3 hexahedra of
+    uniform order N, optionally warped by warp*sin(x)sin(y)sin(z) with curved faces given as
+    patches of order patch_order. It carries what the Oracle and the benchmark's CPU reference
+    timing need (``desc``, ``x``, ``ndof``) without the product library."""
+
+    def __init__(self, n, lo, hi, order, node_type=0, warp=0.0, patch_order=0):
+        from horses3d_gb300 import _abi  # ctypes declarations of the C ABI structures only
+
+        lo = np.ascontiguousarray(lo, dtype=np.float64)
+        hi = np.ascontiguousarray(hi, dtype=np.float64)
+        self._h = lib().orc_box_mesh_create(n, n, n, lo.ctypes.data_as(_f64p), hi.ctypes.data_as(_f64p), warp,
+                                            patch_order, node_type, order)
+        if not self._h:
+            raise ValueError("invalid box mesh arguments")
+        self.desc = _abi.DgMeshDesc()
+        if lib().orc_box_mesh_describe(self._h, C.byref(self.desc)) != 0:
+            raise RuntimeError("orc_box_mesh_describe failed")
+        self.n_elements = n ** 3
+        self.order = order
+        self.ndof = self.n_elements * (order + 1) ** 3
+        self.n_faces = int(self.desc.n_faces)
+        self.n_boundary_faces = 0
+        self.x = np.ctypeslib.as_array(self.desc.x, shape=(3 * self.ndof,))
+
+    def array(self, name, count):
+        return np.ctypeslib.as_array(getattr(self.desc, name), shape=(count,))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_box_mesh_free(self._h)
+            self._h = None
