@@ -53,12 +53,15 @@ def lib():
         L.orc_box_mesh_describe.restype = C.c_int
         L.orc_box_mesh_describe.argtypes = [C.c_void_p, C.c_void_p]
         L.orc_box_mesh_free.argtypes = [C.c_void_p]
+        L.orc_set_threads.argtypes = [C.c_int]
         _lib = L
     return _lib
 
 
 def set_threads(n: int) -> None:
+    """OpenMP threads of the oracle's later parallel regions."""
     os.environ["OMP_NUM_THREADS"] = str(n)
+    lib().orc_set_threads(int(n))
 
 
 class Oracle:
