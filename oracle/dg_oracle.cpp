@@ -18,6 +18,8 @@
 #include <mutex>
 #include <vector>
 
+#include <omp.h>
+
 #include "horses3d_gb300.h"
 #include "spectral.hpp"
 
@@ -1083,23 +1085,30 @@ static void prolong(const Solver& s, const Elem& e, int nv, const double* A, std
 static int face_dims(const Elem& e, int side, int a) { return e.P[axis_of(side, a)]; }
 
 // ---------------------------------------------------------------- right-hand side ----------
-static void compute_rhs(Solver& s, double t) {
+// phase < 0: the whole right-hand side. An element partition runs it in three phases with the
+// reference's face exchanges between them (HexMesh_UpdateMPIFacesSolution before phase 1,
+// HexMesh_UpdateMPIFacesGradients before phase 2; HexMesh.f90:1199-1730, MPI_Face.f90:203-383):
+// phase 0 prolongs Q to the faces, phase 1 forms the BR1 gradients and their face traces, phase 2
+// the time derivative.
+static void compute_rhs(Solver& s, double t, int phase = -1) {
     const int K = s.K;
     const bool ns = s.ph.ns;
     // 1) prolong Q to faces (HexMesh.f90:948-1036)
+    if (phase < 0 || phase == 0) {
 #pragma omp parallel for schedule(static)
-    for (int id = 0; id < K; ++id) {
-        const Elem& e = s.el[id];
-        std::vector<double> tr[6];
-        prolong(s, e, 5, &s.Q[5 * e.off], tr);
-        for (int side = 1; side <= 6; ++side) {
-            Face& f = s.fa[e.face[side - 1]];
-            const int fs = e.fside[side - 1];
-            adapt_to_face(f, fs, 5, tr[side - 1], face_dims(e, side, 0), face_dims(e, side, 1), f.Q[fs - 1], s.nodes);
+        for (int id = 0; id < K; ++id) {
+            const Elem& e = s.el[id];
+            std::vector<double> tr[6];
+            prolong(s, e, 5, &s.Q[5 * e.off], tr);
+            for (int side = 1; side <= 6; ++side) {
+                Face& f = s.fa[e.face[side - 1]];
+                const int fs = e.fside[side - 1];
+                adapt_to_face(f, fs, 5, tr[side - 1], face_dims(e, side, 0), face_dims(e, side, 1), f.Q[fs - 1], s.nodes);
+            }
         }
     }
     // 2) BR1 gradients (EllipticBR1.f90:71-159, 168-397)
-    if (ns) {
+    if (ns && (phase < 0 || phase == 1)) {
 #pragma omp parallel for schedule(static)
         for (int id = 0; id < K; ++id) {  // HexElement_ComputeLocalGradient (HexElementClass.f90:427-531)
             const Elem& e = s.el[id];
@@ -1212,6 +1221,7 @@ static void compute_rhs(Solver& s, double t) {
         }
     }
     // 3) TimeDerivative_ComputeQDot (SpatialDiscretization.f90:379-685)
+    if (phase >= 0 && phase != 2) return;
     if (ns) {
 #pragma omp parallel for schedule(static)
         for (int64_t g = 0; g < s.ndof; ++g) mu_kappa(s.ph, &s.Q[5 * g], s.mu2[2 * g], s.mu2[2 * g + 1]);
@@ -1460,9 +1470,21 @@ static double max_dt(const Solver& s, double cfl, double dcfl) {
 // ---------------------------------------------------------------- C API ----------------------
 using orc::Solver;
 
+// n_ghost > 0: an element partition. Faces may name the remote elements n_elements ..
+// n_elements + n_ghost - 1 (the order array holds their orders too); those elements have no
+// storage here, and their face sides are filled by orc_face_trace (the MPI faces of the reference).
+static Solver* create(const dg_mesh_desc* m, int n_ghost, const dg_physics* ph, const dg_options* op);
+
 extern "C" {
 
-void* orc_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op) {
+void* orc_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op) { return create(m, 0, ph, op); }
+void* orc_create_partition(const dg_mesh_desc* m, int n_ghost, const dg_physics* ph, const dg_options* op) {
+    return n_ghost >= 0 ? create(m, n_ghost, ph, op) : nullptr;
+}
+
+}  // extern "C"
+
+static Solver* create(const dg_mesh_desc* m, int n_ghost, const dg_physics* ph, const dg_options* op) {
     auto* s = new Solver();
     s->opt = *op;
     s->nodes = m->node_type;
@@ -1484,13 +1506,13 @@ void* orc_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* 
     const double TRef = 520.0 * 5.0 / 9.0;
     s->ph.S_div_TRef = (198.6 * 5.0 / 9.0) / TRef;
     s->ph.TReNorm = TRef / TRef;
-    s->el.resize(s->K);
+    s->el.resize(s->K + n_ghost);
     int64_t off = 0;
-    for (int e = 0; e < s->K; ++e) {
+    for (int e = 0; e < s->K + n_ghost; ++e) {
         auto& E = s->el[e];
         for (int d = 0; d < 3; ++d) { E.N[d] = m->order[3 * e + d]; E.P[d] = E.N[d] + 1; }
-        E.off = off;
-        off += static_cast<int64_t>(E.P[0]) * E.P[1] * E.P[2];
+        E.off = e < s->K ? off : -1;
+        if (e < s->K) off += static_cast<int64_t>(E.P[0]) * E.P[1] * E.P[2];
     }
     s->ndof = off;
     auto cp = [&](const double* src, int64_t n) { return std::vector<double>(src, src + n); };
@@ -1543,7 +1565,13 @@ void* orc_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* 
     return s;
 }
 
+extern "C" {
+
 void orc_destroy(void* h) { delete static_cast<Solver*>(h); }
+// OpenMP threads of the following parallel regions (the checker's own sizing; all cores by default).
+void orc_set_threads(int n) {
+    if (n > 0) omp_set_num_threads(n);
+}
 int64_t orc_ndof(void* h) { return static_cast<Solver*>(h)->ndof; }
 
 void orc_set_state(void* h, const double* q) {
@@ -1560,6 +1588,51 @@ void orc_get(void* h, int field, double* out) {
 }
 
 void orc_rhs(void* h, double t) { orc::compute_rhs(*static_cast<Solver*>(h), t); }
+
+// One phase (0, 1, 2) of the right-hand side at time t; see compute_rhs.
+void orc_rhs_phase(void* h, double t, int phase) { orc::compute_rhs(*static_cast<Solver*>(h), t, phase); }
+
+// The data an MPI face moves (MPI_Face_SendQ / the gradient sends, MPI_Face.f90:203-383): one side
+// (1 or 2) of face f at its face points in the face's frame, Q (what 0, 5 per point) or the gradient
+// traces U_x, U_y, U_z (what 1, three blocks of 5 per point). set = 0 copies out, 1 copies in.
+// Returns the number of values, or -1 for bad arguments.
+int64_t orc_face_trace(void* h, int f, int side, int what, double* buf, int set) {
+    auto* s = static_cast<Solver*>(h);
+    if (f < 0 || f >= static_cast<int>(s->fa.size()) || side < 1 || side > 2 || what < 0 || what > 1) return -1;
+    orc::Face& F = s->fa[f];
+    const int64_t np = static_cast<int64_t>(F.Nf[0] + 1) * (F.Nf[1] + 1);
+    std::vector<double>* blocks[3] = {&F.Q[side - 1], nullptr, nullptr};
+    int nb = 1;
+    if (what == 1) {
+        blocks[0] = &F.Ux[side - 1];
+        blocks[1] = &F.Uy[side - 1];
+        blocks[2] = &F.Uz[side - 1];
+        nb = 3;
+    }
+    for (int b = 0; b < nb; ++b) {
+        std::vector<double>& v = *blocks[b];
+        if (set) {
+            v.assign(buf + 5 * np * b, buf + 5 * np * (b + 1));
+        } else {
+            if (static_cast<int64_t>(v.size()) != 5 * np) return -1;
+            std::memcpy(buf + 5 * np * b, v.data(), sizeof(double) * 5 * np);
+        }
+    }
+    return 5 * np * nb;
+}
+
+// Stage k (0..2) of the low-storage update after the stage's right-hand side (ExplicitMethods.f90:748-779).
+void orc_rk3_update(void* h, int k, double dt) {
+    auto* s = static_cast<Solver*>(h);
+    const double a[3] = {0.0, -5.0 / 9.0, -153.0 / 128.0};
+    const double c[3] = {1.0 / 3.0, 15.0 / 16.0, 8.0 / 15.0};
+    const int64_t n = 5 * s->ndof;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        s->G[i] = a[k] * s->G[i] + s->QDot[i];
+        s->Q[i] = s->Q[i] + c[k] * dt * s->G[i];
+    }
+}
 
 // ExplicitMethods.f90:748-779 (the dt_vec-free branch).
 void orc_rk3_step(void* h, double t, double dt) {
