@@ -212,19 +212,28 @@ __device__ __forceinline__ void gst5(R* base, int64_t nsp, int64_t idx, const R*
 // Offsets (values of R) of one element's k_volume workspace; every region starts on 16 bytes.
 //   Q4/Q1  state, 5-vector per node
 //   G4/G1  lifted gradient, 3 directions per node (later the contravariant or viscous fluxes)
+//   M      metric vectors per node (split form only; empty otherwise)
 //   U4/U1  BR1 jumps uStar n per face point of the six sides, 3 directions
 //   T4/T1  own Q traces per face point of the six sides
-//   M      metric vectors per node (split form only)
+//   F4/F1  split form: the two-point fluxes of one direction, D = P/2 pairs per node, staged over
+//          U, T and beyond once the gradient phases are done
 template <int P, typename R>
 struct VolLayout {
     static constexpr int P2 = P * P, P3 = P * P * P, A = 16 / static_cast<int>(sizeof(R));
+    static constexpr int D = P / 2;
     __host__ __device__ static constexpr int up(int x) { return (x + A - 1) / A * A; }
     static constexpr int Q4 = 0, Q1 = Q4 + up(4 * P3);
     static constexpr int G4 = Q1 + up(P3), G1 = G4 + up(12 * P3);
-    static constexpr int U4 = G1 + up(3 * P3), U1 = U4 + up(72 * P2);
-    static constexpr int T4 = U1 + up(18 * P2), T1 = T4 + up(24 * P2);
-    static constexpr int M = T1 + up(6 * P2);
-    __host__ __device__ static constexpr int values(bool split) { return M + (split ? up(9 * P3) : 0); }
+    static constexpr int M = G1 + up(3 * P3);
+    __host__ __device__ static constexpr int U4(bool split) { return M + (split ? up(9 * P3) : 0); }
+    __host__ __device__ static constexpr int U1(bool split) { return U4(split) + up(72 * P2); }
+    __host__ __device__ static constexpr int T4(bool split) { return U1(split) + up(18 * P2); }
+    __host__ __device__ static constexpr int T1(bool split) { return T4(split) + up(24 * P2); }
+    __host__ __device__ static constexpr int end_faces(bool split) { return T1(split) + up(6 * P2); }
+    static constexpr int F4 = M + up(9 * P3), F1 = F4 + up(4 * P3 * D), F_END = F1 + up(P3 * D);
+    __host__ __device__ static constexpr int values(bool split) {
+        return split ? (end_faces(true) > F_END ? end_faces(true) : F_END) : end_faces(false);
+    }
 };
 
 template <int P, typename R>
@@ -323,10 +332,10 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
     R* Q1 = base + L::Q1;
     R* G4 = base + L::G4;  // lifted gradient, then the fluxes (same layout)
     R* G1 = base + L::G1;
-    R* U4 = base + L::U4;
-    R* U1 = base + L::U1;
-    R* T4 = base + L::T4;
-    R* T1 = base + L::T1;
+    R* U4 = base + L::U4(split);
+    R* U1 = base + L::U1(split);
+    R* T4 = base + L::T4(split);
+    R* T1 = base + L::T1(split);
     R* sM = base + L::M;
     const int e = blockIdx.x * Geo<P>::EPB + le;
     const bool active = e < a.K;
@@ -585,9 +594,17 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
 #pragma unroll
         for (int v = 0; v < 5; ++v) a.QDot[5 * g + v] = acc[v];
     } else {
-        // Split form (Gauss-Lobatto): two-point fluxes of each node with the nodes of its lines
-        // (HyperbolicSplitForm.f90:64-116), accumulated line by line as
-        // volInt += sharpD(i,l) f#(l,i) + hatD(i,l) Fv(l) (DGIntegrals.f90:92-129), QDot = -volInt.
+        // Split form (Gauss-Lobatto, HyperbolicSplitForm.f90:64-116): the two-point flux f#(a,b) of
+        // a pair of nodes on a line is symmetric, and the reference evaluates it once per pair (for
+        // l > i, copied to f#(l,i)). Here node s of a line evaluates the pairs (s, s + delta mod P),
+        // delta = 1..D with D = P/2, which covers every pair once for odd P; for even P the pairs at
+        // distance P/2 belong to the nodes s < P/2. The lower line index is "left" as in the
+        // reference. One direction at a time, the fluxes are staged per (line, s, delta) in shared
+        // memory, then every node sums its line in line order:
+        // volInt += sharpD(i,l) f#(i,l) + hatD(i,l) Fv(l), QDot = -volInt (DGIntegrals.f90:92-129).
+        constexpr int D = L::D;
+        R* F4 = base + L::F4;
+        R* F1 = base + L::F1;
         if (active) {
 #pragma unroll
             for (int d = 0; d < 3; ++d) st5(G4, n * 3 + d, G1, d * P3 + n, Fv[d]);
@@ -599,38 +616,59 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
             }
         }
         __syncthreads();
-        if (!active) return;
         R acc[5] = {0, 0, 0, 0, 0};
         const R* myJ[3] = {jxs, jes, jzs};
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             const int self = d == 0 ? i : (d == 1 ? j : k);
+            const int line = d == 0 ? (j + P * k) : (d == 1 ? (i + P * k) : (i + P * j));
+            const int stride = d == 0 ? 1 : (d == 1 ? P : P2);
+            const int first = n - self * stride;  // node of line position 0
+            if (active) {
 #pragma unroll
-            for (int l = 0; l < P; ++l) {
-                const int m = d == 0 ? (l + P * (j + P * k)) : (d == 1 ? (i + P * (l + P * k)) : (i + P * (j + P * l)));
-                R fs[5];
-                if (l == self) {
-#pragma unroll
-                    for (int v = 0; v < 5; ++v) fs[v] = Fi[d][v];
-                } else {
-                    R qo[5], jo[3];
+                for (int dl = 1; dl <= D; ++dl) {
+                    if ((P % 2) == 0 && dl == D && self >= D) continue;
+                    const int l = (self + dl) % P;
+                    const int m = first + l * stride;
+                    R qo[5], jo[3], fs[5];
                     ld5(Q4, m, Q1, m, qo);
 #pragma unroll
                     for (int c = 0; c < 3; ++c) jo[c] = sM[(3 * d + c) * P3 + m];
-                    // each pair is evaluated with the lower line index as "left", as the reference does
                     if (self < l) two_point_flux(a.ph, q, qo, myJ[d], jo, fs);
                     else two_point_flux(a.ph, qo, q, jo, myJ[d], fs);
+                    const int idx = (line * P + self) * D + (dl - 1);
+                    st5(F4, idx, F1, idx, fs);
                 }
-                const R sh = a.ops.sharpD[self * kMaxP + l];
-                const R h = a.ops.hatD[self * kMaxP + l];
-                R fv[5];
-                ld5(G4, m * 3 + d, G1, d * P3 + m, fv);
-#pragma unroll
-                for (int v = 0; v < 5; ++v) acc[v] = acc[v] + sh * fs[v] + h * fv[v];
             }
-        }
+            __syncthreads();
+            if (active) {
 #pragma unroll
-        for (int v = 0; v < 5; ++v) a.QDot[5 * g + v] = -acc[v];
+                for (int l = 0; l < P; ++l) {
+                    const int m = first + l * stride;
+                    R fs[5];
+                    if (l == self) {
+#pragma unroll
+                        for (int v = 0; v < 5; ++v) fs[v] = Fi[d][v];
+                    } else {
+                        const int dl = (l - self + P) % P;
+                        const bool mine = dl < D || (dl == D && ((P % 2) == 1 || self < D));
+                        const int idx = mine ? (line * P + self) * D + (dl - 1) : (line * P + l) * D + (P - dl - 1);
+                        ld5(F4, idx, F1, idx, fs);
+                    }
+                    const R sh = a.ops.sharpD[self * kMaxP + l];
+                    const R h = a.ops.hatD[self * kMaxP + l];
+                    R fv[5];
+                    ld5(G4, m * 3 + d, G1, d * P3 + m, fv);
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) acc[v] = acc[v] + sh * fs[v] + h * fv[v];
+                }
+            }
+            __syncthreads();  // the next direction overwrites the staged fluxes
+        }
+        if (active) {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) a.QDot[5 * g + v] = -acc[v];
+        }
     }
 }
 
