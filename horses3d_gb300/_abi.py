@@ -37,6 +37,7 @@ DG_SOURCE_NONE, DG_SOURCE_MMS_CONVERGENCE, DG_SOURCE_MMS_LAMB_VECTOR = 0, 1, 2
 DG_GRADVARS_STATE, DG_GRADVARS_ENTROPY, DG_GRADVARS_ENERGY = 0, 1, 2
 DG_BC_NO_SLIP_WALL, DG_BC_FREE_SLIP_WALL, DG_BC_INFLOW, DG_BC_OUTFLOW = 1, 2, 3, 4
 DG_FIELD_Q, DG_FIELD_QDOT, DG_FIELD_G, DG_FIELD_UX, DG_FIELD_UY, DG_FIELD_UZ = range(6)
+DG_HALO_Q_TRACES, DG_HALO_VISCOUS_FLUX = 0, 1
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
@@ -131,6 +132,14 @@ SIGNATURES = [
                                     C.c_int, C.POINTER(DgPhysics), C.c_double, C.c_double, C.c_void_p, _f64p]),
     ("dg_max_dt_noalloc_max_dof", C.c_int64, []),
     ("dg_measure_fp64_peak", C.c_int, [_f64p]),
+    ("dg_create_partition", C.c_int, [C.POINTER(DgMeshDesc), C.c_int32, C.POINTER(DgPhysics), C.POINTER(DgOptions),
+                                      C.POINTER(C.c_void_p)]),
+    ("dg_halo_set_slots", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_int32)]),
+    ("dg_halo_slot_bytes", C.c_int64, [C.c_void_p]),
+    ("dg_halo_pack", C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    ("dg_halo_unpack", C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    ("dg_partition_stage", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]),
+    ("dg_set_energy_reference", C.c_int, [C.c_void_p, C.c_double]),
     ("dg_residuals", C.c_int, [C.c_void_p, _f64p, C.POINTER(C.c_int)]),
     ("dg_synchronize", C.c_int, [C.c_void_p]),
     ("dg_create_batch", C.c_int, [C.c_int, C.POINTER(DgMeshDesc), C.POINTER(DgPhysics), C.POINTER(DgOptions),

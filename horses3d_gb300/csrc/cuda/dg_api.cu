@@ -55,7 +55,7 @@ template <typename R>
 int setup_store(dg_ctx* c, Store<R>& st, const dg_mesh_desc* m) {
     const size_t nd = static_cast<size_t>(c->ndof);
     const size_t nfp = static_cast<size_t>(c->F) * c->P * c->P;
-    const size_t nslot = 6 * static_cast<size_t>(c->K);
+    const size_t nslot = c->n_slots();
     int rc;
     if ((rc = upload_convert(st.ja_xi, m->ja_xi, 3 * nd, c->stream))) return rc;
     if ((rc = upload_convert(st.ja_eta, m->ja_eta, 3 * nd, c->stream))) return rc;
@@ -244,7 +244,7 @@ namespace {
 
 using h3dctx::validate_boundary_face;
 
-int validate(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op) {
+int validate(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op, int n_ghost) {
     if (!m || !ph || !op) return h3d::fail(DG_ERR_INVALID, "null argument");
     if (m->n_elements < 1 || m->n_faces < 1) return h3d::fail(DG_ERR_INVALID, "empty mesh");
     if (!m->order || !m->x || !m->ja_xi || !m->ja_eta || !m->ja_zeta || !m->jacobian || !m->inv_jacobian ||
@@ -254,7 +254,7 @@ int validate(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op) 
     if (m->node_type != DG_NODES_GAUSS && m->node_type != DG_NODES_GAUSS_LOBATTO)
         return h3d::fail(DG_ERR_INVALID, "unknown node type");
     const int N = m->order[0];
-    for (int e = 0; e < m->n_elements; ++e)
+    for (int e = 0; e < m->n_elements + n_ghost; ++e)
         for (int d = 0; d < 3; ++d)
             if (m->order[3 * e + d] != N)
                 return h3d::fail(DG_ERR_UNSUPPORTED, "the GPU path needs one isotropic order on every element");
@@ -269,12 +269,16 @@ int validate(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op) 
             int rc = validate_boundary_face(m, f);
             if (rc) return rc;
         }
+        int ghosts = 0;
         for (int s = 0; s < (boundary ? 1 : 2); ++s) {
             const int e = m->face_elem[2 * f + s], side = m->face_side[2 * f + s];
-            if (e < 0 || e >= m->n_elements || side < 1 || side > 6)
+            if (e < 0 || e >= m->n_elements + n_ghost || side < 1 || side > 6)
                 return h3d::fail(DG_ERR_INVALID, "face connectivity out of range");
-            ++sides;
+            if (e < m->n_elements) ++sides;
+            else ++ghosts;
         }
+        if (ghosts > (boundary ? 0 : 1))
+            return h3d::fail(DG_ERR_INVALID, "a face of a partition must have one of its own elements");
     }
     if (sides != 6 * static_cast<int64_t>(m->n_elements))
         return h3d::fail(DG_ERR_INVALID, "the faces do not cover every element side once");
@@ -308,11 +312,39 @@ int dg_device_count(int* count) {
     return DG_OK;
 }
 
+namespace {
+
+int create_uniform(const dg_mesh_desc* m, int n_ghost, const dg_physics* ph, const dg_options* op, dg_ctx** out);
+
+}  // namespace
+
 int dg_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op, dg_ctx** out) {
     if (!out) return h3d::fail(DG_ERR_INVALID, "null output pointer");
     *out = nullptr;
     if (m && ph && op && h3dvar::needs_variable_path(m)) return h3dvar::create(1, m, ph, op, out);
-    int rc = validate(m, ph, op);
+    return create_uniform(m, 0, ph, op, out);
+}
+
+int dg_create_partition(const dg_mesh_desc* m, int32_t n_ghost, const dg_physics* ph, const dg_options* op,
+                        dg_ctx** out) {
+    if (!out) return h3d::fail(DG_ERR_INVALID, "null output pointer");
+    *out = nullptr;
+    if (n_ghost < 0) return h3d::fail(DG_ERR_INVALID, "negative ghost element count");
+    if (m && m->n_elements > 0 && m->order) {
+        const int N = m->order[0];
+        for (int64_t q = 0; q < 3 * (static_cast<int64_t>(m->n_elements) + n_ghost); ++q)
+            if (m->order[q] != N)
+                return h3d::fail(DG_ERR_UNSUPPORTED, "element partitions need one isotropic order on every element");
+    }
+    return create_uniform(m, n_ghost, ph, op, out);
+}
+
+}  // extern "C"
+
+namespace {
+
+int create_uniform(const dg_mesh_desc* m, int n_ghost, const dg_physics* ph, const dg_options* op, dg_ctx** out) {
+    int rc = validate(m, ph, op, n_ghost);
     if (rc) return rc;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return h3d::fail(DG_ERR_NODEVICE, "no CUDA device visible");
@@ -321,6 +353,7 @@ int dg_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op,
     c->opt = *op;
     if (m->n_boundaries > 0 && m->boundaries) c->bcs.assign(m->boundaries, m->boundaries + m->n_boundaries);
     c->K = m->n_elements;
+    c->n_ghost = n_ghost;
     c->F = m->n_faces;
     c->P = m->order[0] + 1;
     c->nodes = m->node_type;
@@ -397,7 +430,7 @@ int dg_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op,
         (e = cudaStreamSynchronize(c->stream)))
         return bail(cuda_fail(e, "copy faces"));
     {  // slot neighbour tables: the other side's slot and (rotation | own side << 3)
-        const size_t nslot = 6 * static_cast<size_t>(c->K);
+        const size_t nslot = c->n_slots();
         std::vector<int> nbs(nslot, -1), nbm(nslot, 0);
         std::vector<char> seen(nslot, 0);
         for (int f = 0; f < c->F; ++f)
@@ -415,7 +448,7 @@ int dg_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op,
                 nbs[sl] = static_cast<int>(so);
                 nbm[sl] = m->face_rotation[f] | ((side + 1) << 3);
             }
-        for (size_t sl = 0; sl < nslot; ++sl)
+        for (size_t sl = 0; sl < 6 * static_cast<size_t>(c->K); ++sl)  // every side of the own elements
             if (!seen[sl]) return bail(h3d::fail(DG_ERR_INVALID, "an element side has no face"));
         if ((e = c->nb_slot.alloc(nslot)) != cudaSuccess || (e = c->nb_map.alloc(nslot)) != cudaSuccess)
             return bail(cuda_fail(e, "alloc slot tables"));
@@ -438,6 +471,10 @@ int dg_create(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op,
     return DG_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
 void dg_destroy(dg_ctx* c) {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
@@ -448,6 +485,7 @@ void dg_destroy(dg_ctx* c) {
     c->Q.free(); c->G.free(); c->x.free(); c->scal.free(); c->red.free(); c->nan_flag.free(); c->err_flag.free();
     c->face_elem.free(); c->face_side.free(); c->face_rot.free(); c->nb_slot.free(); c->nb_map.free();
     c->mon.free(); c->mon_count.free(); c->esum.free(); c->dt_bmin.free();
+    c->halo_send.free(); c->halo_recv.free();
     if (c->h_scal) cudaFreeHost(c->h_scal);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -473,6 +511,21 @@ int dg_upload_state(dg_ctx* c, const double* q) {
     }
     CK(cudaMemsetAsync(c->G.p, 0, sizeof(double) * 5 * c->ndof, c->stream));
     CK(run_stage(c, dg::kTraces, 0.0, 0));  // face traces of the new state
+    CK(cudaStreamSynchronize(c->stream));
+    return DG_OK;
+}
+
+int dg_set_energy_reference(dg_ctx* c, double e_ref) {
+    if (!c) return h3d::fail(DG_ERR_INVALID, "null context");
+    if (!std::isfinite(e_ref)) return h3d::fail(DG_ERR_INVALID, "the energy reference must be finite");
+    if (c->var) return h3d::fail(DG_ERR_UNSUPPORTED, "energy reference of a uniform-order context only");
+    if (!c->mixed) return DG_OK;
+    if (e_ref != c->s32.args.e_ref) {
+        c->s32.args.e_ref = e_ref;
+        dg::set_reference_energy(c->s32.args.ph, c->pc.gm1, e_ref);
+        h3dctx::drop_graphs(c);  // kernel arguments changed
+    }
+    CK(run_stage(c, dg::kTraces, 0.0, 0));  // the traces carry the energy relative to the reference
     CK(cudaStreamSynchronize(c->stream));
     return DG_OK;
 }
@@ -525,6 +578,22 @@ int dg_rhs(dg_ctx* c, double t) {
     int rc = set_scalars(c, t, 0.0);
     if (rc) return rc;
     CK(run_stage(c, -1, 0.0, dg::kStoreGrad | dg::kWriteQDot));
+    CK(cudaStreamSynchronize(c->stream));
+    return check_device_error(c);
+}
+
+int dg_partition_stage(dg_ctx* c, int stage, int phase, double t, double dt) {
+    static const double b[3] = {0.0, 1.0 / 3.0, 3.0 / 4.0};
+    if (!c) return h3d::fail(DG_ERR_INVALID, "null context");
+    if (c->var) return h3d::fail(DG_ERR_UNSUPPORTED, "partition stages need a uniform-order context");
+    if (stage < -1 || stage > 2 || phase < 0 || phase > 1) return h3d::fail(DG_ERR_INVALID, "stage or phase out of range");
+    if (stage >= 0 && (!(dt > 0.0) || !std::isfinite(dt))) return h3d::fail(DG_ERR_INVALID, "dt must be positive and finite");
+    CK(cudaStreamSynchronize(c->stream));  // the pinned scalar staging is free again
+    int rc = set_scalars(c, t, stage >= 0 ? dt : 0.0);
+    if (rc) return rc;
+    const int part = phase == 0 ? dg::kVolumeOnly : dg::kSurfaceOnly;
+    const int keep = stage < 0 ? (dg::kStoreGrad | dg::kWriteQDot) : (stage == 2 ? dg::kWriteQDot : 0);
+    CK(run_stage(c, stage, stage >= 0 ? b[stage] : 0.0, part | keep));
     CK(cudaStreamSynchronize(c->stream));
     return check_device_error(c);
 }

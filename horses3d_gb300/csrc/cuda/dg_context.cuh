@@ -92,6 +92,12 @@ struct dg_ctx {
     cudaStream_t stream = nullptr;
     int K = 0, F = 0, P = 0, nodes = 0;
     int64_t ndof = 0;
+    // element partition: remote neighbours as ghost elements K .. K + n_ghost - 1, which own face
+    // slots (filled by the halo exchange) but no nodes; 0 for a whole mesh
+    int n_ghost = 0;
+    size_t n_slots() const { return 6 * (static_cast<size_t>(K) + static_cast<size_t>(n_ghost)); }
+    h3dctx::DevBuf<int> halo_send, halo_recv;  // slots packed for the neighbours / ghost slots filled
+    int n_halo_send = 0, n_halo_recv = 0;
     dg_physics phys{};
     dg_options opt{};
     std::vector<dg_boundary> bcs;  // boundary conditions (variable-order path: of all cases, appended)

@@ -14,6 +14,11 @@ constexpr int kPrepare = -2;
 constexpr int kTraces = -3;
 constexpr int kStoreGrad = 1;
 constexpr int kWriteQDot = 2;
+// Element partitions run a stage in two halves with halo exchanges before each: kVolumeOnly launches
+// the volume kernel alone (after the ghost slots received the neighbours' Q traces), kSurfaceOnly the
+// face flux and update kernels (after they received the neighbours' viscous normal fluxes).
+constexpr int kVolumeOnly = 4;
+constexpr int kSurfaceOnly = 8;
 
 template <typename R>
 using StageFn = cudaError_t (*)(const Args<R>& a, int stage, double tshift, int flags, cudaStream_t s);
@@ -55,7 +60,9 @@ cudaError_t run_stage(const Args<R>& a, int stage, double tshift, int flags, cud
         k_traces<P, GL, R><<<eblocks, THREADS, 0, s>>>(a);
         return cudaGetLastError();
     }
-    k_volume<P, GL, R><<<eblocks, THREADS, volume_smem_bytes<P, R>(a.inviscid), s>>>(a, flags & kStoreGrad);
+    if (!(flags & kSurfaceOnly))
+        k_volume<P, GL, R><<<eblocks, THREADS, volume_smem_bytes<P, R>(a.inviscid), s>>>(a, flags & kStoreGrad);
+    if (flags & kVolumeOnly) return cudaGetLastError();
     launch_flux<P, R>(a, fblocks, s);
     if (a.source) launch_update<P, GL, true>(a, eblocks, stage, tshift, (flags & kWriteQDot) ? 1 : 0, s);
     else launch_update<P, GL, false>(a, eblocks, stage, tshift, (flags & kWriteQDot) ? 1 : 0, s);

@@ -150,6 +150,11 @@ void dg_destroy(dg_ctx* ctx);
 /* State transfer in the reference layout (Q(1:5,i,j,k) element after element). */
 int dg_upload_state(dg_ctx* ctx, const double* q);
 int dg_download(dg_ctx* ctx, int field, double* dst);
+/* The mixed form carries the energy in FP32 relative to a constant reference, by default the mean
+ * energy of each upload. Element partitions of one mesh must share one reference: set it after
+ * dg_upload_state (e.g. to the mean over all partitions). Recomputes the face traces; no effect on
+ * the plain form. Uniform-order contexts only. No reference counterpart (the reference is FP64). */
+int dg_set_energy_reference(dg_ctx* ctx, double e_ref);
 int64_t dg_ndof(const dg_ctx* ctx);
 
 /* ComputeTimeDerivative: QDot = RHS(Q, t) (SpatialDiscretization.f90:227-685). */
@@ -213,6 +218,39 @@ int64_t dg_max_dt_noalloc_max_dof(void);
 
 /* ComputeMaxResiduals: max|QDot| per conserved variable; *nan_found = 1 if Q holds NaN/Inf. */
 int dg_residuals(dg_ctx* ctx, double maxres[5], int* nan_found);
+
+/* Element partitions (multi-GPU domain decomposition, one partition per GPU; the reference's MPI
+ * path: MPI_Face.f90:203-383, HexMesh_UpdateMPIFacesSolution/Gradients in HexMesh.f90:1199-1730,
+ * the dt and residual reductions of DGSEMClass.f90:1019-1021 and :770-868).
+ *
+ * dg_create_partition: `mesh` describes the partition's own elements (n_elements, with their nodes
+ * and metric terms) and every face that touches them. A face to a remote element names it as
+ * n_elements + g, g in 0..n_ghost-1 (`order` holds 3*(n_elements + n_ghost) entries; one isotropic
+ * order throughout), keeps the global face's left/right sides, rotation and geometry, and must have
+ * one of the partition's own elements. Each ghost element owns six face slots (slot = 6*element +
+ * side - 1) that the halo exchange fills; it has no nodes. */
+int dg_create_partition(const dg_mesh_desc* mesh, int32_t n_ghost, const dg_physics* phys, const dg_options* opts,
+                        dg_ctx** out);
+/* Registers the slots packed for the neighbours (own slots, 0 .. 6*n_elements-1) and the ghost
+ * slots filled from them (6*n_elements .. 6*(n_elements+n_ghost)-1), in the order both sides agree
+ * on (e.g. neighbour by neighbour, faces in global order). */
+int dg_halo_set_slots(dg_ctx* ctx, int32_t n_send, const int32_t* send_slots, int32_t n_recv, const int32_t* recv_slots);
+/* Bytes of one slot's payload: P^2 points x 5 values of the working precision (8 bytes plain, 4 mixed). */
+int64_t dg_halo_slot_bytes(const dg_ctx* ctx);
+/* DG_HALO_Q_TRACES: the Q traces of the current state, exchanged before the volume phase.
+ * DG_HALO_VISCOUS_FLUX: each side's viscous normal flux Fv(Q, grad U).n, exchanged before the
+ * surface phase (Navier-Stokes only). dst/src are device buffers of n_send/n_recv slot payloads;
+ * both calls return when the data is in place. */
+enum { DG_HALO_Q_TRACES = 0, DG_HALO_VISCOUS_FLUX = 1 };
+int dg_halo_pack(dg_ctx* ctx, int field, void* dst);
+int dg_halo_unpack(dg_ctx* ctx, int field, const void* src);
+/* One half of an RK stage on a partition: phase 0 the volume kernel (gradients, BR1 lifting, the
+ * sides' viscous normal fluxes, volume integral), phase 1 the face fluxes and the surface integral
+ * with the low-storage update of RK stage `stage` (0..2, at time t + b_k dt, then the Q traces of the
+ * new state) or, with stage -1, the right-hand side alone at time t (QDot and the lifted gradients
+ * kept). A step is, for k = 0..2: exchange Q traces, phase 0, exchange viscous fluxes (NS), phase 1;
+ * dt and residuals are reduced over the partitions by the caller (MIN, MAX). */
+int dg_partition_stage(dg_ctx* ctx, int stage, int phase, double t, double dt);
 
 /* Block until all work queued on the context's stream is done. */
 int dg_synchronize(dg_ctx* ctx);

@@ -54,6 +54,12 @@ def lib():
         L.orc_box_mesh_describe.argtypes = [C.c_void_p, C.c_void_p]
         L.orc_box_mesh_free.argtypes = [C.c_void_p]
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_create_partition.restype = C.c_void_p
+        L.orc_create_partition.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        L.orc_rhs_phase.argtypes = [C.c_void_p, C.c_double, C.c_int]
+        L.orc_face_trace.restype = C.c_int64
+        L.orc_face_trace.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _f64p, C.c_int]
+        L.orc_rk3_update.argtypes = [C.c_void_p, C.c_int, C.c_double]
         _lib = L
     return _lib
 
@@ -152,3 +158,109 @@ class BoxMesh:
         if getattr(self, "_h", None):
             lib().orc_box_mesh_free(self._h)
             self._h = None
+
+
+class OraclePartition:
+    """The oracle on one element partition (orc_create_partition; ``part`` from
+    horses3d_gb300.partition.partition_mesh): the right-hand side in its three phases with the
+    reference's MPI-face exchanges between them (the face Q after phase 0, the face gradients after
+    phase 1; MPI_Face.f90:203-383). Payloads are numpy arrays, one per neighbour: the faces shared
+    with it in ascending global order, each side's face-frame trace."""
+
+    Q, GRADIENTS = 0, 1
+
+    def __init__(self, part, physics, options):
+        self.part = part
+        self.ns = physics.navier_stokes != 0
+        self._h = lib().orc_create_partition(C.byref(part.desc), part.n_ghost, C.byref(physics), C.byref(options))
+        if not self._h:
+            raise ValueError("orc_create_partition failed")
+        self.ndof = int(lib().orc_ndof(self._h))
+        self._np = {}
+        nf = np.ctypeslib.as_array(part.desc.face_nf, shape=(2 * part.desc.n_faces,)).reshape(-1, 2)
+        for n in part.neighbours:
+            self._np[n.rank] = [(int(nf[f, 0]) + 1) * (int(nf[f, 1]) + 1) for f in n.faces]
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_destroy(self._h)
+            self._h = None
+
+    def set_state(self, q):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        assert q.size == 5 * self.ndof
+        lib().orc_set_state(self._h, q.ctypes.data_as(_f64p))
+
+    def get(self, field: int) -> np.ndarray:
+        out = np.empty(5 * self.ndof)
+        lib().orc_get(self._h, field, out.ctypes.data_as(_f64p))
+        return out
+
+    def phase(self, t: float, k: int) -> None:
+        lib().orc_rhs_phase(self._h, t, k)
+
+    def update(self, k: int, dt: float) -> None:
+        lib().orc_rk3_update(self._h, k, dt)
+
+    def max_dt(self, cfl: float, dcfl: float) -> float:
+        return float(lib().orc_max_dt(self._h, cfl, dcfl))
+
+    def _size(self, what: int, q: int) -> int:
+        return sum(self._np[q]) * (5 if what == self.Q else 15)
+
+    def pack(self, what: int) -> dict:
+        out = {}
+        for n in self.part.neighbours:
+            buf = np.empty(self._size(what, n.rank))
+            a = 0
+            for f, side, npts in zip(n.faces, n.own_side, self._np[n.rank]):
+                m = npts * (5 if what == self.Q else 15)
+                got = lib().orc_face_trace(self._h, int(f), int(side), what, buf[a:a + m].ctypes.data_as(_f64p), 0)
+                assert got == m, (f, side, got, m)
+                a += m
+            out[(self.part.rank, n.rank)] = buf
+        return out
+
+    def recv_like(self, what: int) -> dict:
+        return {(self.part.rank, n.rank): np.empty(self._size(what, n.rank)) for n in self.part.neighbours}
+
+    def unpack(self, what: int, recvs: dict) -> None:
+        for n in self.part.neighbours:
+            buf = np.ascontiguousarray(recvs[(self.part.rank, n.rank)], dtype=np.float64)
+            a = 0
+            for f, side, npts in zip(n.faces, n.own_side, self._np[n.rank]):
+                m = npts * (5 if what == self.Q else 15)
+                lib().orc_face_trace(self._h, int(f), int(3 - side), what, buf[a:a + m].ctypes.data_as(_f64p), 1)
+                a += m
+
+
+def partition_rhs(parts, t: float, exchange) -> None:
+    """ComputeTimeDerivative over OraclePartitions; exchange(sends, recv_like) -> recvs moves the
+    per-neighbour numpy payloads (keys (this rank, neighbour))."""
+    def move(what):
+        sends, like = {}, {}
+        for p in parts:
+            sends.update(p.pack(what))
+            like.update(p.recv_like(what))
+        recvs = exchange(sends, like)
+        for p in parts:
+            p.unpack(what, recvs)
+
+    for p in parts:
+        p.phase(t, 0)
+    move(OraclePartition.Q)
+    if parts and parts[0].ns:
+        for p in parts:
+            p.phase(t, 1)
+        move(OraclePartition.GRADIENTS)
+    for p in parts:
+        p.phase(t, 2)
+
+
+def partition_rk3_step(parts, t: float, dt: float, exchange) -> None:
+    """TakeRK3Step over OraclePartitions (ExplicitMethods.f90:748-779)."""
+    b = (0.0, 1.0 / 3.0, 3.0 / 4.0)
+    for k in range(3):
+        partition_rhs(parts, t + b[k] * dt, exchange)
+        for p in parts:
+            p.update(k, dt)
