@@ -32,7 +32,7 @@ DG_RIEMANN_STD_ROE, DG_RIEMANN_ROE_PIKE, DG_RIEMANN_LOW_DISS_ROE = 4, 5, 6
 DG_RIEMANN_MATRIX_DISS, DG_RIEMANN_VISCOUS_NS, DG_RIEMANN_U_DISS = 7, 8, 9
 DG_AVG_STANDARD, DG_AVG_PIROZZOLI, DG_AVG_DUCROS, DG_AVG_MORINISHI, DG_AVG_KENNEDY_GRUBER = 0, 1, 2, 3, 4
 DG_AVG_ENTROPY_CONSERVING, DG_AVG_CHANDRASEKAR = 5, 6
-DG_PRECISION_FP64, DG_PRECISION_MIXED = 0, 1
+DG_PRECISION_FP64, DG_PRECISION_MIXED, DG_PRECISION_MIXED_TC = 0, 1, 2
 DG_SOURCE_NONE, DG_SOURCE_MMS_CONVERGENCE, DG_SOURCE_MMS_LAMB_VECTOR = 0, 1, 2
 DG_GRADVARS_STATE, DG_GRADVARS_ENTROPY, DG_GRADVARS_ENERGY = 0, 1, 2
 DG_BC_NO_SLIP_WALL, DG_BC_FREE_SLIP_WALL, DG_BC_INFLOW, DG_BC_OUTFLOW = 1, 2, 3, 4
@@ -132,6 +132,7 @@ SIGNATURES = [
                                     C.c_int, C.POINTER(DgPhysics), C.c_double, C.c_double, C.c_void_p, _f64p]),
     ("dg_max_dt_noalloc_max_dof", C.c_int64, []),
     ("dg_measure_fp64_peak", C.c_int, [_f64p]),
+    ("dg_tc_selftest", C.c_int, [C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int]),
     ("dg_create_partition", C.c_int, [C.POINTER(DgMeshDesc), C.c_int32, C.POINTER(DgPhysics), C.POINTER(DgOptions),
                                       C.POINTER(C.c_void_p)]),
     ("dg_halo_set_slots", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_int32)]),

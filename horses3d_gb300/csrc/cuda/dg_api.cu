@@ -291,8 +291,14 @@ int validate(const dg_mesh_desc* m, const dg_physics* ph, const dg_options* op, 
     if (op->riemann < DG_RIEMANN_ROE || op->riemann > DG_RIEMANN_U_DISS) return h3d::fail(DG_ERR_UNSUPPORTED, "riemann solver");
     if (op->averaging < DG_AVG_STANDARD || op->averaging > DG_AVG_CHANDRASEKAR)
         return h3d::fail(DG_ERR_UNSUPPORTED, "averaging");
-    if (op->precision != DG_PRECISION_FP64 && op->precision != DG_PRECISION_MIXED)
+    if (op->precision != DG_PRECISION_FP64 && op->precision != DG_PRECISION_MIXED &&
+        op->precision != DG_PRECISION_MIXED_TC)
         return h3d::fail(DG_ERR_UNSUPPORTED, "precision");
+    if (op->precision == DG_PRECISION_MIXED_TC &&
+        (N != 5 || m->node_type != DG_NODES_GAUSS || op->inviscid != DG_INVISCID_STANDARD ||
+         (ph->navier_stokes && op->gradient_variables != DG_GRADVARS_STATE)))
+        return h3d::fail(DG_ERR_UNSUPPORTED,
+                         "the tensor-core form needs N = 5 Gauss nodes, the standard volume form and state gradients");
     if (op->source < DG_SOURCE_NONE || op->source > DG_SOURCE_MMS_LAMB_VECTOR)
         return h3d::fail(DG_ERR_UNSUPPORTED, "source");
     if (op->gradient_variables < DG_GRADVARS_STATE || op->gradient_variables > DG_GRADVARS_ENERGY)
@@ -358,7 +364,7 @@ int create_uniform(const dg_mesh_desc* m, int n_ghost, const dg_physics* ph, con
     c->P = m->order[0] + 1;
     c->nodes = m->node_type;
     c->ndof = static_cast<int64_t>(c->K) * c->P * c->P * c->P;
-    c->mixed = op->precision == DG_PRECISION_MIXED;
+    c->mixed = op->precision == DG_PRECISION_MIXED || op->precision == DG_PRECISION_MIXED_TC;
     // PhysicsStorage_NS.f90:186-290,413-429 (air, Sutherland defaults)
     dg::PhysConst& pc = c->pc;
     pc.gamma = 1.4;
@@ -458,6 +464,7 @@ int create_uniform(const dg_mesh_desc* m, int n_ghost, const dg_physics* ph, con
     }
     if (c->mixed) {
         if ((rc = setup_store(c, c->s32, m))) return bail(rc);
+        c->s32.args.tc = op->precision == DG_PRECISION_MIXED_TC ? 1 : 0;
         c->s32.stage = dg::stage_fn_fp32(c->P, c->nodes == DG_NODES_GAUSS_LOBATTO);
         c->s32.times = dg::times_fn_fp32(c->P, c->nodes == DG_NODES_GAUSS_LOBATTO);
     } else {

@@ -26,6 +26,7 @@
 
 #include "dg_convert.cuh"
 #include "dg_physics.cuh"
+#include "dg_tc.cuh"
 #include "dg_tma.cuh"
 
 namespace dg {
@@ -44,6 +45,7 @@ struct Args {
     PhysR<R> ph;
     Ops<R> ops;
     int inviscid, source;
+    int tc;  // volume kernel with the tensor-core gradient contractions (DG_PRECISION_MIXED_TC)
     // geometry per node
     const R* ja_xi;
     const R* ja_eta;
@@ -241,6 +243,21 @@ __host__ __device__ constexpr int volume_smem_values(bool split) {
     return VolLayout<P, R>::values(split);
 }
 
+// Tensor-core gradient of k_volume (one element per CTA): the A operand of one direction, rows
+// (variable v, line) = v P^2 + line with K = the node's position on the line (hi and lo TF32 parts,
+// 2 x 128-row blocks), and the B operand [D; vL; vR] (16 rows, hi and lo), after the FP32 workspace
+// at a 128-byte boundary.
+struct TcLayout {
+    static constexpr uint32_t kARows = 256, kBRows = 16;
+    static constexpr uint32_t A_HI = 0, A_LO = tc::operand_bytes(kARows), B_HI = 2 * tc::operand_bytes(kARows),
+                              B_LO = B_HI + tc::operand_bytes(kBRows), BYTES = B_LO + tc::operand_bytes(kBRows);
+    static constexpr uint32_t kCols = 32;  // TMEM columns: 2 blocks of N = 16
+};
+template <int P, typename R>
+__host__ __device__ constexpr size_t volume_tc_offset() {
+    return (static_cast<size_t>(VolLayout<P, R>::values(false)) * sizeof(R) + 127) / 128 * 128;
+}
+
 // Work item tt of the 6 P^2 face points of an element -> (side, point). For Gauss nodes the two ends
 // of a line are adjacent items (lanes 2q and 2q+1): their traces read the same shared-memory words in
 // the same instructions, which the hardware serves as one broadcast; Gauss-Lobatto traces read one
@@ -319,10 +336,11 @@ __global__ void __launch_bounds__(Geo<P>::THREADS) k_traces(Args<R> a) {
 // ------------------------------------------------------------------------------------------------
 // k_volume: gradient, BR1 lifting, viscous normal fluxes on the faces, volume integral -> QDot.
 // ------------------------------------------------------------------------------------------------
-template <int P, bool GL, typename R>
+template <int P, bool GL, typename R, bool TC = false>
 __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_volume(Args<R> a, int store_grad) {
     using L = VolLayout<P, R>;
     constexpr int P2 = Geo<P>::P2, P3 = Geo<P>::P3, F6 = 6 * P2;
+    static_assert(!TC || (Geo<P>::EPB == 1 && 5 * P2 <= 192 && P + 2 <= 16), "tensor-core gradient: one element per CTA");
     const bool split = a.inviscid != 0;
     const bool ns = a.ph.ns;
     extern __shared__ __align__(16) unsigned char dsm[];
@@ -344,6 +362,32 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
 
     R q[5];
     R jxs[3], jes[3], jzs[3];
+    __shared__ __align__(8) uint64_t tc_bar;
+    __shared__ uint32_t tc_slot;
+    unsigned char* tcm = dsm + volume_tc_offset<P, R>();
+    if constexpr (TC) {
+        // TMEM for the accumulators, zero A operands (the padding rows and K = P..7 stay zero), the
+        // B operand [D; vL; vR] split into TF32 hi and lo parts, the MMA completion barrier
+        if (threadIdx.x < 32) {
+            tc::tmem_alloc(&tc_slot, TcLayout::kCols);
+            tc::fence_before_sync();
+        }
+        for (int w = threadIdx.x; w < static_cast<int>(TcLayout::B_HI / 16); w += blockDim.x)
+            reinterpret_cast<float4*>(tcm)[w] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int w = threadIdx.x; w < static_cast<int>(TcLayout::kBRows) * 8; w += blockDim.x) {
+            const int nr = w >> 3, kk = w & 7;
+            float x = 0.f;
+            if (kk < P) x = nr < P ? float(a.ops.D[nr * kMaxP + kk]) : nr == P ? float(a.ops.vL[kk])
+                                                                     : nr == P + 1 ? float(a.ops.vR[kk]) : 0.f;
+            const float hi = tc::tf32_hi(x);
+            *reinterpret_cast<float*>(tcm + TcLayout::B_HI + tc::operand_offset(nr, kk)) = hi;
+            *reinterpret_cast<float*>(tcm + TcLayout::B_LO + tc::operand_offset(nr, kk)) = x - hi;
+        }
+        if (threadIdx.x == 0) {
+            mbar_init(&tc_bar, 1);
+            mbar_init_fence();
+        }
+    }
     if (active) {
         load_state(a, g, q);
         st5(Q4, n, Q1, n, q);
@@ -355,6 +399,92 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
         }
     }
     __syncthreads();
+    if constexpr (TC) {
+        // Gradient contractions on the tensor cores (HexElement_ComputeLocalGradient,
+        // HexElementClass.f90:427-531, and the Q traces of ProlongSolutionToFaces): per direction,
+        // C = X [D; vL; vR]^T with X the lines of Q as TF32 split products, the derivatives at the
+        // line's nodes in columns 0..P-1 and its two end values in columns P, P+1. The derivatives
+        // go to the G workspace as [direction][variable][node], the end values to the own-trace
+        // workspace T. One direction at a time through one A buffer and 32 TMEM columns.
+        tc::fence_after_sync();
+        const uint32_t tbase = tc_slot;
+        bool ok = true;
+        if (ns) {
+            R* Gs = G4;  // the lifted gradient's space, free until the lifting writes it
+            const int w = threadIdx.x >> 5;
+            for (int d = 0; d < 3; ++d) {
+                const int self = d == 0 ? i : (d == 1 ? j : k);
+                const int line = d == 0 ? (j + P * k) : (d == 1 ? (i + P * k) : (i + P * j));
+                if (active) {
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) {
+                        const float x = float(q[v]), hi = tc::tf32_hi(x);
+                        const uint32_t off = tc::operand_offset(v * P2 + line, self);
+                        *reinterpret_cast<float*>(tcm + TcLayout::A_HI + off) = hi;
+                        *reinterpret_cast<float*>(tcm + TcLayout::A_LO + off) = x - hi;
+                    }
+                }
+                fence_proxy_async_smem();  // the operand stores before the tensor core reads them
+                tc::fence_before_sync();
+                __syncthreads();
+                tc::fence_after_sync();
+                if (threadIdx.x == 0) {
+                    constexpr uint32_t id = tc::idesc_tf32(128, 16);
+                    const uint64_t bh = tc::smem_desc(tcm + TcLayout::B_HI), bl = tc::smem_desc(tcm + TcLayout::B_LO);
+#pragma unroll
+                    for (int b = 0; b < 2; ++b) {
+                        const uint32_t ta = tbase + 16u * b;
+                        const uint32_t ob = b * tc::operand_bytes(128);
+                        tc::mma_tf32(ta, tc::smem_desc(tcm + TcLayout::A_HI + ob), bh, id, false);
+                        tc::mma_tf32(ta, tc::smem_desc(tcm + TcLayout::A_HI + ob), bl, id, true);
+                        tc::mma_tf32(ta, tc::smem_desc(tcm + TcLayout::A_LO + ob), bh, id, true);
+                    }
+                    tc::commit(&tc_bar);
+                }
+                const bool done = mbar_wait(&tc_bar, d & 1);
+                if (__syncthreads_or(!done)) {  // block-uniform
+                    ok = false;
+                    if (threadIdx.x == 0) {
+                        atomicOr(a.err, 1);
+                        mbar_wait(&tc_bar, d & 1, kWaitNs / 4);  // bounded: let a late MMA land before TMEM is freed
+                    }
+                    __syncthreads();
+                    break;
+                }
+                tc::fence_after_sync();
+                if (w < 6) {  // full warps: warps 0-3 read block 0, warps 4-5 lanes 0-63 of block 1
+                    const int b = w >> 2;
+                    const int row = 128 * b + 32 * (w & 3) + (threadIdx.x & 31);
+                    float val[16];
+                    tc::ld_32x32b_x16(tbase + 16u * b + ((32u * (w & 3)) << 16), val);
+                    if (row < 5 * P2) {
+                        const int v = row / P2, ln = row - v * P2;
+#pragma unroll
+                        for (int l = 0; l < P; ++l) {
+                            const int node = d == 0 ? (l + P * ln) : (d == 1 ? ((ln % P) + P * l + P2 * (ln / P)) : (ln + P2 * l));
+                            Gs[(d * 5 + v) * P3 + node] = R(val[l]);
+                        }
+                        // own Q traces at the two end faces of the line, in the sides' face
+                        // coordinates: LEFT (6) / RIGHT (4), FRONT (1) / BACK (2), BOTTOM (3) / TOP (5)
+                        const int tl = ((d == 0 ? 6 : (d == 1 ? 1 : 3)) - 1) * P2 + ln;
+                        const int tr = ((d == 0 ? 4 : (d == 1 ? 2 : 5)) - 1) * P2 + ln;
+                        if (v < 4) {
+                            T4[4 * tl + v] = R(val[P]);
+                            T4[4 * tr + v] = R(val[P + 1]);
+                        } else {
+                            T1[tl] = R(val[P]);
+                            T1[tr] = R(val[P + 1]);
+                        }
+                    }
+                }
+                tc::fence_before_sync();
+                __syncthreads();  // the next direction reuses the A buffer and the accumulators
+            }
+        }
+        tc::fence_after_sync();
+        if (threadIdx.x < 32) tc::tmem_dealloc(tbase, TcLayout::kCols);
+        if (!ok) return;
+    }
 
     R U[3][5];
     // gradient variables other than the state are formed per node into the (still unused) gradient
@@ -375,6 +505,14 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
         if (active) {
             // local gradient: U_x = (U_xi Ja^xi_x + U_eta Ja^eta_x + U_zeta Ja^zeta_x) / J
             R uxi[5] = {0, 0, 0, 0, 0}, ueta[5] = {0, 0, 0, 0, 0}, uzeta[5] = {0, 0, 0, 0, 0};
+            if constexpr (TC) {
+#pragma unroll
+                for (int v = 0; v < 5; ++v) {
+                    uxi[v] = G4[(0 * 5 + v) * P3 + n];
+                    ueta[v] = G4[(1 * 5 + v) * P3 + n];
+                    uzeta[v] = G4[(2 * 5 + v) * P3 + n];
+                }
+            } else {
 #pragma unroll
             for (int l = 0; l < P; ++l) {
                 const R w = a.ops.D[i * kMaxP + l];
@@ -402,6 +540,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
 #pragma unroll
                 for (int v = 0; v < 5; ++v) uzeta[v] = uzeta[v] + x[v] * w;
             }
+            }
             const R ij = a.inv_jac[g];
 #pragma unroll
             for (int v = 0; v < 5; ++v) {
@@ -417,8 +556,12 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
                 const int ca = p % P, cb = p / P;
                 const int64_t s = slot(e, side);
                 R own[1][5], nbr[5];
-                trace5<P, GL, 1>(a.ops, Q4, Q1, P3, side, ca, cb, own);
-                st5(T4, t, T1, t, own[0]);
+                if constexpr (TC) {
+                    ld5(T4, t, T1, t, own[0]);  // from the tensor-core contraction
+                } else {
+                    trace5<P, GL, 1>(a.ops, Q4, Q1, P3, side, ca, cb, own);
+                    st5(T4, t, T1, t, own[0]);
+                }
                 const int map = a.nb_map[s];
                 const int nb = a.nb_slot[s];
                 const R* sg = a.sgeo + s * 4 * P2 + p;

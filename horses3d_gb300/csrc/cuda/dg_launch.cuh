@@ -28,6 +28,27 @@ size_t volume_smem_bytes(int inviscid) {
     return static_cast<size_t>(Geo<P>::EPB) * volume_smem_values<P, R>(inviscid != 0) * sizeof(R);
 }
 
+// The tensor-core gradient variant exists for the headline configuration: N = 5 on Gauss nodes,
+// FP32 arithmetic (the mixed form), standard volume form.
+template <int P, bool GL, typename R>
+constexpr bool kTcVolume = (P == 6 && !GL && sizeof(R) == 4);
+
+template <int P, typename R>
+size_t volume_tc_smem_bytes() {
+    return volume_tc_offset<P, R>() + TcLayout::BYTES;
+}
+
+template <int P, bool GL, typename R>
+void launch_volume(const Args<R>& a, int blocks, int store_grad, cudaStream_t s) {
+    if constexpr (kTcVolume<P, GL, R>) {
+        if (a.tc) {
+            k_volume<P, GL, R, true><<<blocks, Geo<P>::THREADS, volume_tc_smem_bytes<P, R>(), s>>>(a, store_grad);
+            return;
+        }
+    }
+    k_volume<P, GL, R><<<blocks, Geo<P>::THREADS, volume_smem_bytes<P, R>(a.inviscid), s>>>(a, store_grad);
+}
+
 // The update kernel stages its element blocks by TMA where one element fills the CTA and its
 // FP64 blocks fit the static shared memory (P = 6, the headline order).
 template <int P>
@@ -53,15 +74,20 @@ cudaError_t run_stage(const Args<R>& a, int stage, double tshift, int flags, cud
     const int eblocks = (a.K + EPB - 1) / EPB;
     const long long fp = static_cast<long long>(a.F) * P * P;
     const int fblocks = static_cast<int>((fp + 127) / 128);
-    if (stage == kPrepare)  // opt in to the large dynamic shared memory once, outside any capture
+    if (stage == kPrepare) {  // opt in to the large dynamic shared memory once, outside any capture
+        if constexpr (kTcVolume<P, GL, R>) {
+            const cudaError_t e = cudaFuncSetAttribute(k_volume<P, GL, R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       static_cast<int>(volume_tc_smem_bytes<P, R>()));
+            if (e != cudaSuccess) return e;
+        }
         return cudaFuncSetAttribute(k_volume<P, GL, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     static_cast<int>(volume_smem_bytes<P, R>(1)));
+    }
     if (stage == kTraces) {
         k_traces<P, GL, R><<<eblocks, THREADS, 0, s>>>(a);
         return cudaGetLastError();
     }
-    if (!(flags & kSurfaceOnly))
-        k_volume<P, GL, R><<<eblocks, THREADS, volume_smem_bytes<P, R>(a.inviscid), s>>>(a, flags & kStoreGrad);
+    if (!(flags & kSurfaceOnly)) launch_volume<P, GL, R>(a, eblocks, flags & kStoreGrad, s);
     if (flags & kVolumeOnly) return cudaGetLastError();
     launch_flux<P, R>(a, fblocks, s);
     if (a.source) launch_update<P, GL, true>(a, eblocks, stage, tshift, (flags & kWriteQDot) ? 1 : 0, s);
@@ -91,7 +117,7 @@ cudaError_t kernel_times(const Args<R>& a, int reps, cudaStream_t s, double* ms)
         cudaEventRecord(e0, s);
         for (int r = 0; r < reps; ++r) {
             switch (kk) {
-                case 0: k_volume<P, GL, R><<<eblocks, THREADS, volume_smem_bytes<P, R>(a.inviscid), s>>>(a, 0); break;
+                case 0: launch_volume<P, GL, R>(a, eblocks, 0, s); break;
                 case 1: launch_flux<P, R>(a, fblocks, s); break;
                 case 2: launch_update<P, GL, false>(a, eblocks, 1, 1.0 / 3.0, 0, s); break;
                 default: k_traces<P, GL, R><<<eblocks, THREADS, 0, s>>>(a); break;

@@ -57,7 +57,10 @@ enum { DG_AVG_STANDARD = 0, DG_AVG_PIROZZOLI = 1,                  /* "averaging
        DG_AVG_DUCROS = 2, DG_AVG_MORINISHI = 3,                    /*  states of every solver but */
        DG_AVG_KENNEDY_GRUBER = 4,                                  /*  Roe and Rusanov, and the */
        DG_AVG_ENTROPY_CONSERVING = 5, DG_AVG_CHANDRASEKAR = 6 };   /*  split form's two-point fluxes) */
-enum { DG_PRECISION_FP64 = 0, DG_PRECISION_MIXED = 1 };            /* plain FP64 / FP32 flux form */
+enum { DG_PRECISION_FP64 = 0, DG_PRECISION_MIXED = 1,             /* plain FP64 / FP32 flux form */
+       DG_PRECISION_MIXED_TC = 2 };  /* mixed form with the gradient contractions and face traces on the
+                                        tensor cores (tcgen05 TF32 split products in TMEM); uniform
+                                        N = 5 on Gauss nodes, standard volume form, state gradients */
 enum { DG_GRADVARS_STATE = 0, DG_GRADVARS_ENTROPY = 1,             /* "gradient variables" of BR1 */
        DG_GRADVARS_ENERGY = 2 };
 enum { DG_SOURCE_NONE = 0,                                         /* UserDefinedSourceTermNS of */
@@ -194,6 +197,12 @@ int dg_kernel_times(dg_ctx* ctx, int reps, double t0, double dt, double ms[5]);
  * independent FMA chains over a grid that fills every SM, timed with CUDA events: the denominator
  * of the plain FP64 form's compute roofline. Measurement helper, no reference counterpart. */
 int dg_measure_fp64_peak(double* tflops);
+
+/* Self-test of the tensor-core building blocks: C (128 x 16) = A (128 x 8) * B (16 x 8)^T, host
+ * row-major FP32 arrays, computed by tcgen05 TF32 MMAs in TMEM (split = 0: one TF32 product;
+ * split = 1: the three-term TF32 split product, about FP32 accurate). Test helper, no reference
+ * counterpart. */
+int dg_tc_selftest(const float* a, const float* b, float* c, int split);
 
 /* MaxTimeStep (DGSEMClass.f90:870-1038) on the device. */
 int dg_max_dt(dg_ctx* ctx, double cfl, double dcfl, double* dt);

@@ -117,7 +117,8 @@ def test_config3_curvilinear32_n5_full_mesh():
         o.rk3_step(s * dt, dt)
     ref = o.get(0)
     del o
-    for precision, tol in ((FP64, STATE_TOL), (MIXED, MIXED_TOL)):
+    # plain, mixed, and the mixed form with the tensor-core gradient contractions
+    for precision, tol in ((FP64, STATE_TOL), (MIXED, MIXED_TOL), (_abi.DG_PRECISION_MIXED_TC, MIXED_TOL)):
         with NavierStokesDG(mesh, _replace(cfg, precision=precision)) as g:
             g.set_state(q0)
             if precision == FP64:
