@@ -504,7 +504,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--elements", type=int, default=N_ELEM, help="elements per direction (profiling runs)")
-    ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
+    ap.add_argument("--profile", choices=["mixed", "fp64", "mixed_tc"], default=None,
                     help="profiling run: only warm-up + timed steps of one form, no extra legs")
     ap.add_argument("--workload", choices=["tgv32_curvilinear", *SECONDARY], default="tgv32_curvilinear",
                     help="the headline workload (default) or one of the other benchmark configurations")
@@ -558,7 +558,7 @@ def main():
         from horses3d_gb300.solver import NavierStokesDG
 
         mesh, q0, base = case
-        prec = 1 if args.profile == "mixed" else 0
+        prec = {"fp64": 0, "mixed": 1, "mixed_tc": 2}[args.profile]
         g = NavierStokesDG(mesh, Config(**base, precision=prec))
         g.set_state(q0)
         dt = g.max_time_step(CFL, CFL)
