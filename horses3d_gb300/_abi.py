@@ -132,6 +132,7 @@ SIGNATURES = [
                                     C.c_int, C.POINTER(DgPhysics), C.c_double, C.c_double, C.c_void_p, _f64p]),
     ("dg_max_dt_noalloc_max_dof", C.c_int64, []),
     ("dg_measure_fp64_peak", C.c_int, [_f64p]),
+    ("dg_keep_gradients", C.c_int, [C.c_void_p, C.c_int]),
     ("dg_tc_selftest", C.c_int, [C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int]),
     ("dg_create_partition", C.c_int, [C.POINTER(DgMeshDesc), C.c_int32, C.POINTER(DgPhysics), C.POINTER(DgOptions),
                                       C.POINTER(C.c_void_p)]),

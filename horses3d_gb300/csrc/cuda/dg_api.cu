@@ -163,7 +163,7 @@ cudaError_t run_stage(dg_ctx* c, int stage, double tshift, int flags) {
 cudaError_t enqueue_step(dg_ctx* c) {
     static const double b[3] = {0.0, 1.0 / 3.0, 3.0 / 4.0};
     for (int k = 0; k < 3; ++k) {
-        cudaError_t e = run_stage(c, k, b[k], k == 2 ? dg::kWriteQDot : 0);
+        cudaError_t e = run_stage(c, k, b[k], k == 2 ? (dg::kWriteQDot | (c->keep_grad ? dg::kStoreGrad : 0)) : 0);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -603,6 +603,17 @@ int dg_partition_stage(dg_ctx* c, int stage, int phase, double t, double dt) {
     CK(run_stage(c, stage, stage >= 0 ? b[stage] : 0.0, part | keep));
     CK(cudaStreamSynchronize(c->stream));
     return check_device_error(c);
+}
+
+int dg_keep_gradients(dg_ctx* c, int on) {
+    if (!c) return h3d::fail(DG_ERR_INVALID, "null context");
+    if (c->var) return h3d::fail(DG_ERR_UNSUPPORTED, "keeping the step gradients needs a uniform-order context");
+    if (!c->pc.ns) return h3d::fail(DG_ERR_INVALID, "an Euler context has no gradients");
+    if ((on != 0) != c->keep_grad) {
+        c->keep_grad = on != 0;
+        h3dctx::drop_graphs(c);  // the captured steps change
+    }
+    return DG_OK;
 }
 
 int dg_rk3_step(dg_ctx* c, double t, double dt) {

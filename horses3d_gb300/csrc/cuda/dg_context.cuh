@@ -125,6 +125,7 @@ struct dg_ctx {
     h3dctx::DevBuf<double> mon;
     h3dctx::DevBuf<int> mon_count;
     int mon_rows = 0;
+    bool keep_grad = false;  // the last stage of every step stores the lifted gradients
 
     // variable-order / multi-case path
     bool var = false;

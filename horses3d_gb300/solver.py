@@ -81,6 +81,10 @@ class NavierStokesDG:
         return self.get(_abi.DG_FIELD_QDOT)
 
     # -- the reference's operator interface --------------------------------------------------------
+    def keep_gradients(self, on: bool = True) -> None:
+        """Keep the last stage's lifted gradients of every step (get(DG_FIELD_UX..UZ)) for monitors."""
+        _abi.check(_abi.lib().dg_keep_gradients(self._h, int(on)), "dg_keep_gradients")
+
     def compute_time_derivative(self, t: float) -> None:
         _abi.check(_abi.lib().dg_rhs(self._h, float(t)), "dg_rhs")
 

@@ -168,6 +168,12 @@ int dg_rhs(dg_ctx* ctx, double t);
  * CFL stepping call dg_max_dt first, as the reference's time loop does (TimeIntegrator.f90:748-754). */
 int dg_rk3_step(dg_ctx* ctx, double t, double dt);
 
+/* Keeps the lifted gradients U_x, U_y, U_z of the last RK stage of every step (dg_download of
+ * DG_FIELD_UX..UZ after the step), which the reference's storage holds after TakeRK3Step and its
+ * monitors read (enstrophy, VolumeIntegrals.f90:267). Off by default: it writes 15 values per node
+ * per step. Navier-Stokes uniform-order contexts. */
+int dg_keep_gradients(dg_ctx* ctx, int on);
+
 /* n RK3 steps from t0 entirely on the device, captured once in a CUDA graph and replayed: no host
  * synchronisation between steps. dt > 0: fixed step. dt <= 0: every step takes the MaxTimeStep
  * value for (cfl, dcfl), computed and applied on the device. t_end (may be NULL) receives the final

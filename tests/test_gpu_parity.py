@@ -389,17 +389,24 @@ def test_taylor_green_reaches_the_reference_goldens(test):
     """NavierStokes TaylorGreen and Euler TaylorGreenKEPEC on the GPU (FP64, 32^3 elements, N=3):
     through the reference-shaped driver the five residuals (tol 1e-7 on value + 1), the kinetic
     energy (1e-11), its rate and, for the Euler case, the entropy rate (1e-11 on value + 1) equal the
-    goldens. The enstrophy golden reads the gradients of the last stage, which the step kernels do
-    not store; the oracle test pins it."""
+    goldens, and for the NavierStokes case the enstrophy (1e-11) from the lifted gradients of the last
+    stage, which the steps keep on request (dg_keep_gradients)."""
     mesh, cfg, q0 = cases.taylor_green_reference_case(test)
     g = NavierStokesDG(mesh, cfg)
     g.set_state(q0)
+    if cfg.flow == "ns":
+        g.keep_gradients(True)
     rep = g.integrate_in_time(t0=0.0)
     gold = cases.TAYLOR_GREEN_GOLDENS[test]
     assert rep.iterations == cfg.n_steps
     assert cases.ftassert_close(gold["residuals"], rep.residuals, 1e-7), rep.residuals - gold["residuals"]
     q, qdot = g.Q, g.QDot
-    ke, rate, _ = cases.volume_monitors(mesh, q, qdot)
+    if cfg.flow == "ns":
+        ke, rate, ens = cases.volume_monitors(mesh, q, qdot, g.get(_abi.DG_FIELD_UX), g.get(_abi.DG_FIELD_UY),
+                                              g.get(_abi.DG_FIELD_UZ))
+        assert cases.ftassert_equal(gold["enstrophy"], ens, 1e-11), ens - gold["enstrophy"]
+    else:
+        ke, rate, _ = cases.volume_monitors(mesh, q, qdot)
     assert cases.ftassert_equal(gold["kinetic_energy"], ke, 1e-11), ke - gold["kinetic_energy"]
     assert cases.ftassert_close(gold["kinetic_energy_rate"], rate, 1e-11), rate - gold["kinetic_energy_rate"]
     if "entropy_rate" in gold:
