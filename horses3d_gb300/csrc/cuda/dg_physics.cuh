@@ -200,54 +200,56 @@ __device__ __forceinline__ void viscous_flux(const PhysR<R>& p, const R* Q, cons
     F[2][4] = txz * u + tyz * v + tzz * w + kappa * nTz;
 }
 
-// RiemannSolvers_NS.f90:1541-1655 RoeRiemannSolver (with its entropy fix).
+// RiemannSolvers_NS.f90:1541-1655 RoeRiemannSolver (with its entropy fix): the upwind side's flux
+// plus the one acoustic wave that can change sign, evaluated at the Roe-averaged state.
 template <typename R>
 __device__ __forceinline__ void roe_flux(const PhysR<R>& p, const R* QL, const R* QR, const R* n, R* flux) {
     const R gm1 = p.gamma - R(1);
-    const R rho = QL[0], rhon = QR[0];
-    const R ul = QL[1] / rho, vl = QL[2] / rho, wl = QL[3] / rho;
-    const R pleft = gm1 * (QL[4] - R(0.5) / rho * (QL[1] * QL[1] + QL[2] * QL[2] + QL[3] * QL[3]));
-    const R ur = QR[1] / rhon, vr = QR[2] / rhon, wr = QR[3] / rhon;
-    const R pright = gm1 * (QR[4] - R(0.5) / rhon * (QR[1] * QR[1] + QR[2] * QR[2] + QR[3] * QR[3]));
-    const R ql = n[0] * ul + n[1] * vl + n[2] * wl;
-    const R qr = n[0] * ur + n[1] * vr + n[2] * wr;
-    const R hl = R(0.5) * (ul * ul + vl * vl + wl * wl) + p.g_over_gm1 * (pleft + p.p_ref) / rho;
-    const R hr = R(0.5) * (ur * ur + vr * vr + wr * wr) + p.g_over_gm1 * (pright + p.p_ref) / rhon;
-    const R rtd = dsqrt(rho * rhon);
-    const R betal = rho / (rho + rtd), betar = R(1) - betal;
-    const R utd = betal * ul + betar * ur, vtd = betal * vl + betar * vr, wtd = betal * wl + betar * wr;
-    const R htd = betal * hl + betar * hr;
-    const R atd2 = gm1 * (htd - R(0.5) * (utd * utd + vtd * vtd + wtd * wtd));
-    const R atd = dsqrt(atd2);
-    const R qtd = utd * n[0] + vtd * n[1] + wtd * n[2];
-    if (qtd >= R(0)) {
-        const R dw1 = R(0.5) * ((pright - pleft) / atd2 - (qr - ql) * rtd / atd);
-        const R sp1 = qtd - atd;
-        const R sp1m = sp1 < R(0) ? sp1 : R(0);
-        const R hd1m = (p.gp1_over_4 * atd / rtd) * dw1;
-        const R eta0 = -fabs(sp1) - hd1m;
-        const R eta1 = eta0 > R(0) ? eta0 : R(0);
-        const R udw1 = dw1 * (sp1m - R(0.5) * eta1);
-        const R rql = rho * ql;
-        flux[0] = rql + udw1;
-        flux[1] = rql * ul + pleft * n[0] + udw1 * (utd - atd * n[0]);
-        flux[2] = rql * vl + pleft * n[1] + udw1 * (vtd - atd * n[1]);
-        flux[3] = rql * wl + pleft * n[2] + udw1 * (wtd - atd * n[2]);
-        flux[4] = rql * hl + udw1 * (htd - qtd * atd);
-    } else {
-        const R dw4 = R(0.5) * ((pright - pleft) / atd2 + (qr - ql) * rtd / atd);
-        const R sp4 = qtd + atd;
-        const R sp4p = sp4 > R(0) ? sp4 : R(0);
-        const R hd4 = (p.gp1_over_4 * atd / rtd) * dw4;
-        const R eta0 = -fabs(sp4) + hd4;
-        const R eta4 = eta0 > R(0) ? eta0 : R(0);
-        const R udw4 = dw4 * (sp4p + R(0.5) * eta4);
-        const R rqr = rhon * qr;
-        flux[0] = rqr - udw4;
-        flux[1] = rqr * ur + pright * n[0] - udw4 * (utd + atd * n[0]);
-        flux[2] = rqr * vr + pright * n[1] - udw4 * (vtd + atd * n[1]);
-        flux[3] = rqr * wr + pright * n[2] - udw4 * (wtd + atd * n[2]);
-        flux[4] = rqr * hr - udw4 * (htd + qtd * atd);
+    const R rL = QL[0], rR = QR[0];
+    const R uL = QL[1] / rL, vL = QL[2] / rL, wL = QL[3] / rL;
+    const R prL = gm1 * (QL[4] - R(0.5) / rL * (QL[1] * QL[1] + QL[2] * QL[2] + QL[3] * QL[3]));
+    const R uR = QR[1] / rR, vR = QR[2] / rR, wR = QR[3] / rR;
+    const R prR = gm1 * (QR[4] - R(0.5) / rR * (QR[1] * QR[1] + QR[2] * QR[2] + QR[3] * QR[3]));
+    const R vnL = n[0] * uL + n[1] * vL + n[2] * wL;  // normal velocities
+    const R vnR = n[0] * uR + n[1] * vR + n[2] * wR;
+    const R HL = R(0.5) * (uL * uL + vL * vL + wL * wL) + p.g_over_gm1 * (prL + p.p_ref) / rL;  // total enthalpies
+    const R HR = R(0.5) * (uR * uR + vR * vR + wR * wR) + p.g_over_gm1 * (prR + p.p_ref) / rR;
+    // Roe average: weights sqrt(rho) / (sqrt(rhoL) + sqrt(rhoR)) in the form rhoL / (rhoL + sqrt(rhoL rhoR))
+    const R r_avg = dsqrt(rL * rR);
+    const R wgtL = rL / (rL + r_avg), wgtR = R(1) - wgtL;
+    const R ua = wgtL * uL + wgtR * uR, va = wgtL * vL + wgtR * vR, wa = wgtL * wL + wgtR * wR;
+    const R Ha = wgtL * HL + wgtR * HR;
+    const R ca2 = gm1 * (Ha - R(0.5) * (ua * ua + va * va + wa * wa));
+    const R ca = dsqrt(ca2);
+    const R vna = ua * n[0] + va * n[1] + wa * n[2];
+    if (vna >= R(0)) {  // left state upwind; the u - c wave
+        const R amp = R(0.5) * ((prR - prL) / ca2 - (vnR - vnL) * r_avg / ca);
+        const R lam = vna - ca;
+        const R lam_neg = lam < R(0) ? lam : R(0);
+        const R spread = (p.gp1_over_4 * ca / r_avg) * amp;  // entropy fix: the wave speeds' jump
+        const R fix0 = -fabs(lam) - spread;
+        const R fix = fix0 > R(0) ? fix0 : R(0);
+        const R wave = amp * (lam_neg - R(0.5) * fix);
+        const R mflux = rL * vnL;
+        flux[0] = mflux + wave;
+        flux[1] = mflux * uL + prL * n[0] + wave * (ua - ca * n[0]);
+        flux[2] = mflux * vL + prL * n[1] + wave * (va - ca * n[1]);
+        flux[3] = mflux * wL + prL * n[2] + wave * (wa - ca * n[2]);
+        flux[4] = mflux * HL + wave * (Ha - vna * ca);
+    } else {  // right state upwind; the u + c wave
+        const R amp = R(0.5) * ((prR - prL) / ca2 + (vnR - vnL) * r_avg / ca);
+        const R lam = vna + ca;
+        const R lam_pos = lam > R(0) ? lam : R(0);
+        const R spread = (p.gp1_over_4 * ca / r_avg) * amp;
+        const R fix0 = -fabs(lam) + spread;
+        const R fix = fix0 > R(0) ? fix0 : R(0);
+        const R wave = amp * (lam_pos + R(0.5) * fix);
+        const R mflux = rR * vnR;
+        flux[0] = mflux - wave;
+        flux[1] = mflux * uR + prR * n[0] - wave * (ua + ca * n[0]);
+        flux[2] = mflux * vR + prR * n[1] - wave * (va + ca * n[1]);
+        flux[3] = mflux * wR + prR * n[2] - wave * (wa + ca * n[2]);
+        flux[4] = mflux * HR - wave * (Ha + vna * ca);
     }
 }
 
@@ -404,25 +406,25 @@ __device__ __forceinline__ void lxf_flux(const PhysR<R>& p, const R* QL, const R
 template <typename R>
 __device__ __forceinline__ void rusanov_flux(const PhysR<R>& p, const R* QL, const R* QR, const R* n, R* flux) {
     const R gm1 = p.gamma - R(1);
-    const R rho = QL[0], rhon = QR[0];
-    const R ul = QL[1] / rho, vl = QL[2] / rho, wl = QL[3] / rho;
-    const R pleft = gm1 * (QL[4] - R(0.5) / rho * (QL[1] * QL[1] + QL[2] * QL[2] + QL[3] * QL[3]));
-    const R ur = QR[1] / rhon, vr = QR[2] / rhon, wr = QR[3] / rhon;
-    const R pright = gm1 * (QR[4] - R(0.5) / rhon * (QR[1] * QR[1] + QR[2] * QR[2] + QR[3] * QR[3]));
-    const R ql = n[0] * ul + n[1] * vl + n[2] * wl;
-    const R qr = n[0] * ur + n[1] * vr + n[2] * wr;
-    const R kl = R(0.5) * (ul * ul + vl * vl + wl * wl), kr = R(0.5) * (ur * ur + vr * vr + wr * wr);
-    const R hl = kl + p.g_over_gm1 * (pleft + p.p_ref) / rho;
-    const R hr = kr + p.g_over_gm1 * (pright + p.p_ref) / rhon;
-    const R ar = dsqrt(gm1 * (hr - kr)), al = dsqrt(gm1 * (hl - kl));
-    const R rql = rho * ql, rqr = rhon * qr;
+    const R rL = QL[0], rR = QR[0];
+    const R uL = QL[1] / rL, vL = QL[2] / rL, wL = QL[3] / rL;
+    const R prL = gm1 * (QL[4] - R(0.5) / rL * (QL[1] * QL[1] + QL[2] * QL[2] + QL[3] * QL[3]));
+    const R uR = QR[1] / rR, vR = QR[2] / rR, wR = QR[3] / rR;
+    const R prR = gm1 * (QR[4] - R(0.5) / rR * (QR[1] * QR[1] + QR[2] * QR[2] + QR[3] * QR[3]));
+    const R vnL = n[0] * uL + n[1] * vL + n[2] * wL;
+    const R vnR = n[0] * uR + n[1] * vR + n[2] * wR;
+    const R keL = R(0.5) * (uL * uL + vL * vL + wL * wL), keR = R(0.5) * (uR * uR + vR * vR + wR * wR);
+    const R HL = keL + p.g_over_gm1 * (prL + p.p_ref) / rL;
+    const R HR = keR + p.g_over_gm1 * (prR + p.p_ref) / rR;
+    const R cR = dsqrt(gm1 * (HR - keR)), cL = dsqrt(gm1 * (HL - keL));
+    const R mL = rL * vnL, mR = rR * vnR;  // normal mass fluxes
     R f[5];
-    f[0] = rql + rqr;
-    f[1] = rql * ul + pleft * n[0] + rqr * ur + pright * n[0];
-    f[2] = rql * vl + pleft * n[1] + rqr * vr + pright * n[1];
-    f[3] = rql * wl + pleft * n[2] + rqr * wr + pright * n[2];
-    f[4] = rql * hl + rqr * hr;
-    const R sR = ar + fabs(qr), sL = al + fabs(ql);
+    f[0] = mL + mR;
+    f[1] = mL * uL + prL * n[0] + mR * uR + prR * n[0];
+    f[2] = mL * vL + prL * n[1] + mR * vR + prR * n[1];
+    f[3] = mL * wL + prL * n[2] + mR * wR + prR * n[2];
+    f[4] = mL * HL + mR * HR;
+    const R sR = cR + fabs(vnR), sL = cL + fabs(vnL);
     const R smax = sR > sL ? sR : sL;
 #pragma unroll
     for (int v = 0; v < 5; ++v) flux[v] = (f[v] - smax * (QR[v] - QL[v])) / R(2);
