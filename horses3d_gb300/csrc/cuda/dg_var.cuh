@@ -39,6 +39,7 @@ namespace dg {
 template <typename R>
 struct OpsP {
     R D[kMaxP * kMaxP], hatD[kMaxP * kMaxP];
+    R sharpD[kMaxP * kMaxP];  // split form (Gauss-Lobatto nodes); zero otherwise
     R vL[kMaxP], vR[kMaxP], bL[kMaxP], bR[kMaxP];
 };
 
@@ -59,6 +60,7 @@ struct VArgs {
     int n_items, n_faces, cap;  // cap: largest node count of an item
     int ns, source;
     int riemann, averaging, grad_vars;  // the host's copies of the solver, average and gradient variables
+    int split;                          // split-form volume integral (Gauss-Lobatto nodes)
     int item0;                     // first item of the launch (the grid covers one class)
     int cls[kItemClasses + 1];     // class c holds items [cls[c], cls[c+1])
     int ccap[kItemClasses];        // largest node count of an item of class c (its shared memory)
@@ -244,6 +246,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 0) kv_volume(VArgs<R
     OpsP<R>* sO = reinterpret_cast<OpsP<R>*>(vsm);  // xi, eta, zeta operators
     R* sQ = reinterpret_cast<R*>(sO + 3);            // 5*ntot: state
     R* sG = sQ + 5 * ntot;                           // 15*ntot: lifted gradient, then the fluxes
+    R* sM = sG + 15 * ntot;                          // split form: 9*ntot metric terms
     load_ops(a.ops, sO, px, py, pz);
     const PhysR<R> ph = a.ph[d.kase];
     const double eref = a.cc[d.kase].e_ref;
@@ -370,7 +373,22 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 0) kv_volume(VArgs<R
             jz[c] = a.ja_zeta[3 * g + c];
         }
         R F[3][5];
-        euler_contravariant(ph, q, jx, je, jz, F);
+        if (a.split) {
+            // split form: the viscous contravariant fluxes here; the two-point fluxes below read
+            // every node's state and metric terms from shared memory
+#pragma unroll
+            for (int dd = 0; dd < 3; ++dd)
+#pragma unroll
+                for (int v = 0; v < 5; ++v) F[dd][v] = R(0);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                sM[c * ntot + t] = jx[c];
+                sM[(3 + c) * ntot + t] = je[c];
+                sM[(6 + c) * ntot + t] = jz[c];
+            }
+        } else {
+            euler_contravariant(ph, q, jx, je, jz, F);
+        }
         if (a.ns) {
             R Ug[15];
 #pragma unroll
@@ -380,18 +398,75 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 0) kv_volume(VArgs<R
             R Cv[3][5];
             viscous_flux(ph, q, Ug, Ug + 5, Ug + 10, mu, kap, Cv);
             const R* ja[3] = {jx, je, jz};
+            const R sgn = a.split ? R(1) : R(-1);  // split: Fv; standard: Finv - Fv
 #pragma unroll
             for (int dd = 0; dd < 3; ++dd)
 #pragma unroll
                 for (int v = 0; v < 5; ++v)
-                    F[dd][v] = F[dd][v] - (Cv[0][v] * ja[dd][0] + Cv[1][v] * ja[dd][1] + Cv[2][v] * ja[dd][2]);
+                    F[dd][v] = F[dd][v] + sgn * (Cv[0][v] * ja[dd][0] + Cv[1][v] * ja[dd][1] + Cv[2][v] * ja[dd][2]);
         }
 #pragma unroll
         for (int dd = 0; dd < 3; ++dd)
 #pragma unroll
             for (int v = 0; v < 5; ++v) sG[(v + 5 * dd) * ntot + t] = F[dd][v];
+        if (a.split && gv) {  // the state in place of the gradient variables
+#pragma unroll
+            for (int v = 0; v < 5; ++v) sQ[v * ntot + t] = q[v];
+        }
     }
     __syncthreads();
+    if (a.split) {
+        // Split form with per-direction orders (HyperbolicSplitForm.f90:64-116, DGIntegrals.f90:92-129):
+        // along each direction's line, volInt += sharpD(i,l) f#(l,i) + hatD(i,l) Fv(l), with the
+        // two-point flux of each pair evaluated with the lower line index as "left" and the node's
+        // own contravariant Euler flux at l = i; QDot = -volInt.
+        for (int t = threadIdx.x; t < ntot; t += blockDim.x) {
+            const int le = t / np, n = t - le * np;
+            const int i = n % px, j = (n / px) % py, k = n / (px * py);
+            const long long g = a.eoff[a.item_elems[d.first + le]] + n;
+            const int b0 = le * np;
+            R q[5], jm[3][3];
+#pragma unroll
+            for (int v = 0; v < 5; ++v) q[v] = sQ[v * ntot + t];
+#pragma unroll
+            for (int dd = 0; dd < 3; ++dd)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) jm[dd][c] = sM[(3 * dd + c) * ntot + t];
+            R Fi[3][5];
+            euler_contravariant(ph, q, jm[0], jm[1], jm[2], Fi);
+            R acc[5] = {0, 0, 0, 0, 0};
+#pragma unroll
+            for (int dd = 0; dd < 3; ++dd) {
+                const int len = dd == 0 ? px : (dd == 1 ? py : pz);
+                const int self = dd == 0 ? i : (dd == 1 ? j : k);
+                const int stride = dd == 0 ? 1 : (dd == 1 ? px : px * py);
+                const int first = n - self * stride;
+                for (int l = 0; l < len; ++l) {
+                    const int m = b0 + first + l * stride;
+                    R fs[5];
+                    if (l == self) {
+#pragma unroll
+                        for (int v = 0; v < 5; ++v) fs[v] = Fi[dd][v];
+                    } else {
+                        R qo[5], jo[3];
+#pragma unroll
+                        for (int v = 0; v < 5; ++v) qo[v] = sQ[v * ntot + m];
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) jo[c] = sM[(3 * dd + c) * ntot + m];
+                        if (self < l) two_point_flux(ph, q, qo, jm[dd], jo, fs);
+                        else two_point_flux(ph, qo, q, jo, jm[dd], fs);
+                    }
+                    const R sh = sO[dd].sharpD[self * kMaxP + l];
+                    const R h = sO[dd].hatD[self * kMaxP + l];
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) acc[v] = acc[v] + sh * fs[v] + h * sG[(v + 5 * dd) * ntot + m];
+                }
+            }
+#pragma unroll
+            for (int v = 0; v < 5; ++v) a.QDot[5 * g + v] = -acc[v];
+        }
+        return;
+    }
     // ScalarWeakIntegrals_StdVolumeGreen
     for (int t = threadIdx.x; t < ntot; t += blockDim.x) {
         const int le = t / np, n = t - le * np;
@@ -1196,7 +1271,7 @@ cudaError_t launch_items(const VArgs<R>& a0, int which, cudaStream_t s, int stor
         VArgs<R> a = a0;
         a.item0 = a0.cls[c];
         const int cap = a0.ccap[c];
-        const size_t smem = which >= 2 ? vupdate_smem<R>(cap) : vitem_smem<R>(cap, which == 1 ? 20 : 5);
+        const size_t smem = which >= 2 ? vupdate_smem<R>(cap) : vitem_smem<R>(cap, which == 1 ? (a0.split ? 29 : 20) : 5);
         cudaError_t e;
         switch (c) {
             case 0: e = launch_item_class<R, 0>(a, which, n, smem, s, store_grad, stage, tshift, wq, cap); break;
@@ -1233,7 +1308,7 @@ cudaError_t set_item_attributes(size_t vol, size_t upd, size_t trc) {
 
 template <typename R>
 cudaError_t vrun_stage(const VArgs<R>& a, int stage, double tshift, int flags, cudaStream_t s) {
-    const size_t vol = vitem_smem<R>(a.cap, 20), trc = vitem_smem<R>(a.cap, 5);
+    const size_t vol = vitem_smem<R>(a.cap, a.split ? 29 : 20), trc = vitem_smem<R>(a.cap, 5);
     const size_t upd = std::max(vupdate_smem<R>(a.cap), vupdate_smem<R>(std::min(a.cap, kStageNodes)));
     if (stage == kPrepare) {
         cudaError_t e;

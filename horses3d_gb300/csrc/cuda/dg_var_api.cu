@@ -151,6 +151,7 @@ int setup_vstore(dg_ctx* c, h3dctx::VStore<R>& st, const Gathered& h) {
             for (int l = 0; l < P; ++l) {
                 ops[P].D[i * dg::kMaxP + l] = static_cast<R>(ns.D[i * P + l]);
                 ops[P].hatD[i * dg::kMaxP + l] = static_cast<R>(ns.hatD[i * P + l]);
+                if (c->nodes == DG_NODES_GAUSS_LOBATTO) ops[P].sharpD[i * dg::kMaxP + l] = static_cast<R>(ns.sharpD[i * P + l]);
             }
             ops[P].vL[i] = static_cast<R>(ns.vL[i]);
             ops[P].vR[i] = static_cast<R>(ns.vR[i]);
@@ -211,6 +212,7 @@ int setup_vstore(dg_ctx* c, h3dctx::VStore<R>& st, const Gathered& h) {
     a.riemann = c->pc.riemann;
     a.averaging = c->pc.averaging;
     a.grad_vars = c->pc.grad_vars;
+    a.split = c->opt.inviscid == DG_INVISCID_SPLIT ? 1 : 0;
     a.items = c->items.p;
     a.item_elems = c->item_elems.p;
     a.eord = c->eord.p;
@@ -451,8 +453,8 @@ int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, cons
     if (!out) return h3d::fail(DG_ERR_INVALID, "null output pointer");
     *out = nullptr;
     if (n_cases < 1 || !meshes || !phys || !op) return h3d::fail(DG_ERR_INVALID, "null argument or no case");
-    if (op->inviscid != DG_INVISCID_STANDARD)
-        return h3d::fail(DG_ERR_UNSUPPORTED, "the variable-order path implements the standard (weak) volume form");
+    if (op->inviscid != DG_INVISCID_STANDARD && op->inviscid != DG_INVISCID_SPLIT)
+        return h3d::fail(DG_ERR_UNSUPPORTED, "inviscid discretization");
     if (op->riemann < DG_RIEMANN_ROE || op->riemann > DG_RIEMANN_U_DISS) return h3d::fail(DG_ERR_UNSUPPORTED, "riemann solver");
     if (op->averaging < DG_AVG_STANDARD || op->averaging > DG_AVG_CHANDRASEKAR)
         return h3d::fail(DG_ERR_UNSUPPORTED, "averaging");
@@ -467,6 +469,8 @@ int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, cons
         if (rc) return rc;
         if (meshes[k].node_type != meshes[0].node_type)
             return h3d::fail(DG_ERR_UNSUPPORTED, "all cases of a batch need the same node type");
+        if (op->inviscid == DG_INVISCID_SPLIT && meshes[k].node_type != DG_NODES_GAUSS_LOBATTO)
+            return h3d::fail(DG_ERR_INVALID, "the split form needs Gauss-Lobatto nodes");
         if ((phys[k].navier_stokes != 0) != (phys[0].navier_stokes != 0))
             return h3d::fail(DG_ERR_UNSUPPORTED, "all cases of a batch need the same equations (Euler or NS)");
     }

@@ -363,3 +363,51 @@ def test_update_store_paths_agree_bit_for_bit(tmp_path):
                        timeout=600)
         out[cap] = np.load(dst)
     assert np.array_equal(out[64], out[512])
+
+
+# ---- split form on p-anisotropic meshes (HyperbolicSplitForm.f90:64-116 works per direction with
+# the element's orders e%Nxyz(1..3)) ----
+def _split(cfg, averaging):
+    import dataclasses
+
+    return dataclasses.replace(cfg, inviscid=_abi.DG_INVISCID_SPLIT, averaging=averaging)
+
+
+@pytest.mark.parametrize("averaging", [_abi.DG_AVG_PIROZZOLI, _abi.DG_AVG_CHANDRASEKAR])
+def test_split_form_anisotropic_ns(averaging):
+    """Taylor-Green on a warped box with per-element orders 1..5 on Gauss-Lobatto nodes, LxF: one
+    right-hand side (1e-10, gradients too) and three RK3 steps (1e-12) against the oracle."""
+    mesh, cfg, q0 = cases.aniso_tgv_case(n=3, lo=1, hi=5, seed=12, nodes=_abi.DG_NODES_GAUSS_LOBATTO,
+                                         riemann=_abi.DG_RIEMANN_LXF, warp=0.1)
+    cfg = _split(cfg, averaging)
+    _check_rhs(mesh, cfg, q0)
+    o, g = _pair(mesh, cfg, q0)
+    t, dt = 0.0, 2e-3
+    for _ in range(3):
+        o.rk3_step(t, dt)
+        g.take_rk3_step(t, dt)
+        t += dt
+    err = rel_l2(g.Q, o.get(0), mesh.quadrature_weights())
+    assert np.all(err <= STATE_TOL), err
+
+
+def test_split_form_anisotropic_euler_and_mixed():
+    """Euler vortex with per-element orders 2..6 (Gauss-Lobatto, Pirozzoli): the plain form within
+    1e-12 and the mixed form within 1e-6 of the oracle after five steps."""
+    for precision, tol in ((_abi.DG_PRECISION_FP64, STATE_TOL), (_abi.DG_PRECISION_MIXED, MIXED_TOL)):
+        mesh, cfg, q0 = cases.aniso_vortex_case(n=3, lo=2, hi=6, seed=13, nodes=_abi.DG_NODES_GAUSS_LOBATTO,
+                                                precision=precision)
+        cfg = _split(cfg, _abi.DG_AVG_PIROZZOLI)
+        o, g = _pair(mesh, cfg, q0)
+        dt = 5e-3
+        for s in range(5):
+            o.rk3_step(s * dt, dt)
+        g.run_steps(5, 0.0, dt=dt)
+        err = rel_l2(g.Q, o.get(0), mesh.quadrature_weights())
+        assert np.all(err <= tol), (precision, err)
+
+
+def test_split_form_needs_gauss_lobatto_nodes():
+    mesh, cfg, _ = cases.aniso_tgv_case(n=2, lo=1, hi=3, seed=1, nodes=_abi.DG_NODES_GAUSS)
+    with pytest.raises(_abi.DgError, match="Gauss-Lobatto"):
+        NavierStokesDG(mesh, _split(cfg, _abi.DG_AVG_PIROZZOLI))
