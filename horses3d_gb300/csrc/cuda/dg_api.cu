@@ -160,17 +160,24 @@ cudaError_t run_stage(dg_ctx* c, int stage, double tshift, int flags) {
 
 // Queue one RK3 step (time and dt are read from device memory). The last stage keeps its QDot for
 // the residuals, as TakeRK3Step leaves the third stage's QDot in storage.
-cudaError_t enqueue_step(dg_ctx* c) {
+cudaError_t enqueue_step(dg_ctx* c, bool fuse_monitor = false) {
     static const double b[3] = {0.0, 1.0 / 3.0, 3.0 / 4.0};
     for (int k = 0; k < 3; ++k) {
-        cudaError_t e = run_stage(c, k, b[k], k == 2 ? (dg::kWriteQDot | (c->keep_grad ? dg::kStoreGrad : 0)) : 0);
+        const int last = dg::kWriteQDot | (c->keep_grad ? dg::kStoreGrad : 0) | (fuse_monitor ? dg::kFuseMonitor : 0);
+        cudaError_t e = run_stage(c, k, b[k], k == 2 ? last : 0);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
 }
 
-cudaError_t enqueue_max_dt(dg_ctx* c, double cfl, double dcfl) {
-    if (c->var) return h3dvar::enqueue_max_dt(c, cfl, dcfl);
+// The monitored time loop can take its residuals, NaN test and MaxTimeStep estimate from the last
+// stage's update (uniform orders with the bulk-copy update, whole meshes).
+bool fused_monitor(const dg_ctx* c) {
+    if (c->var || c->n_ghost != 0) return false;
+    return c->mixed ? c->s32.mon.begin != nullptr : c->s64.mon.begin != nullptr;
+}
+
+dg::DtArgs dt_args(dg_ctx* c, double cfl, double dcfl) {
     dg::DtArgs d;
     d.ndof = c->ndof;
     d.cfl = cfl;
@@ -181,6 +188,37 @@ cudaError_t enqueue_max_dt(dg_ctx* c, double cfl, double dcfl) {
     d.S_div_TRef = c->pc.S_div_TRef; d.TReNorm = c->pc.TReNorm;
     d.Q = c->Q.p;
     d.red = c->red.p;
+    return d;
+}
+
+// Points the kernel arguments at the monitor records and the time-step constants of (cfl, dcfl).
+int setup_fused_monitor(dg_ctx* c, double cfl, double dcfl) {
+    if (!c->mon_part.p) CK(c->mon_part.alloc(8 * static_cast<size_t>(c->K)));
+    const dg::DtConst32 c32 = dg::dt_const32(cfl, dcfl, c->dxi, c->pc.gamma, c->pc.gm1, c->pc.gammaM2, c->pc.S_div_TRef,
+                                             c->pc.TReNorm, c->pc.ns);
+    c->s32.args.mon = c->mon_part.p;
+    c->s32.args.dtc = c32;
+    c->s64.args.mon = c->mon_part.p;
+    c->s64.args.dtc = c32;
+    return DG_OK;
+}
+
+cudaError_t enqueue_monitor_begin(dg_ctx* c) {
+    return c->mixed ? c->s32.mon.begin(c->s32.args, c->red.p, c->nan_flag.p, c->stream)
+                    : c->s64.mon.begin(c->s64.args, c->red.p, c->nan_flag.p, c->stream);
+}
+
+cudaError_t enqueue_max_dt_fused(dg_ctx* c, double cfl, double dcfl) {
+    const dg::DtArgs d = dt_args(c, cfl, dcfl);
+    cudaError_t e = c->mixed ? c->s32.mon.exact(c->s32.args, d, c->stream) : c->s64.mon.exact(c->s64.args, d, c->stream);
+    if (e != cudaSuccess) return e;
+    dg::k_dt_final<<<1, 1, 0, c->stream>>>(c->red.p, c->scal.p + 1);
+    return cudaGetLastError();
+}
+
+cudaError_t enqueue_max_dt(dg_ctx* c, double cfl, double dcfl) {
+    if (c->var) return h3dvar::enqueue_max_dt(c, cfl, dcfl);
+    const dg::DtArgs d = dt_args(c, cfl, dcfl);
     const dg::DtConst32 c32 = dg::dt_const32(cfl, dcfl, c->dxi, d.gamma, d.gm1, d.gammaM2, d.S_div_TRef, d.TReNorm, d.ns);
     const int blocks = dg::kDtBlocks;
     if (c->mixed) {
@@ -465,10 +503,12 @@ int create_uniform(const dg_mesh_desc* m, int n_ghost, const dg_physics* ph, con
     if (c->mixed) {
         if ((rc = setup_store(c, c->s32, m))) return bail(rc);
         c->s32.args.tc = op->precision == DG_PRECISION_MIXED_TC ? 1 : 0;
+        c->s32.mon = dg::monitor_fns_fp32(c->P, c->nodes == DG_NODES_GAUSS_LOBATTO);
         c->s32.stage = dg::stage_fn_fp32(c->P, c->nodes == DG_NODES_GAUSS_LOBATTO);
         c->s32.times = dg::times_fn_fp32(c->P, c->nodes == DG_NODES_GAUSS_LOBATTO);
     } else {
         if ((rc = setup_store(c, c->s64, m))) return bail(rc);
+        c->s64.mon = dg::monitor_fns_fp64(c->P, c->nodes == DG_NODES_GAUSS_LOBATTO);
         c->s64.stage = dg::stage_fn_fp64(c->P, c->nodes == DG_NODES_GAUSS_LOBATTO);
         c->s64.times = dg::times_fn_fp64(c->P, c->nodes == DG_NODES_GAUSS_LOBATTO);
     }
@@ -492,7 +532,7 @@ void dg_destroy(dg_ctx* c) {
     c->Q.free(); c->G.free(); c->x.free(); c->scal.free(); c->red.free(); c->nan_flag.free(); c->err_flag.free();
     c->face_elem.free(); c->face_side.free(); c->face_rot.free(); c->nb_slot.free(); c->nb_map.free();
     c->mon.free(); c->mon_count.free(); c->esum.free(); c->dt_bmin.free();
-    c->halo_send.free(); c->halo_recv.free();
+    c->halo_send.free(); c->halo_recv.free(); c->mon_part.free();
     if (c->h_scal) cudaFreeHost(c->h_scal);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -643,10 +683,15 @@ int prepare_graph(dg_ctx* c, int mode, double cfl, double dcfl) {
     if (c->graph) cudaGraphExecDestroy(c->graph);
     c->graph = nullptr;
     cudaGraph_t g = nullptr;
+    const bool fused = fused_monitor(c);
+    if (fused) {
+        int rc = setup_fused_monitor(c, cfl, dcfl);
+        if (rc) return rc;
+    }
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
-    if (mode == 1) e = enqueue_max_dt(c, cfl, dcfl);
-    if (e == cudaSuccess) e = enqueue_step(c);
+    if (mode == 1) e = fused ? enqueue_max_dt_fused(c, cfl, dcfl) : enqueue_max_dt(c, cfl, dcfl);
+    if (e == cudaSuccess) e = enqueue_step(c, fused);
     if (e == cudaSuccess) {
         if (c->var) {
             e = h3dvar::enqueue_advance_time(c);
@@ -678,10 +723,15 @@ int prepare_monitor_graph(dg_ctx* c, int mode, double cfl, double dcfl) {
     if (c->mgraph) cudaGraphExecDestroy(c->mgraph);
     c->mgraph = nullptr;
     cudaGraph_t g = nullptr;
+    const bool fused = fused_monitor(c);
+    if (fused) {
+        int rc = setup_fused_monitor(c, cfl, dcfl);
+        if (rc) return rc;
+    }
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
-    if (mode == 1) e = enqueue_max_dt(c, cfl, dcfl);
-    if (e == cudaSuccess) e = enqueue_step(c);
+    if (mode == 1) e = fused ? enqueue_max_dt_fused(c, cfl, dcfl) : enqueue_max_dt(c, cfl, dcfl);
+    if (e == cudaSuccess) e = enqueue_step(c, fused);
     if (e == cudaSuccess) {
         if (c->var) {
             e = h3dvar::enqueue_advance_time(c);
@@ -701,7 +751,12 @@ int prepare_monitor_graph(dg_ctx* c, int mode, double cfl, double dcfl) {
         } else {
             e = cudaMemsetAsync(c->red.p + 2, 0, 5 * sizeof(unsigned long long), c->stream);
             if (e == cudaSuccess) e = cudaMemsetAsync(c->nan_flag.p, 0, sizeof(int), c->stream);
-            if (e == cudaSuccess) {
+            if (e == cudaSuccess && fused) {
+                dg::k_monitor_fold<<<dg::kFoldBlocks, 256, 0, c->stream>>>(c->mon_part.p, c->K, c->red.p, c->nan_flag.p);
+                dg::k_record_monitor<<<1, 1, 0, c->stream>>>(c->red.p, 0, c->nan_flag.p, 1, c->mon.p, c->mon_count.p,
+                                                             c->mon_rows);
+                e = cudaGetLastError();
+            } else if (e == cudaSuccess) {
                 if (c->mixed)
                     dg::k_residuals<float><<<152 * 4, 256, 0, c->stream>>>(c->ndof, c->s32.QDot.p, c->Q.p, c->red.p + 2,
                                                                            c->nan_flag.p);
@@ -800,7 +855,13 @@ int integrate_core(dg_ctx* c, int n, int mode, double cfl, double dcfl, double* 
     int rc = prepare_monitor_graph(c, mode, cfl, dcfl);
     if (rc) return rc;
     CK(cudaMemsetAsync(c->mon_count.p, 0, sizeof(int), c->stream));
+    const bool fused = fused_monitor(c);
+    if (fused) CK(enqueue_monitor_begin(c));  // the records of the current state: the first step's estimate
     for (int s = 0; s < n; ++s) CK(cudaGraphLaunch(c->mgraph, c->stream));
+    if (fused) {  // the estimate slot must not carry this loop's minimum into a later MaxTimeStep
+        dg::k_reset_estimate<<<1, 1, 0, c->stream>>>(c->red.p);
+        CK(cudaGetLastError());
+    }
     std::vector<double> rows(static_cast<size_t>(n) * 6 * nc);
     CK(cudaMemcpyAsync(rows.data(), c->mon.p, sizeof(double) * rows.size(), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(c->h_scal, c->scal.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream));

@@ -55,6 +55,7 @@ struct Store {
     dg::Args<R> args;
     dg::StageFn<R> stage = nullptr;
     dg::KernelTimesFn<R> times = nullptr;
+    dg::MonitorFns<R> mon{nullptr, nullptr};  // fused time-loop monitor (the kTmaUpdate orders)
     void free() {
         for (DevBuf<R>* b : {&ja_xi, &ja_eta, &ja_zeta, &jac, &inv_jac, &fn, &ft1, &ft2, &fj, &sgeo, &QDot, &Ux, &Uy,
                              &Uz, &QF, &FV, &FS})
@@ -126,6 +127,7 @@ struct dg_ctx {
     h3dctx::DevBuf<int> mon_count;
     int mon_rows = 0;
     bool keep_grad = false;  // the last stage of every step stores the lifted gradients
+    h3dctx::DevBuf<unsigned long long> mon_part;  // fused time-loop monitor: 8 words per element
 
     // variable-order / multi-case path
     bool var = false;

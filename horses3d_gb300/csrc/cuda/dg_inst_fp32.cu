@@ -3,6 +3,15 @@
 
 namespace dg {
 
+MonitorFns<float> monitor_fns_fp32(int P, bool gl) {
+    MonitorFns<float> f{nullptr, nullptr};
+    if (P == 6) {
+        f.begin = gl ? monitor_begin<6, true, float> : monitor_begin<6, false, float>;
+        f.exact = gl ? monitor_exact<6, true, float> : monitor_exact<6, false, float>;
+    }
+    return f;
+}
+
 StageFn<float> stage_fn_fp32(int P, bool gl) {
     switch (P) {
         case 2: return gl ? run_stage<2, true, float> : run_stage<2, false, float>;

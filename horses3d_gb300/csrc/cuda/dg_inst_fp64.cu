@@ -3,6 +3,15 @@
 
 namespace dg {
 
+MonitorFns<double> monitor_fns_fp64(int P, bool gl) {
+    MonitorFns<double> f{nullptr, nullptr};
+    if (P == 6) {
+        f.begin = gl ? monitor_begin<6, true, double> : monitor_begin<6, false, double>;
+        f.exact = gl ? monitor_exact<6, true, double> : monitor_exact<6, false, double>;
+    }
+    return f;
+}
+
 StageFn<double> stage_fn_fp64(int P, bool gl) {
     switch (P) {
         case 2: return gl ? run_stage<2, true, double> : run_stage<2, false, double>;

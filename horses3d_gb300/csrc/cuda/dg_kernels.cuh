@@ -25,6 +25,7 @@
 #include <cstdint>
 
 #include "dg_convert.cuh"
+#include "dg_dt.cuh"
 #include "dg_physics.cuh"
 #include "dg_tc.cuh"
 #include "dg_tma.cuh"
@@ -83,6 +84,11 @@ struct Args {
     double e_ref;        // energy reference of the mixed form (0 for the plain form)
     const BoundaryR<R>* bc;  // boundary conditions (a boundary slot has nb_slot = -1 - its index)
     int* err;            // set by a kernel whose bounded wait on a bulk copy gave up
+    // device time loop with the residual monitor and the MaxTimeStep estimate fused into the last
+    // stage's update: per element 8 words (max |QDot| per variable as FP64 bit images, a NaN/Inf
+    // flag, the FP32 convective and viscous estimates of the new state as bit images)
+    unsigned long long* mon;
+    DtConst32 dtc;
     uint32_t extra_tx;   // bytes the update kernel's mbarrier expects beyond its copies (fault injection; 0)
     // manufactured-solution source constants
     double src_gm1, src_gM2, src_mu, src_kappa;
@@ -1018,13 +1024,62 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
     }
 }
 
+// The monitor record of one element (one CTA): max |QDot| per variable (FP64 bit images), a
+// NaN/Inf flag and the minima of the FP32 time-step estimates over the CTA's threads, reduced through
+// shared memory by warp 0 (the CTA may end in a partial warp) and written by thread 0.
+template <int NT>
+__device__ __forceinline__ void monitor_element(const unsigned long long m[5], int bad, float cv, float vs,
+                                                unsigned long long* out) {
+    __shared__ unsigned long long sm[5][NT];
+    __shared__ float sc[NT], sv[NT];
+    __shared__ int sb[NT];
+    const int t = threadIdx.x, nt = blockDim.x;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) sm[v][t] = m[v];
+    sc[t] = cv;
+    sv[t] = vs;
+    sb[t] = bad;
+    __syncthreads();
+    if (t < 32) {
+        unsigned long long mm[5] = {0, 0, 0, 0, 0};
+        float c = 3.0e38f, w = 3.0e38f;
+        int b = 0;
+        for (int q = t; q < nt; q += 32) {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) mm[v] = sm[v][q] > mm[v] ? sm[v][q] : mm[v];
+            c = fminf(c, sc[q]);
+            w = fminf(w, sv[q]);
+            b |= sb[q];
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) {
+                const unsigned long long x = __shfl_down_sync(0xffffffffu, mm[v], o);
+                mm[v] = x > mm[v] ? x : mm[v];
+            }
+            c = fminf(c, __shfl_down_sync(0xffffffffu, c, o));
+            w = fminf(w, __shfl_down_sync(0xffffffffu, w, o));
+            b |= __shfl_down_sync(0xffffffffu, b, o);
+        }
+        if (t == 0) {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) out[v] = mm[v];
+            out[5] = b ? 1ull : 0ull;
+            out[6] = __float_as_uint(c);
+            out[7] = __float_as_uint(w);
+        }
+    }
+}
+
 // ------------------------------------------------------------------------------------------------
 // k_update_tma: k_update for one element per CTA whose Q, G (FP64), QDot and J blocks are 16-byte
 // aligned (P = 6): the four element blocks arrive in shared memory as TMA bulk copies on an
 // mbarrier while the threads fetch their surface fluxes; the updated Q and G leave as bulk stores.
 // A copy that does not complete within the bounded wait sets *a.err and the CTA returns.
 // ------------------------------------------------------------------------------------------------
-template <int P, bool GL, bool SRC, typename R>
+// FUSE (the last stage of a monitored time-loop step): the element's residual/NaN record and the
+// FP32 MaxTimeStep estimate of the new state go to a.mon (monitor_element).
+template <int P, bool GL, bool SRC, typename R, bool FUSE = false>
 __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
     k_update_tma(Args<R> a, int stage, double tshift, int write_qdot) {
     static_assert(Geo<P>::EPB == 1, "one element per CTA");
@@ -1092,6 +1147,20 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
     const R qn[5] = {from_f64<R>(qq[0]), from_f64<R>(qq[1]), from_f64<R>(qq[2]), from_f64<R>(qq[3]),
                      from_f64<R>(qq[4] - a.e_ref)};
     st5(sQ4, n, sQ1, n, qn);
+    if constexpr (FUSE) {
+        // ComputeMaxResiduals (max |QDot| of this stage) and checkForNan (the new Q) of the element,
+        // and the FP32 time-step estimates of the new state (the first pass of MaxTimeStep)
+        unsigned long long m[5];
+        int bad = 0;
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+            m[v] = abs_bits_as_double(abs_bits(qd[v]), static_cast<const R*>(nullptr));
+            bad |= nonfinite(qq[v]);
+        }
+        float cv, vs;
+        dt_estimate(a.dtc, qq, a.ja_xi + 3 * g, a.ja_eta + 3 * g, a.ja_zeta + 3 * g, sJ[n], cv, vs);
+        monitor_element<P3>(m, bad, cv, vs, a.mon + 8 * static_cast<int64_t>(e));
+    }
     fence_proxy_async_smem();  // this thread's Q, G writes before the bulk stores read them
     __syncthreads();
     if (n == 0) {

@@ -19,6 +19,8 @@ constexpr int kWriteQDot = 2;
 // face flux and update kernels (after they received the neighbours' viscous normal fluxes).
 constexpr int kVolumeOnly = 4;
 constexpr int kSurfaceOnly = 8;
+// The monitored device time loop: the update of this stage writes the monitor records (a.mon).
+constexpr int kFuseMonitor = 16;
 
 template <typename R>
 using StageFn = cudaError_t (*)(const Args<R>& a, int stage, double tshift, int flags, cudaStream_t s);
@@ -54,10 +56,16 @@ void launch_volume(const Args<R>& a, int blocks, int store_grad, cudaStream_t s)
 template <int P>
 constexpr bool kTmaUpdate = (P == 6);
 
+// fuse: the monitored time loop's last stage also writes each element's residual/NaN record and
+// MaxTimeStep estimate (kTmaUpdate orders only).
 template <int P, bool GL, bool SRC, typename R>
-void launch_update(const Args<R>& a, int blocks, int stage, double tshift, int wq, cudaStream_t s) {
-    if constexpr (kTmaUpdate<P>) k_update_tma<P, GL, SRC, R><<<blocks, Geo<P>::THREADS, 0, s>>>(a, stage, tshift, wq);
-    else k_update<P, GL, SRC, R><<<blocks, Geo<P>::THREADS, 0, s>>>(a, stage, tshift, wq);
+void launch_update(const Args<R>& a, int blocks, int stage, double tshift, int wq, cudaStream_t s, bool fuse = false) {
+    if constexpr (kTmaUpdate<P>) {
+        if (fuse) k_update_tma<P, GL, SRC, R, true><<<blocks, Geo<P>::THREADS, 0, s>>>(a, stage, tshift, wq);
+        else k_update_tma<P, GL, SRC, R><<<blocks, Geo<P>::THREADS, 0, s>>>(a, stage, tshift, wq);
+    } else {
+        k_update<P, GL, SRC, R><<<blocks, Geo<P>::THREADS, 0, s>>>(a, stage, tshift, wq);
+    }
 }
 
 // The interface-flux kernel in its common variant (Roe, LxF, central, Rusanov, u-diss with the
@@ -90,8 +98,9 @@ cudaError_t run_stage(const Args<R>& a, int stage, double tshift, int flags, cud
     if (!(flags & kSurfaceOnly)) launch_volume<P, GL, R>(a, eblocks, flags & kStoreGrad, s);
     if (flags & kVolumeOnly) return cudaGetLastError();
     launch_flux<P, R>(a, fblocks, s);
-    if (a.source) launch_update<P, GL, true>(a, eblocks, stage, tshift, (flags & kWriteQDot) ? 1 : 0, s);
-    else launch_update<P, GL, false>(a, eblocks, stage, tshift, (flags & kWriteQDot) ? 1 : 0, s);
+    const bool fuse = (flags & kFuseMonitor) != 0;
+    if (a.source) launch_update<P, GL, true>(a, eblocks, stage, tshift, (flags & kWriteQDot) ? 1 : 0, s, fuse);
+    else launch_update<P, GL, false>(a, eblocks, stage, tshift, (flags & kWriteQDot) ? 1 : 0, s, fuse);
     return cudaGetLastError();
 }
 
@@ -135,128 +144,133 @@ cudaError_t kernel_times(const Args<R>& a, int reps, cudaStream_t s, double* ms)
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ fused time-loop monitor ----
+// The monitored device time loop (dg_integrate) of the kTmaUpdate orders reads the residuals, the
+// NaN test and the first MaxTimeStep pass from the records the last stage's update writes per
+// element (k_update_tma<..., true>), so the loop needs no separate pass over Q and QDot:
+//   before the loop  k_monitor_estimate  records of the uploaded state, k_monitor_fold -> red[7]
+//   every step       k_dt_exact_elem (elements whose estimate lies in the window) + k_dt_final,
+//                    the three stages (the last one writes the records), k_advance_time,
+//                    k_monitor_fold (residuals red[2..6], NaN flag, estimate minimum red[7] for the
+//                    next step) and the history row
+// The dt equals the two-pass reduction's bit for bit (the same window argument, per element instead
+// of per chunk), and the residuals equal k_residuals' (maxima of the same values).
+constexpr int kFoldBlocks = 152;
+
+template <int P, typename R>
+__global__ void __launch_bounds__(Geo<P>::THREADS) k_monitor_estimate(Args<R> a) {
+    const int e = blockIdx.x, n = threadIdx.x;
+    const int64_t g = static_cast<int64_t>(e) * Geo<P>::P3 + n;
+    float cv, vs;
+    dt_estimate(a.dtc, a.Q + 5 * g, a.ja_xi + 3 * g, a.ja_eta + 3 * g, a.ja_zeta + 3 * g, a.jac[g], cv, vs);
+    const unsigned long long m[5] = {0, 0, 0, 0, 0};
+    monitor_element<Geo<P>::P3>(m, 0, cv, vs, a.mon + 8 * static_cast<int64_t>(e));
+}
+
+// Folds the element records into red[2..6] (max |QDot|), *nan_flag and the FP32 estimate minima of
+// red[7].
+__global__ static void __launch_bounds__(256) k_monitor_fold(const unsigned long long* __restrict__ mon, int K,
+                                                             unsigned long long* red, int* nan_flag) {
+    unsigned long long m[5] = {0, 0, 0, 0, 0};
+    float c = 3.0e38f, w = 3.0e38f;
+    int b = 0;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < K; e += gridDim.x * blockDim.x) {
+        const unsigned long long* r = mon + 8 * static_cast<int64_t>(e);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) m[v] = r[v] > m[v] ? r[v] : m[v];
+        b |= r[5] != 0;
+        c = fminf(c, __uint_as_float(static_cast<unsigned>(r[6])));
+        w = fminf(w, __uint_as_float(static_cast<unsigned>(r[7])));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+            const unsigned long long x = __shfl_down_sync(0xffffffffu, m[v], o);
+            m[v] = x > m[v] ? x : m[v];
+        }
+        c = fminf(c, __shfl_down_sync(0xffffffffu, c, o));
+        w = fminf(w, __shfl_down_sync(0xffffffffu, w, o));
+        b |= __shfl_down_sync(0xffffffffu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) atomicMax(&red[2 + v], m[v]);
+        if (b) atomicOr(nan_flag, 1);
+        unsigned int* s32 = reinterpret_cast<unsigned int*>(red + 7);
+        atomicMin(&s32[0], fbits(c));
+        atomicMin(&s32[1], fbits(w));
+    }
+}
+
+static __global__ void k_reset_estimate(unsigned long long* red) { red[7] = kDtEstimateInit; }
+
+// The exact pass per element: an element none of whose nodes can be in the window leaves at once.
+template <int P, typename R>
+__global__ void __launch_bounds__(Geo<P>::THREADS) k_dt_exact_elem(Args<R> a, DtArgs d) {
+    constexpr int NT = Geo<P>::P3;
+    const int e = blockIdx.x, n = threadIdx.x;
+    const unsigned int* s32 = reinterpret_cast<const unsigned int*>(d.red + 7);
+    const float thr_c = __uint_as_float(s32[0]) * (1.0f + kDtWindow);
+    const float thr_v = __uint_as_float(s32[1]) * (1.0f + kDtWindow);
+    const unsigned long long* rec = a.mon + 8 * static_cast<int64_t>(e);
+    const float ec = __uint_as_float(static_cast<unsigned>(rec[6])), evs = __uint_as_float(static_cast<unsigned>(rec[7]));
+    if (ec > thr_c && !(d.ns && !(evs > thr_v))) return;  // block-uniform, before any barrier
+    const int64_t g = static_cast<int64_t>(e) * NT + n;
+    const double* Q = d.Q + 5 * g;
+    float cv, vs;
+    dt_estimate(a.dtc, Q, a.ja_xi + 3 * g, a.ja_eta + 3 * g, a.ja_zeta + 3 * g, a.jac[g], cv, vs);
+    double conv = 1.0e300, visc = 1.0e300;
+    const bool wc = !(cv > thr_c), wv = d.ns && !(vs > thr_v);
+    if (wc || wv)
+        dt_exact(d, d.dxi, d.dxi2, Q, a.ja_xi + 3 * g, a.ja_eta + 3 * g, a.ja_zeta + 3 * g, a.jac[g], d.gammaM2, wc, wv,
+                 conv, visc);
+    __shared__ double sc[NT], sv[NT];
+    sc[n] = conv;
+    sv[n] = visc;
+    __syncthreads();
+    if (n < 32) {
+        for (int q = n + 32; q < NT; q += 32) {
+            conv = fmin(conv, sc[q]);
+            visc = fmin(visc, sv[q]);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            conv = fmin(conv, __shfl_down_sync(0xffffffffu, conv, o));
+            visc = fmin(visc, __shfl_down_sync(0xffffffffu, visc, o));
+        }
+        if (n == 0) {
+            atomicMin(&d.red[0], dbits(conv));
+            atomicMin(&d.red[1], dbits(visc));
+        }
+    }
+}
+
+template <typename R>
+struct MonitorFns {
+    cudaError_t (*begin)(const Args<R>& a, unsigned long long* red, int* nan_flag, cudaStream_t s);
+    cudaError_t (*exact)(const Args<R>& a, const DtArgs& d, cudaStream_t s);
+};
+
+template <int P, bool GL, typename R>
+cudaError_t monitor_begin(const Args<R>& a, unsigned long long* red, int* nan_flag, cudaStream_t s) {
+    k_reset_estimate<<<1, 1, 0, s>>>(red);
+    k_monitor_estimate<P, R><<<a.K, Geo<P>::THREADS, 0, s>>>(a);
+    k_monitor_fold<<<kFoldBlocks, 256, 0, s>>>(a.mon, a.K, red, nan_flag);
+    return cudaGetLastError();
+}
+
+template <int P, bool GL, typename R>
+cudaError_t monitor_exact(const Args<R>& a, const DtArgs& d, cudaStream_t s) {
+    k_dt_exact_elem<P, R><<<a.K, Geo<P>::THREADS, 0, s>>>(a, d);
+    return cudaGetLastError();
+}
+
 // Resolved in the instantiation translation units.
+MonitorFns<double> monitor_fns_fp64(int P, bool gl);
+MonitorFns<float> monitor_fns_fp32(int P, bool gl);
 StageFn<double> stage_fn_fp64(int P, bool gl);
 StageFn<float> stage_fn_fp32(int P, bool gl);
 KernelTimesFn<double> times_fn_fp64(int P, bool gl);
 KernelTimesFn<float> times_fn_fp32(int P, bool gl);
-
-// ------------------------------------------------------------------------ reductions ----------
-// Non-negative doubles order like their bit patterns, so atomicMin/atomicMax on the 64-bit image
-// implement min/max reductions exactly.
-__device__ __forceinline__ unsigned long long dbits(double x) { return static_cast<unsigned long long>(__double_as_longlong(x)); }
-
-// |x| as its bit pattern (float: 31 bits, double: 63 bits); the maximum of such patterns is the
-// pattern of the maximum |x|.
-__device__ __forceinline__ unsigned long long abs_bits(float x) { return __float_as_uint(x) & 0x7fffffffu; }
-__device__ __forceinline__ unsigned long long abs_bits(double x) { return dbits(x) & 0x7fffffffffffffffull; }
-// The double image (for the FP64 reduction slots) of a maximum pattern of the element type.
-__device__ __forceinline__ unsigned long long abs_bits_as_double(unsigned long long m, const float*) {
-    return dbits(static_cast<double>(__uint_as_float(static_cast<unsigned>(m))));
-}
-__device__ __forceinline__ unsigned long long abs_bits_as_double(unsigned long long m, const double*) { return m; }
-// NaN or Inf: all exponent bits set.
-__device__ __forceinline__ int nonfinite(double x) { return (dbits(x) & 0x7ff0000000000000ull) == 0x7ff0000000000000ull; }
-
-struct DtArgs {
-    long long ndof;
-    double cfl, dcfl, dxi[3], dxi2[3];
-    int ns;
-    double gamma, gm1, gammaM2, S_div_TRef, TReNorm;
-    const double* Q;
-    unsigned long long* red;  // [0] convective, [1] viscous (FP64 bit images), [7] FP32 estimates (2 x 32 bit)
-};
-
-// MaxTimeStep (DGSEMClass.f90:870-1038) in two passes. The minimum is taken over FP64 quotients
-// that need about ten FP64 divisions and square roots per node, so evaluating every node in FP64
-// costs milliseconds on a part whose FP64 rate is 1/64 of FP32. Pass 1 estimates each node's
-// convective and viscous limits in FP32 and reduces their minima m32. Pass 2 repeats the estimate
-// and evaluates the exact FP64 expressions only at nodes whose estimate is within kDtWindow of m32
-// (or not a number). An FP32 estimate differs from the FP64 value by a relative 1e-6 or less for
-// physical states, far inside the window, so the node that attains the FP64 minimum is always
-// evaluated and the result equals the FP64 minimum over all nodes bit for bit.
-constexpr float kDtWindow = 1.0e-3f;
-constexpr unsigned long long kDtEstimateInit = 0x7F8000007F800000ull;  // two FP32 +inf
-
-struct DtConst32 {
-    float cfl, dcfl, dxi[3], dxi2[3], gamma, gm1, gammaM2, S_div_TRef, TReNorm;
-    int ns;
-};
-
-__host__ __device__ inline DtConst32 dt_const32(double cfl, double dcfl, const double* dxi, double gamma, double gm1,
-                                                double gammaM2, double S_div_TRef, double TReNorm, int ns) {
-    DtConst32 c;
-    c.cfl = float(cfl);
-    c.dcfl = float(dcfl);
-    for (int r = 0; r < 3; ++r) {
-        c.dxi[r] = float(dxi[r]);
-        c.dxi2[r] = float(dxi[r] * dxi[r]);
-    }
-    c.gamma = float(gamma);
-    c.gm1 = float(gm1);
-    c.gammaM2 = float(gammaM2);
-    c.S_div_TRef = float(S_div_TRef);
-    c.TReNorm = float(TReNorm);
-    c.ns = ns;
-    return c;
-}
-
-// FP32 estimates of one node's convective and viscous time-step limits.
-template <typename R>
-__device__ __forceinline__ void dt_estimate(const DtConst32& d, const double* Q, const R* jx, const R* je, const R* jz,
-                                            R jac, float& conv, float& visc) {
-    const float rho = to_f32(Q[0]), ru = to_f32(Q[1]), rv = to_f32(Q[2]), rw = to_f32(Q[3]), E = to_f32(Q[4]);
-    const float ir = 1.0f / rho;
-    const float p = d.gm1 * (E - 0.5f * (ru * ru + rv * rv + rw * rw) * ir);
-    const float a = sqrtf(d.gamma * p * ir);
-    const float ev[3] = {fabsf(ru * ir) + a, fabsf(rv * ir) + a, fabsf(rw * ir) + a};
-    const float J = fabsf(float(jac));
-    const R* ja[3] = {jx, je, jz};
-    float lam = 0.0f;
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-        lam += fabsf(float(ja[r][0]) * ev[0] + float(ja[r][1]) * ev[1] + float(ja[r][2]) * ev[2]) * d.dxi[r];
-    conv = d.cfl * J / lam;
-    visc = 3.0e38f;
-    if (d.ns) {
-        const float t = d.gammaM2 * p * ir * d.TReNorm;
-        const float mu = (1.0f + d.S_div_TRef) / (t + d.S_div_TRef) * t * sqrtf(t);
-        float lv = 0.0f;
-#pragma unroll
-        for (int r = 0; r < 3; ++r) lv += mu * d.dxi2[r] * fabsf(float(ja[r][0]) + float(ja[r][1]) + float(ja[r][2]));
-        visc = d.dcfl * J / lv;
-    }
-}
-
-// The exact FP64 limits of one node (the reference's expressions and operation order).
-template <typename R>
-__device__ __forceinline__ void dt_exact(const DtArgs& d, const double* dx, const double* dx2, const double* Q,
-                                         const R* jx, const R* je, const R* jz, R jac, double gammaM2, bool want_conv,
-                                         bool want_visc, double& conv, double& visc) {
-    const double p = d.gm1 * (Q[4] - 0.5 * (Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3]) / Q[0]);
-    const double J = fabs(double(jac));
-    const R* ja[3] = {jx, je, jz};
-    if (want_conv) {
-        const double a = sqrt(d.gamma * p / Q[0]);
-        const double ev[3] = {fabs(Q[1] / Q[0]) + a, fabs(Q[2] / Q[0]) + a, fabs(Q[3] / Q[0]) + a};
-        double l3[3];
-#pragma unroll
-        for (int r = 0; r < 3; ++r)
-            l3[r] = fabs(double(ja[r][0]) * ev[0] + double(ja[r][1]) * ev[1] + double(ja[r][2]) * ev[2]) * dx[r];
-        conv = d.cfl * J / (l3[0] + l3[1] + l3[2]);
-    }
-    if (want_visc) {
-        const double T = gammaM2 * p / Q[0];
-        const double t = T * d.TReNorm;
-        const double mu = (1.0 + d.S_div_TRef) / (t + d.S_div_TRef) * t * sqrt(t);
-        double v3[3];
-#pragma unroll
-        for (int r = 0; r < 3; ++r) v3[r] = mu * dx2[r] * fabs(double(ja[r][0]) + double(ja[r][1]) + double(ja[r][2]));
-        visc = d.dcfl * J / (v3[0] + v3[1] + v3[2]);
-    }
-}
-
-__device__ __forceinline__ unsigned int fbits(float x) { return __float_as_uint(x); }
 
 // Block minimum of two values, folded into the 64-bit (double) or 32-bit (float) slots by atomicMin on
 // the bit images (non-negative values order like their bit patterns).

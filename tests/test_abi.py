@@ -57,8 +57,9 @@ def test_create_validates_before_touching_the_device():
 def test_variable_order_path_validates_before_touching_the_device():
     # anisotropic orders go to the variable-order path (a batch of one case)
     aniso = HexMesh.box(2, [0, 0, 0], [1, 1, 1], np.tile([2, 3, 4], 8), node_type=_abi.DG_NODES_GAUSS)
-    assert _ctx_create(aniso, Config(inviscid=_abi.DG_INVISCID_SPLIT)) == _abi.DG_ERR_UNSUPPORTED
-    assert b"standard" in _abi.lib().dg_last_error()
+    # split form needs Gauss-Lobatto nodes here too
+    assert _ctx_create(aniso, Config(inviscid=_abi.DG_INVISCID_SPLIT)) == _abi.DG_ERR_INVALID
+    assert b"Gauss-Lobatto" in _abi.lib().dg_last_error()
     assert _ctx_create(aniso, Config(mach=0.0)) == _abi.DG_ERR_INVALID
     # a face order that is not the larger of its two sides' orders
     nf = np.ctypeslib.as_array(aniso.desc.face_nf, shape=(2 * aniso.desc.n_faces,))
