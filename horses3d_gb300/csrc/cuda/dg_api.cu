@@ -683,15 +683,10 @@ int prepare_graph(dg_ctx* c, int mode, double cfl, double dcfl) {
     if (c->graph) cudaGraphExecDestroy(c->graph);
     c->graph = nullptr;
     cudaGraph_t g = nullptr;
-    const bool fused = fused_monitor(c);
-    if (fused) {
-        int rc = setup_fused_monitor(c, cfl, dcfl);
-        if (rc) return rc;
-    }
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
-    if (mode == 1) e = fused ? enqueue_max_dt_fused(c, cfl, dcfl) : enqueue_max_dt(c, cfl, dcfl);
-    if (e == cudaSuccess) e = enqueue_step(c, fused);
+    if (mode == 1) e = enqueue_max_dt(c, cfl, dcfl);
+    if (e == cudaSuccess) e = enqueue_step(c);
     if (e == cudaSuccess) {
         if (c->var) {
             e = h3dvar::enqueue_advance_time(c);

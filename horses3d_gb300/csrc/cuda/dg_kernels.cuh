@@ -1024,49 +1024,72 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
     }
 }
 
-// The monitor record of one element (one CTA): max |QDot| per variable (FP64 bit images), a
-// NaN/Inf flag and the minima of the FP32 time-step estimates over the CTA's threads, reduced through
-// shared memory by warp 0 (the CTA may end in a partial warp) and written by thread 0.
+// The monitor record of one element (one CTA of NT threads): max |QDot| per variable (FP64 bit
+// images), a NaN/Inf flag and the minima of the FP32 time-step estimates. Each warp reduces its
+// lanes by shuffles (the CTA may end in a partial warp, whose missing lanes are left out), warp 0
+// folds the warp partials, thread 0 writes the record.
+struct MonitorPart {
+    unsigned long long m[5];
+    float c, w;
+    int b;
+};
+
+__device__ __forceinline__ void monitor_fold(MonitorPart& p, const MonitorPart& q) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) p.m[v] = q.m[v] > p.m[v] ? q.m[v] : p.m[v];
+    p.c = fminf(p.c, q.c);
+    p.w = fminf(p.w, q.w);
+    p.b |= q.b;
+}
+
+// Shuffle-down reduction over the first `cnt` lanes of a warp (mask: exactly those lanes).
+__device__ __forceinline__ void monitor_warp(MonitorPart& p, unsigned mask, int cnt) {
+    const int lane = threadIdx.x & 31;
+    for (int o = 16; o > 0; o >>= 1) {
+        MonitorPart q;
+#pragma unroll
+        for (int v = 0; v < 5; ++v) q.m[v] = __shfl_down_sync(mask, p.m[v], o);
+        q.c = __shfl_down_sync(mask, p.c, o);
+        q.w = __shfl_down_sync(mask, p.w, o);
+        q.b = __shfl_down_sync(mask, p.b, o);
+        if (lane + o < cnt) monitor_fold(p, q);
+    }
+}
+
 template <int NT>
 __device__ __forceinline__ void monitor_element(const unsigned long long m[5], int bad, float cv, float vs,
                                                 unsigned long long* out) {
-    __shared__ unsigned long long sm[5][NT];
-    __shared__ float sc[NT], sv[NT];
-    __shared__ int sb[NT];
-    const int t = threadIdx.x, nt = blockDim.x;
+    constexpr int NW = (NT + 31) / 32;
+    static_assert(NT >= 32, "warp 0 is full");
+    __shared__ MonitorPart sp[NW];
+    const int t = threadIdx.x, w = t >> 5;
+    MonitorPart p;
 #pragma unroll
-    for (int v = 0; v < 5; ++v) sm[v][t] = m[v];
-    sc[t] = cv;
-    sv[t] = vs;
-    sb[t] = bad;
+    for (int v = 0; v < 5; ++v) p.m[v] = m[v];
+    p.c = cv;
+    p.w = vs;
+    p.b = bad;
+    const int cnt = NT - 32 * w < 32 ? NT - 32 * w : 32;
+    monitor_warp(p, cnt == 32 ? 0xffffffffu : (1u << cnt) - 1u, cnt);
+    if ((t & 31) == 0) sp[w] = p;
     __syncthreads();
-    if (t < 32) {
-        unsigned long long mm[5] = {0, 0, 0, 0, 0};
-        float c = 3.0e38f, w = 3.0e38f;
-        int b = 0;
-        for (int q = t; q < nt; q += 32) {
+    if (w == 0) {
+        if (t < NW) {
+            p = sp[t];
+        } else {
 #pragma unroll
-            for (int v = 0; v < 5; ++v) mm[v] = sm[v][q] > mm[v] ? sm[v][q] : mm[v];
-            c = fminf(c, sc[q]);
-            w = fminf(w, sv[q]);
-            b |= sb[q];
+            for (int v = 0; v < 5; ++v) p.m[v] = 0;
+            p.c = 3.0e38f;
+            p.w = 3.0e38f;
+            p.b = 0;
         }
-        for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-            for (int v = 0; v < 5; ++v) {
-                const unsigned long long x = __shfl_down_sync(0xffffffffu, mm[v], o);
-                mm[v] = x > mm[v] ? x : mm[v];
-            }
-            c = fminf(c, __shfl_down_sync(0xffffffffu, c, o));
-            w = fminf(w, __shfl_down_sync(0xffffffffu, w, o));
-            b |= __shfl_down_sync(0xffffffffu, b, o);
-        }
+        monitor_warp(p, 0xffffffffu, NW);
         if (t == 0) {
 #pragma unroll
-            for (int v = 0; v < 5; ++v) out[v] = mm[v];
-            out[5] = b ? 1ull : 0ull;
-            out[6] = __float_as_uint(c);
-            out[7] = __float_as_uint(w);
+            for (int v = 0; v < 5; ++v) out[v] = p.m[v];
+            out[5] = p.b ? 1ull : 0ull;
+            out[6] = __float_as_uint(p.c);
+            out[7] = __float_as_uint(p.w);
         }
     }
 }
