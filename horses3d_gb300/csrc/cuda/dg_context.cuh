@@ -145,6 +145,7 @@ struct dg_ctx {
     h3dctx::DevBuf<double> pstat;  // mixed form: momentum residual of the state at rest per unit pressure
     h3dctx::VStore<double> v64;
     h3dctx::VStore<float> v32;
+    dg::Lanes lanes;  // side streams of the stage phases
     int n_items = 0;
     int cls[dg::kItemClasses + 1] = {};  // item class ranges (see dg::VArgs::cls)
     int ccap[dg::kItemClasses] = {};     // largest item per class

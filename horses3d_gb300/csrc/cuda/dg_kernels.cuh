@@ -1057,11 +1057,16 @@ __device__ __forceinline__ void monitor_warp(MonitorPart& p, unsigned mask, int 
 }
 
 template <int NT>
-__device__ __forceinline__ void monitor_element(const unsigned long long m[5], int bad, float cv, float vs,
-                                                unsigned long long* out) {
-    constexpr int NW = (NT + 31) / 32;
+struct MonitorScratch {
+    static constexpr int NW = (NT + 31) / 32;
+    MonitorPart w[NW];
+};
+
+// First half: every warp's partial record into shared memory (before a CTA barrier).
+template <int NT>
+__device__ __forceinline__ void monitor_partial(const unsigned long long m[5], int bad, float cv, float vs,
+                                                MonitorScratch<NT>& sp) {
     static_assert(NT >= 32, "warp 0 is full");
-    __shared__ MonitorPart sp[NW];
     const int t = threadIdx.x, w = t >> 5;
     MonitorPart p;
 #pragma unroll
@@ -1071,27 +1076,42 @@ __device__ __forceinline__ void monitor_element(const unsigned long long m[5], i
     p.b = bad;
     const int cnt = NT - 32 * w < 32 ? NT - 32 * w : 32;
     monitor_warp(p, cnt == 32 ? 0xffffffffu : (1u << cnt) - 1u, cnt);
-    if ((t & 31) == 0) sp[w] = p;
-    __syncthreads();
-    if (w == 0) {
-        if (t < NW) {
-            p = sp[t];
-        } else {
+    if ((t & 31) == 0) sp.w[w] = p;
+}
+
+// Second half (after the barrier, warp 0): the warp partials folded, the record written by thread 0.
+template <int NT>
+__device__ __forceinline__ void monitor_finish(const MonitorScratch<NT>& sp, unsigned long long* out) {
+    constexpr int NW = MonitorScratch<NT>::NW;
+    const int t = threadIdx.x;
+    if (t >= 32) return;
+    MonitorPart p;
+    if (t < NW) {
+        p = sp.w[t];
+    } else {
 #pragma unroll
-            for (int v = 0; v < 5; ++v) p.m[v] = 0;
-            p.c = 3.0e38f;
-            p.w = 3.0e38f;
-            p.b = 0;
-        }
-        monitor_warp(p, 0xffffffffu, NW);
-        if (t == 0) {
-#pragma unroll
-            for (int v = 0; v < 5; ++v) out[v] = p.m[v];
-            out[5] = p.b ? 1ull : 0ull;
-            out[6] = __float_as_uint(p.c);
-            out[7] = __float_as_uint(p.w);
-        }
+        for (int v = 0; v < 5; ++v) p.m[v] = 0;
+        p.c = 3.0e38f;
+        p.w = 3.0e38f;
+        p.b = 0;
     }
+    monitor_warp(p, 0xffffffffu, NW);
+    if (t == 0) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) out[v] = p.m[v];
+        out[5] = p.b ? 1ull : 0ull;
+        out[6] = __float_as_uint(p.c);
+        out[7] = __float_as_uint(p.w);
+    }
+}
+
+template <int NT>
+__device__ __forceinline__ void monitor_element(const unsigned long long m[5], int bad, float cv, float vs,
+                                                unsigned long long* out) {
+    __shared__ MonitorScratch<NT> sp;
+    monitor_partial<NT>(m, bad, cv, vs, sp);
+    __syncthreads();
+    monitor_finish<NT>(sp, out);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -1115,6 +1135,14 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
     __shared__ __align__(128) R sJ[P3];
     __shared__ __align__(16) R sQ4[4 * P3];
     __shared__ R sQ1[P3];
+    // FUSE: the element's metric blocks (Ja^xi, Ja^eta, Ja^zeta) for the time-step estimate (staged
+    // in the FP32 form; the FP64 form has no static shared memory left for them and reads them from
+    // global memory), and the warp partials of its monitor record
+    constexpr bool STAGE_JA = FUSE && sizeof(R) == 4;
+    constexpr uint32_t BA = 3 * P3 * sizeof(R);
+    static_assert(BA % 16 == 0, "bulk copies move multiples of 16 bytes");
+    __shared__ __align__(128) R sJa[STAGE_JA ? 9 * P3 : 4];
+    __shared__ MonitorScratch<FUSE ? P3 : 32> smon;
     __shared__ __align__(8) uint64_t bar;
     const int n = threadIdx.x;
     const int e = blockIdx.x;
@@ -1126,13 +1154,18 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
     }
     __syncthreads();
     if (n == 0) {
-        mbar_arrive_expect_tx(&bar, (stage >= 0 ? 2 * BQ : 0) + BD + BJ + a.extra_tx);
+        mbar_arrive_expect_tx(&bar, (stage >= 0 ? 2 * BQ : 0) + BD + BJ + (STAGE_JA ? 3 * BA : 0) + a.extra_tx);
         if (stage >= 0) {
             bulk_load(sQd, a.Q + 5 * g0, BQ, &bar);
             bulk_load(sGd, a.G + 5 * g0, BQ, &bar);
         }
         bulk_load(sDot, a.QDot + 5 * g0, BD, &bar);
         bulk_load(sJ, a.jac + g0, BJ, &bar);
+        if constexpr (STAGE_JA) {
+            bulk_load(sJa, a.ja_xi + 3 * g0, BA, &bar);
+            bulk_load(sJa + 3 * P3, a.ja_eta + 3 * g0, BA, &bar);
+            bulk_load(sJa + 6 * P3, a.ja_zeta + 3 * g0, BA, &bar);
+        }
     }
     R fs[6][5];
     bool use[6];
@@ -1181,8 +1214,11 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
             bad |= nonfinite(qq[v]);
         }
         float cv, vs;
-        dt_estimate(a.dtc, qq, a.ja_xi + 3 * g, a.ja_eta + 3 * g, a.ja_zeta + 3 * g, sJ[n], cv, vs);
-        monitor_element<P3>(m, bad, cv, vs, a.mon + 8 * static_cast<int64_t>(e));
+        if constexpr (STAGE_JA)
+            dt_estimate(a.dtc, qq, sJa + 3 * n, sJa + 3 * P3 + 3 * n, sJa + 6 * P3 + 3 * n, sJ[n], cv, vs);
+        else
+            dt_estimate(a.dtc, qq, a.ja_xi + 3 * g, a.ja_eta + 3 * g, a.ja_zeta + 3 * g, sJ[n], cv, vs);
+        monitor_partial<P3>(m, bad, cv, vs, smon);
     }
     fence_proxy_async_smem();  // this thread's Q, G writes before the bulk stores read them
     __syncthreads();
@@ -1191,6 +1227,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
         bulk_store(a.G + 5 * g0, sGd, BQ);
         bulk_commit();
     }
+    if constexpr (FUSE) monitor_finish<P3>(smon, a.mon + 8 * static_cast<int64_t>(e));
     for (int t = n; t < 6 * P2; t += P3) {  // Q traces of the updated state
         const int side = 1 + t / P2, p = t - (side - 1) * P2;
         R tq[1][5];

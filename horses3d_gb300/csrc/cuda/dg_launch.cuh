@@ -204,43 +204,49 @@ __global__ static void __launch_bounds__(256) k_monitor_fold(const unsigned long
 
 static __global__ void k_reset_estimate(unsigned long long* red) { red[7] = kDtEstimateInit; }
 
-// The exact pass per element: an element none of whose nodes can be in the window leaves at once.
+// The exact pass: a grid of kExactBlocks CTAs strides over the elements; an element none of whose
+// nodes can be in the window is skipped (a block-uniform test on its record).
+constexpr int kExactBlocks = 4 * 152;
 template <int P, typename R>
 __global__ void __launch_bounds__(Geo<P>::THREADS) k_dt_exact_elem(Args<R> a, DtArgs d) {
     constexpr int NT = Geo<P>::P3;
-    const int e = blockIdx.x, n = threadIdx.x;
+    const int n = threadIdx.x;
     const unsigned int* s32 = reinterpret_cast<const unsigned int*>(d.red + 7);
     const float thr_c = __uint_as_float(s32[0]) * (1.0f + kDtWindow);
     const float thr_v = __uint_as_float(s32[1]) * (1.0f + kDtWindow);
-    const unsigned long long* rec = a.mon + 8 * static_cast<int64_t>(e);
-    const float ec = __uint_as_float(static_cast<unsigned>(rec[6])), evs = __uint_as_float(static_cast<unsigned>(rec[7]));
-    if (ec > thr_c && !(d.ns && !(evs > thr_v))) return;  // block-uniform, before any barrier
-    const int64_t g = static_cast<int64_t>(e) * NT + n;
-    const double* Q = d.Q + 5 * g;
-    float cv, vs;
-    dt_estimate(a.dtc, Q, a.ja_xi + 3 * g, a.ja_eta + 3 * g, a.ja_zeta + 3 * g, a.jac[g], cv, vs);
-    double conv = 1.0e300, visc = 1.0e300;
-    const bool wc = !(cv > thr_c), wv = d.ns && !(vs > thr_v);
-    if (wc || wv)
-        dt_exact(d, d.dxi, d.dxi2, Q, a.ja_xi + 3 * g, a.ja_eta + 3 * g, a.ja_zeta + 3 * g, a.jac[g], d.gammaM2, wc, wv,
-                 conv, visc);
     __shared__ double sc[NT], sv[NT];
-    sc[n] = conv;
-    sv[n] = visc;
-    __syncthreads();
-    if (n < 32) {
-        for (int q = n + 32; q < NT; q += 32) {
-            conv = fmin(conv, sc[q]);
-            visc = fmin(visc, sv[q]);
+    for (int e = blockIdx.x; e < a.K; e += gridDim.x) {
+        const unsigned long long* rec = a.mon + 8 * static_cast<int64_t>(e);
+        const float ec = __uint_as_float(static_cast<unsigned>(rec[6]));
+        const float evs = __uint_as_float(static_cast<unsigned>(rec[7]));
+        if (ec > thr_c && !(d.ns && !(evs > thr_v))) continue;  // block-uniform
+        const int64_t g = static_cast<int64_t>(e) * NT + n;
+        const double* Q = d.Q + 5 * g;
+        float cv, vs;
+        dt_estimate(a.dtc, Q, a.ja_xi + 3 * g, a.ja_eta + 3 * g, a.ja_zeta + 3 * g, a.jac[g], cv, vs);
+        double conv = 1.0e300, visc = 1.0e300;
+        const bool wc = !(cv > thr_c), wv = d.ns && !(vs > thr_v);
+        if (wc || wv)
+            dt_exact(d, d.dxi, d.dxi2, Q, a.ja_xi + 3 * g, a.ja_eta + 3 * g, a.ja_zeta + 3 * g, a.jac[g], d.gammaM2, wc,
+                     wv, conv, visc);
+        sc[n] = conv;
+        sv[n] = visc;
+        __syncthreads();
+        if (n < 32) {
+            for (int q = n + 32; q < NT; q += 32) {
+                conv = fmin(conv, sc[q]);
+                visc = fmin(visc, sv[q]);
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                conv = fmin(conv, __shfl_down_sync(0xffffffffu, conv, o));
+                visc = fmin(visc, __shfl_down_sync(0xffffffffu, visc, o));
+            }
+            if (n == 0) {
+                atomicMin(&d.red[0], dbits(conv));
+                atomicMin(&d.red[1], dbits(visc));
+            }
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            conv = fmin(conv, __shfl_down_sync(0xffffffffu, conv, o));
-            visc = fmin(visc, __shfl_down_sync(0xffffffffu, visc, o));
-        }
-        if (n == 0) {
-            atomicMin(&d.red[0], dbits(conv));
-            atomicMin(&d.red[1], dbits(visc));
-        }
+        __syncthreads();  // sc, sv are reused by the next element
     }
 }
 
@@ -260,7 +266,7 @@ cudaError_t monitor_begin(const Args<R>& a, unsigned long long* red, int* nan_fl
 
 template <int P, bool GL, typename R>
 cudaError_t monitor_exact(const Args<R>& a, const DtArgs& d, cudaStream_t s) {
-    k_dt_exact_elem<P, R><<<a.K, Geo<P>::THREADS, 0, s>>>(a, d);
+    k_dt_exact_elem<P, R><<<a.K < kExactBlocks ? a.K : kExactBlocks, Geo<P>::THREADS, 0, s>>>(a, d);
     return cudaGetLastError();
 }
 

@@ -1190,33 +1190,118 @@ size_t vitem_smem(int cap, int nv) {
     return 3 * sizeof(OpsP<R>) + static_cast<size_t>(nv) * cap * sizeof(R);
 }
 
+struct Lanes;
 template <typename R>
-using VStageFn = cudaError_t (*)(const VArgs<R>& a, int stage, double tshift, int flags, cudaStream_t s);
+using VStageFn = cudaError_t (*)(const VArgs<R>& a, int stage, double tshift, int flags, cudaStream_t s,
+                                  const Lanes* lanes);
 
 template <typename R>
 using VTimesFn = cudaError_t (*)(const VArgs<R>& a, int reps, cudaStream_t s, double* ms);
 
+// Side streams for the independent launches of one phase (the item classes of a kernel, the two
+// face lists, and for the Euler equations the face fluxes beside the volume kernels), so that their
+// tails and latency-bound stretches overlap. A Fork records an event on the stage's stream when it
+// opens; a side stream joins at its first launch by waiting on that event, and join() makes the
+// stage's stream wait for every side stream used. Inside a stream capture the side streams become
+// branches of the graph. Without lanes every launch goes to the stage's stream in order.
+constexpr int kLanes = 3;
+struct Lanes {
+    int n = 0;
+    cudaStream_t side[kLanes] = {};
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t done[kLanes] = {};
+};
+
+class Fork {
+  public:
+    Fork(const Lanes* l, cudaStream_t s) : l_(l && l->n > 0 ? l : nullptr), s_(s) {
+        if (l_) note(cudaEventRecord(l_->fork, s_));
+    }
+    explicit Fork(cudaStream_t s) : l_(nullptr), s_(s) {}
+    // The stream of the next independent launch (round robin over the stage's stream and the lanes).
+    cudaStream_t next() {
+        if (!l_) return s_;
+        const int k = turn_++ % (l_->n + 1);
+        if (k == 0) return s_;
+        if (!(used_ & (1u << k))) {
+            note(cudaStreamWaitEvent(l_->side[k - 1], l_->fork, 0));
+            used_ |= 1u << k;
+        }
+        return l_->side[k - 1];
+    }
+    // The stage's stream waits for the lanes used since the fork; the first error of the fork.
+    cudaError_t join() {
+        if (l_) {
+            for (int k = 1; k <= l_->n; ++k) {
+                if (!(used_ & (1u << k))) continue;
+                note(cudaEventRecord(l_->done[k - 1], l_->side[k - 1]));
+                note(cudaStreamWaitEvent(s_, l_->done[k - 1], 0));
+            }
+            used_ = 0;
+        }
+        return err_;
+    }
+    void note(cudaError_t e) {
+        if (err_ == cudaSuccess) err_ = e;
+    }
+    cudaError_t error() const { return err_; }
+
+  private:
+    const Lanes* l_;
+    cudaStream_t s_;
+    int turn_ = 0;
+    unsigned used_ = 0;
+    cudaError_t err_ = cudaSuccess;
+};
+
+// Lanes of a context: kLanes non-blocking side streams and their events (n = 0 if any creation failed).
+inline cudaError_t create_lanes(Lanes& l) {
+    cudaError_t e = cudaEventCreateWithFlags(&l.fork, cudaEventDisableTiming);
+    for (int k = 0; k < kLanes && e == cudaSuccess; ++k) {
+        e = cudaStreamCreateWithFlags(&l.side[k], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&l.done[k], cudaEventDisableTiming);
+    }
+    l.n = e == cudaSuccess ? kLanes : 0;
+    return e;
+}
+inline void destroy_lanes(Lanes& l) {
+    for (int k = 0; k < kLanes; ++k) {
+        if (l.side[k]) cudaStreamDestroy(l.side[k]);
+        if (l.done[k]) cudaEventDestroy(l.done[k]);
+        l.side[k] = nullptr;
+        l.done[k] = nullptr;
+    }
+    if (l.fork) cudaEventDestroy(l.fork);
+    l.fork = nullptr;
+    l.n = 0;
+}
+
 template <typename R, int MODE, int V>
-cudaError_t launch_face_variant(const VArgs<R>& a, cudaStream_t s) {
+cudaError_t launch_face_variant(const VArgs<R>& a, Fork& f) {
     using Cfg = FaceCfg<R, MODE>;
     if (a.n_nc > 0) {
         const int blocks = (a.n_nc + Cfg::FPB - 1) / Cfg::FPB;
-        kv_face<R, MODE, V><<<blocks, Cfg::THREADS, Cfg::SMEM, s>>>(a);
+        kv_face<R, MODE, V><<<blocks, Cfg::THREADS, Cfg::SMEM, f.next()>>>(a);
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
     const int npts = a.gp0[a.n_groups];
     if (npts > 0) {
-        kv_face_direct<R, MODE, V><<<(npts + 127) / 128, 128, 0, s>>>(a);
+        kv_face_direct<R, MODE, V><<<(npts + 127) / 128, 128, 0, f.next()>>>(a);
         return cudaGetLastError();
     }
     return cudaSuccess;
 }
 
 template <typename R, int MODE>
-cudaError_t launch_face(const VArgs<R>& a, cudaStream_t s) {
+cudaError_t launch_face(const VArgs<R>& a, Fork& f) {
     const bool v = MODE == kJump ? a.grad_vars != 0 : ((a.riemann >= 4 && a.riemann <= 8) || a.averaging >= 5);
-    return v ? launch_face_variant<R, MODE, 1>(a, s) : launch_face_variant<R, MODE, 0>(a, s);
+    return v ? launch_face_variant<R, MODE, 1>(a, f) : launch_face_variant<R, MODE, 0>(a, f);
+}
+template <typename R, int MODE>
+cudaError_t launch_face(const VArgs<R>& a, cudaStream_t s) {
+    Fork f(s);
+    return launch_face<R, MODE>(a, f);
 }
 
 // Item kernels of one class: 0 traces, 1 volume, 2 update, 3 update with the manufactured source.
@@ -1263,11 +1348,12 @@ cudaError_t launch_item_class(const VArgs<R>& a, int which, int n, size_t smem, 
 // compile-time P), each with the shared memory of its own largest item. which: 0 traces, 1 volume,
 // 2 update, 3 update with the manufactured source.
 template <typename R>
-cudaError_t launch_items(const VArgs<R>& a0, int which, cudaStream_t s, int store_grad = 0, int stage = 0,
+cudaError_t launch_items(const VArgs<R>& a0, int which, Fork& f, int store_grad = 0, int stage = 0,
                          double tshift = 0.0, int wq = 0) {
     for (int c = 0; c < kItemClasses; ++c) {
         const int n = a0.cls[c + 1] - a0.cls[c];
         if (n <= 0) continue;
+        const cudaStream_t s = f.next();
         VArgs<R> a = a0;
         a.item0 = a0.cls[c];
         const int cap = a0.ccap[c];
@@ -1289,6 +1375,13 @@ cudaError_t launch_items(const VArgs<R>& a0, int which, cudaStream_t s, int stor
     return cudaSuccess;
 }
 
+template <typename R>
+cudaError_t launch_items(const VArgs<R>& a0, int which, cudaStream_t s, int store_grad = 0, int stage = 0,
+                         double tshift = 0.0, int wq = 0) {
+    Fork f(s);
+    return launch_items(a0, which, f, store_grad, stage, tshift, wq);
+}
+
 template <typename R, int PC>
 cudaError_t set_item_attributes(size_t vol, size_t upd, size_t trc) {
     cudaError_t e;
@@ -1307,7 +1400,7 @@ cudaError_t set_item_attributes(size_t vol, size_t upd, size_t trc) {
 }
 
 template <typename R>
-cudaError_t vrun_stage(const VArgs<R>& a, int stage, double tshift, int flags, cudaStream_t s) {
+cudaError_t vrun_stage(const VArgs<R>& a, int stage, double tshift, int flags, cudaStream_t s, const Lanes* lanes) {
     const size_t vol = vitem_smem<R>(a.cap, a.split ? 29 : 20), trc = vitem_smem<R>(a.cap, 5);
     const size_t upd = std::max(vupdate_smem<R>(a.cap), vupdate_smem<R>(std::min(a.cap, kStageNodes)));
     if (stage == kPrepare) {
@@ -1331,13 +1424,29 @@ cudaError_t vrun_stage(const VArgs<R>& a, int stage, double tshift, int flags, c
             return e;
         return cudaSuccess;
     }
-    if (stage == kTraces) return launch_items(a, 0, s);
+    // each phase forks and joins; a failed launch still joins its lanes before the error returns
+    auto phase = [&](auto&& launches) -> cudaError_t {
+        Fork f(lanes, s);
+        f.note(launches(f));
+        return f.join();
+    };
+    if (stage == kTraces) return phase([&](Fork& f) { return launch_items(a, 0, f); });
     cudaError_t e;
-    if (a.ns && (e = launch_face<R, kJump>(a, s)) != cudaSuccess) return e;
-    if ((e = launch_items(a, 1, s, flags & kStoreGrad)) != cudaSuccess) return e;
-    if ((e = a.ns ? launch_face<R, kFluxNS>(a, s) : launch_face<R, kFluxEuler>(a, s)) != cudaSuccess) return e;
+    if (a.ns) {
+        // jumps -> volume (gradient traces) -> fluxes: three phases
+        if ((e = phase([&](Fork& f) { return launch_face<R, kJump>(a, f); })) != cudaSuccess) return e;
+        if ((e = phase([&](Fork& f) { return launch_items(a, 1, f, flags & kStoreGrad); })) != cudaSuccess) return e;
+        if ((e = phase([&](Fork& f) { return launch_face<R, kFluxNS>(a, f); })) != cudaSuccess) return e;
+    } else {
+        // Euler: the face fluxes read only the Q traces, so they run beside the volume kernels
+        e = phase([&](Fork& f) {
+            const cudaError_t ef = launch_face<R, kFluxEuler>(a, f);
+            return ef != cudaSuccess ? ef : launch_items(a, 1, f, flags & kStoreGrad);
+        });
+        if (e != cudaSuccess) return e;
+    }
     const int wq = (flags & kWriteQDot) ? 1 : 0;
-    return launch_items(a, a.source ? 3 : 2, s, 0, stage, tshift, wq);
+    return phase([&](Fork& f) { return launch_items(a, a.source ? 3 : 2, f, 0, stage, tshift, wq); });
 }
 
 // Average device time of each kernel alone: ms[0] volume, [1] face flux, [2] update (stage 1),

@@ -417,8 +417,8 @@ int static_pressure_residual(dg_ctx* c, const Gathered& h) {
         q[5 * g + 4] = 1.0 / c->pc.gm1;
     }
     if ((e = cudaMemcpyAsync(c->Q.p, q.data(), sizeof(double) * q.size(), cudaMemcpyHostToDevice, s)) ||
-        (e = fn(a, dg::kPrepare, 0.0, 0, s)) || (e = fn(a, dg::kTraces, 0.0, 0, s)) ||
-        (e = fn(a, -1, 0.0, dg::kWriteQDot, s)) ||
+        (e = fn(a, dg::kPrepare, 0.0, 0, s, nullptr)) || (e = fn(a, dg::kTraces, 0.0, 0, s, nullptr)) ||
+        (e = fn(a, -1, 0.0, dg::kWriteQDot, s, nullptr)) ||
         (e = cudaMemcpyAsync(q.data(), st.QDot.p, sizeof(double) * q.size(), cudaMemcpyDeviceToHost, s)) ||
         (e = cudaMemsetAsync(c->Q.p, 0, sizeof(double) * q.size(), s)) || (e = cudaStreamSynchronize(s)))
         return done(cuda_fail(e, "static pressure residual"));
@@ -626,6 +626,7 @@ int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, cons
     if ((e = cudaGetDevice(&c->device)) != cudaSuccess) return bail(cuda_fail(e, "cudaGetDevice"));
     if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess)
         return bail(cuda_fail(e, "cudaStreamCreate"));
+    if ((e = dg::create_lanes(c->lanes)) != cudaSuccess) return bail(cuda_fail(e, "side streams"));
     if ((e = cudaMallocHost(reinterpret_cast<void**>(&c->h_scal), sizeof(double) * (4 * n_cases + 8))) != cudaSuccess)
         return bail(cuda_fail(e, "cudaMallocHost"));
     cudaStream_t s = c->stream;
@@ -690,6 +691,7 @@ int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, cons
 }
 
 void release(dg_ctx* c) {
+    dg::destroy_lanes(c->lanes);
     c->v64.free();
     c->v32.free();
     for (auto* b : {&c->items, &c->faces4}) b->free();
@@ -736,8 +738,8 @@ int upload(dg_ctx* c, const double* q) {
 }
 
 cudaError_t stage(dg_ctx* c, int st, double tshift, int flags) {
-    if (c->mixed) return c->v32.stage(c->v32.args, st, tshift, flags, c->stream);
-    return c->v64.stage(c->v64.args, st, tshift, flags, c->stream);
+    if (c->mixed) return c->v32.stage(c->v32.args, st, tshift, flags, c->stream, &c->lanes);
+    return c->v64.stage(c->v64.args, st, tshift, flags, c->stream, &c->lanes);
 }
 
 cudaError_t enqueue_max_dt(dg_ctx* c, double cfl, double dcfl) {
@@ -830,7 +832,7 @@ int apply_items(dg_ctx* c, h3dctx::VStore<R>& st, const ItemTable& t) {
     a.cap = t.cap;
     for (int q = 0; q <= dg::kItemClasses; ++q) a.cls[q] = t.cls[q];
     for (int q = 0; q < dg::kItemClasses; ++q) a.ccap[q] = t.ccap[q];
-    CK(st.stage(a, dg::kPrepare, 0.0, 0, c->stream));
+    CK(st.stage(a, dg::kPrepare, 0.0, 0, c->stream, nullptr));
     h3dctx::drop_graphs(c);
     return DG_OK;
 }
@@ -855,7 +857,7 @@ int autotune_store(dg_ctx* c, h3dctx::VStore<R>& st, int reps) {
     {
         dg::VArgs<R> big = st.args;
         big.cap = 2 * kItemNodes;  // kernel attributes for the largest candidate
-        CK(st.stage(big, dg::kPrepare, 0.0, 0, s));
+        CK(st.stage(big, dg::kPrepare, 0.0, 0, s, nullptr));
     }
     const int candidates[] = {kItemNodes / 4, kItemNodes / 2, kItemNodes, 2 * kItemNodes};
     std::map<int, std::vector<int>> class_ords;  // class -> its order triples
