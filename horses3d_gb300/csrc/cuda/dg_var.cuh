@@ -135,6 +135,57 @@ __device__ __forceinline__ ItemDims item_dims(const int4 it) {
     return d;
 }
 
+// Quotient of a small non-negative integer by a runtime divisor through the FP32 reciprocal:
+// trunc((n + 1/2) rn(1/d)). (n + 1/2)/d lies at least 1/(2d) from an integer, and the two roundings
+// move the product by at most (n + 1/2)/d * 1.5 * 2^-23, which stays below 1/(2d) for n < 2^21; the
+// item and face indices decoded here are far below that. Five instructions instead of the integer
+// division's twenty.
+struct Div {
+    int d;
+    float r;
+};
+__device__ __forceinline__ Div make_div(int d) { return {d, __frcp_rn(static_cast<float>(d))}; }
+__device__ __forceinline__ int quot(int n, const Div& v) {
+    return __float2int_rz((static_cast<float>(n) + 0.5f) * v.r);
+}
+
+// Item node t -> (local element le, node n, indices i, j, k); compile-time orders keep the constant
+// divisions.
+template <int PC>
+struct NodeDecoder {
+    int np, px, py;
+    Div dnp, dpx, dpxy;
+    __device__ __forceinline__ explicit NodeDecoder(const ItemDims& d) : np(d.np), px(d.px), py(d.py) {
+        if constexpr (PC == 0) {
+            dnp = make_div(np);
+            dpx = make_div(px);
+            dpxy = make_div(px * py);
+        }
+    }
+    __device__ __forceinline__ void elem(int t, int& le, int& n) const {
+        if constexpr (PC > 0) le = t / (PC * PC * PC);
+        else le = quot(t, dnp);
+        n = t - le * np;
+    }
+    __device__ __forceinline__ void ijk(int n, int& i, int& j, int& k) const {
+        if constexpr (PC > 0) {
+            i = n % PC;
+            j = (n / PC) % PC;
+            k = n / (PC * PC);
+        } else {
+            const int a = quot(n, dpx);
+            k = quot(n, dpxy);
+            i = n - a * px;
+            j = a - k * py;
+        }
+    }
+};
+
+// Barrier of one group of nthreads threads (named barrier id, 1..15), e.g. the threads of one face.
+__device__ __forceinline__ void group_sync(int id, int nthreads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
 // Face point counts of a side (first, second face direction), sides numbered as the reference.
 __device__ __forceinline__ void side_dims(int side, int ord, int& d1, int& d2) {
     const int px = ord & 255, py = (ord >> 8) & 255, pz = (ord >> 16) & 255;
@@ -185,13 +236,14 @@ template <typename R, int NV, int PC>
 __device__ __forceinline__ void write_traces(const VArgs<R>& a, const ItemDims& d, const OpsP<R>* sO, const R* s,
                                              R* dst) {
     const int A = d.px * d.pz, B = d.px * d.py, C = d.py * d.pz, Te = 2 * (A + B + C);
+    const Div dte = make_div(Te), dx = make_div(d.px), dy = make_div(d.py);
     for (int t = threadIdx.x; t < d.count * Te; t += blockDim.x) {
-        const int le = t / Te;
+        const int le = PC ? t / (6 * PC * PC) : quot(t, dte);
         int p;
         const int side = side_of_task(t - le * Te, A, B, C, p);
         const int ns = side <= 2 ? A : ((side == 3 || side == 5) ? B : C);
         const int d1 = side <= 2 ? d.px : ((side == 3 || side == 5) ? d.px : d.py);
-        const int ca = p % d1, cb = p / d1;
+        const int cb = PC ? p / PC : quot(p, side == 4 || side == 6 ? dy : dx), ca = p - cb * d1;
         const int dir = side <= 2 ? 1 : ((side == 3 || side == 5) ? 2 : 0);
         const int L = dir == 0 ? d.px : (dir == 1 ? d.py : d.pz);
         const R* v = (side == 2 || side == 4 || side == 5) ? sO[dir].vR : sO[dir].vL;
@@ -224,8 +276,10 @@ __global__ void __launch_bounds__(256) kv_traces(VArgs<R> a) {
     R* sQ = reinterpret_cast<R*>(sO + 3);
     load_ops(a.ops, sO, d.px, d.py, d.pz);
     const double eref = a.cc[d.kase].e_ref;
+    const NodeDecoder<PC> nd(d);
     for (int t = threadIdx.x; t < d.ntot; t += blockDim.x) {
-        const int le = t / d.np, n = t - le * d.np;
+        int le, n;
+        nd.elem(t, le, n);
         const long long g = a.eoff[a.item_elems[d.first + le]] + n;
 #pragma unroll
         for (int v = 0; v < 4; ++v) sQ[v * d.ntot + t] = R(a.Q[5 * g + v]);
@@ -253,8 +307,10 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 0) kv_volume(VArgs<R
     // sQ holds the gradient variables while the gradient is formed: the state itself, or U(Q) for
     // the entropy and energy variables (then the fluxes below read the state from global memory)
     const bool gv = a.ns && ph.grad_vars != 0;
+    const NodeDecoder<PC> nd(d);
     for (int t = threadIdx.x; t < ntot; t += blockDim.x) {
-        const int le = t / np, n = t - le * np;
+        int le, n;
+        nd.elem(t, le, n);
         const long long g = a.eoff[a.item_elems[d.first + le]] + n;
         R x[5];
 #pragma unroll
@@ -274,8 +330,9 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 0) kv_volume(VArgs<R
     if (a.ns) {
         const int A = px * pz, B = px * py, C = py * pz;
         for (int t = threadIdx.x; t < ntot; t += blockDim.x) {
-            const int le = t / np, n = t - le * np;
-            const int i = n % px, j = (n / px) % py, k = n / (px * py);
+            int le, n, i, j, k;
+            nd.elem(t, le, n);
+            nd.ijk(n, i, j, k);
             const int e = a.item_elems[d.first + le];
             const long long g = a.eoff[e] + n;
             const R* q0 = sQ + le * np;
@@ -355,7 +412,8 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 0) kv_volume(VArgs<R
     }
     // contravariant fluxes F = Finv - Fvisc at each node, over the node's own gradient column
     for (int t = threadIdx.x; t < ntot; t += blockDim.x) {
-        const int le = t / np, n = t - le * np;
+        int le, n;
+        nd.elem(t, le, n);
         const long long g = a.eoff[a.item_elems[d.first + le]] + n;
         R q[5], jx[3], je[3], jz[3];
         if (gv) {
@@ -421,8 +479,9 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 0) kv_volume(VArgs<R
         // two-point flux of each pair evaluated with the lower line index as "left" and the node's
         // own contravariant Euler flux at l = i; QDot = -volInt.
         for (int t = threadIdx.x; t < ntot; t += blockDim.x) {
-            const int le = t / np, n = t - le * np;
-            const int i = n % px, j = (n / px) % py, k = n / (px * py);
+            int le, n, i, j, k;
+            nd.elem(t, le, n);
+            nd.ijk(n, i, j, k);
             const long long g = a.eoff[a.item_elems[d.first + le]] + n;
             const int b0 = le * np;
             R q[5], jm[3][3];
@@ -469,8 +528,9 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 0) kv_volume(VArgs<R
     }
     // ScalarWeakIntegrals_StdVolumeGreen
     for (int t = threadIdx.x; t < ntot; t += blockDim.x) {
-        const int le = t / np, n = t - le * np;
-        const int i = n % px, j = (n / px) % py, k = n / (px * py);
+        int le, n, i, j, k;
+        nd.elem(t, le, n);
+        nd.ijk(n, i, j, k);
         const long long g = a.eoff[a.item_elems[d.first + le]] + n;
         const R* F0 = sG + le * np;
         R acc[5] = {0, 0, 0, 0, 0};
@@ -516,15 +576,17 @@ struct FaceCfg {
 };
 
 // Interpolation of NV values from (s1 x s2) points in S to the face's (q1 x q2) points; returns the
-// buffer that holds the result (S or A). Every thread of the CTA must call it (it synchronises).
+// buffer that holds the result (S or A). Every thread of the face's group must call it (it
+// synchronises the group on barrier bar).
 template <typename R, int NV>
 __device__ __forceinline__ R* to_face_points(const R* tset, R* S, R* A, int s1, int s2, int q1, int q2, int lane,
-                                             bool active) {
+                                             bool active, int bar) {
     const bool d1 = active && s1 != q1, d2 = active && s2 != q2;
+    const Div dq1 = make_div(q1);
     if (d1) {  // along the first face direction: A(i, l) = sum_m T1(i, m) S(m, l)
         const R* T = tset + ((s1 - 1) * kMaxP + (q1 - 1)) * kTsetStride;
         for (int p = lane; p < q1 * s2; p += kFacePts) {
-            const int i = p % q1, l = p / q1;
+            const int l = quot(p, dq1), i = p - l * q1;
             R acc[NV];
 #pragma unroll
             for (int v = 0; v < NV; ++v) acc[v] = R(0);
@@ -537,13 +599,13 @@ __device__ __forceinline__ R* to_face_points(const R* tset, R* S, R* A, int s1, 
             for (int v = 0; v < NV; ++v) A[v * kFacePts + p] = acc[v];
         }
     }
-    __syncthreads();
+    group_sync(bar, kFacePts);
     R* cur = d1 ? A : S;
     R* nxt = d1 ? S : A;
     if (d2) {  // along the second: nxt(i, j) = sum_l T2(j, l) cur(i, l)
         const R* T = tset + ((s2 - 1) * kMaxP + (q2 - 1)) * kTsetStride;
         for (int p = lane; p < q1 * q2; p += kFacePts) {
-            const int i = p % q1, j = p / q1;
+            const int j = quot(p, dq1), i = p - j * q1;
             R acc[NV];
 #pragma unroll
             for (int v = 0; v < NV; ++v) acc[v] = R(0);
@@ -556,7 +618,7 @@ __device__ __forceinline__ R* to_face_points(const R* tset, R* S, R* A, int s1, 
             for (int v = 0; v < NV; ++v) nxt[v * kFacePts + p] = acc[v];
         }
     }
-    __syncthreads();
+    group_sync(bar, kFacePts);
     return d2 ? nxt : cur;
 }
 
@@ -609,8 +671,9 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS, (sizeof(R) == 4 && 
                 for (int c = 0; c < 15; ++c) SL[(5 + c) * NP + p] = a.GF[offL * 15 + c * nL + p];
             }
         }
+        const Div ds1R = make_div(s1R);
         for (int p = lane; p < nR; p += NP) {  // right trace in the left side's orientation
-            const int i = p % s1R, j = p / s1R;
+            const int j = quot(p, ds1R), i = p - j * s1R;
             int ii, jj;
             left2right(i, j, s1R - 1, s2R - 1, rot, ii, jj);
             const int src = ii + r1 * jj;
@@ -622,9 +685,10 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS, (sizeof(R) == 4 && 
             }
         }
     }
-    __syncthreads();
-    const R* XL = to_face_points<R, NVIN>(a.tset, SL, AL, l1, l2, q1, q2, lane, active);
-    const R* XR = to_face_points<R, NVIN>(a.tset, SR, AR, s1R, s2R, q1, q2, lane, active);
+    const int bar = 1 + grp;  // the face's own barrier: the groups of a CTA never wait for each other
+    group_sync(bar, NP);
+    const R* XL = to_face_points<R, NVIN>(a.tset, SL, AL, l1, l2, q1, q2, lane, active, bar);
+    const R* XR = to_face_points<R, NVIN>(a.tset, SR, AR, s1R, s2R, q1, q2, lane, active, bar);
     R out[NVOUT];
     const bool point = active && lane < q1 * q2;
     if (point) {
@@ -699,19 +763,20 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS, (sizeof(R) == 4 && 
             for (int v = 0; v < 5; ++v) out[v] = (inv[v] - visc[v]) * J;
         }
     }
-    __syncthreads();  // the traces are consumed: SL holds the face values from here on
+    group_sync(bar, NP);  // the traces are consumed: SL holds the face values from here on
     if (point) {
 #pragma unroll
         for (int v = 0; v < NVOUT; ++v) SL[v * NP + lane] = out[v];
     }
-    __syncthreads();
+    group_sync(bar, NP);
     // projection to each side's order (transposed Tset), first direction into AL / AR
     const bool pL1 = active && l1 != q1, pL2 = active && l2 != q2;
     const bool pR1 = active && s1R != q1, pR2 = active && s2R != q2;
+    const Div dl1 = make_div(l1), dsR = make_div(s1R);
     if (pL1) {
         const R* T = a.tset + ((q1 - 1) * kMaxP + (l1 - 1)) * kTsetStride;
         for (int p = lane; p < l1 * q2; p += NP) {
-            const int i = p % l1, l = p / l1;
+            const int l = quot(p, dl1), i = p - l * l1;
 #pragma unroll
             for (int v = 0; v < NVOUT; ++v) {
                 R acc = R(0);
@@ -723,7 +788,7 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS, (sizeof(R) == 4 && 
     if (pR1) {
         const R* T = a.tset + ((q1 - 1) * kMaxP + (s1R - 1)) * kTsetStride;
         for (int p = lane; p < s1R * q2; p += NP) {
-            const int i = p % s1R, l = p / s1R;
+            const int l = quot(p, dsR), i = p - l * s1R;
 #pragma unroll
             for (int v = 0; v < NVOUT; ++v) {
                 R acc = R(0);
@@ -732,7 +797,7 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS, (sizeof(R) == 4 && 
             }
         }
     }
-    __syncthreads();
+    group_sync(bar, NP);
     if (!active) return;
     R* dstL = MODE == kJump ? a.UJ + offL * 15 : a.FS + offL * 5;
     R* dstR = MODE == kJump ? a.UJ + offR * 15 : a.FS + offR * 5;
@@ -741,7 +806,7 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS, (sizeof(R) == 4 && 
         const R* src = pL1 ? AL : SL;  // (l1 x q2) points
         const R* T = a.tset + ((q2 - 1) * kMaxP + (l2 - 1)) * kTsetStride;
         for (int p = lane; p < nL; p += NP) {
-            const int i = p % l1, j = p / l1;
+            const int j = quot(p, dl1), i = p - j * l1;
 #pragma unroll
             for (int v = 0; v < NVOUT; ++v) {
                 R val;
@@ -759,7 +824,7 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS, (sizeof(R) == 4 && 
         const R* src = pR1 ? AR : SL;  // (s1R x q2) points
         const R* T = a.tset + ((q2 - 1) * kMaxP + (s2R - 1)) * kTsetStride;
         for (int p = lane; p < nR; p += NP) {
-            const int i = p % s1R, j = p / s1R;
+            const int j = quot(p, dsR), i = p - j * s1R;
             int ii, jj;
             left2right(i, j, s1R - 1, s2R - 1, rot, ii, jj);
             const int o = ii + r1 * jj;
@@ -978,9 +1043,11 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 && !SRC && !PST ? 6 : 0)
     const double ak = stage == 0 ? 0.0 : (stage == 1 ? -5.0 / 9.0 : -153.0 / 128.0);
     const double ck = stage == 0 ? 1.0 / 3.0 : (stage == 1 ? 15.0 / 16.0 : 8.0 / 15.0);
     const int A = px * d.pz, B = px * py, C = py * d.pz;
+    const NodeDecoder<PC> nd(d);
     for (int t = threadIdx.x; t < ntot; t += blockDim.x) {
-        const int le = t / np, n = t - le * np;
-        const int i = n % px, j = (n / px) % py, k = n / (px * py);
+        int le, n, i, j, k;
+        nd.elem(t, le, n);
+        nd.ijk(n, i, j, k);
         const int e = a.item_elems[d.first + le];
         const long long g = a.eoff[e] + n;
         const long long s0 = 6LL * e;
