@@ -181,11 +181,6 @@ struct NodeDecoder {
     }
 };
 
-// Barrier of one group of nthreads threads (named barrier id, 1..15), e.g. the threads of one face.
-__device__ __forceinline__ void group_sync(int id, int nthreads) {
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
-}
-
 // Face point counts of a side (first, second face direction), sides numbered as the reference.
 __device__ __forceinline__ void side_dims(int side, int ord, int& d1, int& d2) {
     const int px = ord & 255, py = (ord >> 8) & 255, pz = (ord >> 16) & 255;
@@ -576,11 +571,10 @@ struct FaceCfg {
 };
 
 // Interpolation of NV values from (s1 x s2) points in S to the face's (q1 x q2) points; returns the
-// buffer that holds the result (S or A). Every thread of the face's group must call it (it
-// synchronises the group on barrier bar).
+// buffer that holds the result (S or A). Every thread of the CTA must call it (it synchronises).
 template <typename R, int NV>
 __device__ __forceinline__ R* to_face_points(const R* tset, R* S, R* A, int s1, int s2, int q1, int q2, int lane,
-                                             bool active, int bar) {
+                                             bool active) {
     const bool d1 = active && s1 != q1, d2 = active && s2 != q2;
     const Div dq1 = make_div(q1);
     if (d1) {  // along the first face direction: A(i, l) = sum_m T1(i, m) S(m, l)
@@ -599,7 +593,7 @@ __device__ __forceinline__ R* to_face_points(const R* tset, R* S, R* A, int s1, 
             for (int v = 0; v < NV; ++v) A[v * kFacePts + p] = acc[v];
         }
     }
-    group_sync(bar, kFacePts);
+    __syncthreads();
     R* cur = d1 ? A : S;
     R* nxt = d1 ? S : A;
     if (d2) {  // along the second: nxt(i, j) = sum_l T2(j, l) cur(i, l)
@@ -618,7 +612,7 @@ __device__ __forceinline__ R* to_face_points(const R* tset, R* S, R* A, int s1, 
             for (int v = 0; v < NV; ++v) nxt[v * kFacePts + p] = acc[v];
         }
     }
-    group_sync(bar, kFacePts);
+    __syncthreads();
     return d2 ? nxt : cur;
 }
 
@@ -685,10 +679,9 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS, (sizeof(R) == 4 && 
             }
         }
     }
-    const int bar = 1 + grp;  // the face's own barrier: the groups of a CTA never wait for each other
-    group_sync(bar, NP);
-    const R* XL = to_face_points<R, NVIN>(a.tset, SL, AL, l1, l2, q1, q2, lane, active, bar);
-    const R* XR = to_face_points<R, NVIN>(a.tset, SR, AR, s1R, s2R, q1, q2, lane, active, bar);
+    __syncthreads();
+    const R* XL = to_face_points<R, NVIN>(a.tset, SL, AL, l1, l2, q1, q2, lane, active);
+    const R* XR = to_face_points<R, NVIN>(a.tset, SR, AR, s1R, s2R, q1, q2, lane, active);
     R out[NVOUT];
     const bool point = active && lane < q1 * q2;
     if (point) {
@@ -763,12 +756,12 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS, (sizeof(R) == 4 && 
             for (int v = 0; v < 5; ++v) out[v] = (inv[v] - visc[v]) * J;
         }
     }
-    group_sync(bar, NP);  // the traces are consumed: SL holds the face values from here on
+    __syncthreads();  // the traces are consumed: SL holds the face values from here on
     if (point) {
 #pragma unroll
         for (int v = 0; v < NVOUT; ++v) SL[v * NP + lane] = out[v];
     }
-    group_sync(bar, NP);
+    __syncthreads();
     // projection to each side's order (transposed Tset), first direction into AL / AR
     const bool pL1 = active && l1 != q1, pL2 = active && l2 != q2;
     const bool pR1 = active && s1R != q1, pR2 = active && s2R != q2;
@@ -797,7 +790,7 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS, (sizeof(R) == 4 && 
             }
         }
     }
-    group_sync(bar, NP);
+    __syncthreads();
     if (!active) return;
     R* dstL = MODE == kJump ? a.UJ + offL * 15 : a.FS + offL * 5;
     R* dstR = MODE == kJump ? a.UJ + offR * 15 : a.FS + offR * 5;
