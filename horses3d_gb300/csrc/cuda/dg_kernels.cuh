@@ -1079,6 +1079,33 @@ __device__ __forceinline__ void monitor_partial(const unsigned long long m[5], i
     if ((t & 31) == 0) sp.w[w] = p;
 }
 
+// First half of the FP32 form: the maxima of the |QDot| bit patterns (31 bits), the minima of the
+// estimates' bit patterns (non-negative floats and NaN, which order like their patterns and lose to
+// every number as fminf does) and the flag by single-instruction warp reductions.
+template <int NT>
+__device__ __forceinline__ void monitor_partial32(const unsigned m[5], int bad, float cv, float vs,
+                                                  MonitorScratch<NT>& sp) {
+    static_assert(NT >= 32, "warp 0 is full");
+    const int t = threadIdx.x, w = t >> 5;
+    const int cnt = NT - 32 * w < 32 ? NT - 32 * w : 32;
+    const unsigned mask = cnt == 32 ? 0xffffffffu : (1u << cnt) - 1u;
+    unsigned mm[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) mm[v] = __reduce_max_sync(mask, m[v]);
+    const unsigned c = __reduce_min_sync(mask, __float_as_uint(cv));
+    const unsigned ww = __reduce_min_sync(mask, __float_as_uint(vs));
+    const unsigned b = __reduce_or_sync(mask, bad ? 1u : 0u);
+    if ((t & 31) == 0) {
+        MonitorPart p;
+#pragma unroll
+        for (int v = 0; v < 5; ++v) p.m[v] = abs_bits_as_double(mm[v], static_cast<const float*>(nullptr));
+        p.c = __uint_as_float(c);
+        p.w = __uint_as_float(ww);
+        p.b = static_cast<int>(b);
+        sp.w[w] = p;
+    }
+}
+
 // Second half (after the barrier, warp 0): the warp partials folded, the record written by thread 0.
 template <int NT>
 __device__ __forceinline__ void monitor_finish(const MonitorScratch<NT>& sp, unsigned long long* out) {
@@ -1206,19 +1233,25 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
     if constexpr (FUSE) {
         // ComputeMaxResiduals (max |QDot| of this stage) and checkForNan (the new Q) of the element,
         // and the FP32 time-step estimates of the new state (the first pass of MaxTimeStep)
-        unsigned long long m[5];
         int bad = 0;
 #pragma unroll
-        for (int v = 0; v < 5; ++v) {
-            m[v] = abs_bits_as_double(abs_bits(qd[v]), static_cast<const R*>(nullptr));
-            bad |= nonfinite(qq[v]);
-        }
+        for (int v = 0; v < 5; ++v) bad |= nonfinite(qq[v]);
         float cv, vs;
         if constexpr (STAGE_JA)
             dt_estimate(a.dtc, qq, sJa + 3 * n, sJa + 3 * P3 + 3 * n, sJa + 6 * P3 + 3 * n, sJ[n], cv, vs);
         else
             dt_estimate(a.dtc, qq, a.ja_xi + 3 * g, a.ja_eta + 3 * g, a.ja_zeta + 3 * g, sJ[n], cv, vs);
-        monitor_partial<P3>(m, bad, cv, vs, smon);
+        if constexpr (sizeof(R) == 4) {
+            unsigned m[5];
+#pragma unroll
+            for (int v = 0; v < 5; ++v) m[v] = static_cast<unsigned>(abs_bits(qd[v]));
+            monitor_partial32<P3>(m, bad, cv, vs, smon);
+        } else {
+            unsigned long long m[5];
+#pragma unroll
+            for (int v = 0; v < 5; ++v) m[v] = abs_bits(qd[v]);
+            monitor_partial<P3>(m, bad, cv, vs, smon);
+        }
     }
     fence_proxy_async_smem();  // this thread's Q, G writes before the bulk stores read them
     __syncthreads();
