@@ -160,21 +160,35 @@ cudaError_t run_stage(dg_ctx* c, int stage, double tshift, int flags) {
 
 // Queue one RK3 step (time and dt are read from device memory). The last stage keeps its QDot for
 // the residuals, as TakeRK3Step leaves the third stage's QDot in storage.
-cudaError_t enqueue_step(dg_ctx* c, bool fuse_monitor = false) {
+// fuse_monitor: the last stage's update writes the elements' residual records; with fused_dt (CFL
+// steps) the first stage's volume kernel writes the time-step estimates and the step's dt is formed
+// between the first stage's volume and flux kernels (enqueue_max_dt_fused).
+cudaError_t enqueue_max_dt_fused(dg_ctx* c, double cfl, double dcfl);
+cudaError_t enqueue_step(dg_ctx* c, bool fuse_monitor = false, bool fused_dt = false, double cfl = 0.0,
+                         double dcfl = 0.0) {
     static const double b[3] = {0.0, 1.0 / 3.0, 3.0 / 4.0};
     for (int k = 0; k < 3; ++k) {
         const int last = dg::kWriteQDot | (c->keep_grad ? dg::kStoreGrad : 0) | (fuse_monitor ? dg::kFuseMonitor : 0);
-        cudaError_t e = run_stage(c, k, b[k], k == 2 ? last : 0);
+        cudaError_t e;
+        if (k == 0 && fused_dt) {
+            e = run_stage(c, 0, b[0], dg::kVolumeOnly | dg::kEstimateDt);
+            if (e == cudaSuccess) e = enqueue_max_dt_fused(c, cfl, dcfl);
+            if (e == cudaSuccess) e = run_stage(c, 0, b[0], dg::kSurfaceOnly);
+        } else {
+            e = run_stage(c, k, b[k], k == 2 ? last : 0);
+        }
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
 }
 
-// The monitored time loop can take its residuals, NaN test and MaxTimeStep estimate from the last
-// stage's update (uniform orders with the bulk-copy update, whole meshes).
+// The monitored time loop takes its residuals and NaN test from the last stage's update and its
+// MaxTimeStep estimate from the first stage's volume kernel (uniform orders with the one-element
+// kernels, whole meshes, the CUDA-core volume form).
 bool fused_monitor(const dg_ctx* c) {
     if (c->var || c->n_ghost != 0) return false;
-    return c->mixed ? c->s32.mon.begin != nullptr : c->s64.mon.begin != nullptr;
+    if (c->mixed && c->s32.args.tc) return false;
+    return c->mixed ? c->s32.mon.dt != nullptr : c->s64.mon.dt != nullptr;
 }
 
 dg::DtArgs dt_args(dg_ctx* c, double cfl, double dcfl) {
@@ -203,14 +217,9 @@ int setup_fused_monitor(dg_ctx* c, double cfl, double dcfl) {
     return DG_OK;
 }
 
-cudaError_t enqueue_monitor_begin(dg_ctx* c) {
-    return c->mixed ? c->s32.mon.begin(c->s32.args, c->red.p, c->nan_flag.p, c->stream)
-                    : c->s64.mon.begin(c->s64.args, c->red.p, c->nan_flag.p, c->stream);
-}
-
 cudaError_t enqueue_max_dt_fused(dg_ctx* c, double cfl, double dcfl) {
     const dg::DtArgs d = dt_args(c, cfl, dcfl);
-    cudaError_t e = c->mixed ? c->s32.mon.exact(c->s32.args, d, c->stream) : c->s64.mon.exact(c->s64.args, d, c->stream);
+    cudaError_t e = c->mixed ? c->s32.mon.dt(c->s32.args, d, c->stream) : c->s64.mon.dt(c->s64.args, d, c->stream);
     if (e != cudaSuccess) return e;
     dg::k_dt_final<<<1, 1, 0, c->stream>>>(c->red.p, c->scal.p + 1);
     return cudaGetLastError();
@@ -725,8 +734,8 @@ int prepare_monitor_graph(dg_ctx* c, int mode, double cfl, double dcfl) {
     }
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
-    if (mode == 1) e = fused ? enqueue_max_dt_fused(c, cfl, dcfl) : enqueue_max_dt(c, cfl, dcfl);
-    if (e == cudaSuccess) e = enqueue_step(c, fused);
+    if (mode == 1 && !fused) e = enqueue_max_dt(c, cfl, dcfl);
+    if (e == cudaSuccess) e = enqueue_step(c, fused, fused && mode == 1, cfl, dcfl);
     if (e == cudaSuccess) {
         if (c->var) {
             e = h3dvar::enqueue_advance_time(c);
@@ -850,13 +859,7 @@ int integrate_core(dg_ctx* c, int n, int mode, double cfl, double dcfl, double* 
     int rc = prepare_monitor_graph(c, mode, cfl, dcfl);
     if (rc) return rc;
     CK(cudaMemsetAsync(c->mon_count.p, 0, sizeof(int), c->stream));
-    const bool fused = fused_monitor(c);
-    if (fused) CK(enqueue_monitor_begin(c));  // the records of the current state: the first step's estimate
     for (int s = 0; s < n; ++s) CK(cudaGraphLaunch(c->mgraph, c->stream));
-    if (fused) {  // the estimate slot must not carry this loop's minimum into a later MaxTimeStep
-        dg::k_reset_estimate<<<1, 1, 0, c->stream>>>(c->red.p);
-        CK(cudaGetLastError());
-    }
     std::vector<double> rows(static_cast<size_t>(n) * 6 * nc);
     CK(cudaMemcpyAsync(rows.data(), c->mon.p, sizeof(double) * rows.size(), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(c->h_scal, c->scal.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream));

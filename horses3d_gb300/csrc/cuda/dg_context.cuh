@@ -55,7 +55,7 @@ struct Store {
     dg::Args<R> args;
     dg::StageFn<R> stage = nullptr;
     dg::KernelTimesFn<R> times = nullptr;
-    dg::MonitorFns<R> mon{nullptr, nullptr};  // fused time-loop monitor (the kTmaUpdate orders)
+    dg::MonitorFns<R> mon{nullptr};  // fused time-loop monitor (the one-element-per-CTA orders)
     void free() {
         for (DevBuf<R>* b : {&ja_xi, &ja_eta, &ja_zeta, &jac, &inv_jac, &fn, &ft1, &ft2, &fj, &sgeo, &QDot, &Ux, &Uy,
                              &Uz, &QF, &FV, &FS})

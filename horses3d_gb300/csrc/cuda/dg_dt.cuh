@@ -70,9 +70,8 @@ __host__ __device__ inline DtConst32 dt_const32(double cfl, double dcfl, const d
 
 // FP32 estimates of one node's convective and viscous time-step limits.
 template <typename R>
-__device__ __forceinline__ void dt_estimate(const DtConst32& d, const double* Q, const R* jx, const R* je, const R* jz,
-                                            R jac, float& conv, float& visc) {
-    const float rho = to_f32(Q[0]), ru = to_f32(Q[1]), rv = to_f32(Q[2]), rw = to_f32(Q[3]), E = to_f32(Q[4]);
+__device__ __forceinline__ void dt_estimate_f(const DtConst32& d, float rho, float ru, float rv, float rw, float E,
+                                              const R* jx, const R* je, const R* jz, R jac, float& conv, float& visc) {
     const float ir = 1.0f / rho;
     const float p = d.gm1 * (E - 0.5f * (ru * ru + rv * rv + rw * rw) * ir);
     const float a = sqrtf(d.gamma * p * ir);
@@ -93,6 +92,17 @@ __device__ __forceinline__ void dt_estimate(const DtConst32& d, const double* Q,
         for (int r = 0; r < 3; ++r) lv += mu * d.dxi2[r] * fabsf(float(ja[r][0]) + float(ja[r][1]) + float(ja[r][2]));
         visc = d.dcfl * J / lv;
     }
+}
+
+// A working-precision value rounded to FP32 (the identity for FP32).
+__device__ __forceinline__ float as_f32(float x) { return x; }
+__device__ __forceinline__ float as_f32(double x) { return to_f32(x); }
+
+// The estimate of the FP64 state Q (each value rounded to FP32 as the FP64 expressions' inputs).
+template <typename R>
+__device__ __forceinline__ void dt_estimate(const DtConst32& d, const double* Q, const R* jx, const R* je, const R* jz,
+                                            R jac, float& conv, float& visc) {
+    dt_estimate_f(d, to_f32(Q[0]), to_f32(Q[1]), to_f32(Q[2]), to_f32(Q[3]), to_f32(Q[4]), jx, je, jz, jac, conv, visc);
 }
 
 // The exact FP64 limits of one node (the reference's expressions and operation order).

@@ -4,10 +4,9 @@
 namespace dg {
 
 MonitorFns<float> monitor_fns_fp32(int P, bool gl) {
-    MonitorFns<float> f{nullptr, nullptr};
+    MonitorFns<float> f{nullptr};
     if (P == 6) {
-        f.begin = gl ? monitor_begin<6, true, float> : monitor_begin<6, false, float>;
-        f.exact = gl ? monitor_exact<6, true, float> : monitor_exact<6, false, float>;
+        f.dt = gl ? monitor_dt<6, true, float> : monitor_dt<6, false, float>;
     }
     return f;
 }

@@ -4,10 +4,9 @@
 namespace dg {
 
 MonitorFns<double> monitor_fns_fp64(int P, bool gl) {
-    MonitorFns<double> f{nullptr, nullptr};
+    MonitorFns<double> f{nullptr};
     if (P == 6) {
-        f.begin = gl ? monitor_begin<6, true, double> : monitor_begin<6, false, double>;
-        f.exact = gl ? monitor_exact<6, true, double> : monitor_exact<6, false, double>;
+        f.dt = gl ? monitor_dt<6, true, double> : monitor_dt<6, false, double>;
     }
     return f;
 }

@@ -342,11 +342,16 @@ __global__ void __launch_bounds__(Geo<P>::THREADS) k_traces(Args<R> a) {
 // ------------------------------------------------------------------------------------------------
 // k_volume: gradient, BR1 lifting, viscous normal fluxes on the faces, volume integral -> QDot.
 // ------------------------------------------------------------------------------------------------
-template <int P, bool GL, typename R, bool TC = false>
+// EST (the first stage of a step of the monitored time loop): the FP32 MaxTimeStep estimate of the
+// step's initial state at every node, its element minima into the element's monitor record
+// (a.mon[8e + 6], [8e + 7]), from the state and metric terms the kernel loads anyway.
+template <int P, bool GL, typename R, bool TC = false, bool EST = false>
 __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_volume(Args<R> a, int store_grad) {
     using L = VolLayout<P, R>;
     constexpr int P2 = Geo<P>::P2, P3 = Geo<P>::P3, F6 = 6 * P2;
     static_assert(!TC || (Geo<P>::EPB == 1 && 5 * P2 <= 192 && P + 2 <= 16), "tensor-core gradient: one element per CTA");
+    static_assert(!EST || (Geo<P>::EPB == 1 && !TC), "time-step estimate: one element per CTA");
+    __shared__ uint2 est_part[EST ? (P3 + 31) / 32 : 1];
     const bool split = a.inviscid != 0;
     const bool ns = a.ph.ns;
     extern __shared__ __align__(16) unsigned char dsm[];
@@ -404,7 +409,32 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
             jzs[c] = a.ja_zeta[3 * g + c];
         }
     }
+    if constexpr (EST) {
+        // the FP32 inputs of the estimate: the state rounded to FP32 (the mixed form's q already is,
+        // except the energy, which it holds relative to e_ref)
+        float cv, vs;
+        const float E = sizeof(R) == 4 ? to_f32(a.Q[5 * g + 4]) : as_f32(q[4]);
+        dt_estimate_f(a.dtc, as_f32(q[0]), as_f32(q[1]), as_f32(q[2]), as_f32(q[3]), E, jxs, jes, jzs, a.jac[g], cv, vs);
+        const int w = n >> 5, cnt = P3 - 32 * w < 32 ? P3 - 32 * w : 32;
+        const unsigned mask = cnt == 32 ? 0xffffffffu : (1u << cnt) - 1u;
+        // minima of non-negative floats (and NaN, which loses to every number) by their bit patterns
+        const unsigned c = __reduce_min_sync(mask, __float_as_uint(cv));
+        const unsigned v = __reduce_min_sync(mask, __float_as_uint(vs));
+        if ((n & 31) == 0) est_part[w] = make_uint2(c, v);
+    }
     __syncthreads();
+    if constexpr (EST) {
+        if (n < 32) {
+            constexpr int NW = (P3 + 31) / 32;
+            const uint2 p = n < NW ? est_part[n] : make_uint2(0xffffffffu, 0xffffffffu);
+            const unsigned c = __reduce_min_sync(0xffffffffu, p.x);
+            const unsigned v = __reduce_min_sync(0xffffffffu, p.y);
+            if (n == 0) {
+                a.mon[8 * static_cast<int64_t>(e) + 6] = c;
+                a.mon[8 * static_cast<int64_t>(e) + 7] = v;
+            }
+        }
+    }
     if constexpr (TC) {
         // Gradient contractions on the tensor cores (HexElement_ComputeLocalGradient,
         // HexElementClass.f90:427-531, and the Q traces of ProlongSolutionToFaces): per direction,
@@ -1024,37 +1054,15 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
     }
 }
 
-// The monitor record of one element (one CTA of NT threads): max |QDot| per variable (FP64 bit
-// images), a NaN/Inf flag and the minima of the FP32 time-step estimates. Each warp reduces its
-// lanes by shuffles (the CTA may end in a partial warp, whose missing lanes are left out), warp 0
-// folds the warp partials, thread 0 writes the record.
+// The residual record of one element (one CTA of NT threads) in the monitored time loop: max |QDot|
+// per variable (FP64 bit images) and a NaN/Inf flag, words 0..5 of the element's 8-word record (the
+// volume kernel of the step's first stage writes the time-step estimates into words 6 and 7). Each
+// warp reduces its lanes (the CTA may end in a partial warp, whose missing lanes are left out) into
+// shared memory before a CTA barrier; after it warp 0 folds the warp partials.
 struct MonitorPart {
     unsigned long long m[5];
-    float c, w;
     int b;
 };
-
-__device__ __forceinline__ void monitor_fold(MonitorPart& p, const MonitorPart& q) {
-#pragma unroll
-    for (int v = 0; v < 5; ++v) p.m[v] = q.m[v] > p.m[v] ? q.m[v] : p.m[v];
-    p.c = fminf(p.c, q.c);
-    p.w = fminf(p.w, q.w);
-    p.b |= q.b;
-}
-
-// Shuffle-down reduction over the first `cnt` lanes of a warp (mask: exactly those lanes).
-__device__ __forceinline__ void monitor_warp(MonitorPart& p, unsigned mask, int cnt) {
-    const int lane = threadIdx.x & 31;
-    for (int o = 16; o > 0; o >>= 1) {
-        MonitorPart q;
-#pragma unroll
-        for (int v = 0; v < 5; ++v) q.m[v] = __shfl_down_sync(mask, p.m[v], o);
-        q.c = __shfl_down_sync(mask, p.c, o);
-        q.w = __shfl_down_sync(mask, p.w, o);
-        q.b = __shfl_down_sync(mask, p.b, o);
-        if (lane + o < cnt) monitor_fold(p, q);
-    }
-}
 
 template <int NT>
 struct MonitorScratch {
@@ -1062,51 +1070,63 @@ struct MonitorScratch {
     MonitorPart w[NW];
 };
 
-// First half: every warp's partial record into shared memory (before a CTA barrier).
+// Shuffle-down maximum over the first `cnt` lanes of a warp (mask: exactly those lanes).
+__device__ __forceinline__ void monitor_warp(MonitorPart& p, unsigned mask, int cnt) {
+    const int lane = threadIdx.x & 31;
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long q[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) q[v] = __shfl_down_sync(mask, p.m[v], o);
+        const int qb = __shfl_down_sync(mask, p.b, o);
+        if (lane + o < cnt) {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) p.m[v] = q[v] > p.m[v] ? q[v] : p.m[v];
+            p.b |= qb;
+        }
+    }
+}
+
+__device__ __forceinline__ unsigned warp_lanes_mask(int nt, int w, int& cnt) {
+    cnt = nt - 32 * w < 32 ? nt - 32 * w : 32;
+    return cnt == 32 ? 0xffffffffu : (1u << cnt) - 1u;
+}
+
+// First half, FP64 patterns (63 bits): shuffles.
 template <int NT>
-__device__ __forceinline__ void monitor_partial(const unsigned long long m[5], int bad, float cv, float vs,
-                                                MonitorScratch<NT>& sp) {
+__device__ __forceinline__ void monitor_partial(const unsigned long long m[5], int bad, MonitorScratch<NT>& sp) {
     static_assert(NT >= 32, "warp 0 is full");
     const int t = threadIdx.x, w = t >> 5;
     MonitorPart p;
 #pragma unroll
     for (int v = 0; v < 5; ++v) p.m[v] = m[v];
-    p.c = cv;
-    p.w = vs;
     p.b = bad;
-    const int cnt = NT - 32 * w < 32 ? NT - 32 * w : 32;
-    monitor_warp(p, cnt == 32 ? 0xffffffffu : (1u << cnt) - 1u, cnt);
+    int cnt;
+    const unsigned mask = warp_lanes_mask(NT, w, cnt);
+    monitor_warp(p, mask, cnt);
     if ((t & 31) == 0) sp.w[w] = p;
 }
 
-// First half of the FP32 form: the maxima of the |QDot| bit patterns (31 bits), the minima of the
-// estimates' bit patterns (non-negative floats and NaN, which order like their patterns and lose to
-// every number as fminf does) and the flag by single-instruction warp reductions.
+// First half, FP32 patterns (31 bits): single-instruction warp reductions.
 template <int NT>
-__device__ __forceinline__ void monitor_partial32(const unsigned m[5], int bad, float cv, float vs,
-                                                  MonitorScratch<NT>& sp) {
+__device__ __forceinline__ void monitor_partial32(const unsigned m[5], int bad, MonitorScratch<NT>& sp) {
     static_assert(NT >= 32, "warp 0 is full");
     const int t = threadIdx.x, w = t >> 5;
-    const int cnt = NT - 32 * w < 32 ? NT - 32 * w : 32;
-    const unsigned mask = cnt == 32 ? 0xffffffffu : (1u << cnt) - 1u;
+    int cnt;
+    const unsigned mask = warp_lanes_mask(NT, w, cnt);
     unsigned mm[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v) mm[v] = __reduce_max_sync(mask, m[v]);
-    const unsigned c = __reduce_min_sync(mask, __float_as_uint(cv));
-    const unsigned ww = __reduce_min_sync(mask, __float_as_uint(vs));
     const unsigned b = __reduce_or_sync(mask, bad ? 1u : 0u);
     if ((t & 31) == 0) {
         MonitorPart p;
 #pragma unroll
         for (int v = 0; v < 5; ++v) p.m[v] = abs_bits_as_double(mm[v], static_cast<const float*>(nullptr));
-        p.c = __uint_as_float(c);
-        p.w = __uint_as_float(ww);
         p.b = static_cast<int>(b);
         sp.w[w] = p;
     }
 }
 
-// Second half (after the barrier, warp 0): the warp partials folded, the record written by thread 0.
+// Second half (after the barrier, warp 0): the warp partials folded, words 0..5 written by thread 0.
 template <int NT>
 __device__ __forceinline__ void monitor_finish(const MonitorScratch<NT>& sp, unsigned long long* out) {
     constexpr int NW = MonitorScratch<NT>::NW;
@@ -1118,8 +1138,6 @@ __device__ __forceinline__ void monitor_finish(const MonitorScratch<NT>& sp, uns
     } else {
 #pragma unroll
         for (int v = 0; v < 5; ++v) p.m[v] = 0;
-        p.c = 3.0e38f;
-        p.w = 3.0e38f;
         p.b = 0;
     }
     monitor_warp(p, 0xffffffffu, NW);
@@ -1127,18 +1145,7 @@ __device__ __forceinline__ void monitor_finish(const MonitorScratch<NT>& sp, uns
 #pragma unroll
         for (int v = 0; v < 5; ++v) out[v] = p.m[v];
         out[5] = p.b ? 1ull : 0ull;
-        out[6] = __float_as_uint(p.c);
-        out[7] = __float_as_uint(p.w);
     }
-}
-
-template <int NT>
-__device__ __forceinline__ void monitor_element(const unsigned long long m[5], int bad, float cv, float vs,
-                                                unsigned long long* out) {
-    __shared__ MonitorScratch<NT> sp;
-    monitor_partial<NT>(m, bad, cv, vs, sp);
-    __syncthreads();
-    monitor_finish<NT>(sp, out);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -1147,8 +1154,8 @@ __device__ __forceinline__ void monitor_element(const unsigned long long m[5], i
 // mbarrier while the threads fetch their surface fluxes; the updated Q and G leave as bulk stores.
 // A copy that does not complete within the bounded wait sets *a.err and the CTA returns.
 // ------------------------------------------------------------------------------------------------
-// FUSE (the last stage of a monitored time-loop step): the element's residual/NaN record and the
-// FP32 MaxTimeStep estimate of the new state go to a.mon (monitor_element).
+// FUSE (the last stage of a monitored time-loop step): the element's residual/NaN record goes to
+// a.mon[8e .. 8e + 5].
 template <int P, bool GL, bool SRC, typename R, bool FUSE = false>
 __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
     k_update_tma(Args<R> a, int stage, double tshift, int write_qdot) {
@@ -1162,14 +1169,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
     __shared__ __align__(128) R sJ[P3];
     __shared__ __align__(16) R sQ4[4 * P3];
     __shared__ R sQ1[P3];
-    // FUSE: the element's metric blocks (Ja^xi, Ja^eta, Ja^zeta) for the time-step estimate (staged
-    // in the FP32 form; the FP64 form has no static shared memory left for them and reads them from
-    // global memory), and the warp partials of its monitor record
-    constexpr bool STAGE_JA = FUSE && sizeof(R) == 4;
-    constexpr uint32_t BA = 3 * P3 * sizeof(R);
-    static_assert(BA % 16 == 0, "bulk copies move multiples of 16 bytes");
-    __shared__ __align__(128) R sJa[STAGE_JA ? 9 * P3 : 4];
-    __shared__ MonitorScratch<FUSE ? P3 : 32> smon;
+    __shared__ MonitorScratch<FUSE ? P3 : 32> smon;  // FUSE: the warp partials of the monitor record
     __shared__ __align__(8) uint64_t bar;
     const int n = threadIdx.x;
     const int e = blockIdx.x;
@@ -1181,18 +1181,13 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
     }
     __syncthreads();
     if (n == 0) {
-        mbar_arrive_expect_tx(&bar, (stage >= 0 ? 2 * BQ : 0) + BD + BJ + (STAGE_JA ? 3 * BA : 0) + a.extra_tx);
+        mbar_arrive_expect_tx(&bar, (stage >= 0 ? 2 * BQ : 0) + BD + BJ + a.extra_tx);
         if (stage >= 0) {
             bulk_load(sQd, a.Q + 5 * g0, BQ, &bar);
             bulk_load(sGd, a.G + 5 * g0, BQ, &bar);
         }
         bulk_load(sDot, a.QDot + 5 * g0, BD, &bar);
         bulk_load(sJ, a.jac + g0, BJ, &bar);
-        if constexpr (STAGE_JA) {
-            bulk_load(sJa, a.ja_xi + 3 * g0, BA, &bar);
-            bulk_load(sJa + 3 * P3, a.ja_eta + 3 * g0, BA, &bar);
-            bulk_load(sJa + 6 * P3, a.ja_zeta + 3 * g0, BA, &bar);
-        }
     }
     R fs[6][5];
     bool use[6];
@@ -1236,21 +1231,16 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
         int bad = 0;
 #pragma unroll
         for (int v = 0; v < 5; ++v) bad |= nonfinite(qq[v]);
-        float cv, vs;
-        if constexpr (STAGE_JA)
-            dt_estimate(a.dtc, qq, sJa + 3 * n, sJa + 3 * P3 + 3 * n, sJa + 6 * P3 + 3 * n, sJ[n], cv, vs);
-        else
-            dt_estimate(a.dtc, qq, a.ja_xi + 3 * g, a.ja_eta + 3 * g, a.ja_zeta + 3 * g, sJ[n], cv, vs);
         if constexpr (sizeof(R) == 4) {
             unsigned m[5];
 #pragma unroll
             for (int v = 0; v < 5; ++v) m[v] = static_cast<unsigned>(abs_bits(qd[v]));
-            monitor_partial32<P3>(m, bad, cv, vs, smon);
+            monitor_partial32<P3>(m, bad, smon);
         } else {
             unsigned long long m[5];
 #pragma unroll
             for (int v = 0; v < 5; ++v) m[v] = abs_bits(qd[v]);
-            monitor_partial<P3>(m, bad, cv, vs, smon);
+            monitor_partial<P3>(m, bad, smon);
         }
     }
     fence_proxy_async_smem();  // this thread's Q, G writes before the bulk stores read them

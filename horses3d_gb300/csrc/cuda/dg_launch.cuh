@@ -19,8 +19,11 @@ constexpr int kWriteQDot = 2;
 // face flux and update kernels (after they received the neighbours' viscous normal fluxes).
 constexpr int kVolumeOnly = 4;
 constexpr int kSurfaceOnly = 8;
-// The monitored device time loop: the update of this stage writes the monitor records (a.mon).
+// The monitored device time loop: kFuseMonitor, the update of this stage writes the elements'
+// residual records (a.mon words 0..5); kEstimateDt, the volume kernel of this stage writes the
+// elements' time-step estimates (words 6, 7).
 constexpr int kFuseMonitor = 16;
+constexpr int kEstimateDt = 32;
 
 template <typename R>
 using StageFn = cudaError_t (*)(const Args<R>& a, int stage, double tshift, int flags, cudaStream_t s);
@@ -40,8 +43,20 @@ size_t volume_tc_smem_bytes() {
     return volume_tc_offset<P, R>() + TcLayout::BYTES;
 }
 
+// The monitored time loop's estimate variant of the volume kernel exists for the orders whose
+// update stages element blocks by TMA (one element per CTA), as the fused residual records do.
+template <int P>
+constexpr bool kEstVolume = (P == 6);
+
 template <int P, bool GL, typename R>
-void launch_volume(const Args<R>& a, int blocks, int store_grad, cudaStream_t s) {
+void launch_volume(const Args<R>& a, int blocks, int store_grad, cudaStream_t s, bool est = false) {
+    if constexpr (kEstVolume<P>) {
+        if (est) {
+            k_volume<P, GL, R, false, true><<<blocks, Geo<P>::THREADS, volume_smem_bytes<P, R>(a.inviscid), s>>>(
+                a, store_grad);
+            return;
+        }
+    }
     if constexpr (kTcVolume<P, GL, R>) {
         if (a.tc) {
             k_volume<P, GL, R, true><<<blocks, Geo<P>::THREADS, volume_tc_smem_bytes<P, R>(), s>>>(a, store_grad);
@@ -88,6 +103,12 @@ cudaError_t run_stage(const Args<R>& a, int stage, double tshift, int flags, cud
                                                        static_cast<int>(volume_tc_smem_bytes<P, R>()));
             if (e != cudaSuccess) return e;
         }
+        if constexpr (kEstVolume<P>) {
+            const cudaError_t e = cudaFuncSetAttribute(k_volume<P, GL, R, false, true>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       static_cast<int>(volume_smem_bytes<P, R>(1)));
+            if (e != cudaSuccess) return e;
+        }
         return cudaFuncSetAttribute(k_volume<P, GL, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     static_cast<int>(volume_smem_bytes<P, R>(1)));
     }
@@ -95,7 +116,7 @@ cudaError_t run_stage(const Args<R>& a, int stage, double tshift, int flags, cud
         k_traces<P, GL, R><<<eblocks, THREADS, 0, s>>>(a);
         return cudaGetLastError();
     }
-    if (!(flags & kSurfaceOnly)) launch_volume<P, GL, R>(a, eblocks, flags & kStoreGrad, s);
+    if (!(flags & kSurfaceOnly)) launch_volume<P, GL, R>(a, eblocks, flags & kStoreGrad, s, (flags & kEstimateDt) != 0);
     if (flags & kVolumeOnly) return cudaGetLastError();
     launch_flux<P, R>(a, fblocks, s);
     const bool fuse = (flags & kFuseMonitor) != 0;
@@ -145,42 +166,28 @@ cudaError_t kernel_times(const Args<R>& a, int reps, cudaStream_t s, double* ms)
 }
 
 // ------------------------------------------------------------------ fused time-loop monitor ----
-// The monitored device time loop (dg_integrate) of the kTmaUpdate orders reads the residuals, the
-// NaN test and the first MaxTimeStep pass from the records the last stage's update writes per
-// element (k_update_tma<..., true>), so the loop needs no separate pass over Q and QDot:
-//   before the loop  k_monitor_estimate  records of the uploaded state, k_monitor_fold -> red[7]
-//   every step       k_dt_exact_elem (elements whose estimate lies in the window) + k_dt_final,
-//                    the three stages (the last one writes the records), k_advance_time,
-//                    k_monitor_fold (residuals red[2..6], NaN flag, estimate minimum red[7] for the
-//                    next step) and the history row
+// The monitored device time loop (dg_integrate) of the orders with the one-element-per-CTA volume and
+// update kernels needs no separate pass over Q, QDot and the geometry for its monitor: per element
+// a record of 8 words (a.mon) is filled by the kernels that hold the data anyway.
+//   stage 1   k_volume<EST>: FP32 MaxTimeStep estimates of the step's initial state (words 6, 7);
+//             k_estimate_fold -> red[7]; k_dt_exact_elem (elements whose estimate lies in the
+//             window) + k_dt_final -> dt; then the stage's flux and update kernels
+//   stage 3   k_update_tma<FUSE>: max |QDot| per variable and the NaN/Inf flag of the new state
+//             (words 0..5); after the step k_monitor_fold -> red[2..6], the NaN flag, the history row
 // The dt equals the two-pass reduction's bit for bit (the same window argument, per element instead
 // of per chunk), and the residuals equal k_residuals' (maxima of the same values).
 constexpr int kFoldBlocks = 152;
 
-template <int P, typename R>
-__global__ void __launch_bounds__(Geo<P>::THREADS) k_monitor_estimate(Args<R> a) {
-    const int e = blockIdx.x, n = threadIdx.x;
-    const int64_t g = static_cast<int64_t>(e) * Geo<P>::P3 + n;
-    float cv, vs;
-    dt_estimate(a.dtc, a.Q + 5 * g, a.ja_xi + 3 * g, a.ja_eta + 3 * g, a.ja_zeta + 3 * g, a.jac[g], cv, vs);
-    const unsigned long long m[5] = {0, 0, 0, 0, 0};
-    monitor_element<Geo<P>::P3>(m, 0, cv, vs, a.mon + 8 * static_cast<int64_t>(e));
-}
-
-// Folds the element records into red[2..6] (max |QDot|), *nan_flag and the FP32 estimate minima of
-// red[7].
+// Folds the element records' residual words into red[2..6] (max |QDot|) and *nan_flag.
 __global__ static void __launch_bounds__(256) k_monitor_fold(const unsigned long long* __restrict__ mon, int K,
                                                              unsigned long long* red, int* nan_flag) {
     unsigned long long m[5] = {0, 0, 0, 0, 0};
-    float c = 3.0e38f, w = 3.0e38f;
     int b = 0;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < K; e += gridDim.x * blockDim.x) {
         const unsigned long long* r = mon + 8 * static_cast<int64_t>(e);
 #pragma unroll
         for (int v = 0; v < 5; ++v) m[v] = r[v] > m[v] ? r[v] : m[v];
         b |= r[5] != 0;
-        c = fminf(c, __uint_as_float(static_cast<unsigned>(r[6])));
-        w = fminf(w, __uint_as_float(static_cast<unsigned>(r[7])));
     }
     for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
@@ -188,21 +195,34 @@ __global__ static void __launch_bounds__(256) k_monitor_fold(const unsigned long
             const unsigned long long x = __shfl_down_sync(0xffffffffu, m[v], o);
             m[v] = x > m[v] ? x : m[v];
         }
-        c = fminf(c, __shfl_down_sync(0xffffffffu, c, o));
-        w = fminf(w, __shfl_down_sync(0xffffffffu, w, o));
         b |= __shfl_down_sync(0xffffffffu, b, o);
     }
     if ((threadIdx.x & 31) == 0) {
 #pragma unroll
         for (int v = 0; v < 5; ++v) atomicMax(&red[2 + v], m[v]);
         if (b) atomicOr(nan_flag, 1);
-        unsigned int* s32 = reinterpret_cast<unsigned int*>(red + 7);
-        atomicMin(&s32[0], fbits(c));
-        atomicMin(&s32[1], fbits(w));
     }
 }
 
-static __global__ void k_reset_estimate(unsigned long long* red) { red[7] = kDtEstimateInit; }
+// Folds the element records' estimate words into the FP32 minima of red[7] (which holds two FP32
+// +inf on entry: k_dt_final leaves it so).
+__global__ static void __launch_bounds__(256) k_estimate_fold(const unsigned long long* __restrict__ mon, int K,
+                                                              unsigned long long* red) {
+    unsigned c = 0xffffffffu, w = 0xffffffffu;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < K; e += gridDim.x * blockDim.x) {
+        const unsigned long long* r = mon + 8 * static_cast<int64_t>(e);
+        const unsigned rc = static_cast<unsigned>(r[6]), rw = static_cast<unsigned>(r[7]);
+        c = rc < c ? rc : c;
+        w = rw < w ? rw : w;
+    }
+    c = __reduce_min_sync(0xffffffffu, c);
+    w = __reduce_min_sync(0xffffffffu, w);
+    if ((threadIdx.x & 31) == 0) {
+        unsigned int* s32 = reinterpret_cast<unsigned int*>(red + 7);
+        atomicMin(&s32[0], c);
+        atomicMin(&s32[1], w);
+    }
+}
 
 // The exact pass: a grid of kExactBlocks CTAs strides over the elements; an element none of whose
 // nodes can be in the window is skipped (a block-uniform test on its record).
@@ -250,22 +270,16 @@ __global__ void __launch_bounds__(Geo<P>::THREADS) k_dt_exact_elem(Args<R> a, Dt
     }
 }
 
+// MaxTimeStep from the estimate records of the current state: the estimate minima into red[7], the
+// exact pass into red[0], red[1] (k_dt_final follows).
 template <typename R>
 struct MonitorFns {
-    cudaError_t (*begin)(const Args<R>& a, unsigned long long* red, int* nan_flag, cudaStream_t s);
-    cudaError_t (*exact)(const Args<R>& a, const DtArgs& d, cudaStream_t s);
+    cudaError_t (*dt)(const Args<R>& a, const DtArgs& d, cudaStream_t s);
 };
 
 template <int P, bool GL, typename R>
-cudaError_t monitor_begin(const Args<R>& a, unsigned long long* red, int* nan_flag, cudaStream_t s) {
-    k_reset_estimate<<<1, 1, 0, s>>>(red);
-    k_monitor_estimate<P, R><<<a.K, Geo<P>::THREADS, 0, s>>>(a);
-    k_monitor_fold<<<kFoldBlocks, 256, 0, s>>>(a.mon, a.K, red, nan_flag);
-    return cudaGetLastError();
-}
-
-template <int P, bool GL, typename R>
-cudaError_t monitor_exact(const Args<R>& a, const DtArgs& d, cudaStream_t s) {
+cudaError_t monitor_dt(const Args<R>& a, const DtArgs& d, cudaStream_t s) {
+    k_estimate_fold<<<kFoldBlocks, 256, 0, s>>>(a.mon, a.K, d.red);
     k_dt_exact_elem<P, R><<<a.K < kExactBlocks ? a.K : kExactBlocks, Geo<P>::THREADS, 0, s>>>(a, d);
     return cudaGetLastError();
 }
