@@ -1106,23 +1106,43 @@ __device__ __forceinline__ void monitor_partial(const unsigned long long m[5], i
     if ((t & 31) == 0) sp.w[w] = p;
 }
 
-// First half, FP32 patterns (31 bits): single-instruction warp reductions.
+// The FP32 form keeps 32-bit patterns (|QDot| as 31-bit FP32 images, the flag) through both halves
+// and reduces them with single-instruction warp reductions; thread 0 widens the maxima to the FP64
+// images at the end.
 template <int NT>
-__device__ __forceinline__ void monitor_partial32(const unsigned m[5], int bad, MonitorScratch<NT>& sp) {
+struct MonitorScratch32 {
+    static constexpr int NW = (NT + 31) / 32;
+    unsigned w[6][NW];
+};
+
+template <int NT>
+__device__ __forceinline__ void monitor_partial32(const unsigned m[5], int bad, MonitorScratch32<NT>& sp) {
     static_assert(NT >= 32, "warp 0 is full");
     const int t = threadIdx.x, w = t >> 5;
     int cnt;
     const unsigned mask = warp_lanes_mask(NT, w, cnt);
-    unsigned mm[5];
+    unsigned mm[6];
 #pragma unroll
     for (int v = 0; v < 5; ++v) mm[v] = __reduce_max_sync(mask, m[v]);
-    const unsigned b = __reduce_or_sync(mask, bad ? 1u : 0u);
+    mm[5] = __reduce_or_sync(mask, bad ? 1u : 0u);
     if ((t & 31) == 0) {
-        MonitorPart p;
 #pragma unroll
-        for (int v = 0; v < 5; ++v) p.m[v] = abs_bits_as_double(mm[v], static_cast<const float*>(nullptr));
-        p.b = static_cast<int>(b);
-        sp.w[w] = p;
+        for (int v = 0; v < 6; ++v) sp.w[v][w] = mm[v];
+    }
+}
+
+template <int NT>
+__device__ __forceinline__ void monitor_finish32(const MonitorScratch32<NT>& sp, unsigned long long* out) {
+    constexpr int NW = MonitorScratch32<NT>::NW;
+    const int t = threadIdx.x;
+    if (t >= 32) return;
+    unsigned mm[6];
+#pragma unroll
+    for (int v = 0; v < 6; ++v) mm[v] = __reduce_max_sync(0xffffffffu, t < NW ? sp.w[v][t] : 0u);
+    if (t == 0) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) out[v] = abs_bits_as_double(mm[v], static_cast<const float*>(nullptr));
+        out[5] = mm[5] ? 1ull : 0ull;
     }
 }
 
@@ -1169,7 +1189,9 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
     __shared__ __align__(128) R sJ[P3];
     __shared__ __align__(16) R sQ4[4 * P3];
     __shared__ R sQ1[P3];
-    __shared__ MonitorScratch<FUSE ? P3 : 32> smon;  // FUSE: the warp partials of the monitor record
+    // FUSE: the warp partials of the monitor record
+    __shared__ MonitorScratch<(FUSE && sizeof(R) == 8) ? P3 : 32> smon;
+    __shared__ MonitorScratch32<(FUSE && sizeof(R) == 4) ? P3 : 32> smon32;
     __shared__ __align__(8) uint64_t bar;
     const int n = threadIdx.x;
     const int e = blockIdx.x;
@@ -1228,14 +1250,19 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
     if constexpr (FUSE) {
         // ComputeMaxResiduals (max |QDot| of this stage) and checkForNan (the new Q) of the element,
         // and the FP32 time-step estimates of the new state (the first pass of MaxTimeStep)
-        int bad = 0;
+        // NaN/Inf: all exponent bits set, tested on the high words
+        unsigned hx = 0;
 #pragma unroll
-        for (int v = 0; v < 5; ++v) bad |= nonfinite(qq[v]);
+        for (int v = 0; v < 5; ++v) {
+            const unsigned h = static_cast<unsigned>(__double2hiint(qq[v])) & 0x7ff00000u;
+            hx |= h == 0x7ff00000u ? 1u : 0u;
+        }
+        const int bad = static_cast<int>(hx);
         if constexpr (sizeof(R) == 4) {
             unsigned m[5];
 #pragma unroll
             for (int v = 0; v < 5; ++v) m[v] = static_cast<unsigned>(abs_bits(qd[v]));
-            monitor_partial32<P3>(m, bad, smon);
+            monitor_partial32<P3>(m, bad, smon32);
         } else {
             unsigned long long m[5];
 #pragma unroll
@@ -1250,7 +1277,10 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::update))
         bulk_store(a.G + 5 * g0, sGd, BQ);
         bulk_commit();
     }
-    if constexpr (FUSE) monitor_finish<P3>(smon, a.mon + 8 * static_cast<int64_t>(e));
+    if constexpr (FUSE) {
+        if constexpr (sizeof(R) == 4) monitor_finish32<P3>(smon32, a.mon + 8 * static_cast<int64_t>(e));
+        else monitor_finish<P3>(smon, a.mon + 8 * static_cast<int64_t>(e));
+    }
     for (int t = n; t < 6 * P2; t += P3) {  // Q traces of the updated state
         const int side = 1 + t / P2, p = t - (side - 1) * P2;
         R tq[1][5];
