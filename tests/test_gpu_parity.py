@@ -348,11 +348,14 @@ def test_gradient_variables(gv, nodes):
 
 
 @pytest.mark.parametrize("precision", [_abi.DG_PRECISION_FP64, _abi.DG_PRECISION_MIXED])
-def test_integrate_on_device_equals_the_step_loop(precision):
+@pytest.mark.parametrize("order,nodes", [(3, _abi.DG_NODES_GAUSS), (5, _abi.DG_NODES_GAUSS),
+                                         (5, _abi.DG_NODES_GAUSS_LOBATTO)])
+def test_integrate_on_device_equals_the_step_loop(precision, order, nodes):
     """dg_integrate (IntegrateInTime on the device, one graph per step with the residual monitor)
     gives the state, time and per-step residuals of the host loop MaxTimeStep + TakeRK3Step +
-    ComputeMaxResiduals bit for bit."""
-    mesh, cfg, q0 = cases.tgv_case(n=3, order=3, nodes=_abi.DG_NODES_GAUSS, perturbation=0.02, seed=12,
+    ComputeMaxResiduals bit for bit. N = 5 runs the fused monitor (the estimate in the first stage's
+    volume kernel, the residual records in the last stage's update)."""
+    mesh, cfg, q0 = cases.tgv_case(n=3, order=order, nodes=nodes, perturbation=0.02, seed=12,
                                    precision=precision)
     g1 = NavierStokesDG(mesh, cfg)
     g1.set_state(q0)
@@ -379,6 +382,20 @@ def test_integrate_on_device_reports_the_first_nan_step():
     g = NavierStokesDG(mesh, cfg)
     q = q0.copy()
     q[7] = np.nan
+    g.set_state(q)
+    with pytest.raises(FloatingPointError, match="after step 1"):
+        g.integrate_on_device(3, 0.0, dt=1e-3)
+
+
+@pytest.mark.parametrize("precision", [_abi.DG_PRECISION_FP64, _abi.DG_PRECISION_MIXED])
+def test_fused_monitor_reports_the_first_nan_step(precision):
+    """N = 5 (the fused residual records): a negative density at one node makes the first step's
+    pressures and wave speeds NaN; the device loop reports step 1 (the mixed form refuses a NaN
+    upload, so the state itself is finite)."""
+    mesh, cfg, q0 = cases.tgv_case(n=2, order=5, nodes=_abi.DG_NODES_GAUSS, precision=precision)
+    g = NavierStokesDG(mesh, cfg)
+    q = q0.copy()
+    q[5 * 7] = -1.0
     g.set_state(q)
     with pytest.raises(FloatingPointError, match="after step 1"):
         g.integrate_on_device(3, 0.0, dt=1e-3)
