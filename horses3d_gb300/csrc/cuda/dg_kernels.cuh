@@ -206,6 +206,34 @@ __device__ __forceinline__ void st5<double>(double* v4, int i4, double* v1, int 
     v1[i1] = x[4];
 }
 
+// A 3-vector padded to four values at v[4*i] (one 128-bit access for float, two for double).
+template <typename R>
+__device__ __forceinline__ void st4(R* v, int i, R x0, R x1, R x2) {
+    if constexpr (sizeof(R) == 4) {
+        *reinterpret_cast<float4*>(v + 4 * i) = make_float4(x0, x1, x2, 0.f);
+    } else {
+        *reinterpret_cast<double2*>(v + 4 * i) = make_double2(x0, x1);
+        *reinterpret_cast<double2*>(v + 4 * i + 2) = make_double2(x2, 0.0);
+    }
+}
+template <typename R>
+__device__ __forceinline__ void ld4(const R* v, int i, R* o) {
+    if constexpr (sizeof(R) == 4) {
+        const float4 t = *reinterpret_cast<const float4*>(v + 4 * i);
+        o[0] = t.x;
+        o[1] = t.y;
+        o[2] = t.z;
+        o[3] = t.w;
+    } else {
+        const double2 x = *reinterpret_cast<const double2*>(v + 4 * i);
+        const double2 y = *reinterpret_cast<const double2*>(v + 4 * i + 2);
+        o[0] = x.x;
+        o[1] = x.y;
+        o[2] = y.x;
+        o[3] = y.y;
+    }
+}
+
 // Slot arrays in global memory use the same split: the 16-byte parts of all slot points first, then
 // the fifth values; the threads of a face read consecutive 16-byte parts (coalesced 128-bit loads).
 template <typename R>
@@ -221,7 +249,8 @@ __device__ __forceinline__ void gst5(R* base, int64_t nsp, int64_t idx, const R*
 //   Q4/Q1  state, 5-vector per node
 //   G4/G1  lifted gradient, 3 directions per node (later the contravariant or viscous fluxes)
 //   M      metric vectors per node (split form only; empty otherwise)
-//   U4/U1  BR1 jumps uStar n per face point of the six sides, 3 directions
+//   U4/U1  BR1 jumps uStar per face point of the six sides (5-vectors)
+//   NN     the face points' unit normals (4 values each, the fourth unused)
 //   T4/T1  own Q traces per face point of the six sides
 //   F4/F1  split form: the two-point fluxes of one direction, D = P/2 pairs per node, staged over
 //          U, T and beyond once the gradient phases are done
@@ -234,8 +263,9 @@ struct VolLayout {
     static constexpr int G4 = Q1 + up(P3), G1 = G4 + up(12 * P3);
     static constexpr int M = G1 + up(3 * P3);
     __host__ __device__ static constexpr int U4(bool split) { return M + (split ? up(9 * P3) : 0); }
-    __host__ __device__ static constexpr int U1(bool split) { return U4(split) + up(72 * P2); }
-    __host__ __device__ static constexpr int T4(bool split) { return U1(split) + up(18 * P2); }
+    __host__ __device__ static constexpr int U1(bool split) { return U4(split) + up(24 * P2); }
+    __host__ __device__ static constexpr int NN(bool split) { return U1(split) + up(6 * P2); }
+    __host__ __device__ static constexpr int T4(bool split) { return NN(split) + up(24 * P2); }
     __host__ __device__ static constexpr int T1(bool split) { return T4(split) + up(24 * P2); }
     __host__ __device__ static constexpr int end_faces(bool split) { return T1(split) + up(6 * P2); }
     static constexpr int F4 = M + up(9 * P3), F1 = F4 + up(4 * P3 * D), F_END = F1 + up(P3 * D);
@@ -363,6 +393,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
     R* G1 = base + L::G1;
     R* U4 = base + L::U4(split);
     R* U1 = base + L::U1(split);
+    R* NN = base + L::NN(split);
     R* T4 = base + L::T4(split);
     R* T1 = base + L::T1(split);
     R* sM = base + L::M;
@@ -619,13 +650,9 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
 #pragma unroll
                     for (int v = 0; v < 5; ++v) u[v] = R(0.5) * (left ? (un[v] - uo[v]) : (uo[v] - un[v])) * J;
                 }
-#pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    R x[5];
-#pragma unroll
-                    for (int v = 0; v < 5; ++v) x[v] = u[v] * nn[d];
-                    st5(U4, t * 3 + d, U1, d * F6 + t, x);
-                }
+                // the jump and the normal; the lifting forms uStar n_d per direction from them
+                st5(U4, t, U1, t, u);
+                st4(NN, t, nn[0], nn[1], nn[2]);
             }
         }
         __syncthreads();
@@ -649,22 +676,29 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
                 for (int sd = 0; sd < 6; ++sd) use[sd] = true;
             }
             if (!GL || use[0] || use[1] || use[2] || use[3] || use[4] || use[5]) {
+                // per side one jump and one normal from shared memory, the three directions'
+                // products uStar n_d in registers (each rounded as a stored product would be)
+                R fi[3][5];
+                bool first = true;
 #pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    R fi[5] = {0, 0, 0, 0, 0};
-                    bool first = true;
+                for (int sd = 0; sd < 6; ++sd) {
+                    if (!use[sd]) continue;
+                    R u[5], nv[4];
+                    ld5(U4, pt[sd], U1, pt[sd], u);
+                    ld4(NN, pt[sd], nv);
 #pragma unroll
-                    for (int sd = 0; sd < 6; ++sd) {
-                        if (!use[sd]) continue;
-                        R h[5];
-                        ld5(U4, pt[sd] * 3 + d, U1, d * F6 + pt[sd], h);
+                    for (int d = 0; d < 3; ++d)
 #pragma unroll
-                        for (int v = 0; v < 5; ++v) fi[v] = first ? h[v] * bw[sd] : fi[v] + h[v] * bw[sd];
-                        first = false;
-                    }
-#pragma unroll
-                    for (int v = 0; v < 5; ++v) U[d][v] = U[d][v] + fi[v] * ij;
+                        for (int v = 0; v < 5; ++v) {
+                            const R h = u[v] * nv[d];
+                            fi[d][v] = first ? h * bw[sd] : fi[d][v] + h * bw[sd];
+                        }
+                    first = false;
                 }
+#pragma unroll
+                for (int d = 0; d < 3; ++d)
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) U[d][v] = U[d][v] + fi[d][v] * ij;
             }
 #pragma unroll
             for (int d = 0; d < 3; ++d) st5(G4, n * 3 + d, G1, d * P3 + n, U[d]);
