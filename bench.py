@@ -567,6 +567,8 @@ def main():
         dt = g.max_time_step(CFL, CFL)
         t = g.run_steps(args.warmup, 0.0, dt=dt)
         t = g.run_steps(args.steps, t, dt=dt)
+        # then the monitored device loop (CFL dt, residuals, NaN check) for as many steps
+        t, _ = g.integrate_on_device(args.steps, t, cfl=CFL, dcfl=CFL)
         print(json.dumps({"profile": args.profile, "elements": args.elements, "ndof": mesh.ndof, "t_end": t}))
         return
     r = run_gpu_arm(args, rank, world, local, case)

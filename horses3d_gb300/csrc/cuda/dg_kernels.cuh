@@ -249,8 +249,10 @@ __device__ __forceinline__ void gst5(R* base, int64_t nsp, int64_t idx, const R*
 //   Q4/Q1  state, 5-vector per node
 //   G4/G1  lifted gradient, 3 directions per node (later the contravariant or viscous fluxes)
 //   M      metric vectors per node (split form only; empty otherwise)
-//   U4/U1  BR1 jumps uStar per face point of the six sides (5-vectors)
-//   NN     the face points' unit normals (4 values each, the fourth unused)
+//   U4/U1  BR1 jumps per face point of the six sides: FP32, uStar (5-vectors) with the unit normals
+//          in NN (4 values each, the fourth unused), the lifting forming uStar n_d in registers;
+//          FP64, uStar n_d for the 3 directions (the FP64 pipe binds that form: the products are
+//          formed once per face point, not once per node and side)
 //   T4/T1  own Q traces per face point of the six sides
 //   F4/F1  split form: the two-point fluxes of one direction, D = P/2 pairs per node, staged over
 //          U, T and beyond once the gradient phases are done
@@ -263,9 +265,10 @@ struct VolLayout {
     static constexpr int G4 = Q1 + up(P3), G1 = G4 + up(12 * P3);
     static constexpr int M = G1 + up(3 * P3);
     __host__ __device__ static constexpr int U4(bool split) { return M + (split ? up(9 * P3) : 0); }
-    __host__ __device__ static constexpr int U1(bool split) { return U4(split) + up(24 * P2); }
-    __host__ __device__ static constexpr int NN(bool split) { return U1(split) + up(6 * P2); }
-    __host__ __device__ static constexpr int T4(bool split) { return NN(split) + up(24 * P2); }
+    static constexpr bool JN = sizeof(R) == 4;  // jumps and normals apart
+    __host__ __device__ static constexpr int U1(bool split) { return U4(split) + up((JN ? 24 : 72) * P2); }
+    __host__ __device__ static constexpr int NN(bool split) { return U1(split) + up((JN ? 6 : 18) * P2); }
+    __host__ __device__ static constexpr int T4(bool split) { return NN(split) + (JN ? up(24 * P2) : 0); }
     __host__ __device__ static constexpr int T1(bool split) { return T4(split) + up(24 * P2); }
     __host__ __device__ static constexpr int end_faces(bool split) { return T1(split) + up(6 * P2); }
     static constexpr int F4 = M + up(9 * P3), F1 = F4 + up(4 * P3 * D), F_END = F1 + up(P3 * D);
@@ -650,9 +653,18 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
 #pragma unroll
                     for (int v = 0; v < 5; ++v) u[v] = R(0.5) * (left ? (un[v] - uo[v]) : (uo[v] - un[v])) * J;
                 }
-                // the jump and the normal; the lifting forms uStar n_d per direction from them
-                st5(U4, t, U1, t, u);
-                st4(NN, t, nn[0], nn[1], nn[2]);
+                if constexpr (L::JN) {  // the jump and the normal; the lifting forms uStar n_d
+                    st5(U4, t, U1, t, u);
+                    st4(NN, t, nn[0], nn[1], nn[2]);
+                } else {
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        R x[5];
+#pragma unroll
+                        for (int v = 0; v < 5; ++v) x[v] = u[v] * nn[d];
+                        st5(U4, t * 3 + d, U1, d * F6 + t, x);
+                    }
+                }
             }
         }
         __syncthreads();
@@ -675,7 +687,26 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
 #pragma unroll
                 for (int sd = 0; sd < 6; ++sd) use[sd] = true;
             }
-            if (!GL || use[0] || use[1] || use[2] || use[3] || use[4] || use[5]) {
+            if constexpr (!L::JN) {
+                if (!GL || use[0] || use[1] || use[2] || use[3] || use[4] || use[5]) {
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        R fi[5] = {0, 0, 0, 0, 0};
+                        bool first = true;
+#pragma unroll
+                        for (int sd = 0; sd < 6; ++sd) {
+                            if (!use[sd]) continue;
+                            R h[5];
+                            ld5(U4, pt[sd] * 3 + d, U1, d * F6 + pt[sd], h);
+#pragma unroll
+                            for (int v = 0; v < 5; ++v) fi[v] = first ? h[v] * bw[sd] : fi[v] + h[v] * bw[sd];
+                            first = false;
+                        }
+#pragma unroll
+                        for (int v = 0; v < 5; ++v) U[d][v] = U[d][v] + fi[v] * ij;
+                    }
+                }
+            } else if (!GL || use[0] || use[1] || use[2] || use[3] || use[4] || use[5]) {
                 // per side one jump and one normal from shared memory, the three directions'
                 // products uStar n_d in registers (each rounded as a stored product would be)
                 R fi[3][5];
