@@ -141,7 +141,7 @@ def build_case(n_elem: int = N_ELEM):
 VOLUME_DRAM_BYTES_PER_DOF = 149.0
 # The unit that binds k_volume<6, gauss, float> in the same ncu capture: the L1/shared-memory pipe
 # (l1tex__throughput.avg.pct_of_peak_sustained_elapsed), ahead of DRAM.
-VOLUME_L1TEX_FRAC = 0.80
+VOLUME_L1TEX_FRAC = 0.73
 # Executed FP64 floating-point operations per DOF and RK stage of the plain form: ncu SASS counts
 # dadd + dmul + 2 dfma of k_volume (1562.0), k_flux (95.5) and k_update_tma (217.0) per DOF, on the
 # 8^3-element N=5 case (the same kernels and per-DOF work as the 32^3 workload).
