@@ -1294,8 +1294,11 @@ using VTimesFn = cudaError_t (*)(const VArgs<R>& a, int reps, cudaStream_t s, do
 // stage's stream wait for every side stream used. Inside a stream capture the side streams become
 // branches of the graph. Without lanes every launch goes to the stage's stream in order.
 constexpr int kLanes = 3;
-// The update kernel runs as one persistent launch over all item classes (kv_update_persistent).
-constexpr bool kPersistentUpdate = true;
+// The update as one persistent launch over all item classes (kv_update_persistent) instead of one
+// launch per class. Measured slower on both variable-order workloads (p-anisotropic 24^3: update
+// 0.193 -> 0.222 ms; 64 cases: 0.826 -> 0.831 ms): each item then waits for its work-counter atomic
+// before its loads start, which the hardware block scheduler does not. Off; kept for the record.
+constexpr bool kPersistentUpdate = false;
 struct Lanes {
     int n = 0;
     cudaStream_t side[kLanes] = {};
