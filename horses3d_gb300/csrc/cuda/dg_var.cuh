@@ -183,18 +183,6 @@ struct NodeDecoder {
     }
 };
 
-// Navier-Stokes volume kernel of the isotropic classes (compile-time P >= 3): the BR1 jumps of the
-// item's elements (15 values per slot point, six slots per element, 90/P per node) are copied into
-// shared memory once, so that the lifting's 90 reads per node are shared-memory loads instead of
-// dependent global ones.
-template <int PC>
-constexpr bool kStageJumps = PC >= 3;
-template <typename R>
-size_t vjump_smem(int cap, int pc, bool ns) {
-    if (!ns || pc < 3) return 0;
-    return static_cast<size_t>(90) * ((cap + pc - 1) / pc) * sizeof(R);
-}
-
 // Face point counts of a side (first, second face direction), sides numbered as the reference.
 __device__ __forceinline__ void side_dims(int side, int ord, int& d1, int& d2) {
     const int px = ord & 255, py = (ord >> 8) & 255, pz = (ord >> 16) & 255;
@@ -310,7 +298,6 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 0) kv_volume(VArgs<R
     R* sQ = reinterpret_cast<R*>(sO + 3);            // 5*ntot: state
     R* sG = sQ + 5 * ntot;                           // 15*ntot: lifted gradient, then the fluxes
     R* sM = sG + 15 * ntot;                          // split form: 9*ntot metric terms
-    R* sU = sM + (a.split ? 9 * ntot : 0);           // staged BR1 jumps (kStageJumps)
     load_ops(a.ops, sO, px, py, pz);
     const PhysR<R> ph = a.ph[d.kase];
     const double eref = a.cc[d.kase].e_ref;
@@ -334,17 +321,6 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 0) kv_volume(VArgs<R
         } else {
 #pragma unroll
             for (int v = 0; v < 5; ++v) sQ[v * ntot + t] = x[v];
-        }
-    }
-    // the jumps of an element's six slots are one contiguous block (its slots are consecutive, each
-    // slot's values variable-major), EL values long, the same for every element of the item
-    constexpr int EL = 90 * PC * PC;
-    if constexpr (kStageJumps<PC>) {
-        if (a.ns) {
-            for (int f = threadIdx.x; f < d.count * EL; f += blockDim.x) {
-                const int le = f / EL;
-                sU[f] = a.UJ[a.soff[6LL * a.item_elems[d.first + le]] * 15 + (f - le * EL)];
-            }
         }
     }
     __syncthreads();
@@ -391,15 +367,14 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 0) kv_volume(VArgs<R
                 U[1][v] = (uxi[v] * jx[1] + ueta[v] * je[1] + uzeta[v] * jz[1]) * ij;
                 U[2][v] = (uxi[v] * jx[2] + ueta[v] * je[2] + uzeta[v] * jz[2]) * ij;
             }
-            // lifting (VectorWeakIntegrals_StdFace order: left, right, front, back, bottom, top);
-            // the element's slots follow each other (sides 1..6 with A, A, B, C, B, C points)
-            const R* ub = kStageJumps<PC> ? sU + le * EL : a.UJ + a.soff[6LL * e] * 15;
-            const R* HF = ub + 0 * 15 + (i + px * k);
-            const R* HB = ub + A * 15 + (i + px * k);
-            const R* HO = ub + (2 * A) * 15 + (i + px * j);
-            const R* HR = ub + (2 * A + B) * 15 + (j + py * k);
-            const R* HT = ub + (2 * A + B + C) * 15 + (i + px * j);
-            const R* HL = ub + (2 * A + 2 * B + C) * 15 + (j + py * k);
+            // lifting (VectorWeakIntegrals_StdFace order: left, right, front, back, bottom, top)
+            const long long s0 = 6LL * e;
+            const R* HF = a.UJ + a.soff[s0 + 0] * 15 + (i + px * k);
+            const R* HB = a.UJ + a.soff[s0 + 1] * 15 + (i + px * k);
+            const R* HO = a.UJ + a.soff[s0 + 2] * 15 + (i + px * j);
+            const R* HR = a.UJ + a.soff[s0 + 3] * 15 + (j + py * k);
+            const R* HT = a.UJ + a.soff[s0 + 4] * 15 + (i + px * j);
+            const R* HL = a.UJ + a.soff[s0 + 5] * 15 + (j + py * k);
             const R bxl = sO[0].bL[i], bxr = sO[0].bR[i], byl = sO[1].bL[j], byr = sO[1].bR[j];
             const R bzl = sO[2].bL[k], bzr = sO[2].bR[k];
 #pragma unroll
@@ -1304,7 +1279,6 @@ size_t vitem_smem(int cap, int nv) {
     return 3 * sizeof(OpsP<R>) + static_cast<size_t>(nv) * cap * sizeof(R);
 }
 
-
 struct Lanes;
 template <typename R>
 using VStageFn = cudaError_t (*)(const VArgs<R>& a, int stage, double tshift, int flags, cudaStream_t s,
@@ -1477,9 +1451,7 @@ cudaError_t launch_items(const VArgs<R>& a0, int which, Fork& f, int store_grad 
         VArgs<R> a = a0;
         a.item0 = a0.cls[c];
         const int cap = a0.ccap[c];
-        const size_t smem = which >= 2 ? vupdate_smem<R>(cap)
-                            : vitem_smem<R>(cap, which == 1 ? (a0.split ? 29 : 20) : 5) +
-                                  (which == 1 ? vjump_smem<R>(cap, c, a0.ns != 0) : 0);
+        const size_t smem = which >= 2 ? vupdate_smem<R>(cap) : vitem_smem<R>(cap, which == 1 ? (a0.split ? 29 : 20) : 5);
         cudaError_t e;
         switch (c) {
             case 0: e = launch_item_class<R, 0>(a, which, n, smem, s, store_grad, stage, tshift, wq, cap); break;
@@ -1505,9 +1477,8 @@ cudaError_t launch_items(const VArgs<R>& a0, int which, cudaStream_t s, int stor
 }
 
 template <typename R, int PC>
-cudaError_t set_item_attributes(size_t vol, size_t upd, size_t trc, int cap, bool ns) {
+cudaError_t set_item_attributes(size_t vol, size_t upd, size_t trc) {
     cudaError_t e;
-    vol += vjump_smem<R>(cap, PC, ns);
     if ((e = cudaFuncSetAttribute(kv_volume<R, PC>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(vol))) ||
         (e = cudaFuncSetAttribute(kv_update<R, 0, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(upd))) ||
@@ -1557,12 +1528,10 @@ cudaError_t vrun_stage(const VArgs<R>& a, int stage, double tshift, int flags, c
     const size_t upd = std::max(vupdate_smem<R>(a.cap), vupdate_smem<R>(std::min(a.cap, kStageNodes)));
     if (stage == kPrepare) {
         cudaError_t e;
-        const bool ns = a.ns != 0;
-        const int cp = a.cap;
-        if ((e = set_item_attributes<R, 0>(vol, upd, trc, cp, ns)) || (e = set_item_attributes<R, 2>(vol, upd, trc, cp, ns)) ||
-            (e = set_item_attributes<R, 3>(vol, upd, trc, cp, ns)) || (e = set_item_attributes<R, 4>(vol, upd, trc, cp, ns)) ||
-            (e = set_item_attributes<R, 5>(vol, upd, trc, cp, ns)) || (e = set_item_attributes<R, 6>(vol, upd, trc, cp, ns)) ||
-            (e = set_item_attributes<R, 7>(vol, upd, trc, cp, ns)) || (e = set_item_attributes<R, 8>(vol, upd, trc, cp, ns)) ||
+        if ((e = set_item_attributes<R, 0>(vol, upd, trc)) || (e = set_item_attributes<R, 2>(vol, upd, trc)) ||
+            (e = set_item_attributes<R, 3>(vol, upd, trc)) || (e = set_item_attributes<R, 4>(vol, upd, trc)) ||
+            (e = set_item_attributes<R, 5>(vol, upd, trc)) || (e = set_item_attributes<R, 6>(vol, upd, trc)) ||
+            (e = set_item_attributes<R, 7>(vol, upd, trc)) || (e = set_item_attributes<R, 8>(vol, upd, trc)) ||
             (e = cudaFuncSetAttribute(kv_face<R, kJump, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       static_cast<int>(FaceCfg<R, kJump>::SMEM))) ||
             (e = cudaFuncSetAttribute(kv_face<R, kJump, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
