@@ -234,12 +234,6 @@ __device__ __forceinline__ void ld4(const R* v, int i, R* o) {
     }
 }
 
-// The lanes of warp w present in a CTA of nt threads (cnt of them, from lane 0).
-__device__ __forceinline__ unsigned warp_lanes_mask(int nt, int w, int& cnt) {
-    cnt = nt - 32 * w < 32 ? nt - 32 * w : 32;
-    return cnt == 32 ? 0xffffffffu : (1u << cnt) - 1u;
-}
-
 // Slot arrays in global memory use the same split: the 16-byte parts of all slot points first, then
 // the fifth values; the threads of a face read consecutive 16-byte parts (coalesced 128-bit loads).
 template <typename R>
@@ -350,66 +344,6 @@ __device__ __forceinline__ void trace5(const Ops<R>& ops, const R* v4, const R* 
             for (int v = 0; v < 5; ++v) out[d][v] = out[d][v] + x[v] * wl;
         }
     }
-}
-
-// The gradient traces (3 directions x 5 values) of a Gauss line at both of its ends, computed by the
-// two lanes that own those ends (lanes 2q and 2q + 1 of the same warp, h = 0 the left end with vL,
-// h = 1 the right end with vR): each lane loads about half of the 15 components of every line node,
-// accumulates them for both ends, and the pair swaps the halves that belong to the partner's end
-// (mask: the warp's lanes present). Each component is summed in line order with the same
-// multiply-adds as trace5, so the result is identical; the pair reads each line node's 15 values once
-// instead of twice.
-//   lane h = 0: direction 0 (values 0..4) and values 0, 1 of direction 1   (7 components)
-//   lane h = 1: direction 2 (values 0..4) and values 2, 3, 4 of direction 1 (8 components)
-template <int P>
-__device__ __forceinline__ void trace_grad_pair(const Ops<float>& ops, const float* G4, const float* G1, int side,
-                                                int ca, int cb, int h, unsigned mask, float out[3][5]) {
-    constexpr int P3 = P * P * P;
-    float lo[8], hi[8];
-#pragma unroll
-    for (int c = 0; c < 8; ++c) lo[c] = hi[c] = 0.f;
-    const int dmain = h ? 2 : 0;
-#pragma unroll
-    for (int l = 0; l < P; ++l) {
-        const int m = line_node<P>(side, ca, cb, l);
-        const float wl = ops.vL[l], wr = ops.vR[l];
-        float x[8];
-        const float4 a4 = *reinterpret_cast<const float4*>(G4 + 4 * (m * 3 + dmain));
-        x[0] = a4.x;
-        x[1] = a4.y;
-        x[2] = a4.z;
-        x[3] = a4.w;
-        x[4] = G1[dmain * P3 + m];
-        const float2 b2 = *reinterpret_cast<const float2*>(G4 + 4 * (m * 3 + 1) + 2 * h);
-        x[5] = b2.x;
-        x[6] = b2.y;
-        x[7] = h ? G1[P3 + m] : 0.f;
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            lo[c] = lo[c] + x[c] * wl;
-            hi[c] = hi[c] + x[c] * wr;
-        }
-    }
-    // own end: lo (h = 0) or hi (h = 1); the partner needs the other one
-    float own[8], got[8];
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        own[c] = h ? hi[c] : lo[c];
-        got[c] = __shfl_xor_sync(mask, h ? lo[c] : hi[c], 1);
-    }
-    // assemble (d, v): own components from own[], the partner's from got[]
-    const float* p0 = h ? got : own;  // lane 0's layout: d0 v0..4, d1 v0, v1
-    const float* p1 = h ? own : got;  // lane 1's layout: d2 v0..4, d1 v2, v3, v4
-#pragma unroll
-    for (int v = 0; v < 5; ++v) {
-        out[0][v] = p0[v];
-        out[2][v] = p1[v];
-    }
-    out[1][0] = p0[5];
-    out[1][1] = p0[6];
-    out[1][2] = p1[5];
-    out[1][3] = p1[6];
-    out[1][4] = p1[7];
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -819,14 +753,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
                 const int64_t s = slot(e, side);
                 R tq[5], tg[3][5];
                 ld5(T4, t, T1, t, tq);
-                if constexpr (P == 6 && !GL && sizeof(R) == 4 && F6 == P3) {
-                    // one face point per thread, the two ends of a line in lanes n and n ^ 1
-                    int cnt;
-                    const unsigned mask = warp_lanes_mask(P3, n >> 5, cnt);
-                    trace_grad_pair<P>(a.ops, G4, G1, side, ca, cb, tt & 1, mask, tg);
-                } else {
-                    trace5<P, GL, 3>(a.ops, G4, G1, P3, side, ca, cb, tg);
-                }
+                trace5<P, GL, 3>(a.ops, G4, G1, P3, side, ca, cb, tg);
                 R mu, kap;
                 mu_kappa(a.ph, tq, mu, kap);
                 R C[3][5];
@@ -1224,6 +1151,10 @@ __device__ __forceinline__ void monitor_warp(MonitorPart& p, unsigned mask, int 
     }
 }
 
+__device__ __forceinline__ unsigned warp_lanes_mask(int nt, int w, int& cnt) {
+    cnt = nt - 32 * w < 32 ? nt - 32 * w : 32;
+    return cnt == 32 ? 0xffffffffu : (1u << cnt) - 1u;
+}
 
 // First half, FP64 patterns (63 bits): shuffles.
 template <int NT>
