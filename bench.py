@@ -7,7 +7,7 @@ whole mesh (3 RHS evaluations + 3 low-storage updates) = 3*NDOF DOF-stage update
 
 value    : mixed form (FP32 fluxes/contractions, FP64 state and RK accumulation), state resident in
            HBM, K steps replayed from a CUDA graph, timed with CUDA events on the solver's stream.
-plain    : the plain FP64 form timed the same way (the spec ratio is value/plain).
+plain    : the plain FP64 form timed the same way (the mixed-over-plain ratio is value/plain).
 e2e      : the reference-facing C ABI driven like IntegrateInTime with host buffers: upload Q from
            pinned host memory, dg_integrate (per step MaxTimeStep + TakeRK3Step + ComputeMaxResiduals /
            checkForNan on the device), download Q and the per-step residuals; all inside the timed
