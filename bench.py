@@ -222,6 +222,19 @@ def run_gpu_arm(args, rank, world, local, case):
                                 "24^3-element case (149.0 B/DOF), scaled by the DOF count",
                 "limiter": {"unit": "l1tex (shared-memory operand loads)", "throughput_frac": VOLUME_L1TEX_FRAC,
                             "source": "ncu l1tex__throughput.avg.pct_of_peak_sustained_elapsed, same capture"}}
+    # the step's other two kernels and the whole step against the same HBM peak (algorithmic bytes:
+    # update 224 B/DOF (stage 1, no QDot store), flux 160 B per face point = 480/P B/DOF, step average
+    # volume + flux + update with the last stage's QDot store)
+    upd_b, flux_b = 224.0, 480.0 / P
+    step_b = volume_bytes(P, 4) + flux_b + upd_b + 20.0 / 3.0
+    roofline["other_kernels"] = {
+        "k_update_tma": {"alg_bytes_per_dof": upd_b, "achieved": round(upd_b * ndof / (kt[2] * 1e-3) / 1e9, 1),
+                         "frac": round(upd_b * ndof / (kt[2] * 1e-3) / 1e9 / hbm, 4)},
+        "k_flux": {"alg_bytes_per_dof": flux_b, "achieved": round(flux_b * ndof / (kt[1] * 1e-3) / 1e9, 1),
+                   "frac": round(flux_b * ndof / (kt[1] * 1e-3) / 1e9 / hbm, 4)}}
+    per_gpu = value / world
+    roofline["step"] = {"alg_bytes_per_dof_stage": round(step_b, 1), "achieved": round(per_gpu * step_b / 1e9, 1),
+                        "frac": round(per_gpu * step_b / 1e9 / hbm, 4)}
 
     # the plain form's compute roofline: FP64 pipe (measured FMA rate of this GPU)
     fp64_peak = C.c_double()
