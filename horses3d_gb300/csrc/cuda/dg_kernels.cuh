@@ -378,15 +378,6 @@ __global__ void __launch_bounds__(Geo<P>::THREADS) k_traces(Args<R> a) {
 // EST (the first stage of a step of the monitored time loop): the FP32 MaxTimeStep estimate of the
 // step's initial state at every node, its element minima into the element's monitor record
 // (a.mon[8e + 6], [8e + 7]), from the state and metric terms the kernel loads anyway.
-//
-// Bulk-copied element blocks (kStageVolume, the headline configuration): the element's FP64 state,
-// metric terms and 1/J (and J for the estimate) arrive in shared memory by cp.async.bulk on an
-// mbarrier, and QDot leaves by one bulk store. Per node these arrays are strided (40 and 12 bytes),
-// so as per-thread global accesses every warp instruction moved several times the bytes it used
-// through the L1 pipe, the kernel's busiest unit; the bulk copies bypass it.
-template <int P, bool GL, typename R>
-constexpr bool kStageVolume = (P == 6 && !GL && sizeof(R) == 4);
-
 template <int P, bool GL, typename R, bool TC = false, bool EST = false>
 __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_volume(Args<R> a, int store_grad) {
     using L = VolLayout<P, R>;
@@ -394,15 +385,6 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
     static_assert(!TC || (Geo<P>::EPB == 1 && 5 * P2 <= 192 && P + 2 <= 16), "tensor-core gradient: one element per CTA");
     static_assert(!EST || (Geo<P>::EPB == 1 && !TC), "time-step estimate: one element per CTA");
     __shared__ uint2 est_part[EST ? (P3 + 31) / 32 : 1];
-    constexpr bool STG = kStageVolume<P, GL, R> && !TC;
-    static_assert(!STG || Geo<P>::EPB == 1, "bulk-copied element blocks: one element per CTA");
-    constexpr uint32_t SQ = 5 * P3 * sizeof(double), SA = 3 * P3 * sizeof(R), SJ = P3 * sizeof(R);
-    static_assert(!STG || (SQ % 16 == 0 && SA % 16 == 0 && SJ % 16 == 0), "bulk copies move multiples of 16 bytes");
-    __shared__ __align__(128) double vQ[STG ? 5 * P3 : 2];
-    __shared__ __align__(128) R vJa[STG ? 9 * P3 : 4];
-    __shared__ __align__(128) R vIJ[STG ? P3 : 4];
-    __shared__ __align__(128) R vJ[(STG && EST) ? P3 : 4];
-    __shared__ __align__(8) uint64_t vbar;
     const bool split = a.inviscid != 0;
     const bool ns = a.ph.ns;
     extern __shared__ __align__(16) unsigned char dsm[];
@@ -451,60 +433,22 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
             mbar_init_fence();
         }
     }
-    if constexpr (STG) {
-        if (n == 0) {
-            mbar_init(&vbar, 1);
-            mbar_init_fence();
-        }
-        __syncthreads();
-        if (n == 0) {
-            const int64_t g0 = static_cast<int64_t>(e) * P3;
-            mbar_arrive_expect_tx(&vbar, SQ + 3 * SA + SJ + (EST ? SJ : 0));
-            bulk_load(vQ, a.Q + 5 * g0, SQ, &vbar);
-            bulk_load(vJa, a.ja_xi + 3 * g0, SA, &vbar);
-            bulk_load(vJa + 3 * P3, a.ja_eta + 3 * g0, SA, &vbar);
-            bulk_load(vJa + 6 * P3, a.ja_zeta + 3 * g0, SA, &vbar);
-            bulk_load(vIJ, a.inv_jac + g0, SJ, &vbar);
-            if constexpr (EST) bulk_load(vJ, a.jac + g0, SJ, &vbar);
-        }
-        const bool arrived = mbar_wait(&vbar, 0);
-        if (__syncthreads_or(!arrived)) {  // block-uniform: every thread leaves
-            if (n == 0) {
-                atomicOr(a.err, 1);
-                mbar_wait(&vbar, 0, kWaitNs / 4);  // bounded: let a late copy land before the CTA's memory is reused
-            }
-            return;
-        }
-    }
     if (active) {
-        if constexpr (STG) {
-#pragma unroll
-            for (int v = 0; v < 4; ++v) q[v] = R(vQ[5 * n + v]);
-            q[4] = R(vQ[5 * n + 4] - a.e_ref);
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                jxs[c] = vJa[3 * n + c];
-                jes[c] = vJa[3 * P3 + 3 * n + c];
-                jzs[c] = vJa[6 * P3 + 3 * n + c];
-            }
-        } else {
-            load_state(a, g, q);
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                jxs[c] = a.ja_xi[3 * g + c];
-                jes[c] = a.ja_eta[3 * g + c];
-                jzs[c] = a.ja_zeta[3 * g + c];
-            }
-        }
+        load_state(a, g, q);
         st5(Q4, n, Q1, n, q);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            jxs[c] = a.ja_xi[3 * g + c];
+            jes[c] = a.ja_eta[3 * g + c];
+            jzs[c] = a.ja_zeta[3 * g + c];
+        }
     }
     if constexpr (EST) {
         // the FP32 inputs of the estimate: the state rounded to FP32 (the mixed form's q already is,
         // except the energy, which it holds relative to e_ref)
         float cv, vs;
-        const float E = sizeof(R) == 4 ? to_f32(STG ? vQ[5 * n + 4] : a.Q[5 * g + 4]) : as_f32(q[4]);
-        const R Jn = STG ? vJ[n] : a.jac[g];
-        dt_estimate_f(a.dtc, as_f32(q[0]), as_f32(q[1]), as_f32(q[2]), as_f32(q[3]), E, jxs, jes, jzs, Jn, cv, vs);
+        const float E = sizeof(R) == 4 ? to_f32(a.Q[5 * g + 4]) : as_f32(q[4]);
+        dt_estimate_f(a.dtc, as_f32(q[0]), as_f32(q[1]), as_f32(q[2]), as_f32(q[3]), E, jxs, jes, jzs, a.jac[g], cv, vs);
         const int w = n >> 5, cnt = P3 - 32 * w < 32 ? P3 - 32 * w : 32;
         const unsigned mask = cnt == 32 ? 0xffffffffu : (1u << cnt) - 1u;
         // minima of non-negative floats (and NaN, which loses to every number) by their bit patterns
@@ -667,7 +611,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
                 for (int v = 0; v < 5; ++v) uzeta[v] = uzeta[v] + x[v] * w;
             }
             }
-            const R ij = STG ? vIJ[n] : a.inv_jac[g];
+            const R ij = a.inv_jac[g];
 #pragma unroll
             for (int v = 0; v < 5; ++v) {
                 U[0][v] = (uxi[v] * jxs[0] + ueta[v] * jes[0] + uzeta[v] * jzs[0]) * ij;
@@ -727,7 +671,7 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
         if (active) {
             // lifting: U += (sum over sides of b (x) uStar n) / J in VectorWeakIntegrals_StdFace order
             // (left, right, front, back, bottom, top)
-            const R ij = STG ? vIJ[n] : a.inv_jac[g];
+            const R ij = a.inv_jac[g];
             const int pt[6] = {(5 * P2) + (j + P * k), (3 * P2) + (j + P * k), (0 * P2) + (i + P * k),
                                (1 * P2) + (i + P * k), (2 * P2) + (i + P * j), (4 * P2) + (i + P * j)};
             R bw[6];
@@ -891,21 +835,8 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
 #pragma unroll
             for (int v = 0; v < 5; ++v) acc[v] = acc[v] + h * x[v];
         }
-        if constexpr (STG) {
-            float* sDot = reinterpret_cast<float*>(vQ);  // the state block was consumed at the start
 #pragma unroll
-            for (int v = 0; v < 5; ++v) sDot[5 * n + v] = acc[v];
-            fence_proxy_async_smem();  // the QDot values before the bulk store reads them
-            __syncthreads();
-            if (n == 0) {
-                bulk_store(a.QDot + 5 * static_cast<int64_t>(e) * P3, sDot, 5 * P3 * sizeof(float));
-                bulk_commit();
-                bulk_wait_all();
-            }
-        } else {
-#pragma unroll
-            for (int v = 0; v < 5; ++v) a.QDot[5 * g + v] = acc[v];
-        }
+        for (int v = 0; v < 5; ++v) a.QDot[5 * g + v] = acc[v];
     } else {
         // Split form (Gauss-Lobatto, HyperbolicSplitForm.f90:64-116): the two-point flux f#(a,b) of
         // a pair of nodes on a line is symmetric, and the reference evaluates it once per pair (for
