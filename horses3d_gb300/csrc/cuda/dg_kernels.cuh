@@ -378,12 +378,6 @@ __global__ void __launch_bounds__(Geo<P>::THREADS) k_traces(Args<R> a) {
 // EST (the first stage of a step of the monitored time loop): the FP32 MaxTimeStep estimate of the
 // step's initial state at every node, its element minima into the element's monitor record
 // (a.mon[8e + 6], [8e + 7]), from the state and metric terms the kernel loads anyway.
-// QDot by one bulk store (kStoreQDotBulk, the headline configuration): per node its five FP32
-// values are 20 bytes apart, so five per-thread stores moved each warp's 640 bytes five times through
-// the L1 pipe, the kernel's busiest unit; staged in shared memory they leave as one copy.
-template <int P, bool GL, typename R>
-constexpr bool kStoreQDotBulk = (P == 6 && !GL && sizeof(R) == 4);
-
 template <int P, bool GL, typename R, bool TC = false, bool EST = false>
 __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_volume(Args<R> a, int store_grad) {
     using L = VolLayout<P, R>;
@@ -391,9 +385,6 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
     static_assert(!TC || (Geo<P>::EPB == 1 && 5 * P2 <= 192 && P + 2 <= 16), "tensor-core gradient: one element per CTA");
     static_assert(!EST || (Geo<P>::EPB == 1 && !TC), "time-step estimate: one element per CTA");
     __shared__ uint2 est_part[EST ? (P3 + 31) / 32 : 1];
-    constexpr bool QBULK = kStoreQDotBulk<P, GL, R>;
-    static_assert(!QBULK || (Geo<P>::EPB == 1 && (5 * P3 * sizeof(float)) % 16 == 0), "QDot bulk store");
-    __shared__ __align__(128) float sDot[QBULK ? 5 * P3 : 4];
     const bool split = a.inviscid != 0;
     const bool ns = a.ph.ns;
     extern __shared__ __align__(16) unsigned char dsm[];
@@ -844,20 +835,8 @@ __global__ void __launch_bounds__(Geo<P>::THREADS, (Occupancy<P, R>::volume)) k_
 #pragma unroll
             for (int v = 0; v < 5; ++v) acc[v] = acc[v] + h * x[v];
         }
-        if constexpr (QBULK) {
 #pragma unroll
-            for (int v = 0; v < 5; ++v) sDot[5 * n + v] = acc[v];
-            fence_proxy_async_smem();  // the QDot values before the bulk store reads them
-            __syncthreads();
-            if (n == 0) {
-                bulk_store(a.QDot + 5 * static_cast<int64_t>(e) * P3, sDot, 5 * P3 * sizeof(float));
-                bulk_commit();
-                bulk_wait_all();
-            }
-        } else {
-#pragma unroll
-            for (int v = 0; v < 5; ++v) a.QDot[5 * g + v] = acc[v];
-        }
+        for (int v = 0; v < 5; ++v) a.QDot[5 * g + v] = acc[v];
     } else {
         // Split form (Gauss-Lobatto, HyperbolicSplitForm.f90:64-116): the two-point flux f#(a,b) of
         // a pair of nodes on a line is symmetric, and the reference evaluates it once per pair (for
