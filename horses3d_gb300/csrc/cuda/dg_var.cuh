@@ -572,50 +572,67 @@ struct FaceCfg {
     static constexpr size_t SMEM = static_cast<size_t>(FPB) * 4 * NVB * kFacePts * sizeof(R);
 };
 
-// Interpolation of NV values from (s1 x s2) points in S to the face's (q1 x q2) points; returns the
-// buffer that holds the result (S or A). Every thread of the CTA must call it (it synchronises).
+// Interpolation of NV values from (s1 x s2) points in S to the face's (q1 x q2) points, one of the
+// two passes (first: along the first face direction, S -> A; second: along the second, cur -> nxt).
 template <typename R, int NV>
-__device__ __forceinline__ R* to_face_points(const R* tset, R* S, R* A, int s1, int s2, int q1, int q2, int lane,
-                                             bool active) {
-    const bool d1 = active && s1 != q1, d2 = active && s2 != q2;
+__device__ __forceinline__ void face_pass1(const R* tset, const R* S, R* A, int s1, int s2, int q1, const Div& dq1,
+                                           int lane) {
+    const R* T = tset + ((s1 - 1) * kMaxP + (q1 - 1)) * kTsetStride;
+    for (int p = lane; p < q1 * s2; p += kFacePts) {  // A(i, l) = sum_m T1(i, m) S(m, l)
+        const int l = quot(p, dq1), i = p - l * q1;
+        R acc[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) acc[v] = R(0);
+        for (int m = 0; m < s1; ++m) {
+            const R w = T[i * kMaxP + m];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) acc[v] = acc[v] + w * S[v * kFacePts + m + s1 * l];
+        }
+#pragma unroll
+        for (int v = 0; v < NV; ++v) A[v * kFacePts + p] = acc[v];
+    }
+}
+template <typename R, int NV>
+__device__ __forceinline__ void face_pass2(const R* tset, const R* cur, R* nxt, int s2, int q1, int q2, const Div& dq1,
+                                           int lane) {
+    const R* T = tset + ((s2 - 1) * kMaxP + (q2 - 1)) * kTsetStride;
+    for (int p = lane; p < q1 * q2; p += kFacePts) {  // nxt(i, j) = sum_l T2(j, l) cur(i, l)
+        const int j = quot(p, dq1), i = p - j * q1;
+        R acc[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) acc[v] = R(0);
+        for (int l = 0; l < s2; ++l) {
+            const R w = T[j * kMaxP + l];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) acc[v] = acc[v] + w * cur[v * kFacePts + i + q1 * l];
+        }
+#pragma unroll
+        for (int v = 0; v < NV; ++v) nxt[v * kFacePts + p] = acc[v];
+    }
+}
+
+// Both sides' traces to the face points: the left side's (l1 x l2) points in SL (work buffer AL) and
+// the right side's (s1R x s2R) points in SR (AR), each pass of the two sides between the same two
+// CTA barriers. XL, XR receive the buffers that hold the results. Every thread of the CTA must call it.
+template <typename R, int NV>
+__device__ __forceinline__ void both_to_face_points(const R* tset, R* SL, R* AL, int l1, int l2, R* SR, R* AR, int s1R,
+                                                    int s2R, int q1, int q2, int lane, bool active, const R*& XL,
+                                                    const R*& XR) {
     const Div dq1 = make_div(q1);
-    if (d1) {  // along the first face direction: A(i, l) = sum_m T1(i, m) S(m, l)
-        const R* T = tset + ((s1 - 1) * kMaxP + (q1 - 1)) * kTsetStride;
-        for (int p = lane; p < q1 * s2; p += kFacePts) {
-            const int l = quot(p, dq1), i = p - l * q1;
-            R acc[NV];
-#pragma unroll
-            for (int v = 0; v < NV; ++v) acc[v] = R(0);
-            for (int m = 0; m < s1; ++m) {
-                const R w = T[i * kMaxP + m];
-#pragma unroll
-                for (int v = 0; v < NV; ++v) acc[v] = acc[v] + w * S[v * kFacePts + m + s1 * l];
-            }
-#pragma unroll
-            for (int v = 0; v < NV; ++v) A[v * kFacePts + p] = acc[v];
-        }
-    }
+    const bool a1 = active && l1 != q1, a2 = active && l2 != q2;
+    const bool b1 = active && s1R != q1, b2 = active && s2R != q2;
+    if (a1) face_pass1<R, NV>(tset, SL, AL, l1, l2, q1, dq1, lane);
+    if (b1) face_pass1<R, NV>(tset, SR, AR, s1R, s2R, q1, dq1, lane);
     __syncthreads();
-    R* cur = d1 ? A : S;
-    R* nxt = d1 ? S : A;
-    if (d2) {  // along the second: nxt(i, j) = sum_l T2(j, l) cur(i, l)
-        const R* T = tset + ((s2 - 1) * kMaxP + (q2 - 1)) * kTsetStride;
-        for (int p = lane; p < q1 * q2; p += kFacePts) {
-            const int j = quot(p, dq1), i = p - j * q1;
-            R acc[NV];
-#pragma unroll
-            for (int v = 0; v < NV; ++v) acc[v] = R(0);
-            for (int l = 0; l < s2; ++l) {
-                const R w = T[j * kMaxP + l];
-#pragma unroll
-                for (int v = 0; v < NV; ++v) acc[v] = acc[v] + w * cur[v * kFacePts + i + q1 * l];
-            }
-#pragma unroll
-            for (int v = 0; v < NV; ++v) nxt[v * kFacePts + p] = acc[v];
-        }
-    }
+    R* curL = a1 ? AL : SL;
+    R* nxtL = a1 ? SL : AL;
+    R* curR = b1 ? AR : SR;
+    R* nxtR = b1 ? SR : AR;
+    if (a2) face_pass2<R, NV>(tset, curL, nxtL, l2, q1, q2, dq1, lane);
+    if (b2) face_pass2<R, NV>(tset, curR, nxtR, s2R, q1, q2, dq1, lane);
     __syncthreads();
-    return d2 ? nxt : cur;
+    XL = a2 ? nxtL : curL;
+    XR = b2 ? nxtR : curR;
 }
 
 // V selects the compiled variant: for kJump, gradient variables other than the state (V = 1); for
@@ -682,8 +699,8 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS, (sizeof(R) == 4 && 
         }
     }
     __syncthreads();
-    const R* XL = to_face_points<R, NVIN>(a.tset, SL, AL, l1, l2, q1, q2, lane, active);
-    const R* XR = to_face_points<R, NVIN>(a.tset, SR, AR, s1R, s2R, q1, q2, lane, active);
+    const R *XL, *XR;
+    both_to_face_points<R, NVIN>(a.tset, SL, AL, l1, l2, SR, AR, s1R, s2R, q1, q2, lane, active, XL, XR);
     R out[NVOUT];
     const bool point = active && lane < q1 * q2;
     if (point) {
