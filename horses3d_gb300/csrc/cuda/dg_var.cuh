@@ -775,17 +775,13 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS, (sizeof(R) == 4 && 
             for (int v = 0; v < 5; ++v) out[v] = (inv[v] - visc[v]) * J;
         }
     }
-    // the face values go to the left work buffer the interpolated traces are not in (FL), so no
-    // barrier has to wait for the traces' readers before they are written; after the barrier the
-    // other left buffer (PL) and AR are free for the projection
-    R* FL = XL == SL ? AL : SL;
-    R* PL = XL == SL ? SL : AL;
+    __syncthreads();  // the traces are consumed: SL holds the face values from here on
     if (point) {
 #pragma unroll
-        for (int v = 0; v < NVOUT; ++v) FL[v * NP + lane] = out[v];
+        for (int v = 0; v < NVOUT; ++v) SL[v * NP + lane] = out[v];
     }
     __syncthreads();
-    // projection to each side's order (transposed Tset), first direction into PL / AR
+    // projection to each side's order (transposed Tset), first direction into AL / AR
     const bool pL1 = active && l1 != q1, pL2 = active && l2 != q2;
     const bool pR1 = active && s1R != q1, pR2 = active && s2R != q2;
     const Div dl1 = make_div(l1), dsR = make_div(s1R);
@@ -796,8 +792,8 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS, (sizeof(R) == 4 && 
 #pragma unroll
             for (int v = 0; v < NVOUT; ++v) {
                 R acc = R(0);
-                for (int m = 0; m < q1; ++m) acc = acc + T[i * kMaxP + m] * FL[v * NP + m + q1 * l];
-                PL[v * NP + p] = acc;
+                for (int m = 0; m < q1; ++m) acc = acc + T[i * kMaxP + m] * SL[v * NP + m + q1 * l];
+                AL[v * NP + p] = acc;
             }
         }
     }
@@ -808,7 +804,7 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS, (sizeof(R) == 4 && 
 #pragma unroll
             for (int v = 0; v < NVOUT; ++v) {
                 R acc = R(0);
-                for (int m = 0; m < q1; ++m) acc = acc + T[i * kMaxP + m] * FL[v * NP + m + q1 * l];
+                for (int m = 0; m < q1; ++m) acc = acc + T[i * kMaxP + m] * SL[v * NP + m + q1 * l];
                 AR[v * NP + p] = acc;
             }
         }
@@ -819,7 +815,7 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS, (sizeof(R) == 4 && 
     R* dstR = MODE == kJump ? a.UJ + offR * 15 : a.FS + offR * 5;
     const R sign2 = MODE == kJump ? R(1) : R(-1);
     {
-        const R* src = pL1 ? PL : FL;  // (l1 x q2) points
+        const R* src = pL1 ? AL : SL;  // (l1 x q2) points
         const R* T = a.tset + ((q2 - 1) * kMaxP + (l2 - 1)) * kTsetStride;
         for (int p = lane; p < nL; p += NP) {
             const int j = quot(p, dl1), i = p - j * l1;
@@ -837,7 +833,7 @@ __global__ void __launch_bounds__(FaceCfg<R, MODE>::THREADS, (sizeof(R) == 4 && 
         }
     }
     {
-        const R* src = pR1 ? AR : FL;  // (s1R x q2) points
+        const R* src = pR1 ? AR : SL;  // (s1R x q2) points
         const R* T = a.tset + ((q2 - 1) * kMaxP + (s2R - 1)) * kTsetStride;
         for (int p = lane; p < nR; p += NP) {
             const int j = quot(p, dsR), i = p - j * s1R;
