@@ -146,7 +146,6 @@ struct dg_ctx {
     h3dctx::VStore<double> v64;
     h3dctx::VStore<float> v32;
     dg::Lanes lanes;  // side streams of the stage phases
-    h3dctx::DevBuf<int> vwork;  // work counter of the persistent update
     int n_items = 0;
     int cls[dg::kItemClasses + 1] = {};  // item class ranges (see dg::VArgs::cls)
     int ccap[dg::kItemClasses] = {};     // largest item per class

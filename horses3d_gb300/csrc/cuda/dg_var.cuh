@@ -58,8 +58,6 @@ constexpr int kItemClasses = kMaxP + 1;
 template <typename R>
 struct VArgs {
     int n_items, n_faces, cap;  // cap: largest node count of an item
-    int* work;                  // work counter of the persistent update (one int)
-    int persist;                // the update as one persistent launch over all classes
     int ns, source;
     int riemann, averaging, grad_vars;  // the host's copies of the solver, average and gradient variables
     int split;                          // split-form volume integral (Gauss-Lobatto nodes)
@@ -1035,15 +1033,11 @@ __device__ __forceinline__ void vupdate_store(const double* shared, double* glob
 // conversions use the integer pipe (bit-exact with the hardware conversion, which runs on the FP64
 // pipe beside the update's FP64 multiply-adds).
 // ------------------------------------------------------------------------------------------------
-// cap: the launch's largest item (its shared-memory layout). any_cap: the launch's shared memory also
-// holds the staged layout of kStageNodes nodes (the persistent launch), so that its items of up to
-// kStageNodes nodes stage their stores even when larger items share the launch.
 template <typename R, int PC, bool SRC, bool PST>
-__device__ __forceinline__ void kv_update_item(const VArgs<R>& a, int item, int stage, double tshift, int write_qdot,
-                                               int cap, bool any_cap = false) {
+__global__ void __launch_bounds__(256, sizeof(R) == 4 && !SRC && !PST ? 6 : 0)
+    kv_update(VArgs<R> a, int stage, double tshift, int write_qdot, int cap) {
     extern __shared__ __align__(16) unsigned char vsm[];
-    const ItemDims d = item_dims<PC>(a.items[item]);
-    if (any_cap && cap > kStageNodes && d.ntot <= kStageNodes) cap = kStageNodes;
+    const ItemDims d = item_dims<PC>(a.items[a.item0 + blockIdx.x]);
     const int px = d.px, py = d.py, np = d.np, ntot = d.ntot;
     OpsP<R>* sO = reinterpret_cast<OpsP<R>*>(vsm);
     R* sQ = reinterpret_cast<R*>(sO + 3);
@@ -1135,29 +1129,6 @@ __device__ __forceinline__ void kv_update_item(const VArgs<R>& a, int item, int 
         vupdate_store(sQd, a.Q, sE, W, 5 * ntot, inv_w);
     }
     write_traces<R, 5, PC>(a, d, sO, sQ, a.QF);
-}
-
-template <typename R, int PC, bool SRC, bool PST>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 && !SRC && !PST ? 6 : 0)
-    kv_update(VArgs<R> a, int stage, double tshift, int write_qdot, int cap) {
-    kv_update_item<R, PC, SRC, PST>(a, a.item0 + blockIdx.x, stage, tshift, write_qdot, cap);
-}
-
-// The same update as a persistent kernel: a grid of resident CTAs takes the items of every class from
-// one work counter (*next, zero at launch), so that the classes share one launch and no CTA waits
-// for a launch tail. No CTA waits on another.
-template <typename R, bool PST>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 && !PST ? 6 : 0)
-    kv_update_persistent(VArgs<R> a, int stage, double tshift, int write_qdot, int* next) {
-    __shared__ int s_item;
-    for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(next, 1);
-        __syncthreads();
-        const int it = s_item;
-        if (it >= a.n_items) break;  // block-uniform
-        kv_update_item<R, 0, false, PST>(a, it, stage, tshift, write_qdot, a.cap, true);
-        __syncthreads();  // shared memory and s_item are reused by the next item
-    }
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -1311,11 +1282,6 @@ using VTimesFn = cudaError_t (*)(const VArgs<R>& a, int reps, cudaStream_t s, do
 // stage's stream wait for every side stream used. Inside a stream capture the side streams become
 // branches of the graph. Without lanes every launch goes to the stage's stream in order.
 constexpr int kLanes = 3;
-// The update as one persistent launch over all item classes (kv_update_persistent) instead of one
-// launch per class. Measured slower on both variable-order workloads (p-anisotropic 24^3: update
-// 0.193 -> 0.222 ms; 64 cases: 0.826 -> 0.831 ms): each item then waits for its work-counter atomic
-// before its loads start, which the hardware block scheduler does not. Off; kept for the record.
-constexpr bool kPersistentUpdate = false;
 struct Lanes {
     int n = 0;
     cudaStream_t side[kLanes] = {};
@@ -1510,33 +1476,11 @@ cudaError_t set_item_attributes(size_t vol, size_t upd, size_t trc) {
     return cudaSuccess;
 }
 
-// Resident CTAs of the persistent update over all SMs for the item table's largest item (0 when the
-// occupancy query fails: the per-class launches are used then).
-template <typename R>
-int persistent_update_grid(const VArgs<R>& a) {
-    const size_t smem = std::max(vupdate_smem<R>(a.cap), vupdate_smem<R>(std::min(a.cap, kStageNodes)));
-    int dev = 0, sms = 0, per = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-        return 0;
-    const void* fn = a.pstat ? reinterpret_cast<const void*>(kv_update_persistent<R, true>)
-                             : reinterpret_cast<const void*>(kv_update_persistent<R, false>);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, smem) != cudaSuccess) return 0;
-    return per > 0 ? per * sms : 0;
-}
-
-// The update of a stage: one persistent launch over all item classes, or one launch per class (the
-// manufactured-source variant, or when the persistent grid is unavailable).
+// The update of a stage: one launch per item class (the manufactured-source variant where a case has
+// a source).
 template <typename R>
 cudaError_t launch_update(const VArgs<R>& a, Fork& f, int stage, double tshift, int wq) {
-    const int grid = !a.source && a.persist && a.work ? persistent_update_grid(a) : 0;
-    if (grid <= 0) return launch_items(a, a.source ? 3 : 2, f, 0, stage, tshift, wq);
-    const cudaStream_t s = f.next();
-    cudaError_t e = cudaMemsetAsync(a.work, 0, sizeof(int), s);
-    if (e != cudaSuccess) return e;
-    const size_t smem = std::max(vupdate_smem<R>(a.cap), vupdate_smem<R>(std::min(a.cap, kStageNodes)));
-    if (a.pstat) kv_update_persistent<R, true><<<grid, 256, smem, s>>>(a, stage, tshift, wq, a.work);
-    else kv_update_persistent<R, false><<<grid, 256, smem, s>>>(a, stage, tshift, wq, a.work);
-    return cudaGetLastError();
+    return launch_items(a, a.source ? 3 : 2, f, 0, stage, tshift, wq);
 }
 
 template <typename R>
@@ -1560,11 +1504,7 @@ cudaError_t vrun_stage(const VArgs<R>& a, int stage, double tshift, int flags, c
             (e = cudaFuncSetAttribute(kv_face<R, kFluxNS, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       static_cast<int>(FaceCfg<R, kFluxNS>::SMEM))) ||
             (e = cudaFuncSetAttribute(kv_face<R, kFluxNS, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      static_cast<int>(FaceCfg<R, kFluxNS>::SMEM))) ||
-            (e = cudaFuncSetAttribute(kv_update_persistent<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      static_cast<int>(upd))) ||
-            (e = cudaFuncSetAttribute(kv_update_persistent<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      static_cast<int>(upd))))
+                                      static_cast<int>(FaceCfg<R, kFluxNS>::SMEM))))
             return e;
         return cudaSuccess;
     }

@@ -668,23 +668,18 @@ int create(int n_cases, const dg_mesh_desc* meshes, const dg_physics* phys, cons
         if ((e = c->dxi_table.upload(dxi.data(), dxi.size(), s)) || (e = c->gamma_M2.upload(gm2.data(), gm2.size(), s)))
             return bail(cuda_fail(e, "upload dt tables"));
     }
-    if ((e = c->vwork.alloc(1)) != cudaSuccess) return bail(cuda_fail(e, "work counter"));
     int rc;
     if (c->mixed) {
         if ((rc = static_pressure_residual(c, h))) return bail(rc);
         if ((rc = setup_vstore(c, c->v32, h))) return bail(rc);
         c->v32.args.pstat = c->pstat.p;
         c->v32.args.cap = cap;
-        c->v32.args.work = c->vwork.p;
-        c->v32.args.persist = dg::kPersistentUpdate ? 1 : 0;
         c->v32.stage = dg::vstage_fn_fp32();
         c->v32.times = dg::vtimes_fn_fp32();
         c->v32.tune = dg::vtune_fn_fp32();
     } else {
         if ((rc = setup_vstore(c, c->v64, h))) return bail(rc);
         c->v64.args.cap = cap;
-        c->v64.args.work = c->vwork.p;
-        c->v64.args.persist = dg::kPersistentUpdate ? 1 : 0;
         c->v64.stage = dg::vstage_fn_fp64();
         c->v64.times = dg::vtimes_fn_fp64();
         c->v64.tune = dg::vtune_fn_fp64();
@@ -704,7 +699,6 @@ void release(dg_ctx* c) {
     for (auto* b : {&c->eoff, &c->soff, &c->foff}) b->free();
     c->cc.free();
     c->pstat.free();
-    c->vwork.free();
     c->esum.free();
     c->dxi_table.free();
     c->gamma_M2.free();
